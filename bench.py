@@ -1,0 +1,416 @@
+"""Benchmark: multi-scatter Woodcock path tracing of the medium AMR dataset
+(4 levels, 128^3 root cells, ~51M cells, 256 Gaussians + noise) at
+1024x1024, 16 spp, <= 8 bounces, albedo 0.8, HG g = 0.3, one directional
+light, 128^3 majorant grid -- through the ExaStitch CUDA path.
+
+A step renders one 1024x1024x16 frame (16.8M camera paths).  Prints one
+JSON line (rank 0).  `--impl reference` times the CPU oracle's restatement
+of the same integrator on the host cores instead (a bounded pixel sample per
+step).  Multi-GPU runs (torchrun) render independent frames per rank
+(replicas: no data-path collective), scaling = weak.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "paths/s"
+WIDTH, HEIGHT, SPP = 1024, 1024, 16
+NUM_MCS = (128, 128, 128)
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="medium", choices=["medium", "small", "tiny"])
+    ap.add_argument("--width", type=int, default=WIDTH)
+    ap.add_argument("--height", type=int, default=HEIGHT)
+    ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="warm-up + 1 step, no extras (for ncu)")
+    return ap.parse_args()
+
+
+def workload_config(a):
+    return {
+        "workload": f"{a.config} AMR ({'4 levels, 128^3 root' if a.config == 'medium' else a.config}), "
+                    f"path tracing {a.width}x{a.height} {a.spp} spp",
+        "dataset": a.config,
+        "width": a.width, "height": a.height, "spp": a.spp,
+        "max_bounces": 8, "albedo": 0.8, "hg_g": 0.3, "light": "directional",
+        "majorant_grid": list(NUM_MCS), "tf": "64-entry linear RGBA ramp",
+        "l2": "flushed between timed steps (256 MiB write)",
+    }
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "render_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_scene(a, rank):
+    """Dataset, model, sampler and launch parameters of the workload."""
+    from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import datagen
+    from owlexastitcher_gb300 import exastitch as E
+    t0 = time.time()
+    ds = datagen.Dataset(a.config)
+    gen_s = time.time() - t0
+    return ds, gen_s
+
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+    from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import exastitch as E
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    ds, gen_s = make_scene(a, rank)
+    ctx = E.Context(local)
+    r = E.Renderer(ctx, E.ExaStitchModel.from_dataset(ctx, ds), NUM_MCS)
+    lo, hi = r.model.cellBounds
+    r.setColorMap(ramp_tf())
+    r.resize(a.width, a.height)
+    r.spp = a.spp
+    cam = orbit_camera(lo, hi, a.width, a.height)
+    setup_render(r.lp, cam, a.width, a.height, E.PATH_TRACING_INTEGRATOR, a.spp, "directional", True)
+    r.lp.ext.frameID = rank  # independent frames per rank
+    paths_per_step = a.width * a.height * a.spp
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        r.accumID = 0
+        r.render()
+
+    # warm-up
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.sync()
+    if a.profile_only:
+        step()
+        torch.cuda.synchronize()
+        return
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(a.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ctx.sync()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * paths_per_step / (ms / 1e3)
+    clocks = clk.summary()
+
+    # counting launch (same frame): algorithmic work of one launch
+    cnt = torch.zeros(8, dtype=torch.int64, device="cuda")
+    r.lp.ext.stepCounters = cnt.data_ptr()
+    step()
+    torch.cuda.synchronize()
+    r.lp.ext.stepCounters = None
+    c = cnt.cpu().numpy()
+    field_samples, g_samples, e_samples, dda_cells, paths = (int(x) for x in c[:5])
+    counts = np.count_nonzero(ds.indices >= 0, axis=1) if len(ds.indices) else np.array([8])
+    avg_nv = float(counts.mean())
+    alg_bytes = g_samples * 64 + e_samples * (32 + 16 * avg_nv) + dda_cells * 4
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    tr = load_traffic()
+    traffic = None
+    if tr and tr.get("dataset") == a.config:
+        traffic = tr["dram_bytes_per_launch"] * (paths_per_step / tr["paths_per_launch"])
+
+    # end-to-end through the public API: render + read the RGBA8 frame back
+    host_fb = torch.empty(a.width * a.height, dtype=torch.int32, pin_memory=True)
+    e2e_t = []
+    for i in range(max(3, a.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step()
+        host_fb.copy_(r.fb, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    lp_bytes = E.C.sizeof(E.LaunchParams)
+
+    # field point queries (1M uniform points in cellBounds), device and e2e
+    rng = np.random.default_rng(42)
+    P = rng.uniform(lo, hi, (1 << 20, 3)).astype(np.float32)
+    pd = torch.from_numpy(P).cuda()
+    out = torch.empty((1 << 20) * 3, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        r.sampler.sample_device(pd.data_ptr(), out.data_ptr(), len(P), cull=False)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1.0)
+    ev0.record(stream)
+    for _ in range(10):
+        r.sampler.sample_device(pd.data_ptr(), out.data_ptr(), len(P), cull=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    q_dev = 10 * len(P) / (ev0.elapsed_time(ev1) / 1e3)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        r.sampler.sample_host(P, cull=False)
+    q_e2e = 5 * len(P) / (time.perf_counter() - t0)
+    ctx.sync()
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded AMR Gaussians + value noise)",
+            "config": workload_config(a),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_render<PATH_TRACING>",
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "field_samples": {"render_per_s": field_samples / (ms / 1e3), "per_step": field_samples,
+                              "gridlet_per_step": g_samples, "element_per_step": e_samples,
+                              "dda_cells_per_step": dda_cells,
+                              "point_query_per_s": q_dev, "point_query_e2e_per_s": q_e2e,
+                              "point_query_n": len(P)},
+            "e2e": {"value": world * paths_per_step / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": lp_bytes,
+                    "d2h_bytes_per_step": a.width * a.height * 4},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": a.steps,
+            "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
+                                                  "numWedges", "numHexes", "numTets")} | {
+                "field_bytes": ds.field_bytes, "gen_seconds": gen_s},
+            "step_ms": step_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def _oracle_scene(a, ds, lp_src, max_ops, gops, eops, tf):
+    import pyoracle
+    from helpers import host_lp
+    f = pyoracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+    f.set_prim_opacities(gops if len(gops) else None, eops if len(eops) else None)
+
+    class O:
+        pass
+    o = O()
+    o.f, o.tf, o.max_ops = f, np.ascontiguousarray(tf, np.float32), np.ascontiguousarray(max_ops, np.float32)
+    return o
+
+
+def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads):
+    """Renders bands of rows spread over the frame until budget_s is used;
+    returns (paths/s, pixels rendered, seconds)."""
+    rows = h
+    bands = 16
+    band_rows = 1
+    total_px, total_s = 0, 0.0
+    for b in range(bands * 64):
+        y = (b * 37) % rows
+        pb, pe = y * w, (y + band_rows) * w
+        t0 = time.perf_counter()
+        o.f.render(bytes(hl), w, h, pb, pe, nthreads)
+        total_s += time.perf_counter() - t0
+        total_px += pe - pb
+        if total_s >= budget_s:
+            break
+    return total_px * spp / total_s, total_px, total_s
+
+
+def cpu_baseline(a, ds, r, budget_s):
+    """The oracle integrator on the host cores, all threads (OpenMP)."""
+    from helpers import host_lp
+    n = os.cpu_count()
+    ranges, ops = r.sampler.majorants(NUM_MCS)
+    _, gops, eops = r.sampler.prim_majorants()
+    o = _oracle_scene(a, ds, r.lp, ops, gops, eops, r.colorMap)
+    hl, *_ = host_lp(r.lp, o, a.width, a.height)
+    rate, px, secs = _cpu_render_rate(o, hl, a.width, a.height, a.spp, budget_s, n)
+    return {"value": rate, "unit": "paths/s", "cores": n, "kind": "port",
+            "sample": f"{px} pixels x {a.spp} spp (rows spread over the frame), {secs:.1f} s, oracle/oracle.c "
+                      f"with OpenMP; majorants taken from the GPU build (bit-identical in the parity tests)"}
+
+
+def run_reference(a):
+    """--impl reference: the CPU restatement of the integrator (the reference's
+    own path needs OptiX/OWL, which are not available)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import ctypes as C
+    import pyoracle
+    from helpers import host_lp, orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import datagen
+    from owlexastitcher_gb300 import exastitch as E
+    ds = datagen.Dataset(a.config)
+    f = pyoracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+    lo, hi, vr = f.bounds()
+    tf = ramp_tf()
+    xf = (np.float32(vr[0]), np.float32(vr[1]))
+    ranges = f.majorants(NUM_MCS, lo, hi)
+    ops = pyoracle.max_opacities(ranges, tf, xf)
+    gops = pyoracle.max_opacities(f.gridlet_value_ranges(), tf, xf) if len(ds.gridlets) else np.zeros(0, np.float32)
+    eops = f.elem_max_opacities(tf, xf) if len(ds.indices) else np.zeros(0, np.float32)
+    f.set_prim_opacities(gops if len(gops) else None, eops if len(eops) else None)
+    lp = E.LaunchParams()
+    lp.integrator = 0
+    lp.render.dt = 1.0
+    lp.transferFunc.opacityScale = 1.0
+    lp.transferFunc.domain.lower, lp.transferFunc.domain.upper = float(xf[0]), float(xf[1])
+    lp.transferFunc.numValues = len(tf)
+    for A in (lp.voxelSpaceTransform, lp.lightSpaceTransform, lp.ext.voxelSpaceTransformInv):
+        A.l.vx.x = A.l.vy.y = A.l.vz.z = 1.0
+    lp.majorantGrid.dims = E.vec3i(*NUM_MCS)
+    lp.majorantGrid.bounds = E._box(lo, hi)
+    lp.worldSpaceBounds = E._box(lo, hi)
+    lp.ext.cullTransparentPrims = 1
+    cam = orbit_camera(lo, hi, a.width, a.height)
+    setup_render(lp, cam, a.width, a.height, 0, a.spp, "directional", True)
+
+    class O:
+        pass
+    o = O()
+    o.f, o.tf, o.max_ops = f, np.ascontiguousarray(tf), np.ascontiguousarray(ops)
+    hl, *_ = host_lp(lp, o, a.width, a.height)
+    n = os.cpu_count()
+    per_step = max(1.0, a.cpu_seconds / max(1, a.steps + a.warmup))
+    for _ in range(a.warmup):
+        _cpu_render_rate(o, hl, a.width, a.height, a.spp, per_step * 0.3, n)
+    rates, pxs, secs = [], 0, 0.0
+    for _ in range(a.steps):
+        rate, px, s = _cpu_render_rate(o, hl, a.width, a.height, a.spp, per_step, n)
+        rates.append(rate)
+        pxs += px
+        secs += s
+    value = pxs * a.spp / secs
+    sample = (f"{pxs} pixels x {a.spp} spp over {a.steps} steps (rows spread over the frame), "
+              f"oracle/oracle.c restatement with OpenMP; the reference's own path needs OptiX/OWL")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * secs / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded AMR Gaussians + value noise)",
+        "config": workload_config(a),
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": n, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,326 @@
+/*
+ * exastitch.h -- C ABI of the GB300-native ExaStitch volume-rendering path.
+ *
+ * The path: per-macrocell majorant build, ExaStitch field sampling (gridlet
+ * trilinear lookup plus point location in the stitched unstructured boundary
+ * elements) and Woodcock / ratio tracking through a DDA-traversed majorant
+ * grid.  Every entry point is a plain C function taking plain pointers and
+ * sizes; no C++ or CUDA type crosses this boundary.  All functions return an
+ * int status (EXA_OK == 0); on failure exa_last_error() holds a message for
+ * the calling thread.  No exception crosses the boundary.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the owlExaStitcher source tree).
+ *
+ * Threading: one exa_context per host thread.  All device work of a context
+ * is issued on the context's CUDA stream (its own, or one the caller hands
+ * in).  Build steps are synchronous at return; exa_render and
+ * exa_sample_points are asynchronous on that stream (call exa_sync).
+ */
+#ifndef EXASTITCH_H
+#define EXASTITCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status codes                                                        */
+/* ------------------------------------------------------------------ */
+#define EXA_OK               0
+#define EXA_ERR_INVALID      1  /* bad argument, unsupported option     */
+#define EXA_ERR_CUDA         2  /* CUDA runtime error                    */
+#define EXA_ERR_STATE        3  /* call out of order (e.g. no model)     */
+#define EXA_ERR_OOM          4  /* device allocation failed              */
+#define EXA_ERR_DEVICE_LIMIT 5  /* a device-side iteration cap was hit   */
+
+/* device error-flag bits (exa_get_device_errors) */
+#define EXA_DEVERR_DDA_CAP      1u  /* DDA walked more cells than the grid has */
+#define EXA_DEVERR_TRACK_CAP    2u  /* delta/ratio tracking step cap            */
+#define EXA_DEVERR_BVH_STACK    4u  /* element-BVH traversal stack overflow     */
+#define EXA_DEVERR_BOUNCE_CAP   8u  /* path exceeded the hard bounce cap        */
+#define EXA_DEVERR_WATCHDOG    16u  /* persistent-kernel work loop cap          */
+
+/* ------------------------------------------------------------------ */
+/* plain data types (layouts equal to the owl::common types they       */
+/* stand in for: vec3f, vec4f, vec3i, box3f, interval<float>, affine3f) */
+/* ------------------------------------------------------------------ */
+typedef struct { float x, y; } exa_vec2f;
+typedef struct { float x, y, z; } exa_vec3f;
+typedef struct { float x, y, z, w; } exa_vec4f;
+typedef struct { int32_t x, y, z; } exa_vec3i;
+typedef struct { exa_vec2f lower, upper; } exa_box2f;
+typedef struct { exa_vec3f lower, upper; } exa_box3f;
+typedef struct { float lower, upper; } exa_range1f;
+typedef struct { exa_vec3f vx, vy, vz; } exa_linear3f;
+typedef struct { exa_linear3f l; exa_vec3f p; } exa_affine3f;
+
+/* Gridlet.h:22-37 -- a brick of level-`level` dual cells, scalars
+ * (dims+1)^3 fp32 starting at gridletScalars[begin], NaN = absent. */
+typedef struct {
+  exa_vec3i lower;
+  int32_t   level;
+  exa_vec3i dims;
+  uint32_t  begin;
+} exa_gridlet;
+
+/* sampler/Sampler.h:72-76 -- primID < 0: empty space; cellID == -1: the
+ * sample came from a stitching element, else from gridlet primID. */
+typedef struct {
+  int32_t primID;
+  int32_t cellID;
+  float   value;
+} exa_sample;
+
+/* Grid.cuh:21-24 */
+typedef struct {
+  exa_vec3i dims;
+  exa_box3f bounds;
+} exa_grid_traversable;
+
+/* KDTree.cuh:141-144 (slot kept for layout; unused by this sampler) */
+typedef struct {
+  void     *nodes;
+  void     *primRefs;
+  exa_box3f modelBounds;
+} exa_kdtree_traversable;
+
+/* sampler/ExaStitchSampler.h:42-49.  sampleBVH holds this library's
+ * point-location handle (an opaque device address) in the slot that held
+ * the OptixTraversableHandle. */
+typedef struct {
+  uint64_t     sampleBVH;
+  exa_gridlet *gridletBuffer;
+  float       *gridletScalarBuffer;
+} exa_stitch_lp;
+
+#define EXA_CLIP_PLANES_MAX 1   /* common.h:36 */
+#define EXA_LIGHTS_MAX      4   /* common.h:37 */
+
+#define EXA_PATH_TRACING_INTEGRATOR 0   /* common.h:46-48 */
+#define EXA_DIRECT_LIGHT_INTEGRATOR 1
+#define EXA_RAY_MARCHING_INTEGRATOR 2
+
+#define EXA_SHADE_MODE_DEFAULT  0       /* common.h:50-52 */
+#define EXA_SHADE_MODE_GRIDLETS 1
+
+#define EXA_LIGHT_POINT       0
+#define EXA_LIGHT_DIRECTIONAL 1
+
+/* Fields appended after the reference's LaunchParams fields.  They have no
+ * reference counterpart; their defaults (exa_launch_params_init) reproduce
+ * the reference's hard-coded behaviour. */
+typedef struct {
+  int32_t   maxBounces;      /* deviceCode.cu:1050 hard-codes 1024          */
+  float     albedo;          /* < 0: albedo = TF rgb (deviceCode.cu:1061)    */
+  float     hgG;             /* HG anisotropy; reference uses 0 (:1089)      */
+  int32_t   lightType[EXA_LIGHTS_MAX]; /* EXA_LIGHT_POINT / _DIRECTIONAL;   */
+                             /* a directional light's lights[i].pos is the  */
+                             /* direction towards the light                 */
+  exa_affine3f voxelSpaceTransformInv; /* rcp(voxelSpaceTransform)         */
+  int32_t   cullTransparentPrims;      /* 1: primitives with max opacity 0  */
+                             /* are invisible to point location (the        */
+                             /* reference's empty-AABB culling)             */
+  uint32_t  frameID;         /* RNG stream selector for batched frames       */
+  uint32_t *deviceErrors;    /* optional: EXA_DEVERR_* bits are OR-ed here   */
+  unsigned long long *stepCounters; /* optional counting launch: [0] field */
+                             /* samples, [1] gridlet samples, [2] element    */
+                             /* samples, [3] DDA cells, [4] paths            */
+  float    *traceT;          /* optional, per pixel: distance (voxel space) */
+                             /* of the first sample's first interaction, -1 */
+                             /* if the ray left the volume                  */
+  float    *traceTr;         /* optional, per pixel: transmittance of the   */
+                             /* first sample's first shadow ray, -1 if none */
+} exa_lp_ext;
+
+/* LaunchParams.h:56-119, field order and types kept; the sampler union
+ * holds only the ExaStitch member; transferFunc is the buffer variant
+ * (values/numValues, LaunchParams.h:84-87). */
+typedef struct {
+  struct { exa_stitch_lp ess; } sampler;
+  uint32_t  *fbPointer;
+  float     *fbDepth;
+  exa_vec4f *accumBuffer;
+  int32_t    accumID;
+  int32_t    integrator;
+  int32_t    shadeMode;
+  float     *maxOpacities;
+  uint64_t   meshBVH;
+  uint64_t   majorantBVH;
+  exa_kdtree_traversable majorantKDTree;
+  exa_grid_traversable   majorantGrid;
+  exa_box3f    worldSpaceBounds;
+  exa_affine3f voxelSpaceTransform;
+  exa_affine3f lightSpaceTransform;
+  struct {
+    exa_vec4f  *values;
+    int32_t     numValues;
+    exa_range1f domain;
+    float       opacityScale;
+  } transferFunc;
+  struct {
+    exa_vec3f org;
+    exa_vec3f dir_00;
+    exa_vec3f dir_du;
+    exa_vec3f dir_dv;
+  } camera;
+  struct {
+    exa_box2f value;
+    exa_box2f selection;
+    int32_t   active;
+    int32_t   selecting;
+  } subImage;
+  struct {
+    float   dt;
+    int32_t heatMapEnabled;
+    float   heatMapScale;
+    int32_t spp;
+  } render;
+  struct {
+    int32_t   enabled;
+    exa_vec3f N;
+    float     d;
+  } clipPlanes[EXA_CLIP_PLANES_MAX];
+  struct {
+    exa_vec3f pos;
+    float     intensity;
+    int32_t   on;
+  } lights[EXA_LIGHTS_MAX];
+  exa_lp_ext ext;
+} exa_launch_params;
+
+/* model/ExaStitchModel.cpp:259-279 (memStats) plus device footprint */
+typedef struct {
+  uint64_t elemVertexBytes;
+  uint64_t elemIndexBytes;
+  uint64_t gridletBytes;
+  uint64_t emptyScalarsBytes;
+  uint64_t nonEmptyScalarsBytes;
+  uint64_t deviceFieldBytes;     /* field arrays resident in HBM           */
+  uint64_t deviceAccelBytes;     /* point-location tables + element BVH     */
+  uint64_t deviceMajorantBytes;  /* value ranges + max opacities            */
+} exa_mem_stats;
+
+typedef struct exa_context exa_context;
+
+/* ------------------------------------------------------------------ */
+/* context                                                             */
+/* ------------------------------------------------------------------ */
+
+/* Replaces owlContextCreate(nullptr,1) (OWLRenderer.cpp:331).  stream: a
+ * cudaStream_t to issue all work on, or 0 to create a private stream. */
+int exa_context_create(exa_context **out, int device, uint64_t stream);
+int exa_context_destroy(exa_context *ctx);
+/* Message of the last failed call on this thread ("" if none). */
+const char *exa_last_error(void);
+/* Waits for the context's stream; returns EXA_ERR_DEVICE_LIMIT if a
+ * kernel raised a device error flag since the last call. */
+int exa_sync(exa_context *ctx);
+/* Reads and clears the context's device error bits (EXA_DEVERR_*). */
+int exa_get_device_errors(exa_context *ctx, uint32_t *bits);
+/* Library version string. */
+const char *exa_version(void);
+/* sizeof of the ABI structs, for FFI bindings to check their layouts:
+ * 0 exa_launch_params, 1 exa_gridlet, 2 exa_sample, 3 exa_mem_stats,
+ * 4 exa_lp_ext; 0 for other keys. */
+uint64_t exa_abi_sizeof(int32_t which);
+
+/* ------------------------------------------------------------------ */
+/* model  (model/Model.h:29-65, model/ExaStitchModel.h:26-55)          */
+/* ------------------------------------------------------------------ */
+
+/* Replaces ExaStitchModel::load (model/ExaStitchModel.cpp:24-257) for
+ * in-memory arrays: vertices (x,y,z,value), indices 8 per element padded
+ * with -1 (4 = tet, 5 = pyramid, 6 = wedge, 8 = hex), gridlets and their
+ * scalars.  Host pointers; arrays are copied.  Computes cellBounds and
+ * valueRange as the loader does.  Either part may be empty. */
+int exa_model_create(exa_context *ctx,
+                     const exa_vec4f *vertices, uint64_t numVertices,
+                     const int32_t *indices, uint64_t numElems,
+                     const exa_gridlet *gridlets, uint64_t numGridlets,
+                     const float *gridletScalars, uint64_t numGridletScalars);
+/* Model::cellBounds / Model::valueRange (model/Model.h:54-55). */
+int exa_model_get_bounds(exa_context *ctx, exa_box3f *cellBounds,
+                         exa_range1f *valueRange);
+/* Model::setNumGridCells (model/Model.cpp:25-33): fails if the grid was
+ * already set. */
+int exa_model_set_num_grid_cells(exa_context *ctx, exa_vec3i numMCs);
+/* Model::setVoxelSpaceTransform (model/Model.cpp:35-48). */
+int exa_model_set_voxel_space_transform(exa_context *ctx, exa_box3f remapFrom,
+                                        exa_box3f remapTo);
+/* Model::getBounds (model/Model.cpp:50-70): world-space bounds. */
+int exa_model_get_world_bounds(exa_context *ctx, exa_box3f *bounds);
+/* ExaStitchModel::memStats (model/ExaStitchModel.cpp:259-279). */
+int exa_model_mem_stats(exa_context *ctx, exa_mem_stats *out);
+
+/* ------------------------------------------------------------------ */
+/* sampler  (sampler/Sampler.h:28-69, sampler/ExaStitchSampler.h)      */
+/* ------------------------------------------------------------------ */
+
+/* ExaStitchSampler::build (sampler/ExaStitchSampler.cpp:23-340): uploads
+ * the field, builds the per-primitive value ranges, the point-location
+ * accel (gridlet tables + element BVH, replacing the OptiX TLAS) and the
+ * majorant grid (Grid::build, Grid.cu:457-594).  EXA_ERR_STATE where the
+ * reference returns false. */
+int exa_sampler_build(exa_context *ctx);
+/* ExaStitchSampler::computeMaxOpacities (sampler/ExaStitchSampler.cu:
+ * 279-376) and Grid::computeMaxOpacities (Grid.cu:721-737).  colorMap is a
+ * host array of numColors RGBA entries. */
+int exa_sampler_compute_max_opacities(exa_context *ctx,
+                                      const exa_vec4f *colorMap,
+                                      int32_t numColors, exa_range1f xfRange);
+/* ExaStitchSampler::setLPs (sampler/ExaStitchSampler.cpp:356-365) plus the
+ * majorant-grid and max-opacity LP variables OWLRenderer::initGPU and
+ * setColorMap set (OWLRenderer.cpp:435-436, 652-657). */
+int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp);
+/* Sampler::className (sampler/ExaStitchSampler.h:59). */
+const char *exa_sampler_class_name(void);
+/* Grid::valueRanges / Grid::maxOpacities (Grid.h:70-73), copied to host
+ * arrays of numMCs entries (either pointer may be NULL). */
+int exa_get_majorants(exa_context *ctx, exa_range1f *valueRanges,
+                      float *maxOpacities);
+/* Per-primitive value ranges and max opacities (gridletValueRanges,
+ * gridletMaxOpacities, umeshMaxOpacities: sampler/ExaStitchSampler.h:
+ * 97-103), host arrays; any pointer may be NULL. */
+int exa_get_prim_majorants(exa_context *ctx, exa_range1f *gridletRanges,
+                           float *gridletMaxOpacities,
+                           float *elemMaxOpacities);
+
+/* ------------------------------------------------------------------ */
+/* field sampling: sample() (sampler/ExaStitchSampler.h:128-140)       */
+/* ------------------------------------------------------------------ */
+
+/* Point query at n positions (voxel space).  Device pointers; async on the
+ * context stream.  cullTransparent: 1 = primitives whose max opacity is 0
+ * are invisible, as in the reference after computeMaxOpacities. */
+int exa_sample_points(exa_context *ctx, const exa_vec3f *posDevice,
+                      uint64_t n, exa_sample *outDevice,
+                      int32_t cullTransparent);
+/* Same, host buffers: copies in, samples, copies out; synchronous. */
+int exa_sample_points_host(exa_context *ctx, const exa_vec3f *posHost,
+                           uint64_t n, exa_sample *outHost,
+                           int32_t cullTransparent);
+
+/* ------------------------------------------------------------------ */
+/* rendering: renderFrame_ExaStitchSampler (deviceCode.cu:1390-1400)   */
+/* ------------------------------------------------------------------ */
+
+/* Fills lp with the reference defaults (OWLRenderer::initGPU,
+ * OWLRenderer.cpp:548-578; render(), :610-622) and the extension
+ * defaults that reproduce the reference behaviour. */
+int exa_launch_params_init(exa_launch_params *lp);
+/* One frame: width*height pixels, lp->render.spp samples each, into
+ * lp->fbPointer (RGBA8) and lp->accumBuffer (device pointers owned by the
+ * caller).  Replaces owlLaunch2D(rayGen,w,h,lp) (OWLRenderer.cpp:621).
+ * Async on the context stream. */
+int exa_render(exa_context *ctx, const exa_launch_params *lp,
+               int32_t width, int32_t height);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXASTITCH_H */

@@ -1,0 +1,1375 @@
+/*
+ * oracle.c -- CPU restatement of the owlExaStitcher ExaStitch rendering path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Only tests/, the
+ * smoke check and bench.py's CPU-baseline leg load this library.
+ *
+ * Built with -ffp-contract=off; every float expression is written in the
+ * operation order of the reference line it cites (file:line relative to the
+ * owlExaStitcher tree), with float literals so nothing is promoted to double.
+ * Third-party helpers the reference takes from OWL (not vendored in the
+ * reference tree) are defined here as plain textbook operations:
+ *   dot(a,b) = a.x*b.x + a.y*b.y + a.z*b.z, cross = the usual determinant
+ *   rows, length = sqrtf(dot), normalize(v) = v * (1.f/sqrtf(dot(v,v))),
+ *   min/max = (a<b?a:b)/(a>b?a:b), box contains/overlaps inclusive,
+ *   rcp(x) = 1.f/x, xfmPoint(A,p) = (p.x*vx + p.y*vy + p.z*vz) + A.p,
+ *   make_rgba = 8 bits per channel, min(255,max(0,int(c*256))).
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef exa_vec3f v3;
+typedef exa_vec4f v4;
+typedef exa_vec3i v3i;
+
+/* ================================================================== */
+/* small vector helpers (textbook definitions, see header comment)     */
+/* ================================================================== */
+static inline v3 mk3(float x, float y, float z) { v3 r = {x, y, z}; return r; }
+static inline v3 add3(v3 a, v3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 sub3(v3 a, v3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 mul3(v3 a, v3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 div3(v3 a, v3 b) { return mk3(a.x / b.x, a.y / b.y, a.z / b.z); }
+static inline v3 muls(v3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+static inline v3 smul(float s, v3 a) { return mk3(s * a.x, s * a.y, s * a.z); }
+static inline float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 cross3(v3 a, v3 b)
+{
+  return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline float fmin_t(float a, float b) { return a < b ? a : b; }
+static inline float fmax_t(float a, float b) { return a > b ? a : b; }
+static inline v3 min3(v3 a, v3 b) { return mk3(fmin_t(a.x, b.x), fmin_t(a.y, b.y), fmin_t(a.z, b.z)); }
+static inline v3 max3(v3 a, v3 b) { return mk3(fmax_t(a.x, b.x), fmax_t(a.y, b.y), fmax_t(a.z, b.z)); }
+static inline float rmin3(v3 a) { return fmin_t(a.x, fmin_t(a.y, a.z)); }
+static inline float rmax3(v3 a) { return fmax_t(a.x, fmax_t(a.y, a.z)); }
+static inline float len3(v3 a) { return sqrtf(dot3(a, a)); }
+static inline v3 norm3(v3 a) { return muls(a, 1.f / sqrtf(dot3(a, a))); }
+static inline v3 xyz(v4 a) { return mk3(a.x, a.y, a.z); }
+static inline int imin_t(int a, int b) { return a < b ? a : b; }
+static inline int imax_t(int a, int b) { return a > b ? a : b; }
+static inline int iclamp(int v, int lo, int hi) { return imin_t(imax_t(v, lo), hi); }
+
+/* owl LinearSpace3f * vec3f: b.x*vx + b.y*vy + b.z*vz */
+static inline v3 xfm_vector(const exa_affine3f *A, v3 v)
+{
+  return add3(add3(smul(v.x, A->l.vx), smul(v.y, A->l.vy)), smul(v.z, A->l.vz));
+}
+static inline v3 xfm_point(const exa_affine3f *A, v3 p)
+{
+  return add3(xfm_vector(A, p), A->p);
+}
+
+/* ================================================================== */
+/* project-defined math                                                */
+/* ================================================================== */
+
+/* splitmix64 finaliser (Steele, Lea, Flood 2014; Vigna's constants) */
+uint64_t oc_mix64(uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
+/* Natural log for positive normal floats: x = m*2^e with m in
+ * [sqrt(1/2), sqrt(2)); log(m) = 2*atanh(s), s = (m-1)/(m+1), by its
+ * Taylor series through s^9; log(2) split in a 16-bit head and a tail. */
+float oc_log(float x)
+{
+  const uint32_t bits = f2u(x);
+  int e = (int)((bits >> 23) & 0xffu) - 127;
+  float m = u2f((bits & 0x7fffffu) | 0x3f800000u);
+  if (m > 1.41421354f) { m = m * 0.5f; e = e + 1; }
+  const float s  = (m - 1.f) / (m + 1.f);
+  const float s2 = s * s;
+  const float p  = s2 * (0.333333343f + s2 * (0.200000003f + s2 * (0.142857149f + s2 * 0.111111112f)));
+  const float lm = 2.f * s + (2.f * s) * p;
+  const float fe = (float)e;
+  return fe * 0.693145752f + (fe * 1.42860677e-06f + lm);
+}
+
+/* sin and cos of 2*pi*u: quadrant from round(4u), remainder angle
+ * theta in [-pi/4, pi/4], Taylor series through theta^9 / theta^8. */
+void oc_sincos_turns(float u, float *s, float *c)
+{
+  const float u4 = u * 4.f;
+  const float q  = floorf(u4 + 0.5f);
+  const float r  = u4 - q;
+  const float t  = r * 1.57079637f;
+  const float t2 = t * t;
+  const float sp = t + (t * t2) * (-0.166666672f + t2 * (0.00833333377f + t2 * (-0.000198412701f + t2 * 2.75573188e-06f)));
+  const float cp = 1.f + t2 * (-0.5f + t2 * (0.0416666679f + t2 * (-0.00138888892f + t2 * 2.48015876e-05f)));
+  const int qi = ((int)q) & 3;
+  if (qi == 0)      { *s = sp;  *c = cp;  }
+  else if (qi == 1) { *s = cp;  *c = -sp; }
+  else if (qi == 2) { *s = -sp; *c = -cp; }
+  else              { *s = -cp; *c = sp;  }
+}
+
+/* Counter-based stream: one key per (pixel, accumulation frame, batch
+ * frame); the n-th draw is mix64(key + n*golden) >> 40 scaled by 2^-24.
+ * Stands in for owl::common::LCG<4> (deviceCode.cu:41,1278). */
+void oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID)
+{
+  r->key = oc_mix64(((uint64_t)pixelID << 32) ^ (uint64_t)accumID ^
+                    oc_mix64((uint64_t)frameID + 0x5851f42d4c957f2dull));
+  r->counter = 0;
+}
+
+float oc_rng_next(oc_rng *r)
+{
+  r->counter += 1;
+  const uint64_t z = oc_mix64(r->key + r->counter * 0x9e3779b97f4a7c15ull);
+  return (float)(uint32_t)(z >> 40) * 5.96046448e-08f;
+}
+
+/* ================================================================== */
+/* Gridlet.h:30-98                                                     */
+/* ================================================================== */
+static inline float lerpf_(float a, float b, float x) /* common.h:64-68 */
+{
+  return (1.f - x) * a + x * b;
+}
+
+int oc_intersect_gridlet(float *value, int *cellID, v3 pos,
+                         const exa_gridlet *g, const float *scalars)
+{
+  /* getBounds, Gridlet.h:31-36 */
+  const float cw = (float)(1 << g->level);
+  const v3 lo = muls(mk3((float)g->lower.x + 0.5f, (float)g->lower.y + 0.5f,
+                         (float)g->lower.z + 0.5f), cw);
+  const v3 hi = muls(mk3(((float)g->lower.x + (float)g->dims.x) + 0.5f,
+                         ((float)g->lower.y + (float)g->dims.y) + 0.5f,
+                         ((float)g->lower.z + (float)g->dims.z) + 0.5f), cw);
+  /* Gridlet.h:48 contains() */
+  if (!(lo.x <= pos.x && lo.y <= pos.y && lo.z <= pos.z &&
+        pos.x <= hi.x && pos.y <= hi.y && pos.z <= hi.z))
+    return 0;
+  const int nx = g->dims.x + 1, ny = g->dims.y + 1, nz = g->dims.z + 1;
+  const float lw = (float)(1 << g->level);
+  const v3 p = mk3((pos.x - lo.x) / lw, (pos.y - lo.y) / lw, (pos.z - lo.z) / lw);
+  const int ix = (int)p.x, iy = (int)p.y, iz = (int)p.z;
+  const int ax = imin_t(ix + 1, nx - 1), ay = imin_t(iy + 1, ny - 1), az = imin_t(iz + 1, nz - 1);
+#define LIN(x, y, z) ((z) * ny * nx + (y) * nx + (x))
+  const float *S = scalars + g->begin;
+  const float f1 = S[LIN(ix, iy, iz)], f2 = S[LIN(ax, iy, iz)];
+  const float f3 = S[LIN(ix, ay, iz)], f4 = S[LIN(ax, ay, iz)];
+  const float f5 = S[LIN(ix, iy, az)], f6 = S[LIN(ax, iy, az)];
+  const float f7 = S[LIN(ix, ay, az)], f8 = S[LIN(ax, ay, az)];
+#undef LIN
+  if (isnan(f1) || isnan(f2) || isnan(f3) || isnan(f4) ||
+      isnan(f5) || isnan(f6) || isnan(f7) || isnan(f8))
+    return 0;
+  const v3 frac = mk3(p.x - (float)ix, p.y - (float)iy, p.z - (float)iz);
+  const float f12 = lerpf_(f1, f2, frac.x);
+  const float f56 = lerpf_(f5, f6, frac.x);
+  const float f34 = lerpf_(f3, f4, frac.x);
+  const float f78 = lerpf_(f7, f8, frac.x);
+  const float f1234 = lerpf_(f12, f34, frac.y);
+  const float f5678 = lerpf_(f56, f78, frac.y);
+  *value = lerpf_(f1234, f5678, frac.z);
+  *cellID = iz * g->dims.y * g->dims.x + iy * g->dims.x + ix;
+  return 1;
+}
+
+/* ================================================================== */
+/* Plane.h:23-99                                                       */
+/* ================================================================== */
+typedef struct { v3 N; float d; } plane_t;
+static inline plane_t make_plane(v3 a, v3 b, v3 c) /* Plane.h:32-38 */
+{
+  plane_t p;
+  p.N = cross3(sub3(b, a), sub3(c, a));
+  p.d = dot3(a, p.N);
+  return p;
+}
+static inline float plane_eval(plane_t p, v3 v) { return dot3(v, p.N) - p.d; }
+
+int oc_intersect_tet(float *value, v3 P, v4 a, v4 b, v4 c, v4 d)
+{
+  const v3 va = sub3(xyz(a), P), vb = sub3(xyz(b), P);
+  const v3 vc = sub3(xyz(c), P), vd = sub3(xyz(d), P);
+  const plane_t pa = make_plane(vb, vd, vc);
+  const plane_t pb = make_plane(va, vc, vd);
+  const plane_t pc = make_plane(va, vd, vb);
+  const plane_t pd = make_plane(va, vb, vc);
+  const v3 zero = mk3(0.f, 0.f, 0.f);
+  const float fa = plane_eval(pa, zero) / plane_eval(pa, va);
+  if (fa < 0.f || fa > 1.f) return 0;
+  /* Plane.h:89,92,95 test fa > 1 (not fb/fc/fd); kept as written */
+  const float fb = plane_eval(pb, zero) / plane_eval(pb, vb);
+  if (fb < 0.f || fa > 1.f) return 0;
+  const float fc = plane_eval(pc, zero) / plane_eval(pc, vc);
+  if (fc < 0.f || fa > 1.f) return 0;
+  const float fd = plane_eval(pd, zero) / plane_eval(pd, vd);
+  if (fd < 0.f || fa > 1.f) return 0;
+  *value = fa * a.w + fb * b.w + fc * c.w + fd * d.w;
+  return 1;
+}
+
+/* ================================================================== */
+/* UElems.h:40-464 (Newton inversion of the trilinear-type maps)       */
+/* ================================================================== */
+static inline float det3(v3 x, v3 y, v3 z) { return dot3(x, cross3(y, z)); }
+
+static void pyr_fns(const float *pc, float *sf) /* UElems.h:46-60 */
+{
+  const float rm = 1.f - pc[0], sm = 1.f - pc[1], tm = 1.f - pc[2];
+  sf[0] = rm * sm * tm;
+  sf[1] = pc[0] * sm * tm;
+  sf[2] = pc[0] * pc[1] * tm;
+  sf[3] = rm * pc[1] * tm;
+  sf[4] = pc[2];
+}
+static void pyr_derivs(const float *pc, float *d) /* UElems.h:62-86 */
+{
+  d[0] = -(pc[1] - 1.f) * (pc[2] - 1.f);
+  d[1] = (pc[1] - 1.f) * (pc[2] - 1.f);
+  d[2] = pc[1] - pc[1] * pc[2];
+  d[3] = pc[1] * (pc[2] - 1.f);
+  d[4] = 0.f;
+  d[5] = -(pc[0] - 1.f) * (pc[2] - 1.f);
+  d[6] = pc[0] * (pc[2] - 1.f);
+  d[7] = pc[0] - pc[0] * pc[2];
+  d[8] = (pc[0] - 1.f) * (pc[2] - 1.f);
+  d[9] = 0.f;
+  d[10] = -(pc[0] - 1.f) * (pc[1] - 1.f);
+  d[11] = pc[0] * (pc[1] - 1.f);
+  d[12] = -pc[0] * pc[1];
+  d[13] = (pc[0] - 1.f) * pc[1];
+  d[14] = 1.f;
+}
+static void wedge_fns(const float *pc, float *sf) /* UElems.h:180-189 */
+{
+  sf[0] = (1.f - pc[0] - pc[1]) * (1.f - pc[2]);
+  sf[1] = pc[0] * (1.f - pc[2]);
+  sf[2] = pc[1] * (1.f - pc[2]);
+  sf[3] = (1.f - pc[0] - pc[1]) * pc[2];
+  sf[4] = pc[0] * pc[2];
+  sf[5] = pc[1] * pc[2];
+}
+static void wedge_derivs(const float *pc, float *d) /* UElems.h:191-217 */
+{
+  d[0] = -1.f + pc[2];
+  d[1] = 1.f - pc[2];
+  d[2] = 0.f;
+  d[3] = -pc[2];
+  d[4] = pc[2];
+  d[5] = 0.f;
+  d[6] = -1.f + pc[2];
+  d[7] = 0.f;
+  d[8] = 1.f - pc[2];
+  d[9] = -pc[2];
+  d[10] = 0.f;
+  d[11] = pc[2];
+  d[12] = -1.f + pc[0] + pc[1];
+  d[13] = -pc[0];
+  d[14] = -pc[1];
+  d[15] = 1.f - pc[0] - pc[1];
+  d[16] = pc[0];
+  d[17] = pc[1];
+}
+static void hex_fns(const float *pc, float *sf) /* UElems.h:313-330 */
+{
+  const float rm = 1.f - pc[0], sm = 1.f - pc[1], tm = 1.f - pc[2];
+  sf[0] = rm * sm * tm;
+  sf[1] = pc[0] * sm * tm;
+  sf[2] = pc[0] * pc[1] * tm;
+  sf[3] = rm * pc[1] * tm;
+  sf[4] = rm * sm * pc[2];
+  sf[5] = pc[0] * sm * pc[2];
+  sf[6] = pc[0] * pc[1] * pc[2];
+  sf[7] = rm * pc[1] * pc[2];
+}
+static void hex_derivs(const float *pc, float *d) /* UElems.h:332-370 */
+{
+  const float rm = 1.f - pc[0], sm = 1.f - pc[1], tm = 1.f - pc[2];
+  d[0] = -sm * tm;
+  d[1] = sm * tm;
+  d[2] = pc[1] * tm;
+  d[3] = -pc[1] * tm;
+  d[4] = -sm * pc[2];
+  d[5] = sm * pc[2];
+  d[6] = pc[1] * pc[2];
+  d[7] = -pc[1] * pc[2];
+  d[8] = -rm * tm;
+  d[9] = -pc[0] * tm;
+  d[10] = pc[0] * tm;
+  d[11] = rm * tm;
+  d[12] = -rm * pc[2];
+  d[13] = -pc[0] * pc[2];
+  d[14] = pc[0] * pc[2];
+  d[15] = rm * pc[2];
+  d[16] = -rm * sm;
+  d[17] = -pc[0] * sm;
+  d[18] = -pc[0] * pc[1];
+  d[19] = -rm * pc[1];
+  d[20] = rm * sm;
+  d[21] = pc[0] * sm;
+  d[22] = pc[0] * pc[1];
+  d[23] = rm * pc[1];
+}
+
+/* shared Newton loop of intersectPyrEXT / WedgeEXT / HexEXT
+ * (UElems.h:98-176, 229-309, 384-463); NV vertices; kind 1 = wedge */
+static int newton_elem(float *value, v3 P, const v4 *V, int NV,
+                       void (*fns)(const float *, float *),
+                       void (*derivs)(const float *, float *), int isWedge)
+{
+  float pc[3] = {0.5f, 0.5f, 0.5f};
+  float d[24];
+  float w[8];
+  int converged = 0;
+  for (int it = 0; !converged && it < 10; it++) {
+    fns(pc, w);
+    derivs(pc, d);
+    v3 fcol = mk3(0.f, 0.f, 0.f), rcol = fcol, scol = fcol, tcol = fcol;
+    for (int i = 0; i < NV; ++i) {
+      const v3 pt = xyz(V[i]);
+      fcol = add3(fcol, muls(pt, w[i]));
+      rcol = add3(rcol, muls(pt, d[i]));
+      scol = add3(scol, muls(pt, d[i + NV]));
+      tcol = add3(tcol, muls(pt, d[i + 2 * NV]));
+    }
+    fcol = sub3(fcol, P);
+    const float dd = det3(rcol, scol, tcol);
+    if (fabsf(dd) < 1e-6f) return 0;
+    const float d0 = det3(fcol, scol, tcol) / dd;
+    const float d1 = det3(rcol, fcol, tcol) / dd;
+    const float d2 = det3(rcol, scol, fcol) / dd;
+    pc[0] = pc[0] - d0;
+    pc[1] = pc[1] - d1;
+    pc[2] = pc[2] - d2;
+    /* UElems.h:147-154: the 1e-4 / 1e6 literals are double constants;
+     * the comparisons therefore run in double, as written there */
+    if (((double)fabsf(d0) < 1e-4) & ((double)fabsf(d1) < 1e-4) &
+        ((double)fabsf(d2) < 1e-4)) {
+      converged = 1;
+    } else if (((double)fabsf(pc[0]) > 1e6) | ((double)fabsf(pc[1]) > 1e6) |
+               ((double)fabsf(pc[2]) > 1e6)) {
+      return 0;
+    }
+  }
+  if (!converged) return 0;
+  /* UElems.h:161-162: 0.f - 1e-6 and 1.f + 1e-6 are double expressions
+   * stored into float */
+  const float lower = (float)(0.0 - 1e-6);
+  const float upper = (float)(1.0 + 1e-6);
+  int inside = pc[0] >= lower && pc[0] <= upper && pc[1] >= lower &&
+               pc[1] <= upper && pc[2] >= lower && pc[2] <= upper;
+  if (isWedge) inside = inside && (pc[0] + pc[1] <= upper);
+  if (!inside) return 0;
+  float val = 0.f;
+  for (int i = 0; i < NV; i++) val += w[i] * V[i].w;
+  *value = val;
+  return 1;
+}
+
+int oc_intersect_pyr(float *value, v3 P, const v4 *v)
+{
+  return newton_elem(value, P, v, 5, pyr_fns, pyr_derivs, 0);
+}
+int oc_intersect_wedge(float *value, v3 P, const v4 *v)
+{
+  return newton_elem(value, P, v, 6, wedge_fns, wedge_derivs, 1);
+}
+int oc_intersect_hex(float *value, v3 P, const v4 *v)
+{
+  return newton_elem(value, P, v, 8, hex_fns, hex_derivs, 0);
+}
+
+/* sampler/programs/ExaStitchSampler.cu:133-161: vertex count selects the
+ * element type (4 tet, 5 pyramid, 6 wedge, 8 hex) */
+int oc_intersect_elem(float *value, v3 P, const int32_t *idx, const v4 *vertices)
+{
+  v4 v[8];
+  int nv = 0;
+  for (int i = 0; i < 8; ++i)
+    if (idx[i] >= 0) { nv++; v[i] = vertices[idx[i]]; }
+  if (nv == 4) return oc_intersect_tet(value, P, v[0], v[1], v[2], v[3]);
+  if (nv == 5) return oc_intersect_pyr(value, P, v);
+  if (nv == 6) return oc_intersect_wedge(value, P, v);
+  if (nv == 8) return oc_intersect_hex(value, P, v);
+  return 0;
+}
+
+/* Grid.cuh:51-59 */
+v3i oc_project_on_grid(v3 V, v3i dims, exa_box3f b)
+{
+  const v3 V01 = div3(sub3(V, b.lower), sub3(b.upper, b.lower));
+  v3i r;
+  r.x = iclamp((int)(V01.x * (float)dims.x), 0, dims.x - 1);
+  r.y = iclamp((int)(V01.y * (float)dims.y), 0, dims.y - 1);
+  r.z = iclamp((int)(V01.z * (float)dims.z), 0, dims.z - 1);
+  return r;
+}
+
+/* ================================================================== */
+/* field container + uniform-grid point-location accel                 */
+/* ================================================================== */
+struct oc_field {
+  const v4 *vertices; uint64_t numVertices;
+  const int32_t *indices; uint64_t numElems;
+  const exa_gridlet *gridlets; uint64_t numGridlets;
+  const float *scalars; uint64_t numScalars;
+  const float *gridletMaxOps, *elemMaxOps;
+  /* accel: uniform grid over the union of primitive bounds; each cell
+   * lists every primitive whose closed AABB touches it (gridlets first,
+   * then elements, each in ascending index) */
+  exa_box3f gb; v3i gd; v3 cs;
+  uint32_t *cellBegin; /* gd.x*gd.y*gd.z + 1 */
+  int32_t *items;      /* >= 0: gridlet id; < 0: -(elem id) - 1 */
+};
+
+static exa_box3f gridlet_bounds(const exa_gridlet *g)
+{
+  const float cw = (float)(1 << g->level);
+  exa_box3f b;
+  b.lower = muls(mk3((float)g->lower.x + 0.5f, (float)g->lower.y + 0.5f,
+                     (float)g->lower.z + 0.5f), cw);
+  b.upper = muls(mk3(((float)g->lower.x + (float)g->dims.x) + 0.5f,
+                     ((float)g->lower.y + (float)g->dims.y) + 0.5f,
+                     ((float)g->lower.z + (float)g->dims.z) + 0.5f), cw);
+  return b;
+}
+
+static exa_box3f elem_bounds(const oc_field *f, uint64_t e)
+{
+  exa_box3f b;
+  b.lower = mk3(INFINITY, INFINITY, INFINITY);
+  b.upper = mk3(-INFINITY, -INFINITY, -INFINITY);
+  for (int i = 0; i < 8; ++i) {
+    const int idx = f->indices[e * 8 + i];
+    if (idx < 0) break;
+    const v3 p = xyz(f->vertices[idx]);
+    b.lower = min3(b.lower, p);
+    b.upper = max3(b.upper, p);
+  }
+  return b;
+}
+
+static void cell_range(const oc_field *f, exa_box3f b, v3i *lo, v3i *hi)
+{
+  lo->x = iclamp((int)floorf((b.lower.x - f->gb.lower.x) / f->cs.x), 0, f->gd.x - 1);
+  lo->y = iclamp((int)floorf((b.lower.y - f->gb.lower.y) / f->cs.y), 0, f->gd.y - 1);
+  lo->z = iclamp((int)floorf((b.lower.z - f->gb.lower.z) / f->cs.z), 0, f->gd.z - 1);
+  hi->x = iclamp((int)floorf((b.upper.x - f->gb.lower.x) / f->cs.x), 0, f->gd.x - 1);
+  hi->y = iclamp((int)floorf((b.upper.y - f->gb.lower.y) / f->cs.y), 0, f->gd.y - 1);
+  hi->z = iclamp((int)floorf((b.upper.z - f->gb.lower.z) / f->cs.z), 0, f->gd.z - 1);
+}
+
+oc_field *oc_field_create(const v4 *vertices, uint64_t numVertices,
+                          const int32_t *indices, uint64_t numElems,
+                          const exa_gridlet *gridlets, uint64_t numGridlets,
+                          const float *scalars, uint64_t numScalars)
+{
+  oc_field *f = (oc_field *)calloc(1, sizeof(oc_field));
+  f->vertices = vertices; f->numVertices = numVertices;
+  f->indices = indices; f->numElems = numElems;
+  f->gridlets = gridlets; f->numGridlets = numGridlets;
+  f->scalars = scalars; f->numScalars = numScalars;
+  exa_box3f all;
+  all.lower = mk3(INFINITY, INFINITY, INFINITY);
+  all.upper = mk3(-INFINITY, -INFINITY, -INFINITY);
+  double vol = 0.0;
+  for (uint64_t g = 0; g < numGridlets; ++g) {
+    const exa_box3f b = gridlet_bounds(&gridlets[g]);
+    all.lower = min3(all.lower, b.lower); all.upper = max3(all.upper, b.upper);
+  }
+  for (uint64_t e = 0; e < numElems; ++e) {
+    const exa_box3f b = elem_bounds(f, e);
+    all.lower = min3(all.lower, b.lower); all.upper = max3(all.upper, b.upper);
+    vol += (double)(b.upper.x - b.lower.x) * (b.upper.y - b.lower.y) * (b.upper.z - b.lower.z);
+  }
+  if (numGridlets + numElems == 0) {
+    all.lower = mk3(0.f, 0.f, 0.f); all.upper = mk3(1.f, 1.f, 1.f);
+  }
+  f->gb = all;
+  /* cell size: about the mean element extent, at most 256 cells per axis */
+  const v3 ext = sub3(all.upper, all.lower);
+  const double maxExt = fmax(fmax(ext.x, ext.y), ext.z);
+  double cellW = numElems ? cbrt(vol / (double)numElems) * 2.0 : maxExt / 32.0;
+  if (cellW < maxExt / 256.0) cellW = maxExt / 256.0;
+  if (cellW <= 0.0) cellW = 1.0;
+  f->gd.x = imax_t(1, (int)ceil(ext.x / cellW));
+  f->gd.y = imax_t(1, (int)ceil(ext.y / cellW));
+  f->gd.z = imax_t(1, (int)ceil(ext.z / cellW));
+  f->cs = mk3(fmax_t(ext.x, 1e-30f) / (float)f->gd.x, fmax_t(ext.y, 1e-30f) / (float)f->gd.y,
+              fmax_t(ext.z, 1e-30f) / (float)f->gd.z);
+  const uint64_t nc = (uint64_t)f->gd.x * f->gd.y * f->gd.z;
+  f->cellBegin = (uint32_t *)calloc(nc + 1, sizeof(uint32_t));
+  /* two passes: count, then fill */
+  for (int pass = 0; pass < 2; ++pass) {
+    uint32_t *cursor = NULL;
+    if (pass == 1) {
+      uint64_t acc = 0;
+      for (uint64_t c = 0; c < nc; ++c) { const uint32_t k = f->cellBegin[c]; f->cellBegin[c] = (uint32_t)acc; acc += k; }
+      f->cellBegin[nc] = (uint32_t)acc;
+      f->items = (int32_t *)malloc((acc ? acc : 1) * sizeof(int32_t));
+      cursor = (uint32_t *)malloc(nc * sizeof(uint32_t));
+      memcpy(cursor, f->cellBegin, nc * sizeof(uint32_t));
+    }
+    for (uint64_t k = 0; k < numGridlets + numElems; ++k) {
+      exa_box3f b = k < numGridlets ? gridlet_bounds(&gridlets[k]) : elem_bounds(f, k - numGridlets);
+      v3i lo, hi;
+      cell_range(f, b, &lo, &hi);
+      for (int z = lo.z; z <= hi.z; ++z)
+        for (int y = lo.y; y <= hi.y; ++y)
+          for (int x = lo.x; x <= hi.x; ++x) {
+            const uint64_t c = ((uint64_t)z * f->gd.y + y) * f->gd.x + x;
+            if (pass == 0) f->cellBegin[c]++;
+            else f->items[cursor[c]++] = k < numGridlets ? (int32_t)k : -(int32_t)(k - numGridlets) - 1;
+          }
+    }
+    free(cursor);
+  }
+  return f;
+}
+
+void oc_field_destroy(oc_field *f)
+{
+  if (!f) return;
+  free(f->cellBegin);
+  free(f->items);
+  free(f);
+}
+
+void oc_field_set_prim_opacities(oc_field *f, const float *g, const float *e)
+{
+  f->gridletMaxOps = g;
+  f->elemMaxOps = e;
+}
+
+/* model/ExaStitchModel.cpp:78-109 and 224-245 */
+void oc_field_bounds(const oc_field *f, exa_box3f *cb, exa_range1f *vr)
+{
+  exa_box3f b;
+  b.lower = mk3(INFINITY, INFINITY, INFINITY);
+  b.upper = mk3(-INFINITY, -INFINITY, -INFINITY);
+  exa_range1f r = {1e30f, -1e30f};
+  for (uint64_t e = 0; e < f->numElems; ++e)
+    for (int j = 0; j < 8; ++j) {
+      const int idx = f->indices[e * 8 + j];
+      if (idx < 0) continue;
+      const v4 v = f->vertices[idx];
+      b.lower = min3(b.lower, xyz(v)); b.upper = max3(b.upper, xyz(v));
+      /* std::min(lower, w): NaN never replaces the running value */
+      if (v.w < r.lower) r.lower = v.w;
+      if (r.upper < v.w) r.upper = v.w;
+    }
+  for (uint64_t g = 0; g < f->numGridlets; ++g) {
+    const exa_gridlet *gl = &f->gridlets[g];
+    const uint64_t n = (uint64_t)(gl->dims.x + 1) * (gl->dims.y + 1) * (gl->dims.z + 1);
+    for (uint64_t i = 0; i < n; ++i) {
+      const float s = f->scalars[gl->begin + i];
+      if (s < r.lower) r.lower = s;
+      if (r.upper < s) r.upper = s;
+    }
+    const exa_box3f gb = gridlet_bounds(gl);
+    b.lower = min3(b.lower, gb.lower); b.upper = max3(b.upper, gb.lower);
+    b.lower = min3(b.lower, gb.upper); b.upper = max3(b.upper, gb.upper);
+  }
+  *cb = b;
+  *vr = r;
+}
+
+static inline int gridlet_visible(const oc_field *f, int g, int cull)
+{
+  return !(cull && f->gridletMaxOps && f->gridletMaxOps[g] == 0.f);
+}
+static inline int elem_visible(const oc_field *f, int e, int cull)
+{
+  return !(cull && f->elemMaxOps && f->elemMaxOps[e] == 0.f);
+}
+
+static inline int64_t lookup_cell(const oc_field *f, v3 p)
+{
+  if (!(p.x >= f->gb.lower.x && p.y >= f->gb.lower.y && p.z >= f->gb.lower.z &&
+        p.x <= f->gb.upper.x && p.y <= f->gb.upper.y && p.z <= f->gb.upper.z))
+    return -1;
+  const int x = iclamp((int)floorf((p.x - f->gb.lower.x) / f->cs.x), 0, f->gd.x - 1);
+  const int y = iclamp((int)floorf((p.y - f->gb.lower.y) / f->cs.y), 0, f->gd.y - 1);
+  const int z = iclamp((int)floorf((p.z - f->gb.lower.z) / f->cs.z), 0, f->gd.z - 1);
+  return ((int64_t)z * f->gd.y + y) * f->gd.x + x;
+}
+
+/* sample() (sampler/ExaStitchSampler.h:128-140) with the OptiX query
+ * replaced by the canonical rule: lowest-index containing gridlet, else
+ * lowest-index containing element; primitives with max opacity 0 are
+ * invisible when culling (programs/ExaStitchSampler.cu:35-41,81-83). */
+exa_sample oc_sample(const oc_field *f, v3 pos, int cull)
+{
+  exa_sample s = {-1, -1, 0.f};
+  const int64_t c = lookup_cell(f, pos);
+  if (c < 0) return s;
+  int bestG = -1, bestE = -1;
+  float gv = 0.f, ev = 0.f;
+  int gc = -1;
+  for (uint32_t i = f->cellBegin[c]; i < f->cellBegin[c + 1]; ++i) {
+    const int32_t it = f->items[i];
+    if (it >= 0) {
+      if (bestG >= 0 && it >= bestG) continue;
+      if (!gridlet_visible(f, it, cull)) continue;
+      float v; int cid;
+      if (oc_intersect_gridlet(&v, &cid, pos, &f->gridlets[it], f->scalars)) {
+        bestG = it; gv = v; gc = cid;
+      }
+    } else if (bestG < 0) {
+      const int e = -it - 1;
+      if (bestE >= 0 && e >= bestE) continue;
+      if (!elem_visible(f, e, cull)) continue;
+      float v;
+      if (oc_intersect_elem(&v, pos, &f->indices[(uint64_t)e * 8], f->vertices)) {
+        bestE = e; ev = v;
+      }
+    }
+  }
+  if (bestG >= 0) { s.primID = bestG; s.cellID = gc; s.value = gv; }
+  else if (bestE >= 0) { s.primID = bestE; s.cellID = -1; s.value = ev; }
+  return s;
+}
+
+void oc_sample_points(const oc_field *f, const v3 *pos, uint64_t n,
+                      exa_sample *out, int cull, int nthreads)
+{
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4096)
+#endif
+  for (int64_t i = 0; i < (int64_t)n; ++i) out[i] = oc_sample(f, pos[i], cull);
+}
+
+int oc_sample_all(const oc_field *f, v3 pos, int cull, int maxOut, int *kinds,
+                  int *ids, float *values)
+{
+  int n = 0;
+  for (uint64_t g = 0; g < f->numGridlets && n < maxOut; ++g) {
+    if (!gridlet_visible(f, (int)g, cull)) continue;
+    float v; int cid;
+    if (oc_intersect_gridlet(&v, &cid, pos, &f->gridlets[g], f->scalars)) {
+      kinds[n] = 0; ids[n] = (int)g; values[n] = v; n++;
+    }
+  }
+  for (uint64_t e = 0; e < f->numElems && n < maxOut; ++e) {
+    if (!elem_visible(f, (int)e, cull)) continue;
+    float v;
+    if (oc_intersect_elem(&v, pos, &f->indices[e * 8], f->vertices)) {
+      kinds[n] = 1; ids[n] = (int)e; values[n] = v; n++;
+    }
+  }
+  return n;
+}
+
+/* ================================================================== */
+/* majorants: Grid.cu:43-246, 687-719; sampler/ExaStitchSampler.cu     */
+/* ================================================================== */
+static inline void update_mc(exa_range1f *vr, v3i id, v3i dims, exa_range1f r)
+{
+  /* Grid.cu:43-50: atomicMin/atomicMax (order independent) */
+  exa_range1f *m = &vr[((size_t)id.z * dims.y + id.y) * dims.x + id.x];
+  if (r.lower < m->lower) m->lower = r.lower;
+  if (r.upper > m->upper) m->upper = r.upper;
+}
+
+void oc_build_majorants(const oc_field *f, v3i dims, exa_box3f wb, exa_range1f *vr)
+{
+  const size_t numMCs = (size_t)dims.x * dims.y * dims.z;
+  for (size_t i = 0; i < numMCs; ++i) { vr[i].lower = 1e30f; vr[i].upper = -1e30f; } /* Grid.cu:61-70 */
+  /* elements: buildGrid<8> (Grid.cu:73-117) */
+  for (uint64_t e = 0; e < f->numElems; ++e) {
+    const int32_t *I = &f->indices[e * 8];
+    exa_box3f cb;
+    cb.lower = mk3(INFINITY, INFINITY, INFINITY);
+    cb.upper = mk3(-INFINITY, -INFINITY, -INFINITY);
+    exa_range1f r = {1e30f, -1e30f};
+    int any = 0;
+    for (int i = 0; i < 8; ++i) {
+      if (I[i] < 0) break;
+      const v4 V = f->vertices[I[i]];
+      if (!isnan(V.w)) {
+        cb.lower = min3(cb.lower, xyz(V)); cb.upper = max3(cb.upper, xyz(V));
+        r.lower = fminf(r.lower, V.w); r.upper = fmaxf(r.upper, V.w);
+        any = 1;
+      }
+    }
+    if (!any) continue; /* empty box: the reference's loop adds nothing */
+    const v3i lo = oc_project_on_grid(cb.lower, dims, wb);
+    const v3i hi = oc_project_on_grid(cb.upper, dims, wb);
+    for (int z = lo.z; z <= hi.z; ++z)
+      for (int y = lo.y; y <= hi.y; ++y)
+        for (int x = lo.x; x <= hi.x; ++x) { v3i id = {x, y, z}; update_mc(vr, id, dims, r); }
+  }
+  /* gridlets: buildGrid (Grid.cu:134-246), one (gridlet, cell) at a time */
+  const v3 mcSize = div3(sub3(wb.upper, wb.lower), mk3((float)dims.x, (float)dims.y, (float)dims.z));
+  for (uint64_t g = 0; g < f->numGridlets; ++g) {
+    const exa_gridlet *gl = &f->gridlets[g];
+    const exa_box3f gb = gridlet_bounds(gl);
+    const v3i lo = oc_project_on_grid(gb.lower, dims, wb);
+    const v3i hi = oc_project_on_grid(gb.upper, dims, wb);
+    const int nx = gl->dims.x + 1, ny = gl->dims.y + 1;
+    const float cw = (float)(1 << gl->level);
+    const float *S = f->scalars + gl->begin;
+    for (int z = 0; z < gl->dims.z; ++z)
+      for (int y = 0; y < gl->dims.y; ++y)
+        for (int x = 0; x < gl->dims.x; ++x) {
+          exa_box3f cellB;
+          cellB.lower = add3(muls(mk3((float)(gl->lower.x + x), (float)(gl->lower.y + y), (float)(gl->lower.z + z)), cw),
+                             mk3(0.5f * cw, 0.5f * cw, 0.5f * cw));
+          cellB.upper = add3(muls(mk3((float)(gl->lower.x + x + 1), (float)(gl->lower.y + y + 1), (float)(gl->lower.z + z + 1)), cw),
+                             mk3(0.5f * cw, 0.5f * cw, 0.5f * cw));
+          float fv[8];
+          fv[0] = S[(z * ny + y) * nx + x];
+          fv[1] = S[(z * ny + y) * nx + x + 1];
+          fv[2] = S[(z * ny + y + 1) * nx + x];
+          fv[3] = S[(z * ny + y + 1) * nx + x + 1];
+          fv[4] = S[((z + 1) * ny + y) * nx + x];
+          fv[5] = S[((z + 1) * ny + y) * nx + x + 1];
+          fv[6] = S[((z + 1) * ny + y + 1) * nx + x];
+          fv[7] = S[((z + 1) * ny + y + 1) * nx + x + 1];
+          exa_range1f cr = {1e30f, -1e30f};
+          for (int k = 0; k < 8; ++k)
+            if (!isnan(fv[k])) { cr.lower = fminf(cr.lower, fv[k]); cr.upper = fmaxf(cr.upper, fv[k]); }
+          for (int mz = lo.z; mz <= hi.z; ++mz)
+            for (int my = lo.y; my <= hi.y; ++my)
+              for (int mx = lo.x; mx <= hi.x; ++mx) {
+                exa_box3f mb;
+                mb.lower = add3(wb.lower, mul3(mk3((float)mx, (float)my, (float)mz), mcSize));
+                mb.upper = add3(wb.lower, mul3(mk3((float)(mx + 1), (float)(my + 1), (float)(mz + 1)), mcSize));
+                /* box3f::overlaps, inclusive */
+                if (mb.lower.x <= cellB.upper.x && mb.lower.y <= cellB.upper.y && mb.lower.z <= cellB.upper.z &&
+                    cellB.lower.x <= mb.upper.x && cellB.lower.y <= mb.upper.y && cellB.lower.z <= mb.upper.z) {
+                  v3i id = {mx, my, mz};
+                  update_mc(vr, id, dims, cr);
+                }
+              }
+        }
+  }
+}
+
+/* Grid.cu:687-719 (== computeGridletMaxOpacitiesGPU,
+ * sampler/ExaStitchSampler.cu:144-176) */
+static float range_max_opacity(exa_range1f vr, const v4 *cm, int n, exa_range1f xf)
+{
+  if (vr.upper < vr.lower) return 0.f;
+  vr.lower -= xf.lower;
+  vr.lower /= xf.upper - xf.lower;
+  vr.upper -= xf.lower;
+  vr.upper /= xf.upper - xf.lower;
+  const int lo = iclamp((int)(vr.lower * (float)(n - 1)), 0, n - 1);
+  const int hi = iclamp((int)(vr.upper * (float)(n - 1)) + 1, 0, n - 1);
+  float m = 0.f;
+  for (int i = lo; i <= hi; ++i) m = fmaxf(m, cm[i].w);
+  return m;
+}
+
+void oc_compute_max_opacities(const exa_range1f *r, uint64_t n, const v4 *cm,
+                              int nc, exa_range1f xf, float *out)
+{
+  for (uint64_t i = 0; i < n; ++i) out[i] = range_max_opacity(r[i], cm, nc, xf);
+}
+
+/* sampler/ExaStitchSampler.cu:52-142: min/max over the non-NaN corners of
+ * every cell == over every non-NaN scalar of the gridlet */
+void oc_gridlet_value_ranges(const oc_field *f, exa_range1f *out)
+{
+  for (uint64_t g = 0; g < f->numGridlets; ++g) {
+    const exa_gridlet *gl = &f->gridlets[g];
+    exa_range1f r = {1e30f, -1e30f};
+    const uint64_t n = (uint64_t)(gl->dims.x + 1) * (gl->dims.y + 1) * (gl->dims.z + 1);
+    if (gl->dims.x > 0 && gl->dims.y > 0 && gl->dims.z > 0)
+      for (uint64_t i = 0; i < n; ++i) {
+        const float s = f->scalars[gl->begin + i];
+        if (!isnan(s)) { r.lower = fminf(r.lower, s); r.upper = fmaxf(r.upper, s); }
+      }
+    out[g] = r;
+  }
+}
+
+/* sampler/ExaStitchSampler.cu:178-227 (computeUmeshMaxOpacitiesGPU<8>) */
+void oc_elem_max_opacities(const oc_field *f, const v4 *cm, int nc,
+                           exa_range1f xf, float *out)
+{
+  for (uint64_t e = 0; e < f->numElems; ++e) {
+    exa_range1f r = {1e30f, -1e30f};
+    for (int i = 0; i < 8; ++i) {
+      const int idx = f->indices[e * 8 + i];
+      if (idx < 0) continue;
+      const float w = f->vertices[idx].w;
+      r.lower = fmin_t(r.lower, w);
+      r.upper = fmax_t(r.upper, w);
+    }
+    out[e] = range_max_opacity(r, cm, nc, xf);
+  }
+}
+
+/* ================================================================== */
+/* rendering (deviceCode.cu)                                           */
+/* ================================================================== */
+typedef struct { v3 org, dir; float tmin, tmax; } ray_t;
+
+enum { BOUNDARY = 0, SCATTERING = 1 };
+
+#define OC_TRACK_CAP (1 << 22)
+
+typedef struct {
+  const oc_field *f;
+  const exa_launch_params *lp;
+  uint32_t err;
+} rctx;
+
+/* deviceCode.cu:320-341, buffer variant */
+static v4 lookup_tf(const exa_launch_params *lp, float f)
+{
+  const exa_range1f d = lp->transferFunc.domain;
+  v4 zero = {0.f, 0.f, 0.f, 0.f};
+  if (d.lower >= d.upper) return zero;
+  f -= d.lower;
+  f /= (d.upper - d.lower);
+  if (lp->transferFunc.numValues == 0) return zero;
+  f = fmax_t(0.f, fmin_t(1.f, f));
+  const int i = imin_t(lp->transferFunc.numValues - 1, (int)(f * (float)lp->transferFunc.numValues));
+  return lp->transferFunc.values[i];
+}
+
+/* sampler/Sampler.h:105-122 */
+static int box_test(ray_t r, exa_box3f b, float *t0, float *t1)
+{
+  const v3 lo = div3(sub3(b.lower, r.org), r.dir);
+  const v3 hi = div3(sub3(b.upper, r.org), r.dir);
+  const v3 nr = min3(lo, hi), fr = max3(lo, hi);
+  *t0 = fmax_t(r.tmin, rmax3(nr));
+  *t1 = fmin_t(r.tmax, rmin3(fr));
+  return *t0 < *t1;
+}
+
+/* sampler/ExaStitchSampler.h:108-126 */
+static exa_sample test_sample(const oc_field *f, v3 pos, int primID)
+{
+  exa_sample s = {-1, -1, 0.f};
+  if (primID < 0) return s;
+  if (oc_intersect_gridlet(&s.value, &s.cellID, pos, &f->gridlets[primID], f->scalars))
+    s.primID = primID;
+  return s;
+}
+
+/* deviceCode.cu:625-651 (Default and Gridlets shade modes) */
+static v4 classify(const rctx *c, exa_sample s)
+{
+  v4 xf = lookup_tf(c->lp, s.value);
+  if (c->lp->shadeMode == EXA_SHADE_MODE_GRIDLETS) {
+    if (s.cellID == -1) { xf.x = 1.f; xf.y = 0.f; xf.z = 0.f; }
+    else {
+      const exa_gridlet *g = &c->f->gridlets[s.primID];
+      const int ix = s.cellID % g->dims.x;
+      const int iy = s.cellID / g->dims.x % g->dims.y;
+      const int iz = s.cellID / (g->dims.x * g->dims.y);
+      int col = (ix % 2 == iy % 2);
+      col = (iz % 2 == 0) ? col : !col;
+      if (col == 0) { xf.x = 1.f; xf.y = 1.f; xf.z = 1.f; }
+      else { xf.x = 0.f; xf.y = 0.f; xf.z = 0.7f; }
+    }
+  }
+  return xf;
+}
+
+/* dda3 (DDA.h:26-113) as a stepper: init = the prologue (:34-70), the
+ * current cell is (leaf, t0, t1), next() = the tie-advancing step
+ * (:352-375); next returns 0 when a stop index is reached. */
+typedef struct {
+  v3 tnext, dist;
+  v3i cell, step, stop, dims;
+  float t0, tmax;
+} oc_dda;
+
+static void dda_init(oc_dda *d, v3 org, v3 dir, float tmin, float tmax, v3i dims, exa_box3f mb)
+{
+  const v3 rcp = mk3(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+  const v3 lo = mul3(sub3(mb.lower, org), rcp);
+  const v3 hi = mul3(sub3(mb.upper, org), rcp);
+  const v3 tnear = min3(lo, hi), tfar = max3(lo, hi);
+  d->dims = dims;
+  d->cell = oc_project_on_grid(org, dims, mb);
+  d->dist = div3(sub3(tfar, tnear), mk3((float)dims.x, (float)dims.y, (float)dims.z));
+  d->step.x = dir.x > 0.f ? 1 : -1; d->step.y = dir.y > 0.f ? 1 : -1; d->step.z = dir.z > 0.f ? 1 : -1;
+  d->stop.x = dir.x > 0.f ? dims.x : -1; d->stop.y = dir.y > 0.f ? dims.y : -1; d->stop.z = dir.z > 0.f ? dims.z : -1;
+  d->tnext.x = dir.x > 0.f ? tnear.x + (float)(d->cell.x + 1) * d->dist.x : tnear.x + (float)(dims.x - d->cell.x) * d->dist.x;
+  d->tnext.y = dir.y > 0.f ? tnear.y + (float)(d->cell.y + 1) * d->dist.y : tnear.y + (float)(dims.y - d->cell.y) * d->dist.y;
+  d->tnext.z = dir.z > 0.f ? tnear.z + (float)(d->cell.z + 1) * d->dist.z : tnear.z + (float)(dims.z - d->cell.z) * d->dist.z;
+  d->t0 = fmax_t(tmin, 0.f);
+  d->tmax = tmax;
+}
+static inline float dda_t1(const oc_dda *d) { return fmin_t(rmin3(d->tnext), d->tmax); }
+static inline int dda_leaf(const oc_dda *d) { return (d->cell.z * d->dims.y + d->cell.y) * d->dims.x + d->cell.x; }
+static int dda_next(oc_dda *d)
+{
+  const float t1 = dda_t1(d);
+  const float tc = rmin3(d->tnext);
+  if (d->tnext.x == tc) { d->tnext.x += d->dist.x; d->cell.x += d->step.x; if (d->cell.x == d->stop.x) return 0; }
+  if (d->tnext.y == tc) { d->tnext.y += d->dist.y; d->cell.y += d->step.y; if (d->cell.y == d->stop.y) return 0; }
+  if (d->tnext.z == tc) { d->tnext.z += d->dist.z; d->cell.z += d->step.z; if (d->cell.z == d->stop.z) return 0; }
+  d->t0 = t1;
+  return 1;
+}
+
+int oc_dda3(exa_vec3f org, exa_vec3f dir, float tmin, float tmax, exa_vec3i dims,
+            exa_box3f box, int maxCells, long long *ids, float *t0s, float *t1s)
+{
+  oc_dda d;
+  int n = 0;
+  dda_init(&d, org, dir, tmin, tmax, dims, box);
+  while (n < maxCells) {
+    ids[n] = dda_leaf(&d); t0s[n] = d.t0; t1s[n] = dda_t1(&d);
+    n++;
+    if (n >= maxCells || !dda_next(&d)) break;
+  }
+  return n;
+}
+
+/* sampleInteraction (deviceCode.cu:699-854) with dda3 (DDA.h:26-113)
+ * inlined; shadow = ratio tracking (:785-839), else Woodcock (:726-783).
+ * Returns the collision type; *pos in world space. */
+static int sample_interaction(rctx *c, ray_t ray, int shadow, v3 *posOut,
+                              float *TrOut, v4 *xfOut, oc_rng *rng, float *tHit)
+{
+  const exa_launch_params *lp = c->lp;
+  const oc_field *f = c->f;
+  ray.org = xfm_point(&lp->voxelSpaceTransform, ray.org);
+  ray.dir = xfm_vector(&lp->voxelSpaceTransform, ray.dir);
+  const float dt_scale = len3(ray.dir);
+  ray.dir = norm3(ray.dir);
+  ray.tmin = ray.tmin * dt_scale;
+  ray.tmax = ray.tmax * dt_scale;
+
+  int type = BOUNDARY;
+  float Tr = 1.f;
+  v3 pos = mk3(0.f, 0.f, 0.f);
+  v4 xf = *xfOut;
+  const float scale = lp->transferFunc.opacityScale;
+  const int cull = lp->ext.cullTransparentPrims;
+
+  oc_dda dda;
+  dda_init(&dda, ray.org, ray.dir, ray.tmin, ray.tmax, lp->majorantGrid.dims, lp->majorantGrid.bounds);
+  const v3i dims = lp->majorantGrid.dims;
+  const int cellCap = dims.x + dims.y + dims.z + 3;
+  int ncells = 0;
+  int done = 0;
+  while (!done) {
+    if (++ncells > cellCap) { c->err |= EXA_DEVERR_DDA_CAP; break; }
+    const float t1 = dda_t1(&dda);
+    const int leafID = dda_leaf(&dda);
+    if (lp->ext.stepCounters) ((unsigned long long *)lp->ext.stepCounters)[3]++;
+    /* ---- woodcockFunc / ratioTrackingFunc body ---- */
+    {
+      const float majorant = lp->maxOpacities[leafID];
+      float t = dda.t0;
+      int primID = -1;
+      int steps = 0;
+      while (1) {
+        if (majorant <= 0.f) break;
+        if (++steps > OC_TRACK_CAP) { c->err |= EXA_DEVERR_TRACK_CAP; done = 1; break; }
+        t -= oc_log(1.f - oc_rng_next(rng)) / (majorant * scale);
+        if (t >= t1) break;
+        pos = add3(ray.org, muls(ray.dir, t));
+        exa_sample s = test_sample(f, pos, primID);
+        if (s.primID < 0) s = oc_sample(f, pos, cull);
+        if (lp->ext.stepCounters) {
+          unsigned long long *sc = (unsigned long long *)lp->ext.stepCounters;
+          sc[0]++;
+          if (s.primID >= 0) sc[s.cellID != -1 ? 1 : 2]++;
+        }
+        if (s.primID < 0) continue;
+        if (s.cellID != -1) primID = s.primID;
+        xf = classify(c, s);
+        const float sigmaT = xf.w;
+        if (!shadow) {
+          const float u = oc_rng_next(rng);
+          if (sigmaT * scale >= u * majorant) {
+            Tr = 0.f; type = SCATTERING; done = 1;
+            if (tHit) *tHit = t;
+            break;
+          }
+        } else {
+          Tr *= 1.f - (sigmaT * scale) / majorant;
+          if (Tr <= 0.f) { type = SCATTERING; done = 1; break; }
+        }
+      }
+    }
+    if (done) break;
+    if (!dda_next(&dda)) break;
+  }
+  *posOut = xfm_point(&lp->ext.voxelSpaceTransformInv, pos);
+  *TrOut = Tr;
+  *xfOut = xf;
+  return type;
+}
+
+/* sampleLight (deviceCode.cu:856-926); directional lights are an
+ * extension: lights[i].pos is the direction towards the light, no
+ * distance falloff */
+static v3 sample_light(rctx *c, v3 pos, oc_rng *rng, int numLights, float *trOut)
+{
+  const exa_launch_params *lp = c->lp;
+  int which = (int)(oc_rng_next(rng) * (float)numLights);
+  if (which == numLights) which = 0;
+  ray_t ray;
+  float Tr, t00 = 1e30f, t11 = -1e30f;
+  v3 np; v4 xf = {0.f, 0.f, 0.f, 0.f};
+  ray.org = pos;
+  ray.tmin = 0.f;
+  if (lp->ext.lightType[which] == EXA_LIGHT_DIRECTIONAL) {
+    ray.dir = norm3(lp->lights[which].pos);
+    ray.tmax = 1e30f;
+    box_test(ray, lp->worldSpaceBounds, &t00, &t11);
+    ray.tmax = t11;
+    sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
+    if (trOut) *trOut = Tr;
+    const float I = Tr * lp->lights[which].intensity;
+    return mk3(I, I, I);
+  }
+  v3 lightDir = sub3(lp->lights[which].pos, pos);
+  const float ld = len3(xfm_vector(&lp->lightSpaceTransform, lightDir));
+  const float ldWorld = len3(lightDir);
+  lightDir = norm3(lightDir);
+  ray.dir = lightDir;
+  ray.tmax = ldWorld;
+  box_test(ray, lp->worldSpaceBounds, &t00, &t11);
+  ray.tmax = t11;
+  sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
+  if (trOut) *trOut = Tr;
+  const float I = Tr / (ld * ld) * lp->lights[which].intensity;
+  return mk3(I, I, I);
+}
+
+/* make_orthonormal_basis (deviceCode.cu:144-149) */
+static void onb(v3 *u, v3 *v, v3 w)
+{
+  *v = fabsf(w.x) > fabsf(w.y) ? norm3(mk3(-w.z, 0.f, w.x)) : norm3(mk3(0.f, w.z, -w.y));
+  *u = cross3(*v, w);
+}
+
+/* henyeyGreensteinSample (deviceCode.cu:965-985); direction only */
+static v3 hg_sample(v3 wo, float g, oc_rng *rng)
+{
+  const int gnz = fabsf(g) >= 1.19209290e-07f;
+  const float u1 = oc_rng_next(rng);
+  const float u2 = oc_rng_next(rng);
+  const float a = gnz ? (1.f - g * g) / (1.f - g + 2.f * g * u1) : 0.f;
+  const float cost = gnz ? (1.f + g * g - a * a) / (2.f * g) : 1.f - 2.f * u1;
+  const float sint = sqrtf(fmaxf(0.f, 1.f - cost * cost));
+  float sphi, cphi;
+  oc_sincos_turns(u2, &sphi, &cphi);
+  v3 u, v;
+  onb(&u, &v, wo);
+  const v3 mw = mk3(-wo.x, -wo.y, -wo.z);
+  return add3(add3(muls(u, sint * cphi), muls(v, sint * sphi)), muls(mw, cost));
+}
+
+static int num_lights(const exa_launch_params *lp)
+{
+  int n = 0;
+  for (int i = 0; i < EXA_LIGHTS_MAX; ++i) if (lp->lights[i].on) n++;
+  return n;
+}
+
+/* pathTracingIntegrate (deviceCode.cu:991-1120) */
+static v4 path_trace(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
+                     float *tHit, float *trOut)
+{
+  const exa_launch_params *lp = c->lp;
+  v3 throughput = mk3(1.f, 1.f, 1.f), Ld = mk3(0.f, 0.f, 0.f);
+  unsigned bounce = 0;
+  float t0 = 1e30f, t1 = -1e30f;
+  const unsigned maxB = (unsigned)lp->ext.maxBounces;
+  if (box_test(ray, lp->worldSpaceBounds, &t0, &t1)) {
+    ray.org = add3(ray.org, muls(ray.dir, t0));
+    t1 -= t0;
+    while (1) {
+      float Tr; v3 pos; v4 xf = {0.f, 0.f, 0.f, 0.f};
+      ray.tmax = t1;
+      const int ct = sample_interaction(c, ray, 0, &pos, &Tr, &xf, rng, bounce == 0 ? tHit : NULL);
+      if (ct == BOUNDARY) break;
+      if (bounce++ >= maxB) { throughput = mk3(0.f, 0.f, 0.f); break; }
+      const v3 albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
+      throughput = mul3(throughput, albedo);
+      const float P = rmax3(throughput);
+      if (P < 0.2f) {
+        if (oc_rng_next(rng) > P) { throughput = mk3(0.f, 0.f, 0.f); break; }
+        throughput = div3(throughput, mk3(P, P, P));
+      }
+      throughput = add3(throughput, mk3(0.f, 0.f, 0.f)); /* += Le (always 0) */
+      if (numLights > 0) Ld = add3(Ld, mul3(throughput, sample_light(c, pos, rng, numLights, bounce == 1 ? trOut : NULL)));
+      const v3 wo = mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z);
+      const v3 sd = hg_sample(wo, lp->ext.hgG, rng);
+      ray.org = pos;
+      ray.dir = sd;
+      box_test(ray, lp->worldSpaceBounds, &t0, &t1);
+    }
+  }
+  if (numLights == 0) Ld = mk3(1.f, 1.f, 1.f);
+  const v3 L = mul3(Ld, throughput);
+  v4 color = {L.x, L.y, L.z, 1.f};
+  return bounce ? color : bg;
+}
+
+/* directLightingIntegrate (deviceCode.cu:1126-1207) */
+static v4 direct_light(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
+                       float *tHit, float *trOut)
+{
+  const exa_launch_params *lp = c->lp;
+  v3 throughput = mk3(1.f, 1.f, 1.f);
+  float t0 = 1e30f, t1 = -1e30f;
+  if (!box_test(ray, lp->worldSpaceBounds, &t0, &t1)) return bg;
+  ray.org = add3(ray.org, muls(ray.dir, t0));
+  t1 -= t0;
+  ray.tmax = t1;
+  float Tr; v3 pos; v4 xf = {0.f, 0.f, 0.f, 0.f};
+  const int ct = sample_interaction(c, ray, 0, &pos, &Tr, &xf, rng, tHit);
+  if (ct == BOUNDARY) return bg;
+  const v3 albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
+  if (numLights > 0) throughput = mul3(throughput, mul3(albedo, sample_light(c, pos, rng, numLights, trOut)));
+  else throughput = mul3(throughput, albedo);
+  v4 color = {throughput.x, throughput.y, throughput.z, 1.f};
+  return color;
+}
+
+static inline uint32_t make_8bit(float f)
+{
+  return (uint32_t)imin_t(255, imax_t(0, (int)(f * 256.f)));
+}
+
+/* renderFrame_Impl (deviceCode.cu:1268-1345) for one pixel */
+static void render_pixel(rctx *c, int width, int height, int px, int py)
+{
+  const exa_launch_params *lp = c->lp;
+  const int pixelID = px + width * py;
+  /* backGroundColor, deviceCode.cu:43-50 */
+  const float tb = (float)py / (float)height;
+  const v4 bg = {(1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f};
+  const int numLights = num_lights(lp);
+  oc_rng rng;
+  oc_rng_init(&rng, (uint32_t)pixelID, (uint32_t)lp->accumID, lp->ext.frameID);
+  v4 acc = {0.f, 0.f, 0.f, 0.f};
+  float tHit = -1.f, trv = -1.f;
+  for (int s = 0; s < lp->render.spp; ++s) {
+    const float rx = oc_rng_next(&rng);
+    const float ry = oc_rng_next(&rng);
+    const float sx = (float)px + rx, sy = (float)py + ry;
+    /* generateRay, deviceCode.cu:88-101 */
+    v3 dir = add3(add3(lp->camera.dir_00, smul(sx, lp->camera.dir_du)), smul(sy, lp->camera.dir_dv));
+    dir = norm3(dir);
+    if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
+    if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
+    if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+    ray_t ray; ray.org = lp->camera.org; ray.dir = dir; ray.tmin = 0.f; ray.tmax = 1e10f;
+    v4 col;
+    if (lp->integrator == EXA_PATH_TRACING_INTEGRATOR)
+      col = path_trace(c, ray, &rng, bg, numLights, s == 0 ? &tHit : NULL, s == 0 ? &trv : NULL);
+    else
+      col = direct_light(c, ray, &rng, bg, numLights, s == 0 ? &tHit : NULL, s == 0 ? &trv : NULL);
+    acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
+  }
+  if (lp->accumID > 0 && lp->accumBuffer) {
+    const v4 o = lp->accumBuffer[pixelID];
+    acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+  }
+  if (lp->accumBuffer) lp->accumBuffer[pixelID] = acc;
+  const float inv = 1.f / (float)(lp->accumID + 1);
+  acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+  const float is = 1.f / (float)lp->render.spp;
+  const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) |
+                        (make_8bit(acc.z * is) << 16) | (make_8bit(acc.w * is) << 24);
+  if (lp->fbPointer) lp->fbPointer[pixelID] = rgba;
+  if (lp->ext.traceT) lp->ext.traceT[pixelID] = tHit;
+  if (lp->ext.traceTr) lp->ext.traceTr[pixelID] = trv;
+}
+
+uint32_t oc_render(const oc_field *f, const exa_launch_params *lp, int width,
+                   int height, int64_t pb, int64_t pe, int nthreads)
+{
+  uint32_t err = 0;
+  if (pe > (int64_t)width * height) pe = (int64_t)width * height;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : err)
+#endif
+  for (int64_t p = pb; p < pe; ++p) {
+    rctx c = {f, lp, 0};
+    render_pixel(&c, width, height, (int)(p % width), (int)(p / width));
+    err |= c.err;
+  }
+  return err;
+}
+
+/* ================================================================== */
+/* binary64 converged reference: direct lighting with ratio tracking    */
+/* ================================================================== */
+typedef struct { double x, y, z; } d3;
+static inline d3 dk(double x, double y, double z) { d3 r = {x, y, z}; return r; }
+
+static double d_sample_value(const oc_field *f, d3 p, int cull, int *hit)
+{
+  /* the field itself is fp32 data: locate in float, interpolate there */
+  v3 pf = mk3((float)p.x, (float)p.y, (float)p.z);
+  exa_sample s = oc_sample(f, pf, cull);
+  *hit = s.primID >= 0;
+  return s.value;
+}
+
+static double d_lookup_alpha(const exa_launch_params *lp, double v, double rgb[3])
+{
+  const exa_range1f d = lp->transferFunc.domain;
+  if (d.lower >= d.upper || lp->transferFunc.numValues == 0) { rgb[0] = rgb[1] = rgb[2] = 0; return 0; }
+  double fv = (v - d.lower) / ((double)d.upper - d.lower);
+  if (fv < 0) fv = 0;
+  if (fv > 1) fv = 1;
+  int i = (int)(fv * lp->transferFunc.numValues);
+  if (i > lp->transferFunc.numValues - 1) i = lp->transferFunc.numValues - 1;
+  const v4 c = lp->transferFunc.values[i];
+  rgb[0] = c.x; rgb[1] = c.y; rgb[2] = c.z;
+  return c.w;
+}
+
+/* expected transmittance by ratio tracking in binary64 over the same
+ * majorant grid (walked densely in fixed steps of the majorant cell) */
+static double d_transmittance(const oc_field *f, const exa_launch_params *lp,
+                              d3 o, d3 dir, double tmax, uint64_t *rs)
+{
+  /* uniform majorant = global max opacity * scale, classic ratio tracking */
+  const int cull = lp->ext.cullTransparentPrims;
+  const double scale = lp->transferFunc.opacityScale;
+  double maj = 0;
+  const int64_t nmc = (int64_t)lp->majorantGrid.dims.x * lp->majorantGrid.dims.y * lp->majorantGrid.dims.z;
+  for (int64_t i = 0; i < nmc; ++i) if (lp->maxOpacities[i] > maj) maj = lp->maxOpacities[i];
+  maj *= scale;
+  if (maj <= 0) return 1.0;
+  double Tr = 1.0, t = 0.0;
+  for (int k = 0; k < OC_TRACK_CAP; ++k) {
+    *rs = oc_mix64(*rs + 0x9e3779b97f4a7c15ull);
+    const double u = ((*rs >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    t -= log(u) / maj;
+    if (t >= tmax) break;
+    int hit;
+    const double v = d_sample_value(f, dk(o.x + dir.x * t, o.y + dir.y * t, o.z + dir.z * t), cull, &hit);
+    if (!hit) continue;
+    double rgb[3];
+    const double a = d_lookup_alpha(lp, v, rgb) * scale;
+    Tr *= 1.0 - a / maj;
+  }
+  return Tr;
+}
+
+void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
+                   int height, int64_t pb, int64_t pe, double *out, int nthreads)
+{
+  if (pe > (int64_t)width * height) pe = (int64_t)width * height;
+  const int numLights = num_lights(lp);
+  const int cull = lp->ext.cullTransparentPrims;
+  const double scale = lp->transferFunc.opacityScale;
+  double maj = 0;
+  const int64_t nmc = (int64_t)lp->majorantGrid.dims.x * lp->majorantGrid.dims.y * lp->majorantGrid.dims.z;
+  for (int64_t i = 0; i < nmc; ++i) if (lp->maxOpacities[i] > maj) maj = lp->maxOpacities[i];
+  maj *= scale;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (int64_t p = pb; p < pe; ++p) {
+    const int px = (int)(p % width), py = (int)(p / width);
+    uint64_t rs = oc_mix64(((uint64_t)p << 20) ^ 0x1234567ull ^ ((uint64_t)lp->accumID << 50));
+    const double tb = (double)py / height;
+    const double bg[3] = {(1 - tb) + tb * 0.5, (1 - tb) + tb * 0.7, 1.0};
+    double acc[3] = {0, 0, 0};
+    for (int s = 0; s < lp->render.spp; ++s) {
+      rs = oc_mix64(rs + 1);
+      const double rx = ((rs >> 11) + 0.5) / 9007199254740992.0;
+      rs = oc_mix64(rs + 1);
+      const double ry = ((rs >> 11) + 0.5) / 9007199254740992.0;
+      d3 dir = dk(lp->camera.dir_00.x + (px + rx) * lp->camera.dir_du.x + (py + ry) * lp->camera.dir_dv.x,
+                  lp->camera.dir_00.y + (px + rx) * lp->camera.dir_du.y + (py + ry) * lp->camera.dir_dv.y,
+                  lp->camera.dir_00.z + (px + rx) * lp->camera.dir_du.z + (py + ry) * lp->camera.dir_dv.z);
+      const double dl = sqrt(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+      dir = dk(dir.x / dl, dir.y / dl, dir.z / dl);
+      const d3 o = dk(lp->camera.org.x, lp->camera.org.y, lp->camera.org.z);
+      /* box test against world bounds (identity voxel transform assumed
+       * by the caller for this reference) */
+      double t0 = 0, t1 = 1e10;
+      const double bl[3] = {lp->worldSpaceBounds.lower.x, lp->worldSpaceBounds.lower.y, lp->worldSpaceBounds.lower.z};
+      const double bu[3] = {lp->worldSpaceBounds.upper.x, lp->worldSpaceBounds.upper.y, lp->worldSpaceBounds.upper.z};
+      const double oo[3] = {o.x, o.y, o.z}, dd[3] = {dir.x, dir.y, dir.z};
+      for (int a = 0; a < 3; ++a) {
+        double ta = (bl[a] - oo[a]) / dd[a], tb2 = (bu[a] - oo[a]) / dd[a];
+        if (ta > tb2) { double tt = ta; ta = tb2; tb2 = tt; }
+        if (ta > t0) t0 = ta;
+        if (tb2 < t1) t1 = tb2;
+      }
+      if (!(t0 < t1) || maj <= 0) { acc[0] += bg[0]; acc[1] += bg[1]; acc[2] += bg[2]; continue; }
+      /* delta tracking for the free-flight distance under the global
+       * majorant, unbiased; the shadow ray uses ratio tracking */
+      double t = t0;
+      int scattered = 0;
+      double rgb[3] = {0, 0, 0};
+      for (int k = 0; k < OC_TRACK_CAP; ++k) {
+        rs = oc_mix64(rs + 1);
+        const double u = ((rs >> 11) + 0.5) / 9007199254740992.0;
+        t -= log(u) / maj;
+        if (t >= t1) break;
+        int hit;
+        const d3 pp = dk(o.x + dir.x * t, o.y + dir.y * t, o.z + dir.z * t);
+        const double v = d_sample_value(f, pp, cull, &hit);
+        if (!hit) continue;
+        const double a = d_lookup_alpha(lp, v, rgb) * scale;
+        rs = oc_mix64(rs + 1);
+        const double u2 = ((rs >> 11) + 0.5) / 9007199254740992.0;
+        if (a >= u2 * maj) { scattered = 1; break; }
+      }
+      if (!scattered) { acc[0] += bg[0]; acc[1] += bg[1]; acc[2] += bg[2]; continue; }
+      const d3 pos = dk(o.x + dir.x * t, o.y + dir.y * t, o.z + dir.z * t);
+      double alb[3];
+      if (lp->ext.albedo < 0.f) { alb[0] = rgb[0]; alb[1] = rgb[1]; alb[2] = rgb[2]; }
+      else { alb[0] = alb[1] = alb[2] = lp->ext.albedo; }
+      double L = 1.0;
+      if (numLights > 0) {
+        /* expectation over the uniformly chosen light */
+        L = 0.0;
+        for (int li = 0; li < numLights; ++li) {
+          d3 ldir; double dist, fall = 1.0;
+          if (lp->ext.lightType[li] == EXA_LIGHT_DIRECTIONAL) {
+            ldir = dk(lp->lights[li].pos.x, lp->lights[li].pos.y, lp->lights[li].pos.z);
+            const double n = sqrt(ldir.x * ldir.x + ldir.y * ldir.y + ldir.z * ldir.z);
+            ldir = dk(ldir.x / n, ldir.y / n, ldir.z / n);
+            dist = 1e30;
+          } else {
+            ldir = dk(lp->lights[li].pos.x - pos.x, lp->lights[li].pos.y - pos.y, lp->lights[li].pos.z - pos.z);
+            dist = sqrt(ldir.x * ldir.x + ldir.y * ldir.y + ldir.z * ldir.z);
+            ldir = dk(ldir.x / dist, ldir.y / dist, ldir.z / dist);
+            fall = 1.0 / (dist * dist);
+          }
+          double te = 1e30;
+          const double po[3] = {pos.x, pos.y, pos.z}, ld3[3] = {ldir.x, ldir.y, ldir.z};
+          for (int a = 0; a < 3; ++a) {
+            const double ta = (bl[a] - po[a]) / ld3[a], tb2 = (bu[a] - po[a]) / ld3[a];
+            const double tf = ta > tb2 ? ta : tb2;
+            if (tf < te) te = tf;
+          }
+          if (dist < te) te = dist;
+          L += d_transmittance(f, lp, pos, ldir, te, &rs) * fall * lp->lights[li].intensity;
+        }
+        L /= numLights;
+      }
+      acc[0] += alb[0] * L; acc[1] += alb[1] * L; acc[2] += alb[2] * L;
+    }
+    out[(p - pb) * 3 + 0] = acc[0] / lp->render.spp;
+    out[(p - pb) * 3 + 1] = acc[1] / lp->render.spp;
+    out[(p - pb) * 3 + 2] = acc[2] / lp->render.spp;
+  }
+}

@@ -1,0 +1,101 @@
+/*
+ * oracle.h -- CPU restatement of the owlExaStitcher ExaStitch rendering path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path
+ * (tests/, the smoke check and the timed CPU baseline in bench.py use it); it
+ * is never linked into, loaded by or called from the product library.
+ *
+ * Arithmetic discipline: every function is plain IEEE-754 binary32 with no
+ * contraction (built with -ffp-contract=off), in the operation order of the
+ * reference source it cites.  The CUDA kernels follow the same order and are
+ * built with --fmad=false, so results are bit-comparable.  log, sin and cos on
+ * the path are the project's own series implementations (oc_log,
+ * oc_sincos_turns) because the reference calls the CUDA math library there.
+ */
+#ifndef EXA_ORACLE_H
+#define EXA_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "../include/exastitch.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- project-defined math and RNG (shared definitions with the GPU) ---- */
+uint64_t oc_mix64(uint64_t z);
+float    oc_log(float x);
+void     oc_sincos_turns(float u, float *s, float *c);
+
+typedef struct { uint64_t key; uint64_t counter; } oc_rng;
+void  oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID);
+float oc_rng_next(oc_rng *r);
+
+/* ---- cell / element interpolation (Gridlet.h, Plane.h, UElems.h) ---- */
+int oc_intersect_gridlet(float *value, int *cellID, exa_vec3f pos,
+                         const exa_gridlet *g, const float *scalars);
+int oc_intersect_tet(float *value, exa_vec3f P, exa_vec4f a, exa_vec4f b,
+                     exa_vec4f c, exa_vec4f d);
+int oc_intersect_pyr(float *value, exa_vec3f P, const exa_vec4f *v5);
+int oc_intersect_wedge(float *value, exa_vec3f P, const exa_vec4f *v6);
+int oc_intersect_hex(float *value, exa_vec3f P, const exa_vec4f *v8);
+/* element test dispatching on the vertex count of an 8-wide index row */
+int oc_intersect_elem(float *value, exa_vec3f P, const int32_t *idx8,
+                      const exa_vec4f *vertices);
+exa_vec3i oc_project_on_grid(exa_vec3f V, exa_vec3i dims, exa_box3f bounds);
+/* dda3 (DDA.h:26-113) recording (cellID, t0, t1) for each visited cell */
+int oc_dda3(exa_vec3f org, exa_vec3f dir, float tmin, float tmax, exa_vec3i dims,
+            exa_box3f box, int maxCells, long long *ids, float *t0s, float *t1s);
+
+/* ---- field container with a uniform-grid point-location accel ---- */
+typedef struct oc_field oc_field;
+oc_field *oc_field_create(const exa_vec4f *vertices, uint64_t numVertices,
+                          const int32_t *indices, uint64_t numElems,
+                          const exa_gridlet *gridlets, uint64_t numGridlets,
+                          const float *scalars, uint64_t numScalars);
+void oc_field_destroy(oc_field *f);
+/* per-primitive max opacities used for culling (NULL: no culling data) */
+void oc_field_set_prim_opacities(oc_field *f, const float *gridletMaxOps,
+                                 const float *elemMaxOps);
+/* cellBounds / valueRange as ExaStitchModel::load computes them */
+void oc_field_bounds(const oc_field *f, exa_box3f *cellBounds,
+                     exa_range1f *valueRange);
+/* canonical point query: lowest-index containing gridlet, else
+ * lowest-index containing element, else {-1,-1,0} */
+exa_sample oc_sample(const oc_field *f, exa_vec3f pos, int cull);
+void oc_sample_points(const oc_field *f, const exa_vec3f *pos, uint64_t n,
+                      exa_sample *out, int cull, int nthreads);
+/* every containing primitive: kinds[i] 0 = gridlet, 1 = element */
+int oc_sample_all(const oc_field *f, exa_vec3f pos, int cull, int maxOut,
+                  int *kinds, int *ids, float *values);
+
+/* ---- majorants (Grid.cu, sampler/ExaStitchSampler.cu) ---- */
+void oc_build_majorants(const oc_field *f, exa_vec3i dims, exa_box3f bounds,
+                        exa_range1f *valueRanges);
+void oc_compute_max_opacities(const exa_range1f *ranges, uint64_t n,
+                              const exa_vec4f *colorMap, int numColors,
+                              exa_range1f xfRange, float *out);
+void oc_gridlet_value_ranges(const oc_field *f, exa_range1f *out);
+void oc_elem_max_opacities(const oc_field *f, const exa_vec4f *colorMap,
+                           int numColors, exa_range1f xfRange, float *out);
+
+/* ---- rendering (deviceCode.cu) ----
+ * lp holds HOST pointers: transferFunc.values, maxOpacities, accumBuffer,
+ * fbPointer.  Renders pixels [pixelBegin, pixelEnd) of a width x height
+ * frame.  Returns the OR of EXA_DEVERR_* bits raised. */
+uint32_t oc_render(const oc_field *f, const exa_launch_params *lp,
+                   int width, int height, int64_t pixelBegin, int64_t pixelEnd,
+                   int nthreads);
+/* Same frame computed in binary64 arithmetic with ratio-tracking
+ * transmittance for the direct-lighting integrator: the converged
+ * reference image for RMSE checks.  Writes linear RGB (3 doubles/pixel,
+ * averaged over spp) into outRGB for pixels [pixelBegin, pixelEnd). */
+void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
+                   int height, int64_t pixelBegin, int64_t pixelEnd,
+                   double *outRGB, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,294 @@
+"""ctypes bindings for the CPU oracle (oracle/liboracle.so) and, where it was
+built, the reference-header library (oracle/_ref/libexaref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
+baseline leg of bench.py.  The product package never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libexaref.so")
+REF_TREE = "/root/reference"
+
+
+def build(ref=True):
+    """Compile the oracle (and the reference-header library when the
+    reference tree exists)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    if ref and os.path.isdir(REF_TREE):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + REF_TREE])
+
+
+# ---------------------------------------------------------------- types
+class Vec3f(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class Vec3i(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
+
+
+class Box3f(C.Structure):
+    _fields_ = [("lower", Vec3f), ("upper", Vec3f)]
+
+
+class Range1f(C.Structure):
+    _fields_ = [("lower", C.c_float), ("upper", C.c_float)]
+
+
+class Sample(C.Structure):
+    _fields_ = [("primID", C.c_int32), ("cellID", C.c_int32), ("value", C.c_float)]
+
+
+GRIDLET_DTYPE = np.dtype([("lower", "<i4", 3), ("level", "<i4"), ("dims", "<i4", 3), ("begin", "<u4")])
+SAMPLE_DTYPE = np.dtype([("primID", "<i4"), ("cellID", "<i4"), ("value", "<f4")])
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def v3(x):
+    return Vec3f(float(x[0]), float(x[1]), float(x[2]))
+
+
+def box(lo, hi):
+    return Box3f(v3(lo), v3(hi))
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(ref=False)
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.oc_log.restype = C.c_float
+        L.oc_log.argtypes = [C.c_float]
+        L.oc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.oc_mix64.restype = C.c_uint64
+        L.oc_mix64.argtypes = [C.c_uint64]
+        L.oc_intersect_gridlet.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_int), Vec3f, vp, vp]
+        L.oc_intersect_pyr.argtypes = [C.POINTER(C.c_float), Vec3f, vp]
+        L.oc_intersect_wedge.argtypes = [C.POINTER(C.c_float), Vec3f, vp]
+        L.oc_intersect_hex.argtypes = [C.POINTER(C.c_float), Vec3f, vp]
+        L.oc_intersect_elem.argtypes = [C.POINTER(C.c_float), Vec3f, vp, vp]
+        L.oc_project_on_grid.restype = Vec3i
+        L.oc_project_on_grid.argtypes = [Vec3f, Vec3i, Box3f]
+        L.oc_dda3.restype = C.c_int
+        L.oc_dda3.argtypes = [Vec3f, Vec3f, C.c_float, C.c_float, Vec3i, Box3f, C.c_int, vp, vp, vp]
+        L.oc_field_create.restype = vp
+        L.oc_field_create.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64]
+        L.oc_field_destroy.argtypes = [vp]
+        L.oc_field_set_prim_opacities.argtypes = [vp, vp, vp]
+        L.oc_field_bounds.argtypes = [vp, C.POINTER(Box3f), C.POINTER(Range1f)]
+        L.oc_sample.restype = Sample
+        L.oc_sample.argtypes = [vp, Vec3f, C.c_int]
+        L.oc_sample_points.argtypes = [vp, vp, C.c_uint64, vp, C.c_int, C.c_int]
+        L.oc_sample_all.restype = C.c_int
+        L.oc_sample_all.argtypes = [vp, Vec3f, C.c_int, C.c_int, vp, vp, vp]
+        L.oc_build_majorants.argtypes = [vp, Vec3i, Box3f, vp]
+        L.oc_compute_max_opacities.argtypes = [vp, C.c_uint64, vp, C.c_int, Range1f, vp]
+        L.oc_gridlet_value_ranges.argtypes = [vp, vp]
+        L.oc_elem_max_opacities.argtypes = [vp, vp, C.c_int, Range1f, vp]
+        L.oc_render.restype = C.c_uint32
+        L.oc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int]
+        L.oc_render_f64.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, vp, C.c_int]
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The reference-header library, or None where it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = C.CDLL(REF_PATH)
+        vp = C.c_void_p
+        R.ref_intersect_gridlet.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_int), vp, vp, vp]
+        for n in ("tet", "pyr", "wedge", "hex"):
+            getattr(R, "ref_intersect_" + n).argtypes = [C.POINTER(C.c_float), vp, vp]
+        R.ref_project_on_grid.argtypes = [vp, vp, vp, vp]
+        R.ref_gridlet_bounds.argtypes = [vp, vp]
+        R.ref_dda3.restype = C.c_int
+        R.ref_dda3.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, C.c_int, vp, vp, vp]
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------- helpers
+def log(x):
+    return lib().oc_log(float(x))
+
+
+def sincos_turns(u):
+    s, c = C.c_float(), C.c_float()
+    lib().oc_sincos_turns(float(u), C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+class Field:
+    """Oracle view of an ExaStitch field (arrays are kept alive here)."""
+
+    def __init__(self, vertices, indices, gridlets, scalars):
+        self.vertices = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 4)
+        self.indices = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 8)
+        self.gridlets = np.ascontiguousarray(gridlets, dtype=GRIDLET_DTYPE)
+        self.scalars = np.ascontiguousarray(scalars, dtype=np.float32)
+        self._gops = None
+        self._eops = None
+        self.h = lib().oc_field_create(
+            _ptr(self.vertices), len(self.vertices), _ptr(self.indices), len(self.indices),
+            _ptr(self.gridlets), len(self.gridlets), _ptr(self.scalars), len(self.scalars))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oc_field_destroy(self.h)
+            self.h = None
+
+    def set_prim_opacities(self, gridlet_ops, elem_ops):
+        self._gops = None if gridlet_ops is None else np.ascontiguousarray(gridlet_ops, dtype=np.float32)
+        self._eops = None if elem_ops is None else np.ascontiguousarray(elem_ops, dtype=np.float32)
+        lib().oc_field_set_prim_opacities(self.h, _ptr(self._gops), _ptr(self._eops))
+
+    def bounds(self):
+        b, r = Box3f(), Range1f()
+        lib().oc_field_bounds(self.h, C.byref(b), C.byref(r))
+        lo = np.array([b.lower.x, b.lower.y, b.lower.z], np.float32)
+        hi = np.array([b.upper.x, b.upper.y, b.upper.z], np.float32)
+        return lo, hi, (r.lower, r.upper)
+
+    def sample(self, pos, cull=0, nthreads=0):
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros(len(pos), SAMPLE_DTYPE)
+        lib().oc_sample_points(self.h, _ptr(pos), len(pos), _ptr(out), int(cull), int(nthreads))
+        return out
+
+    def sample_all(self, p, cull=0, max_out=16):
+        kinds = np.zeros(max_out, np.int32)
+        ids = np.zeros(max_out, np.int32)
+        vals = np.zeros(max_out, np.float32)
+        n = lib().oc_sample_all(self.h, v3(p), int(cull), max_out, _ptr(kinds), _ptr(ids), _ptr(vals))
+        return [(int(kinds[i]), int(ids[i]), float(vals[i])) for i in range(n)]
+
+    def majorants(self, dims, lo, hi):
+        n = int(dims[0]) * int(dims[1]) * int(dims[2])
+        out = np.zeros((n, 2), np.float32)
+        lib().oc_build_majorants(self.h, Vec3i(*[int(d) for d in dims]), box(lo, hi), _ptr(out))
+        return out
+
+    def gridlet_value_ranges(self):
+        out = np.zeros((len(self.gridlets), 2), np.float32)
+        lib().oc_gridlet_value_ranges(self.h, _ptr(out))
+        return out
+
+    def elem_max_opacities(self, cmap, xf_range):
+        cmap = np.ascontiguousarray(cmap, dtype=np.float32).reshape(-1, 4)
+        out = np.zeros(len(self.indices), np.float32)
+        lib().oc_elem_max_opacities(self.h, _ptr(cmap), len(cmap), Range1f(*xf_range), _ptr(out))
+        return out
+
+    def render(self, lp_bytes, width, height, pixel_begin=0, pixel_end=None, nthreads=0):
+        if pixel_end is None:
+            pixel_end = width * height
+        return lib().oc_render(self.h, lp_bytes, width, height, pixel_begin, pixel_end, nthreads)
+
+    def render_f64(self, lp_bytes, width, height, pixel_begin=0, pixel_end=None, nthreads=0):
+        if pixel_end is None:
+            pixel_end = width * height
+        out = np.zeros((pixel_end - pixel_begin, 3), np.float64)
+        lib().oc_render_f64(self.h, lp_bytes, width, height, pixel_begin, pixel_end, _ptr(out), nthreads)
+        return out
+
+
+def max_opacities(ranges, cmap, xf_range):
+    ranges = np.ascontiguousarray(ranges, dtype=np.float32).reshape(-1, 2)
+    cmap = np.ascontiguousarray(cmap, dtype=np.float32).reshape(-1, 4)
+    out = np.zeros(len(ranges), np.float32)
+    lib().oc_compute_max_opacities(_ptr(ranges), len(ranges), _ptr(cmap), len(cmap), Range1f(*xf_range), _ptr(out))
+    return out
+
+
+def project_on_grid(V, dims, lo, hi):
+    r = lib().oc_project_on_grid(v3(V), Vec3i(*[int(d) for d in dims]), box(lo, hi))
+    return (r.x, r.y, r.z)
+
+
+def dda3(org, dirv, tmin, tmax, dims, lo, hi, max_cells=4096):
+    ids = np.zeros(max_cells, np.int64)
+    t0 = np.zeros(max_cells, np.float32)
+    t1 = np.zeros(max_cells, np.float32)
+    n = lib().oc_dda3(v3(org), v3(dirv), float(tmin), float(tmax), Vec3i(*[int(d) for d in dims]),
+                      box(lo, hi), max_cells, _ptr(ids), _ptr(t0), _ptr(t1))
+    return ids[:n], t0[:n], t1[:n]
+
+
+def intersect_gridlet(pos, gridlet, scalars):
+    g = np.ascontiguousarray(np.array([gridlet], dtype=GRIDLET_DTYPE) if not isinstance(gridlet, np.ndarray) else gridlet.reshape(1))
+    s = np.ascontiguousarray(scalars, dtype=np.float32)
+    v, c = C.c_float(0), C.c_int(-1)
+    hit = lib().oc_intersect_gridlet(C.byref(v), C.byref(c), v3(pos), _ptr(g), _ptr(s))
+    return bool(hit), v.value, c.value
+
+
+def intersect_elem(pos, verts):
+    """verts: (n,4) with n in {4,5,6,8}."""
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 4)
+    idx = np.full(8, -1, np.int32)
+    idx[: len(verts)] = np.arange(len(verts))
+    v = C.c_float(0)
+    hit = lib().oc_intersect_elem(C.byref(v), v3(pos), _ptr(idx), _ptr(verts))
+    return bool(hit), v.value
+
+
+# ---------------------------------------------------------------- reference
+def ref_intersect_elem(pos, verts):
+    R = ref()
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 4)
+    P = np.ascontiguousarray(pos, dtype=np.float32)
+    name = {4: "tet", 5: "pyr", 6: "wedge", 8: "hex"}[len(verts)]
+    v = C.c_float(0)
+    hit = getattr(R, "ref_intersect_" + name)(C.byref(v), _ptr(P), _ptr(verts))
+    return bool(hit), v.value
+
+
+def ref_intersect_gridlet(pos, gridlet, scalars):
+    R = ref()
+    g = np.ascontiguousarray(np.array([gridlet], dtype=GRIDLET_DTYPE) if not isinstance(gridlet, np.ndarray) else gridlet.reshape(1))
+    s = np.ascontiguousarray(scalars, dtype=np.float32)
+    P = np.ascontiguousarray(pos, dtype=np.float32)
+    v, c = C.c_float(0), C.c_int(-1)
+    hit = R.ref_intersect_gridlet(C.byref(v), C.byref(c), _ptr(P), _ptr(g), _ptr(s))
+    return bool(hit), v.value, c.value
+
+
+def ref_project_on_grid(V, dims, lo, hi):
+    R = ref()
+    V = np.ascontiguousarray(V, np.float32)
+    d = np.ascontiguousarray(dims, np.int32)
+    b = np.ascontiguousarray(np.concatenate([lo, hi]), np.float32)
+    out = np.zeros(3, np.int32)
+    R.ref_project_on_grid(_ptr(V), _ptr(d), _ptr(b), _ptr(out))
+    return tuple(int(x) for x in out)
+
+
+def ref_dda3(org, dirv, tmin, tmax, dims, lo, hi, max_cells=4096):
+    R = ref()
+    o = np.ascontiguousarray(org, np.float32)
+    dv = np.ascontiguousarray(dirv, np.float32)
+    d = np.ascontiguousarray(dims, np.int32)
+    b = np.ascontiguousarray(np.concatenate([lo, hi]), np.float32)
+    ids = np.zeros(max_cells, np.int64)
+    t0 = np.zeros(max_cells, np.float32)
+    t1 = np.zeros(max_cells, np.float32)
+    n = R.ref_dda3(_ptr(o), _ptr(dv), float(tmin), float(tmax), _ptr(d), _ptr(b), max_cells,
+                   _ptr(ids), _ptr(t0), _ptr(t1))
+    return ids[:n], t0[:n], t1[:n]

@@ -1,0 +1,91 @@
+"""Builds the native parts in-tree:
+  libexastitch.so -- the CUDA path (sm_103a kernels + C++ host + C ABI)
+  libexagen.so    -- the dataset generator (host C++)
+Compiles translation units in parallel and skips up-to-date outputs.
+
+    python -m owlexastitcher_gb300.build
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(ROOT, "_build")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# --fmad=false: no contracted multiply-add, so float results follow the
+# source's operation order exactly (the CPU oracle builds the same way)
+NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
+CUDA_SOURCES = ["exa_build.cu", "exa_render.cu", "exa_api.cpp"]
+HEADERS = ["exa_device.cuh", "exa_accel.cuh", "exa_host.h"]
+
+
+def nvcc():
+    for c in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _newer(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build_exastitch(verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(PKG, "libexastitch.so")
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "exastitch.h")]
+    objs, jobs = [], []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if _newer(o, [s] + hdrs):
+            cmd = [nvcc()] + ARCH + NVFLAGS + ["-x", "cu", "-c", s, "-o", o]
+            if verbose:
+                cmd += ["-Xptxas", "-v"]
+            jobs.append(cmd)
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for log in ex.map(_run, jobs):
+            if verbose and log:
+                print(log)
+    if _newer(out, objs):
+        _run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", out] + objs)
+    return out
+
+
+def build_exagen():
+    out = os.path.join(PKG, "libexagen.so")
+    src = os.path.join(CSRC, "gen", "exagen.cpp")
+    deps = [src, os.path.join(INCLUDE, "exastitch_gen.h"), os.path.join(INCLUDE, "exastitch.h")]
+    if _newer(out, deps):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c++17", "-o", out, src])
+    return out
+
+
+def build_all(verbose=False):
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        a = ex.submit(build_exastitch, verbose)
+        b = ex.submit(build_exagen)
+        return a.result(), b.result()
+
+
+if __name__ == "__main__":
+    print(build_all(verbose="-v" in sys.argv))

@@ -1,0 +1,203 @@
+// exa_accel.cuh -- point location for the ExaStitch field, replacing the
+// OptiX TLAS over the gridlet and stitching-element BLASes
+// (sampler/ExaStitchSampler.cpp:71-323) and the zero-length-ray query of
+// sample() (sampler/ExaStitchSampler.h:128-140).
+//
+// Gridlets: one table per level over the level's dual-cell lattice, one
+// entry per 2^shift-wide block (8 for makeGrids bricks, makeGrids.cpp:46).
+// An entry holds the single gridlet whose half-open interior touches the
+// block, or a list.  A query on an exact block face also looks at the
+// neighbouring block, so the reference's inclusive box test is honoured.
+// Stitching elements: a linear BVH (Karras 2012, "Maximizing parallelism in
+// the construction of BVHs, octrees and k-d trees") built on the GPU; each
+// 64-byte node stores both child boxes and child max opacities.
+//
+// Canonical answer when several primitives contain the point (shared
+// faces): the lowest-index gridlet, else the lowest-index element.
+// Primitives whose max opacity is 0 are invisible when culling (the
+// reference gives them empty AABBs: programs/ExaStitchSampler.cu:35-41,81-83).
+#pragma once
+
+#include "exa_device.cuh"
+
+namespace exa {
+
+constexpr int kMaxLevels = 16;
+constexpr int kBvhStack = 64;
+
+struct GridletTable {
+  int level;
+  int shift;       // block width 2^shift dual cells
+  int origin[3];   // lattice coordinate of block (0,0,0)
+  int n[3];        // blocks per axis
+  const int32_t *entries;  // -1 empty; >= 0 gridlet; <= -2 list at items[-e-2]
+  const int32_t *items;    // list: count, ids ascending
+};
+
+struct BvhNode {   // 64 B: two child boxes, two child refs, two opacities
+  float lo0[3], hi0[3];
+  float lo1[3], hi1[3];
+  int32_t child[2];     // >= 0 internal node, < 0 leaf element ~child
+  float op[2];          // max opacity of each child subtree
+};
+
+struct AccelView {
+  const exa_gridlet *gridlets;
+  const float *scalars;
+  const float *gridletMaxOps;   // may be null (no TF yet)
+  const float4 *vertices;
+  const int32_t *indices;
+  const float *elemMaxOps;      // may be null
+  const BvhNode *nodes;
+  int numGridlets;
+  int numElems;
+  int numTables;
+  int tablesSorted;             // 1: tables in ascending gridlet-index order
+  GridletTable tables[kMaxLevels];
+};
+
+EXA_D int floor_div_pow2(int v, int shift) { return v >> shift; }  // arithmetic shift floors
+
+// test every candidate gridlet of one table; keeps the lowest index hit
+EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool cull, int &best,
+                       float &bestVal, int &bestCell)
+{
+  const float inv = __uint_as_float((uint32_t)(127 - T.level) << 23);  // 2^-level
+  const float u[3] = {pos.x * inv - 0.5f, pos.y * inv - 0.5f, pos.z * inv - 0.5f};
+  int b0[3], nb[3];
+  for (int a = 0; a < 3; ++a) {
+    const float fu = floorf(u[a]);
+    if (!(fu >= -2147483520.f && fu <= 2147483520.f)) return;  // NaN / far outside
+    const int iu = (int)fu - T.origin[a];
+    int b = floor_div_pow2(iu, T.shift);
+    // exactly on a block face: the gridlet ending there is listed in the
+    // block below
+    const bool face = (fu == u[a]) && ((iu & ((1 << T.shift) - 1)) == 0);
+    nb[a] = face ? 2 : 1;
+    b0[a] = face ? b - 1 : b;
+  }
+  for (int dz = 0; dz < nb[2]; ++dz)
+    for (int dy = 0; dy < nb[1]; ++dy)
+      for (int dx = 0; dx < nb[0]; ++dx) {
+        const int bx = b0[0] + dx, by = b0[1] + dy, bz = b0[2] + dz;
+        if (bx < 0 || by < 0 || bz < 0 || bx >= T.n[0] || by >= T.n[1] || bz >= T.n[2]) continue;
+        const int e = __ldg(T.entries + ((size_t)bz * T.n[1] + by) * T.n[0] + bx);
+        if (e == -1) continue;
+        int cnt = 1;
+        const int32_t *list = nullptr;
+        if (e <= -2) {
+          list = T.items + (-e - 2);
+          cnt = __ldg(list);
+        }
+        for (int k = 0; k < cnt; ++k) {
+          const int g = list ? __ldg(list + 1 + k) : e;
+          if (g >= best) break;  // lists are ascending
+          if (cull && A.gridletMaxOps && __ldg(A.gridletMaxOps + g) == 0.f) continue;
+          float v;
+          int c;
+          if (intersect_gridlet(v, c, pos, A.gridlets + g, A.scalars)) {
+            best = g;
+            bestVal = v;
+            bestCell = c;
+          }
+        }
+      }
+}
+
+EXA_D bool box_contains(const float *lo, const float *hi, V3 p)
+{
+  return lo[0] <= p.x && lo[1] <= p.y && lo[2] <= p.z && p.x <= hi[0] && p.y <= hi[1] && p.z <= hi[2];
+}
+
+// full traversal: lowest-index containing element; returns false on stack
+// overflow (error flag raised by the caller)
+EXA_D bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal)
+{
+  if (A.numElems <= 0) return true;
+  int stack[kBvhStack];
+  int sp = 0;
+  int node = 0;
+  const bool useOps = cull && A.elemMaxOps;
+  // a well-formed tree visits each of its numElems-1 nodes at most once
+  for (int visits = 0; visits <= A.numElems + 1; ++visits) {
+    const float4 *np = reinterpret_cast<const float4 *>(A.nodes + node);
+    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+    const float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
+    const float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
+    const int c0 = __float_as_int(q3.x), c1 = __float_as_int(q3.y);
+    const bool in0 = box_contains(lo0, hi0, pos) && !(useOps && q3.z == 0.f);
+    const bool in1 = box_contains(lo1, hi1, pos) && !(useOps && q3.w == 0.f);
+    int next = -1;
+    if (in0) {
+      if (c0 < 0) {
+        const int e = ~c0;
+        float v;
+        if (e < best && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) { best = e; bestVal = v; }
+      } else {
+        next = c0;
+      }
+    }
+    if (in1) {
+      if (c1 < 0) {
+        const int e = ~c1;
+        float v;
+        if (e < best && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) { best = e; bestVal = v; }
+      } else if (next < 0) {
+        next = c1;
+      } else {
+        if (sp >= kBvhStack) return false;
+        stack[sp++] = c1;
+      }
+    }
+    if (next < 0) {
+      if (sp == 0) return true;
+      next = stack[--sp];
+    }
+    node = next;
+  }
+  return false;
+}
+
+// sample() (sampler/ExaStitchSampler.h:128-140); sets EXA_DEVERR bits in err
+EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err)
+{
+  exa_sample s;
+  s.primID = -1;
+  s.cellID = -1;
+  s.value = 0.f;
+  int best = 0x7fffffff, cell = -1;
+  float val = 0.f;
+  for (int t = 0; t < A.numTables; ++t) {
+    query_table(A, A.tables[t], pos, cull, best, val, cell);
+    if (A.tablesSorted && best != 0x7fffffff) break;
+  }
+  if (best != 0x7fffffff) {
+    s.primID = best;
+    s.cellID = cell;
+    s.value = val;
+    return s;
+  }
+  int be = 0x7fffffff;
+  float ev = 0.f;
+  if (!query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
+  if (be != 0x7fffffff) {
+    s.primID = be;
+    s.cellID = -1;
+    s.value = ev;
+  }
+  return s;
+}
+
+// testSample (sampler/ExaStitchSampler.h:108-126): the cached gridlet only
+EXA_D exa_sample test_sample(const AccelView &A, V3 pos, int primID)
+{
+  exa_sample s;
+  s.primID = -1;
+  s.cellID = -1;
+  s.value = 0.f;
+  if (primID < 0) return s;
+  if (intersect_gridlet(s.value, s.cellID, pos, A.gridlets + primID, A.scalars)) s.primID = primID;
+  return s;
+}
+
+} // namespace exa

@@ -1,0 +1,710 @@
+// exa_api.cpp -- host classes (Model, ExaStitchModel, ExaStitchSampler,
+// Grid) and the C ABI of exastitch.h.  No exception crosses the C boundary.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+
+#include "exa_host.h"
+
+namespace exa {
+
+// ================================================================ Model
+void Model::setNumGridCells(exa_vec3i numMCs)
+{
+  if (grid) throw Error(EXA_ERR_STATE, "must set num grid cells before calling initGPU!");
+  if (numMCs.x <= 0 || numMCs.y <= 0 || numMCs.z <= 0) throw Error(EXA_ERR_INVALID, "grid dims must be positive");
+  grid = std::make_shared<Grid>();
+  grid->dims = numMCs;
+}
+
+static exa_affine3f affine_identity()
+{
+  exa_affine3f a;
+  std::memset(&a, 0, sizeof(a));
+  a.l.vx.x = a.l.vy.y = a.l.vz.z = 1.f;
+  return a;
+}
+
+// affine3f::translate(lower) * affine3f::scale(span), and its inverse
+static exa_affine3f affine_box(exa_box3f b, bool inverse)
+{
+  exa_affine3f a = affine_identity();
+  const float sx = b.upper.x - b.lower.x, sy = b.upper.y - b.lower.y, sz = b.upper.z - b.lower.z;
+  if (!inverse) {
+    a.l.vx.x = sx; a.l.vy.y = sy; a.l.vz.z = sz;
+    a.p = b.lower;
+  } else {
+    a.l.vx.x = 1.f / sx; a.l.vy.y = 1.f / sy; a.l.vz.z = 1.f / sz;
+    a.p.x = -b.lower.x / sx; a.p.y = -b.lower.y / sy; a.p.z = -b.lower.z / sz;
+  }
+  return a;
+}
+
+// composition of two diagonal-linear affines: (A*B)(p) = A(B(p))
+static exa_affine3f affine_mul_diag(const exa_affine3f &A, const exa_affine3f &B)
+{
+  exa_affine3f r = affine_identity();
+  r.l.vx.x = A.l.vx.x * B.l.vx.x;
+  r.l.vy.y = A.l.vy.y * B.l.vy.y;
+  r.l.vz.z = A.l.vz.z * B.l.vz.z;
+  r.p.x = A.l.vx.x * B.p.x + A.p.x;
+  r.p.y = A.l.vy.y * B.p.y + A.p.y;
+  r.p.z = A.l.vz.z * B.p.z + A.p.z;
+  return r;
+}
+
+// Model.cpp:35-48: voxel = voxelCoordSys * rcp(worldCoordSys)
+void Model::setVoxelSpaceTransform(exa_box3f from, exa_box3f to)
+{
+  voxelSpaceTransform = affine_mul_diag(affine_box(from, false), affine_box(to, true));
+  voxelSpaceTransformInv = affine_mul_diag(affine_box(to, false), affine_box(from, true));
+}
+
+static exa_vec3f xfm_point_h(const exa_affine3f &A, exa_vec3f p)
+{
+  exa_vec3f r;
+  r.x = (p.x * A.l.vx.x + p.y * A.l.vy.x + p.z * A.l.vz.x) + A.p.x;
+  r.y = (p.x * A.l.vx.y + p.y * A.l.vy.y + p.z * A.l.vz.y) + A.p.y;
+  r.z = (p.x * A.l.vx.z + p.y * A.l.vy.z + p.z * A.l.vz.z) + A.p.z;
+  return r;
+}
+
+exa_box3f Model::getBounds() const
+{
+  exa_box3f b;
+  b.lower = xfm_point_h(voxelSpaceTransformInv, cellBounds.lower);
+  b.upper = xfm_point_h(voxelSpaceTransformInv, cellBounds.upper);
+  return b;
+}
+
+void ExaStitchModel::assign(const exa_vec4f *v, size_t nv, const int32_t *idx, size_t ne, const exa_gridlet *g,
+                            size_t ng, const float *s, size_t ns)
+{
+  vertices.assign(v, v + nv);
+  indices.assign(idx, idx + ne * 8);
+  gridlets.assign(g, g + ng);
+  gridletScalars.assign(s, s + ns);
+  voxelSpaceTransform = affine_identity();
+  voxelSpaceTransformInv = affine_identity();
+  lightSpaceTransform = affine_identity();
+  // model/ExaStitchModel.cpp:78-114 (elements) and 188-247 (gridlets)
+  cellBounds.lower = {INFINITY, INFINITY, INFINITY};
+  cellBounds.upper = {-INFINITY, -INFINITY, -INFINITY};
+  valueRange = {1e30f, -1e30f};
+  auto extend = [&](float x, float y, float z) {
+    cellBounds.lower.x = std::min(cellBounds.lower.x, x); cellBounds.upper.x = std::max(cellBounds.upper.x, x);
+    cellBounds.lower.y = std::min(cellBounds.lower.y, y); cellBounds.upper.y = std::max(cellBounds.upper.y, y);
+    cellBounds.lower.z = std::min(cellBounds.lower.z, z); cellBounds.upper.z = std::max(cellBounds.upper.z, z);
+  };
+  for (size_t e = 0; e < ne; ++e)
+    for (int j = 0; j < 8; ++j) {
+      const int id = indices[e * 8 + j];
+      if (id < 0) continue;
+      if ((size_t)id >= nv) throw Error(EXA_ERR_INVALID, "element index out of range");
+      const exa_vec4f &p = vertices[id];
+      extend(p.x, p.y, p.z);
+      valueRange.lower = std::min(valueRange.lower, p.w);
+      valueRange.upper = std::max(valueRange.upper, p.w);
+    }
+  numScalarsTotal = 0;
+  numEmptyScalars = 0;
+  for (size_t k = 0; k < ng; ++k) {
+    const exa_gridlet &gl = gridlets[k];
+    if (gl.dims.x < 0 || gl.dims.y < 0 || gl.dims.z < 0 || gl.level < 0 || gl.level > 30)
+      throw Error(EXA_ERR_INVALID, "invalid gridlet header");
+    const size_t n = (size_t)(gl.dims.x + 1) * (gl.dims.y + 1) * (gl.dims.z + 1);
+    if ((size_t)gl.begin + n > ns) throw Error(EXA_ERR_INVALID, "gridlet scalars out of range");
+    for (size_t i = 0; i < n; ++i) {
+      const float v = gridletScalars[gl.begin + i];
+      if (std::isnan(v)) numEmptyScalars++;
+      valueRange.lower = std::min(valueRange.lower, v);
+      valueRange.upper = std::max(valueRange.upper, v);
+    }
+    numScalarsTotal += n;
+    const float cw = (float)(1 << gl.level);
+    extend(((float)gl.lower.x + 0.5f) * cw, ((float)gl.lower.y + 0.5f) * cw, ((float)gl.lower.z + 0.5f) * cw);
+    extend((((float)gl.lower.x + (float)gl.dims.x) + 0.5f) * cw, (((float)gl.lower.y + (float)gl.dims.y) + 0.5f) * cw,
+           (((float)gl.lower.z + (float)gl.dims.z) + 0.5f) * cw);
+  }
+}
+
+// model/ExaStitchModel.cpp:259-279
+void ExaStitchModel::memStats(size_t &elemVertexBytes, size_t &elemIndexBytes, size_t &gridletBytes,
+                              size_t &emptyScalarsBytes, size_t &nonEmptyScalarsBytes) const
+{
+  elemVertexBytes = vertices.size() * sizeof(exa_vec4f);
+  elemIndexBytes = indices.size() * sizeof(int32_t);
+  gridletBytes = gridlets.size() * sizeof(exa_gridlet);
+  emptyScalarsBytes = numEmptyScalars * sizeof(float);
+  nonEmptyScalarsBytes = (numScalarsTotal - numEmptyScalars) * sizeof(float);
+}
+
+// ================================================================ sampler
+size_t ExaStitchSampler::accelBytes() const
+{
+  size_t b = bvhNodes.bytes() + bvhParents.bytes() + bvhLeafElem.bytes();
+  for (auto &t : tableEntries) b += t.bytes();
+  for (auto &t : tableItems) b += t.bytes();
+  return b;
+}
+
+// Per-level block tables over the dual-cell lattice.  Block width 8
+// (makeGrids bricks); widened when a level's table would be very large.
+void ExaStitchSampler::buildGridletTables(cudaStream_t s)
+{
+  const auto &G = model->gridlets;
+  std::map<int, std::vector<int>> byLevel;
+  for (size_t i = 0; i < G.size(); ++i) byLevel[G[i].level].push_back((int)i);
+  if ((int)byLevel.size() > kMaxLevels) throw Error(EXA_ERR_INVALID, "more than 16 gridlet levels");
+  struct Tab { GridletTable t; std::vector<int32_t> entries, items; int minIdx, maxIdx; };
+  std::vector<Tab> tabs;
+  for (auto &kv : byLevel) {
+    Tab T;
+    std::memset(&T.t, 0, sizeof(T.t));
+    T.t.level = kv.first;
+    int lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    T.minIdx = INT32_MAX;
+    T.maxIdx = -1;
+    for (int gi : kv.second) {
+      const exa_gridlet &g = G[gi];
+      const int gl[3] = {g.lower.x, g.lower.y, g.lower.z}, gd[3] = {g.dims.x, g.dims.y, g.dims.z};
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], gl[a]);
+        hi[a] = std::max(hi[a], gl[a] + std::max(gd[a], 1));
+      }
+      T.minIdx = std::min(T.minIdx, gi);
+      T.maxIdx = std::max(T.maxIdx, gi);
+    }
+    int shift = 3;
+    auto blocks = [&](int sh, int a) { return (int)(((int64_t)(hi[a] - lo[a]) + (1ll << sh) - 1) >> sh) + 1; };
+    while ((int64_t)blocks(shift, 0) * blocks(shift, 1) * blocks(shift, 2) > (1ll << 27) && shift < 20) shift++;
+    T.t.shift = shift;
+    for (int a = 0; a < 3; ++a) { T.t.origin[a] = lo[a]; T.t.n[a] = blocks(shift, a); }
+    const size_t nb = (size_t)T.t.n[0] * T.t.n[1] * T.t.n[2];
+    std::vector<std::vector<int32_t>> lists(nb);
+    for (int gi : kv.second) {
+      const exa_gridlet &g = G[gi];
+      const int gl[3] = {g.lower.x, g.lower.y, g.lower.z}, gd[3] = {g.dims.x, g.dims.y, g.dims.z};
+      int b0[3], b1[3];
+      for (int a = 0; a < 3; ++a) {
+        b0[a] = (gl[a] - lo[a]) >> shift;
+        b1[a] = (gl[a] + std::max(gd[a], 1) - 1 - lo[a]) >> shift;
+      }
+      for (int z = b0[2]; z <= b1[2]; ++z)
+        for (int y = b0[1]; y <= b1[1]; ++y)
+          for (int x = b0[0]; x <= b1[0]; ++x)
+            lists[((size_t)z * T.t.n[1] + y) * T.t.n[0] + x].push_back(gi);
+    }
+    T.entries.assign(nb, -1);
+    for (size_t b = 0; b < nb; ++b) {
+      auto &L = lists[b];
+      if (L.empty()) continue;
+      if (L.size() == 1) { T.entries[b] = L[0]; continue; }
+      std::sort(L.begin(), L.end());
+      T.entries[b] = -(int32_t)T.items.size() - 2;
+      T.items.push_back((int32_t)L.size());
+      T.items.insert(T.items.end(), L.begin(), L.end());
+    }
+    tabs.push_back(std::move(T));
+  }
+  std::sort(tabs.begin(), tabs.end(), [](const Tab &a, const Tab &b) { return a.minIdx < b.minIdx; });
+  bool sorted = true;
+  for (size_t i = 1; i < tabs.size(); ++i)
+    if (tabs[i].minIdx <= tabs[i - 1].maxIdx) sorted = false;
+  tableEntries.clear();
+  tableItems.clear();
+  tableEntries.resize(tabs.size());
+  tableItems.resize(tabs.size());
+  accel.numTables = (int)tabs.size();
+  accel.tablesSorted = sorted ? 1 : 0;
+  for (size_t i = 0; i < tabs.size(); ++i) {
+    tableEntries[i].upload(tabs[i].entries.data(), tabs[i].entries.size(), s);
+    if (tabs[i].items.empty()) tabs[i].items.push_back(0);
+    tableItems[i].upload(tabs[i].items.data(), tabs[i].items.size(), s);
+    accel.tables[i] = tabs[i].t;
+    accel.tables[i].entries = tableEntries[i].ptr;
+    accel.tables[i].items = tableItems[i].ptr;
+  }
+}
+
+void ExaStitchSampler::buildElementBVH(cudaStream_t s)
+{
+  const size_t ne = model->indices.size() / 8;
+  accel.numElems = (int)ne;
+  if (!ne) { accel.nodes = nullptr; return; }
+  bvhNodes.alloc(ne > 1 ? ne - 1 : 1);
+  bvhParents.alloc((ne > 1 ? ne - 1 : 0) + ne);
+  bvhLeafElem.alloc(ne);
+  exa_box3f sb;
+  sb.lower = {INFINITY, INFINITY, INFINITY};
+  sb.upper = {-INFINITY, -INFINITY, -INFINITY};
+  for (const exa_vec4f &v : model->vertices) {
+    sb.lower.x = std::min(sb.lower.x, v.x); sb.upper.x = std::max(sb.upper.x, v.x);
+    sb.lower.y = std::min(sb.lower.y, v.y); sb.upper.y = std::max(sb.upper.y, v.y);
+    sb.lower.z = std::min(sb.lower.z, v.z); sb.upper.z = std::max(sb.upper.z, v.z);
+  }
+  launchBuildBVH(vertexBuffer.ptr, indexBuffer.ptr, ne, sb, bvhNodes.ptr, bvhParents.ptr, bvhLeafElem.ptr, s);
+  accel.nodes = bvhNodes.ptr;
+}
+
+// sampler/ExaStitchSampler.cpp:23-340
+bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
+{
+  if (!mod) return false;
+  model = std::dynamic_pointer_cast<ExaStitchModel>(mod);
+  if (!model) return false;
+  if (model->gridlets.empty() && model->indices.empty()) return false;
+  if (!model->grid || model->grid->dims.x == 0) return false;
+  std::memset(&accel, 0, sizeof(accel));
+  // gridlet geometry
+  gridletBuffer.upload(model->gridlets.data(), model->gridlets.size(), s);
+  gridletScalarBuffer.upload(model->gridletScalars.data(), model->gridletScalars.size(), s);
+  gridletValueRanges.alloc(model->gridlets.size());
+  gridletMaxOpacities.alloc(model->gridlets.size());
+  // stitching geometry
+  static_assert(sizeof(float4) == sizeof(exa_vec4f), "vec4f layout");
+  vertexBuffer.upload(reinterpret_cast<const float4 *>(model->vertices.data()), model->vertices.size(), s);
+  indexBuffer.upload(model->indices.data(), model->indices.size(), s);
+  elemValueRanges.alloc(model->indices.size() / 8);
+  umeshMaxOpacities.alloc(model->indices.size() / 8);
+  accel.gridlets = gridletBuffer.ptr;
+  accel.scalars = gridletScalarBuffer.ptr;
+  accel.vertices = vertexBuffer.ptr;
+  accel.indices = indexBuffer.ptr;
+  accel.numGridlets = (int)model->gridlets.size();
+  buildGridletTables(s);
+  buildElementBVH(s);
+  // the majorant grid (Grid::build, Grid.cu:457-594) over cellBounds
+  Grid &g = *model->grid;
+  g.worldBounds = model->cellBounds;
+  const size_t numMCs = (size_t)g.dims.x * g.dims.y * g.dims.z;
+  g.valueRanges.alloc(numMCs);
+  g.maxOpacities.alloc(numMCs);
+  cudaCheck(cudaMemsetAsync(g.maxOpacities.ptr, 0, g.maxOpacities.bytes(), s), "memset maxOpacities");
+  launchInitRanges(g.valueRanges.ptr, numMCs, s);
+  launchInitRanges(gridletValueRanges.ptr, gridletValueRanges.count, s);
+  launchElemMajorants(vertexBuffer.ptr, indexBuffer.ptr, model->indices.size() / 8, g.dims, g.worldBounds,
+                      g.valueRanges.ptr, elemValueRanges.ptr, s);
+  launchGridletMajorants(gridletBuffer.ptr, gridletScalarBuffer.ptr, model->gridlets.size(), g.dims, g.worldBounds,
+                         g.valueRanges.ptr, gridletValueRanges.ptr, s);
+  g.deviceTraversable.dims = g.dims;
+  g.deviceTraversable.bounds = g.worldBounds;
+  deviceAccel.alloc(1);
+  cudaCheck(cudaMemcpyAsync(deviceAccel.ptr, &accel, sizeof(accel), cudaMemcpyHostToDevice, s), "accel handle");
+  cudaCheck(cudaStreamSynchronize(s), "sampler build");
+  majorantAccel.grid = model->grid;
+  maxOpacities = g.maxOpacities.ptr;
+  hasTF = false;
+  return true;
+}
+
+// sampler/ExaStitchSampler.cu:279-376 + Grid::computeMaxOpacities
+void ExaStitchSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors, exa_range1f xf, cudaStream_t s)
+{
+  if (!model || !model->grid || model->grid->dims.x == 0) return;
+  if (numColors <= 0) throw Error(EXA_ERR_INVALID, "empty color map");
+  colorMap.upload(reinterpret_cast<const float4 *>(cmap), (size_t)numColors, s);
+  Grid &g = *model->grid;
+  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, g.maxOpacities.ptr, s);
+  launchMaxOpacity(gridletValueRanges.ptr, gridletValueRanges.count, colorMap.ptr, numColors, xf,
+                   gridletMaxOpacities.ptr, s);
+  launchMaxOpacity(elemValueRanges.ptr, elemValueRanges.count, colorMap.ptr, numColors, xf, umeshMaxOpacities.ptr, s);
+  if (accel.numElems > 0)
+    launchRefitBVH(vertexBuffer.ptr, indexBuffer.ptr, (size_t)accel.numElems, bvhNodes.ptr, bvhParents.ptr,
+                   bvhLeafElem.ptr, umeshMaxOpacities.ptr, false, s);
+  accel.gridletMaxOps = gridletMaxOpacities.ptr;
+  accel.elemMaxOps = umeshMaxOpacities.ptr;
+  cudaCheck(cudaMemcpyAsync(deviceAccel.ptr, &accel, sizeof(accel), cudaMemcpyHostToDevice, s), "accel handle");
+  cudaCheck(cudaStreamSynchronize(s), "computeMaxOpacities");
+  hasTF = true;
+}
+
+// sampler/ExaStitchSampler.cpp:356-365
+void ExaStitchSampler::setLPs(exa_launch_params &lp)
+{
+  lp.sampler.ess.sampleBVH = (uint64_t)(uintptr_t)deviceAccel.ptr;
+  lp.sampler.ess.gridletBuffer = gridletBuffer.ptr;
+  lp.sampler.ess.gridletScalarBuffer = gridletScalarBuffer.ptr;
+}
+
+} // namespace exa
+
+// ================================================================ C ABI
+using namespace exa;
+
+struct exa_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  std::shared_ptr<ExaStitchModel> model;
+  std::shared_ptr<ExaStitchSampler> sampler;
+  exa_range1f xfRange{0.f, 1.f};
+  int numColors = 0;
+  DBuf<uint32_t> errors;
+  DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
+  DBuf<exa_sample> hostOut;
+};
+
+namespace {
+thread_local std::string g_lastError;
+
+template <typename F>
+int guarded(F &&f)
+{
+  try {
+    f();
+    g_lastError.clear();
+    return EXA_OK;
+  } catch (const Error &e) {
+    g_lastError = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_lastError = "host allocation failed";
+    return EXA_ERR_OOM;
+  } catch (const std::exception &e) {
+    g_lastError = e.what();
+    return EXA_ERR_INVALID;
+  }
+}
+
+void need(bool c, int code, const char *msg)
+{
+  if (!c) throw Error(code, msg);
+}
+
+void setDevice(exa_context *ctx) { cudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+} // namespace
+
+extern "C" {
+
+const char *exa_version(void) { return "exastitch-gb300 0.1 (sm_103a)"; }
+
+uint64_t exa_abi_sizeof(int32_t which)
+{
+  switch (which) {
+    case 0: return sizeof(exa_launch_params);
+    case 1: return sizeof(exa_gridlet);
+    case 2: return sizeof(exa_sample);
+    case 3: return sizeof(exa_mem_stats);
+    case 4: return sizeof(exa_lp_ext);
+    default: return 0;
+  }
+}
+
+const char *exa_last_error(void) { return g_lastError.c_str(); }
+
+const char *exa_sampler_class_name(void) { return "ExaStitchSampler"; }
+
+int exa_context_create(exa_context **out, int device, uint64_t stream)
+{
+  return guarded([&] {
+    need(out != nullptr, EXA_ERR_INVALID, "out is null");
+    int n = 0;
+    cudaCheck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    need(device >= 0 && device < n, EXA_ERR_INVALID, "device index out of range");
+    std::unique_ptr<exa_context> c(new exa_context());
+    c->device = device;
+    cudaCheck(cudaSetDevice(device), "cudaSetDevice");
+    if (stream) {
+      c->stream = reinterpret_cast<cudaStream_t>(stream);
+    } else {
+      cudaCheck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      c->ownStream = true;
+    }
+    c->errors.alloc(1);
+    cudaCheck(cudaMemsetAsync(c->errors.ptr, 0, sizeof(uint32_t), c->stream), "memset errors");
+    cudaCheck(cudaStreamSynchronize(c->stream), "sync");
+    *out = c.release();
+  });
+}
+
+int exa_context_destroy(exa_context *ctx)
+{
+  return guarded([&] {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    const bool own = ctx->ownStream;
+    cudaStream_t s = ctx->stream;
+    delete ctx;
+    if (own) cudaStreamDestroy(s);
+  });
+}
+
+int exa_get_device_errors(exa_context *ctx, uint32_t *bits)
+{
+  return guarded([&] {
+    need(ctx && bits, EXA_ERR_INVALID, "null argument");
+    setDevice(ctx);
+    uint32_t v = 0;
+    cudaCheck(cudaMemcpyAsync(&v, ctx->errors.ptr, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "read errors");
+    cudaCheck(cudaMemsetAsync(ctx->errors.ptr, 0, sizeof(v), ctx->stream), "clear errors");
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "sync");
+    *bits = v;
+  });
+}
+
+int exa_sync(exa_context *ctx)
+{
+  uint32_t bits = 0;
+  const int rc = guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    setDevice(ctx);
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "exa_sync");
+  });
+  if (rc != EXA_OK) return rc;
+  const int rc2 = exa_get_device_errors(ctx, &bits);
+  if (rc2 != EXA_OK) return rc2;
+  if (bits) {
+    g_lastError = "device iteration cap hit (EXA_DEVERR bits " + std::to_string(bits) + ")";
+    return EXA_ERR_DEVICE_LIMIT;
+  }
+  return EXA_OK;
+}
+
+int exa_model_create(exa_context *ctx, const exa_vec4f *vertices, uint64_t numVertices, const int32_t *indices,
+                     uint64_t numElems, const exa_gridlet *gridlets, uint64_t numGridlets,
+                     const float *gridletScalars, uint64_t numGridletScalars)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    need(numVertices == 0 || vertices, EXA_ERR_INVALID, "vertices is null");
+    need(numElems == 0 || indices, EXA_ERR_INVALID, "indices is null");
+    need(numGridlets == 0 || gridlets, EXA_ERR_INVALID, "gridlets is null");
+    need(numGridletScalars == 0 || gridletScalars, EXA_ERR_INVALID, "gridletScalars is null");
+    need(numElems < 0x7fffffffull && numGridlets < 0x7fffffffull && numVertices < 0x7fffffffull &&
+             numGridletScalars <= 0xffffffffull,
+         EXA_ERR_INVALID, "array too large for 32-bit indices");
+    auto m = std::make_shared<ExaStitchModel>();
+    m->assign(vertices, numVertices, indices, numElems, gridlets, numGridlets, gridletScalars, numGridletScalars);
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+int exa_model_get_bounds(exa_context *ctx, exa_box3f *cellBounds, exa_range1f *valueRange)
+{
+  return guarded([&] {
+    need(ctx && ctx->model, EXA_ERR_STATE, "no model");
+    if (cellBounds) *cellBounds = ctx->model->cellBounds;
+    if (valueRange) *valueRange = ctx->model->valueRange;
+  });
+}
+
+int exa_model_set_num_grid_cells(exa_context *ctx, exa_vec3i numMCs)
+{
+  return guarded([&] {
+    need(ctx && ctx->model, EXA_ERR_STATE, "no model");
+    ctx->model->setNumGridCells(numMCs);
+  });
+}
+
+int exa_model_set_voxel_space_transform(exa_context *ctx, exa_box3f from, exa_box3f to)
+{
+  return guarded([&] {
+    need(ctx && ctx->model, EXA_ERR_STATE, "no model");
+    ctx->model->setVoxelSpaceTransform(from, to);
+  });
+}
+
+int exa_model_get_world_bounds(exa_context *ctx, exa_box3f *bounds)
+{
+  return guarded([&] {
+    need(ctx && ctx->model && bounds, EXA_ERR_STATE, "no model");
+    *bounds = ctx->model->getBounds();
+  });
+}
+
+int exa_model_mem_stats(exa_context *ctx, exa_mem_stats *out)
+{
+  return guarded([&] {
+    need(ctx && ctx->model && out, EXA_ERR_STATE, "no model");
+    size_t a, b, c, d, e;
+    ctx->model->memStats(a, b, c, d, e);
+    std::memset(out, 0, sizeof(*out));
+    out->elemVertexBytes = a;
+    out->elemIndexBytes = b;
+    out->gridletBytes = c;
+    out->emptyScalarsBytes = d;
+    out->nonEmptyScalarsBytes = e;
+    if (auto &S = ctx->sampler) {
+      out->deviceFieldBytes = S->gridletBuffer.bytes() + S->gridletScalarBuffer.bytes() + S->vertexBuffer.bytes() +
+                              S->indexBuffer.bytes();
+      out->deviceAccelBytes = S->accelBytes();
+      const auto &g = *ctx->model->grid;
+      out->deviceMajorantBytes = g.valueRanges.bytes() + g.maxOpacities.bytes() + S->gridletValueRanges.bytes() +
+                                 S->gridletMaxOpacities.bytes() + S->elemValueRanges.bytes() +
+                                 S->umeshMaxOpacities.bytes();
+    }
+  });
+}
+
+int exa_sampler_build(exa_context *ctx)
+{
+  return guarded([&] {
+    need(ctx && ctx->model, EXA_ERR_STATE, "no model");
+    need(ctx->model->grid != nullptr, EXA_ERR_STATE, "numGridCells not set");
+    setDevice(ctx);
+    auto s = std::make_shared<ExaStitchSampler>();
+    if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, "ExaStitchSampler::build failed");
+    ctx->sampler = s;
+  });
+}
+
+int exa_sampler_compute_max_opacities(exa_context *ctx, const exa_vec4f *colorMap, int32_t numColors,
+                                      exa_range1f xfRange)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(colorMap && numColors > 0, EXA_ERR_INVALID, "empty color map");
+    setDevice(ctx);
+    ctx->sampler->computeMaxOpacities(colorMap, numColors, xfRange, ctx->stream);
+    ctx->xfRange = xfRange;
+    ctx->numColors = numColors;
+  });
+}
+
+int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler && lp, EXA_ERR_STATE, "sampler not built");
+    ctx->sampler->setLPs(*lp);
+    const auto &m = *ctx->model;
+    lp->majorantGrid = m.grid->deviceTraversable;         // OWLRenderer.cpp:435-436
+    lp->maxOpacities = ctx->sampler->maxOpacities;         // :655-657
+    lp->worldSpaceBounds = m.getBounds();                  // :548-555
+    lp->voxelSpaceTransform = m.voxelSpaceTransform;       // :577
+    lp->lightSpaceTransform = m.lightSpaceTransform;       // :578
+    lp->ext.voxelSpaceTransformInv = m.voxelSpaceTransformInv;
+    if (ctx->sampler->hasTF) {                             // :710-711, 724
+      lp->transferFunc.values = reinterpret_cast<exa_vec4f *>(ctx->sampler->colorMap.ptr);
+      lp->transferFunc.numValues = ctx->numColors;
+      lp->transferFunc.domain = ctx->xfRange;
+    }
+    lp->ext.deviceErrors = ctx->errors.ptr;
+  });
+}
+
+int exa_get_majorants(exa_context *ctx, exa_range1f *valueRanges, float *maxOpacities)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    setDevice(ctx);
+    const Grid &g = *ctx->model->grid;
+    if (valueRanges)
+      cudaCheck(cudaMemcpyAsync(valueRanges, g.valueRanges.ptr, g.valueRanges.bytes(), cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy ranges");
+    if (maxOpacities)
+      cudaCheck(cudaMemcpyAsync(maxOpacities, g.maxOpacities.ptr, g.maxOpacities.bytes(), cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy maxOpacities");
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "sync");
+  });
+}
+
+int exa_get_prim_majorants(exa_context *ctx, exa_range1f *gridletRanges, float *gridletMaxOpacities,
+                           float *elemMaxOpacities)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    setDevice(ctx);
+    auto &S = *ctx->sampler;
+    if (gridletRanges && S.gridletValueRanges.count)
+      cudaCheck(cudaMemcpyAsync(gridletRanges, S.gridletValueRanges.ptr, S.gridletValueRanges.bytes(),
+                                cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    if (gridletMaxOpacities && S.gridletMaxOpacities.count)
+      cudaCheck(cudaMemcpyAsync(gridletMaxOpacities, S.gridletMaxOpacities.ptr, S.gridletMaxOpacities.bytes(),
+                                cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    if (elemMaxOpacities && S.umeshMaxOpacities.count)
+      cudaCheck(cudaMemcpyAsync(elemMaxOpacities, S.umeshMaxOpacities.ptr, S.umeshMaxOpacities.bytes(),
+                                cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "sync");
+  });
+}
+
+int exa_sample_points(exa_context *ctx, const exa_vec3f *posDevice, uint64_t n, exa_sample *outDevice,
+                      int32_t cullTransparent)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(n == 0 || (posDevice && outDevice), EXA_ERR_INVALID, "null buffer");
+    need(!cullTransparent || ctx->sampler->hasTF, EXA_ERR_STATE, "culling needs computeMaxOpacities first");
+    setDevice(ctx);
+    launchSamplePoints(ctx->sampler->accel, posDevice, n, outDevice, cullTransparent, ctx->errors.ptr, ctx->stream);
+  });
+}
+
+int exa_sample_points_host(exa_context *ctx, const exa_vec3f *posHost, uint64_t n, exa_sample *outHost,
+                           int32_t cullTransparent)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(n == 0 || (posHost && outHost), EXA_ERR_INVALID, "null buffer");
+    need(!cullTransparent || ctx->sampler->hasTF, EXA_ERR_STATE, "culling needs computeMaxOpacities first");
+    setDevice(ctx);
+    if (ctx->hostPos.count < n) { ctx->hostPos.alloc(n); ctx->hostOut.alloc(n); }
+    cudaCheck(cudaMemcpyAsync(ctx->hostPos.ptr, posHost, n * sizeof(exa_vec3f), cudaMemcpyHostToDevice, ctx->stream),
+              "copy in");
+    launchSamplePoints(ctx->sampler->accel, ctx->hostPos.ptr, n, ctx->hostOut.ptr, cullTransparent, ctx->errors.ptr,
+                       ctx->stream);
+    cudaCheck(cudaMemcpyAsync(outHost, ctx->hostOut.ptr, n * sizeof(exa_sample), cudaMemcpyDeviceToHost, ctx->stream),
+              "copy out");
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "sync");
+  });
+}
+
+int exa_launch_params_init(exa_launch_params *lp)
+{
+  return guarded([&] {
+    need(lp != nullptr, EXA_ERR_INVALID, "null lp");
+    std::memset(lp, 0, sizeof(*lp));
+    lp->integrator = EXA_PATH_TRACING_INTEGRATOR;     // OWLRenderer.cpp:569
+    lp->shadeMode = EXA_SHADE_MODE_DEFAULT;           // :571
+    lp->subImage.value.upper.y = 1.f;                 // :562-565
+    lp->subImage.selection.upper.x = 1.f;
+    lp->subImage.selection.upper.y = 1.f;
+    lp->render.dt = 1.f;                              // :616
+    lp->render.spp = 1;                               // :617
+    lp->render.heatMapScale = 1.f;
+    lp->transferFunc.opacityScale = 1.f;              // 1.1^(100-100)
+    lp->transferFunc.domain.lower = 0.f;
+    lp->transferFunc.domain.upper = 1.f;
+    exa_affine3f I;
+    std::memset(&I, 0, sizeof(I));
+    I.l.vx.x = I.l.vy.y = I.l.vz.z = 1.f;
+    lp->voxelSpaceTransform = I;
+    lp->lightSpaceTransform = I;
+    lp->ext.voxelSpaceTransformInv = I;
+    lp->ext.maxBounces = 1024;                        // deviceCode.cu:1050
+    lp->ext.albedo = -1.f;                            // :1061 (TF rgb)
+    lp->ext.hgG = 0.f;                                // :1089
+    lp->ext.cullTransparentPrims = 1;
+  });
+}
+
+int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(lp != nullptr, EXA_ERR_INVALID, "null lp");
+    need(width > 0 && height > 0, EXA_ERR_INVALID, "bad frame size");
+    need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
+    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
+         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
+         "shade mode not supported");
+    need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
+    need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
+    need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
+    need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
+         "lp.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
+    need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
+         "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
+    need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    setDevice(ctx);
+    launchRender(ctx->sampler->accel, *lp, width, height, ctx->stream);
+  });
+}
+
+} // extern "C"

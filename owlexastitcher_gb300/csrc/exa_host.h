@@ -1,0 +1,172 @@
+// exa_host.h -- C++ host side of the ExaStitch path: the reference's plugin
+// classes (model/Model.h:29-65, model/ExaStitchModel.h:26-55,
+// sampler/Sampler.h:28-69, sampler/ExaStitchSampler.h:37-106, Grid.h:33-86)
+// with the OWL handles replaced by owned device buffers.  The C ABI in
+// exastitch.h is a thin layer over these classes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/exastitch.h"
+#include "exa_accel.cuh"
+
+namespace exa {
+
+// status-carrying exception used inside the library; converted to an int
+// status at the C boundary
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void cudaCheck(cudaError_t e, const char *what);
+
+// owned device allocation
+template <typename T>
+struct DBuf {
+  T *ptr = nullptr;
+  size_t count = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : ptr(o.ptr), count(o.count) { o.ptr = nullptr; o.count = 0; }
+  DBuf &operator=(DBuf &&o) noexcept
+  {
+    if (this != &o) { release(); ptr = o.ptr; count = o.count; o.ptr = nullptr; o.count = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release()
+  {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+  void alloc(size_t n)
+  {
+    release();
+    if (n == 0) return;
+    cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      (void)cudaGetLastError();
+      throw Error(e == cudaErrorMemoryAllocation ? EXA_ERR_OOM : EXA_ERR_CUDA,
+                  std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
+    }
+    count = n;
+  }
+  void upload(const T *host, size_t n, cudaStream_t s)
+  {
+    if (n != count || !ptr) alloc(n);
+    if (n) cudaCheck(cudaMemcpyAsync(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+  }
+  size_t bytes() const { return count * sizeof(T); }
+};
+
+struct Grid {  // Grid.h:33-86
+  exa_vec3i dims{0, 0, 0};
+  exa_box3f worldBounds{};
+  DBuf<exa_range1f> valueRanges;
+  DBuf<float> maxOpacities;
+  exa_grid_traversable deviceTraversable{};
+};
+
+struct Model {  // model/Model.h:29-65
+  virtual ~Model() = default;
+  void setNumGridCells(exa_vec3i numMCs);                     // Model.cpp:25-33
+  void setVoxelSpaceTransform(exa_box3f from, exa_box3f to);  // Model.cpp:35-48
+  exa_box3f getBounds() const;                                // Model.cpp:50-70
+  std::shared_ptr<Grid> grid;
+  exa_box3f cellBounds{};
+  exa_range1f valueRange{1e30f, -1e30f};
+  exa_affine3f voxelSpaceTransform{};
+  exa_affine3f voxelSpaceTransformInv{};
+  exa_affine3f lightSpaceTransform{};
+};
+
+struct ExaStitchModel : Model {  // model/ExaStitchModel.h:26-55
+  std::vector<int32_t> indices;
+  std::vector<exa_vec4f> vertices;
+  std::vector<exa_gridlet> gridlets;
+  std::vector<float> gridletScalars;
+  size_t numScalarsTotal = 0;
+  size_t numEmptyScalars = 0;
+  // arrays in, then the loader's bounds / value-range / statistics pass
+  // (model/ExaStitchModel.cpp:78-114, 188-254)
+  void assign(const exa_vec4f *v, size_t nv, const int32_t *idx, size_t ne, const exa_gridlet *g, size_t ng,
+              const float *s, size_t ns);
+  void memStats(size_t &elemVertexBytes, size_t &elemIndexBytes, size_t &gridletBytes, size_t &emptyScalarsBytes,
+                size_t &nonEmptyScalarsBytes) const;
+};
+
+struct Sampler {  // sampler/Sampler.h:28-69
+  virtual ~Sampler() = default;
+  virtual bool build(std::shared_ptr<Model> model, cudaStream_t s) = 0;
+  virtual void computeMaxOpacities(const exa_vec4f *colorMap, int numColors, exa_range1f xfRange,
+                                   cudaStream_t s) = 0;
+  virtual void setLPs(exa_launch_params &lp) = 0;
+  virtual std::string className() = 0;
+  struct {
+    std::shared_ptr<Grid> grid;
+  } majorantAccel;
+  float *maxOpacities = nullptr;
+};
+
+class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
+ public:
+  bool build(std::shared_ptr<Model> model, cudaStream_t s) override;
+  void computeMaxOpacities(const exa_vec4f *colorMap, int numColors, exa_range1f xfRange, cudaStream_t s) override;
+  void setLPs(exa_launch_params &lp) override;
+  std::string className() override { return "ExaStitchSampler"; }
+
+  std::shared_ptr<ExaStitchModel> model;
+  // device field
+  DBuf<exa_gridlet> gridletBuffer;
+  DBuf<float> gridletScalarBuffer;
+  DBuf<float4> vertexBuffer;
+  DBuf<int32_t> indexBuffer;
+  // per-primitive ranges and opacities
+  DBuf<exa_range1f> gridletValueRanges;
+  DBuf<float> gridletMaxOpacities;
+  DBuf<exa_range1f> elemValueRanges;
+  DBuf<float> umeshMaxOpacities;
+  // point-location accel
+  std::vector<DBuf<int32_t>> tableEntries, tableItems;
+  DBuf<BvhNode> bvhNodes;
+  DBuf<int32_t> bvhParents;     // internal nodes then leaves: parent*2+slot
+  DBuf<int32_t> bvhLeafElem;    // leaf (sorted position) -> element id
+  DBuf<AccelView> deviceAccel;  // the handle stored in LP.sampler.ess.sampleBVH
+  AccelView accel{};
+  bool hasTF = false;
+  DBuf<float4> colorMap;
+
+  size_t accelBytes() const;
+
+ private:
+  void buildGridletTables(cudaStream_t s);
+  void buildElementBVH(cudaStream_t s);
+};
+
+// ---------------------------------------------------------------- kernels
+// launchers implemented in exa_build.cu / exa_render.cu
+void launchInitRanges(exa_range1f *r, size_t n, cudaStream_t s);
+void launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, exa_vec3i dims, exa_box3f wb,
+                            exa_range1f *mcRanges, exa_range1f *gridletRanges, cudaStream_t s);
+void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa_vec3i dims, exa_box3f wb,
+                         exa_range1f *mcRanges, exa_range1f *elemRanges, cudaStream_t s);
+void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf,
+                      float *out, cudaStream_t s);
+void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,
+                    int32_t *parents, int32_t *leafElem, cudaStream_t s);
+void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
+                    const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
+void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,
+                        uint32_t *errors, cudaStream_t s);
+void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, cudaStream_t s);
+
+} // namespace exa

@@ -1,0 +1,495 @@
+"""Python host binding of the ExaStitch C ABI (include/exastitch.h).
+
+Mirrors the reference's plugin interface for the path:
+  ExaStitchModel      -- model/ExaStitchModel.h:26-55 (+ Model, model/Model.h)
+  ExaStitchSampler    -- sampler/ExaStitchSampler.h:37-106 (+ Sampler)
+  LaunchParams        -- LaunchParams.h:56-119 (field order kept)
+  Renderer            -- the parts of OWLRenderer (OWLRenderer.h:30-175) that
+                         drive this path: setCamera, resize, render,
+                         setType, setColorMap, setRange, setOpacityScale,
+                         setLightSource, setShadeMode
+All compute goes through libexastitch.so; there is no Python or CPU
+fallback.  Device buffers are torch tensors (plumbing only).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native
+
+# ------------------------------------------------------------------ status
+EXA_OK = 0
+EXA_ERR_INVALID = 1
+EXA_ERR_CUDA = 2
+EXA_ERR_STATE = 3
+EXA_ERR_OOM = 4
+EXA_ERR_DEVICE_LIMIT = 5
+
+PATH_TRACING_INTEGRATOR = 0
+DIRECT_LIGHT_INTEGRATOR = 1
+RAY_MARCHING_INTEGRATOR = 2
+SHADE_MODE_DEFAULT = 0
+SHADE_MODE_GRIDLETS = 1
+LIGHT_POINT = 0
+LIGHT_DIRECTIONAL = 1
+
+
+class ExaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+# ------------------------------------------------------------------ types
+class vec2f(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float)]
+
+
+class vec3f(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+    def tolist(self):
+        return [self.x, self.y, self.z]
+
+
+class vec4f(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("w", C.c_float)]
+
+
+class vec3i(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
+
+
+class box2f(C.Structure):
+    _fields_ = [("lower", vec2f), ("upper", vec2f)]
+
+
+class box3f(C.Structure):
+    _fields_ = [("lower", vec3f), ("upper", vec3f)]
+
+
+class range1f(C.Structure):
+    _fields_ = [("lower", C.c_float), ("upper", C.c_float)]
+
+
+class linear3f(C.Structure):
+    _fields_ = [("vx", vec3f), ("vy", vec3f), ("vz", vec3f)]
+
+
+class affine3f(C.Structure):
+    _fields_ = [("l", linear3f), ("p", vec3f)]
+
+
+class Gridlet(C.Structure):
+    _fields_ = [("lower", vec3i), ("level", C.c_int32), ("dims", vec3i), ("begin", C.c_uint32)]
+
+
+class Sample(C.Structure):
+    _fields_ = [("primID", C.c_int32), ("cellID", C.c_int32), ("value", C.c_float)]
+
+
+class GridTraversable(C.Structure):
+    _fields_ = [("dims", vec3i), ("bounds", box3f)]
+
+
+class KDTreeTraversable(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("primRefs", C.c_void_p), ("modelBounds", box3f)]
+
+
+class StitchLP(C.Structure):
+    _fields_ = [("sampleBVH", C.c_uint64), ("gridletBuffer", C.c_void_p), ("gridletScalarBuffer", C.c_void_p)]
+
+
+class _SamplerUnion(C.Structure):
+    _fields_ = [("ess", StitchLP)]
+
+
+class _TF(C.Structure):
+    _fields_ = [("values", C.c_void_p), ("numValues", C.c_int32), ("domain", range1f), ("opacityScale", C.c_float)]
+
+
+class _Camera(C.Structure):
+    _fields_ = [("org", vec3f), ("dir_00", vec3f), ("dir_du", vec3f), ("dir_dv", vec3f)]
+
+
+class _SubImage(C.Structure):
+    _fields_ = [("value", box2f), ("selection", box2f), ("active", C.c_int32), ("selecting", C.c_int32)]
+
+
+class _Render(C.Structure):
+    _fields_ = [("dt", C.c_float), ("heatMapEnabled", C.c_int32), ("heatMapScale", C.c_float), ("spp", C.c_int32)]
+
+
+class _ClipPlane(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("N", vec3f), ("d", C.c_float)]
+
+
+class _Light(C.Structure):
+    _fields_ = [("pos", vec3f), ("intensity", C.c_float), ("on", C.c_int32)]
+
+
+class LPExt(C.Structure):
+    _fields_ = [
+        ("maxBounces", C.c_int32),
+        ("albedo", C.c_float),
+        ("hgG", C.c_float),
+        ("lightType", C.c_int32 * 4),
+        ("voxelSpaceTransformInv", affine3f),
+        ("cullTransparentPrims", C.c_int32),
+        ("frameID", C.c_uint32),
+        ("deviceErrors", C.c_void_p),
+        ("stepCounters", C.c_void_p),
+        ("traceT", C.c_void_p),
+        ("traceTr", C.c_void_p),
+    ]
+
+
+class LaunchParams(C.Structure):
+    """LaunchParams.h:56-119 (ExaStitch sampler, buffer transfer function)."""
+
+    _fields_ = [
+        ("sampler", _SamplerUnion),
+        ("fbPointer", C.c_void_p),
+        ("fbDepth", C.c_void_p),
+        ("accumBuffer", C.c_void_p),
+        ("accumID", C.c_int32),
+        ("integrator", C.c_int32),
+        ("shadeMode", C.c_int32),
+        ("maxOpacities", C.c_void_p),
+        ("meshBVH", C.c_uint64),
+        ("majorantBVH", C.c_uint64),
+        ("majorantKDTree", KDTreeTraversable),
+        ("majorantGrid", GridTraversable),
+        ("worldSpaceBounds", box3f),
+        ("voxelSpaceTransform", affine3f),
+        ("lightSpaceTransform", affine3f),
+        ("transferFunc", _TF),
+        ("camera", _Camera),
+        ("subImage", _SubImage),
+        ("render", _Render),
+        ("clipPlanes", _ClipPlane * 1),
+        ("lights", _Light * 4),
+        ("ext", LPExt),
+    ]
+
+
+class MemStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "elemVertexBytes", "elemIndexBytes", "gridletBytes", "emptyScalarsBytes", "nonEmptyScalarsBytes",
+        "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes")]
+
+
+GRIDLET_DTYPE = np.dtype([("lower", "<i4", 3), ("level", "<i4"), ("dims", "<i4", 3), ("begin", "<u4")])
+SAMPLE_DTYPE = np.dtype([("primID", "<i4"), ("cellID", "<i4"), ("value", "<f4")])
+
+EXPORTED = [
+    "exa_context_create", "exa_context_destroy", "exa_last_error", "exa_sync", "exa_get_device_errors",
+    "exa_version", "exa_abi_sizeof", "exa_model_create", "exa_model_get_bounds", "exa_model_set_num_grid_cells",
+    "exa_model_set_voxel_space_transform", "exa_model_get_world_bounds", "exa_model_mem_stats",
+    "exa_sampler_build", "exa_sampler_compute_max_opacities", "exa_sampler_set_lps", "exa_sampler_class_name",
+    "exa_get_majorants", "exa_get_prim_majorants", "exa_sample_points", "exa_sample_points_host",
+    "exa_launch_params_init", "exa_render",
+]
+
+_lib = None
+
+
+def lib():
+    """Loads libexastitch.so and checks the struct layouts against it."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    L = C.CDLL(_native.lib_path("libexastitch.so"))
+    vp, i32, u64 = C.c_void_p, C.c_int32, C.c_uint64
+    ctx_p = C.c_void_p
+    sig = {
+        "exa_context_create": ([C.POINTER(C.c_void_p), C.c_int, u64], C.c_int),
+        "exa_context_destroy": ([ctx_p], C.c_int),
+        "exa_last_error": ([], C.c_char_p),
+        "exa_sync": ([ctx_p], C.c_int),
+        "exa_get_device_errors": ([ctx_p, C.POINTER(C.c_uint32)], C.c_int),
+        "exa_version": ([], C.c_char_p),
+        "exa_abi_sizeof": ([i32], u64),
+        "exa_model_create": ([ctx_p, vp, u64, vp, u64, vp, u64, vp, u64], C.c_int),
+        "exa_model_get_bounds": ([ctx_p, C.POINTER(box3f), C.POINTER(range1f)], C.c_int),
+        "exa_model_set_num_grid_cells": ([ctx_p, vec3i], C.c_int),
+        "exa_model_set_voxel_space_transform": ([ctx_p, box3f, box3f], C.c_int),
+        "exa_model_get_world_bounds": ([ctx_p, C.POINTER(box3f)], C.c_int),
+        "exa_model_mem_stats": ([ctx_p, C.POINTER(MemStats)], C.c_int),
+        "exa_sampler_build": ([ctx_p], C.c_int),
+        "exa_sampler_compute_max_opacities": ([ctx_p, vp, i32, range1f], C.c_int),
+        "exa_sampler_set_lps": ([ctx_p, C.POINTER(LaunchParams)], C.c_int),
+        "exa_sampler_class_name": ([], C.c_char_p),
+        "exa_get_majorants": ([ctx_p, vp, vp], C.c_int),
+        "exa_get_prim_majorants": ([ctx_p, vp, vp, vp], C.c_int),
+        "exa_sample_points": ([ctx_p, vp, u64, vp, i32], C.c_int),
+        "exa_sample_points_host": ([ctx_p, vp, u64, vp, i32], C.c_int),
+        "exa_launch_params_init": ([C.POINTER(LaunchParams)], C.c_int),
+        "exa_render": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt)):
+        if L.exa_abi_sizeof(key) != C.sizeof(st):
+            raise RuntimeError(f"ABI layout mismatch for {st.__name__}: C {L.exa_abi_sizeof(key)} vs ctypes {C.sizeof(st)}")
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != EXA_OK:
+        raise ExaError(rc, lib().exa_last_error().decode())
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _v3(x):
+    return vec3f(float(x[0]), float(x[1]), float(x[2]))
+
+
+def _box(lo, hi):
+    return box3f(_v3(lo), _v3(hi))
+
+
+# ------------------------------------------------------------------ classes
+class Context:
+    """One device + one CUDA stream (torch's current stream by default)."""
+
+    def __init__(self, device=0, stream=None):
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream(device).cuda_stream
+        self.device = device
+        h = C.c_void_p()
+        _check(lib().exa_context_create(C.byref(h), device, int(stream)))
+        self.h = h
+
+    def sync(self):
+        _check(lib().exa_sync(self.h))
+
+    def device_errors(self):
+        b = C.c_uint32()
+        _check(lib().exa_get_device_errors(self.h, C.byref(b)))
+        return b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().exa_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ExaStitchModel:
+    """model/ExaStitchModel.h:26-55, built from in-memory arrays."""
+
+    def __init__(self, ctx, vertices, indices, gridlets, gridlet_scalars):
+        self.ctx = ctx
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1, 8)
+        self.gridlets = np.ascontiguousarray(gridlets, GRIDLET_DTYPE)
+        self.gridlet_scalars = np.ascontiguousarray(gridlet_scalars, np.float32)
+        _check(lib().exa_model_create(ctx.h, _np_ptr(self.vertices), len(self.vertices), _np_ptr(self.indices),
+                                      len(self.indices), _np_ptr(self.gridlets), len(self.gridlets),
+                                      _np_ptr(self.gridlet_scalars), len(self.gridlet_scalars)))
+
+    @classmethod
+    def from_dataset(cls, ctx, ds):
+        return cls(ctx, ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+
+    @property
+    def cellBounds(self):
+        b, r = box3f(), range1f()
+        _check(lib().exa_model_get_bounds(self.ctx.h, C.byref(b), C.byref(r)))
+        return np.array(b.lower.tolist(), np.float32), np.array(b.upper.tolist(), np.float32)
+
+    @property
+    def valueRange(self):
+        b, r = box3f(), range1f()
+        _check(lib().exa_model_get_bounds(self.ctx.h, C.byref(b), C.byref(r)))
+        return (r.lower, r.upper)
+
+    def setNumGridCells(self, dims):
+        _check(lib().exa_model_set_num_grid_cells(self.ctx.h, vec3i(*[int(d) for d in dims])))
+
+    def setVoxelSpaceTransform(self, remap_from, remap_to):
+        _check(lib().exa_model_set_voxel_space_transform(self.ctx.h, _box(*remap_from), _box(*remap_to)))
+
+    def getBounds(self):
+        b = box3f()
+        _check(lib().exa_model_get_world_bounds(self.ctx.h, C.byref(b)))
+        return np.array(b.lower.tolist(), np.float32), np.array(b.upper.tolist(), np.float32)
+
+    def memStats(self):
+        m = MemStats()
+        _check(lib().exa_model_mem_stats(self.ctx.h, C.byref(m)))
+        return {f: getattr(m, f) for f, _ in MemStats._fields_}
+
+
+class ExaStitchSampler:
+    """sampler/ExaStitchSampler.h:37-106."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.model = None
+        self.num_mcs = None
+
+    @staticmethod
+    def className():
+        return lib().exa_sampler_class_name().decode()
+
+    def build(self, model):
+        _check(lib().exa_sampler_build(self.ctx.h))
+        self.model = model
+        return True
+
+    def computeMaxOpacities(self, colorMap, xfRange):
+        cm = np.ascontiguousarray(colorMap, np.float32).reshape(-1, 4)
+        self._cmap = cm
+        _check(lib().exa_sampler_compute_max_opacities(self.ctx.h, _np_ptr(cm), len(cm), range1f(*xfRange)))
+
+    def setLPs(self, lp):
+        _check(lib().exa_sampler_set_lps(self.ctx.h, C.byref(lp)))
+
+    def majorants(self, num_mcs):
+        n = int(np.prod(num_mcs))
+        ranges = np.zeros((n, 2), np.float32)
+        ops = np.zeros(n, np.float32)
+        _check(lib().exa_get_majorants(self.ctx.h, _np_ptr(ranges), _np_ptr(ops)))
+        return ranges, ops
+
+    def prim_majorants(self):
+        ng = len(self.model.gridlets)
+        ne = len(self.model.indices)
+        gr = np.zeros((ng, 2), np.float32)
+        gop = np.zeros(ng, np.float32)
+        eop = np.zeros(ne, np.float32)
+        _check(lib().exa_get_prim_majorants(self.ctx.h, _np_ptr(gr) if ng else None, _np_ptr(gop) if ng else None,
+                                            _np_ptr(eop) if ne else None))
+        return gr, gop, eop
+
+    def sample_device(self, pos_dev, out_dev, n, cull=False):
+        """pos_dev / out_dev: device addresses (e.g. torch data_ptr())."""
+        _check(lib().exa_sample_points(self.ctx.h, pos_dev, n, out_dev, int(bool(cull))))
+
+    def sample_host(self, pos, cull=False):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        out = np.zeros(len(pos), SAMPLE_DTYPE)
+        _check(lib().exa_sample_points_host(self.ctx.h, _np_ptr(pos), len(pos), _np_ptr(out), int(bool(cull))))
+        return out
+
+
+def new_launch_params():
+    lp = LaunchParams()
+    _check(lib().exa_launch_params_init(C.byref(lp)))
+    return lp
+
+
+def camera_vectors(pos, at, up, fovy_deg, width, height):
+    """Pinhole camera in the SimpleCamera convention the renderer's
+    setCamera takes: dir = dir_00 + (x+rx)*dir_du + (y+ry)*dir_dv."""
+    pos, at, up = (np.asarray(v, np.float64) for v in (pos, at, up))
+    d = at - pos
+    d /= np.linalg.norm(d)
+    u = np.cross(d, up)
+    u /= np.linalg.norm(u)
+    v = np.cross(u, d)
+    h = 2.0 * np.tan(np.radians(fovy_deg) * 0.5)
+    aspect = width / float(height)
+    du = u * (h * aspect / width)
+    dv = v * (h / height)
+    d00 = d - 0.5 * width * du - 0.5 * height * dv
+    return pos.astype(np.float32), d00.astype(np.float32), du.astype(np.float32), dv.astype(np.float32)
+
+
+class Renderer:
+    """The OWLRenderer calls that drive this path (OWLRenderer.cpp:309-807),
+    on device buffers held as torch tensors."""
+
+    def __init__(self, ctx, model, num_mcs=(128, 128, 128)):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.model = model
+        self.num_mcs = tuple(int(d) for d in num_mcs)
+        model.setNumGridCells(self.num_mcs)
+        self.sampler = ExaStitchSampler(ctx)
+        self.sampler.build(model)
+        self.lp = new_launch_params()
+        self.sampler.setLPs(self.lp)
+        self.accumID = 0
+        self.spp = 1
+        self.fbSize = (0, 0)
+        self.absDomain = tuple(model.valueRange)
+        self.relDomain = (0.0, 100.0)
+        self.colorMap = None
+        self.fb = None
+        self.accum = None
+
+    def _xf_range(self):
+        a0, a1 = self.absDomain
+        r0, r1 = self.relDomain
+        return (np.float32(a0 + (r0 / 100.0) * (a1 - a0)), np.float32(a0 + (r1 / 100.0) * (a1 - a0)))
+
+    def setColorMap(self, cm):
+        self.colorMap = np.ascontiguousarray(cm, np.float32).reshape(-1, 4)
+        self.sampler.computeMaxOpacities(self.colorMap, self._xf_range())
+        self.sampler.setLPs(self.lp)
+        self.accumID = 0
+
+    def setRange(self, lo, hi):
+        self.absDomain = (float(lo), float(hi))
+        if self.colorMap is not None:
+            self.sampler.computeMaxOpacities(self.colorMap, self._xf_range())
+            self.sampler.setLPs(self.lp)
+
+    def setOpacityScale(self, s):
+        self.lp.transferFunc.opacityScale = float(np.power(np.float32(1.1), np.float32(s - 100)))
+
+    def setType(self, integrator):
+        self.lp.integrator = int(integrator)
+        self.accumID = 0
+
+    def setShadeMode(self, sm):
+        self.lp.shadeMode = int(sm)
+        self.accumID = 0
+
+    def setLightSource(self, i, pos, intensity, on, kind=LIGHT_POINT):
+        self.lp.lights[i].pos = _v3(pos)
+        self.lp.lights[i].intensity = float(intensity)
+        self.lp.lights[i].on = int(bool(on))
+        self.lp.ext.lightType[i] = int(kind)
+        self.accumID = 0
+
+    def setCamera(self, org, dir_00, dir_du, dir_dv):
+        c = self.lp.camera
+        c.org, c.dir_00, c.dir_du, c.dir_dv = _v3(org), _v3(dir_00), _v3(dir_du), _v3(dir_dv)
+        self.accumID = 0
+
+    def resize(self, w, h):
+        if (w, h) != self.fbSize:
+            t = self.torch
+            self.fb = t.zeros(w * h, dtype=t.int32, device=f"cuda:{self.ctx.device}")
+            self.accum = t.zeros(w * h * 4, dtype=t.float32, device=f"cuda:{self.ctx.device}")
+            self.fbSize = (w, h)
+            self.accumID = 0
+
+    def render(self, fbPointer=None):
+        """OWLRenderer::render (OWLRenderer.cpp:610-622): one frame of spp
+        samples per pixel, accumulated progressively."""
+        w, h = self.fbSize
+        self.lp.fbPointer = fbPointer if fbPointer is not None else self.fb.data_ptr()
+        self.lp.accumBuffer = self.accum.data_ptr()
+        self.lp.accumID = self.accumID
+        self.accumID += 1
+        self.lp.render.dt = 1.0
+        self.lp.render.spp = max(self.spp, 1)
+        _check(lib().exa_render(self.ctx.h, C.byref(self.lp), w, h))
