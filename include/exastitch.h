@@ -210,8 +210,10 @@ typedef struct exa_context exa_context;
 /* context                                                             */
 /* ------------------------------------------------------------------ */
 
-/* Replaces owlContextCreate(nullptr,1) (OWLRenderer.cpp:331).  stream: a
- * cudaStream_t to issue all work on, or 0 to create a private stream. */
+/* Replaces owlContextCreate(nullptr,1) (OWLRenderer.cpp:331).  stream: the
+ * cudaStream_t to issue all work on (0 is the CUDA default stream), or
+ * EXA_STREAM_PRIVATE to have the context create and own a stream. */
+#define EXA_STREAM_PRIVATE (~(uint64_t)0)
 int exa_context_create(exa_context **out, int device, uint64_t stream);
 int exa_context_destroy(exa_context *ctx);
 /* Message of the last failed call on this thread ("" if none). */

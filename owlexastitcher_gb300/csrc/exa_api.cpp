@@ -407,7 +407,7 @@ int exa_context_create(exa_context **out, int device, uint64_t stream)
     std::unique_ptr<exa_context> c(new exa_context());
     c->device = device;
     cudaCheck(cudaSetDevice(device), "cudaSetDevice");
-    if (stream) {
+    if (stream != EXA_STREAM_PRIVATE) {
       c->stream = reinterpret_cast<cudaStream_t>(stream);
     } else {
       cudaCheck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");

@@ -256,8 +256,13 @@ def _box(lo, hi):
 
 
 # ------------------------------------------------------------------ classes
+STREAM_PRIVATE = (1 << 64) - 1
+
+
 class Context:
-    """One device + one CUDA stream (torch's current stream by default)."""
+    """One device + one CUDA stream: torch's current stream by default (so
+    torch events and copies order with the library's kernels), or
+    STREAM_PRIVATE for a stream the context owns."""
 
     def __init__(self, device=0, stream=None):
         if stream is None:

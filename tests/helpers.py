@@ -91,6 +91,8 @@ def host_lp(lp, orc, width, height, accum=None):
     h.ext.traceTr = tTr.ctypes.data
     h.ext.deviceErrors = None
     h.ext.stepCounters = None
+    # the struct holds raw addresses: keep the arrays alive with it
+    h._keep = (fb, acc, tT, tTr, orc.tf, orc.max_ops)
     return h, fb, acc, tT, tTr
 
 
