@@ -343,6 +343,7 @@ struct exa_context {
   exa_range1f xfRange{0.f, 1.f};
   int numColors = 0;
   DBuf<uint32_t> errors;
+  DBuf<unsigned> jobCounter; // work counter of the persistent render kernel
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
 };
@@ -414,6 +415,7 @@ int exa_context_create(exa_context **out, int device, uint64_t stream)
       c->ownStream = true;
     }
     c->errors.alloc(1);
+    c->jobCounter.alloc(1);
     cudaCheck(cudaMemsetAsync(c->errors.ptr, 0, sizeof(uint32_t), c->stream), "memset errors");
     cudaCheck(cudaStreamSynchronize(c->stream), "sync");
     *out = c.release();
@@ -703,7 +705,7 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     setDevice(ctx);
-    launchRender(ctx->sampler->accel, *lp, width, height, ctx->stream);
+    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->stream);
   });
 }
 

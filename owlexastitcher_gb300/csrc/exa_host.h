@@ -167,6 +167,7 @@ void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode 
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,
                         uint32_t *errors, cudaStream_t s);
-void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, cudaStream_t s);
+void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
+                  cudaStream_t s);
 
 } // namespace exa

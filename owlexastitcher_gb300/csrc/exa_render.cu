@@ -6,9 +6,8 @@
 // pathTracingIntegrate (:991-1120), directLightingIntegrate (:1126-1207)
 // and renderFrame_Impl (:1268-1345).
 //
-// One thread per pixel; pixels are assigned in 8x16 tiles so that a warp's
-// rays start coherent.  The launch parameters and the accel view are kernel
-// parameters (constant bank).
+// The launch parameters and the accel view are kernel parameters (constant
+// bank).
 #include "exa_host.h"
 
 namespace exa {
@@ -16,7 +15,7 @@ namespace exa {
 constexpr int kTrackCap = 1 << 22;  // delta / ratio tracking steps per macrocell
 
 struct Counters {
-  unsigned long long fieldSamples, gridletSamples, elemSamples, ddaCells;
+  unsigned long long fieldSamples, gridletSamples, elemSamples, ddaCells, paths;
 };
 
 struct RayS {
@@ -114,112 +113,6 @@ struct PathCtx {
   bool counting;
 };
 
-// sampleInteraction (deviceCode.cu:699-854); SHADOW selects ratio tracking
-template <bool SHADOW>
-EXA_D int sample_interaction(PathCtx &c, RayS ray, V3 &posOut, float &TrOut, float4 &xf, Rng &rng, float *tHit)
-{
-  const exa_launch_params &lp = c.lp;
-  ray.org = xfm_point(lp.voxelSpaceTransform, ray.org);
-  ray.dir = xfm_vector(lp.voxelSpaceTransform, ray.dir);
-  const float dt_scale = len3(ray.dir);
-  ray.dir = norm3(ray.dir);
-  ray.tmin = ray.tmin * dt_scale;
-  ray.tmax = ray.tmax * dt_scale;
-  int type = BOUNDARY;
-  float Tr = 1.f;
-  V3 pos = mk3(0.f, 0.f, 0.f);
-  const float scale = lp.transferFunc.opacityScale;
-  const bool cull = lp.ext.cullTransparentPrims != 0;
-  const exa_grid_traversable &G = lp.majorantGrid;
-  Dda dda;
-  dda_init(dda, ray.org, ray.dir, ray.tmin, ray.tmax, G);
-  const int cellCap = G.dims.x + G.dims.y + G.dims.z + 3;
-  int ncells = 0;
-  bool done = false;
-  while (!done) {
-    if (++ncells > cellCap) { c.err |= EXA_DEVERR_DDA_CAP; break; }
-    const float t1 = fmin_t(rmin3(dda.tnext), dda.tmax);
-    const int leafID = (dda.cell.z * G.dims.y + dda.cell.y) * G.dims.x + dda.cell.x;
-    if (c.counting) c.cnt.ddaCells++;
-    const float majorant = __ldg(lp.maxOpacities + leafID);
-    float t = dda.t0;
-    int primID = -1;
-    int steps = 0;
-    while (true) {
-      if (majorant <= 0.f) break;
-      if (++steps > kTrackCap) { c.err |= EXA_DEVERR_TRACK_CAP; done = true; break; }
-      t -= __fdiv_rn(exa_log(1.f - rng.next()), majorant * scale);
-      if (t >= t1) break;
-      pos = add3(ray.org, muls(ray.dir, t));
-      exa_sample s = test_sample(c.A, pos, primID);
-      if (s.primID < 0) s = sample_field(c.A, pos, cull, c.err);
-      if (c.counting) {
-        c.cnt.fieldSamples++;
-        if (s.primID >= 0) { if (s.cellID != -1) c.cnt.gridletSamples++; else c.cnt.elemSamples++; }
-      }
-      if (s.primID < 0) continue;
-      if (s.cellID != -1) primID = s.primID;
-      xf = classify(c.A, lp, s);
-      const float sigmaT = xf.w;
-      if (!SHADOW) {
-        const float u = rng.next();
-        if (sigmaT * scale >= u * majorant) {
-          Tr = 0.f;
-          type = SCATTERING;
-          done = true;
-          if (tHit) *tHit = t;
-          break;
-        }
-      } else {
-        Tr *= 1.f - __fdiv_rn(sigmaT * scale, majorant);
-        if (Tr <= 0.f) { type = SCATTERING; done = true; break; }
-      }
-    }
-    if (done) break;
-    if (!dda_next(dda)) break;
-  }
-  posOut = xfm_point(lp.ext.voxelSpaceTransformInv, pos);
-  TrOut = Tr;
-  return type;
-}
-
-// sampleLight (deviceCode.cu:856-926); directional lights (extension) use
-// lights[i].pos as the direction towards the light, no falloff
-EXA_D V3 sample_light(PathCtx &c, V3 pos, Rng &rng, int numLights, float *trOut)
-{
-  const exa_launch_params &lp = c.lp;
-  int which = (int)(rng.next() * (float)numLights);
-  if (which == numLights) which = 0;
-  RayS ray;
-  float Tr, t00 = 1e30f, t11 = -1e30f;
-  V3 np;
-  float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
-  ray.org = pos;
-  ray.tmin = 0.f;
-  if (lp.ext.lightType[which] == EXA_LIGHT_DIRECTIONAL) {
-    ray.dir = norm3(mk3(lp.lights[which].pos));
-    ray.tmax = 1e30f;
-    box_test(ray, lp.worldSpaceBounds, t00, t11);
-    ray.tmax = t11;
-    sample_interaction<true>(c, ray, np, Tr, xf, rng, nullptr);
-    if (trOut) *trOut = Tr;
-    const float I = Tr * lp.lights[which].intensity;
-    return mk3(I, I, I);
-  }
-  V3 lightDir = sub3(mk3(lp.lights[which].pos), pos);
-  const float ld = len3(xfm_vector(lp.lightSpaceTransform, lightDir));
-  const float ldWorld = len3(lightDir);
-  lightDir = norm3(lightDir);
-  ray.dir = lightDir;
-  ray.tmax = ldWorld;
-  box_test(ray, lp.worldSpaceBounds, t00, t11);
-  ray.tmax = t11;
-  sample_interaction<true>(c, ray, np, Tr, xf, rng, nullptr);
-  if (trOut) *trOut = Tr;
-  const float I = __fdiv_rn(Tr, ld * ld) * lp.lights[which].intensity;
-  return mk3(I, I, I);
-}
-
 // make_orthonormal_basis (deviceCode.cu:144-149) + HG sampling (:965-985)
 EXA_D V3 hg_sample(V3 wo, float g, Rng &rng)
 {
@@ -244,153 +137,414 @@ EXA_D int num_lights(const exa_launch_params &lp)
   return n;
 }
 
-// pathTracingIntegrate (deviceCode.cu:991-1120)
-EXA_D float4 path_trace(PathCtx &c, RayS ray, Rng &rng, float4 bg, int numLights, float *tHit, float *trOut)
-{
-  const exa_launch_params &lp = c.lp;
-  V3 throughput = mk3(1.f, 1.f, 1.f), Ld = mk3(0.f, 0.f, 0.f);
-  unsigned bounce = 0;
-  float t0 = 1e30f, t1 = -1e30f;
-  const unsigned maxB = (unsigned)lp.ext.maxBounces;
-  if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
-    ray.org = add3(ray.org, muls(ray.dir, t0));
-    t1 -= t0;
-    while (true) {
-      float Tr;
-      V3 pos;
-      float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
-      ray.tmax = t1;
-      const int ct = sample_interaction<false>(c, ray, pos, Tr, xf, rng, bounce == 0 ? tHit : nullptr);
-      if (ct == BOUNDARY) break;
-      if (bounce++ >= maxB) {
-        throughput = mk3(0.f, 0.f, 0.f);
-        break;
-      }
-      const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
-      throughput = mul3(throughput, albedo);
-      const float P = rmax3(throughput);
-      if (P < 0.2f) {
-        if (rng.next() > P) {
-          throughput = mk3(0.f, 0.f, 0.f);
-          break;
-        }
-        throughput = div3(throughput, mk3(P, P, P));
-      }
-      throughput = add3(throughput, mk3(0.f, 0.f, 0.f));
-      if (numLights > 0) Ld = add3(Ld, mul3(throughput, sample_light(c, pos, rng, numLights, bounce == 1 ? trOut : nullptr)));
-      const V3 wo = mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z);
-      const V3 sd = hg_sample(wo, lp.ext.hgG, rng);
-      ray.org = pos;
-      ray.dir = sd;
-      box_test(ray, lp.worldSpaceBounds, t0, t1);
-    }
-  }
-  if (numLights == 0) Ld = mk3(1.f, 1.f, 1.f);
-  const V3 L = mul3(Ld, throughput);
-  return bounce ? make_float4(L.x, L.y, L.z, 1.f) : bg;
-}
-
-// directLightingIntegrate (deviceCode.cu:1126-1207)
-EXA_D float4 direct_light(PathCtx &c, RayS ray, Rng &rng, float4 bg, int numLights, float *tHit, float *trOut)
-{
-  const exa_launch_params &lp = c.lp;
-  V3 throughput = mk3(1.f, 1.f, 1.f);
-  float t0 = 1e30f, t1 = -1e30f;
-  if (!box_test(ray, lp.worldSpaceBounds, t0, t1)) return bg;
-  ray.org = add3(ray.org, muls(ray.dir, t0));
-  t1 -= t0;
-  ray.tmax = t1;
-  float Tr;
-  V3 pos;
-  float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int ct = sample_interaction<false>(c, ray, pos, Tr, xf, rng, tHit);
-  if (ct == BOUNDARY) return bg;
-  const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
-  if (numLights > 0) throughput = mul3(throughput, mul3(albedo, sample_light(c, pos, rng, numLights, trOut)));
-  else throughput = mul3(throughput, albedo);
-  return make_float4(throughput.x, throughput.y, throughput.z, 1.f);
-}
-
 EXA_D uint32_t make_8bit(float f) { return (uint32_t)imin_t(255, imax_t(0, (int)(f * 256.f))); }
 
-template <int INTEGRATOR>
-__global__ void __launch_bounds__(128) k_render(const AccelView A, const exa_launch_params lp, int width, int height)
+// ------------------------------------------------------------------------
+// sampleInteraction (deviceCode.cu:699-854) as a resumable walk: begin()
+// is the ray set-up and dda3 prologue, step() is one iteration of the
+// delta-tracking (Woodcock, :726-783) or ratio-tracking (:785-839) loop,
+// with the DDA advance (DDA.h:339-376) folded in whenever the free flight
+// leaves the current macrocell.  Executing step() until it returns false
+// performs exactly the operations of the nested reference loops.
+struct Walk {
+  V3 org, dir;      // voxel space
+  Dda dda;
+  V3 pos;           // last sample position (voxel space)
+  float4 xf;        // last classified sample
+  float t, t1, maj, Tr;
+  int primID, steps, ncells;
+  int type;
+  bool needCell;
+};
+
+EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
 {
-  // 8x16 tiles: block = 128 threads
-  const int tilesX = (width + 15) / 16;
-  const int tile = blockIdx.x;
-  const int px = (tile % tilesX) * 16 + (threadIdx.x & 15);
-  const int py = (tile / tilesX) * 8 + (threadIdx.x >> 4);
-  const bool active = px < width && py < height;
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
-  if (active) {
-    const int pixelID = px + width * py;
-    const float tb = __fdiv_rn((float)py, (float)height);
-    const float4 bg = make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
-    const int numLights = num_lights(lp);
-    Rng rng;
-    rng.init((uint32_t)pixelID, (uint32_t)lp.accumID, lp.ext.frameID);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    float tHit = -1.f, trv = -1.f;
-    for (int s = 0; s < lp.render.spp; ++s) {
-      const float rx = rng.next();
-      const float ry = rng.next();
-      const float sx = (float)px + rx, sy = (float)py + ry;
-      V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
-      dir = norm3(dir);
-      if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
-      if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
-      if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
-      RayS ray;
-      ray.org = mk3(lp.camera.org);
-      ray.dir = dir;
-      ray.tmin = 0.f;
-      ray.tmax = 1e10f;
-      float4 col;
-      if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR)
-        col = path_trace(c, ray, rng, bg, numLights, s == 0 ? &tHit : nullptr, s == 0 ? &trv : nullptr);
-      else
-        col = direct_light(c, ray, rng, bg, numLights, s == 0 ? &tHit : nullptr, s == 0 ? &trv : nullptr);
-      acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
+  ray.org = xfm_point(lp.voxelSpaceTransform, ray.org);
+  ray.dir = xfm_vector(lp.voxelSpaceTransform, ray.dir);
+  const float dt_scale = len3(ray.dir);
+  ray.dir = norm3(ray.dir);
+  ray.tmin = ray.tmin * dt_scale;
+  ray.tmax = ray.tmax * dt_scale;
+  w.org = ray.org;
+  w.dir = ray.dir;
+  dda_init(w.dda, ray.org, ray.dir, ray.tmin, ray.tmax, lp.majorantGrid);
+  w.pos = mk3(0.f, 0.f, 0.f);
+  w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+  w.Tr = 1.f;
+  w.type = BOUNDARY;
+  w.ncells = 0;
+  w.needCell = true;
+}
+
+template <bool SHADOW>
+EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng)
+{
+  const exa_launch_params &lp = c.lp;
+  const exa_grid_traversable &G = lp.majorantGrid;
+  const float scale = lp.transferFunc.opacityScale;
+  while (w.needCell) {
+    if (++w.ncells > G.dims.x + G.dims.y + G.dims.z + 3) {
+      c.err |= EXA_DEVERR_DDA_CAP;
+      return false;
     }
+    w.t1 = fmin_t(rmin3(w.dda.tnext), w.dda.tmax);
+    const int leafID = (w.dda.cell.z * G.dims.y + w.dda.cell.y) * G.dims.x + w.dda.cell.x;
+    if (c.counting) c.cnt.ddaCells++;
+    w.maj = __ldg(lp.maxOpacities + leafID);
+    w.t = w.dda.t0;
+    w.primID = -1;
+    w.steps = 0;
+    if (w.maj <= 0.f) {
+      if (!dda_next(w.dda)) return false;
+      continue;
+    }
+    w.needCell = false;
+  }
+  if (++w.steps > kTrackCap) {
+    c.err |= EXA_DEVERR_TRACK_CAP;
+    return false;
+  }
+  w.t -= __fdiv_rn(exa_log(1.f - rng.next()), w.maj * scale);
+  if (w.t >= w.t1) {
+    w.needCell = true;
+    return dda_next(w.dda);
+  }
+  w.pos = add3(w.org, muls(w.dir, w.t));
+  exa_sample s = test_sample(c.A, w.pos, w.primID);
+  if (s.primID < 0) s = sample_field(c.A, w.pos, lp.ext.cullTransparentPrims != 0, c.err);
+  if (c.counting) {
+    c.cnt.fieldSamples++;
+    if (s.primID >= 0) { if (s.cellID != -1) c.cnt.gridletSamples++; else c.cnt.elemSamples++; }
+  }
+  if (s.primID < 0) return true;
+  if (s.cellID != -1) w.primID = s.primID;
+  w.xf = classify(c.A, lp, s);
+  const float sigmaT = w.xf.w;
+  if (!SHADOW) {
+    const float u = rng.next();
+    if (sigmaT * scale >= u * w.maj) {
+      w.Tr = 0.f;
+      w.type = SCATTERING;
+      return false;
+    }
+  } else {
+    w.Tr *= 1.f - __fdiv_rn(sigmaT * scale, w.maj);
+    if (w.Tr <= 0.f) {
+      w.type = SCATTERING;
+      return false;
+    }
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------------
+// renderFrame_Impl (deviceCode.cu:1268-1345) with directLightingIntegrate
+// (:1126-1207) or pathTracingIntegrate (:991-1120) and sampleLight
+// (:856-926), as a per-lane state machine in a persistent kernel.  A lane
+// owns one pixel (all its spp samples, one RNG stream) at a time; each
+// loop iteration advances every lane by one tracking step or integrator
+// event, so lanes stay busy while their paths differ in length.  Lanes
+// that finish a pixel take the next one from a global counter
+// (one atomic per warp).  Pixels are handed out in 16x8 tiles.
+enum : int { PH_FETCH = 0, PH_TRACK = 1, PH_DONE = 2 };
+
+struct Lane {
+  // pixel
+  int px, py, pixelID, s;
+  float4 acc;
+  float tHit, trv;
+  // path
+  RayS ray;
+  V3 throughput, Ld, pos, albedo;
+  unsigned bounce;
+  float lightDen, lightI;  // point light: (Tr / lightDen) * lightI; directional: Tr * lightI
+  bool lightDirectional;
+  bool shadow;             // the running walk is a shadow walk
+  int phase;
+  Rng rng;
+  Walk w;
+};
+
+template <int INTEGRATOR>
+struct Machine {
+  PathCtx &c;
+  const exa_launch_params &lp;
+  int width, height, numLights;
+  unsigned maxB;
+
+  EXA_D float4 background(const Lane &L) const
+  {
+    const float tb = __fdiv_rn((float)L.py, (float)height);
+    return make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
+  }
+
+  EXA_D void begin_pixel(Lane &L)
+  {
+    L.pixelID = L.px + width * L.py;
+    L.rng.init((uint32_t)L.pixelID, (uint32_t)lp.accumID, lp.ext.frameID);
+    L.acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    L.tHit = -1.f;
+    L.trv = -1.f;
+    L.s = 0;
+    begin_sample(L);
+  }
+
+  EXA_D void finish_pixel(Lane &L)
+  {
+    float4 acc = L.acc;
     if (lp.accumID > 0 && lp.accumBuffer) {
-      const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
+      const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[L.pixelID];
       acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
     }
-    if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[pixelID] = acc;
+    if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[L.pixelID] = acc;
     const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
     acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
     const float is = __fdiv_rn(1.f, (float)lp.render.spp);
     const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
                           (make_8bit(acc.w * is) << 24);
-    if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
-    if (lp.ext.traceT) lp.ext.traceT[pixelID] = tHit;
-    if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = trv;
+    if (lp.fbPointer) lp.fbPointer[L.pixelID] = rgba;
+    if (lp.ext.traceT) lp.ext.traceT[L.pixelID] = L.tHit;
+    if (lp.ext.traceTr) lp.ext.traceTr[L.pixelID] = L.trv;
+    L.phase = PH_FETCH;
+  }
+
+  EXA_D void finish_sample(Lane &L, float4 col)
+  {
+    L.acc.x += col.x; L.acc.y += col.y; L.acc.z += col.z; L.acc.w += col.w;
+    if (c.counting) c.cnt.paths++;
+    if (++L.s < lp.render.spp) begin_sample(L);
+    else finish_pixel(L);
+  }
+
+  // generateRay (deviceCode.cu:88-101) and the integrator's box test
+  EXA_D void begin_sample(Lane &L)
+  {
+    const float rx = L.rng.next();
+    const float ry = L.rng.next();
+    const float sx = (float)L.px + rx, sy = (float)L.py + ry;
+    V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
+    dir = norm3(dir);
+    if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
+    if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
+    if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+    L.ray.org = mk3(lp.camera.org);
+    L.ray.dir = dir;
+    L.ray.tmin = 0.f;
+    L.ray.tmax = 1e10f;
+    L.throughput = mk3(1.f, 1.f, 1.f);
+    L.Ld = mk3(0.f, 0.f, 0.f);
+    L.bounce = 0;
+    float t0 = 1e30f, t1 = -1e30f;
+    if (!box_test(L.ray, lp.worldSpaceBounds, t0, t1)) {
+      if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) finish_path(L);
+      else finish_sample(L, background(L));
+      return;
+    }
+    L.ray.org = add3(L.ray.org, muls(L.ray.dir, t0));
+    t1 -= t0;
+    L.ray.tmax = t1;
+    L.shadow = false;
+    walk_begin(L.w, lp, L.ray);
+    L.phase = PH_TRACK;
+  }
+
+  // sampleLight prologue (deviceCode.cu:866-895): pick a light, start the
+  // shadow walk from pos (world space)
+  EXA_D void begin_light(Lane &L)
+  {
+    int which = (int)(L.rng.next() * (float)numLights);
+    if (which == numLights) which = 0;
+    RayS ray;
+    float t00 = 1e30f, t11 = -1e30f;
+    ray.org = L.pos;
+    ray.tmin = 0.f;
+    if (lp.ext.lightType[which] == EXA_LIGHT_DIRECTIONAL) {
+      ray.dir = norm3(mk3(lp.lights[which].pos));
+      ray.tmax = 1e30f;
+      box_test(ray, lp.worldSpaceBounds, t00, t11);
+      ray.tmax = t11;
+      L.lightDirectional = true;
+    } else {
+      V3 lightDir = sub3(mk3(lp.lights[which].pos), L.pos);
+      const float ld = len3(xfm_vector(lp.lightSpaceTransform, lightDir));
+      const float ldWorld = len3(lightDir);
+      lightDir = norm3(lightDir);
+      ray.dir = lightDir;
+      ray.tmax = ldWorld;
+      box_test(ray, lp.worldSpaceBounds, t00, t11);
+      ray.tmax = t11;
+      L.lightDen = ld * ld;
+      L.lightDirectional = false;
+    }
+    L.lightI = lp.lights[which].intensity;
+    L.shadow = true;
+    walk_begin(L.w, lp, ray);
+    L.phase = PH_TRACK;
+  }
+
+  EXA_D float light_result(const Lane &L) const
+  {
+    return L.lightDirectional ? L.w.Tr * L.lightI : __fdiv_rn(L.w.Tr, L.lightDen) * L.lightI;
+  }
+
+  // end of pathTracingIntegrate (deviceCode.cu:1111-1119)
+  EXA_D void finish_path(Lane &L)
+  {
+    if (numLights == 0) L.Ld = mk3(1.f, 1.f, 1.f);
+    const V3 Lr = mul3(L.Ld, L.throughput);
+    finish_sample(L, L.bounce ? make_float4(Lr.x, Lr.y, Lr.z, 1.f) : background(L));
+  }
+
+  // pathTracingIntegrate (:1092-1107): phase function, next segment
+  EXA_D void scatter(Lane &L)
+  {
+    const V3 wo = mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z);
+    const V3 sd = hg_sample(wo, lp.ext.hgG, L.rng);
+    L.ray.org = L.pos;
+    L.ray.dir = sd;
+    float t0 = 1e30f, t1 = -1e30f;
+    box_test(L.ray, lp.worldSpaceBounds, t0, t1);
+    L.ray.tmax = t1;
+    L.shadow = false;
+    walk_begin(L.w, lp, L.ray);
+  }
+
+  EXA_D void primary_done(Lane &L)
+  {
+    // first interaction of the pixel's first sample: its free-flight distance
+    if (L.s == 0 && L.bounce == 0 && L.w.type == SCATTERING) L.tHit = L.w.t;
+    L.pos = xfm_point(lp.ext.voxelSpaceTransformInv, L.w.pos);
+    const float4 xf = L.w.xf;
+    if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
+      if (L.w.type == BOUNDARY) { finish_path(L); return; }
+      if (L.bounce++ >= maxB) {
+        L.throughput = mk3(0.f, 0.f, 0.f);
+        finish_path(L);
+        return;
+      }
+      const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+      L.throughput = mul3(L.throughput, albedo);
+      const float P = rmax3(L.throughput);
+      if (P < 0.2f) {
+        if (L.rng.next() > P) {
+          L.throughput = mk3(0.f, 0.f, 0.f);
+          finish_path(L);
+          return;
+        }
+        L.throughput = div3(L.throughput, mk3(P, P, P));
+      }
+      L.throughput = add3(L.throughput, mk3(0.f, 0.f, 0.f));
+      if (numLights > 0) begin_light(L);
+      else scatter(L);
+    } else {
+      if (L.w.type == BOUNDARY) { finish_sample(L, background(L)); return; }
+      L.albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+      if (numLights > 0) {
+        begin_light(L);
+      } else {
+        const V3 tp = mul3(mk3(1.f, 1.f, 1.f), L.albedo);
+        finish_sample(L, make_float4(tp.x, tp.y, tp.z, 1.f));
+      }
+    }
+  }
+
+  EXA_D void shadow_done(Lane &L)
+  {
+    const float I = light_result(L);
+    const bool first = L.s == 0 && (INTEGRATOR != EXA_PATH_TRACING_INTEGRATOR || L.bounce == 1);
+    if (first) L.trv = L.w.Tr;
+    if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
+      L.Ld = add3(L.Ld, mul3(L.throughput, mk3(I, I, I)));
+      scatter(L);
+    } else {
+      const V3 tp = mul3(mk3(1.f, 1.f, 1.f), mul3(L.albedo, mk3(I, I, I)));
+      finish_sample(L, make_float4(tp.x, tp.y, tp.z, 1.f));
+    }
+  }
+
+  EXA_D void advance(Lane &L)
+  {
+    const bool more = L.shadow ? walk_step<true>(L.w, c, L.rng) : walk_step<false>(L.w, c, L.rng);
+    if (more) return;
+    if (L.shadow) shadow_done(L);
+    else primary_done(L);
+  }
+};
+
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128) k_render(const __grid_constant__ AccelView A,
+                                                const __grid_constant__ exa_launch_params lp, int width, int height,
+                                                unsigned *jobCounter)
+{
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces};
+  const int tilesX = (width + 15) / 16;
+  const int numJobs = tilesX * ((height + 7) / 8) * 128;
+  const unsigned lane = threadIdx.x & 31;
+  Lane L;
+  L.phase = PH_FETCH;
+  while (true) {
+    // warp-aggregated job fetch for the lanes that need a pixel
+    unsigned need = __ballot_sync(0xffffffffu, L.phase == PH_FETCH);
+    while (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(jobCounter, (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (L.phase == PH_FETCH) {
+        const unsigned job = base + __popc(need & ((1u << lane) - 1u));
+        if (job >= (unsigned)numJobs) {
+          L.phase = PH_DONE;
+        } else {
+          const int tile = (int)(job >> 7), within = (int)(job & 127);
+          L.px = (tile % tilesX) * 16 + (within & 15);
+          L.py = (tile / tilesX) * 8 + (within >> 4);
+          if (L.px < width && L.py < height) M.begin_pixel(L);
+        }
+      }
+      // lanes whose job fell outside the frame (or whose pixel finished
+      // without any tracking) fetch again
+      need = __ballot_sync(0xffffffffu, L.phase == PH_FETCH);
+    }
+    if (__all_sync(0xffffffffu, L.phase == PH_DONE)) break;
+    if (L.phase == PH_TRACK) M.advance(L);
   }
   if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
   if (c.counting) {
     unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
-                               active ? 1ull : 0ull};
+                               c.cnt.paths};
     for (int k = 0; k < 5; ++k) {
       unsigned long long x = v[k];
       for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if ((threadIdx.x & 31) == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
+      if (lane == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
     }
   }
 }
 
-void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, cudaStream_t s)
+void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
+                  cudaStream_t s)
 {
+  int dev = 0, sms = 152, perSM = 4;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
+  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &perSM, pt ? k_render<EXA_PATH_TRACING_INTEGRATOR> : k_render<EXA_DIRECT_LIGHT_INTEGRATOR>, 128, 0),
+            "occupancy");
   const int tiles = ((width + 15) / 16) * ((height + 7) / 8);
-  if (lp.integrator == EXA_PATH_TRACING_INTEGRATOR)
-    k_render<EXA_PATH_TRACING_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);
+  int blocks = sms * (perSM > 0 ? perSM : 1);
+  if (blocks > tiles) blocks = tiles;
+  cudaCheck(cudaMemsetAsync(jobCounter, 0, sizeof(unsigned), s), "reset job counter");
+  if (pt)
+    k_render<EXA_PATH_TRACING_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, jobCounter);
   else
-    k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);
+    k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, jobCounter);
   cudaCheck(cudaGetLastError(), "k_render");
 }
 
 // ------------------------------------------------------------ point query
-__global__ void __launch_bounds__(256) k_sample_points(const AccelView A, const exa_vec3f *__restrict__ pos, size_t n,
+__global__ void __launch_bounds__(256) k_sample_points(const __grid_constant__ AccelView A,
+                                                       const exa_vec3f *__restrict__ pos, size_t n,
                                                        exa_sample *out, int cull, uint32_t *errors)
 {
   uint32_t err = 0;

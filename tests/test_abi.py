@@ -1,0 +1,62 @@
+"""The C-ABI library loads on a host without a GPU, exports every function
+include/*.h declares, and its struct layouts match the Python binding."""
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(exa_[a-z0-9_]+)\s*\(", src)))
+
+
+def exported(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+    return {l.split()[-1] for l in out.splitlines() if " T " in l}
+
+
+def test_exastitch_exports_all_declared(native):
+    from owlexastitcher_gb300 import exastitch as E
+    lib = os.path.join(ROOT, "owlexastitcher_gb300", "libexastitch.so")
+    names = declared("exastitch.h")
+    assert len(names) >= 20
+    missing = [n for n in names if n not in exported(lib)]
+    assert not missing, missing
+    assert set(E.EXPORTED) <= set(names)
+    E.lib()  # loads and checks the struct layouts
+
+
+def test_generator_exports_all_declared(native):
+    lib = os.path.join(ROOT, "owlexastitcher_gb300", "libexagen.so")
+    names = declared("exastitch_gen.h")
+    missing = [n for n in names if n not in exported(lib)]
+    assert not missing, missing
+
+
+def test_abi_sizes(native):
+    from owlexastitcher_gb300 import exastitch as E
+    L = E.lib()
+    assert L.exa_abi_sizeof(0) == E.C.sizeof(E.LaunchParams)
+    assert L.exa_abi_sizeof(1) == 32 and L.exa_abi_sizeof(2) == 12
+    assert L.exa_sampler_class_name() == b"ExaStitchSampler"
+
+
+def test_launch_params_defaults(native):
+    from owlexastitcher_gb300 import exastitch as E
+    lp = E.new_launch_params()
+    assert lp.integrator == E.PATH_TRACING_INTEGRATOR and lp.render.spp == 1
+    assert lp.ext.maxBounces == 1024 and lp.ext.albedo < 0 and lp.ext.hgG == 0.0
+    assert lp.voxelSpaceTransform.l.vx.x == 1.0 and lp.transferFunc.opacityScale == 1.0
+
+
+def test_calls_without_context_fail_cleanly(native):
+    from owlexastitcher_gb300 import exastitch as E
+    L = E.lib()
+    assert L.exa_sampler_build(None) == E.EXA_ERR_STATE
+    assert b"no model" in L.exa_last_error()
+    assert L.exa_render(None, None, 1, 1) == E.EXA_ERR_STATE

@@ -1,0 +1,93 @@
+"""Known-answer tests of the oracle's interpolation and tracking: linear
+fields are reproduced by every cell type, and Woodcock tracking through a
+homogeneous medium scatters with probability 1 - exp(-sigma*d)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from golden.make_golden import SHAPES
+
+
+def lin(p):
+    return 0.3 + 0.2 * p[..., 0] - 0.1 * p[..., 1] + 0.05 * p[..., 2]
+
+
+@pytest.mark.parametrize("nv", [4, 5, 6, 8])
+def test_linear_field_elements(oracle, nv):
+    """Tets are exact to rounding; pyramids/wedges/hexes to the Newton
+    convergence tolerance of UElems.h (|delta| < 1e-4 in parametric space),
+    and Newton may give up on a point inside (the reference's behaviour)."""
+    rng = np.random.default_rng(nv)
+    misses = 0
+    for _ in range(300):
+        V = np.zeros((nv, 4), np.float32)
+        V[:, :3] = (SHAPES[nv] + rng.normal(0, 0.03, SHAPES[nv].shape)) * 2.0 + 10
+        V[:, 3] = lin(V[:, :3])
+        w = rng.dirichlet(np.ones(nv))
+        P = (w[:, None] * V[:, :3]).sum(0).astype(np.float32)   # inside the element
+        h, v = oracle.intersect_elem(P, V)
+        if not h:
+            misses += 1
+            continue
+        assert abs(v - lin(P)) < (1e-6 if nv == 4 else 1e-4)
+    assert misses <= (0 if nv == 4 else 3)
+
+
+def test_linear_field_gridlet(oracle):
+    g = np.zeros(1, oracle.GRIDLET_DTYPE)
+    g["lower"], g["level"], g["dims"], g["begin"] = (3, 4, 5), 1, (4, 3, 2), 0
+    idx = np.stack(np.meshgrid(np.arange(5), np.arange(4), np.arange(3), indexing="ij"), -1)
+    pos = ((idx + g["lower"][0]) + 0.5) * 2.0
+    sc = lin(pos).transpose(2, 1, 0).reshape(-1).astype(np.float32)  # x fastest
+    rng = np.random.default_rng(3)
+    lo, hi = (g["lower"][0] + 0.5) * 2, (g["lower"][0] + g["dims"][0] + 0.5) * 2
+    for P in rng.uniform(lo, hi, (300, 3)).astype(np.float32):
+        h, v, c = oracle.intersect_gridlet(P, g[0], sc)
+        assert h and abs(v - lin(P)) < 2e-6
+
+
+def test_homogeneous_medium_scatter_probability(oracle, native):
+    """One 8^3 gridlet of constant value; alpha = 0.05 everywhere; rays
+    along +x across the full 8-unit slab: P(scatter) = 1 - exp(-0.05*8)."""
+    from helpers import host_lp
+    from owlexastitcher_gb300 import exastitch as E
+    g = np.zeros(1, oracle.GRIDLET_DTYPE)
+    g["lower"], g["level"], g["dims"], g["begin"] = (0, 0, 0), 0, (8, 8, 8), 0
+    sc = np.full(9 ** 3, 0.5, np.float32)
+    f = oracle.Field(np.zeros((0, 4), np.float32), np.zeros((0, 8), np.int32), g, sc)
+    lo, hi, _ = f.bounds()
+    tf = np.tile(np.float32([[1, 1, 1, 0.05]]), (16, 1))
+    ranges = f.majorants((4, 4, 4), lo, hi)
+    ops = oracle.max_opacities(ranges, tf, (0.0, 1.0))
+    W, H = 64, 64
+    lp = E.LaunchParams()
+    E.lib().exa_launch_params_init(C.byref(lp))
+    lp.integrator = 1
+    lp.render.spp = 1
+    lp.transferFunc.domain.lower, lp.transferFunc.domain.upper = 0.0, 1.0
+    lp.transferFunc.numValues = 16
+    lp.majorantGrid.dims = E.vec3i(4, 4, 4)
+    lp.majorantGrid.bounds = E._box(lo, hi)
+    lp.worldSpaceBounds = E._box(lo, hi)
+    lp.ext.cullTransparentPrims = 0
+    # orthographic-like: rays start left of the slab, direction +x, one per pixel row/col
+    lp.camera.org = E._v3([-50.0, 4.5, 4.5])
+    lp.camera.dir_00 = E._v3([1.0, -1e-3 * W / 2, -1e-3 * H / 2])
+    lp.camera.dir_du = E._v3([0.0, 1e-3, 0.0])
+    lp.camera.dir_dv = E._v3([0.0, 0.0, 1e-3])
+
+    class O:
+        pass
+    o = O()
+    o.f, o.tf, o.max_ops = f, tf, ops
+    tot, n = 0, 0
+    for frame in range(20):
+        lp.accumID = frame
+        hl, fb, acc, tT, tTr = host_lp(lp, o, W, H)
+        f.render(bytes(hl), W, H)
+        tot += (tT >= 0).sum()
+        n += len(tT)
+    p = tot / n
+    expect = 1 - np.exp(-0.05 * (hi[0] - lo[0]))
+    assert abs(p - expect) < 4 * np.sqrt(expect * (1 - expect) / n)
