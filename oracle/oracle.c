@@ -117,12 +117,14 @@ void oc_sincos_turns(float u, float *s, float *c)
 }
 
 /* Counter-based stream: one key per (pixel, accumulation frame, batch
- * frame); the n-th draw is mix64(key + n*golden) >> 40 scaled by 2^-24.
- * Stands in for owl::common::LCG<4> (deviceCode.cu:41,1278). */
-void oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID)
+ * frame, sample); the n-th draw is mix64(key + n*golden) >> 40 scaled by
+ * 2^-24.  Stands in for owl::common::LCG<4> (deviceCode.cu:41,1278), whose
+ * one stream per pixel runs through all of the pixel's samples; keying by
+ * sample makes every camera sample an independent unit of work. */
+void oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID, uint32_t sampleID)
 {
-  r->key = oc_mix64(((uint64_t)pixelID << 32) ^ (uint64_t)accumID ^
-                    oc_mix64((uint64_t)frameID + 0x5851f42d4c957f2dull));
+  r->key = oc_mix64((((uint64_t)pixelID << 32) | (uint64_t)accumID) ^
+                    oc_mix64((((uint64_t)frameID << 32) | (uint64_t)sampleID) + 0x5851f42d4c957f2dull));
   r->counter = 0;
 }
 
@@ -1157,10 +1159,10 @@ static void render_pixel(rctx *c, int width, int height, int px, int py)
   const v4 bg = {(1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f};
   const int numLights = num_lights(lp);
   oc_rng rng;
-  oc_rng_init(&rng, (uint32_t)pixelID, (uint32_t)lp->accumID, lp->ext.frameID);
   v4 acc = {0.f, 0.f, 0.f, 0.f};
   float tHit = -1.f, trv = -1.f;
   for (int s = 0; s < lp->render.spp; ++s) {
+    oc_rng_init(&rng, (uint32_t)pixelID, (uint32_t)lp->accumID, lp->ext.frameID, (uint32_t)s);
     const float rx = oc_rng_next(&rng);
     const float ry = oc_rng_next(&rng);
     const float sx = (float)px + rx, sy = (float)py + ry;

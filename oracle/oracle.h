@@ -29,7 +29,7 @@ float    oc_log(float x);
 void     oc_sincos_turns(float u, float *s, float *c);
 
 typedef struct { uint64_t key; uint64_t counter; } oc_rng;
-void  oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID);
+void  oc_rng_init(oc_rng *r, uint32_t pixelID, uint32_t accumID, uint32_t frameID, uint32_t sampleID);
 float oc_rng_next(oc_rng *r);
 
 /* ---- cell / element interpolation (Gridlet.h, Plane.h, UElems.h) ---- */

@@ -57,7 +57,9 @@ def build_exastitch(verbose=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if _newer(o, [s] + hdrs):
-            cmd = [nvcc()] + ARCH + NVFLAGS + ["-x", "cu", "-c", s, "-o", o]
+            # EXA_NVCC_EXTRA: extra nvcc flags (e.g. -DEXA_RENDER_MIN_BLOCKS=3)
+            extra = os.environ.get("EXA_NVCC_EXTRA", "").split()
+            cmd = [nvcc()] + ARCH + NVFLAGS + extra + ["-x", "cu", "-c", s, "-o", o]
             if verbose:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

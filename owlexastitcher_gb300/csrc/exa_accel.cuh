@@ -110,8 +110,10 @@ EXA_D bool box_contains(const float *lo, const float *hi, V3 p)
 }
 
 // full traversal: lowest-index containing element; returns false on stack
-// overflow (error flag raised by the caller)
-EXA_D bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal)
+// overflow (error flag raised by the caller).  Out of line: element samples
+// are rare next to gridlet samples, and keeping the BVH walk and the three
+// Newton solvers out of the tracking loop keeps that loop's code small.
+static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal)
 {
   if (A.numElems <= 0) return true;
   int stack[kBvhStack];

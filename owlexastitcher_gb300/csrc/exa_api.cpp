@@ -344,6 +344,7 @@ struct exa_context {
   int numColors = 0;
   DBuf<uint32_t> errors;
   DBuf<unsigned> jobCounter; // work counter of the persistent render kernel
+  DBuf<float4> sampleColors; // one colour per camera sample of the frame
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
 };
@@ -692,6 +693,8 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
     need(lp != nullptr, EXA_ERR_INVALID, "null lp");
     need(width > 0 && height > 0, EXA_ERR_INVALID, "bad frame size");
     need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
+    need((long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp->render.spp < 0xffffffffll, EXA_ERR_INVALID,
+         "frame too large: width*height*spp must stay below 2^32 samples per launch");
     need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
          EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
     need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
@@ -705,7 +708,9 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     setDevice(ctx);
-    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->stream);
+    const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
+    if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
+    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
   });
 }
 

@@ -97,15 +97,17 @@ EXA_D void exa_sincos_turns(float u, float &s, float &c)
   else { s = -cp; c = sp; }
 }
 
-// Counter-based per-pixel stream (stands in for owl::common::LCG<4>,
-// deviceCode.cu:41,1278): key from (pixel, accumID, frameID); the n-th
-// draw is mix64(key + n*golden) >> 40 scaled by 2^-24.
+// Counter-based stream (stands in for owl::common::LCG<4>,
+// deviceCode.cu:41,1278): key from (pixel, accumID, frameID, sample); the
+// n-th draw is mix64(key + n*golden) >> 40 scaled by 2^-24.  One stream per
+// camera sample makes every (pixel, sample) an independent unit of work.
 struct Rng {
   uint64_t key;
   uint32_t counter;
-  EXA_D void init(uint32_t pixelID, uint32_t accumID, uint32_t frameID)
+  EXA_D void init(uint32_t pixelID, uint32_t accumID, uint32_t frameID, uint32_t sampleID)
   {
-    key = mix64(((uint64_t)pixelID << 32) ^ (uint64_t)accumID ^ mix64((uint64_t)frameID + 0x5851f42d4c957f2dull));
+    key = mix64((((uint64_t)pixelID << 32) | (uint64_t)accumID) ^
+                mix64((((uint64_t)frameID << 32) | (uint64_t)sampleID) + 0x5851f42d4c957f2dull));
     counter = 0;
   }
   EXA_D float next()

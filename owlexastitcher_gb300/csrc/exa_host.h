@@ -168,6 +168,6 @@ void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode 
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,
                         uint32_t *errors, cudaStream_t s);
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
-                  cudaStream_t s);
+                  float4 *colors, cudaStream_t s);
 
 } // namespace exa

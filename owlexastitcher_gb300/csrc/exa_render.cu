@@ -14,6 +14,12 @@ namespace exa {
 
 constexpr int kTrackCap = 1 << 22;  // delta / ratio tracking steps per macrocell
 
+// resident 128-thread blocks per SM the render kernel is compiled for
+// (bounds its registers: 65536 / (128 * n))
+#ifndef EXA_RENDER_MIN_BLOCKS
+#define EXA_RENDER_MIN_BLOCKS 4
+#endif
+
 struct Counters {
   unsigned long long fieldSamples, gridletSamples, elemSamples, ddaCells, paths;
 };
@@ -176,8 +182,7 @@ EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
   w.needCell = true;
 }
 
-template <bool SHADOW>
-EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng)
+EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
 {
   const exa_launch_params &lp = c.lp;
   const exa_grid_traversable &G = lp.majorantGrid;
@@ -220,7 +225,7 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng)
   if (s.cellID != -1) w.primID = s.primID;
   w.xf = classify(c.A, lp, s);
   const float sigmaT = w.xf.w;
-  if (!SHADOW) {
+  if (!shadow) {
     const float u = rng.next();
     if (sigmaT * scale >= u * w.maj) {
       w.Tr = 0.f;
@@ -240,20 +245,18 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng)
 // ------------------------------------------------------------------------
 // renderFrame_Impl (deviceCode.cu:1268-1345) with directLightingIntegrate
 // (:1126-1207) or pathTracingIntegrate (:991-1120) and sampleLight
-// (:856-926), as a per-lane state machine in a persistent kernel.  A lane
-// owns one pixel (all its spp samples, one RNG stream) at a time; each
-// loop iteration advances every lane by one tracking step or integrator
-// event, so lanes stay busy while their paths differ in length.  Lanes
-// that finish a pixel take the next one from a global counter
-// (one atomic per warp).  Pixels are handed out in 16x8 tiles.
+// (:856-926), as a per-lane state machine in a persistent kernel.  The unit
+// of work is one camera sample (pixel, s) with its own RNG stream; each loop
+// iteration advances every lane by one tracking step or integrator event,
+// and a lane that finishes its sample takes the next one from a global
+// counter (one atomic per warp).  Jobs run pixel-major (the spp samples of
+// a pixel are adjacent) over 16x8 pixel tiles.  Each sample's colour goes to
+// a scratch slot; k_resolve then sums a pixel's samples in sample order, as
+// renderFrame_Impl's spp loop does, and applies the progressive average.
 enum : int { PH_FETCH = 0, PH_TRACK = 1, PH_DONE = 2 };
 
 struct Lane {
-  // pixel
   int px, py, pixelID, s;
-  float4 acc;
-  float tHit, trv;
-  // path
   RayS ray;
   V3 throughput, Ld, pos, albedo;
   unsigned bounce;
@@ -271,6 +274,7 @@ struct Machine {
   const exa_launch_params &lp;
   int width, height, numLights;
   unsigned maxB;
+  float4 *colors;
 
   EXA_D float4 background(const Lane &L) const
   {
@@ -278,47 +282,22 @@ struct Machine {
     return make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
   }
 
-  EXA_D void begin_pixel(Lane &L)
-  {
-    L.pixelID = L.px + width * L.py;
-    L.rng.init((uint32_t)L.pixelID, (uint32_t)lp.accumID, lp.ext.frameID);
-    L.acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    L.tHit = -1.f;
-    L.trv = -1.f;
-    L.s = 0;
-    begin_sample(L);
-  }
-
-  EXA_D void finish_pixel(Lane &L)
-  {
-    float4 acc = L.acc;
-    if (lp.accumID > 0 && lp.accumBuffer) {
-      const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[L.pixelID];
-      acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
-    }
-    if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[L.pixelID] = acc;
-    const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
-    acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
-    const float is = __fdiv_rn(1.f, (float)lp.render.spp);
-    const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
-                          (make_8bit(acc.w * is) << 24);
-    if (lp.fbPointer) lp.fbPointer[L.pixelID] = rgba;
-    if (lp.ext.traceT) lp.ext.traceT[L.pixelID] = L.tHit;
-    if (lp.ext.traceTr) lp.ext.traceTr[L.pixelID] = L.trv;
-    L.phase = PH_FETCH;
-  }
-
   EXA_D void finish_sample(Lane &L, float4 col)
   {
-    L.acc.x += col.x; L.acc.y += col.y; L.acc.z += col.z; L.acc.w += col.w;
+    colors[(size_t)L.pixelID * lp.render.spp + L.s] = col;
     if (c.counting) c.cnt.paths++;
-    if (++L.s < lp.render.spp) begin_sample(L);
-    else finish_pixel(L);
+    L.phase = PH_FETCH;
   }
 
   // generateRay (deviceCode.cu:88-101) and the integrator's box test
   EXA_D void begin_sample(Lane &L)
   {
+    L.pixelID = L.px + width * L.py;
+    L.rng.init((uint32_t)L.pixelID, (uint32_t)lp.accumID, lp.ext.frameID, (uint32_t)L.s);
+    if (L.s == 0) {
+      if (lp.ext.traceT) lp.ext.traceT[L.pixelID] = -1.f;
+      if (lp.ext.traceTr) lp.ext.traceTr[L.pixelID] = -1.f;
+    }
     const float rx = L.rng.next();
     const float ry = L.rng.next();
     const float sx = (float)L.px + rx, sy = (float)L.py + ry;
@@ -382,11 +361,6 @@ struct Machine {
     L.phase = PH_TRACK;
   }
 
-  EXA_D float light_result(const Lane &L) const
-  {
-    return L.lightDirectional ? L.w.Tr * L.lightI : __fdiv_rn(L.w.Tr, L.lightDen) * L.lightI;
-  }
-
   // end of pathTracingIntegrate (deviceCode.cu:1111-1119)
   EXA_D void finish_path(Lane &L)
   {
@@ -412,7 +386,7 @@ struct Machine {
   EXA_D void primary_done(Lane &L)
   {
     // first interaction of the pixel's first sample: its free-flight distance
-    if (L.s == 0 && L.bounce == 0 && L.w.type == SCATTERING) L.tHit = L.w.t;
+    if (L.s == 0 && L.bounce == 0 && L.w.type == SCATTERING && lp.ext.traceT) lp.ext.traceT[L.pixelID] = L.w.t;
     L.pos = xfm_point(lp.ext.voxelSpaceTransformInv, L.w.pos);
     const float4 xf = L.w.xf;
     if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
@@ -450,9 +424,9 @@ struct Machine {
 
   EXA_D void shadow_done(Lane &L)
   {
-    const float I = light_result(L);
+    const float I = L.lightDirectional ? L.w.Tr * L.lightI : __fdiv_rn(L.w.Tr, L.lightDen) * L.lightI;
     const bool first = L.s == 0 && (INTEGRATOR != EXA_PATH_TRACING_INTEGRATOR || L.bounce == 1);
-    if (first) L.trv = L.w.Tr;
+    if (first && lp.ext.traceTr) lp.ext.traceTr[L.pixelID] = L.w.Tr;
     if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
       L.Ld = add3(L.Ld, mul3(L.throughput, mk3(I, I, I)));
       scatter(L);
@@ -464,27 +438,27 @@ struct Machine {
 
   EXA_D void advance(Lane &L)
   {
-    const bool more = L.shadow ? walk_step<true>(L.w, c, L.rng) : walk_step<false>(L.w, c, L.rng);
-    if (more) return;
+    if (walk_step(L.w, c, L.rng, L.shadow)) return;
     if (L.shadow) shadow_done(L);
     else primary_done(L);
   }
 };
 
 template <int INTEGRATOR>
-__global__ void __launch_bounds__(128) k_render(const __grid_constant__ AccelView A,
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render(const __grid_constant__ AccelView A,
                                                 const __grid_constant__ exa_launch_params lp, int width, int height,
-                                                unsigned *jobCounter)
+                                                unsigned *jobCounter, float4 *colors)
 {
   PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
-  Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces};
+  Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
+  const int spp = lp.render.spp;
   const int tilesX = (width + 15) / 16;
-  const int numJobs = tilesX * ((height + 7) / 8) * 128;
+  const unsigned numJobs = (unsigned)(tilesX * ((height + 7) / 8) * 128) * (unsigned)spp;
   const unsigned lane = threadIdx.x & 31;
   Lane L;
   L.phase = PH_FETCH;
   while (true) {
-    // warp-aggregated job fetch for the lanes that need a pixel
+    // warp-aggregated job fetch for the lanes that need a sample
     unsigned need = __ballot_sync(0xffffffffu, L.phase == PH_FETCH);
     while (need) {
       const int leader = __ffs(need) - 1;
@@ -493,17 +467,19 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ AccelVie
       base = __shfl_sync(0xffffffffu, base, leader);
       if (L.phase == PH_FETCH) {
         const unsigned job = base + __popc(need & ((1u << lane) - 1u));
-        if (job >= (unsigned)numJobs) {
+        if (job >= numJobs) {
           L.phase = PH_DONE;
         } else {
-          const int tile = (int)(job >> 7), within = (int)(job & 127);
+          const unsigned pj = job / (unsigned)spp;
+          L.s = (int)(job - pj * (unsigned)spp);
+          const int tile = (int)(pj >> 7), within = (int)(pj & 127);
           L.px = (tile % tilesX) * 16 + (within & 15);
           L.py = (tile / tilesX) * 8 + (within >> 4);
-          if (L.px < width && L.py < height) M.begin_pixel(L);
+          if (L.px < width && L.py < height) M.begin_sample(L);
         }
       }
-      // lanes whose job fell outside the frame (or whose pixel finished
-      // without any tracking) fetch again
+      // lanes whose job fell outside the frame, or whose sample finished
+      // without tracking, fetch again
       need = __ballot_sync(0xffffffffu, L.phase == PH_FETCH);
     }
     if (__all_sync(0xffffffffu, L.phase == PH_DONE)) break;
@@ -521,8 +497,35 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ AccelVie
   }
 }
 
+// renderFrame_Impl (deviceCode.cu:1283-1344) after the spp loop: sum the
+// pixel's samples in order, progressive accumulation, RGBA8 output
+__global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int width, int height,
+                          const float4 *__restrict__ colors)
+{
+  const int pixelID = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pixelID >= width * height) return;
+  const int spp = lp.render.spp;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 *cp = colors + (size_t)pixelID * spp;
+  for (int s = 0; s < spp; ++s) {
+    const float4 col = __ldg(cp + s);
+    acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
+  }
+  if (lp.accumID > 0 && lp.accumBuffer) {
+    const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
+    acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+  }
+  if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[pixelID] = acc;
+  const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
+  acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+  const float is = __fdiv_rn(1.f, (float)spp);
+  const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
+                        (make_8bit(acc.w * is) << 24);
+  if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
+}
+
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
-                  cudaStream_t s)
+                  float4 *colors, cudaStream_t s)
 {
   int dev = 0, sms = 152, perSM = 4;
   cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
@@ -531,15 +534,17 @@ void launchRender(const AccelView &A, const exa_launch_params &lp, int width, in
   cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &perSM, pt ? k_render<EXA_PATH_TRACING_INTEGRATOR> : k_render<EXA_DIRECT_LIGHT_INTEGRATOR>, 128, 0),
             "occupancy");
-  const int tiles = ((width + 15) / 16) * ((height + 7) / 8);
-  int blocks = sms * (perSM > 0 ? perSM : 1);
-  if (blocks > tiles) blocks = tiles;
+  const long long jobs = (long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp.render.spp;
+  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
+  if (blocks * 128 > jobs) blocks = (jobs + 127) / 128;
   cudaCheck(cudaMemsetAsync(jobCounter, 0, sizeof(unsigned), s), "reset job counter");
   if (pt)
-    k_render<EXA_PATH_TRACING_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, jobCounter);
+    k_render<EXA_PATH_TRACING_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
   else
-    k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, jobCounter);
+    k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
   cudaCheck(cudaGetLastError(), "k_render");
+  k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
+  cudaCheck(cudaGetLastError(), "k_resolve");
 }
 
 // ------------------------------------------------------------ point query
