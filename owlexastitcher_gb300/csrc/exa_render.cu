@@ -497,6 +497,228 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render(const __g
   }
 }
 
+// ------------------------------------------------------------------------
+// Nested-loop form of the same integrators (one thread runs a whole camera
+// sample, or a whole pixel, to completion): sampleInteraction as one walk
+// run to its end, then the integrator logic in program order.
+template <bool SHADOW>
+EXA_D int track(PathCtx &c, RayS ray, V3 &posOut, float &TrOut, float4 &xf, Rng &rng, float &tOut)
+{
+  Walk w;
+  walk_begin(w, c.lp, ray);
+  while (walk_step(w, c, rng, SHADOW)) {
+  }
+  posOut = xfm_point(c.lp.ext.voxelSpaceTransformInv, w.pos);
+  TrOut = w.Tr;
+  xf = w.xf;
+  tOut = w.t;
+  return w.type;
+}
+
+EXA_D V3 light_nested(PathCtx &c, V3 pos, Rng &rng, int numLights, float *trOut)
+{
+  const exa_launch_params &lp = c.lp;
+  int which = (int)(rng.next() * (float)numLights);
+  if (which == numLights) which = 0;
+  RayS ray;
+  float Tr, t00 = 1e30f, t11 = -1e30f, tt;
+  V3 np;
+  float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
+  ray.org = pos;
+  ray.tmin = 0.f;
+  if (lp.ext.lightType[which] == EXA_LIGHT_DIRECTIONAL) {
+    ray.dir = norm3(mk3(lp.lights[which].pos));
+    ray.tmax = 1e30f;
+    box_test(ray, lp.worldSpaceBounds, t00, t11);
+    ray.tmax = t11;
+    track<true>(c, ray, np, Tr, xf, rng, tt);
+    if (trOut) *trOut = Tr;
+    const float I = Tr * lp.lights[which].intensity;
+    return mk3(I, I, I);
+  }
+  V3 lightDir = sub3(mk3(lp.lights[which].pos), pos);
+  const float ld = len3(xfm_vector(lp.lightSpaceTransform, lightDir));
+  const float ldWorld = len3(lightDir);
+  lightDir = norm3(lightDir);
+  ray.dir = lightDir;
+  ray.tmax = ldWorld;
+  box_test(ray, lp.worldSpaceBounds, t00, t11);
+  ray.tmax = t11;
+  track<true>(c, ray, np, Tr, xf, rng, tt);
+  if (trOut) *trOut = Tr;
+  const float I = __fdiv_rn(Tr, ld * ld) * lp.lights[which].intensity;
+  return mk3(I, I, I);
+}
+
+template <int INTEGRATOR>
+EXA_D float4 sample_nested(PathCtx &c, int px, int py, int pixelID, int s, int height, int numLights, float *tHit,
+                           float *trv)
+{
+  const exa_launch_params &lp = c.lp;
+  Rng rng;
+  rng.init((uint32_t)pixelID, (uint32_t)lp.accumID, lp.ext.frameID, (uint32_t)s);
+  const float tb = __fdiv_rn((float)py, (float)height);
+  const float4 bg = make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
+  const float rx = rng.next();
+  const float ry = rng.next();
+  const float sx = (float)px + rx, sy = (float)py + ry;
+  V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
+  dir = norm3(dir);
+  if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
+  if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
+  if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+  RayS ray;
+  ray.org = mk3(lp.camera.org);
+  ray.dir = dir;
+  ray.tmin = 0.f;
+  ray.tmax = 1e10f;
+  float t0 = 1e30f, t1 = -1e30f, tt;
+  if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
+    V3 throughput = mk3(1.f, 1.f, 1.f), Ld = mk3(0.f, 0.f, 0.f);
+    unsigned bounce = 0;
+    const unsigned maxB = (unsigned)lp.ext.maxBounces;
+    if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
+      ray.org = add3(ray.org, muls(ray.dir, t0));
+      t1 -= t0;
+      while (true) {
+        float Tr;
+        V3 pos;
+        float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
+        ray.tmax = t1;
+        const int ct = track<false>(c, ray, pos, Tr, xf, rng, tt);
+        if (bounce == 0 && ct == SCATTERING && tHit) *tHit = tt;
+        if (ct == BOUNDARY) break;
+        if (bounce++ >= maxB) {
+          throughput = mk3(0.f, 0.f, 0.f);
+          break;
+        }
+        const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+        throughput = mul3(throughput, albedo);
+        const float P = rmax3(throughput);
+        if (P < 0.2f) {
+          if (rng.next() > P) {
+            throughput = mk3(0.f, 0.f, 0.f);
+            break;
+          }
+          throughput = div3(throughput, mk3(P, P, P));
+        }
+        throughput = add3(throughput, mk3(0.f, 0.f, 0.f));
+        if (numLights > 0)
+          Ld = add3(Ld, mul3(throughput, light_nested(c, pos, rng, numLights, bounce == 1 ? trv : nullptr)));
+        const V3 wo = mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z);
+        const V3 sd = hg_sample(wo, lp.ext.hgG, rng);
+        ray.org = pos;
+        ray.dir = sd;
+        box_test(ray, lp.worldSpaceBounds, t0, t1);
+      }
+    }
+    if (numLights == 0) Ld = mk3(1.f, 1.f, 1.f);
+    const V3 L = mul3(Ld, throughput);
+    return bounce ? make_float4(L.x, L.y, L.z, 1.f) : bg;
+  } else {
+    V3 throughput = mk3(1.f, 1.f, 1.f);
+    if (!box_test(ray, lp.worldSpaceBounds, t0, t1)) return bg;
+    ray.org = add3(ray.org, muls(ray.dir, t0));
+    t1 -= t0;
+    ray.tmax = t1;
+    float Tr;
+    V3 pos;
+    float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int ct = track<false>(c, ray, pos, Tr, xf, rng, tt);
+    if (ct == SCATTERING && tHit) *tHit = tt;
+    if (ct == BOUNDARY) return bg;
+    const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+    if (numLights > 0) throughput = mul3(throughput, mul3(albedo, light_nested(c, pos, rng, numLights, trv)));
+    else throughput = mul3(throughput, albedo);
+    return make_float4(throughput.x, throughput.y, throughput.z, 1.f);
+  }
+}
+
+// S1: one thread per pixel, the spp loop inside (renderFrame_Impl as is)
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(const __grid_constant__ AccelView A,
+                                                                             const __grid_constant__ exa_launch_params lp,
+                                                                             int width, int height)
+{
+  const int tilesX = (width + 15) / 16;
+  const int px = (blockIdx.x % tilesX) * 16 + (threadIdx.x & 15);
+  const int py = (blockIdx.x / tilesX) * 8 + (threadIdx.x >> 4);
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  if (px < width && py < height) {
+    const int pixelID = px + width * py;
+    const int numLights = num_lights(lp);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float tHit = -1.f, trv = -1.f;
+    for (int s = 0; s < lp.render.spp; ++s) {
+      const float4 col = sample_nested<INTEGRATOR>(c, px, py, pixelID, s, height, numLights, s == 0 ? &tHit : nullptr,
+                                                   s == 0 ? &trv : nullptr);
+      acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
+      if (c.counting) c.cnt.paths++;
+    }
+    if (lp.accumID > 0 && lp.accumBuffer) {
+      const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
+      acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+    }
+    if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[pixelID] = acc;
+    const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
+    acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+    const float is = __fdiv_rn(1.f, (float)lp.render.spp);
+    const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
+                          (make_8bit(acc.w * is) << 24);
+    if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
+    if (lp.ext.traceT) lp.ext.traceT[pixelID] = tHit;
+    if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = trv;
+  }
+  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
+  if (c.counting) {
+    unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
+                               c.cnt.paths};
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
+    }
+  }
+}
+
+// S2: one thread per camera sample (pixel-major), colours to scratch
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_sample(const __grid_constant__ AccelView A,
+                                                                              const __grid_constant__ exa_launch_params lp,
+                                                                              int width, int height, float4 *colors)
+{
+  const int spp = lp.render.spp;
+  const int tilesX = (width + 15) / 16;
+  const unsigned job = blockIdx.x * 128u + threadIdx.x;
+  const unsigned pj = job / (unsigned)spp;
+  const int s = (int)(job - pj * (unsigned)spp);
+  const int tile = (int)(pj >> 7), within = (int)(pj & 127);
+  const int px = (tile % tilesX) * 16 + (within & 15);
+  const int py = (tile / tilesX) * 8 + (within >> 4);
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  if (px < width && py < height) {
+    const int pixelID = px + width * py;
+    float tHit = -1.f, trv = -1.f;
+    const float4 col = sample_nested<INTEGRATOR>(c, px, py, pixelID, s, height, num_lights(lp), &tHit, &trv);
+    colors[(size_t)pixelID * spp + s] = col;
+    if (c.counting) c.cnt.paths++;
+    if (s == 0) {
+      if (lp.ext.traceT) lp.ext.traceT[pixelID] = tHit;
+      if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = trv;
+    }
+  }
+  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
+  if (c.counting) {
+    unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
+                               c.cnt.paths};
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
+    }
+  }
+}
+
 // renderFrame_Impl (deviceCode.cu:1283-1344) after the spp loop: sum the
 // pixel's samples in order, progressive accumulation, RGBA8 output
 __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int width, int height,
@@ -524,25 +746,45 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
   if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
 }
 
+// EXA_RENDER_STRATEGY: 1 thread per pixel, 2 thread per sample + resolve,
+// 3 persistent state machine + resolve
+#ifndef EXA_RENDER_STRATEGY
+#define EXA_RENDER_STRATEGY 1
+#endif
+
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
                   float4 *colors, cudaStream_t s)
 {
-  int dev = 0, sms = 152, perSM = 4;
-  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
-  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
-  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &perSM, pt ? k_render<EXA_PATH_TRACING_INTEGRATOR> : k_render<EXA_DIRECT_LIGHT_INTEGRATOR>, 128, 0),
-            "occupancy");
-  const long long jobs = (long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp.render.spp;
-  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
-  if (blocks * 128 > jobs) blocks = (jobs + 127) / 128;
-  cudaCheck(cudaMemsetAsync(jobCounter, 0, sizeof(unsigned), s), "reset job counter");
-  if (pt)
-    k_render<EXA_PATH_TRACING_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
-  else
-    k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
-  cudaCheck(cudaGetLastError(), "k_render");
+  const int tiles = ((width + 15) / 16) * ((height + 7) / 8);
+  const long long jobs = (long long)tiles * 128 * lp.render.spp;
+  if (EXA_RENDER_STRATEGY == 1) {
+    if (pt) k_render_pixel<EXA_PATH_TRACING_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);
+    else k_render_pixel<EXA_DIRECT_LIGHT_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);
+    cudaCheck(cudaGetLastError(), "k_render_pixel");
+    return;
+  }
+  if (EXA_RENDER_STRATEGY == 2) {
+    const unsigned blocks = (unsigned)((jobs + 127) / 128);
+    if (pt) k_render_sample<EXA_PATH_TRACING_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, colors);
+    else k_render_sample<EXA_DIRECT_LIGHT_INTEGRATOR><<<blocks, 128, 0, s>>>(A, lp, width, height, colors);
+    cudaCheck(cudaGetLastError(), "k_render_sample");
+  } else {
+    int dev = 0, sms = 152, perSM = 4;
+    cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &perSM, pt ? k_render<EXA_PATH_TRACING_INTEGRATOR> : k_render<EXA_DIRECT_LIGHT_INTEGRATOR>, 128, 0),
+              "occupancy");
+    long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
+    if (blocks * 128 > jobs) blocks = (jobs + 127) / 128;
+    cudaCheck(cudaMemsetAsync(jobCounter, 0, sizeof(unsigned), s), "reset job counter");
+    if (pt)
+      k_render<EXA_PATH_TRACING_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
+    else
+      k_render<EXA_DIRECT_LIGHT_INTEGRATOR><<<(unsigned)blocks, 128, 0, s>>>(A, lp, width, height, jobCounter, colors);
+    cudaCheck(cudaGetLastError(), "k_render");
+  }
   k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
   cudaCheck(cudaGetLastError(), "k_resolve");
 }
