@@ -749,7 +749,7 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
 // EXA_RENDER_STRATEGY: 1 thread per pixel, 2 thread per sample + resolve,
 // 3 persistent state machine + resolve
 #ifndef EXA_RENDER_STRATEGY
-#define EXA_RENDER_STRATEGY 1
+#define EXA_RENDER_STRATEGY 2
 #endif
 
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
