@@ -41,6 +41,18 @@ struct BvhNode {   // 64 B: two child boxes, two child refs, two opacities
   float op[2];          // max opacity of each child subtree
 };
 
+// Conservative element occupancy: one bit per cell of a uniform grid over
+// the elements' bounds, set where any element's closed AABB touches the
+// cell.  cell(p) = floor((p - origin) / cellSize) is monotonic in p, so a
+// point inside an element's AABB always maps to a marked cell; a clear bit
+// proves no element contains the point.
+struct ElemOccupancy {
+  float origin[3];
+  float cellSize[3];
+  int n[3];
+  const uint32_t *bits;
+};
+
 struct AccelView {
   const exa_gridlet *gridlets;
   const float *scalars;
@@ -53,8 +65,26 @@ struct AccelView {
   int numElems;
   int numTables;
   int tablesSorted;             // 1: tables in ascending gridlet-index order
+  ElemOccupancy occ;
   GridletTable tables[kMaxLevels];
 };
+
+EXA_HD int occ_coord(float p, float origin, float cs, int n)
+{
+  const float f = floorf((p - origin) / cs);
+  return f < 0.f ? -1 : (f >= (float)n ? n : (int)f);
+}
+
+// false: no element's AABB contains pos
+EXA_D bool occ_maybe(const ElemOccupancy &O, V3 pos)
+{
+  const int x = occ_coord(pos.x, O.origin[0], O.cellSize[0], O.n[0]);
+  const int y = occ_coord(pos.y, O.origin[1], O.cellSize[1], O.n[1]);
+  const int z = occ_coord(pos.z, O.origin[2], O.cellSize[2], O.n[2]);
+  if (x < 0 || y < 0 || z < 0 || x >= O.n[0] || y >= O.n[1] || z >= O.n[2]) return false;
+  const size_t c = ((size_t)z * O.n[1] + y) * O.n[0] + x;
+  return (__ldg(O.bits + (c >> 5)) >> (c & 31)) & 1u;
+}
 
 EXA_D int floor_div_pow2(int v, int shift) { return v >> shift; }  // arithmetic shift floors
 
@@ -181,7 +211,7 @@ EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &e
   }
   int be = 0x7fffffff;
   float ev = 0.f;
-  if (!query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
+  if (A.numElems > 0 && occ_maybe(A.occ, pos) && !query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
   if (be != 0x7fffffff) {
     s.primID = be;
     s.cellID = -1;

@@ -144,7 +144,7 @@ void ExaStitchModel::memStats(size_t &elemVertexBytes, size_t &elemIndexBytes, s
 // ================================================================ sampler
 size_t ExaStitchSampler::accelBytes() const
 {
-  size_t b = bvhNodes.bytes() + bvhParents.bytes() + bvhLeafElem.bytes();
+  size_t b = bvhNodes.bytes() + bvhParents.bytes() + bvhLeafElem.bytes() + occBits.bytes();
   for (auto &t : tableEntries) b += t.bytes();
   for (auto &t : tableItems) b += t.bytes();
   return b;
@@ -247,6 +247,28 @@ void ExaStitchSampler::buildElementBVH(cudaStream_t s)
   }
   launchBuildBVH(vertexBuffer.ptr, indexBuffer.ptr, ne, sb, bvhNodes.ptr, bvhParents.ptr, bvhLeafElem.ptr, s);
   accel.nodes = bvhNodes.ptr;
+  // occupancy grid: about 2 finest-cell widths per cell, at most 2^27 cells
+  ElemOccupancy &O = accel.occ;
+  const float ext[3] = {sb.upper.x - sb.lower.x, sb.upper.y - sb.lower.y, sb.upper.z - sb.lower.z};
+  const float org[3] = {sb.lower.x, sb.lower.y, sb.lower.z};
+  float cs = 2.f;
+  auto cells = [&](float c) {
+    double t = 1;
+    for (int a = 0; a < 3; ++a) t *= std::max(1.0, std::ceil((double)ext[a] / c) + 1);
+    return t;
+  };
+  while (cells(cs) > (double)(1 << 27)) cs *= 2.f;
+  size_t nc = 1;
+  for (int a = 0; a < 3; ++a) {
+    O.origin[a] = org[a];
+    O.cellSize[a] = cs;
+    O.n[a] = (int)std::max(1.0, std::ceil((double)ext[a] / cs) + 1);
+    nc *= (size_t)O.n[a];
+  }
+  const size_t words = (nc + 31) / 32;
+  occBits.alloc(words);
+  launchElemOccupancy(vertexBuffer.ptr, indexBuffer.ptr, ne, O, occBits.ptr, words, s);
+  O.bits = occBits.ptr;
 }
 
 // sampler/ExaStitchSampler.cpp:23-340

@@ -352,6 +352,38 @@ __global__ void k_bvh_refit(const float4 *verts, const int32_t *indices, int n, 
   }
 }
 
+// element occupancy bitmap: mark every cell an element's closed AABB
+// touches (same monotonic cell mapping as the query)
+__global__ void k_elem_occupancy(const float4 *verts, const int32_t *indices, size_t ne, ElemOccupancy O,
+                                 uint32_t *bits)
+{
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  V3 lo, hi;
+  elem_box(verts, indices, e, lo, hi);
+  const int x0 = imax_t(0, occ_coord(lo.x, O.origin[0], O.cellSize[0], O.n[0]));
+  const int y0 = imax_t(0, occ_coord(lo.y, O.origin[1], O.cellSize[1], O.n[1]));
+  const int z0 = imax_t(0, occ_coord(lo.z, O.origin[2], O.cellSize[2], O.n[2]));
+  const int x1 = imin_t(O.n[0] - 1, occ_coord(hi.x, O.origin[0], O.cellSize[0], O.n[0]));
+  const int y1 = imin_t(O.n[1] - 1, occ_coord(hi.y, O.origin[1], O.cellSize[1], O.n[1]));
+  const int z1 = imin_t(O.n[2] - 1, occ_coord(hi.z, O.origin[2], O.cellSize[2], O.n[2]));
+  for (int z = z0; z <= z1; ++z)
+    for (int y = y0; y <= y1; ++y)
+      for (int x = x0; x <= x1; ++x) {
+        const size_t c = ((size_t)z * O.n[1] + y) * O.n[0] + x;
+        atomicOr(bits + (c >> 5), 1u << (c & 31));
+      }
+}
+
+void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, const ElemOccupancy &O, uint32_t *bits,
+                         size_t words, cudaStream_t s)
+{
+  cudaCheck(cudaMemsetAsync(bits, 0, words * sizeof(uint32_t), s), "memset occupancy");
+  if (!ne) return;
+  k_elem_occupancy<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, ne, O, bits);
+  cudaCheck(cudaGetLastError(), "k_elem_occupancy");
+}
+
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sb, BvhNode *nodes,
                     int32_t *parents, int32_t *leafElem, cudaStream_t s)
 {

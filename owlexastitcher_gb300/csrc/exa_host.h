@@ -140,6 +140,7 @@ class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
   DBuf<BvhNode> bvhNodes;
   DBuf<int32_t> bvhParents;     // internal nodes then leaves: parent*2+slot
   DBuf<int32_t> bvhLeafElem;    // leaf (sorted position) -> element id
+  DBuf<uint32_t> occBits;       // element occupancy bitmap
   DBuf<AccelView> deviceAccel;  // the handle stored in LP.sampler.ess.sampleBVH
   AccelView accel{};
   bool hasTF = false;
@@ -163,6 +164,8 @@ void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, i
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,
                     int32_t *parents, int32_t *leafElem, cudaStream_t s);
+void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, const ElemOccupancy &O, uint32_t *bits,
+                         size_t words, cudaStream_t s);
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,

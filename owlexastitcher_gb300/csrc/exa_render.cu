@@ -501,18 +501,37 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render(const __g
 // Nested-loop form of the same integrators (one thread runs a whole camera
 // sample, or a whole pixel, to completion): sampleInteraction as one walk
 // run to its end, then the integrator logic in program order.
-template <bool SHADOW>
-EXA_D int track(PathCtx &c, RayS ray, V3 &posOut, float &TrOut, float4 &xf, Rng &rng, float &tOut)
+// EXA_TRACK_NOINLINE 1: one out-of-line copy of the walk, shared by primary
+// and shadow rays (smaller code); 0: inlined at both call sites
+#ifndef EXA_TRACK_NOINLINE
+#define EXA_TRACK_NOINLINE 1
+#endif
+#if EXA_TRACK_NOINLINE
+#define EXA_TRACK_ATTR static __device__ __noinline__
+#else
+#define EXA_TRACK_ATTR EXA_D
+#endif
+
+EXA_TRACK_ATTR int track_walk(PathCtx &c, RayS ray, const bool shadow, Rng &rngRef, V3 &posOut, float &TrOut,
+                              float4 &xf, float &tOut)
 {
+  Rng rng = rngRef;
   Walk w;
   walk_begin(w, c.lp, ray);
-  while (walk_step(w, c, rng, SHADOW)) {
+  while (walk_step(w, c, rng, shadow)) {
   }
+  rngRef = rng;
   posOut = xfm_point(c.lp.ext.voxelSpaceTransformInv, w.pos);
   TrOut = w.Tr;
   xf = w.xf;
   tOut = w.t;
   return w.type;
+}
+
+template <bool SHADOW>
+EXA_D int track(PathCtx &c, RayS ray, V3 &posOut, float &TrOut, float4 &xf, Rng &rng, float &tOut)
+{
+  return track_walk(c, ray, SHADOW, rng, posOut, TrOut, xf, tOut);
 }
 
 EXA_D V3 light_nested(PathCtx &c, V3 pos, Rng &rng, int numLights, float *trOut)
