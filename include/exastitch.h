@@ -321,6 +321,34 @@ int exa_launch_params_init(exa_launch_params *lp);
 int exa_render(exa_context *ctx, const exa_launch_params *lp,
                int32_t width, int32_t height);
 
+/* ------------------------------------------------------------------ */
+/* allocation-free rendering                                           */
+/* ------------------------------------------------------------------ */
+
+/* Largest width * height * spp one exa_render_noalloc call accepts. */
+#define EXA_NOALLOC_MAX_SAMPLES (1u << 20)
+
+/* The same frame as exa_render, for callers that must not allocate device
+ * memory in their frame loop: exa_render allocates its per-sample colour
+ * buffer with cudaMalloc the first time it sees a frame size, and cudaMalloc
+ * synchronizes the device (stalling a pipelined render loop) and fails in
+ * hosts that have handed all device memory to their own pool.  This entry
+ * point calls no cudaMalloc, cudaFree or other allocating routine; its
+ * scratch is a fixed 16 MiB array in the library's device image
+ * (EXA_NOALLOC_MAX_SAMPLES float4 sample colours), which every GPU that
+ * loads the library holds until the process exits.  Frames with
+ * width * height * lp->render.spp above EXA_NOALLOC_MAX_SAMPLES are
+ * rejected with EXA_ERR_INVALID.
+ * The first call on a device looks up that array's device address (and,
+ * with lazy module loading, loads the module): make the first call before
+ * any stream capture.  All calls share the one array; calls whose kernels
+ * overlap on the GPU (e.g. from two contexts on different streams) race on
+ * it.  Every sample slot a frame reads is written by the same frame, so
+ * nothing has to be cleared between calls.
+ * This entry point has no counterpart in the reference. */
+int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
+                       int32_t width, int32_t height);
+
 #ifdef __cplusplus
 }
 #endif

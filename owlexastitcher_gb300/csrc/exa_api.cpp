@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 
 #include "exa_host.h"
@@ -737,3 +738,55 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
 }
 
 } // extern "C"
+
+// ================================================================ no-alloc
+// Scratch of exa_render_noalloc: one colour per camera sample, in the
+// library's device image instead of a cudaMalloc'd buffer.  The host-side
+// name is a stand-in for the symbol; kernels get the device address that
+// cudaGetSymbolAddress returns (looked up once per device).
+static __device__ __align__(256) float4 g_noallocSampleColors[EXA_NOALLOC_MAX_SAMPLES];
+
+namespace {
+std::mutex g_noallocMutex;
+float4 *g_noallocAddr[256] = {};
+}
+
+extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(lp != nullptr, EXA_ERR_INVALID, "null lp");
+    need(width > 0 && height > 0, EXA_ERR_INVALID, "bad frame size");
+    need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
+    const unsigned long long samples = (unsigned long long)width * (unsigned long long)height * (unsigned)lp->render.spp;
+    if (samples > EXA_NOALLOC_MAX_SAMPLES)
+      throw Error(EXA_ERR_INVALID, "exa_render_noalloc: width*height*spp = " + std::to_string(samples) +
+                                       " exceeds its static scratch of " + std::to_string(EXA_NOALLOC_MAX_SAMPLES) +
+                                       " samples; use exa_render for larger frames");
+    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
+         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
+         "shade mode not supported");
+    need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
+    need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
+    need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
+    need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
+         "lp.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
+    need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
+         "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
+    need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    need(ctx->device >= 0 && ctx->device < 256, EXA_ERR_INVALID, "device index out of range");
+    setDevice(ctx);
+    float4 *scratch = nullptr;
+    {
+      std::lock_guard<std::mutex> lock(g_noallocMutex);
+      if (!g_noallocAddr[ctx->device]) {
+        void *p = nullptr;
+        cudaCheck(cudaGetSymbolAddress(&p, g_noallocSampleColors), "cudaGetSymbolAddress(noalloc scratch)");
+        g_noallocAddr[ctx->device] = static_cast<float4 *>(p);
+      }
+      scratch = g_noallocAddr[ctx->device];
+    }
+    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, scratch, ctx->stream);
+  });
+}

@@ -188,8 +188,9 @@ EXPORTED = [
     "exa_model_set_voxel_space_transform", "exa_model_get_world_bounds", "exa_model_mem_stats",
     "exa_sampler_build", "exa_sampler_compute_max_opacities", "exa_sampler_set_lps", "exa_sampler_class_name",
     "exa_get_majorants", "exa_get_prim_majorants", "exa_sample_points", "exa_sample_points_host",
-    "exa_launch_params_init", "exa_render",
+    "exa_launch_params_init", "exa_render", "exa_render_noalloc",
 ]
+NOALLOC_MAX_SAMPLES = 1 << 20
 
 _lib = None
 
@@ -226,6 +227,7 @@ def lib():
         "exa_sample_points_host": ([ctx_p, vp, u64, vp, i32], C.c_int),
         "exa_launch_params_init": ([C.POINTER(LaunchParams)], C.c_int),
         "exa_render": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
+        "exa_render_noalloc": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
