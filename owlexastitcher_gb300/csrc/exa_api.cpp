@@ -368,6 +368,9 @@ struct exa_context {
   DBuf<uint32_t> errors;
   DBuf<unsigned> jobCounter; // work counter of the persistent render kernel
   DBuf<float4> sampleColors; // one colour per camera sample of the frame
+  DBuf<uint32_t> wfRecords;  // wavefront path records: 3 queues x 60 words x capacity
+  DBuf<unsigned> wfCounters; // wavefront queue sizes
+  unsigned wfCap = 0;
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
 };
@@ -733,7 +736,20 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
     setDevice(ctx);
     const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
     if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
-    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
+    if (useWavefront()) {
+      // queue capacity: the frame's samples, at most 4M records in flight
+      const unsigned cap = (unsigned)std::min<size_t>((size_t)((width + 15) / 16) * ((height + 7) / 8) * 128 *
+                                                          (size_t)lp->render.spp, (size_t)1 << 22);
+      if (ctx->wfCap < cap) {
+        ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
+        ctx->wfCounters.alloc(3);
+        ctx->wfCap = cap;
+      }
+      renderWavefront(ctx->sampler->accel, *lp, width, height, ctx->sampleColors.ptr, ctx->wfRecords.ptr, ctx->wfCap,
+                      ctx->wfCounters.ptr, ctx->stream);
+    } else {
+      launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
+    }
   });
 }
 

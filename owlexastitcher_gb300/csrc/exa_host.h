@@ -168,6 +168,11 @@ void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, con
                          size_t words, cudaStream_t s);
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
+// wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 3 words
+void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s);
+bool useWavefront();
+constexpr int kWfLaneWords = 61;
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,
                         uint32_t *errors, cudaStream_t s);
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,

@@ -8,6 +8,8 @@
 //
 // The launch parameters and the accel view are kernel parameters (constant
 // bank).
+#include <algorithm>
+
 #include "exa_host.h"
 
 namespace exa {
@@ -765,11 +767,295 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
   if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
 }
 
-// EXA_RENDER_STRATEGY: 1 thread per pixel, 2 thread per sample + resolve,
-// 3 persistent state machine + resolve
+// ------------------------------------------------------------------------
+// Wavefront form: path records in structure-of-arrays buffers (word k of
+// record i at buf[k * cap + i], so a warp's loads and stores coalesce).  A
+// walk kernel advances each queued walk by at most K tracking steps and
+// compacts the records into a continue queue and an event queue with
+// warp-aggregated appends (ballot, popc, one atomic per warp, shuffle of the
+// base); an event kernel applies the integrator step that follows a walk
+// (sampleLight, Russian roulette, HG scatter, sample end) and queues the next
+// walk; a camera kernel refills the free capacity with new camera samples.
+// Each path runs the same operations in the same order as in the nested
+// form, so the result is bit-identical; only the interleaving of paths
+// differs.
+// record = path part (words [0, kPathWords)) + walk part; the walk kernel
+// only touches the walk part and copies the path part through
+constexpr int kPathWords = 26;
+constexpr int kWalkWords = 35;
+constexpr int kLaneWords = kPathWords + kWalkWords;
+static_assert(kLaneWords == kWfLaneWords, "record size");
+
+struct WfQueues {
+  uint32_t *in, *out, *ev;  // record buffers (kLaneWords * cap words each)
+  unsigned *cnt;            // [0] in, [1] out, [2] ev
+  unsigned cap;
+};
+
+#define W(v) b[(size_t)(k++) * cap + i] = (v)
+#define WF(v) W(__float_as_uint(v))
+#define R() __ldg(b + (size_t)(k++) * cap + i)
+#define RF() __uint_as_float(R())
+
+EXA_D void wf_store_path(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
+{
+  unsigned k = 0;
+  W((uint32_t)L.px); W((uint32_t)L.py); W((uint32_t)L.s);
+  WF(L.ray.org.x); WF(L.ray.org.y); WF(L.ray.org.z); WF(L.ray.dir.x); WF(L.ray.dir.y); WF(L.ray.dir.z); WF(L.ray.tmax);
+  WF(L.throughput.x); WF(L.throughput.y); WF(L.throughput.z); WF(L.Ld.x); WF(L.Ld.y); WF(L.Ld.z);
+  WF(L.pos.x); WF(L.pos.y); WF(L.pos.z); WF(L.albedo.x); WF(L.albedo.y); WF(L.albedo.z);
+  W(L.bounce); WF(L.lightDen); WF(L.lightI); W((uint32_t)L.lightDirectional);
+}
+
+EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width)
+{
+  unsigned k = 0;
+  L.px = (int)R(); L.py = (int)R(); L.s = (int)R();
+  L.pixelID = L.px + width * L.py;
+  L.ray.org.x = RF(); L.ray.org.y = RF(); L.ray.org.z = RF();
+  L.ray.dir.x = RF(); L.ray.dir.y = RF(); L.ray.dir.z = RF(); L.ray.tmax = RF(); L.ray.tmin = 0.f;
+  L.throughput.x = RF(); L.throughput.y = RF(); L.throughput.z = RF();
+  L.Ld.x = RF(); L.Ld.y = RF(); L.Ld.z = RF();
+  L.pos.x = RF(); L.pos.y = RF(); L.pos.z = RF();
+  L.albedo.x = RF(); L.albedo.y = RF(); L.albedo.z = RF();
+  L.bounce = R(); L.lightDen = RF(); L.lightI = RF(); L.lightDirectional = R() != 0u;
+}
+
+// shadow flag, RNG and the walk
+EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
+{
+  unsigned k = kPathWords;
+  const Walk &w = L.w;
+  W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2));
+  W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
+  WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
+  WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
+  W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
+  WF(w.pos.x); WF(w.pos.y); WF(w.pos.z); WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
+  WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
+  W((uint32_t)w.primID); W((uint32_t)w.steps); W((uint32_t)w.ncells);
+}
+
+EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i,
+                        const exa_grid_traversable &G)
+{
+  unsigned k = kPathWords;
+  Walk &w = L.w;
+  const uint32_t flags = R();
+  L.shadow = flags & 1u;
+  w.needCell = (flags >> 1) & 1u;
+  w.type = (int)(flags >> 2);
+  const uint32_t lo = R(), hi = R();
+  L.rng.key = ((uint64_t)hi << 32) | lo;
+  L.rng.counter = R();
+  w.org.x = RF(); w.org.y = RF(); w.org.z = RF(); w.dir.x = RF(); w.dir.y = RF(); w.dir.z = RF();
+  w.dda.tnext.x = RF(); w.dda.tnext.y = RF(); w.dda.tnext.z = RF();
+  w.dda.dist.x = RF(); w.dda.dist.y = RF(); w.dda.dist.z = RF();
+  w.dda.cell.x = (int)R(); w.dda.cell.y = (int)R(); w.dda.cell.z = (int)R();
+  w.dda.t0 = RF(); w.dda.tmax = RF();
+  // step / stop follow from the ray direction as in dda_init
+  w.dda.step.x = w.dir.x > 0.f ? 1 : -1; w.dda.step.y = w.dir.y > 0.f ? 1 : -1; w.dda.step.z = w.dir.z > 0.f ? 1 : -1;
+  w.dda.stop.x = w.dir.x > 0.f ? G.dims.x : -1; w.dda.stop.y = w.dir.y > 0.f ? G.dims.y : -1;
+  w.dda.stop.z = w.dir.z > 0.f ? G.dims.z : -1;
+  w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
+  w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
+  w.t = RF(); w.t1 = RF(); w.maj = RF(); w.Tr = RF();
+  w.primID = (int)R(); w.steps = (int)R(); w.ncells = (int)R();
+}
+
+#undef W
+#undef WF
+#undef R
+#undef RF
+
+EXA_D void wf_store(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
+{
+  wf_store_path(L, b, cap, i);
+  wf_store_walk(L, b, cap, i);
+}
+
+EXA_D void wf_load(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width,
+                   const exa_grid_traversable &G)
+{
+  wf_load_path(L, b, cap, i, width);
+  wf_load_walk(L, b, cap, i, G);
+}
+
+EXA_D void wf_copy_path(const uint32_t *__restrict__ src, unsigned i, uint32_t *dst, unsigned j, unsigned cap)
+{
+#pragma unroll
+  for (int k = 0; k < kPathWords; ++k) dst[(size_t)k * cap + j] = __ldg(src + (size_t)k * cap + i);
+}
+
+// warp-aggregated append: returns this lane's slot (valid where pred)
+EXA_D unsigned warp_append(unsigned *counter, bool pred)
+{
+  const unsigned mask = __activemask();
+  const unsigned ballot = __ballot_sync(mask, pred);
+  const unsigned lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned base = 0;
+  if ((int)lane == leader && ballot) base = atomicAdd(counter, (unsigned)__popc(ballot));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(ballot & ((1u << lane) - 1u));
+}
+
+EXA_D void flush_counters(PathCtx &c, const exa_launch_params &lp)
+{
+  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
+  if (c.counting) {
+    const unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
+                                     c.cnt.paths};
+    for (int k = 0; k < 5; ++k)
+      if (v[k]) atomicAdd(lp.ext.stepCounters + k, v[k]);
+  }
+}
+
+// camera: samples [first, first + n) of the frame's job order; those that
+// start a walk are appended to the input queue
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ AccelView A,
+                                                   const __grid_constant__ exa_launch_params lp, int width, int height,
+                                                   float4 *colors, WfQueues Q, unsigned first, unsigned n)
+{
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
+  const int spp = lp.render.spp;
+  const int tilesX = (width + 15) / 16;
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + threadIdx.x;
+    Lane L;
+    bool tracking = false;
+    if (i < n) {
+      const unsigned job = first + i;
+      const unsigned pj = job / (unsigned)spp;
+      L.s = (int)(job - pj * (unsigned)spp);
+      const int tile = (int)(pj >> 7), within = (int)(pj & 127);
+      L.px = (tile % tilesX) * 16 + (within & 15);
+      L.py = (tile / tilesX) * 8 + (within >> 4);
+      if (L.px < width && L.py < height) {
+        M.begin_sample(L);
+        tracking = L.phase == PH_TRACK;
+      }
+    }
+    const unsigned slot = warp_append(&Q.cnt[0], tracking);
+    if (tracking) wf_store(L, Q.in, Q.cap, slot);
+  }
+  flush_counters(c, lp);
+}
+
+// walks: at most K tracking steps each, then compaction
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __grid_constant__ AccelView A,
+                                                 const __grid_constant__ exa_launch_params lp, int width, WfQueues Q,
+                                                 int K)
+{
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  const unsigned n = Q.cnt[0];
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + threadIdx.x;
+    Lane L;
+    bool more = false, ended = false;
+    if (i < n) {
+      wf_load_walk(L, Q.in, Q.cap, i, lp.majorantGrid);
+      more = true;
+      for (int k = 0; k < K && more; ++k) more = walk_step(L.w, c, L.rng, L.shadow);
+      ended = !more;
+    }
+    const unsigned so = warp_append(&Q.cnt[1], more);
+    if (more) { wf_store_walk(L, Q.out, Q.cap, so); wf_copy_path(Q.in, i, Q.out, so, Q.cap); }
+    const unsigned se = warp_append(&Q.cnt[2], ended);
+    if (ended) { wf_store_walk(L, Q.ev, Q.cap, se); wf_copy_path(Q.in, i, Q.ev, se, Q.cap); }
+  }
+  flush_counters(c, lp);
+}
+
+// walk ends: the integrator step after a primary or shadow walk
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ AccelView A,
+                                                   const __grid_constant__ exa_launch_params lp, int width, int height,
+                                                   float4 *colors, WfQueues Q)
+{
+  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
+  const unsigned n = Q.cnt[2];
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + threadIdx.x;
+    Lane L;
+    bool tracking = false;
+    if (i < n) {
+      wf_load(L, Q.ev, Q.cap, i, width, lp.majorantGrid);
+      L.phase = PH_TRACK;
+      if (L.shadow) M.shadow_done(L);
+      else M.primary_done(L);
+      tracking = L.phase == PH_TRACK;
+    }
+    const unsigned slot = warp_append(&Q.cnt[1], tracking);
+    if (tracking) wf_store(L, Q.out, Q.cap, slot);
+  }
+  flush_counters(c, lp);
+}
+
+#ifndef EXA_WF_STEPS
+#define EXA_WF_STEPS 8
+#endif
+
+// host loop of the wavefront renderer; synchronizes the stream once per
+// round to read the queue sizes
+void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s)
+{
+  const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const unsigned long long total = (unsigned long long)((width + 15) / 16) * ((height + 7) / 8) * 128ull * lp.render.spp;
+  const size_t words = (size_t)kLaneWords * cap;
+  uint32_t *buf[3] = {bufs, bufs + words, bufs + 2 * words};
+  unsigned long long issued = 0;
+  unsigned nIn = 0;
+  int inIdx = 0, outIdx = 1;
+  const unsigned grid = (unsigned)sms * 16;
+  cudaCheck(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned), s), "reset queues");
+  for (int round = 0; round < (1 << 24); ++round) {
+    WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap};
+    const unsigned nNew = (unsigned)std::min<unsigned long long>(cap - nIn, total - issued);
+    if (nNew) {
+      const unsigned g = std::min<unsigned>(grid, (nNew + 127) / 128);
+      if (pt) k_wf_camera<EXA_PATH_TRACING_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
+      else k_wf_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
+      issued += nNew;
+    }
+    // a small queue is run further per round (fewer rounds in the tail)
+    const int K = nIn + nNew < cap / 8 ? 64 : EXA_WF_STEPS;
+    k_wf_walk<<<grid, 128, 0, s>>>(A, lp, width, Q, K);
+    if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
+    else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
+    cudaCheck(cudaGetLastError(), "wavefront round");
+    unsigned h[3];
+    cudaCheck(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s), "read queues");
+    cudaCheck(cudaStreamSynchronize(s), "wavefront round");
+    nIn = h[1];
+    if (nIn == 0 && issued >= total) break;
+    // next round: the out queue becomes the input
+    const unsigned next[3] = {h[1], 0u, 0u};
+    cudaCheck(cudaMemcpyAsync(counters, next, sizeof(next), cudaMemcpyHostToDevice, s), "swap queues");
+    std::swap(inIdx, outIdx);
+  }
+  k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
+  cudaCheck(cudaGetLastError(), "k_resolve");
+}
+
+// EXA_RENDER_STRATEGY (the single-launch renderer): 1 thread per pixel,
+// 2 thread per sample + resolve, 3 persistent state machine + resolve.
+// EXA_WAVEFRONT 1: exa_render uses the wavefront renderer instead.
 #ifndef EXA_RENDER_STRATEGY
 #define EXA_RENDER_STRATEGY 2
 #endif
+#ifndef EXA_WAVEFRONT
+#define EXA_WAVEFRONT 1
+#endif
+
+bool useWavefront() { return EXA_WAVEFRONT != 0; }
 
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,
                   float4 *colors, cudaStream_t s)
