@@ -198,6 +198,7 @@ def run_ours(a):
         torch.cuda.synchronize()
         barrier()
     ctx.sync()
+    render_stats = ctx.render_stats()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
     if world > 1:
@@ -219,7 +220,10 @@ def run_ours(a):
     avg_nv = float(counts.mean())
     alg_bytes = g_samples * 64 + e_samples * (32 + 16 * avg_nv) + dda_cells * 4
     peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (ms / 1e3) / 1e9
+    # dominant kernel: the wavefront walk kernel (all field samples and DDA
+    # cells happen there); its time summed over the frame's launches
+    walk_ms = render_stats["walkMs"] if render_stats["wavefront"] else ms
+    achieved = alg_bytes / (walk_ms / 1e3) / 1e9
     tr = load_traffic()
     traffic = None
     if tr and tr.get("dataset") == a.config:
@@ -271,7 +275,9 @@ def run_ours(a):
             "config": workload_config(a),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_render<PATH_TRACING>",
+                         "kernel": "k_wf_walk (summed over the frame's launches)" if render_stats["wavefront"] else
+                         "k_render_sample<PATH_TRACING>",
+                         "kernel_ms_per_step": walk_ms,
                          "algorithmic_bytes_per_launch": alg_bytes},
             "field_samples": {"render_per_s": field_samples / (ms / 1e3), "per_step": field_samples,
                               "gridlet_per_step": g_samples, "element_per_step": e_samples,
@@ -282,7 +288,8 @@ def run_ours(a):
                     "d2h_bytes_per_step": a.width * a.height * 4},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": a.steps,
+            "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
+            "render": render_stats,
             "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
                                                   "numWedges", "numHexes", "numTets")} | {
                 "field_bytes": ds.field_bytes, "gen_seconds": gen_s},

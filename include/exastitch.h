@@ -317,9 +317,24 @@ int exa_launch_params_init(exa_launch_params *lp);
 /* One frame: width*height pixels, lp->render.spp samples each, into
  * lp->fbPointer (RGBA8) and lp->accumBuffer (device pointers owned by the
  * caller).  Replaces owlLaunch2D(rayGen,w,h,lp) (OWLRenderer.cpp:621).
- * Async on the context stream. */
+ * The wavefront renderer reads its queue sizes back once per round, so
+ * the call returns after the frame's kernels have been issued and most of
+ * them have run; call exa_sync before reading the outputs. */
 int exa_render(exa_context *ctx, const exa_launch_params *lp,
                int32_t width, int32_t height);
+
+/* How the last exa_render call ran (no reference counterpart). */
+typedef struct {
+  uint32_t wavefront;      /* 1: the wavefront renderer ran               */
+  uint32_t rounds;         /* camera / walk / event rounds                */
+  uint32_t peakQueue;      /* most path records queued after a round      */
+  uint32_t queueCapacity;  /* record capacity of each queue               */
+  uint32_t walkLaunches;   /* walk-kernel launches                        */
+  float    cameraMs;       /* summed GPU time of the camera kernels       */
+  float    walkMs;         /* summed GPU time of the walk kernels         */
+  float    eventMs;        /* summed GPU time of the event kernels        */
+} exa_render_stats;
+int exa_get_render_stats(exa_context *ctx, exa_render_stats *out);
 
 /* ------------------------------------------------------------------ */
 /* allocation-free rendering                                           */

@@ -371,6 +371,7 @@ struct exa_context {
   DBuf<uint32_t> wfRecords;  // wavefront path records: 3 queues x 60 words x capacity
   DBuf<unsigned> wfCounters; // wavefront queue sizes
   unsigned wfCap = 0;
+  exa_render_stats lastStats{};
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
 };
@@ -683,6 +684,14 @@ int exa_sample_points_host(exa_context *ctx, const exa_vec3f *posHost, uint64_t 
   });
 }
 
+int exa_get_render_stats(exa_context *ctx, exa_render_stats *out)
+{
+  return guarded([&] {
+    need(ctx && out, EXA_ERR_INVALID, "null argument");
+    *out = ctx->lastStats;
+  });
+}
+
 int exa_launch_params_init(exa_launch_params *lp)
 {
   return guarded([&] {
@@ -745,9 +754,19 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
         ctx->wfCounters.alloc(3);
         ctx->wfCap = cap;
       }
+      WfStats st;
       renderWavefront(ctx->sampler->accel, *lp, width, height, ctx->sampleColors.ptr, ctx->wfRecords.ptr, ctx->wfCap,
-                      ctx->wfCounters.ptr, ctx->stream);
+                      ctx->wfCounters.ptr, ctx->stream, &st);
+      ctx->lastStats.wavefront = 1;
+      ctx->lastStats.rounds = st.rounds;
+      ctx->lastStats.peakQueue = st.peakQueue;
+      ctx->lastStats.queueCapacity = ctx->wfCap;
+      ctx->lastStats.walkLaunches = st.walkLaunches;
+      ctx->lastStats.cameraMs = st.cameraMs;
+      ctx->lastStats.walkMs = st.walkMs;
+      ctx->lastStats.eventMs = st.eventMs;
     } else {
+      ctx->lastStats = exa_render_stats{};
       launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
     }
   });

@@ -169,8 +169,12 @@ void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, con
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
 // wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 3 words
+struct WfStats {
+  unsigned rounds = 0, peakQueue = 0, walkLaunches = 0;
+  float cameraMs = 0.f, walkMs = 0.f, eventMs = 0.f;
+};
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
-                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s);
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats);
 bool useWavefront();
 constexpr int kWfLaneWords = 61;
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,

@@ -996,13 +996,13 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
 }
 
 #ifndef EXA_WF_STEPS
-#define EXA_WF_STEPS 8
+#define EXA_WF_STEPS 4
 #endif
 
 // host loop of the wavefront renderer; synchronizes the stream once per
 // round to read the queue sizes
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
-                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s)
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats)
 {
   const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
   int dev = 0, sms = 152;
@@ -1015,10 +1015,18 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   unsigned nIn = 0;
   int inIdx = 0, outIdx = 1;
   const unsigned grid = (unsigned)sms * 16;
+  // per-kernel-class timing on this stream: camera, walk, events
+  cudaEvent_t ev[4];
+  for (auto &e : ev) cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
+  struct EvGuard {
+    cudaEvent_t *e;
+    ~EvGuard() { for (int k = 0; k < 4; ++k) cudaEventDestroy(e[k]); }
+  } evGuard{ev};
   cudaCheck(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned), s), "reset queues");
   for (int round = 0; round < (1 << 24); ++round) {
     WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap};
     const unsigned nNew = (unsigned)std::min<unsigned long long>(cap - nIn, total - issued);
+    cudaCheck(cudaEventRecord(ev[0], s), "event");
     if (nNew) {
       const unsigned g = std::min<unsigned>(grid, (nNew + 127) / 128);
       if (pt) k_wf_camera<EXA_PATH_TRACING_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
@@ -1027,14 +1035,29 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     }
     // a small queue is run further per round (fewer rounds in the tail)
     const int K = nIn + nNew < cap / 8 ? 64 : EXA_WF_STEPS;
+    cudaCheck(cudaEventRecord(ev[1], s), "event");
     k_wf_walk<<<grid, 128, 0, s>>>(A, lp, width, Q, K);
+    cudaCheck(cudaEventRecord(ev[2], s), "event");
     if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
     else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
+    cudaCheck(cudaEventRecord(ev[3], s), "event");
     cudaCheck(cudaGetLastError(), "wavefront round");
     unsigned h[3];
     cudaCheck(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s), "read queues");
     cudaCheck(cudaStreamSynchronize(s), "wavefront round");
+    if (stats) {
+      float ms[3] = {0.f, 0.f, 0.f};
+      for (int k = 0; k < 3; ++k) cudaCheck(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]), "event time");
+      stats->cameraMs += ms[0];
+      stats->walkMs += ms[1];
+      stats->eventMs += ms[2];
+      stats->walkLaunches++;
+    }
     nIn = h[1];
+    if (stats) {
+      stats->rounds = round + 1;
+      stats->peakQueue = std::max(stats->peakQueue, nIn + h[2]);
+    }
     if (nIn == 0 && issued >= total) break;
     // next round: the out queue becomes the input
     const unsigned next[3] = {h[1], 0u, 0u};

@@ -173,6 +173,12 @@ class LaunchParams(C.Structure):
     ]
 
 
+class RenderStats(C.Structure):
+    _fields_ = [("wavefront", C.c_uint32), ("rounds", C.c_uint32), ("peakQueue", C.c_uint32),
+                ("queueCapacity", C.c_uint32), ("walkLaunches", C.c_uint32), ("cameraMs", C.c_float),
+                ("walkMs", C.c_float), ("eventMs", C.c_float)]
+
+
 class MemStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "elemVertexBytes", "elemIndexBytes", "gridletBytes", "emptyScalarsBytes", "nonEmptyScalarsBytes",
@@ -188,7 +194,7 @@ EXPORTED = [
     "exa_model_set_voxel_space_transform", "exa_model_get_world_bounds", "exa_model_mem_stats",
     "exa_sampler_build", "exa_sampler_compute_max_opacities", "exa_sampler_set_lps", "exa_sampler_class_name",
     "exa_get_majorants", "exa_get_prim_majorants", "exa_sample_points", "exa_sample_points_host",
-    "exa_launch_params_init", "exa_render", "exa_render_noalloc",
+    "exa_launch_params_init", "exa_render", "exa_render_noalloc", "exa_get_render_stats",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -228,6 +234,7 @@ def lib():
         "exa_launch_params_init": ([C.POINTER(LaunchParams)], C.c_int),
         "exa_render": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
         "exa_render_noalloc": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
+        "exa_get_render_stats": ([ctx_p, C.POINTER(RenderStats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -277,6 +284,11 @@ class Context:
 
     def sync(self):
         _check(lib().exa_sync(self.h))
+
+    def render_stats(self):
+        st = RenderStats()
+        _check(lib().exa_get_render_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in RenderStats._fields_}
 
     def device_errors(self):
         b = C.c_uint32()
