@@ -751,7 +751,7 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int
                                                           (size_t)lp->render.spp, (size_t)1 << 22);
       if (ctx->wfCap < cap) {
         ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
-        ctx->wfCounters.alloc(3);
+        ctx->wfCounters.alloc(4);
         ctx->wfCap = cap;
       }
       WfStats st;

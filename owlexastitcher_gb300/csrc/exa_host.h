@@ -168,7 +168,7 @@ void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, con
                          size_t words, cudaStream_t s);
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
-// wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 3 words
+// wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 4 words
 struct WfStats {
   unsigned rounds = 0, peakQueue = 0, walkLaunches = 0;
   float cameraMs = 0.f, walkMs = 0.f, eventMs = 0.f;

@@ -788,7 +788,7 @@ static_assert(kLaneWords == kWfLaneWords, "record size");
 
 struct WfQueues {
   uint32_t *in, *out, *ev;  // record buffers (kLaneWords * cap words each)
-  unsigned *cnt;            // [0] in, [1] out, [2] ev
+  unsigned *cnt;            // [0] in, [1] out, [2] ev, [3] walk fetch cursor
   unsigned cap;
 };
 
@@ -944,27 +944,46 @@ __global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ Accel
   flush_counters(c, lp);
 }
 
-// walks: at most K tracking steps each, then compaction
+// walks: persistent warps; every lane takes one tracking step per
+// iteration, and a lane whose walk ended appends the record to the event
+// queue and fetches the next walk (one atomic per warp).  Lanes stay busy
+// until the input is used up, and each record is read and written once per
+// walk.
 __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __grid_constant__ AccelView A,
-                                                 const __grid_constant__ exa_launch_params lp, int width, WfQueues Q,
-                                                 int K)
+                                                                        const __grid_constant__ exa_launch_params lp,
+                                                                        WfQueues Q)
 {
   PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
   const unsigned n = Q.cnt[0];
-  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    const unsigned i = base + threadIdx.x;
-    Lane L;
-    bool more = false, ended = false;
-    if (i < n) {
-      wf_load_walk(L, Q.in, Q.cap, i, lp.majorantGrid);
-      more = true;
-      for (int k = 0; k < K && more; ++k) more = walk_step(L.w, c, L.rng, L.shadow);
-      ended = !more;
+  const unsigned lane = threadIdx.x & 31;
+  Lane L;
+  bool active = false, exhausted = false;
+  unsigned src = 0;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need && !exhausted) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(&Q.cnt[3], (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (unsigned)__popc(need) >= n) exhausted = true;
+      if (!active) {
+        const unsigned idx = base + __popc(need & ((1u << lane) - 1u));
+        if (idx < n) {
+          wf_load_walk(L, Q.in, Q.cap, idx, lp.majorantGrid);
+          active = true;
+          src = idx;
+        }
+      }
     }
-    const unsigned so = warp_append(&Q.cnt[1], more);
-    if (more) { wf_store_walk(L, Q.out, Q.cap, so); wf_copy_path(Q.in, i, Q.out, so, Q.cap); }
-    const unsigned se = warp_append(&Q.cnt[2], ended);
-    if (ended) { wf_store_walk(L, Q.ev, Q.cap, se); wf_copy_path(Q.in, i, Q.ev, se, Q.cap); }
+    if (!__any_sync(0xffffffffu, active)) break;
+    const bool ended = active && !walk_step(L.w, c, L.rng, L.shadow);
+    const unsigned slot = warp_append(&Q.cnt[2], ended);
+    if (ended) {
+      wf_store_walk(L, Q.ev, Q.cap, slot);
+      wf_copy_path(Q.in, src, Q.ev, slot, Q.cap);
+      active = false;
+    }
   }
   flush_counters(c, lp);
 }
@@ -995,10 +1014,6 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
   flush_counters(c, lp);
 }
 
-#ifndef EXA_WF_STEPS
-#define EXA_WF_STEPS 4
-#endif
-
 // host loop of the wavefront renderer; synchronizes the stream once per
 // round to read the queue sizes
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
@@ -1015,6 +1030,9 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   unsigned nIn = 0;
   int inIdx = 0, outIdx = 1;
   const unsigned grid = (unsigned)sms * 16;
+  int perSM = 4;
+  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk, 128, 0), "occupancy");
+  const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
   // per-kernel-class timing on this stream: camera, walk, events
   cudaEvent_t ev[4];
   for (auto &e : ev) cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
@@ -1022,7 +1040,7 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     cudaEvent_t *e;
     ~EvGuard() { for (int k = 0; k < 4; ++k) cudaEventDestroy(e[k]); }
   } evGuard{ev};
-  cudaCheck(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned), s), "reset queues");
+  cudaCheck(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned), s), "reset queues");
   for (int round = 0; round < (1 << 24); ++round) {
     WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap};
     const unsigned nNew = (unsigned)std::min<unsigned long long>(cap - nIn, total - issued);
@@ -1033,10 +1051,8 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
       else k_wf_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
       issued += nNew;
     }
-    // a small queue is run further per round (fewer rounds in the tail)
-    const int K = nIn + nNew < cap / 8 ? 64 : EXA_WF_STEPS;
     cudaCheck(cudaEventRecord(ev[1], s), "event");
-    k_wf_walk<<<grid, 128, 0, s>>>(A, lp, width, Q, K);
+    k_wf_walk<<<walkGrid, 128, 0, s>>>(A, lp, Q);
     cudaCheck(cudaEventRecord(ev[2], s), "event");
     if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
     else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
@@ -1056,11 +1072,11 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     nIn = h[1];
     if (stats) {
       stats->rounds = round + 1;
-      stats->peakQueue = std::max(stats->peakQueue, nIn + h[2]);
+      stats->peakQueue = std::max(stats->peakQueue, h[2]);
     }
     if (nIn == 0 && issued >= total) break;
     // next round: the out queue becomes the input
-    const unsigned next[3] = {h[1], 0u, 0u};
+    const unsigned next[4] = {h[1], 0u, 0u, 0u};
     cudaCheck(cudaMemcpyAsync(counters, next, sizeof(next), cudaMemcpyHostToDevice, s), "swap queues");
     std::swap(inIdx, outIdx);
   }
