@@ -209,13 +209,15 @@ def run_ours(a):
     clocks = clk.summary()
 
     # counting launch (same frame): algorithmic work of one launch
-    cnt = torch.zeros(8, dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(16, dtype=torch.int64, device="cuda")
     r.lp.ext.stepCounters = cnt.data_ptr()
     step()
     torch.cuda.synchronize()
     r.lp.ext.stepCounters = None
     c = cnt.cpu().numpy()
     field_samples, g_samples, e_samples, dda_cells, paths = (int(x) for x in c[:5])
+    work = dict(zip(["cache_misses", "table_queries", "gridlet_tests", "bvh_walks", "walks"],
+                    (int(x) for x in c[5:10])))
     counts = np.count_nonzero(ds.indices >= 0, axis=1) if len(ds.indices) else np.array([8])
     avg_nv = float(counts.mean())
     alg_bytes = g_samples * 64 + e_samples * (32 + 16 * avg_nv) + dda_cells * 4
@@ -283,7 +285,7 @@ def run_ours(a):
                               "gridlet_per_step": g_samples, "element_per_step": e_samples,
                               "dda_cells_per_step": dda_cells,
                               "point_query_per_s": q_dev, "point_query_e2e_per_s": q_e2e,
-                              "point_query_n": len(P)},
+                              "point_query_n": len(P), "work_per_step": work},
             "e2e": {"value": world * paths_per_step / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": lp_bytes,
                     "d2h_bytes_per_step": a.width * a.height * 4},
             "cpu_baseline": cpu,

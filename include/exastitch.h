@@ -126,9 +126,13 @@ typedef struct {
                              /* reference's empty-AABB culling)             */
   uint32_t  frameID;         /* RNG stream selector for batched frames       */
   uint32_t *deviceErrors;    /* optional: EXA_DEVERR_* bits are OR-ed here   */
-  unsigned long long *stepCounters; /* optional counting launch: [0] field */
-                             /* samples, [1] gridlet samples, [2] element    */
-                             /* samples, [3] DDA cells, [4] paths            */
+  unsigned long long *stepCounters; /* optional counting launch (16 u64): */
+                             /* [0] field samples, [1] gridlet samples,      */
+                             /* [2] element samples, [3] DDA cells,          */
+                             /* [4] paths; wavefront renderer also: [5]      */
+                             /* gridlet-cache misses, [6] table queries,     */
+                             /* [7] gridlet tests, [8] element-BVH walks,     */
+                             /* [9] walks                                    */
   float    *traceT;          /* optional, per pixel: distance (voxel space) */
                              /* of the first sample's first interaction, -1 */
                              /* if the ray left the volume                  */

@@ -3,10 +3,12 @@
 // (sampler/ExaStitchSampler.cpp:71-323) and the zero-length-ray query of
 // sample() (sampler/ExaStitchSampler.h:128-140).
 //
-// Gridlets: one table per level over the level's dual-cell lattice, one
-// entry per 2^shift-wide block (8 for makeGrids bricks, makeGrids.cpp:46).
-// An entry holds the single gridlet whose half-open interior touches the
-// block, or a list.  A query on an exact block face also looks at the
+// Gridlets: block tables over a dual-cell lattice, one entry per
+// 2^shift-wide block (8 for makeGrids bricks, makeGrids.cpp:46): one table
+// over the finest level's lattice listing the gridlets of every level, or,
+// when that grid would be too large, one table per level.  An entry holds
+// the single gridlet whose extent meets the block's open interior, or an
+// ascending list.  A query on an exact block face also looks at the
 // neighbouring block, so the reference's inclusive box test is honoured.
 // Stitching elements: a linear BVH (Karras 2012, "Maximizing parallelism in
 // the construction of BVHs, octrees and k-d trees") built on the GPU; each
@@ -88,30 +90,49 @@ EXA_D bool occ_maybe(const ElemOccupancy &O, V3 pos)
 
 EXA_D int floor_div_pow2(int v, int shift) { return v >> shift; }  // arithmetic shift floors
 
-// test every candidate gridlet of one table; keeps the lowest index hit
-EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool cull, int &best,
-                       float &bestVal, int &bestCell)
+// optional per-thread work counters of the point query (counting launches)
+struct QueryStats {
+  unsigned tables, gridletTests, bvhWalks;
+};
+
+// the block of table T holding pos, and whether pos lies on the block's low
+// face along each axis (then the block below is looked at too); false when
+// pos is NaN or far outside the lattice
+EXA_D bool table_block(const GridletTable &T, V3 pos, int b0[3], int nb[3])
 {
   const float inv = __uint_as_float((uint32_t)(127 - T.level) << 23);  // 2^-level
   const float u[3] = {pos.x * inv - 0.5f, pos.y * inv - 0.5f, pos.z * inv - 0.5f};
-  int b0[3], nb[3];
   for (int a = 0; a < 3; ++a) {
     const float fu = floorf(u[a]);
-    if (!(fu >= -2147483520.f && fu <= 2147483520.f)) return;  // NaN / far outside
+    if (!(fu >= -2147483520.f && fu <= 2147483520.f)) return false;
     const int iu = (int)fu - T.origin[a];
-    int b = floor_div_pow2(iu, T.shift);
+    const int b = floor_div_pow2(iu, T.shift);
     // exactly on a block face: the gridlet ending there is listed in the
     // block below
     const bool face = (fu == u[a]) && ((iu & ((1 << T.shift) - 1)) == 0);
     nb[a] = face ? 2 : 1;
     b0[a] = face ? b - 1 : b;
   }
+  return true;
+}
+
+EXA_D int table_entry(const GridletTable &T, int bx, int by, int bz)
+{
+  if (bx < 0 || by < 0 || bz < 0 || bx >= T.n[0] || by >= T.n[1] || bz >= T.n[2]) return -1;
+  return __ldg(T.entries + ((size_t)bz * T.n[1] + by) * T.n[0] + bx);
+}
+
+// test every candidate gridlet of one table; keeps the lowest index hit
+EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool cull, int &best,
+                       float &bestVal, int &bestCell, QueryStats *qs)
+{
+  if (qs) qs->tables++;
+  int b0[3], nb[3];
+  if (!table_block(T, pos, b0, nb)) return;
   for (int dz = 0; dz < nb[2]; ++dz)
     for (int dy = 0; dy < nb[1]; ++dy)
       for (int dx = 0; dx < nb[0]; ++dx) {
-        const int bx = b0[0] + dx, by = b0[1] + dy, bz = b0[2] + dz;
-        if (bx < 0 || by < 0 || bz < 0 || bx >= T.n[0] || by >= T.n[1] || bz >= T.n[2]) continue;
-        const int e = __ldg(T.entries + ((size_t)bz * T.n[1] + by) * T.n[0] + bx);
+        const int e = table_entry(T, b0[0] + dx, b0[1] + dy, b0[2] + dz);
         if (e == -1) continue;
         int cnt = 1;
         const int32_t *list = nullptr;
@@ -125,6 +146,7 @@ EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool c
           if (cull && A.gridletMaxOps && __ldg(A.gridletMaxOps + g) == 0.f) continue;
           float v;
           int c;
+          if (qs) qs->gridletTests++;
           if (intersect_gridlet(v, c, pos, A.gridlets + g, A.scalars)) {
             best = g;
             bestVal = v;
@@ -191,7 +213,7 @@ static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, b
 }
 
 // sample() (sampler/ExaStitchSampler.h:128-140); sets EXA_DEVERR bits in err
-EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err)
+EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
 {
   exa_sample s;
   s.primID = -1;
@@ -200,7 +222,7 @@ EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &e
   int best = 0x7fffffff, cell = -1;
   float val = 0.f;
   for (int t = 0; t < A.numTables; ++t) {
-    query_table(A, A.tables[t], pos, cull, best, val, cell);
+    query_table(A, A.tables[t], pos, cull, best, val, cell, qs);
     if (A.tablesSorted && best != 0x7fffffff) break;
   }
   if (best != 0x7fffffff) {
@@ -211,7 +233,10 @@ EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &e
   }
   int be = 0x7fffffff;
   float ev = 0.f;
-  if (A.numElems > 0 && occ_maybe(A.occ, pos) && !query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
+  if (A.numElems > 0 && occ_maybe(A.occ, pos)) {
+    if (qs) qs->bvhWalks++;
+    if (!query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
+  }
   if (be != 0x7fffffff) {
     s.primID = be;
     s.cellID = -1;

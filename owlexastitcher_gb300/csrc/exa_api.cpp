@@ -153,49 +153,75 @@ size_t ExaStitchSampler::accelBytes() const
 
 // Per-level block tables over the dual-cell lattice.  Block width 8
 // (makeGrids bricks); widened when a level's table would be very large.
+// Block tables over dual-cell lattices.  A gridlet of level L covers, along
+// each axis, the closed interval [lower + 0.5, lower + dims + 0.5] * 2^L of
+// voxel space, which is [(2 lower + 1) r - 1, (2 (lower + dims) + 1) r - 1] / 2
+// in units of the dual lattice of a table of level Lt <= L (r = 2^(L - Lt)).
+// A gridlet is listed in every block whose open interior meets that
+// interval; a query exactly on a block's low face also looks at the block
+// below, so every gridlet whose closed box holds the point is seen.
+//
+// One table over the finest lattice holds every gridlet when its block grid
+// fits (one lookup per query, lists sorted so the first hit is the lowest
+// index); otherwise there is one table per level.
 void ExaStitchSampler::buildGridletTables(cudaStream_t s)
 {
   const auto &G = model->gridlets;
-  std::map<int, std::vector<int>> byLevel;
-  for (size_t i = 0; i < G.size(); ++i) byLevel[G[i].level].push_back((int)i);
-  if ((int)byLevel.size() > kMaxLevels) throw Error(EXA_ERR_INVALID, "more than 16 gridlet levels");
   struct Tab { GridletTable t; std::vector<int32_t> entries, items; int minIdx, maxIdx; };
-  std::vector<Tab> tabs;
-  for (auto &kv : byLevel) {
-    Tab T;
+  // doubled extents of gridlet gi in the lattice of level lt, relative to
+  // nothing (origin subtracted later)
+  auto extent2 = [&](int gi, int lt, int64_t lo2[3], int64_t hi2[3]) {
+    const exa_gridlet &g = G[gi];
+    const int64_t r = (int64_t)1 << (g.level - lt);
+    const int64_t gl[3] = {g.lower.x, g.lower.y, g.lower.z};
+    const int64_t gd[3] = {std::max(g.dims.x, 1), std::max(g.dims.y, 1), std::max(g.dims.z, 1)};
+    for (int a = 0; a < 3; ++a) {
+      lo2[a] = (2 * gl[a] + 1) * r - 1;
+      hi2[a] = (2 * (gl[a] + gd[a]) + 1) * r - 1;
+    }
+  };
+  auto floorDiv = [](int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+  // blocks [b0, b1] of a table (lattice origin org, block width 2^shift)
+  // whose open interiors meet the gridlet's interval
+  auto blockRange = [&](int gi, int lt, const int org[3], int shift, int b0[3], int b1[3]) {
+    int64_t lo2[3], hi2[3];
+    extent2(gi, lt, lo2, hi2);
+    const int64_t w2 = (int64_t)2 << shift;
+    for (int a = 0; a < 3; ++a) {
+      b0[a] = (int)floorDiv(lo2[a] - 2 * (int64_t)org[a], w2);
+      b1[a] = (int)(floorDiv(hi2[a] - 2 * (int64_t)org[a] + w2 - 1, w2) - 1);
+    }
+  };
+  auto makeTable = [&](const std::vector<int> &ids, int lt, int shift, Tab &T) {
     std::memset(&T.t, 0, sizeof(T.t));
-    T.t.level = kv.first;
-    int lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    T.t.level = lt;
+    T.t.shift = shift;
     T.minIdx = INT32_MAX;
     T.maxIdx = -1;
-    for (int gi : kv.second) {
-      const exa_gridlet &g = G[gi];
-      const int gl[3] = {g.lower.x, g.lower.y, g.lower.z}, gd[3] = {g.dims.x, g.dims.y, g.dims.z};
+    int64_t lo[3] = {INT64_MAX, INT64_MAX, INT64_MAX}, hi[3] = {INT64_MIN, INT64_MIN, INT64_MIN};
+    for (int gi : ids) {
+      int64_t lo2[3], hi2[3];
+      extent2(gi, lt, lo2, hi2);
       for (int a = 0; a < 3; ++a) {
-        lo[a] = std::min(lo[a], gl[a]);
-        hi[a] = std::max(hi[a], gl[a] + std::max(gd[a], 1));
+        lo[a] = std::min(lo[a], floorDiv(lo2[a], 2));
+        hi[a] = std::max(hi[a], floorDiv(hi2[a] + 1, 2));
       }
       T.minIdx = std::min(T.minIdx, gi);
       T.maxIdx = std::max(T.maxIdx, gi);
     }
-    int shift = 3;
-    auto blocks = [&](int sh, int a) { return (int)(((int64_t)(hi[a] - lo[a]) + (1ll << sh) - 1) >> sh) + 1; };
-    while ((int64_t)blocks(shift, 0) * blocks(shift, 1) * blocks(shift, 2) > (1ll << 27) && shift < 20) shift++;
-    T.t.shift = shift;
-    for (int a = 0; a < 3; ++a) { T.t.origin[a] = lo[a]; T.t.n[a] = blocks(shift, a); }
+    for (int a = 0; a < 3; ++a) {
+      if (lo[a] < INT32_MIN / 2 || hi[a] > INT32_MAX / 2) throw Error(EXA_ERR_INVALID, "gridlet lattice out of range");
+      T.t.origin[a] = (int)lo[a];
+      T.t.n[a] = (int)(((hi[a] - lo[a]) + (1ll << shift) - 1) >> shift) + 1;
+    }
     const size_t nb = (size_t)T.t.n[0] * T.t.n[1] * T.t.n[2];
     std::vector<std::vector<int32_t>> lists(nb);
-    for (int gi : kv.second) {
-      const exa_gridlet &g = G[gi];
-      const int gl[3] = {g.lower.x, g.lower.y, g.lower.z}, gd[3] = {g.dims.x, g.dims.y, g.dims.z};
+    for (int gi : ids) {
       int b0[3], b1[3];
-      for (int a = 0; a < 3; ++a) {
-        b0[a] = (gl[a] - lo[a]) >> shift;
-        b1[a] = (gl[a] + std::max(gd[a], 1) - 1 - lo[a]) >> shift;
-      }
-      for (int z = b0[2]; z <= b1[2]; ++z)
-        for (int y = b0[1]; y <= b1[1]; ++y)
-          for (int x = b0[0]; x <= b1[0]; ++x)
+      blockRange(gi, lt, T.t.origin, shift, b0, b1);
+      for (int z = std::max(b0[2], 0); z <= std::min(b1[2], T.t.n[2] - 1); ++z)
+        for (int y = std::max(b0[1], 0); y <= std::min(b1[1], T.t.n[1] - 1); ++y)
+          for (int x = std::max(b0[0], 0); x <= std::min(b1[0], T.t.n[0] - 1); ++x)
             lists[((size_t)z * T.t.n[1] + y) * T.t.n[0] + x].push_back(gi);
     }
     T.entries.assign(nb, -1);
@@ -208,7 +234,63 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
       T.items.push_back((int32_t)L.size());
       T.items.insert(T.items.end(), L.begin(), L.end());
     }
-    tabs.push_back(std::move(T));
+  };
+  // smallest shift >= 3 whose block grid has at most 2^27 blocks
+  auto pickShift = [&](const std::vector<int> &ids, int lt, int64_t &listed) {
+    int64_t lo[3] = {INT64_MAX, INT64_MAX, INT64_MAX}, hi[3] = {INT64_MIN, INT64_MIN, INT64_MIN};
+    for (int gi : ids) {
+      int64_t lo2[3], hi2[3];
+      extent2(gi, lt, lo2, hi2);
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], floorDiv(lo2[a], 2));
+        hi[a] = std::max(hi[a], floorDiv(hi2[a] + 1, 2));
+      }
+    }
+    int shift = 3;
+    auto blocks = [&](int sh, int a) { return ((hi[a] - lo[a]) + (1ll << sh) - 1) / (1ll << sh) + 1; };
+    while (blocks(shift, 0) * blocks(shift, 1) * blocks(shift, 2) > (1ll << 27) && shift < 20) shift++;
+    const int org[3] = {(int)std::max<int64_t>(lo[0], INT32_MIN / 2), (int)std::max<int64_t>(lo[1], INT32_MIN / 2),
+                        (int)std::max<int64_t>(lo[2], INT32_MIN / 2)};
+    listed = 0;
+    for (int gi : ids) {
+      int b0[3], b1[3];
+      blockRange(gi, lt, org, shift, b0, b1);
+      listed += (int64_t)(b1[0] - b0[0] + 1) * (b1[1] - b0[1] + 1) * (b1[2] - b0[2] + 1);
+    }
+    return shift;
+  };
+
+  std::map<int, std::vector<int>> byLevel;
+  for (size_t i = 0; i < G.size(); ++i) {
+    if (G[i].level < 0 || G[i].level > 30) throw Error(EXA_ERR_INVALID, "gridlet level out of range");
+    byLevel[G[i].level].push_back((int)i);
+  }
+  std::vector<Tab> tabs;
+  bool unified = false;
+  if (byLevel.size() > 1) {
+    std::vector<int> all(G.size());
+    for (size_t i = 0; i < G.size(); ++i) all[i] = (int)i;
+    const int lmin = byLevel.begin()->first;
+    int64_t listed = 0;
+    const int shift = pickShift(all, lmin, listed);
+    // one table when its blocks stay 8 finest dual cells wide and the lists
+    // stay modest next to the gridlets themselves
+    if (shift == 3 && listed <= std::max<int64_t>(64 * (int64_t)G.size(), 1 << 20) && listed < (1ll << 28)) {
+      Tab T;
+      makeTable(all, lmin, shift, T);
+      tabs.push_back(std::move(T));
+      unified = true;
+    }
+  }
+  if (!unified) {
+    if ((int)byLevel.size() > kMaxLevels) throw Error(EXA_ERR_INVALID, "more than 16 gridlet levels");
+    for (auto &kv : byLevel) {
+      int64_t listed = 0;
+      const int shift = pickShift(kv.second, kv.first, listed);
+      Tab T;
+      makeTable(kv.second, kv.first, shift, T);
+      tabs.push_back(std::move(T));
+    }
   }
   std::sort(tabs.begin(), tabs.end(), [](const Tab &a, const Tab &b) { return a.minIdx < b.minIdx; });
   bool sorted = true;

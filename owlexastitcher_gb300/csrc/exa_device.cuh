@@ -134,7 +134,11 @@ EXA_D bool intersect_gridlet(float &value, int &cellID, V3 pos, const exa_gridle
   if (!(lo.x <= pos.x && lo.y <= pos.y && lo.z <= pos.z && pos.x <= hi.x && pos.y <= hi.y && pos.z <= hi.z))
     return false;
   const int nx = h1.x + 1, ny = h1.y + 1, nz = h1.z + 1;
-  const V3 p = mk3(__fdiv_rn(pos.x - lo.x, cw), __fdiv_rn(pos.y - lo.y, cw), __fdiv_rn(pos.z - lo.z, cw));
+  // x / 2^level == x * 2^-level exactly in IEEE arithmetic (both are the
+  // correctly rounded quotient), so the division of Gridlet.h:50 is a
+  // multiplication here
+  const float icw = __uint_as_float((uint32_t)(127 - level) << 23);
+  const V3 p = mk3((pos.x - lo.x) * icw, (pos.y - lo.y) * icw, (pos.z - lo.z) * icw);
   const int ix = (int)p.x, iy = (int)p.y, iz = (int)p.z;
   const int ax = imin_t(ix + 1, nx - 1), ay = imin_t(iy + 1, ny - 1), az = imin_t(iz + 1, nz - 1);
   const float *S = scalars + (uint32_t)h1.w;

@@ -22,9 +22,14 @@ constexpr int kTrackCap = 1 << 22;  // delta / ratio tracking steps per macrocel
 #define EXA_RENDER_MIN_BLOCKS 4
 #endif
 
-struct Counters {
-  unsigned long long fieldSamples, gridletSamples, elemSamples, ddaCells, paths;
+// work counters of a counting launch (lp.ext.stepCounters set); the index is
+// the slot in stepCounters
+enum : int {
+  CNT_FIELD, CNT_GRIDLET, CNT_ELEM, CNT_DDA, CNT_PATHS, CNT_MISS, CNT_TABLES, CNT_GTESTS, CNT_BVH, CNT_WALKS, CNT_N
 };
+// one column per thread in shared memory, so that an ordinary launch holds no
+// registers for them; every render kernel runs 128 threads per block
+static __shared__ unsigned s_cnt[CNT_N][128];
 
 struct RayS {
   V3 org, dir;
@@ -117,9 +122,33 @@ struct PathCtx {
   const AccelView &A;
   const exa_launch_params &lp;
   uint32_t err;
-  Counters cnt;
   bool counting;
 };
+
+EXA_D void cnt_add(const PathCtx &c, int k, unsigned v = 1)
+{
+  if (c.counting) s_cnt[k][threadIdx.x] += v;
+}
+
+EXA_D PathCtx make_ctx(const AccelView &A, const exa_launch_params &lp)
+{
+  PathCtx c{A, lp, 0u, lp.ext.stepCounters != nullptr};
+  if (c.counting)
+    for (int k = 0; k < CNT_N; ++k) s_cnt[k][threadIdx.x] = 0u;
+  return c;
+}
+
+// device-error bits and this thread's counters to global memory; any lane
+// mask
+EXA_D void flush_counters(const PathCtx &c, const exa_launch_params &lp)
+{
+  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
+  if (c.counting)
+    for (int k = 0; k < CNT_N; ++k) {
+      const unsigned v = s_cnt[k][threadIdx.x];
+      if (v) atomicAdd(lp.ext.stepCounters + k, (unsigned long long)v);
+    }
+}
 
 // make_orthonormal_basis (deviceCode.cu:144-149) + HG sampling (:965-985)
 EXA_D V3 hg_sample(V3 wo, float g, Rng &rng)
@@ -196,7 +225,7 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
     }
     w.t1 = fmin_t(rmin3(w.dda.tnext), w.dda.tmax);
     const int leafID = (w.dda.cell.z * G.dims.y + w.dda.cell.y) * G.dims.x + w.dda.cell.x;
-    if (c.counting) c.cnt.ddaCells++;
+    cnt_add(c, CNT_DDA);
     w.maj = __ldg(lp.maxOpacities + leafID);
     w.t = w.dda.t0;
     w.primID = -1;
@@ -218,10 +247,19 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
   }
   w.pos = add3(w.org, muls(w.dir, w.t));
   exa_sample s = test_sample(c.A, w.pos, w.primID);
-  if (s.primID < 0) s = sample_field(c.A, w.pos, lp.ext.cullTransparentPrims != 0, c.err);
+  if (s.primID < 0) {
+    QueryStats q{0u, 0u, 0u};
+    s = sample_field(c.A, w.pos, lp.ext.cullTransparentPrims != 0, c.err, &q);
+    if (c.counting) {
+      cnt_add(c, CNT_MISS);
+      cnt_add(c, CNT_TABLES, q.tables);
+      cnt_add(c, CNT_GTESTS, q.gridletTests);
+      cnt_add(c, CNT_BVH, q.bvhWalks);
+    }
+  }
   if (c.counting) {
-    c.cnt.fieldSamples++;
-    if (s.primID >= 0) { if (s.cellID != -1) c.cnt.gridletSamples++; else c.cnt.elemSamples++; }
+    cnt_add(c, CNT_FIELD);
+    if (s.primID >= 0) cnt_add(c, s.cellID != -1 ? CNT_GRIDLET : CNT_ELEM);
   }
   if (s.primID < 0) return true;
   if (s.cellID != -1) w.primID = s.primID;
@@ -287,7 +325,7 @@ struct Machine {
   EXA_D void finish_sample(Lane &L, float4 col)
   {
     colors[(size_t)L.pixelID * lp.render.spp + L.s] = col;
-    if (c.counting) c.cnt.paths++;
+    cnt_add(c, CNT_PATHS);
     L.phase = PH_FETCH;
   }
 
@@ -451,7 +489,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render(const __g
                                                 const __grid_constant__ exa_launch_params lp, int width, int height,
                                                 unsigned *jobCounter, float4 *colors)
 {
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
   const int spp = lp.render.spp;
   const int tilesX = (width + 15) / 16;
@@ -487,16 +525,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render(const __g
     if (__all_sync(0xffffffffu, L.phase == PH_DONE)) break;
     if (L.phase == PH_TRACK) M.advance(L);
   }
-  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
-  if (c.counting) {
-    unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
-                               c.cnt.paths};
-    for (int k = 0; k < 5; ++k) {
-      unsigned long long x = v[k];
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if (lane == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
-    }
-  }
+  flush_counters(c, lp);
 }
 
 // ------------------------------------------------------------------------
@@ -664,7 +693,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(con
   const int tilesX = (width + 15) / 16;
   const int px = (blockIdx.x % tilesX) * 16 + (threadIdx.x & 15);
   const int py = (blockIdx.x / tilesX) * 8 + (threadIdx.x >> 4);
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   if (px < width && py < height) {
     const int pixelID = px + width * py;
     const int numLights = num_lights(lp);
@@ -674,7 +703,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(con
       const float4 col = sample_nested<INTEGRATOR>(c, px, py, pixelID, s, height, numLights, s == 0 ? &tHit : nullptr,
                                                    s == 0 ? &trv : nullptr);
       acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
-      if (c.counting) c.cnt.paths++;
+      cnt_add(c, CNT_PATHS);
     }
     if (lp.accumID > 0 && lp.accumBuffer) {
       const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
@@ -690,16 +719,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(con
     if (lp.ext.traceT) lp.ext.traceT[pixelID] = tHit;
     if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = trv;
   }
-  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
-  if (c.counting) {
-    unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
-                               c.cnt.paths};
-    for (int k = 0; k < 5; ++k) {
-      unsigned long long x = v[k];
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if ((threadIdx.x & 31) == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
-    }
-  }
+  flush_counters(c, lp);
 }
 
 // S2: one thread per camera sample (pixel-major), colours to scratch
@@ -716,28 +736,19 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_sample(co
   const int tile = (int)(pj >> 7), within = (int)(pj & 127);
   const int px = (tile % tilesX) * 16 + (within & 15);
   const int py = (tile / tilesX) * 8 + (within >> 4);
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   if (px < width && py < height) {
     const int pixelID = px + width * py;
     float tHit = -1.f, trv = -1.f;
     const float4 col = sample_nested<INTEGRATOR>(c, px, py, pixelID, s, height, num_lights(lp), &tHit, &trv);
     colors[(size_t)pixelID * spp + s] = col;
-    if (c.counting) c.cnt.paths++;
+    cnt_add(c, CNT_PATHS);
     if (s == 0) {
       if (lp.ext.traceT) lp.ext.traceT[pixelID] = tHit;
       if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = trv;
     }
   }
-  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
-  if (c.counting) {
-    unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
-                               c.cnt.paths};
-    for (int k = 0; k < 5; ++k) {
-      unsigned long long x = v[k];
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if ((threadIdx.x & 31) == 0 && x) atomicAdd(lp.ext.stepCounters + k, x);
-    }
-  }
+  flush_counters(c, lp);
 }
 
 // renderFrame_Impl (deviceCode.cu:1283-1344) after the spp loop: sum the
@@ -790,7 +801,15 @@ struct WfQueues {
   uint32_t *in, *out, *ev;  // record buffers (kLaneWords * cap words each)
   unsigned *cnt;            // [0] in, [1] out, [2] ev, [3] walk fetch cursor
   unsigned cap;
+  int park;                 // walk kernel may park unfinished walks in out
 };
+
+// a warp whose input is used up parks its unfinished walks in the next
+// round's input once fewer than this many of its lanes are still walking,
+// instead of stepping the round's longest walks with the other lanes idle
+#ifndef EXA_WF_PARK_LANES
+#define EXA_WF_PARK_LANES 28
+#endif
 
 #define W(v) b[(size_t)(k++) * cap + i] = (v)
 #define WF(v) W(__float_as_uint(v))
@@ -900,16 +919,6 @@ EXA_D unsigned warp_append(unsigned *counter, bool pred)
   return base + __popc(ballot & ((1u << lane) - 1u));
 }
 
-EXA_D void flush_counters(PathCtx &c, const exa_launch_params &lp)
-{
-  if (c.err && lp.ext.deviceErrors) atomicOr(lp.ext.deviceErrors, c.err);
-  if (c.counting) {
-    const unsigned long long v[5] = {c.cnt.fieldSamples, c.cnt.gridletSamples, c.cnt.elemSamples, c.cnt.ddaCells,
-                                     c.cnt.paths};
-    for (int k = 0; k < 5; ++k)
-      if (v[k]) atomicAdd(lp.ext.stepCounters + k, v[k]);
-  }
-}
 
 // camera: samples [first, first + n) of the frame's job order; those that
 // start a walk are appended to the input queue
@@ -918,7 +927,7 @@ __global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ Accel
                                                    const __grid_constant__ exa_launch_params lp, int width, int height,
                                                    float4 *colors, WfQueues Q, unsigned first, unsigned n)
 {
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
   const int spp = lp.render.spp;
   const int tilesX = (width + 15) / 16;
@@ -947,13 +956,13 @@ __global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ Accel
 // walks: persistent warps; every lane takes one tracking step per
 // iteration, and a lane whose walk ended appends the record to the event
 // queue and fetches the next walk (one atomic per warp).  Lanes stay busy
-// until the input is used up, and each record is read and written once per
-// walk.
+// until the input is used up; then, in a large round, a warp left with few
+// walking lanes parks their walks in the next round's input and exits.
 __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __grid_constant__ AccelView A,
                                                                         const __grid_constant__ exa_launch_params lp,
                                                                         WfQueues Q)
 {
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   const unsigned n = Q.cnt[0];
   const unsigned lane = threadIdx.x & 31;
   Lane L;
@@ -973,10 +982,22 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
           wf_load_walk(L, Q.in, Q.cap, idx, lp.majorantGrid);
           active = true;
           src = idx;
+          cnt_add(c, CNT_WALKS);
         }
       }
     }
-    if (!__any_sync(0xffffffffu, active)) break;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES) {
+      // the walk record holds the complete walk state (position in the DDA,
+      // RNG counter, cached gridlet), so a parked walk resumes exactly
+      const unsigned slot = warp_append(&Q.cnt[1], active);
+      if (active) {
+        wf_store_walk(L, Q.out, Q.cap, slot);
+        wf_copy_path(Q.in, src, Q.out, slot, Q.cap);
+      }
+      break;
+    }
     const bool ended = active && !walk_step(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
@@ -994,7 +1015,7 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
                                                    const __grid_constant__ exa_launch_params lp, int width, int height,
                                                    float4 *colors, WfQueues Q)
 {
-  PathCtx c{A, lp, 0u, {0, 0, 0, 0, 0}, lp.ext.stepCounters != nullptr};
+  PathCtx c = make_ctx(A, lp);
   Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
   const unsigned n = Q.cnt[2];
   for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -1042,8 +1063,11 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   } evGuard{ev};
   cudaCheck(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned), s), "reset queues");
   for (int round = 0; round < (1 << 24); ++round) {
-    WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap};
     const unsigned nNew = (unsigned)std::min<unsigned long long>(cap - nIn, total - issued);
+    // parking pays while a round has several walks per walk-kernel thread;
+    // small rounds (the end of the frame) run their walks to completion
+    const int park = (unsigned long long)nIn + nNew >= 4ull * walkGrid * 128u ? 1 : 0;
+    WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap, park};
     cudaCheck(cudaEventRecord(ev[0], s), "event");
     if (nNew) {
       const unsigned g = std::min<unsigned>(grid, (nNew + 127) / 128);
