@@ -368,6 +368,99 @@ int exa_get_render_stats(exa_context *ctx, exa_render_stats *out);
 int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
                        int32_t width, int32_t height);
 
+/* ------------------------------------------------------------------ */
+/* learned field (no counterpart in the reference)                     */
+/* ------------------------------------------------------------------ */
+
+/* A multiresolution hash-grid encoding (16 levels x 2 FP16 features) and
+ * an MLP (32 -> 64 -> 64 -> 1, ReLU, BF16 weights, FP32 accumulation on the
+ * tensor cores) trained on (position, value) pairs that the exact sampler
+ * draws.  Majorants of macrocells where it is used are widened by the
+ * macrocell's measured maximum error; the other macrocells keep the exact
+ * sampler. */
+typedef struct exa_surrogate_params {
+  int32_t log2TableSize;      /* hash-table entries per level: 2^this (19)  */
+  int32_t baseResolution;     /* coarsest level's grid resolution (16)      */
+  float growth;               /* resolution factor between levels (1.5)     */
+  float importanceFraction;   /* share of pairs drawn inside refined        */
+                              /* gridlets, the rest uniform (0.5)           */
+  uint64_t numSamples;        /* training pairs (2^24)                      */
+  int32_t batch;              /* pairs per training step (2^18)             */
+  float learningRate;         /* Adam step size at the start of each        */
+                              /* exa_surrogate_train call (1e-2)            */
+  uint64_t seed;
+  float learningRateFinal;    /* step size at its end, reached by           */
+                              /* exponential decay (1e-3)                   */
+  int32_t pad0;
+} exa_surrogate_params;
+
+typedef struct exa_surrogate_stats {
+  float loss;                 /* mean squared error of the last training    */
+                              /* batch, value range normalised to 1         */
+  int32_t steps;              /* training steps taken                       */
+  float tolerance;            /* of the last exa_surrogate_evaluate         */
+  int32_t pad0;
+  double rmse;                /* over the probe points, / value range       */
+  double maxError;            /* largest |error| / value range              */
+  uint64_t probePoints;
+  uint64_t numMacrocells;
+  uint64_t numSurrogateMacrocells;  /* macrocells using the learned field   */
+  uint64_t tableBytes;        /* FP16 inference table                       */
+  uint64_t weightBytes;       /* BF16 weights                               */
+  uint64_t inferenceBytes;    /* table + weights + macrocell modes and      */
+                              /* widened majorants                          */
+  uint64_t fieldBytes;        /* exact field: gridlets, scalars, vertices,  */
+                              /* indices and point-location structures      */
+  uint64_t fallbackFieldBytes; /* the part of fieldBytes the exact-sampler  */
+                              /* macrocells still need (primitives whose    */
+                              /* bounds touch one) plus the point-location  */
+                              /* structures                                 */
+} exa_surrogate_stats;
+
+/* Geometry of the encoding: per-level grid resolutions, levels indexed
+ * densely (bit l), normalisation x = (pos - lo) * inv and value = vmin +
+ * y * vrange. */
+typedef struct exa_surrogate_geometry {
+  int32_t log2TableSize;
+  uint32_t denseMask;
+  int32_t res[16];
+  float lo[3], inv[3];
+  float vmin, vrange;
+} exa_surrogate_geometry;
+
+void exa_surrogate_params_default(exa_surrogate_params *p);
+/* Initialises the encoding and network and draws the training pairs with
+ * the exact sampler (needs exa_sampler_build). */
+int exa_surrogate_create(exa_context *ctx, const exa_surrogate_params *p);
+/* steps training steps; loss (may be null) as in exa_surrogate_stats. */
+int exa_surrogate_train(exa_context *ctx, int32_t steps, float *loss);
+/* Probes every macrocell of the majorant grid (about pointsTarget points
+ * in all, at least 8 per macrocell), sets each macrocell's mode (learned
+ * field where it holds no empty space and its largest error is at most
+ * tolerance x value range) and the widened majorants for the current
+ * transfer function (recomputed by exa_sampler_compute_max_opacities). */
+int exa_surrogate_evaluate(exa_context *ctx, float tolerance, uint64_t pointsTarget);
+int exa_surrogate_get_stats(exa_context *ctx, exa_surrogate_stats *out);
+int exa_surrogate_get_geometry(exa_context *ctx, exa_surrogate_geometry *out);
+/* Learned-field values at n device positions (device output). */
+int exa_surrogate_sample_points(exa_context *ctx, const exa_vec3f *posDevice, uint64_t n, float *outDevice);
+/* FP32 master parameters, host arrays: weights 6208 floats (W1 64x32,
+ * W2 64x64, w3 64, row-major out x in); table 2 x 16 x 2^log2TableSize
+ * floats (level-major, feature pairs).  Either pointer may be null. */
+int exa_surrogate_get_params(exa_context *ctx, float *weights, float *table);
+int exa_surrogate_set_params(exa_context *ctx, const float *weights, const float *table);
+/* Gradients of the training loss over n pairs (host float x 4: x, y, z,
+ * value; NaN value = no sample) at the current parameters, without a
+ * step: host outputs as in exa_surrogate_get_params (either may be null). */
+int exa_surrogate_gradients(exa_context *ctx, const float *pairs, int32_t n, float *gWeights, float *gTable,
+                            float *loss);
+/* Per-macrocell results of exa_surrogate_evaluate, host arrays of
+ * numMacrocells (any may be null): mode 1 = learned field, largest
+ * measured |error| in value units, widened majorant. */
+int exa_surrogate_get_macrocells(exa_context *ctx, uint8_t *mode, double *maxError, float *majorants);
+/* exa_render with the learned field in the macrocells that use it. */
+int exa_render_surrogate(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,24 @@ void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
                    int height, int64_t pixelBegin, int64_t pixelEnd,
                    double *outRGB, int nthreads);
 
+/* ---- learned field (surrogate.c): hash-grid encoding + MLP ---- */
+typedef struct os_geom {
+  int32_t log2T;
+  uint32_t denseMask;
+  int32_t res[16];
+  float lo[3], inv[3];
+  float vmin, vrange;
+} os_geom;
+float os_bf16(float f);
+void os_set_exact(int on);
+float os_half(float f);
+void os_geom_init(os_geom *g, int log2T, int baseRes, float growth, const float lo[3], const float hi[3], float vmin,
+                  float vmax);
+void os_encode(const os_geom *g, const float *table, const float pos[3], int half, float feat[32]);
+void os_forward(const os_geom *g, const float *w, const float *table, const float *pos, int64_t n, double *y);
+double os_gradients(const os_geom *g, const float *w, const float *table, const float *pairs, int n, double *gW,
+                    double *gTable);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,16 @@ def lib():
         L.oc_render.restype = C.c_uint32
         L.oc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int]
         L.oc_render_f64.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, vp, C.c_int]
+        L.os_bf16.restype = C.c_float
+        L.os_bf16.argtypes = [C.c_float]
+        L.os_set_exact.argtypes = [C.c_int]
+        L.os_half.restype = C.c_float
+        L.os_half.argtypes = [C.c_float]
+        L.os_geom_init.argtypes = [vp, C.c_int, C.c_int, C.c_float, vp, vp, C.c_float, C.c_float]
+        L.os_encode.argtypes = [vp, vp, vp, C.c_int, vp]
+        L.os_forward.argtypes = [vp, vp, vp, vp, C.c_int64, vp]
+        L.os_gradients.restype = C.c_double
+        L.os_gradients.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp]
         _lib = L
     return _lib
 
@@ -292,3 +302,47 @@ def ref_dda3(org, dirv, tmin, tmax, dims, lo, hi, max_cells=4096):
     n = R.ref_dda3(_ptr(o), _ptr(dv), float(tmin), float(tmax), _ptr(d), _ptr(b), max_cells,
                    _ptr(ids), _ptr(t0), _ptr(t1))
     return ids[:n], t0[:n], t1[:n]
+
+
+# ------------------------------------------------------------ learned field
+class SurGeom(C.Structure):
+    """os_geom (oracle.h); same layout as exa_surrogate_geometry."""
+    _fields_ = [("log2T", C.c_int32), ("denseMask", C.c_uint32), ("res", C.c_int32 * 16),
+                ("lo", C.c_float * 3), ("inv", C.c_float * 3), ("vmin", C.c_float), ("vrange", C.c_float)]
+
+
+def sur_geom(log2T, base_res, growth, lo, hi, vmin, vmax):
+    g = SurGeom()
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    lib().os_geom_init(C.byref(g), int(log2T), int(base_res), float(growth), _ptr(lo), _ptr(hi), float(vmin),
+                       float(vmax))
+    return g
+
+
+def sur_encode(geom, table, pos, half=False):
+    table = np.ascontiguousarray(table, np.float32)
+    p = np.ascontiguousarray(pos, np.float32)
+    out = np.zeros(32, np.float32)
+    lib().os_encode(C.byref(geom), _ptr(table), _ptr(p), int(bool(half)), _ptr(out))
+    return out
+
+
+def sur_forward(geom, weights, table, pos):
+    """normalised outputs y of the inference path (binary16 table)"""
+    w = np.ascontiguousarray(weights, np.float32)
+    t = np.ascontiguousarray(table, np.float32)
+    p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    y = np.zeros(len(p), np.float64)
+    lib().os_forward(C.byref(geom), _ptr(w), _ptr(t), _ptr(p), len(p), _ptr(y))
+    return y
+
+
+def sur_gradients(geom, weights, table, pairs):
+    w = np.ascontiguousarray(weights, np.float32)
+    t = np.ascontiguousarray(table, np.float32)
+    pr = np.ascontiguousarray(pairs, np.float32).reshape(-1, 4)
+    gw = np.zeros(len(w), np.float64)
+    gt = np.zeros(len(t), np.float64)
+    loss = lib().os_gradients(C.byref(geom), _ptr(w), _ptr(t), _ptr(pr), len(pr), _ptr(gw), _ptr(gt))
+    return gw, gt, loss

@@ -456,6 +456,8 @@ struct exa_context {
   exa_render_stats lastStats{};
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
+  std::unique_ptr<Surrogate> surrogate;
+  float surrogateTol = 0.f;
 };
 
 namespace {
@@ -488,6 +490,72 @@ void need(bool c, int code, const char *msg)
 void setDevice(exa_context *ctx) { cudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice"); }
 } // namespace
 
+namespace {
+void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height, bool learned)
+{
+  {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(lp != nullptr, EXA_ERR_INVALID, "null lp");
+    need(width > 0 && height > 0, EXA_ERR_INVALID, "bad frame size");
+    need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
+    need((long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp->render.spp < 0xffffffffll, EXA_ERR_INVALID,
+         "frame too large: width*height*spp must stay below 2^32 samples per launch");
+    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
+         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
+         "shade mode not supported");
+    need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
+    need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
+    need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
+    need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
+         "lp.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
+    need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
+         "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
+    need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    setDevice(ctx);
+    const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
+    if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
+    exa_launch_params lpUse = *lp;
+    SurrogateView sv{};
+    if (learned) {
+      Surrogate *S = ctx->surrogate.get();
+      need(S && S->evaluated, EXA_ERR_STATE, "no evaluated surrogate (call exa_surrogate_evaluate)");
+      const exa_vec3i d = ctx->model->grid->dims;
+      need(d.x == S->evalDims.x && d.y == S->evalDims.y && d.z == S->evalDims.z, EXA_ERR_STATE,
+           "majorant grid changed since exa_surrogate_evaluate");
+      need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT, EXA_ERR_INVALID, "the learned field renders shade mode default only");
+      lpUse.maxOpacities = S->majorants.ptr;
+      sv = S->deviceView();
+    }
+    if (useWavefront() || learned) {
+      // queue capacity: the frame's samples, at most 4M records in flight
+      const unsigned cap = (unsigned)std::min<size_t>((size_t)((width + 15) / 16) * ((height + 7) / 8) * 128 *
+                                                          (size_t)lp->render.spp, (size_t)1 << 22);
+      if (ctx->wfCap < cap) {
+        ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
+        ctx->wfCounters.alloc(4);
+        ctx->wfCap = cap;
+      }
+      WfStats st;
+      renderWavefront(ctx->sampler->accel, lpUse, width, height, ctx->sampleColors.ptr, ctx->wfRecords.ptr, ctx->wfCap,
+                      ctx->wfCounters.ptr, ctx->stream, &st, learned ? &sv : nullptr);
+      ctx->lastStats.wavefront = 1;
+      ctx->lastStats.rounds = st.rounds;
+      ctx->lastStats.peakQueue = st.peakQueue;
+      ctx->lastStats.queueCapacity = ctx->wfCap;
+      ctx->lastStats.walkLaunches = st.walkLaunches;
+      ctx->lastStats.cameraMs = st.cameraMs;
+      ctx->lastStats.walkMs = st.walkMs;
+      ctx->lastStats.eventMs = st.eventMs;
+    } else {
+      ctx->lastStats = exa_render_stats{};
+      launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
+    }
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *exa_version(void) { return "exastitch-gb300 0.1 (sm_103a)"; }
@@ -500,6 +568,9 @@ uint64_t exa_abi_sizeof(int32_t which)
     case 2: return sizeof(exa_sample);
     case 3: return sizeof(exa_mem_stats);
     case 4: return sizeof(exa_lp_ext);
+    case 5: return sizeof(exa_surrogate_params);
+    case 6: return sizeof(exa_surrogate_stats);
+    case 7: return sizeof(exa_surrogate_geometry);
     default: return 0;
   }
 }
@@ -675,6 +746,8 @@ int exa_sampler_compute_max_opacities(exa_context *ctx, const exa_vec4f *colorMa
     ctx->sampler->computeMaxOpacities(colorMap, numColors, xfRange, ctx->stream);
     ctx->xfRange = xfRange;
     ctx->numColors = numColors;
+    if (ctx->surrogate && ctx->surrogate->evaluated)
+      ctx->surrogate->computeMajorants(ctx->sampler->colorMap.ptr, numColors, xfRange, ctx->stream);
   });
 }
 
@@ -805,53 +878,240 @@ int exa_launch_params_init(exa_launch_params *lp)
 
 int exa_render(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height)
 {
+  return guarded([&] { renderFrame(ctx, lp, width, height, false); });
+}
+
+// ------------------------------------------------------------ learned field
+void exa_surrogate_params_default(exa_surrogate_params *p)
+{
+  if (!p) return;
+  const SurrogateConfig c;
+  std::memset(p, 0, sizeof(*p));
+  p->log2TableSize = c.log2T;
+  p->baseResolution = c.baseRes;
+  p->growth = c.growth;
+  p->importanceFraction = c.importance;
+  p->numSamples = c.numSamples;
+  p->batch = c.batch;
+  p->learningRate = c.lrTable;
+  p->learningRateFinal = c.lrFinal;
+  p->seed = c.seed;
+}
+
+int exa_surrogate_create(exa_context *ctx, const exa_surrogate_params *p)
+{
   return guarded([&] {
     need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
-    need(lp != nullptr, EXA_ERR_INVALID, "null lp");
-    need(width > 0 && height > 0, EXA_ERR_INVALID, "bad frame size");
-    need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
-    need((long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp->render.spp < 0xffffffffll, EXA_ERR_INVALID,
-         "frame too large: width*height*spp must stay below 2^32 samples per launch");
-    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
-         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
-    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
-         "shade mode not supported");
-    need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
-    need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
-    need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
-    need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
-         "lp.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
-    need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
-         "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
-    need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    need(p != nullptr, EXA_ERR_INVALID, "null params");
+    need(p->numSamples >= 32 && p->numSamples <= ((uint64_t)1 << 28), EXA_ERR_INVALID, "numSamples out of range");
+    need(p->baseResolution >= 1 && p->growth >= 1.f && p->growth <= 4.f, EXA_ERR_INVALID, "bad grid resolutions");
+    need(p->importanceFraction >= 0.f && p->importanceFraction <= 1.f, EXA_ERR_INVALID, "bad importance fraction");
+    need(p->learningRate > 0.f && p->learningRateFinal > 0.f, EXA_ERR_INVALID, "bad learning rate");
     setDevice(ctx);
-    const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
-    if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
-    if (useWavefront()) {
-      // queue capacity: the frame's samples, at most 4M records in flight
-      const unsigned cap = (unsigned)std::min<size_t>((size_t)((width + 15) / 16) * ((height + 7) / 8) * 128 *
-                                                          (size_t)lp->render.spp, (size_t)1 << 22);
-      if (ctx->wfCap < cap) {
-        ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
-        ctx->wfCounters.alloc(4);
-        ctx->wfCap = cap;
-      }
-      WfStats st;
-      renderWavefront(ctx->sampler->accel, *lp, width, height, ctx->sampleColors.ptr, ctx->wfRecords.ptr, ctx->wfCap,
-                      ctx->wfCounters.ptr, ctx->stream, &st);
-      ctx->lastStats.wavefront = 1;
-      ctx->lastStats.rounds = st.rounds;
-      ctx->lastStats.peakQueue = st.peakQueue;
-      ctx->lastStats.queueCapacity = ctx->wfCap;
-      ctx->lastStats.walkLaunches = st.walkLaunches;
-      ctx->lastStats.cameraMs = st.cameraMs;
-      ctx->lastStats.walkMs = st.walkMs;
-      ctx->lastStats.eventMs = st.eventMs;
-    } else {
-      ctx->lastStats = exa_render_stats{};
-      launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
-    }
+    SurrogateConfig c;
+    c.log2T = p->log2TableSize;
+    c.baseRes = p->baseResolution;
+    c.growth = p->growth;
+    c.importance = p->importanceFraction;
+    c.numSamples = (size_t)p->numSamples;
+    c.batch = p->batch;
+    c.lrTable = c.lrMlp = p->learningRate;
+    c.lrFinal = p->learningRateFinal;
+    c.seed = p->seed;
+    auto S = std::make_unique<Surrogate>();
+    S->configure(c, *ctx->model);
+    S->allocate(ctx->stream);
+    S->generateSamples(*ctx->sampler, ctx->stream);
+    ctx->surrogate = std::move(S);
   });
+}
+
+int exa_surrogate_train(exa_context *ctx, int32_t steps, float *loss)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate, EXA_ERR_STATE, "no surrogate");
+    need(steps >= 0, EXA_ERR_INVALID, "negative steps");
+    setDevice(ctx);
+    const float l = steps > 0 ? ctx->surrogate->trainSteps(steps, ctx->stream) : ctx->surrogate->lastLoss;
+    ctx->surrogate->evaluated = false;  // the network changed: errors must be measured again
+    if (loss) *loss = l;
+  });
+}
+
+int exa_surrogate_evaluate(exa_context *ctx, float tolerance, uint64_t pointsTarget)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate && ctx->sampler, EXA_ERR_STATE, "no surrogate");
+    need(tolerance >= 0.f, EXA_ERR_INVALID, "negative tolerance");
+    need(ctx->sampler->hasTF && ctx->numColors > 0, EXA_ERR_STATE, "no transfer function (compute max opacities first)");
+    setDevice(ctx);
+    Surrogate &S = *ctx->surrogate;
+    const Grid &g = *ctx->model->grid;
+    S.evaluate(*ctx->sampler, g, (double)tolerance, (size_t)std::max<uint64_t>(pointsTarget, 1), ctx->stream);
+    S.computeMajorants(ctx->sampler->colorMap.ptr, ctx->numColors, ctx->xfRange, ctx->stream);
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "surrogate majorants");
+    ctx->surrogateTol = tolerance;
+  });
+}
+
+namespace {
+// exact-field bytes the exact-sampler macrocells still need: primitives
+// whose bounds touch a macrocell in exact mode, plus the point-location
+// structures
+size_t fallbackBytes(exa_context *ctx)
+{
+  const ExaStitchModel &m = *ctx->model;
+  const Grid &g = *m.grid;
+  const size_t nmc = (size_t)g.dims.x * g.dims.y * g.dims.z;
+  std::vector<uint8_t> mode(nmc);
+  cudaCheck(cudaMemcpy(mode.data(), ctx->surrogate->mcMode.ptr, nmc, cudaMemcpyDeviceToHost), "d2h");
+  const exa_box3f wb = g.worldBounds;
+  auto proj = [&](float v, float lo, float hi, int d) {
+    int i = (int)((v - lo) / (hi - lo) * (float)d);
+    return i < 0 ? 0 : (i > d - 1 ? d - 1 : i);
+  };
+  auto touchesExact = [&](exa_vec3f lo, exa_vec3f hi) {
+    const int x0 = proj(lo.x, wb.lower.x, wb.upper.x, g.dims.x), x1 = proj(hi.x, wb.lower.x, wb.upper.x, g.dims.x);
+    const int y0 = proj(lo.y, wb.lower.y, wb.upper.y, g.dims.y), y1 = proj(hi.y, wb.lower.y, wb.upper.y, g.dims.y);
+    const int z0 = proj(lo.z, wb.lower.z, wb.upper.z, g.dims.z), z1 = proj(hi.z, wb.lower.z, wb.upper.z, g.dims.z);
+    for (int z = z0; z <= z1; ++z)
+      for (int y = y0; y <= y1; ++y)
+        for (int x = x0; x <= x1; ++x)
+          if (!mode[((size_t)z * g.dims.y + y) * g.dims.x + x]) return true;
+    return false;
+  };
+  size_t bytes = ctx->sampler->accelBytes();
+  for (const exa_gridlet &gl : m.gridlets) {
+    const float cw = (float)(1 << gl.level);
+    const exa_vec3f lo{((float)gl.lower.x + 0.5f) * cw, ((float)gl.lower.y + 0.5f) * cw, ((float)gl.lower.z + 0.5f) * cw};
+    const exa_vec3f hi{((float)(gl.lower.x + gl.dims.x) + 0.5f) * cw, ((float)(gl.lower.y + gl.dims.y) + 0.5f) * cw,
+                       ((float)(gl.lower.z + gl.dims.z) + 0.5f) * cw};
+    if (touchesExact(lo, hi))
+      bytes += sizeof(exa_gridlet) + sizeof(float) * (size_t)(gl.dims.x + 1) * (gl.dims.y + 1) * (gl.dims.z + 1);
+  }
+  const size_t ne = m.indices.size() / 8;
+  std::vector<uint8_t> vertUsed(m.vertices.size(), 0);
+  for (size_t e = 0; e < ne; ++e) {
+    exa_vec3f lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
+    for (int j = 0; j < 8; ++j) {
+      const int id = m.indices[e * 8 + j];
+      if (id < 0) break;
+      const exa_vec4f &v = m.vertices[id];
+      lo = {std::min(lo.x, v.x), std::min(lo.y, v.y), std::min(lo.z, v.z)};
+      hi = {std::max(hi.x, v.x), std::max(hi.y, v.y), std::max(hi.z, v.z)};
+    }
+    if (!touchesExact(lo, hi)) continue;
+    bytes += 8 * sizeof(int32_t);
+    for (int j = 0; j < 8; ++j) {
+      const int id = m.indices[e * 8 + j];
+      if (id < 0) break;
+      if (!vertUsed[id]) { vertUsed[id] = 1; bytes += sizeof(exa_vec4f); }
+    }
+  }
+  return bytes;
+}
+}  // namespace
+
+int exa_surrogate_get_stats(exa_context *ctx, exa_surrogate_stats *out)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate && out, EXA_ERR_STATE, "no surrogate");
+    setDevice(ctx);
+    const Surrogate &S = *ctx->surrogate;
+    std::memset(out, 0, sizeof(*out));
+    out->loss = S.lastLoss;
+    out->steps = S.step;
+    out->tolerance = ctx->surrogateTol;
+    out->rmse = S.stats.rmse;
+    out->maxError = S.stats.maxError;
+    out->probePoints = S.stats.probePoints;
+    out->numMacrocells = S.stats.numMacrocells;
+    out->numSurrogateMacrocells = S.stats.numSurrogateMCs;
+    out->tableBytes = S.table16.bytes();
+    out->weightBytes = S.wbf.bytes();
+    out->inferenceBytes = S.inferenceBytes();
+    const ExaStitchSampler &sm = *ctx->sampler;
+    out->fieldBytes = sm.gridletBuffer.bytes() + sm.gridletScalarBuffer.bytes() + sm.vertexBuffer.bytes() +
+                      sm.indexBuffer.bytes() + sm.accelBytes();
+    out->fallbackFieldBytes = S.evaluated ? fallbackBytes(ctx) : out->fieldBytes;
+  });
+}
+
+int exa_surrogate_get_geometry(exa_context *ctx, exa_surrogate_geometry *out)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate && out, EXA_ERR_STATE, "no surrogate");
+    const SurrogateView &v = ctx->surrogate->view;
+    std::memset(out, 0, sizeof(*out));
+    out->log2TableSize = v.log2T;
+    out->denseMask = v.denseMask;
+    for (int l = 0; l < 16; ++l) out->res[l] = v.res[l];
+    for (int a = 0; a < 3; ++a) { out->lo[a] = v.lo[a]; out->inv[a] = v.inv[a]; }
+    out->vmin = v.vmin;
+    out->vrange = v.vrange;
+  });
+}
+
+int exa_surrogate_sample_points(exa_context *ctx, const exa_vec3f *posDevice, uint64_t n, float *outDevice)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate, EXA_ERR_STATE, "no surrogate");
+    need(n == 0 || (posDevice && outDevice), EXA_ERR_INVALID, "null buffer");
+    setDevice(ctx);
+    launchSurrogatePoints(ctx->surrogate->deviceView(), posDevice, n, outDevice, ctx->stream);
+  });
+}
+
+int exa_surrogate_get_params(exa_context *ctx, float *weights, float *table)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate, EXA_ERR_STATE, "no surrogate");
+    setDevice(ctx);
+    const Surrogate &S = *ctx->surrogate;
+    if (weights) cudaCheck(cudaMemcpy(weights, S.w32.ptr, S.w32.bytes(), cudaMemcpyDeviceToHost), "d2h");
+    if (table) cudaCheck(cudaMemcpy(table, S.table.ptr, S.table.bytes(), cudaMemcpyDeviceToHost), "d2h");
+  });
+}
+
+int exa_surrogate_set_params(exa_context *ctx, const float *weights, const float *table)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate, EXA_ERR_STATE, "no surrogate");
+    setDevice(ctx);
+    Surrogate &S = *ctx->surrogate;
+    if (weights) S.setWeights(weights, ctx->stream);
+    if (table) S.setTable(table, ctx->stream);
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "surrogate params");
+    S.evaluated = false;
+  });
+}
+
+int exa_surrogate_gradients(exa_context *ctx, const float *pairs, int32_t n, float *gWeights, float *gTable,
+                            float *loss)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate, EXA_ERR_STATE, "no surrogate");
+    need(pairs != nullptr && n > 0, EXA_ERR_INVALID, "no pairs");
+    setDevice(ctx);
+    ctx->surrogate->gradients(reinterpret_cast<const float4 *>(pairs), n, gWeights, gTable, loss, ctx->stream);
+  });
+}
+
+int exa_surrogate_get_macrocells(exa_context *ctx, uint8_t *mode, double *maxError, float *majorants)
+{
+  return guarded([&] {
+    need(ctx && ctx->surrogate && ctx->surrogate->evaluated, EXA_ERR_STATE, "no evaluated surrogate");
+    setDevice(ctx);
+    const Surrogate &S = *ctx->surrogate;
+    if (mode) cudaCheck(cudaMemcpy(mode, S.mcMode.ptr, S.mcMode.bytes(), cudaMemcpyDeviceToHost), "d2h");
+    if (maxError) cudaCheck(cudaMemcpy(maxError, S.mcErr.ptr, S.mcErr.bytes(), cudaMemcpyDeviceToHost), "d2h");
+    if (majorants) cudaCheck(cudaMemcpy(majorants, S.majorants.ptr, S.majorants.bytes(), cudaMemcpyDeviceToHost), "d2h");
+  });
+}
+
+int exa_render_surrogate(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height)
+{
+  return guarded([&] { renderFrame(ctx, lp, width, height, true); });
 }
 
 } // extern "C"

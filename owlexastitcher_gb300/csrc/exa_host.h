@@ -14,6 +14,7 @@
 
 #include "../../include/exastitch.h"
 #include "exa_accel.cuh"
+#include "exa_surrogate.cuh"
 
 namespace exa {
 
@@ -174,7 +175,66 @@ struct WfStats {
   float cameraMs = 0.f, walkMs = 0.f, eventMs = 0.f;
 };
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
-                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats);
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats,
+                     const SurrogateView *sur = nullptr);
+
+// ------------------------------------------------------------ learned field
+constexpr int kSurParams = kSurHidden * kSurIn + kSurHidden * kSurHidden + kSurHidden;  // 6208
+
+struct SurrogateConfig {
+  int levels = kSurLevels;
+  int log2T = 19;
+  int baseRes = 16;
+  float growth = 1.5f;
+  size_t numSamples = (size_t)1 << 24;
+  float importance = 0.5f;  // fraction of samples inside refined gridlets
+  int batch = 1 << 18;
+  float lrTable = 1e-2f, lrMlp = 1e-2f;
+  float lrFinal = 1e-3f;  // each trainSteps call decays lr exponentially to this
+  uint64_t seed = 1234;
+};
+
+struct SurrogateStats {
+  double rmse = 0.0, maxError = 0.0;  // over the probe points, in units of the value range
+  size_t probePoints = 0, numMacrocells = 0, numSurrogateMCs = 0;
+};
+
+// hash-grid encoding + MLP trained on the exact sampler's values
+struct Surrogate {
+  SurrogateConfig cfg;
+  SurrogateView view{};  // geometry of the encoding (pointers set by deviceView)
+  DBuf<float2> table, gtable, mTable, vTable;  // FP32 master table, gradient, Adam moments
+  DBuf<__half2> table16;                       // inference copy
+  DBuf<float> w32, gw, mw, vw;                 // MLP: w1 | w2 | w3
+  DBuf<__nv_bfloat16> wbf;
+  DBuf<float4> samples;                        // (x, y, z, value or NaN)
+  DBuf<__nv_bfloat16> feats;
+  DBuf<float> dfeat, lossBuf;
+  DBuf<uint8_t> mcMode;
+  DBuf<unsigned long long> mcErr;
+  DBuf<unsigned> mcEmpty;
+  DBuf<exa_range1f> widenedRanges;
+  DBuf<float> majorants;
+  uint64_t cursor = 0;
+  int step = 0;
+  float lastLoss = 0.f;
+  bool evaluated = false;
+  exa_vec3i evalDims{0, 0, 0};
+  SurrogateStats stats;
+
+  void configure(const SurrogateConfig &c, const ExaStitchModel &model);
+  void allocate(cudaStream_t s);
+  void setWeights(const float *w, cudaStream_t s);
+  void setTable(const float *t, cudaStream_t s);
+  void generateSamples(const ExaStitchSampler &sampler, cudaStream_t s);
+  float trainSteps(int steps, cudaStream_t s);
+  void gradients(const float4 *hostSamples, int n, float *gW, float *gTable, float *loss, cudaStream_t s);
+  void evaluate(const ExaStitchSampler &sampler, const Grid &grid, double tol, size_t pointsTarget, cudaStream_t s);
+  void computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, cudaStream_t s);
+  SurrogateView deviceView() const;
+  size_t inferenceBytes() const;
+};
+void launchSurrogatePoints(const SurrogateView &S, const exa_vec3f *pos, size_t n, float *out, cudaStream_t s);
 bool useWavefront();
 constexpr int kWfLaneWords = 61;
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,

@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "exa_host.h"
+#include "exa_surrogate.cuh"
 
 namespace exa {
 
@@ -25,7 +26,8 @@ constexpr int kTrackCap = 1 << 22;  // delta / ratio tracking steps per macrocel
 // work counters of a counting launch (lp.ext.stepCounters set); the index is
 // the slot in stepCounters
 enum : int {
-  CNT_FIELD, CNT_GRIDLET, CNT_ELEM, CNT_DDA, CNT_PATHS, CNT_MISS, CNT_TABLES, CNT_GTESTS, CNT_BVH, CNT_WALKS, CNT_N
+  CNT_FIELD, CNT_GRIDLET, CNT_ELEM, CNT_DDA, CNT_PATHS, CNT_MISS, CNT_TABLES, CNT_GTESTS, CNT_BVH, CNT_WALKS,
+  CNT_SURR, CNT_VIOL, CNT_N
 };
 // one column per thread in shared memory, so that an ordinary launch holds no
 // registers for them; every render kernel runs 128 threads per block
@@ -213,7 +215,12 @@ EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
   w.needCell = true;
 }
 
-EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
+// walk_advance: the DDA advance and the free flight of one step.
+// Returns 0 when the walk ended, 1 when the step took no sample (the flight
+// left the macrocell), 2 when a sample at w.pos is due.
+enum : int { WALK_END = 0, WALK_ON = 1, WALK_SAMPLE = 2 };
+
+EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
 {
   const exa_launch_params &lp = c.lp;
   const exa_grid_traversable &G = lp.majorantGrid;
@@ -221,7 +228,7 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
   while (w.needCell) {
     if (++w.ncells > G.dims.x + G.dims.y + G.dims.z + 3) {
       c.err |= EXA_DEVERR_DDA_CAP;
-      return false;
+      return WALK_END;
     }
     w.t1 = fmin_t(rmin3(w.dda.tnext), w.dda.tmax);
     const int leafID = (w.dda.cell.z * G.dims.y + w.dda.cell.y) * G.dims.x + w.dda.cell.x;
@@ -231,25 +238,32 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
     w.primID = -1;
     w.steps = 0;
     if (w.maj <= 0.f) {
-      if (!dda_next(w.dda)) return false;
+      if (!dda_next(w.dda)) return WALK_END;
       continue;
     }
     w.needCell = false;
   }
   if (++w.steps > kTrackCap) {
     c.err |= EXA_DEVERR_TRACK_CAP;
-    return false;
+    return WALK_END;
   }
   w.t -= __fdiv_rn(exa_log(1.f - rng.next()), w.maj * scale);
   if (w.t >= w.t1) {
     w.needCell = true;
-    return dda_next(w.dda);
+    return dda_next(w.dda) ? WALK_ON : WALK_END;
   }
   w.pos = add3(w.org, muls(w.dir, w.t));
+  return WALK_SAMPLE;
+}
+
+// the exact sampler at w.pos: the cached gridlet first (testSample,
+// deviceCode.cu:749), then the full point location
+EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
+{
   exa_sample s = test_sample(c.A, w.pos, w.primID);
   if (s.primID < 0) {
     QueryStats q{0u, 0u, 0u};
-    s = sample_field(c.A, w.pos, lp.ext.cullTransparentPrims != 0, c.err, &q);
+    s = sample_field(c.A, w.pos, c.lp.ext.cullTransparentPrims != 0, c.err, &q);
     if (c.counting) {
       cnt_add(c, CNT_MISS);
       cnt_add(c, CNT_TABLES, q.tables);
@@ -261,10 +275,21 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
     cnt_add(c, CNT_FIELD);
     if (s.primID >= 0) cnt_add(c, s.cellID != -1 ? CNT_GRIDLET : CNT_ELEM);
   }
-  if (s.primID < 0) return true;
+  return s;
+}
+
+// the collision test of one step given its sample; primID -1 is empty
+// space, -2 a value of the learned field (never cached).  Returns false
+// when the walk ended.
+EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const exa_sample &s)
+{
+  const exa_launch_params &lp = c.lp;
+  const float scale = lp.transferFunc.opacityScale;
+  if (s.primID == -1) return true;
   if (s.cellID != -1) w.primID = s.primID;
   w.xf = classify(c.A, lp, s);
   const float sigmaT = w.xf.w;
+  if (s.primID == -2 && c.counting && sigmaT * scale > w.maj) cnt_add(c, CNT_VIOL);
   if (!shadow) {
     const float u = rng.next();
     if (sigmaT * scale >= u * w.maj) {
@@ -280,6 +305,14 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
     }
   }
   return true;
+}
+
+EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
+{
+  const int st = walk_advance(w, c, rng);
+  if (st != WALK_SAMPLE) return st == WALK_ON;
+  const exa_sample s = walk_sample_exact(w, c);
+  return walk_collide(w, c, rng, shadow, s);
 }
 
 // ------------------------------------------------------------------------
@@ -1009,6 +1042,89 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
   flush_counters(c, lp);
 }
 
+// walks with the learned field: k_wf_walk with the sample of a step taken
+// from the surrogate in macrocells marked for it (one warp-wide evaluation
+// per iteration for all lanes that need one) and from the exact sampler
+// elsewhere; lp.maxOpacities holds the widened majorants.  Dynamic shared
+// memory: the network and the warps' scratch (kSurWalkSmem bytes).
+constexpr size_t kSurWalkSmem = sizeof(SurWeightsSmem) + 4 * sizeof(SurWarpSmem);
+
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(const __grid_constant__ AccelView A,
+                                                                            const __grid_constant__ exa_launch_params lp,
+                                                                            WfQueues Q,
+                                                                            const __grid_constant__ SurrogateView S)
+{
+  extern __shared__ __align__(16) unsigned char surSm[];
+  SurWeightsSmem &W = *reinterpret_cast<SurWeightsSmem *>(surSm);
+  SurWarpSmem &ws = reinterpret_cast<SurWarpSmem *>(surSm + sizeof(SurWeightsSmem))[threadIdx.x >> 5];
+  sur_load_weights(W, S);
+  __syncthreads();
+  PathCtx c = make_ctx(A, lp);
+  const exa_grid_traversable &G = lp.majorantGrid;
+  const unsigned n = Q.cnt[0];
+  const unsigned lane = threadIdx.x & 31;
+  Lane L;
+  bool active = false, exhausted = false;
+  unsigned src = 0;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need && !exhausted) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(&Q.cnt[3], (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (unsigned)__popc(need) >= n) exhausted = true;
+      if (!active) {
+        const unsigned idx = base + __popc(need & ((1u << lane) - 1u));
+        if (idx < n) {
+          wf_load_walk(L, Q.in, Q.cap, idx, lp.majorantGrid);
+          active = true;
+          src = idx;
+          cnt_add(c, CNT_WALKS);
+        }
+      }
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES) {
+      const unsigned slot = warp_append(&Q.cnt[1], active);
+      if (active) {
+        wf_store_walk(L, Q.out, Q.cap, slot);
+        wf_copy_path(Q.in, src, Q.out, slot, Q.cap);
+      }
+      break;
+    }
+    const int st = active ? walk_advance(L.w, c, L.rng) : WALK_END;
+    bool sur = false;
+    exa_sample s;
+    s.primID = -1;
+    s.cellID = -1;
+    s.value = 0.f;
+    if (st == WALK_SAMPLE) {
+      const int leafID = (L.w.dda.cell.z * G.dims.y + L.w.dda.cell.y) * G.dims.x + L.w.dda.cell.x;
+      sur = __ldg(S.mcMode + leafID) != 0;
+      if (!sur) s = walk_sample_exact(L.w, c);
+    }
+    if (__any_sync(0xffffffffu, sur)) {
+      const float y = sur_eval_warp(S, W, ws, L.w.pos, sur);
+      if (sur) {
+        s.primID = -2;
+        s.value = S.vmin + y * S.vrange;
+        cnt_add(c, CNT_SURR);
+      }
+    }
+    const bool ended =
+        active && (st == WALK_END || (st == WALK_SAMPLE && !walk_collide(L.w, c, L.rng, L.shadow, s)));
+    const unsigned slot = warp_append(&Q.cnt[2], ended);
+    if (ended) {
+      wf_store_walk(L, Q.ev, Q.cap, slot);
+      wf_copy_path(Q.in, src, Q.ev, slot, Q.cap);
+      active = false;
+    }
+  }
+  flush_counters(c, lp);
+}
+
 // walk ends: the integrator step after a primary or shadow walk
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ AccelView A,
@@ -1038,7 +1154,8 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
 // host loop of the wavefront renderer; synchronizes the stream once per
 // round to read the queue sizes
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
-                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats)
+                     uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats,
+                     const SurrogateView *sur)
 {
   const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
   int dev = 0, sms = 152;
@@ -1052,7 +1169,13 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   int inIdx = 0, outIdx = 1;
   const unsigned grid = (unsigned)sms * 16;
   int perSM = 4;
-  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk, 128, 0), "occupancy");
+  if (sur) {
+    cudaCheck(cudaFuncSetAttribute(k_wf_walk_sur, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSurWalkSmem),
+              "walk smem");
+    cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk_sur, 128, kSurWalkSmem), "occupancy");
+  } else {
+    cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk, 128, 0), "occupancy");
+  }
   const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
   // per-kernel-class timing on this stream: camera, walk, events
   cudaEvent_t ev[4];
@@ -1076,7 +1199,8 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
       issued += nNew;
     }
     cudaCheck(cudaEventRecord(ev[1], s), "event");
-    k_wf_walk<<<walkGrid, 128, 0, s>>>(A, lp, Q);
+    if (sur) k_wf_walk_sur<<<walkGrid, 128, kSurWalkSmem, s>>>(A, lp, Q, *sur);
+    else k_wf_walk<<<walkGrid, 128, 0, s>>>(A, lp, Q);
     cudaCheck(cudaEventRecord(ev[2], s), "event");
     if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
     else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);

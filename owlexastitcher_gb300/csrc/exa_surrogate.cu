@@ -1,0 +1,796 @@
+// exa_surrogate.cu -- training, error bounds and majorants of the learned
+// field (hash-grid encoding + MLP, exa_surrogate.cuh).  No counterpart in
+// the reference: this is the learned stand-in beside the exact ExaStitch
+// sampler.
+//
+// Training data: (position, value) pairs drawn by the exact sampler
+// (sample() of sampler/ExaStitchSampler.h:128-140, here sample_field), half
+// uniform over the cell bounds and half uniform inside gridlets of the
+// refined levels.  One training step on a batch of B pairs is three kernels:
+//   k_sur_encode_fwd  encoding of the batch from the FP32 master table
+//                     (one thread per pair) -> BF16 inputs [B][32]
+//   k_sur_mlp_train   forward and backward of the MLP on the tensor cores,
+//                     32 pairs per warp; weight gradients summed per block in
+//                     shared memory; input gradients [B][32] FP32
+//   k_sur_encode_bwd  scatter of the input gradients into the table
+//                     gradient (float2 atomics)
+// then Adam over the table and the weights, which also refreshes the FP16
+// table and BF16 weights used for inference.
+//
+// Error bounds: every macrocell is probed on a jittered s^3 lattice; the
+// largest |surrogate - exact| (FP64) of a macrocell widens its value range
+// before the max-opacity lookup, and a macrocell whose error exceeds the
+// tolerance, or that holds empty space, keeps the exact sampler.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "exa_host.h"
+#include "exa_surrogate.cuh"
+
+namespace exa {
+
+namespace {
+
+inline unsigned gridFor(size_t n, unsigned bs)
+{
+  const size_t g = (n + bs - 1) / bs;
+  return (unsigned)std::min<size_t>(g, 1u << 30);
+}
+
+EXA_HD float u01(uint64_t key, uint64_t n)
+{
+  return (float)(uint32_t)(mix64(key + n * 0x9e3779b97f4a7c15ull) >> 40) * 5.96046448e-08f;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------- training data
+// samples[i] = (x, y, z, value); value is NaN where no primitive holds the
+// point.  The first nUniform are uniform over the bounds, the rest uniform
+// inside a gridlet picked uniformly from refined[].
+__global__ void k_sur_samples(const __grid_constant__ AccelView A, exa_box3f bounds, size_t n, size_t nUniform,
+                              const int32_t *__restrict__ refined, int numRefined, uint64_t seed, float4 *out)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t key = mix64(seed ^ mix64(i + 0x632be59bd9b4e019ull));
+  V3 pos;
+  if (i < nUniform || numRefined == 0) {
+    pos = mk3(bounds.lower.x + u01(key, 1) * (bounds.upper.x - bounds.lower.x),
+              bounds.lower.y + u01(key, 2) * (bounds.upper.y - bounds.lower.y),
+              bounds.lower.z + u01(key, 3) * (bounds.upper.z - bounds.lower.z));
+  } else {
+    const int pick = min((int)(u01(key, 4) * (float)numRefined), numRefined - 1);
+    const exa_gridlet g = A.gridlets[refined[pick]];
+    const float cw = (float)(1 << g.level);
+    const V3 lo = muls(mk3((float)g.lower.x + 0.5f, (float)g.lower.y + 0.5f, (float)g.lower.z + 0.5f), cw);
+    pos = mk3(lo.x + u01(key, 1) * (float)g.dims.x * cw, lo.y + u01(key, 2) * (float)g.dims.y * cw,
+              lo.z + u01(key, 3) * (float)g.dims.z * cw);
+  }
+  uint32_t err = 0;
+  const exa_sample s = sample_field(A, pos, false, err);
+  out[i] = make_float4(pos.x, pos.y, pos.z, s.primID >= 0 ? s.value : __int_as_float(0x7fc00000));
+}
+
+// ------------------------------------------------------- encoding, forward
+__global__ void k_sur_encode_fwd(const __grid_constant__ SurrogateView S, const float2 *__restrict__ table,
+                                 const float4 *__restrict__ samples, size_t first, size_t numSamples, int B,
+                                 __nv_bfloat16 *feats)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  const float4 sp = samples[(first + (size_t)i) % numSamples];
+  const V3 x = sur_normalize(S, mk3(sp.x, sp.y, sp.z));
+  const size_t T = (size_t)1 << S.log2T;
+  uint32_t packed[kSurIn / 2];
+  for (int l = 0; l < kSurLevels; ++l) {
+    uint32_t idx[8];
+    float w[8];
+    sur_corners(S, l, x, idx, w);
+    float f0 = 0.f, f1 = 0.f;
+    const float2 *tab = table + (size_t)l * T;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float2 e = __ldg(tab + idx[k]);
+      f0 += w[k] * e.x;
+      f1 += w[k] * e.y;
+    }
+    const __nv_bfloat162 v = __floats2bfloat162_rn(f0, f1);
+    packed[l] = *reinterpret_cast<const uint32_t *>(&v);
+  }
+  uint4 *dst = reinterpret_cast<uint4 *>(feats + (size_t)i * kSurIn);
+  for (int q = 0; q < 4; ++q) dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+}
+
+// ------------------------------------------------------ encoding, backward
+__global__ void k_sur_encode_bwd(const __grid_constant__ SurrogateView S, const float4 *__restrict__ samples,
+                                 size_t first, size_t numSamples, int B, const float *__restrict__ dfeat, float2 *gtable)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  const float4 sp = samples[(first + (size_t)i) % numSamples];
+  const V3 x = sur_normalize(S, mk3(sp.x, sp.y, sp.z));
+  const size_t T = (size_t)1 << S.log2T;
+  const float *d = dfeat + (size_t)i * kSurIn;
+  for (int l = 0; l < kSurLevels; ++l) {
+    const float g0 = d[2 * l], g1 = d[2 * l + 1];
+    if (g0 == 0.f && g1 == 0.f) continue;
+    uint32_t idx[8];
+    float w[8];
+    sur_corners(S, l, x, idx, w);
+    float2 *tab = gtable + (size_t)l * T;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) atomicAdd(tab + idx[k], make_float2(w[k] * g0, w[k] * g1));
+  }
+}
+
+// ------------------------------------------------------------ MLP training
+struct alignas(16) TrainSmem {
+  __nv_bfloat16 w1[kSurHidden * kSurLdIn];    // [64][40]  W1 (j, i)
+  __nv_bfloat16 w1t[kSurIn * kSurLdHid];      // [32][72]  W1^T (i, j)
+  __nv_bfloat16 w2[kSurHidden * kSurLdHid];   // [64][72]  W2 (j, i)
+  __nv_bfloat16 w2t[kSurHidden * kSurLdHid];  // [64][72]  W2^T (i, j)
+  float w3[kSurHidden];
+  float gw1[kSurHidden * kSurIn];
+  float gw2[kSurHidden * kSurHidden];
+  float gw3[kSurHidden];
+  float loss;
+};
+
+struct alignas(16) TrainWarpSmem {
+  __nv_bfloat16 a[32 * kSurLdIn];         // inputs (r, i)
+  __nv_bfloat16 at[kSurIn * kSurLdIn];    // inputs^T (i, r)
+  __nv_bfloat16 h1[32 * kSurLdHid];       // (r, j)
+  __nv_bfloat16 h1t[kSurHidden * kSurLdIn];  // (j, r)
+  __nv_bfloat16 h2[32 * kSurLdHid];       // (r, j), then d1 (r, i)
+  __nv_bfloat16 d2[32 * kSurLdHid];       // (r, j), then din as FP32 [32][36]
+  __nv_bfloat16 d2t[kSurHidden * kSurLdIn];  // (j, r)
+  __nv_bfloat16 d1t[kSurHidden * kSurLdIn];  // (i, r)
+};
+constexpr int kTrainWarps = 4;
+constexpr size_t kTrainSmemBytes = sizeof(TrainSmem) + kTrainWarps * sizeof(TrainWarpSmem);
+static_assert(sizeof(TrainSmem) % 16 == 0 && sizeof(TrainWarpSmem) % 16 == 0, "16-byte rows");
+
+EXA_D void st_bf16x2(__nv_bfloat16 *p, float a, float b) { *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(a, b); }
+
+// Forward and backward of the MLP for B pairs (32 per warp iteration).
+// Loss: mean over valid pairs of (y - target)^2 with target the normalised
+// value.  Gradients (see exa_surrogate.cuh for the forward):
+//   g = 2 (y - target) / B;  gw3 += g h2
+//   d2 = bf16(g w3) where h2 > 0;  gw2 += d2 (x) h1
+//   d1 = bf16(W2^T d2) where h1 > 0;  gw1 += d1 (x) a0
+//   din = W1^T d1 (FP32)
+__global__ void __launch_bounds__(32 * kTrainWarps) k_sur_mlp_train(
+    const __nv_bfloat16 *__restrict__ w1g, const __nv_bfloat16 *__restrict__ w2g, const __nv_bfloat16 *__restrict__ w3g,
+    const __nv_bfloat16 *__restrict__ feats, const float4 *__restrict__ samples, size_t first, size_t numSamples, int B,
+    float vmin, float invRange, float invB, float *gw, float *lossOut, float *dfeat)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  TrainSmem &S = *reinterpret_cast<TrainSmem *>(smraw);
+  TrainWarpSmem &ws = reinterpret_cast<TrainWarpSmem *>(smraw + sizeof(TrainSmem))[threadIdx.x >> 5];
+  for (int i = threadIdx.x; i < kSurHidden * kSurIn; i += blockDim.x) {
+    const int j = i / kSurIn, k = i % kSurIn;
+    S.w1[j * kSurLdIn + k] = w1g[i];
+    S.w1t[k * kSurLdHid + j] = w1g[i];
+    S.gw1[i] = 0.f;
+  }
+  for (int i = threadIdx.x; i < kSurHidden * kSurHidden; i += blockDim.x) {
+    const int j = i / kSurHidden, k = i % kSurHidden;
+    S.w2[j * kSurLdHid + k] = w2g[i];
+    S.w2t[k * kSurLdHid + j] = w2g[i];
+    S.gw2[i] = 0.f;
+  }
+  for (int i = threadIdx.x; i < kSurHidden; i += blockDim.x) {
+    S.w3[i] = __bfloat162float(w3g[i]);
+    S.gw3[i] = 0.f;
+  }
+  if (threadIdx.x == 0) S.loss = 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int warpsTotal = gridDim.x * kTrainWarps;
+  const int tiles = (B + 31) / 32;
+  float acc3lo = 0.f, acc3hi = 0.f, lossAcc = 0.f;
+  for (int tile = blockIdx.x * kTrainWarps + (threadIdx.x >> 5); tile < tiles; tile += warpsTotal) {
+    const int r = tile * 32 + lane;
+    const bool inB = r < B;
+    // inputs and target
+    float target = 0.f;
+    bool valid = false;
+    {
+      uint4 q[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+      if (inB) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(feats + (size_t)r * kSurIn);
+        for (int k = 0; k < 4; ++k) q[k] = src[k];
+        const float v = samples[(first + (size_t)r) % numSamples].w;
+        valid = v == v;
+        target = valid ? (v - vmin) * invRange : 0.f;
+      }
+      uint4 *dst = reinterpret_cast<uint4 *>(ws.a + lane * kSurLdIn);
+      for (int k = 0; k < 4; ++k) dst[k] = q[k];
+      const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(q);
+      for (int i = 0; i < kSurIn; ++i) ws.at[i * kSurLdIn + lane] = e[i];
+    }
+    __syncwarp();
+    // layer 1
+    for (int mt = 0; mt < 2; ++mt)
+      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < kSurIn / 16; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.a, kSurLdIn, mt * 16, kt * 16, lane);
+          frag_b(b, S.w1, kSurLdIn, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
+        const __nv_bfloat16 v0 = __float2bfloat16_rn(fmaxf(d[0], 0.f)), v1 = __float2bfloat16_rn(fmaxf(d[1], 0.f));
+        const __nv_bfloat16 v2 = __float2bfloat16_rn(fmaxf(d[2], 0.f)), v3 = __float2bfloat16_rn(fmaxf(d[3], 0.f));
+        ws.h1[rr * kSurLdHid + c] = v0;
+        ws.h1[rr * kSurLdHid + c + 1] = v1;
+        ws.h1[(rr + 8) * kSurLdHid + c] = v2;
+        ws.h1[(rr + 8) * kSurLdHid + c + 1] = v3;
+        ws.h1t[c * kSurLdIn + rr] = v0;
+        ws.h1t[(c + 1) * kSurLdIn + rr] = v1;
+        ws.h1t[c * kSurLdIn + rr + 8] = v2;
+        ws.h1t[(c + 1) * kSurLdIn + rr + 8] = v3;
+      }
+    __syncwarp();
+    // layer 2
+    for (int mt = 0; mt < 2; ++mt)
+      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.h1, kSurLdHid, mt * 16, kt * 16, lane);
+          frag_b(b, S.w2, kSurLdHid, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
+        st_bf16x2(ws.h2 + rr * kSurLdHid + c, fmaxf(d[0], 0.f), fmaxf(d[1], 0.f));
+        st_bf16x2(ws.h2 + (rr + 8) * kSurLdHid + c, fmaxf(d[2], 0.f), fmaxf(d[3], 0.f));
+      }
+    __syncwarp();
+    // output, loss and its gradient (row of this lane)
+    float y = 0.f;
+    for (int j = 0; j < kSurHidden; ++j) y += __bfloat162float(ws.h2[lane * kSurLdHid + j]) * S.w3[j];
+    const float diff = y - target;
+    const float gr = (inB && valid) ? 2.f * diff * invB : 0.f;
+    if (inB && valid) lossAcc += diff * diff;
+    // gw3 (columns lane and lane + 32) and d2 = bf16(g w3) where h2 > 0
+    for (int rr = 0; rr < 32; ++rr) {
+      const float gv = __shfl_sync(0xffffffffu, gr, rr);
+      acc3lo += gv * __bfloat162float(ws.h2[rr * kSurLdHid + lane]);
+      acc3hi += gv * __bfloat162float(ws.h2[rr * kSurLdHid + lane + 32]);
+    }
+    __syncwarp();
+    for (int j = 0; j < kSurHidden; ++j) {
+      const bool on = __bfloat162float(ws.h2[lane * kSurLdHid + j]) > 0.f;
+      const __nv_bfloat16 v = __float2bfloat16_rn(on ? gr * S.w3[j] : 0.f);
+      ws.d2[lane * kSurLdHid + j] = v;
+      ws.d2t[j * kSurLdIn + lane] = v;
+    }
+    __syncwarp();
+    // d1 = bf16(d2 W2) where h1 > 0, into the h2 buffer (h2 is no longer read)
+    for (int mt = 0; mt < 2; ++mt)
+      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.d2, kSurLdHid, mt * 16, kt * 16, lane);
+          frag_b(b, S.w2t, kSurLdHid, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
+        const float m0 = __bfloat162float(ws.h1[rr * kSurLdHid + c]) > 0.f ? d[0] : 0.f;
+        const float m1 = __bfloat162float(ws.h1[rr * kSurLdHid + c + 1]) > 0.f ? d[1] : 0.f;
+        const float m2 = __bfloat162float(ws.h1[(rr + 8) * kSurLdHid + c]) > 0.f ? d[2] : 0.f;
+        const float m3 = __bfloat162float(ws.h1[(rr + 8) * kSurLdHid + c + 1]) > 0.f ? d[3] : 0.f;
+        const __nv_bfloat16 v0 = __float2bfloat16_rn(m0), v1 = __float2bfloat16_rn(m1);
+        const __nv_bfloat16 v2 = __float2bfloat16_rn(m2), v3 = __float2bfloat16_rn(m3);
+        ws.h2[rr * kSurLdHid + c] = v0;
+        ws.h2[rr * kSurLdHid + c + 1] = v1;
+        ws.h2[(rr + 8) * kSurLdHid + c] = v2;
+        ws.h2[(rr + 8) * kSurLdHid + c + 1] = v3;
+        ws.d1t[c * kSurLdIn + rr] = v0;
+        ws.d1t[(c + 1) * kSurLdIn + rr] = v1;
+        ws.d1t[c * kSurLdIn + rr + 8] = v2;
+        ws.d1t[(c + 1) * kSurLdIn + rr + 8] = v3;
+      }
+    __syncwarp();
+    // din = d1 W1 (FP32, into the d2 buffer: d2 is no longer read)
+    float *din = reinterpret_cast<float *>(ws.d2);
+    constexpr int ldDin = 36;
+    for (int mt = 0; mt < 2; ++mt)
+      for (int nt = 0; nt < kSurIn / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.h2, kSurLdHid, mt * 16, kt * 16, lane);
+          frag_b(b, S.w1t, kSurLdHid, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
+        din[rr * ldDin + c] = d[0];
+        din[rr * ldDin + c + 1] = d[1];
+        din[(rr + 8) * ldDin + c] = d[2];
+        din[(rr + 8) * ldDin + c + 1] = d[3];
+      }
+    // gw2 += d2^T h1 (m = j, n = i, k = r)
+    for (int mt = 0; mt < kSurHidden / 16; ++mt)
+      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < 2; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.d2t, kSurLdIn, mt * 16, kt * 16, lane);
+          frag_b(b, ws.h1t, kSurLdIn, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int j = mt * 16 + g, c = nt * 8 + 2 * t;
+        atomicAdd(&S.gw2[j * kSurHidden + c], d[0]);
+        atomicAdd(&S.gw2[j * kSurHidden + c + 1], d[1]);
+        atomicAdd(&S.gw2[(j + 8) * kSurHidden + c], d[2]);
+        atomicAdd(&S.gw2[(j + 8) * kSurHidden + c + 1], d[3]);
+      }
+    // gw1 += d1^T a0 (m = j, n = i, k = r)
+    for (int mt = 0; mt < kSurHidden / 16; ++mt)
+      for (int nt = 0; nt < kSurIn / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kt = 0; kt < 2; ++kt) {
+          uint32_t a[4], b[2];
+          frag_a(a, ws.d1t, kSurLdIn, mt * 16, kt * 16, lane);
+          frag_b(b, ws.at, kSurLdIn, nt * 8, kt * 16, lane);
+          mma16816(d, a, b);
+        }
+        const int j = mt * 16 + g, c = nt * 8 + 2 * t;
+        atomicAdd(&S.gw1[j * kSurIn + c], d[0]);
+        atomicAdd(&S.gw1[j * kSurIn + c + 1], d[1]);
+        atomicAdd(&S.gw1[(j + 8) * kSurIn + c], d[2]);
+        atomicAdd(&S.gw1[(j + 8) * kSurIn + c + 1], d[3]);
+      }
+    __syncwarp();
+    if (inB) {
+      float4 *dst = reinterpret_cast<float4 *>(dfeat + (size_t)r * kSurIn);
+      const float *src = din + lane * ldDin;
+      for (int k = 0; k < kSurIn / 4; ++k) dst[k] = make_float4(src[4 * k], src[4 * k + 1], src[4 * k + 2], src[4 * k + 3]);
+    }
+    __syncwarp();
+  }
+  atomicAdd(&S.gw3[lane], acc3lo);
+  atomicAdd(&S.gw3[lane + 32], acc3hi);
+  for (int o = 16; o > 0; o >>= 1) lossAcc += __shfl_xor_sync(0xffffffffu, lossAcc, o);
+  if (lane == 0) atomicAdd(&S.loss, lossAcc);
+  __syncthreads();
+  // weight gradient layout in gw: w1 (2048), w2 (4096), w3 (64)
+  for (int i = threadIdx.x; i < kSurHidden * kSurIn; i += blockDim.x)
+    if (S.gw1[i] != 0.f) atomicAdd(gw + i, S.gw1[i]);
+  for (int i = threadIdx.x; i < kSurHidden * kSurHidden; i += blockDim.x)
+    if (S.gw2[i] != 0.f) atomicAdd(gw + kSurHidden * kSurIn + i, S.gw2[i]);
+  for (int i = threadIdx.x; i < kSurHidden; i += blockDim.x)
+    if (S.gw3[i] != 0.f) atomicAdd(gw + kSurHidden * kSurIn + kSurHidden * kSurHidden + i, S.gw3[i]);
+  if (threadIdx.x == 0) atomicAdd(lossOut, S.loss);
+}
+
+// --------------------------------------------------------------------- Adam
+// p -= lr * mhat / (sqrt(vhat) + eps); the gradient is cleared.  n2 pairs.
+__global__ void k_sur_adam_table(float2 *p, float2 *gr, float2 *m, float2 *v, size_t n, float lr, float b1, float b2,
+                                 float c1, float c2, float eps, __half2 *half)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 g = gr[i];
+  float2 mm = m[i], vv = v[i], pp = p[i];
+  mm.x = b1 * mm.x + (1.f - b1) * g.x;
+  mm.y = b1 * mm.y + (1.f - b1) * g.y;
+  vv.x = b2 * vv.x + (1.f - b2) * g.x * g.x;
+  vv.y = b2 * vv.y + (1.f - b2) * g.y * g.y;
+  pp.x -= lr * (mm.x * c1) / (sqrtf(vv.x * c2) + eps);
+  pp.y -= lr * (mm.y * c1) / (sqrtf(vv.y * c2) + eps);
+  m[i] = mm;
+  v[i] = vv;
+  p[i] = pp;
+  gr[i] = make_float2(0.f, 0.f);
+  half[i] = __floats2half2_rn(pp.x, pp.y);
+}
+
+__global__ void k_sur_adam_mlp(float *p, float *gr, float *m, float *v, int n, float lr, float b1, float b2, float c1,
+                               float c2, float eps, __nv_bfloat16 *bf)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = gr[i];
+  const float mm = b1 * m[i] + (1.f - b1) * g;
+  const float vv = b2 * v[i] + (1.f - b2) * g * g;
+  const float pp = p[i] - lr * (mm * c1) / (sqrtf(vv * c2) + eps);
+  m[i] = mm;
+  v[i] = vv;
+  p[i] = pp;
+  gr[i] = 0.f;
+  bf[i] = __float2bfloat16_rn(pp);
+}
+
+__global__ void k_sur_init_table(float2 *p, size_t n, uint64_t seed, float scale, __half2 *half)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t key = mix64(seed ^ (i * 0x9e3779b97f4a7c15ull));
+  const float a = (u01(key, 1) * 2.f - 1.f) * scale, b = (u01(key, 2) * 2.f - 1.f) * scale;
+  p[i] = make_float2(a, b);
+  half[i] = __floats2half2_rn(a, b);
+}
+
+__global__ void k_f32_to_bf16(const float *p, int n, __nv_bfloat16 *bf)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) bf[i] = __float2bfloat16_rn(p[i]);
+}
+
+// -------------------------------------------------------------- inference
+// values of n points (one warp per 32 points); value = vmin + y * vrange
+__global__ void __launch_bounds__(128) k_sur_points(const __grid_constant__ SurrogateView S, const exa_vec3f *pos,
+                                                     size_t n, float *out)
+{
+  __shared__ SurWeightsSmem W;
+  __shared__ SurWarpSmem ws[4];
+  sur_load_weights(W, S);
+  __syncthreads();
+  const size_t warps = (size_t)gridDim.x * 4;
+  for (size_t base = (blockIdx.x * (size_t)4 + (threadIdx.x >> 5)) * 32; base < n; base += warps * 32) {
+    const size_t i = base + (threadIdx.x & 31);
+    const bool want = i < n;
+    V3 p = mk3(0.f, 0.f, 0.f);
+    if (want) p = mk3(pos[i].x, pos[i].y, pos[i].z);
+    const float y = sur_eval_warp(S, W, ws[threadIdx.x >> 5], p, want);
+    if (want) out[i] = S.vmin + y * S.vrange;
+  }
+}
+
+// ---------------------------------------------------------- error bounds
+// point p of n: macrocell p / s^3, jittered lattice point p % s^3 in it
+__global__ void __launch_bounds__(128) k_sur_mc_error(const __grid_constant__ AccelView A,
+                                                       const __grid_constant__ SurrogateView S, exa_vec3i dims,
+                                                       exa_box3f wb, int s, size_t n, uint64_t seed,
+                                                       unsigned long long *mcErr, unsigned *mcEmpty, double *sums)
+{
+  __shared__ SurWeightsSmem W;
+  __shared__ SurWarpSmem ws[4];
+  sur_load_weights(W, S);
+  __syncthreads();
+  const size_t warps = (size_t)gridDim.x * 4;
+  const size_t s3 = (size_t)s * s * s;
+  double sq = 0.0, cnt = 0.0;
+  for (size_t base = (blockIdx.x * (size_t)4 + (threadIdx.x >> 5)) * 32; base < n; base += warps * 32) {
+    const size_t i = base + (threadIdx.x & 31);
+    const bool inRange = i < n;
+    size_t mc = 0;
+    V3 p = mk3(0.f, 0.f, 0.f);
+    exa_sample ex{-1, -1, 0.f};
+    if (inRange) {
+      mc = i / s3;
+      const size_t sub = i - mc * s3;
+      const int mx = (int)(mc % dims.x), my = (int)((mc / dims.x) % dims.y), mz = (int)(mc / ((size_t)dims.x * dims.y));
+      const int sx = (int)(sub % s), sy = (int)((sub / s) % s), sz = (int)(sub / ((size_t)s * s));
+      const uint64_t key = mix64(seed ^ mix64(i + 0x2545f4914f6cdd1dull));
+      const float fx = ((float)mx + ((float)sx + u01(key, 1)) / (float)s) / (float)dims.x;
+      const float fy = ((float)my + ((float)sy + u01(key, 2)) / (float)s) / (float)dims.y;
+      const float fz = ((float)mz + ((float)sz + u01(key, 3)) / (float)s) / (float)dims.z;
+      p = mk3(wb.lower.x + fx * (wb.upper.x - wb.lower.x), wb.lower.y + fy * (wb.upper.y - wb.lower.y),
+              wb.lower.z + fz * (wb.upper.z - wb.lower.z));
+      uint32_t err = 0;
+      ex = sample_field(A, p, false, err);
+    }
+    const float y = sur_eval_warp(S, W, ws[threadIdx.x >> 5], p, inRange);
+    if (inRange) {
+      if (ex.primID < 0) {
+        atomicOr(mcEmpty + mc, 1u);
+      } else {
+        const double e = fabs((double)(S.vmin + y * S.vrange) - (double)ex.value);
+        atomicMax(mcErr + mc, (unsigned long long)__double_as_longlong(e));
+        sq += e * e;
+        cnt += 1.0;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sums, sq);
+    atomicAdd(sums + 1, cnt);
+  }
+}
+
+// mode and widened value range of every macrocell
+__global__ void k_sur_widen(const exa_range1f *ranges, const unsigned long long *mcErr, const unsigned *mcEmpty,
+                            size_t n, double tolAbs, uint8_t *mode, exa_range1f *widened, unsigned *numSurrogate)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const exa_range1f r = ranges[i];
+  const double e = __longlong_as_double((long long)mcErr[i]);
+  const bool ok = mcEmpty[i] == 0u && r.lower <= r.upper && e <= tolAbs;
+  mode[i] = ok ? 1 : 0;
+  if (ok) {
+    // widened outward: the FP32 bounds are rounded away from the range
+    const float ef = __double2float_ru(e);
+    widened[i] = exa_range1f{__fsub_rd(r.lower, ef), __fadd_ru(r.upper, ef)};
+    atomicAdd(numSurrogate, 1u);
+  } else {
+    widened[i] = r;
+  }
+}
+
+// ------------------------------------------------------------------- host
+void Surrogate::configure(const SurrogateConfig &c, const ExaStitchModel &model)
+{
+  cfg = c;
+  if (cfg.levels != kSurLevels) throw Error(EXA_ERR_INVALID, "the surrogate has 16 levels");
+  if (cfg.log2T < 10 || cfg.log2T > 24) throw Error(EXA_ERR_INVALID, "log2 table size must be in [10, 24]");
+  if (cfg.batch < 32 || cfg.batch > (1 << 22)) throw Error(EXA_ERR_INVALID, "batch must be in [32, 2^22]");
+  std::memset(&view, 0, sizeof(view));
+  view.levels = kSurLevels;
+  view.log2T = cfg.log2T;
+  view.denseMask = 0;
+  const uint64_t T = 1ull << cfg.log2T;
+  for (int l = 0; l < kSurLevels; ++l) {
+    const int r = (int)std::floor((double)cfg.baseRes * std::pow((double)cfg.growth, (double)l));
+    view.res[l] = std::max(r, 1);
+    const uint64_t side = (uint64_t)view.res[l] + 1;
+    if (side * side * side <= T) view.denseMask |= 1u << l;
+  }
+  const exa_box3f b = model.cellBounds;
+  view.lo[0] = b.lower.x;
+  view.lo[1] = b.lower.y;
+  view.lo[2] = b.lower.z;
+  view.inv[0] = 1.f / std::max(b.upper.x - b.lower.x, 1e-30f);
+  view.inv[1] = 1.f / std::max(b.upper.y - b.lower.y, 1e-30f);
+  view.inv[2] = 1.f / std::max(b.upper.z - b.lower.z, 1e-30f);
+  float vmin = model.valueRange.lower, vmax = model.valueRange.upper;
+  if (!(vmin <= vmax)) { vmin = 0.f; vmax = 1.f; }
+  view.vmin = vmin;
+  view.vrange = vmax > vmin ? vmax - vmin : 1.f;
+}
+
+void Surrogate::allocate(cudaStream_t s)
+{
+  const size_t n = (size_t)kSurLevels << cfg.log2T;
+  table.alloc(n);
+  gtable.alloc(n);
+  mTable.alloc(n);
+  vTable.alloc(n);
+  table16.alloc(n);
+  cudaCheck(cudaMemsetAsync(gtable.ptr, 0, gtable.bytes(), s), "memset");
+  cudaCheck(cudaMemsetAsync(mTable.ptr, 0, mTable.bytes(), s), "memset");
+  cudaCheck(cudaMemsetAsync(vTable.ptr, 0, vTable.bytes(), s), "memset");
+  k_sur_init_table<<<gridFor(n, 256), 256, 0, s>>>(table.ptr, n, cfg.seed ^ 0x7a1b, 1e-4f, table16.ptr);
+  cudaCheck(cudaGetLastError(), "k_sur_init_table");
+  // MLP: uniform He-style initialisation from a host RNG stream
+  std::vector<float> w(kSurParams);
+  uint64_t key = mix64(cfg.seed ^ 0x5eedull);
+  auto uni = [&](uint64_t k) { return (float)(uint32_t)(mix64(key + k * 0x9e3779b97f4a7c15ull) >> 40) * 5.96046448e-08f; };
+  const float a1 = std::sqrt(6.f / (float)(kSurIn + kSurHidden));
+  const float a2 = std::sqrt(6.f / (float)(kSurHidden + kSurHidden));
+  const float a3 = std::sqrt(6.f / (float)(kSurHidden + 1));
+  for (int i = 0; i < kSurParams; ++i) {
+    const float a = i < kSurHidden * kSurIn ? a1 : (i < kSurHidden * kSurIn + kSurHidden * kSurHidden ? a2 : a3);
+    w[i] = (uni((uint64_t)i + 1) * 2.f - 1.f) * a;
+  }
+  setWeights(w.data(), s);
+  std::vector<float> z(kSurParams, 0.f);
+  gw.upload(z.data(), z.size(), s);
+  mw.upload(z.data(), z.size(), s);
+  vw.upload(z.data(), z.size(), s);
+  step = 0;
+}
+
+void Surrogate::setWeights(const float *w, cudaStream_t s)
+{
+  w32.upload(w, kSurParams, s);
+  if (wbf.count != (size_t)kSurParams) wbf.alloc(kSurParams);
+  k_f32_to_bf16<<<gridFor(kSurParams, 256), 256, 0, s>>>(w32.ptr, kSurParams, wbf.ptr);
+  cudaCheck(cudaGetLastError(), "k_f32_to_bf16");
+}
+
+void Surrogate::setTable(const float *t, cudaStream_t s)
+{
+  const size_t n = (size_t)kSurLevels << cfg.log2T;
+  table.upload(reinterpret_cast<const float2 *>(t), n, s);
+  std::vector<__half2> h(n);
+  for (size_t i = 0; i < n; ++i) h[i] = __floats2half2_rn(t[2 * i], t[2 * i + 1]);
+  table16.upload(h.data(), n, s);
+}
+
+SurrogateView Surrogate::deviceView() const
+{
+  SurrogateView v = view;
+  v.table = table16.ptr;
+  v.w1 = wbf.ptr;
+  v.w2 = wbf.ptr + kSurHidden * kSurIn;
+  v.w3 = wbf.ptr + kSurHidden * kSurIn + kSurHidden * kSurHidden;
+  v.mcMode = mcMode.ptr;
+  return v;
+}
+
+void Surrogate::generateSamples(const ExaStitchSampler &sampler, cudaStream_t s)
+{
+  const auto &G = sampler.model->gridlets;
+  int maxLevel = 0;
+  for (const auto &g : G) maxLevel = std::max(maxLevel, g.level);
+  std::vector<int32_t> refined;
+  for (size_t i = 0; i < G.size(); ++i)
+    if (G[i].level < maxLevel) refined.push_back((int32_t)i);
+  DBuf<int32_t> dRefined;
+  if (!refined.empty()) dRefined.upload(refined.data(), refined.size(), s);
+  samples.alloc(cfg.numSamples);
+  const size_t nUniform = refined.empty() ? cfg.numSamples : (size_t)((double)cfg.numSamples * (1.0 - cfg.importance));
+  k_sur_samples<<<gridFor(cfg.numSamples, 256), 256, 0, s>>>(sampler.accel, sampler.model->cellBounds,
+                                                              cfg.numSamples, nUniform, dRefined.ptr,
+                                                              (int)refined.size(), cfg.seed, samples.ptr);
+  cudaCheck(cudaGetLastError(), "k_sur_samples");
+  cudaCheck(cudaStreamSynchronize(s), "surrogate samples");
+}
+
+float Surrogate::trainSteps(int steps, cudaStream_t s)
+{
+  if (!samples.ptr) throw Error(EXA_ERR_INVALID, "no training samples");
+  const int B = cfg.batch;
+  if (feats.count < (size_t)B * kSurIn) feats.alloc((size_t)B * kSurIn);
+  if (dfeat.count < (size_t)B * kSurIn) dfeat.alloc((size_t)B * kSurIn);
+  if (!lossBuf.ptr) lossBuf.alloc(2);
+  cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmemBytes),
+            "train smem");
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const size_t nTab = (size_t)kSurLevels << cfg.log2T;
+  const SurrogateView v = deviceView();
+  const unsigned mlpBlocks = (unsigned)std::min<int>((B / 32 + kTrainWarps - 1) / kTrainWarps, sms * 2);
+  cudaCheck(cudaMemsetAsync(lossBuf.ptr, 0, 2 * sizeof(float), s), "memset loss");
+  for (int it = 0; it < steps; ++it) {
+    const size_t first = (size_t)(cursor % cfg.numSamples);
+    cursor += (uint64_t)B;
+    k_sur_encode_fwd<<<gridFor(B, 128), 128, 0, s>>>(v, table.ptr, samples.ptr, first, cfg.numSamples, B, feats.ptr);
+    float *lossSlot = lossBuf.ptr + (it == steps - 1 ? 1 : 0);
+    if (it == steps - 1) cudaCheck(cudaMemsetAsync(lossSlot, 0, sizeof(float), s), "memset loss");
+    k_sur_mlp_train<<<mlpBlocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(
+        v.w1, v.w2, v.w3, feats.ptr, samples.ptr, first, cfg.numSamples, B, view.vmin, 1.f / view.vrange,
+        1.f / (float)B, gw.ptr, lossSlot, dfeat.ptr);
+    k_sur_encode_bwd<<<gridFor(B, 128), 128, 0, s>>>(v, samples.ptr, first, cfg.numSamples, B, dfeat.ptr, gtable.ptr);
+    step++;
+    const float b1 = 0.9f, b2 = 0.99f;
+    const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, (double)step)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, (double)step)));
+    // exponential decay from the configured rate to lrFinal over this call
+    const double frac = steps > 1 ? (double)it / (double)(steps - 1) : 0.0;
+    const float lrT = (float)((double)cfg.lrTable * std::pow((double)cfg.lrFinal / (double)cfg.lrTable, frac));
+    const float lrM = (float)((double)cfg.lrMlp * std::pow((double)cfg.lrFinal / (double)cfg.lrMlp, frac));
+    k_sur_adam_table<<<gridFor(nTab, 256), 256, 0, s>>>(table.ptr, gtable.ptr, mTable.ptr, vTable.ptr, nTab, lrT, b1,
+                                                        b2, c1, c2, 1e-15f, table16.ptr);
+    k_sur_adam_mlp<<<gridFor(kSurParams, 256), 256, 0, s>>>(w32.ptr, gw.ptr, mw.ptr, vw.ptr, kSurParams, lrM, b1, b2,
+                                                           c1, c2, 1e-15f, wbf.ptr);
+    cudaCheck(cudaGetLastError(), "surrogate training step");
+  }
+  float h[2] = {0.f, 0.f};
+  cudaCheck(cudaMemcpyAsync(h, lossBuf.ptr, sizeof(h), cudaMemcpyDeviceToHost, s), "loss");
+  cudaCheck(cudaStreamSynchronize(s), "surrogate training");
+  // mean squared error (normalised units) of the last step's batch
+  lastLoss = h[1] / (float)B;
+  return lastLoss;
+}
+
+void Surrogate::gradients(const float4 *hostSamples, int n, float *gW, float *gTable, float *loss, cudaStream_t s)
+{
+  // one step's gradients for the given pairs without updating anything
+  if (n < 1 || n > cfg.batch) throw Error(EXA_ERR_INVALID, "gradient batch size out of range");
+  DBuf<float4> sm;
+  sm.upload(hostSamples, (size_t)n, s);
+  DBuf<__nv_bfloat16> f;
+  f.alloc((size_t)n * kSurIn);
+  DBuf<float> df;
+  df.alloc((size_t)n * kSurIn);
+  DBuf<float> gwl, lossl;
+  std::vector<float> z(kSurParams, 0.f);
+  gwl.upload(z.data(), z.size(), s);
+  float zero = 0.f;
+  lossl.upload(&zero, 1, s);
+  const size_t nTab = (size_t)kSurLevels << cfg.log2T;
+  DBuf<float2> gt;
+  gt.alloc(nTab);
+  cudaCheck(cudaMemsetAsync(gt.ptr, 0, gt.bytes(), s), "memset");
+  cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmemBytes),
+            "train smem");
+  const SurrogateView v = deviceView();
+  k_sur_encode_fwd<<<gridFor(n, 128), 128, 0, s>>>(v, table.ptr, sm.ptr, 0, (size_t)n, n, f.ptr);
+  const unsigned blocks = (unsigned)(((n + 31) / 32 + kTrainWarps - 1) / kTrainWarps);
+  k_sur_mlp_train<<<blocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(v.w1, v.w2, v.w3, f.ptr, sm.ptr, 0, (size_t)n, n,
+                                                                    view.vmin, 1.f / view.vrange, 1.f / (float)n,
+                                                                    gwl.ptr, lossl.ptr, df.ptr);
+  k_sur_encode_bwd<<<gridFor(n, 128), 128, 0, s>>>(v, sm.ptr, 0, (size_t)n, n, df.ptr, gt.ptr);
+  cudaCheck(cudaGetLastError(), "surrogate gradients");
+  if (gW) cudaCheck(cudaMemcpyAsync(gW, gwl.ptr, kSurParams * sizeof(float), cudaMemcpyDeviceToHost, s), "d2h");
+  if (gTable) cudaCheck(cudaMemcpyAsync(gTable, gt.ptr, gt.bytes(), cudaMemcpyDeviceToHost, s), "d2h");
+  float l = 0.f;
+  cudaCheck(cudaMemcpyAsync(&l, lossl.ptr, sizeof(float), cudaMemcpyDeviceToHost, s), "d2h");
+  cudaCheck(cudaStreamSynchronize(s), "surrogate gradients");
+  if (loss) *loss = l / (float)n;
+}
+
+void Surrogate::evaluate(const ExaStitchSampler &sampler, const Grid &grid, double tol, size_t pointsTarget,
+                         cudaStream_t s)
+{
+  const size_t nmc = (size_t)grid.dims.x * grid.dims.y * grid.dims.z;
+  if (!nmc) throw Error(EXA_ERR_INVALID, "no majorant grid");
+  mcMode.alloc(nmc);
+  mcErr.alloc(nmc);
+  mcEmpty.alloc(nmc);
+  widenedRanges.alloc(nmc);
+  majorants.alloc(nmc);
+  DBuf<double> sums;
+  sums.alloc(2);
+  DBuf<unsigned> nsur;
+  nsur.alloc(1);
+  cudaCheck(cudaMemsetAsync(mcErr.ptr, 0, mcErr.bytes(), s), "memset");
+  cudaCheck(cudaMemsetAsync(mcEmpty.ptr, 0, mcEmpty.bytes(), s), "memset");
+  cudaCheck(cudaMemsetAsync(sums.ptr, 0, sums.bytes(), s), "memset");
+  cudaCheck(cudaMemsetAsync(nsur.ptr, 0, nsur.bytes(), s), "memset");
+  int sp = (int)std::floor(std::cbrt((double)pointsTarget / (double)nmc));
+  sp = std::max(2, std::min(sp, 16));
+  const size_t n = nmc * (size_t)sp * sp * sp;
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 127) / 128, (size_t)sms * 8);
+  const SurrogateView v = deviceView();
+  k_sur_mc_error<<<blocks, 128, 0, s>>>(sampler.accel, v, grid.dims, grid.worldBounds, sp, n, cfg.seed ^ 0xe44,
+                                        mcErr.ptr, mcEmpty.ptr, sums.ptr);
+  cudaCheck(cudaGetLastError(), "k_sur_mc_error");
+  k_sur_widen<<<gridFor(nmc, 256), 256, 0, s>>>(grid.valueRanges.ptr, mcErr.ptr, mcEmpty.ptr, nmc,
+                                                tol * (double)view.vrange, mcMode.ptr, widenedRanges.ptr, nsur.ptr);
+  cudaCheck(cudaGetLastError(), "k_sur_widen");
+  double hs[2];
+  unsigned hn = 0;
+  cudaCheck(cudaMemcpyAsync(hs, sums.ptr, sizeof(hs), cudaMemcpyDeviceToHost, s), "d2h");
+  cudaCheck(cudaMemcpyAsync(&hn, nsur.ptr, sizeof(hn), cudaMemcpyDeviceToHost, s), "d2h");
+  std::vector<unsigned long long> errs(nmc);
+  cudaCheck(cudaMemcpyAsync(errs.data(), mcErr.ptr, mcErr.bytes(), cudaMemcpyDeviceToHost, s), "d2h");
+  cudaCheck(cudaStreamSynchronize(s), "surrogate evaluate");
+  double emax = 0.0;
+  for (unsigned long long e : errs) {
+    double d;
+    std::memcpy(&d, &e, sizeof(d));
+    emax = std::max(emax, d);
+  }
+  stats.probePoints = n;
+  stats.rmse = hs[1] > 0.0 ? std::sqrt(hs[0] / hs[1]) / (double)view.vrange : 0.0;
+  stats.maxError = emax / (double)view.vrange;
+  stats.numMacrocells = nmc;
+  stats.numSurrogateMCs = hn;
+  evalDims = grid.dims;
+  evaluated = true;
+}
+
+void Surrogate::computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, cudaStream_t s)
+{
+  if (!evaluated) return;
+  launchMaxOpacity(widenedRanges.ptr, widenedRanges.count, cmap, ncolors, xf, majorants.ptr, s);
+}
+
+size_t Surrogate::inferenceBytes() const
+{
+  return table16.bytes() + wbf.bytes() + mcMode.bytes() + majorants.bytes();
+}
+
+void launchSurrogatePoints(const SurrogateView &S, const exa_vec3f *pos, size_t n, float *out, cudaStream_t s)
+{
+  if (!n) return;
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 127) / 128, (size_t)sms * 8);
+  k_sur_points<<<blocks, 128, 0, s>>>(S, pos, n, out);
+  cudaCheck(cudaGetLastError(), "k_sur_points");
+}
+
+} // namespace exa

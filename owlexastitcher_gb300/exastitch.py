@@ -185,6 +185,27 @@ class MemStats(C.Structure):
         "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes")]
 
 
+class SurrogateParams(C.Structure):
+    _fields_ = [("log2TableSize", C.c_int32), ("baseResolution", C.c_int32), ("growth", C.c_float),
+                ("importanceFraction", C.c_float), ("numSamples", C.c_uint64), ("batch", C.c_int32),
+                ("learningRate", C.c_float), ("seed", C.c_uint64), ("learningRateFinal", C.c_float),
+                ("pad0", C.c_int32)]
+
+
+class SurrogateStats(C.Structure):
+    _fields_ = [("loss", C.c_float), ("steps", C.c_int32), ("tolerance", C.c_float), ("pad0", C.c_int32),
+                ("rmse", C.c_double), ("maxError", C.c_double)] + [(n, C.c_uint64) for n in (
+                    "probePoints", "numMacrocells", "numSurrogateMacrocells", "tableBytes", "weightBytes",
+                    "inferenceBytes", "fieldBytes", "fallbackFieldBytes")]
+
+
+class SurrogateGeometry(C.Structure):
+    _fields_ = [("log2TableSize", C.c_int32), ("denseMask", C.c_uint32), ("res", C.c_int32 * 16),
+                ("lo", C.c_float * 3), ("inv", C.c_float * 3), ("vmin", C.c_float), ("vrange", C.c_float)]
+
+
+SURROGATE_PARAMS = 64 * 32 + 64 * 64 + 64  # W1 | W2 | w3
+
 GRIDLET_DTYPE = np.dtype([("lower", "<i4", 3), ("level", "<i4"), ("dims", "<i4", 3), ("begin", "<u4")])
 SAMPLE_DTYPE = np.dtype([("primID", "<i4"), ("cellID", "<i4"), ("value", "<f4")])
 
@@ -195,6 +216,10 @@ EXPORTED = [
     "exa_sampler_build", "exa_sampler_compute_max_opacities", "exa_sampler_set_lps", "exa_sampler_class_name",
     "exa_get_majorants", "exa_get_prim_majorants", "exa_sample_points", "exa_sample_points_host",
     "exa_launch_params_init", "exa_render", "exa_render_noalloc", "exa_get_render_stats",
+    "exa_surrogate_params_default", "exa_surrogate_create", "exa_surrogate_train", "exa_surrogate_evaluate",
+    "exa_surrogate_get_stats", "exa_surrogate_get_geometry", "exa_surrogate_sample_points",
+    "exa_surrogate_get_params", "exa_surrogate_set_params", "exa_surrogate_gradients",
+    "exa_surrogate_get_macrocells", "exa_render_surrogate",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -235,12 +260,25 @@ def lib():
         "exa_render": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
         "exa_render_noalloc": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
         "exa_get_render_stats": ([ctx_p, C.POINTER(RenderStats)], C.c_int),
+        "exa_surrogate_params_default": ([C.POINTER(SurrogateParams)], None),
+        "exa_surrogate_create": ([ctx_p, C.POINTER(SurrogateParams)], C.c_int),
+        "exa_surrogate_train": ([ctx_p, i32, C.POINTER(C.c_float)], C.c_int),
+        "exa_surrogate_evaluate": ([ctx_p, C.c_float, u64], C.c_int),
+        "exa_surrogate_get_stats": ([ctx_p, C.POINTER(SurrogateStats)], C.c_int),
+        "exa_surrogate_get_geometry": ([ctx_p, C.POINTER(SurrogateGeometry)], C.c_int),
+        "exa_surrogate_sample_points": ([ctx_p, vp, u64, vp], C.c_int),
+        "exa_surrogate_get_params": ([ctx_p, vp, vp], C.c_int),
+        "exa_surrogate_set_params": ([ctx_p, vp, vp], C.c_int),
+        "exa_surrogate_gradients": ([ctx_p, vp, i32, vp, vp, vp], C.c_int),
+        "exa_surrogate_get_macrocells": ([ctx_p, vp, vp, vp], C.c_int),
+        "exa_render_surrogate": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = res
-    for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt)):
+    for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt), (5, SurrogateParams),
+                    (6, SurrogateStats), (7, SurrogateGeometry)):
         if L.exa_abi_sizeof(key) != C.sizeof(st):
             raise RuntimeError(f"ABI layout mismatch for {st.__name__}: C {L.exa_abi_sizeof(key)} vs ctypes {C.sizeof(st)}")
     _lib = L
@@ -452,6 +490,7 @@ class Renderer:
         self.colorMap = None
         self.fb = None
         self.accum = None
+        self.learned = False  # render with the learned field (Surrogate) where it is valid
 
     def _xf_range(self):
         a0, a1 = self.absDomain
@@ -511,4 +550,68 @@ class Renderer:
         self.accumID += 1
         self.lp.render.dt = 1.0
         self.lp.render.spp = max(self.spp, 1)
-        _check(lib().exa_render(self.ctx.h, C.byref(self.lp), w, h))
+        fn = lib().exa_render_surrogate if self.learned else lib().exa_render
+        _check(fn(self.ctx.h, C.byref(self.lp), w, h))
+
+
+class Surrogate:
+    """The learned field of a context: hash-grid encoding + MLP trained on
+    the exact sampler's values (exa_surrogate_* in exastitch.h)."""
+
+    def __init__(self, ctx, **params):
+        self.ctx = ctx
+        p = SurrogateParams()
+        lib().exa_surrogate_params_default(C.byref(p))
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        _check(lib().exa_surrogate_create(ctx.h, C.byref(p)))
+        g = SurrogateGeometry()
+        _check(lib().exa_surrogate_get_geometry(ctx.h, C.byref(g)))
+        self.geometry = g
+        self.table_floats = 2 * 16 * (1 << p.log2TableSize)
+
+    def train(self, steps):
+        loss = C.c_float(0.0)
+        _check(lib().exa_surrogate_train(self.ctx.h, int(steps), C.byref(loss)))
+        return float(loss.value)
+
+    def evaluate(self, tolerance=0.02, points=1 << 24):
+        _check(lib().exa_surrogate_evaluate(self.ctx.h, float(tolerance), int(points)))
+
+    def stats(self):
+        st = SurrogateStats()
+        _check(lib().exa_surrogate_get_stats(self.ctx.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in SurrogateStats._fields_ if k != "pad0"}
+
+    def params_host(self):
+        w = np.zeros(SURROGATE_PARAMS, np.float32)
+        t = np.zeros(self.table_floats, np.float32)
+        _check(lib().exa_surrogate_get_params(self.ctx.h, _np_ptr(w), _np_ptr(t)))
+        return w, t
+
+    def set_params(self, weights=None, table=None):
+        wp = _np_ptr(np.ascontiguousarray(weights, np.float32)) if weights is not None else None
+        tp = _np_ptr(np.ascontiguousarray(table, np.float32)) if table is not None else None
+        keep = (weights, table)
+        _check(lib().exa_surrogate_set_params(self.ctx.h, wp, tp))
+        del keep
+
+    def gradients(self, pairs):
+        pairs = np.ascontiguousarray(pairs, np.float32).reshape(-1, 4)
+        gw = np.zeros(SURROGATE_PARAMS, np.float32)
+        gt = np.zeros(self.table_floats, np.float32)
+        loss = C.c_float(0.0)
+        _check(lib().exa_surrogate_gradients(self.ctx.h, _np_ptr(pairs), len(pairs), _np_ptr(gw), _np_ptr(gt),
+                                             C.byref(loss)))
+        return gw, gt, float(loss.value)
+
+    def sample_device(self, pos_dev, out_dev, n):
+        _check(lib().exa_surrogate_sample_points(self.ctx.h, C.c_void_p(pos_dev), int(n), C.c_void_p(out_dev)))
+
+    def macrocells(self, num_mcs):
+        mode = np.zeros(num_mcs, np.uint8)
+        err = np.zeros(num_mcs, np.float64)
+        maj = np.zeros(num_mcs, np.float32)
+        _check(lib().exa_surrogate_get_macrocells(self.ctx.h, _np_ptr(mode), _np_ptr(err), _np_ptr(maj)))
+        return mode, err, maj
