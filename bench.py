@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + 1 step, no extras (for ncu)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-field (surrogate) measurements")
+    ap.add_argument("--learned-steps", type=int, default=1600, help="surrogate training steps")
     return ap.parse_args()
 
 
@@ -269,6 +271,16 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
 
+    learned = None
+    if rank == 0 and not a.no_learned:
+        from owlexastitcher_gb300 import datagen
+        learned = {
+            # the small config's field (3 levels, 32^3 root) with its 32^3 majorant grid
+            "small_field": run_learned(a, local, datagen.Dataset("small"), (32, 32, 32), flush),
+            # the same method on this workload's field and majorant grid
+            "workload_field": run_learned(a, local, ds, NUM_MCS, flush),
+        }
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
@@ -292,6 +304,7 @@ def run_ours(a):
             "clocks": clocks,
             "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
             "render": render_stats,
+            "learned_field": learned,
             "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
                                                   "numWedges", "numHexes", "numTets")} | {
                 "field_bytes": ds.field_bytes, "gen_seconds": gen_s},
@@ -300,6 +313,112 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_learned(a, local, ds, num_mcs, flush, timed=3):
+    """The learned field on one dataset: training, per-macrocell error
+    bounds, memory, and the same path-traced frame rendered with the exact
+    sampler and with the learned field (+ exact fallback), both through
+    the public API, timed with CUDA events on the current stream."""
+    import torch
+    from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import exastitch as E
+    ctx = E.Context(local)
+    r = E.Renderer(ctx, E.ExaStitchModel.from_dataset(ctx, ds), num_mcs)
+    lo, hi = r.model.cellBounds
+    r.setColorMap(ramp_tf())
+    r.resize(a.width, a.height)
+    r.spp = a.spp
+    setup_render(r.lp, orbit_camera(lo, hi, a.width, a.height), a.width, a.height, E.PATH_TRACING_INTEGRATOR,
+                 a.spp, "directional", True)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    S = E.Surrogate(ctx, log2TableSize=19, baseResolution=16, growth=1.5, numSamples=1 << 24, batch=1 << 18,
+                    importanceFraction=0.5, seed=1234)
+    torch.cuda.synchronize()
+    sample_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = S.train(a.learned_steps)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    S.evaluate(0.02, 1 << 24)
+    eval_s = time.perf_counter() - t0
+    st = S.stats()
+    res = {}
+    imgs = {}
+    for name, learned in (("exact", False), ("learned", True)):
+        r.learned = learned
+        for _ in range(2):
+            r.accumID = 0
+            r.render()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(timed)]
+        for e0, e1 in ev:
+            flush.fill_(2.0)
+            r.accumID = 0
+            e0.record(stream)
+            r.render()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.sync()
+        ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / timed
+        imgs[name] = r.accum.cpu().numpy().reshape(-1, 4)[:, :3] / a.spp
+        cnt = torch.zeros(16, dtype=torch.int64, device="cuda")
+        r.lp.ext.stepCounters = cnt.data_ptr()
+        r.accumID = 0
+        r.render()
+        torch.cuda.synchronize()
+        r.lp.ext.stepCounters = None
+        c = cnt.cpu().numpy()
+        res[name] = {"paths_per_s": a.width * a.height * a.spp / (ms / 1e3), "ms_per_frame": ms,
+                     "walk_ms": ctx.render_stats()["walkMs"],
+                     "exact_field_samples": int(c[0]), "learned_samples": int(c[10]),
+                     "majorant_violations": int(c[11])}
+    r.learned = False
+    # point queries: learned value vs exact sample at 1M uniform points
+    rng = np.random.default_rng(42)
+    P = rng.uniform(lo, hi, (1 << 20, 3)).astype(np.float32)
+    pd = torch.from_numpy(P).cuda()
+    vals = torch.empty(1 << 20, dtype=torch.float32, device="cuda")
+    ex = torch.empty((1 << 20) * 3, dtype=torch.int32, device="cuda")
+    q = {}
+    for name, fn in (("exact", lambda: r.sampler.sample_device(pd.data_ptr(), ex.data_ptr(), len(P), cull=False)),
+                     ("learned", lambda: S.sample_device(pd.data_ptr(), vals.data_ptr(), len(P)))):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(3.0)
+        e0.record(stream)
+        for _ in range(10):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        q[name] = 10 * len(P) / (e0.elapsed_time(e1) / 1e3)
+    ctx.sync()
+    rmse = float(np.sqrt(np.mean((imgs["exact"] - imgs["learned"]) ** 2)))
+    out = {
+        "dataset": ds.config if hasattr(ds, "config") else None, "majorant_grid": list(num_mcs),
+        "encoding": {"levels": 16, "features": 2, "table_entries_per_level": 1 << 19, "base_resolution": 16,
+                     "growth": 1.5},
+        "mlp": "32-64-64-1 ReLU, BF16 weights, FP32 accumulate (mma.sync m16n8k16)",
+        "training": {"pairs": 1 << 24, "importance_fraction": 0.5, "batch": 1 << 18, "steps": a.learned_steps,
+                     "final_batch_mse": loss, "sample_seconds": sample_s, "train_seconds": train_s,
+                     "pairs_per_s": a.learned_steps * (1 << 18) / train_s},
+        "errors": {"tolerance": 0.02, "probe_points": st["probePoints"], "probe_rmse": st["rmse"],
+                   "probe_max_error": st["maxError"], "eval_seconds": eval_s},
+        "macrocells": {"total": st["numMacrocells"], "learned": st["numSurrogateMacrocells"],
+                       "fraction_learned": st["numSurrogateMacrocells"] / max(st["numMacrocells"], 1)},
+        "memory_bytes": {"learned_inference": st["inferenceBytes"], "exact_field": st["fieldBytes"],
+                         "exact_fallback_needed": st["fallbackFieldBytes"],
+                         "learned_plus_fallback_over_exact": (st["inferenceBytes"] + st["fallbackFieldBytes"]) /
+                         max(st["fieldBytes"], 1)},
+        "render": res,
+        "paths_per_s_learned_over_exact": res["learned"]["paths_per_s"] / res["exact"]["paths_per_s"],
+        "image_rmse_vs_exact_same_rng": rmse,
+        "point_queries_per_s": q,
+    }
+    ctx.close()
+    return out
 
 
 def _oracle_scene(a, ds, lp_src, max_ops, gops, eops, tf):

@@ -907,6 +907,12 @@ static void dda_init(oc_dda *d, v3 org, v3 dir, float tmin, float tmax, v3i dims
   d->tnext.x = dir.x > 0.f ? tnear.x + (float)(d->cell.x + 1) * d->dist.x : tnear.x + (float)(dims.x - d->cell.x) * d->dist.x;
   d->tnext.y = dir.y > 0.f ? tnear.y + (float)(d->cell.y + 1) * d->dist.y : tnear.y + (float)(dims.y - d->cell.y) * d->dist.y;
   d->tnext.z = dir.z > 0.f ? tnear.z + (float)(d->cell.z + 1) * d->dist.z : tnear.z + (float)(dims.z - d->cell.z) * d->dist.z;
+  /* a direction component of 0 (or one whose reciprocal overflows) gives a
+   * NaN crossing, on which DDA.h's loop never advances: that axis is never
+   * crossed, so its next crossing is at +inf (other rays are unaffected) */
+  if (isnan(d->tnext.x)) d->tnext.x = INFINITY;
+  if (isnan(d->tnext.y)) d->tnext.y = INFINITY;
+  if (isnan(d->tnext.z)) d->tnext.z = INFINITY;
   d->t0 = fmax_t(tmin, 0.f);
   d->tmax = tmax;
 }

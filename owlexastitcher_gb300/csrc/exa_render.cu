@@ -104,6 +104,13 @@ EXA_D void dda_init(Dda &d, V3 org, V3 dir, float tmin, float tmax, const exa_gr
   d.tnext.x = dir.x > 0.f ? tnear.x + (float)(d.cell.x + 1) * d.dist.x : tnear.x + (float)(dims.x - d.cell.x) * d.dist.x;
   d.tnext.y = dir.y > 0.f ? tnear.y + (float)(d.cell.y + 1) * d.dist.y : tnear.y + (float)(dims.y - d.cell.y) * d.dist.y;
   d.tnext.z = dir.z > 0.f ? tnear.z + (float)(d.cell.z + 1) * d.dist.z : tnear.z + (float)(dims.z - d.cell.z) * d.dist.z;
+  // A direction component of 0 (or one whose reciprocal overflows) makes
+  // that axis's crossing NaN, and DDA.h's loop then never advances; such an
+  // axis is never crossed, so its next crossing is at +inf.  Every other ray
+  // is unaffected.
+  if (isnan(d.tnext.x)) d.tnext.x = INFINITY;
+  if (isnan(d.tnext.y)) d.tnext.y = INFINITY;
+  if (isnan(d.tnext.z)) d.tnext.z = INFINITY;
   d.t0 = fmax_t(tmin, 0.f);
   d.tmax = tmax;
 }
@@ -1048,6 +1055,9 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
 // elsewhere; lp.maxOpacities holds the widened majorants.  Dynamic shared
 // memory: the network and the warps' scratch (kSurWalkSmem bytes).
 constexpr size_t kSurWalkSmem = sizeof(SurWeightsSmem) + 4 * sizeof(SurWarpSmem);
+#ifndef EXA_SUR_BATCH
+#define EXA_SUR_BATCH 20
+#endif
 
 __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(const __grid_constant__ AccelView A,
                                                                             const __grid_constant__ exa_launch_params lp,
@@ -1064,7 +1074,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
   const unsigned n = Q.cnt[0];
   const unsigned lane = threadIdx.x & 31;
   Lane L;
-  bool active = false, exhausted = false;
+  bool active = false, exhausted = false, pending = false;
   unsigned src = 0;
   while (true) {
     const unsigned need = __ballot_sync(0xffffffffu, !active);
@@ -1086,7 +1096,9 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     }
     const unsigned act = __ballot_sync(0xffffffffu, active);
     if (!act) break;
-    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES) {
+    // a lane waiting for a learned sample is never parked: its free flight
+    // is done, its sample not yet taken
+    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES && !__any_sync(0xffffffffu, pending)) {
       const unsigned slot = warp_append(&Q.cnt[1], active);
       if (active) {
         wf_store_walk(L, Q.out, Q.cap, slot);
@@ -1094,27 +1106,38 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
       }
       break;
     }
-    const int st = active ? walk_advance(L.w, c, L.rng) : WALK_END;
-    bool sur = false;
-    exa_sample s;
-    s.primID = -1;
-    s.cellID = -1;
-    s.value = 0.f;
-    if (st == WALK_SAMPLE) {
-      const int leafID = (L.w.dda.cell.z * G.dims.y + L.w.dda.cell.y) * G.dims.x + L.w.dda.cell.x;
-      sur = __ldg(S.mcMode + leafID) != 0;
-      if (!sur) s = walk_sample_exact(L.w, c);
-    }
-    if (__any_sync(0xffffffffu, sur)) {
-      const float y = sur_eval_warp(S, W, ws, L.w.pos, sur);
-      if (sur) {
-        s.primID = -2;
-        s.value = S.vmin + y * S.vrange;
-        cnt_add(c, CNT_SURR);
+    bool ended = false;
+    if (active && !pending) {
+      const int st = walk_advance(L.w, c, L.rng);
+      if (st == WALK_END) {
+        ended = true;
+      } else if (st == WALK_SAMPLE) {
+        const int leafID = (L.w.dda.cell.z * G.dims.y + L.w.dda.cell.y) * G.dims.x + L.w.dda.cell.x;
+        if (__ldg(S.mcMode + leafID) != 0) {
+          pending = true;
+        } else {
+          const exa_sample s = walk_sample_exact(L.w, c);
+          ended = !walk_collide(L.w, c, L.rng, L.shadow, s);
+        }
       }
     }
-    const bool ended =
-        active && (st == WALK_END || (st == WALK_SAMPLE && !walk_collide(L.w, c, L.rng, L.shadow, s)));
+    // the network runs for a batch of waiting lanes: at least
+    // EXA_SUR_BATCH of them, or every lane still walking
+    const unsigned pm = __ballot_sync(0xffffffffu, pending);
+    const unsigned am = __ballot_sync(0xffffffffu, active && !ended);
+    if (pm && (__popc(pm) >= EXA_SUR_BATCH || pm == am || exhausted)) {
+      const float y = sur_eval_warp(S, W, ws, L.w.pos, pending);
+      if (pending) {
+        exa_sample s;
+        s.primID = -2;
+        s.cellID = -1;
+        s.value = S.vmin + y * S.vrange;
+        cnt_add(c, CNT_SURR);
+        pending = false;
+        ended = !walk_collide(L.w, c, L.rng, L.shadow, s);
+      }
+    }
+    ended = active && ended;
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
       wf_store_walk(L, Q.ev, Q.cap, slot);

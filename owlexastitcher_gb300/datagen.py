@@ -116,6 +116,7 @@ class Dataset:
     """Generated ExaStitch arrays (numpy copies) plus the analytic field."""
 
     def __init__(self, config="small", **overrides):
+        self.config = config
         self.params = params(config, **overrides)
         h = C.c_void_p()
         rc = lib().exa_gen_run(C.byref(self.params), C.byref(h))

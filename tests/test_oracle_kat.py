@@ -91,3 +91,24 @@ def test_homogeneous_medium_scatter_probability(oracle, native):
     p = tot / n
     expect = 1 - np.exp(-0.05 * (hi[0] - lo[0]))
     assert abs(p - expect) < 4 * np.sqrt(expect * (1 - expect) / n)
+
+
+@pytest.mark.parametrize("zero_axes", [(2,), (1,), (0, 2)])
+def test_dda_axis_parallel_ray(oracle, zero_axes):
+    """A ray with direction components of exactly 0 never crosses that axis's
+    planes: the walk ends at the grid's far side with those cell indices
+    fixed, and visits at most one cell per crossing."""
+    dims = (16, 12, 10)
+    lo, hi = np.zeros(3, np.float32), np.array([16, 12, 10], np.float32)
+    d = np.array([0.6, -0.5, 0.62], np.float32)
+    for a in zero_axes:
+        d[a] = 0.0
+    d /= np.linalg.norm(d)
+    for org in (np.array([7.3, 5.1, 4.4], np.float32), np.array([7.0, 6.0, 5.0], np.float32)):
+        ids, t0, t1 = oracle.dda3(org, d, 0.0, 1e3, dims, lo, hi)
+        assert 0 < len(ids) <= sum(dims)
+        cells = np.stack([ids % dims[0], (ids // dims[0]) % dims[1], ids // (dims[0] * dims[1])], axis=1)
+        start = [min(int(org[a]), dims[a] - 1) for a in range(3)]
+        for a in zero_axes:
+            assert np.all(cells[:, a] == start[a])
+        assert np.all(np.isfinite(t0)) and np.all(np.isfinite(t1)) and np.all(t1 >= t0)
