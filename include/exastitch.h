@@ -369,6 +369,62 @@ int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
                        int32_t width, int32_t height);
 
 /* ------------------------------------------------------------------ */
+/* batched frames (no counterpart in the reference)                    */
+/* ------------------------------------------------------------------ */
+
+/* One frame of a batch: camera (LaunchParams.camera), size, samples per
+ * pixel, transfer function (index into exa_batch_set_transfer_functions),
+ * progressive-accumulation index and RNG frame index, and device output
+ * buffers (either may be null; accumBuffer is needed when accumID > 0). */
+typedef struct exa_batch_frame {
+  exa_vec3f org, dir_00, dir_du, dir_dv;
+  int32_t width, height, spp, tf;
+  uint32_t accumID, frameID;
+  uint32_t *fbPointer;
+  exa_vec4f *accumBuffer;
+} exa_batch_frame;
+
+/* Result of exa_batch_autotune: the chosen majorant-grid resolution and job
+ * tile width, and every trial's time for the sampled workload. */
+typedef struct exa_batch_tuning {
+  exa_vec3i dims;
+  int32_t tileWidth;
+  float msBest;
+  int32_t numTrials;
+  exa_vec3i trialDims[16];
+  int32_t trialTileWidth[16];
+  float trialMs[16];
+} exa_batch_tuning;
+
+/* Transfer functions of the batch: host colour maps (RGBA), their sizes,
+ * value ranges and opacity scales (null: 1).  Computes each one's max
+ * opacities on the batch's majorant grid and its primitive culling data. */
+int exa_batch_set_transfer_functions(exa_context *ctx, int32_t numTFs, const exa_vec4f *const *colorMaps,
+                                     const int32_t *numColors, const exa_range1f *xfRanges,
+                                     const float *opacityScales);
+/* Majorant grid of the batch over the model's cell bounds (default: the
+ * model's grid).  Rebuilds the value ranges and every transfer function's
+ * max opacities. */
+int exa_batch_set_majorant_grid(exa_context *ctx, exa_vec3i dims);
+/* Width of the 128-job pixel tiles of the batch's job order: 8, 16 or 32. */
+int exa_batch_set_tile_width(exa_context *ctx, int32_t tileWidth);
+/* Renders numFrames frames in one wavefront (one set of queues; each
+ * frame's result equals exa_render of that frame with the same parameters
+ * and majorant grid).  lpTemplate supplies everything a frame does not
+ * (integrator, lights, bounces, albedo, phase function, shade mode,
+ * transforms, counters); exa_sampler_set_lps must have filled it.
+ * useGraph != 0: the rounds run from the device inside one CUDA graph (built
+ * on the first call for a batch shape, then replayed); else a host loop
+ * synchronizes once per round.  Asynchronous (exa_sync). */
+int exa_render_batch(exa_context *ctx, const exa_launch_params *lpTemplate, const exa_batch_frame *frames,
+                     int32_t numFrames, int32_t useGraph);
+/* Times the batch's workload (every sampleEvery-th frame at 1 spp) on
+ * majorant grids of 32^3, 64^3, 128^3 and 256^3 and tile widths 8, 16 and
+ * 32, keeps the fastest setting for the batch, and reports all trials. */
+int exa_batch_autotune(exa_context *ctx, const exa_launch_params *lpTemplate, const exa_batch_frame *frames,
+                       int32_t numFrames, int32_t sampleEvery, exa_batch_tuning *out);
+
+/* ------------------------------------------------------------------ */
 /* learned field (no counterpart in the reference)                     */
 /* ------------------------------------------------------------------ */
 

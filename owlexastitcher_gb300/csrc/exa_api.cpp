@@ -458,6 +458,35 @@ struct exa_context {
   DBuf<exa_sample> hostOut;
   std::unique_ptr<Surrogate> surrogate;
   float surrogateTol = 0.f;
+  std::unique_ptr<struct BatchState> batch;
+};
+
+// state of exa_render_batch: transfer functions, the batch's majorant grid,
+// per-transfer-function culling data, frame tables, scratch and the cached
+// CUDA graph
+struct BatchState {
+  std::vector<DBuf<float4>> tfColors;
+  std::vector<int> tfCount;
+  std::vector<exa_range1f> tfRange;
+  std::vector<float> tfScale;
+  exa_vec3i dims{0, 0, 0};
+  DBuf<exa_range1f> ranges;
+  std::vector<DBuf<float>> maxOps;  // per transfer function, on dims
+  // per transfer function: primitive max opacities, the element BVH refit
+  // with them, and the point-location view that culls by them
+  std::vector<DBuf<float>> gOps, eOps;
+  std::vector<DBuf<BvhNode>> nodes;
+  DBuf<AccelView> accels;
+  int tileW = 16;
+  DBuf<exa_launch_params> lps;
+  DBuf<WfFrame> frames;
+  DBuf<WfCtl> ctl;
+  DBuf<float4> colors;
+  DBuf<uint32_t> records;
+  DBuf<unsigned> counters;
+  unsigned cap = 0;
+  BatchGraph graph;
+  WfStats last;
 };
 
 namespace {
@@ -571,6 +600,8 @@ uint64_t exa_abi_sizeof(int32_t which)
     case 5: return sizeof(exa_surrogate_params);
     case 6: return sizeof(exa_surrogate_stats);
     case 7: return sizeof(exa_surrogate_geometry);
+    case 8: return sizeof(exa_batch_frame);
+    case 9: return sizeof(exa_batch_tuning);
     default: return 0;
   }
 }
@@ -1112,6 +1143,288 @@ int exa_surrogate_get_macrocells(exa_context *ctx, uint8_t *mode, double *maxErr
 int exa_render_surrogate(exa_context *ctx, const exa_launch_params *lp, int32_t width, int32_t height)
 {
   return guarded([&] { renderFrame(ctx, lp, width, height, true); });
+}
+
+// ------------------------------------------------------------ batched frames
+namespace {
+BatchState &batchOf(exa_context *ctx)
+{
+  if (!ctx->batch) ctx->batch = std::make_unique<BatchState>();
+  return *ctx->batch;
+}
+
+// value ranges of the batch's majorant grid (Grid::build's kernels) and
+// every transfer function's max opacities on it
+void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
+{
+  const ExaStitchSampler &S = *ctx->sampler;
+  const ExaStitchModel &m = *ctx->model;
+  const size_t n = (size_t)B.dims.x * B.dims.y * B.dims.z;
+  B.ranges.alloc(n);
+  launchInitRanges(B.ranges.ptr, n, ctx->stream);
+  DBuf<exa_range1f> gr, er;
+  gr.alloc(std::max<size_t>(m.gridlets.size(), 1));
+  er.alloc(std::max<size_t>(m.indices.size() / 8, 1));
+  launchInitRanges(gr.ptr, gr.count, ctx->stream);
+  launchInitRanges(er.ptr, er.count, ctx->stream);
+  launchElemMajorants(S.vertexBuffer.ptr, S.indexBuffer.ptr, m.indices.size() / 8, B.dims, m.cellBounds, B.ranges.ptr,
+                      er.ptr, ctx->stream);
+  launchGridletMajorants(S.gridletBuffer.ptr, S.gridletScalarBuffer.ptr, m.gridlets.size(), B.dims, m.cellBounds,
+                         B.ranges.ptr, gr.ptr, ctx->stream);
+  B.maxOps.resize(B.tfColors.size());
+  for (size_t t = 0; t < B.tfColors.size(); ++t) {
+    B.maxOps[t].alloc(n);
+    launchMaxOpacity(B.ranges.ptr, n, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], B.maxOps[t].ptr, ctx->stream);
+  }
+  cudaCheck(cudaStreamSynchronize(ctx->stream), "batch majorants");
+}
+
+// the culling data of every transfer function (ExaStitchSampler::
+// computeMaxOpacities for each one, into the batch's own buffers)
+void rebuildBatchCulling(exa_context *ctx, BatchState &B)
+{
+  ExaStitchSampler &S = *ctx->sampler;
+  const size_t ng = S.gridletValueRanges.count, ne = (size_t)S.accel.numElems;
+  const size_t nt = B.tfColors.size();
+  B.gOps.clear();
+  B.eOps.clear();
+  B.nodes.clear();
+  B.gOps.resize(nt);
+  B.eOps.resize(nt);
+  B.nodes.resize(nt);
+  std::vector<AccelView> views(nt, S.accel);
+  for (size_t t = 0; t < nt; ++t) {
+    B.gOps[t].alloc(std::max<size_t>(ng, 1));
+    B.eOps[t].alloc(std::max<size_t>(S.elemValueRanges.count, 1));
+    launchMaxOpacity(S.gridletValueRanges.ptr, ng, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], B.gOps[t].ptr,
+                     ctx->stream);
+    launchMaxOpacity(S.elemValueRanges.ptr, S.elemValueRanges.count, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t],
+                     B.eOps[t].ptr, ctx->stream);
+    if (ne > 0) {
+      B.nodes[t].alloc(S.bvhNodes.count);
+      cudaCheck(cudaMemcpyAsync(B.nodes[t].ptr, S.bvhNodes.ptr, S.bvhNodes.bytes(), cudaMemcpyDeviceToDevice,
+                                ctx->stream), "copy BVH");
+      launchRefitBVH(S.vertexBuffer.ptr, S.indexBuffer.ptr, ne, B.nodes[t].ptr, S.bvhParents.ptr, S.bvhLeafElem.ptr,
+                     B.eOps[t].ptr, false, ctx->stream);
+      views[t].nodes = B.nodes[t].ptr;
+    }
+    views[t].gridletMaxOps = B.gOps[t].ptr;
+    views[t].elemMaxOps = B.eOps[t].ptr;
+  }
+  B.accels.upload(views.data(), nt, ctx->stream);
+  cudaCheck(cudaStreamSynchronize(ctx->stream), "batch culling");
+}
+
+void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch_frame *fr, int numFrames,
+                 bool useGraph)
+{
+  need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+  need(tpl != nullptr && fr != nullptr && numFrames > 0, EXA_ERR_INVALID, "no frames");
+  BatchState &B = batchOf(ctx);
+  need(!B.tfColors.empty(), EXA_ERR_STATE, "no transfer functions (exa_batch_set_transfer_functions)");
+  need(tpl->integrator == EXA_PATH_TRACING_INTEGRATOR || tpl->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
+       EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+  need(tpl->shadeMode == EXA_SHADE_MODE_DEFAULT || tpl->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
+       "shade mode not supported");
+  need(!tpl->clipPlanes[0].enabled && !tpl->subImage.active && !tpl->render.heatMapEnabled && tpl->meshBVH == 0,
+       EXA_ERR_INVALID, "clip planes, sub-image, heat map and surface meshes are not supported");
+  need(tpl->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
+       "lpTemplate.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
+  need(tpl->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+  need(B.tileW == 8 || B.tileW == 16 || B.tileW == 32, EXA_ERR_INVALID, "bad tile width");
+  setDevice(ctx);
+  const int th = 128 / B.tileW;
+  std::vector<exa_launch_params> lps((size_t)numFrames);
+  std::vector<WfFrame> frames((size_t)numFrames);
+  unsigned long long jobs = 0, samples = 0, pixels = 0;
+  for (int i = 0; i < numFrames; ++i) {
+    const exa_batch_frame &f = fr[i];
+    need(f.width > 0 && f.height > 0 && f.spp >= 1, EXA_ERR_INVALID, "bad frame size or spp");
+    need(f.tf >= 0 && f.tf < (int)B.tfColors.size(), EXA_ERR_INVALID, "frame transfer function out of range");
+    need(f.accumID == 0 || f.accumBuffer != nullptr, EXA_ERR_INVALID, "accumID > 0 needs an accumBuffer");
+    exa_launch_params lp = *tpl;
+    lp.camera.org = f.org;
+    lp.camera.dir_00 = f.dir_00;
+    lp.camera.dir_du = f.dir_du;
+    lp.camera.dir_dv = f.dir_dv;
+    lp.render.spp = f.spp;
+    lp.accumID = (int32_t)f.accumID;
+    lp.ext.frameID = f.frameID;
+    lp.fbPointer = f.fbPointer;
+    lp.accumBuffer = f.accumBuffer;
+    lp.transferFunc.values = reinterpret_cast<exa_vec4f *>(B.tfColors[f.tf].ptr);
+    lp.transferFunc.numValues = B.tfCount[f.tf];
+    lp.transferFunc.domain = B.tfRange[f.tf];
+    lp.transferFunc.opacityScale = B.tfScale[f.tf];
+    lp.maxOpacities = B.maxOps[f.tf].ptr;
+    lp.majorantGrid.dims = B.dims;
+    lp.majorantGrid.bounds = ctx->model->cellBounds;
+    lp.ext.traceT = nullptr;
+    lp.ext.traceTr = nullptr;
+    lp.ext.deviceErrors = ctx->errors.ptr;
+    lps[i] = lp;
+    WfFrame &F = frames[i];
+    F.width = f.width;
+    F.height = f.height;
+    F.tf = f.tf;
+    F.pad = 0;
+    F.jobBase = jobs;
+    F.sampleBase = samples;
+    F.pixelBase = pixels;
+    jobs += (unsigned long long)((f.width + B.tileW - 1) / B.tileW) * ((f.height + th - 1) / th) * 128ull *
+            (unsigned long long)f.spp;
+    samples += (unsigned long long)f.width * f.height * f.spp;
+    pixels += (unsigned long long)f.width * f.height;
+  }
+  // lps / frames keep their device addresses while the batch size stays
+  if (B.lps.count != (size_t)numFrames) {
+    B.lps.alloc(numFrames);
+    B.frames.alloc(numFrames);
+  }
+  cudaCheck(cudaMemcpyAsync(B.lps.ptr, lps.data(), lps.size() * sizeof(exa_launch_params), cudaMemcpyHostToDevice,
+                            ctx->stream), "frame table");
+  cudaCheck(cudaMemcpyAsync(B.frames.ptr, frames.data(), frames.size() * sizeof(WfFrame), cudaMemcpyHostToDevice,
+                            ctx->stream), "frame table");
+  if (!B.ctl.ptr) B.ctl.alloc(1);
+  if (B.colors.count < samples) B.colors.alloc(samples);
+  const unsigned cap = (unsigned)std::min<unsigned long long>(jobs, 1ull << 22);
+  if (B.cap < cap) {
+    B.records.alloc((size_t)3 * kWfLaneWords * cap);
+    B.counters.alloc(4);
+    B.cap = cap;
+  }
+  WfBatchView V;
+  V.accels = B.accels.ptr;
+  V.lps = B.lps.ptr;
+  V.frames = B.frames.ptr;
+  V.numFrames = numFrames;
+  V.tileW = B.tileW;
+  V.totalJobs = jobs;
+  V.totalPixels = pixels;
+  renderWavefrontBatch(ctx->sampler->accel, lps[0], V, B.records.ptr, B.cap, B.counters.ptr, B.ctl.ptr, B.colors.ptr,
+                       ctx->errors.ptr, useGraph, &B.graph, ctx->stream, &B.last);
+  ctx->lastStats = exa_render_stats{};
+  ctx->lastStats.wavefront = 2;
+  ctx->lastStats.rounds = B.last.rounds;
+  ctx->lastStats.peakQueue = B.last.peakQueue;
+  ctx->lastStats.queueCapacity = B.cap;
+  ctx->lastStats.walkLaunches = B.last.walkLaunches;
+  ctx->lastStats.walkMs = B.last.walkMs;
+}
+}  // namespace
+
+int exa_batch_set_transfer_functions(exa_context *ctx, int32_t numTFs, const exa_vec4f *const *colorMaps,
+                                     const int32_t *numColors, const exa_range1f *xfRanges,
+                                     const float *opacityScales)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(numTFs > 0 && colorMaps && numColors && xfRanges, EXA_ERR_INVALID, "no transfer functions");
+    setDevice(ctx);
+    BatchState &B = batchOf(ctx);
+    B.tfColors.clear();
+    B.tfColors.resize(numTFs);
+    B.tfCount.assign(numTFs, 0);
+    B.tfRange.assign(xfRanges, xfRanges + numTFs);
+    B.tfScale.assign(numTFs, 1.f);
+    for (int t = 0; t < numTFs; ++t) {
+      need(colorMaps[t] && numColors[t] > 0, EXA_ERR_INVALID, "empty colour map");
+      B.tfColors[t].upload(reinterpret_cast<const float4 *>(colorMaps[t]), (size_t)numColors[t], ctx->stream);
+      B.tfCount[t] = numColors[t];
+      if (opacityScales) B.tfScale[t] = opacityScales[t];
+    }
+    if (B.dims.x == 0) B.dims = ctx->model->grid->dims;
+    rebuildBatchMajorants(ctx, B);
+    rebuildBatchCulling(ctx, B);
+  });
+}
+
+int exa_batch_set_majorant_grid(exa_context *ctx, exa_vec3i dims)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
+    need(dims.x > 0 && dims.y > 0 && dims.z > 0 && (int64_t)dims.x * dims.y * dims.z <= (1ll << 30), EXA_ERR_INVALID,
+         "bad majorant grid");
+    setDevice(ctx);
+    BatchState &B = batchOf(ctx);
+    B.dims = dims;
+    rebuildBatchMajorants(ctx, B);
+  });
+}
+
+int exa_batch_set_tile_width(exa_context *ctx, int32_t tileWidth)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_STATE, "no context");
+    need(tileWidth == 8 || tileWidth == 16 || tileWidth == 32, EXA_ERR_INVALID, "tile width must be 8, 16 or 32");
+    batchOf(ctx).tileW = tileWidth;
+  });
+}
+
+int exa_render_batch(exa_context *ctx, const exa_launch_params *lpTemplate, const exa_batch_frame *frames,
+                     int32_t numFrames, int32_t useGraph)
+{
+  return guarded([&] { renderBatch(ctx, lpTemplate, frames, numFrames, useGraph != 0); });
+}
+
+int exa_batch_autotune(exa_context *ctx, const exa_launch_params *lpTemplate, const exa_batch_frame *frames,
+                       int32_t numFrames, int32_t sampleEvery, exa_batch_tuning *out)
+{
+  return guarded([&] {
+    need(ctx && ctx->sampler && frames && numFrames > 0 && out, EXA_ERR_INVALID, "bad arguments");
+    need(sampleEvery >= 1, EXA_ERR_INVALID, "sampleEvery must be >= 1");
+    setDevice(ctx);
+    BatchState &B = batchOf(ctx);
+    need(!B.tfColors.empty(), EXA_ERR_STATE, "no transfer functions (exa_batch_set_transfer_functions)");
+    // the sampled workload: every sampleEvery-th frame at 1 spp, no outputs
+    std::vector<exa_batch_frame> sub;
+    for (int i = 0; i < numFrames; i += sampleEvery) {
+      exa_batch_frame f = frames[i];
+      f.spp = 1;
+      f.accumID = 0;
+      f.fbPointer = nullptr;
+      f.accumBuffer = nullptr;
+      sub.push_back(f);
+    }
+    std::memset(out, 0, sizeof(*out));
+    const int res[4] = {32, 64, 128, 256};
+    const int tiles[3] = {8, 16, 32};
+    cudaEvent_t e0, e1;
+    cudaCheck(cudaEventCreate(&e0), "cudaEventCreate");
+    cudaCheck(cudaEventCreate(&e1), "cudaEventCreate");
+    struct EvGuard {
+      cudaEvent_t a, b;
+      ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } evGuard{e0, e1};
+    float best = 1e30f;
+    exa_vec3i bestDims{0, 0, 0};
+    int bestTile = 16;
+    for (int r : res) {
+      B.dims = exa_vec3i{r, r, r};
+      rebuildBatchMajorants(ctx, B);
+      for (int tw : tiles) {
+        B.tileW = tw;
+        renderBatch(ctx, lpTemplate, sub.data(), (int)sub.size(), true);  // builds the graph
+        cudaCheck(cudaEventRecord(e0, ctx->stream), "event");
+        renderBatch(ctx, lpTemplate, sub.data(), (int)sub.size(), true);
+        cudaCheck(cudaEventRecord(e1, ctx->stream), "event");
+        cudaCheck(cudaStreamSynchronize(ctx->stream), "autotune");
+        float ms = 0.f;
+        cudaCheck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+        const int k = out->numTrials++;
+        out->trialDims[k] = B.dims;
+        out->trialTileWidth[k] = tw;
+        out->trialMs[k] = ms;
+        if (ms < best) { best = ms; bestDims = B.dims; bestTile = tw; }
+      }
+    }
+    B.dims = bestDims;
+    B.tileW = bestTile;
+    rebuildBatchMajorants(ctx, B);
+    out->dims = bestDims;
+    out->tileWidth = bestTile;
+    out->msBest = best;
+  });
 }
 
 } // extern "C"

@@ -237,6 +237,51 @@ struct Surrogate {
 void launchSurrogatePoints(const SurrogateView &S, const exa_vec3f *pos, size_t n, float *out, cudaStream_t s);
 bool useWavefront();
 constexpr int kWfLaneWords = 61;
+
+// ---------------------------------------------------------- batched frames
+struct WfFrame {                    // per frame of a batch (device table)
+  int width, height;
+  int tf, pad;                      // transfer function (index into WfBatchView.accels)
+  unsigned long long jobBase;       // first job of the frame in the batch
+  unsigned long long sampleBase;    // first colour slot of the frame
+  unsigned long long pixelBase;     // first pixel of the frame (resolve)
+};
+struct WfBatchView {
+  const AccelView *accels;          // per transfer function: primitive culling opacities (device)
+  const exa_launch_params *lps;     // per frame (device)
+  const WfFrame *frames;            // per frame (device)
+  int numFrames;
+  int tileW;                        // job tile width (tile height 128 / tileW)
+  unsigned long long totalJobs, totalPixels;
+};
+struct WfCtl {                      // device-side round control
+  unsigned long long issued;
+  unsigned nIn, nNew, rounds, peak;
+  int flip;
+  unsigned more, error;
+};
+constexpr unsigned kBatchRoundCap = 1u << 20;
+struct BatchKey {
+  const void *accel, *accels, *lps, *frames;
+  int numFrames, tileW;
+  unsigned long long totalJobs, totalPixels;
+  const void *bufs;
+  unsigned cap;
+  const void *counters, *ctl, *colors, *errors;
+  int integrator;
+  unsigned grid, walkGrid;
+};
+struct BatchGraph {                 // instantiated graph of one batch shape
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  BatchKey key{};
+  cudaStream_t captureStream = nullptr;
+  void release();
+  ~BatchGraph();
+};
+void renderWavefrontBatch(const AccelView &A, const exa_launch_params &lp0, const WfBatchView &B, uint32_t *bufs,
+                          unsigned cap, unsigned *counters, WfCtl *ctl, float4 *colors, uint32_t *deviceErrors,
+                          bool useGraph, BatchGraph *cache, cudaStream_t s, WfStats *stats);
 void launchSamplePoints(const AccelView &A, const exa_vec3f *pos, size_t n, exa_sample *out, int cull,
                         uint32_t *errors, cudaStream_t s);
 void launchRender(const AccelView &A, const exa_launch_params &lp, int width, int height, unsigned *jobCounter,

@@ -9,6 +9,7 @@
 // The launch parameters and the accel view are kernel parameters (constant
 // bank).
 #include <algorithm>
+#include <cstring>
 
 #include "exa_host.h"
 #include "exa_surrogate.cuh"
@@ -337,11 +338,12 @@ enum : int { PH_FETCH = 0, PH_TRACK = 1, PH_DONE = 2 };
 
 struct Lane {
   int px, py, pixelID, s;
+  int frame = 0;           // frame of a batch (0 for a single frame)
   RayS ray;
   V3 throughput, Ld, pos, albedo;
   unsigned bounce;
   float lightDen, lightI;  // point light: (Tr / lightDen) * lightI; directional: Tr * lightI
-  bool lightDirectional;
+  bool lightDirectional = false;
   bool shadow;             // the running walk is a shadow walk
   int phase;
   Rng rng;
@@ -863,7 +865,7 @@ EXA_D void wf_store_path(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
   WF(L.ray.org.x); WF(L.ray.org.y); WF(L.ray.org.z); WF(L.ray.dir.x); WF(L.ray.dir.y); WF(L.ray.dir.z); WF(L.ray.tmax);
   WF(L.throughput.x); WF(L.throughput.y); WF(L.throughput.z); WF(L.Ld.x); WF(L.Ld.y); WF(L.Ld.z);
   WF(L.pos.x); WF(L.pos.y); WF(L.pos.z); WF(L.albedo.x); WF(L.albedo.y); WF(L.albedo.z);
-  W(L.bounce); WF(L.lightDen); WF(L.lightI); W((uint32_t)L.lightDirectional);
+  W(L.bounce); WF(L.lightDen); WF(L.lightI); W((L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1));
 }
 
 EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width)
@@ -877,7 +879,10 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   L.Ld.x = RF(); L.Ld.y = RF(); L.Ld.z = RF();
   L.pos.x = RF(); L.pos.y = RF(); L.pos.z = RF();
   L.albedo.x = RF(); L.albedo.y = RF(); L.albedo.z = RF();
-  L.bounce = R(); L.lightDen = RF(); L.lightI = RF(); L.lightDirectional = R() != 0u;
+  L.bounce = R(); L.lightDen = RF(); L.lightI = RF();
+  const uint32_t lf = R();
+  L.lightDirectional = (lf & 1u) != 0u;
+  L.frame = (int)(lf >> 1);
 }
 
 // shadow flag, RNG and the walk
@@ -1253,6 +1258,406 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   }
   k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
   cudaCheck(cudaGetLastError(), "k_resolve");
+}
+
+// ======================================================== batched frames
+// Many frames -- each with its own camera, size, spp, transfer function and
+// output buffers, given as a full launch-parameter block per frame -- share
+// one set of queues.  The batch's jobs are the frames' jobs one after the
+// other, a path record carries its frame, and every kernel reads the
+// frame's parameters (and the point-location view of the frame's transfer
+// function, whose primitive opacities decide culling) where the
+// single-frame kernels read the launch's, so each frame's result is the one
+// exa_render gives for it.  Rounds are driven from the device: after each
+// round an update kernel moves the queue counters and decides whether
+// another round runs, which lets the whole batch be one CUDA graph (a
+// conditional while node around the round).
+
+EXA_D int batch_frame_of(const WfFrame *F, int n, unsigned long long v, bool pixels)
+{
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const unsigned long long b = pixels ? F[mid].pixelBase : F[mid].jobBase;
+    if (b <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct WfQueuesB {
+  uint32_t *buf[2];  // input / output queues, swapped every round (WfCtl.flip)
+  uint32_t *ev;
+  unsigned *cnt;     // [0] in, [1] out, [2] ev, [3] walk fetch cursor
+  unsigned cap;
+};
+
+__global__ void k_wfb_init(WfCtl *ctl, unsigned *cnt)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    ctl->issued = 0;
+    ctl->nIn = 0;
+    ctl->nNew = 0;
+    ctl->rounds = 0;
+    ctl->peak = 0;
+    ctl->flip = 0;
+    ctl->more = 1;
+    ctl->error = 0;
+    for (int k = 0; k < 4; ++k) cnt[k] = 0;
+  }
+}
+
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128) k_wfb_camera(const __grid_constant__ AccelView A,
+                                                    const __grid_constant__ exa_launch_params lp0, WfBatchView B,
+                                                    WfQueuesB Q, WfCtl *ctl, float4 *colors)
+{
+  PathCtx c = make_ctx(A, lp0);
+  const unsigned long long first = ctl->issued;
+  const unsigned nIn = ctl->nIn;
+  const unsigned long long left = B.totalJobs - first;
+  const unsigned n = (unsigned)(left < (unsigned long long)(Q.cap - nIn) ? left : (unsigned long long)(Q.cap - nIn));
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->nNew = n;
+  uint32_t *in = Q.buf[ctl->flip];
+  const int tw = B.tileW, th = 128 / B.tileW;
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + threadIdx.x;
+    Lane L;
+    bool tracking = false;
+    if (i < n) {
+      const unsigned long long job = first + i;
+      const int f = batch_frame_of(B.frames, B.numFrames, job, false);
+      const WfFrame F = B.frames[f];
+      const exa_launch_params &flp = B.lps[f];
+      PathCtx cf{A, flp, 0u, c.counting};
+      Machine<INTEGRATOR> M{cf, flp, F.width, F.height, num_lights(flp), (unsigned)flp.ext.maxBounces,
+                            colors + F.sampleBase};
+      const unsigned long long local = job - F.jobBase;
+      const unsigned spp = (unsigned)flp.render.spp;
+      const unsigned long long pj = local / spp;
+      L.s = (int)(local - pj * spp);
+      L.frame = f;
+      const int tilesX = (F.width + tw - 1) / tw;
+      const int tile = (int)(pj >> 7), within = (int)(pj & 127);
+      L.px = (tile % tilesX) * tw + within % tw;
+      L.py = (tile / tilesX) * th + within / tw;
+      if (L.px < F.width && L.py < F.height) {
+        M.begin_sample(L);
+        tracking = L.phase == PH_TRACK;
+      }
+      c.err |= cf.err;
+    }
+    const unsigned slot = warp_append(&Q.cnt[0], tracking);
+    if (tracking) wf_store(L, in, Q.cap, slot);
+  }
+  flush_counters(c, lp0);
+}
+
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const __grid_constant__ AccelView A,
+                                                                         const __grid_constant__ exa_launch_params lp0,
+                                                                         WfBatchView B, WfQueuesB Q, const WfCtl *ctl)
+{
+  PathCtx c = make_ctx(A, lp0);
+  const unsigned n = Q.cnt[0];
+  const int flip = ctl->flip;
+  const uint32_t *in = Q.buf[flip];
+  uint32_t *out = Q.buf[flip ^ 1];
+  const bool park = n >= 4u * gridDim.x * blockDim.x;
+  const unsigned lane = threadIdx.x & 31;
+  Lane L;
+  const exa_launch_params *flp = &lp0;
+  const AccelView *fa = &A;  // the frame's transfer function decides which primitives are culled
+  bool active = false, exhausted = false;
+  unsigned src = 0;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active);
+    if (need && !exhausted) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(&Q.cnt[3], (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (unsigned)__popc(need) >= n) exhausted = true;
+      if (!active) {
+        const unsigned idx = base + __popc(need & ((1u << lane) - 1u));
+        if (idx < n) {
+          wf_load_walk(L, in, Q.cap, idx, lp0.majorantGrid);
+          // the frame index sits in the path part of the record
+          L.frame = (int)(__ldg(in + (size_t)(kPathWords - 1) * Q.cap + idx) >> 1);
+          flp = B.lps + L.frame;
+          fa = B.accels + B.frames[L.frame].tf;
+          active = true;
+          src = idx;
+          cnt_add(c, CNT_WALKS);
+        }
+      }
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    if (exhausted && park && __popc(act) < EXA_WF_PARK_LANES) {
+      const unsigned slot = warp_append(&Q.cnt[1], active);
+      if (active) {
+        wf_store_walk(L, out, Q.cap, slot);
+        wf_copy_path(in, src, out, slot, Q.cap);
+      }
+      break;
+    }
+    bool ended = false;
+    if (active) {
+      PathCtx cf{*fa, *flp, 0u, c.counting};
+      ended = !walk_step(L.w, cf, L.rng, L.shadow);
+      c.err |= cf.err;
+    }
+    const unsigned slot = warp_append(&Q.cnt[2], ended);
+    if (ended) {
+      wf_store_walk(L, Q.ev, Q.cap, slot);
+      wf_copy_path(in, src, Q.ev, slot, Q.cap);
+      active = false;
+    }
+  }
+  flush_counters(c, lp0);
+}
+
+template <int INTEGRATOR>
+__global__ void __launch_bounds__(128) k_wfb_events(const __grid_constant__ AccelView A,
+                                                    const __grid_constant__ exa_launch_params lp0, WfBatchView B,
+                                                    WfQueuesB Q, const WfCtl *ctl, float4 *colors)
+{
+  PathCtx c = make_ctx(A, lp0);
+  const unsigned n = Q.cnt[2];
+  uint32_t *out = Q.buf[ctl->flip ^ 1];
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + threadIdx.x;
+    Lane L;
+    bool tracking = false;
+    if (i < n) {
+      wf_load(L, Q.ev, Q.cap, i, 0, lp0.majorantGrid);
+      const WfFrame F = B.frames[L.frame];
+      L.pixelID = L.px + F.width * L.py;
+      const exa_launch_params &flp = B.lps[L.frame];
+      PathCtx cf{A, flp, 0u, c.counting};
+      Machine<INTEGRATOR> M{cf, flp, F.width, F.height, num_lights(flp), (unsigned)flp.ext.maxBounces,
+                            colors + F.sampleBase};
+      L.phase = PH_TRACK;
+      if (L.shadow) M.shadow_done(L);
+      else M.primary_done(L);
+      tracking = L.phase == PH_TRACK;
+      c.err |= cf.err;
+    }
+    const unsigned slot = warp_append(&Q.cnt[1], tracking);
+    if (tracking) wf_store(L, out, Q.cap, slot);
+  }
+  flush_counters(c, lp0);
+}
+
+// end of a round: the output queue becomes the next input; another round
+// runs while walks remain or camera jobs are left.  A round cap stops a
+// batch that makes no progress (error bit EXA_DEVERR_WATCHDOG).
+__global__ void k_wfb_update(WfBatchView B, WfQueuesB Q, WfCtl *ctl, uint32_t *deviceErrors,
+                             cudaGraphConditionalHandle handle, int useHandle)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned nOut = Q.cnt[1], nEv = Q.cnt[2];
+  ctl->issued += ctl->nNew;
+  ctl->nIn = nOut;
+  ctl->rounds += 1;
+  if (nEv > ctl->peak) ctl->peak = nEv;
+  ctl->flip ^= 1;
+  Q.cnt[0] = nOut;
+  Q.cnt[1] = 0;
+  Q.cnt[2] = 0;
+  Q.cnt[3] = 0;
+  unsigned more = (nOut > 0 || ctl->issued < B.totalJobs) ? 1u : 0u;
+  if (more && ctl->rounds >= kBatchRoundCap) {
+    more = 0;
+    ctl->error = 1;
+    if (deviceErrors) atomicOr(deviceErrors, EXA_DEVERR_WATCHDOG);
+  }
+  ctl->more = more;
+  if (useHandle) cudaGraphSetConditional(handle, more);
+}
+
+// resolve of every frame's pixels (k_resolve per frame)
+__global__ void k_wfb_resolve(WfBatchView B, const float4 *__restrict__ colors)
+{
+  const unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (p >= B.totalPixels) return;
+  const int f = batch_frame_of(B.frames, B.numFrames, p, true);
+  const WfFrame F = B.frames[f];
+  const exa_launch_params &lp = B.lps[f];
+  const int pixelID = (int)(p - F.pixelBase);
+  const int spp = lp.render.spp;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 *cp = colors + F.sampleBase + (size_t)pixelID * spp;
+  for (int s = 0; s < spp; ++s) {
+    const float4 col = __ldg(cp + s);
+    acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
+  }
+  if (lp.accumID > 0 && lp.accumBuffer) {
+    const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
+    acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+  }
+  if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[pixelID] = acc;
+  const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
+  acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+  const float is = __fdiv_rn(1.f, (float)spp);
+  const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
+                        (make_8bit(acc.w * is) << 24);
+  if (lp.fbPointer) lp.fbPointer[pixelID] = rgba;
+}
+
+namespace {
+// the kernels of one round (camera, walk, events, update) on stream s
+void batchRound(const AccelView &A, const exa_launch_params &lp0, const WfBatchView &B, const WfQueuesB &Q,
+                WfCtl *ctl, float4 *colors, uint32_t *deviceErrors, cudaGraphConditionalHandle handle,
+                int useHandle, unsigned grid, unsigned walkGrid, cudaStream_t s)
+{
+  const bool pt = lp0.integrator == EXA_PATH_TRACING_INTEGRATOR;
+  if (pt) k_wfb_camera<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp0, B, Q, ctl, colors);
+  else k_wfb_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp0, B, Q, ctl, colors);
+  k_wfb_walk<<<walkGrid, 128, 0, s>>>(A, lp0, B, Q, ctl);
+  if (pt) k_wfb_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp0, B, Q, ctl, colors);
+  else k_wfb_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp0, B, Q, ctl, colors);
+  k_wfb_update<<<1, 32, 0, s>>>(B, Q, ctl, deviceErrors, handle, useHandle);
+}
+}  // namespace
+
+void BatchGraph::release()
+{
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  exec = nullptr;
+  graph = nullptr;
+}
+
+BatchGraph::~BatchGraph()
+{
+  release();
+  if (captureStream) cudaStreamDestroy(captureStream);
+}
+
+void renderWavefrontBatch(const AccelView &A, const exa_launch_params &lp0, const WfBatchView &B, uint32_t *bufs,
+                          unsigned cap, unsigned *counters, WfCtl *ctl, float4 *colors, uint32_t *deviceErrors,
+                          bool useGraph, BatchGraph *cache, cudaStream_t s, WfStats *stats)
+{
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  int perSM = 4;
+  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wfb_walk, 128, 0), "occupancy");
+  const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
+  const unsigned grid = (unsigned)sms * 16;
+  const size_t words = (size_t)kLaneWords * cap;
+  WfQueuesB Q{{bufs, bufs + words}, bufs + 2 * words, counters, cap};
+  const unsigned long long totalPixels = B.totalPixels;
+  cudaEvent_t e0, e1;
+  cudaCheck(cudaEventCreate(&e0), "cudaEventCreate");
+  cudaCheck(cudaEventCreate(&e1), "cudaEventCreate");
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+  } evGuard{e0, e1};
+  cudaCheck(cudaEventRecord(e0, s), "event");
+  if (useGraph) {
+    // the graph bakes in every pointer and the batch's shape; the frame
+    // tables it reads are device memory, so new cameras need no rebuild
+    BatchKey key;
+    std::memset(&key, 0, sizeof(key));  // padding too: keys are compared bytewise
+    key.accel = A.gridlets;
+    key.accels = B.accels;
+    key.lps = B.lps;
+    key.frames = B.frames;
+    key.numFrames = B.numFrames;
+    key.tileW = B.tileW;
+    key.totalJobs = B.totalJobs;
+    key.totalPixels = B.totalPixels;
+    key.bufs = bufs;
+    key.cap = cap;
+    key.counters = counters;
+    key.ctl = ctl;
+    key.colors = colors;
+    key.errors = deviceErrors;
+    key.integrator = lp0.integrator;
+    key.grid = grid;
+    key.walkGrid = walkGrid;
+    if (!cache->exec || std::memcmp(&cache->key, &key, sizeof(key)) != 0) {
+      cache->release();
+      // captured on the cache's own stream (the legacy default stream, which
+      // a caller may render on, cannot be captured); launched on s
+      if (!cache->captureStream)
+        cudaCheck(cudaStreamCreateWithFlags(&cache->captureStream, cudaStreamNonBlocking), "capture stream");
+      cudaStream_t cs = cache->captureStream;
+      // load every kernel of the graph before capturing (lazy module loading)
+      cudaFuncAttributes fa;
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_init), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_camera<EXA_PATH_TRACING_INTEGRATOR>), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_camera<EXA_DIRECT_LIGHT_INTEGRATOR>), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_walk), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_events<EXA_PATH_TRACING_INTEGRATOR>), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_events<EXA_DIRECT_LIGHT_INTEGRATOR>), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_update), "load");
+      cudaCheck(cudaFuncGetAttributes(&fa, k_wfb_resolve), "load");
+      cudaCheck(cudaStreamSynchronize(s), "batch inputs");
+      cudaGraph_t g;
+      cudaCheck(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+      cache->graph = g;
+      cudaGraphConditionalHandle handle;
+      cudaCheck(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault), "conditional handle");
+      cudaCheck(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                "capture");
+      k_wfb_init<<<1, 1, 0, cs>>>(ctl, counters);
+      cudaStreamCaptureStatus st;
+      const cudaGraphNode_t *deps = nullptr;
+      size_t ndeps = 0;
+      cudaCheck(cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &ndeps), "capture info");
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t loop;
+      cudaCheck(cudaGraphAddNode(&loop, g, deps, nullptr, ndeps, &cp), "conditional node");
+      cudaCheck(cudaStreamUpdateCaptureDependencies(cs, &loop, nullptr, 1, cudaStreamSetCaptureDependencies),
+                "capture dependencies");
+      k_wfb_resolve<<<(unsigned)((totalPixels + 255) / 256), 256, 0, cs>>>(B, colors);
+      cudaGraph_t captured = nullptr;
+      cudaCheck(cudaStreamEndCapture(cs, &captured), "end capture");
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      cudaCheck(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                "capture body");
+      batchRound(A, lp0, B, Q, ctl, colors, deviceErrors, handle, 1, grid, walkGrid, cs);
+      cudaGraph_t bodyOut = nullptr;
+      cudaCheck(cudaStreamEndCapture(cs, &bodyOut), "end capture body");
+      cudaCheck(cudaGraphInstantiate(&cache->exec, g, 0), "cudaGraphInstantiate");
+      cache->key = key;
+    }
+    cudaCheck(cudaGraphLaunch(cache->exec, s), "cudaGraphLaunch");
+  } else {
+    k_wfb_init<<<1, 1, 0, s>>>(ctl, counters);
+    for (unsigned round = 0; round < kBatchRoundCap; ++round) {
+      batchRound(A, lp0, B, Q, ctl, colors, deviceErrors, 0, 0, grid, walkGrid, s);
+      cudaCheck(cudaGetLastError(), "batch round");
+      unsigned more = 0;
+      cudaCheck(cudaMemcpyAsync(&more, &ctl->more, sizeof(more), cudaMemcpyDeviceToHost, s), "read ctl");
+      cudaCheck(cudaStreamSynchronize(s), "batch round");
+      if (!more) break;
+    }
+    k_wfb_resolve<<<(unsigned)((totalPixels + 255) / 256), 256, 0, s>>>(B, colors);
+  }
+  cudaCheck(cudaGetLastError(), "batch");
+  cudaCheck(cudaEventRecord(e1, s), "event");
+  if (stats) {
+    WfCtl h;
+    cudaCheck(cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, s), "read ctl");
+    cudaCheck(cudaStreamSynchronize(s), "batch");
+    float ms = 0.f;
+    cudaCheck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+    stats->rounds = h.rounds;
+    stats->peakQueue = h.peak;
+    stats->walkLaunches = h.rounds;
+    stats->cameraMs = 0.f;
+    stats->walkMs = ms;  // whole batch (kernel classes are not timed apart inside a graph)
+    stats->eventMs = 0.f;
+  }
 }
 
 // EXA_RENDER_STRATEGY (the single-launch renderer): 1 thread per pixel,

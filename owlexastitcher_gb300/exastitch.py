@@ -206,6 +206,17 @@ class SurrogateGeometry(C.Structure):
 
 SURROGATE_PARAMS = 64 * 32 + 64 * 64 + 64  # W1 | W2 | w3
 
+
+class BatchFrame(C.Structure):
+    _fields_ = [("org", vec3f), ("dir_00", vec3f), ("dir_du", vec3f), ("dir_dv", vec3f), ("width", C.c_int32),
+                ("height", C.c_int32), ("spp", C.c_int32), ("tf", C.c_int32), ("accumID", C.c_uint32),
+                ("frameID", C.c_uint32), ("fbPointer", C.c_void_p), ("accumBuffer", C.c_void_p)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("dims", vec3i), ("tileWidth", C.c_int32), ("msBest", C.c_float), ("numTrials", C.c_int32),
+                ("trialDims", vec3i * 16), ("trialTileWidth", C.c_int32 * 16), ("trialMs", C.c_float * 16)]
+
 GRIDLET_DTYPE = np.dtype([("lower", "<i4", 3), ("level", "<i4"), ("dims", "<i4", 3), ("begin", "<u4")])
 SAMPLE_DTYPE = np.dtype([("primID", "<i4"), ("cellID", "<i4"), ("value", "<f4")])
 
@@ -219,7 +230,8 @@ EXPORTED = [
     "exa_surrogate_params_default", "exa_surrogate_create", "exa_surrogate_train", "exa_surrogate_evaluate",
     "exa_surrogate_get_stats", "exa_surrogate_get_geometry", "exa_surrogate_sample_points",
     "exa_surrogate_get_params", "exa_surrogate_set_params", "exa_surrogate_gradients",
-    "exa_surrogate_get_macrocells", "exa_render_surrogate",
+    "exa_surrogate_get_macrocells", "exa_render_surrogate", "exa_batch_set_transfer_functions",
+    "exa_batch_set_majorant_grid", "exa_batch_set_tile_width", "exa_render_batch", "exa_batch_autotune",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -272,13 +284,18 @@ def lib():
         "exa_surrogate_gradients": ([ctx_p, vp, i32, vp, vp, vp], C.c_int),
         "exa_surrogate_get_macrocells": ([ctx_p, vp, vp, vp], C.c_int),
         "exa_render_surrogate": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
+        "exa_batch_set_transfer_functions": ([ctx_p, i32, vp, vp, vp, vp], C.c_int),
+        "exa_batch_set_majorant_grid": ([ctx_p, vec3i], C.c_int),
+        "exa_batch_set_tile_width": ([ctx_p, i32], C.c_int),
+        "exa_render_batch": ([ctx_p, C.POINTER(LaunchParams), vp, i32, i32], C.c_int),
+        "exa_batch_autotune": ([ctx_p, C.POINTER(LaunchParams), vp, i32, i32, C.POINTER(BatchTuning)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = res
     for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt), (5, SurrogateParams),
-                    (6, SurrogateStats), (7, SurrogateGeometry)):
+                    (6, SurrogateStats), (7, SurrogateGeometry), (8, BatchFrame), (9, BatchTuning)):
         if L.exa_abi_sizeof(key) != C.sizeof(st):
             raise RuntimeError(f"ABI layout mismatch for {st.__name__}: C {L.exa_abi_sizeof(key)} vs ctypes {C.sizeof(st)}")
     _lib = L
@@ -615,3 +632,52 @@ class Surrogate:
         maj = np.zeros(num_mcs, np.float32)
         _check(lib().exa_surrogate_get_macrocells(self.ctx.h, _np_ptr(mode), _np_ptr(err), _np_ptr(maj)))
         return mode, err, maj
+
+
+class Batch:
+    """Many frames in one wavefront (exa_render_batch): per-frame camera,
+    size, spp, transfer function and output buffers."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self._keep = None
+
+    def set_transfer_functions(self, tfs, xf_ranges, opacity_scales=None):
+        maps = [np.ascontiguousarray(t, np.float32).reshape(-1, 4) for t in tfs]
+        ptrs = (C.c_void_p * len(maps))(*[m.ctypes.data for m in maps])
+        counts = np.array([len(m) for m in maps], np.int32)
+        ranges = np.ascontiguousarray(np.array(xf_ranges, np.float32).reshape(-1, 2))
+        scales = np.ones(len(maps), np.float32) if opacity_scales is None else np.asarray(opacity_scales, np.float32)
+        _check(lib().exa_batch_set_transfer_functions(self.ctx.h, len(maps), ptrs, _np_ptr(counts), _np_ptr(ranges),
+                                                      _np_ptr(scales)))
+
+    def set_majorant_grid(self, dims):
+        _check(lib().exa_batch_set_majorant_grid(self.ctx.h, vec3i(*[int(d) for d in dims])))
+
+    def set_tile_width(self, w):
+        _check(lib().exa_batch_set_tile_width(self.ctx.h, int(w)))
+
+    @staticmethod
+    def frames(specs):
+        """specs: dicts with cam (org, dir_00, dir_du, dir_dv), width, height,
+        spp, tf, and optional accumID, frameID, fb, accum (device pointers)"""
+        arr = (BatchFrame * len(specs))()
+        for f, sp in zip(arr, specs):
+            org, d00, du, dv = sp["cam"]
+            f.org, f.dir_00, f.dir_du, f.dir_dv = _v3(org), _v3(d00), _v3(du), _v3(dv)
+            f.width, f.height, f.spp, f.tf = sp["width"], sp["height"], sp["spp"], sp["tf"]
+            f.accumID, f.frameID = sp.get("accumID", 0), sp.get("frameID", 0)
+            f.fbPointer, f.accumBuffer = sp.get("fb"), sp.get("accum")
+        return arr
+
+    def render(self, lp, frames, graph=True):
+        self._keep = frames
+        _check(lib().exa_render_batch(self.ctx.h, C.byref(lp), C.cast(frames, C.c_void_p), len(frames), int(graph)))
+
+    def autotune(self, lp, frames, sample_every=8):
+        t = BatchTuning()
+        _check(lib().exa_batch_autotune(self.ctx.h, C.byref(lp), C.cast(frames, C.c_void_p), len(frames),
+                                        int(sample_every), C.byref(t)))
+        return {"dims": (t.dims.x, t.dims.y, t.dims.z), "tileWidth": t.tileWidth, "msBest": t.msBest,
+                "trials": [((t.trialDims[i].x, t.trialDims[i].y, t.trialDims[i].z), t.trialTileWidth[i], t.trialMs[i])
+                           for i in range(t.numTrials)]}
