@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--profile-only", action="store_true", help="warm-up + 1 step, no extras (for ncu)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-field (surrogate) measurements")
     ap.add_argument("--learned-steps", type=int, default=1600, help="surrogate training steps")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-frames measurements")
     return ap.parse_args()
 
 
@@ -271,6 +272,10 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
 
+    batched = None
+    if rank == 0 and not a.no_batched:
+        batched = run_batched(a, local, flush)
+
     learned = None
     if rank == 0 and not a.no_learned:
         from owlexastitcher_gb300 import datagen
@@ -305,6 +310,7 @@ def run_ours(a):
             "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
             "render": render_stats,
             "learned_field": learned,
+            "batched_frames": batched,
             "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
                                                   "numWedges", "numHexes", "numTets")} | {
                 "field_bytes": ds.field_bytes, "gen_seconds": gen_s},
@@ -416,6 +422,115 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3):
         "paths_per_s_learned_over_exact": res["learned"]["paths_per_s"] / res["exact"]["paths_per_s"],
         "image_rmse_vs_exact_same_rng": rmse,
         "point_queries_per_s": q,
+    }
+    ctx.close()
+    return out
+
+
+def run_batched(a, local, flush):
+    """256 frames of the small config's field (64 seeded orbit cameras x 4
+    transfer functions, square sides drawn from 256..1024, 4 spp, path
+    tracing) in one wavefront: autotuned and at the 32^3 grid, run as one
+    CUDA graph, against the same frames rendered one exa_render call after
+    another (grouped by transfer function)."""
+    import ctypes as C
+    import torch
+    from helpers import orbit_camera, ramp_tf, random_tf, setup_render, step_tf, two_peak_tf
+    from owlexastitcher_gb300 import datagen
+    from owlexastitcher_gb300 import exastitch as E
+    ds = datagen.Dataset("small")
+    ctx = E.Context(local)
+    model = E.ExaStitchModel.from_dataset(ctx, ds)
+    model.setNumGridCells((32, 32, 32))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    lo, hi = model.cellBounds
+    vr = model.valueRange
+    xf = (np.float32(vr[0]), np.float32(vr[1]))
+    tfs = [ramp_tf(), step_tf(), two_peak_tf(), random_tf()]
+    sampler.computeMaxOpacities(tfs[0], xf)
+    lp = E.new_launch_params()
+    sampler.setLPs(lp)
+    setup_render(lp, orbit_camera(lo, hi, 8, 8), 8, 8, E.PATH_TRACING_INTEGRATOR, 4, "directional", True)
+    lp.ext.traceT = lp.ext.traceTr = None
+    rng = np.random.default_rng(1234)
+    spp = 4
+    specs, bufs = [], []
+    for cam_i in range(64):
+        angle = 2 * np.pi * cam_i / 64 + rng.uniform(-0.05, 0.05)
+        elev = rng.uniform(0.1, 0.6)
+        for t in range(4):
+            side = int(rng.choice([256, 512, 768, 1024]))
+            cam = orbit_camera(lo, hi, side, side, angle=angle, elev=elev)
+            fb = torch.zeros(side * side, dtype=torch.int32, device="cuda")
+            bufs.append(fb)
+            specs.append({"cam": cam, "width": side, "height": side, "spp": spp, "tf": t,
+                          "frameID": cam_i * 4 + t, "fb": fb.data_ptr()})
+    paths = sum(s_["width"] * s_["height"] * s_["spp"] for s_ in specs)
+    stream = torch.cuda.current_stream()
+    B = E.Batch(ctx)
+    B.set_transfer_functions(tfs, [xf] * 4)
+    frames = B.frames(specs)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.fill_(4.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        ctx.sync()
+        return min(ms)
+
+    # the model's 32^3 grid, tile width 16
+    B.set_majorant_grid((32, 32, 32))
+    B.set_tile_width(16)
+    ms_fixed = timed(lambda: B.render(lp, frames, graph=True))
+    st_fixed = ctx.render_stats()
+    ms_host = timed(lambda: B.render(lp, frames, graph=False), reps=1)
+    # autotuned (every 16th frame at 1 spp for the trials)
+    t0 = time.perf_counter()
+    tune = B.autotune(lp, frames, sample_every=16)
+    tune_s = time.perf_counter() - t0
+    ms_tuned = timed(lambda: B.render(lp, frames, graph=True))
+    st_tuned = ctx.render_stats()
+
+    # the same frames one exa_render call after another
+    def sequential():
+        for t in range(4):
+            sampler.computeMaxOpacities(tfs[t], xf)
+            sampler.setLPs(lp)
+            for sp in specs:
+                if sp["tf"] != t:
+                    continue
+                org, d00, du, dv = sp["cam"]
+                lp.camera.org, lp.camera.dir_00, lp.camera.dir_du, lp.camera.dir_dv = (E._v3(org), E._v3(d00),
+                                                                                       E._v3(du), E._v3(dv))
+                lp.render.spp = sp["spp"]
+                lp.ext.frameID = sp["frameID"]
+                lp.accumID = 0
+                lp.fbPointer, lp.accumBuffer = sp["fb"], None
+                E._check(E.lib().exa_render(ctx.h, C.byref(lp), sp["width"], sp["height"]))
+    ms_seq = timed(sequential, reps=1)
+    out = {
+        "workload": "small field, 64 orbit cameras x 4 transfer functions = 256 frames, square sides drawn from "
+                    "{256,512,768,1024}, 4 spp, path tracing <= 8 bounces",
+        "frames": len(specs), "paths": paths,
+        "batched_graph_autotuned": {"paths_per_s": paths / (ms_tuned / 1e3), "ms": ms_tuned,
+                                    "majorant_grid": list(tune["dims"]), "tile_width": tune["tileWidth"],
+                                    "rounds": st_tuned["rounds"], "autotune_seconds": tune_s,
+                                    "trials": [{"grid": d[0], "tile_width": tw, "ms": m} for d, tw, m in
+                                               tune["trials"]]},
+        "batched_graph_grid32": {"paths_per_s": paths / (ms_fixed / 1e3), "ms": ms_fixed,
+                                 "rounds": st_fixed["rounds"]},
+        "batched_host_loop_grid32": {"paths_per_s": paths / (ms_host / 1e3), "ms": ms_host},
+        "sequential_exa_render_grid32": {"paths_per_s": paths / (ms_seq / 1e3), "ms": ms_seq},
+        "speedup_batched_autotuned_over_sequential": ms_seq / ms_tuned,
     }
     ctx.close()
     return out
