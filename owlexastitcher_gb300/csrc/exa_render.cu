@@ -821,8 +821,8 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
 }
 
 // ------------------------------------------------------------------------
-// Wavefront form: path records in structure-of-arrays buffers (word k of
-// record i at buf[k * cap + i], so a warp's loads and stores coalesce).  A
+// Wavefront form: path records in queue buffers (walk state as
+// structure-of-arrays, so a warp's loads and stores coalesce).  A
 // walk kernel advances each queued walk by at most K tracking steps and
 // compacts the records into a continue queue and an event queue with
 // warp-aggregated appends (ballot, popc, one atomic per warp, shuffle of the
@@ -832,11 +832,14 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
 // Each path runs the same operations in the same order as in the nested
 // form, so the result is bit-identical; only the interleaving of paths
 // differs.
-// record = path part (words [0, kPathWords)) + walk part; the walk kernel
-// only touches the walk part and copies the path part through
+// record = path part (AoS: record i at words [i * kPathStride, +kPathWords))
+// + walk part (SoA: word k of record i at (kPathStride + k) * cap + i); the
+// walk kernel reads and writes only walk parts, and an ended walk leaves a
+// short event record that points at its path part.
 constexpr int kPathWords = 26;
+constexpr int kPathStride = 28;  // path words padded to whole 16-byte vectors
 constexpr int kWalkWords = 35;
-constexpr int kLaneWords = kPathWords + kWalkWords;
+constexpr int kLaneWords = kPathStride + kWalkWords;
 static_assert(kLaneWords == kWfLaneWords, "record size");
 
 struct WfQueues {
@@ -858,37 +861,48 @@ struct WfQueues {
 #define R() __ldg(b + (size_t)(k++) * cap + i)
 #define RF() __uint_as_float(R())
 
+// path part: AoS, kPathStride words per record (16-byte aligned), so that
+// the integrator step, which reads records in an order unrelated to their
+// slots, touches 4 sectors per record instead of one per word
 EXA_D void wf_store_path(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
 {
-  unsigned k = 0;
-  W((uint32_t)L.px); W((uint32_t)L.py); W((uint32_t)L.s);
-  WF(L.ray.org.x); WF(L.ray.org.y); WF(L.ray.org.z); WF(L.ray.dir.x); WF(L.ray.dir.y); WF(L.ray.dir.z); WF(L.ray.tmax);
-  WF(L.throughput.x); WF(L.throughput.y); WF(L.throughput.z); WF(L.Ld.x); WF(L.Ld.y); WF(L.Ld.z);
-  WF(L.pos.x); WF(L.pos.y); WF(L.pos.z); WF(L.albedo.x); WF(L.albedo.y); WF(L.albedo.z);
-  W(L.bounce); WF(L.lightDen); WF(L.lightI); W((L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1));
+  (void)cap;
+  uint4 *p = reinterpret_cast<uint4 *>(b + (size_t)i * kPathStride);
+  const auto f = [](float v) { return __float_as_uint(v); };
+  p[0] = make_uint4((uint32_t)L.px, (uint32_t)L.py, (uint32_t)L.s, f(L.ray.org.x));
+  p[1] = make_uint4(f(L.ray.org.y), f(L.ray.org.z), f(L.ray.dir.x), f(L.ray.dir.y));
+  p[2] = make_uint4(f(L.ray.dir.z), f(L.ray.tmax), f(L.throughput.x), f(L.throughput.y));
+  p[3] = make_uint4(f(L.throughput.z), f(L.Ld.x), f(L.Ld.y), f(L.Ld.z));
+  p[4] = make_uint4(f(L.pos.x), f(L.pos.y), f(L.pos.z), f(L.albedo.x));
+  p[5] = make_uint4(f(L.albedo.y), f(L.albedo.z), L.bounce, f(L.lightDen));
+  p[6] = make_uint4(f(L.lightI), (L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1), 0u, 0u);
 }
 
 EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width)
 {
-  unsigned k = 0;
-  L.px = (int)R(); L.py = (int)R(); L.s = (int)R();
+  (void)cap;
+  const uint4 *p = reinterpret_cast<const uint4 *>(b + (size_t)i * kPathStride);
+  const uint4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4),
+              q5 = __ldg(p + 5), q6 = __ldg(p + 6);
+  const auto f = [](uint32_t v) { return __uint_as_float(v); };
+  L.px = (int)q0.x; L.py = (int)q0.y; L.s = (int)q0.z;
   L.pixelID = L.px + width * L.py;
-  L.ray.org.x = RF(); L.ray.org.y = RF(); L.ray.org.z = RF();
-  L.ray.dir.x = RF(); L.ray.dir.y = RF(); L.ray.dir.z = RF(); L.ray.tmax = RF(); L.ray.tmin = 0.f;
-  L.throughput.x = RF(); L.throughput.y = RF(); L.throughput.z = RF();
-  L.Ld.x = RF(); L.Ld.y = RF(); L.Ld.z = RF();
-  L.pos.x = RF(); L.pos.y = RF(); L.pos.z = RF();
-  L.albedo.x = RF(); L.albedo.y = RF(); L.albedo.z = RF();
-  L.bounce = R(); L.lightDen = RF(); L.lightI = RF();
-  const uint32_t lf = R();
-  L.lightDirectional = (lf & 1u) != 0u;
-  L.frame = (int)(lf >> 1);
+  L.ray.org = mk3(f(q0.w), f(q1.x), f(q1.y));
+  L.ray.dir = mk3(f(q1.z), f(q1.w), f(q2.x));
+  L.ray.tmax = f(q2.y); L.ray.tmin = 0.f;
+  L.throughput = mk3(f(q2.z), f(q2.w), f(q3.x));
+  L.Ld = mk3(f(q3.y), f(q3.z), f(q3.w));
+  L.pos = mk3(f(q4.x), f(q4.y), f(q4.z));
+  L.albedo = mk3(f(q4.w), f(q5.x), f(q5.y));
+  L.bounce = q5.z; L.lightDen = f(q5.w); L.lightI = f(q6.x);
+  L.lightDirectional = (q6.y & 1u) != 0u;
+  L.frame = (int)(q6.y >> 1);
 }
 
 // shadow flag, RNG and the walk
 EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
 {
-  unsigned k = kPathWords;
+  unsigned k = kPathStride;
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2));
   W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
@@ -903,7 +917,7 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
 EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i,
                         const exa_grid_traversable &G)
 {
-  unsigned k = kPathWords;
+  unsigned k = kPathStride;
   Walk &w = L.w;
   const uint32_t flags = R();
   L.shadow = flags & 1u;
@@ -927,6 +941,41 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.primID = (int)R(); w.steps = (int)R(); w.ncells = (int)R();
 }
 
+// event record of a walk that ended: the fields the integrator step reads,
+// and the slot of the walk's path part, which stays in the round's input
+// queue (that buffer is rewritten only in the next round)
+constexpr int kEventWords = 14;
+
+EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, unsigned src)
+{
+  unsigned k = 0;
+  const Walk &w = L.w;
+  W((uint32_t)L.shadow | ((uint32_t)w.type << 2));
+  W(src);
+  W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
+  WF(w.t); WF(w.Tr);
+  WF(w.pos.x); WF(w.pos.y); WF(w.pos.z);
+  WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
+}
+
+// returns the slot of the path part
+EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i)
+{
+  unsigned k = 0;
+  Walk &w = L.w;
+  const uint32_t flags = R();
+  L.shadow = flags & 1u;
+  w.type = (int)(flags >> 2);
+  const unsigned src = R();
+  const uint32_t lo = R(), hi = R();
+  L.rng.key = ((uint64_t)hi << 32) | lo;
+  L.rng.counter = R();
+  w.t = RF(); w.Tr = RF();
+  w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
+  w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
+  return src;
+}
+
 #undef W
 #undef WF
 #undef R
@@ -948,7 +997,11 @@ EXA_D void wf_load(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsign
 EXA_D void wf_copy_path(const uint32_t *__restrict__ src, unsigned i, uint32_t *dst, unsigned j, unsigned cap)
 {
 #pragma unroll
-  for (int k = 0; k < kPathWords; ++k) dst[(size_t)k * cap + j] = __ldg(src + (size_t)k * cap + i);
+  (void)cap;
+  const uint4 *a = reinterpret_cast<const uint4 *>(src + (size_t)i * kPathStride);
+  uint4 *d = reinterpret_cast<uint4 *>(dst + (size_t)j * kPathStride);
+#pragma unroll
+  for (int k = 0; k < kPathStride / 4; ++k) d[k] = __ldg(a + k);
 }
 
 // warp-aggregated append: returns this lane's slot (valid where pred)
@@ -1046,8 +1099,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
     const bool ended = active && !walk_step(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
-      wf_store_walk(L, Q.ev, Q.cap, slot);
-      wf_copy_path(Q.in, src, Q.ev, slot, Q.cap);
+      wf_store_event(L, Q.ev, Q.cap, slot, src);
       active = false;
     }
   }
@@ -1145,8 +1197,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     ended = active && ended;
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
-      wf_store_walk(L, Q.ev, Q.cap, slot);
-      wf_copy_path(Q.in, src, Q.ev, slot, Q.cap);
+      wf_store_event(L, Q.ev, Q.cap, slot, src);
       active = false;
     }
   }
@@ -1167,7 +1218,7 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
     Lane L;
     bool tracking = false;
     if (i < n) {
-      wf_load(L, Q.ev, Q.cap, i, width, lp.majorantGrid);
+      wf_load_path(L, Q.in, Q.cap, wf_load_event(L, Q.ev, Q.cap, i), width);
       L.phase = PH_TRACK;
       if (L.shadow) M.shadow_done(L);
       else M.primary_done(L);
@@ -1190,6 +1241,9 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
   cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   const unsigned long long total = (unsigned long long)((width + 15) / 16) * ((height + 7) / 8) * 128ull * lp.render.spp;
+  // path parts are read as 16-byte vectors: every queue must start 16-byte
+  // aligned (capacities are multiples of the 128-job tile)
+  if (cap % 4 != 0) throw Error(EXA_ERR_INVALID, "queue capacity must be a multiple of 4");
   const size_t words = (size_t)kLaneWords * cap;
   uint32_t *buf[3] = {bufs, bufs + words, bufs + 2 * words};
   unsigned long long issued = 0;
@@ -1382,7 +1436,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
         if (idx < n) {
           wf_load_walk(L, in, Q.cap, idx, lp0.majorantGrid);
           // the frame index sits in the path part of the record
-          L.frame = (int)(__ldg(in + (size_t)(kPathWords - 1) * Q.cap + idx) >> 1);
+          L.frame = (int)(__ldg(in + (size_t)idx * kPathStride + 25) >> 1);
           flp = B.lps + L.frame;
           fa = B.accels + B.frames[L.frame].tf;
           active = true;
@@ -1409,8 +1463,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
     }
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
-      wf_store_walk(L, Q.ev, Q.cap, slot);
-      wf_copy_path(in, src, Q.ev, slot, Q.cap);
+      wf_store_event(L, Q.ev, Q.cap, slot, src);
       active = false;
     }
   }
@@ -1430,7 +1483,7 @@ __global__ void __launch_bounds__(128) k_wfb_events(const __grid_constant__ Acce
     Lane L;
     bool tracking = false;
     if (i < n) {
-      wf_load(L, Q.ev, Q.cap, i, 0, lp0.majorantGrid);
+      wf_load_path(L, Q.buf[ctl->flip], Q.cap, wf_load_event(L, Q.ev, Q.cap, i), 0);
       const WfFrame F = B.frames[L.frame];
       L.pixelID = L.px + F.width * L.py;
       const exa_launch_params &flp = B.lps[L.frame];
@@ -1546,6 +1599,9 @@ void renderWavefrontBatch(const AccelView &A, const exa_launch_params &lp0, cons
   cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wfb_walk, 128, 0), "occupancy");
   const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
   const unsigned grid = (unsigned)sms * 16;
+  // path parts are read as 16-byte vectors: every queue must start 16-byte
+  // aligned (capacities are multiples of the 128-job tile)
+  if (cap % 4 != 0) throw Error(EXA_ERR_INVALID, "queue capacity must be a multiple of 4");
   const size_t words = (size_t)kLaneWords * cap;
   WfQueuesB Q{{bufs, bufs + words}, bufs + 2 * words, counters, cap};
   const unsigned long long totalPixels = B.totalPixels;

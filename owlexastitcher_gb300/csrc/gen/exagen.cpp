@@ -310,9 +310,10 @@ struct Builder {
   bool refineCrit(double v, int L, double maxAbs) const
   {
     if (P.fieldKind == EXA_FIELD_GAUSSIANS) return std::fabs(v) > (double)P.refineThreshold * maxAbs;
-    // cloud: deeper levels need denser cloud (thresholds t, 4t, 16t, ...)
+    // cloud: deeper levels need denser cloud (thresholds t, 2t, 4t, ...), so
+    // that with t well below 1/2^(levels-2) every level is populated
     const int depth = Lroot - L;
-    return v > (double)P.refineThreshold * std::pow(4.0, depth);
+    return v > (double)P.refineThreshold * std::pow(2.0, depth);
   }
 
   void buildTree()

@@ -96,7 +96,9 @@ def params(config="small", **overrides):
         p.rootDims[:] = [256, 256, 256]
         p.fieldKind = FIELD_CLOUD
         p.noiseOctaves = 6
-        p.refineThreshold = 0.01
+        # refinement thresholds 0.09, 0.18, 0.36, 0.72 of the [0, 1] cloud
+        # density for the four refined levels: ~400M cells at 256^3 roots
+        p.refineThreshold = 0.09
         p.cloudEmptyFraction = 0.7
     elif config == "tiny":
         p.numLevels = 3
