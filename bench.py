@@ -29,6 +29,8 @@ METRIC = "paths/s"
 WIDTH, HEIGHT, SPP = 1024, 1024, 16
 NUM_MCS = (128, 128, 128)
 L2_BYTES = 129 * 1024 * 1024
+DESCR = {"medium": "4 levels, 128^3 root, 256 Gaussians + noise",
+         "cloud": "5 levels, 256^3 root, exp(3 fBm) cloud with 70% of root cells empty"}
 
 
 def parse():
@@ -37,26 +39,39 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="medium", choices=["medium", "small", "tiny"])
-    ap.add_argument("--width", type=int, default=WIDTH)
-    ap.add_argument("--height", type=int, default=HEIGHT)
-    ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--config", default="medium", choices=["medium", "small", "tiny", "cloud"],
+                    help="cloud: the large sparse cloud field (5 levels, 256^3 roots, ~394M cells) rendered at "
+                         "1920x1080, 64 spp, <= 16 bounces, with the learned field (2^21 entries per level)")
+    ap.add_argument("--width", type=int, default=None)
+    ap.add_argument("--height", type=int, default=None)
+    ap.add_argument("--spp", type=int, default=None)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="warm-up + 1 step, no extras (for ncu)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-field (surrogate) measurements")
     ap.add_argument("--learned-steps", type=int, default=1600, help="surrogate training steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-frames measurements")
-    return ap.parse_args()
+    a = ap.parse_args()
+    big = a.config == "cloud"
+    a.width = a.width or (1920 if big else WIDTH)
+    a.height = a.height or (1080 if big else HEIGHT)
+    a.spp = a.spp or (64 if big else SPP)
+    a.bounces = 16 if big else 8
+    if big:
+        # the oracle's field for ~400M cells is too large for a bounded CPU
+        # sample; the batched workload is defined on the small field
+        a.no_cpu_baseline = True
+        a.no_batched = True
+    return a
 
 
 def workload_config(a):
     return {
-        "workload": f"{a.config} AMR ({'4 levels, 128^3 root' if a.config == 'medium' else a.config}), "
+        "workload": f"{a.config} AMR ({DESCR.get(a.config, a.config)}), "
                     f"path tracing {a.width}x{a.height} {a.spp} spp",
         "dataset": a.config,
         "width": a.width, "height": a.height, "spp": a.spp,
-        "max_bounces": 8, "albedo": 0.8, "hg_g": 0.3, "light": "directional",
+        "max_bounces": a.bounces, "albedo": 0.8, "hg_g": 0.3, "light": "directional",
         "majorant_grid": list(NUM_MCS), "tf": "64-entry linear RGBA ramp",
         "l2": "flushed between timed steps (256 MiB write)",
     }
@@ -169,6 +184,7 @@ def run_ours(a):
     r.spp = a.spp
     cam = orbit_camera(lo, hi, a.width, a.height)
     setup_render(r.lp, cam, a.width, a.height, E.PATH_TRACING_INTEGRATOR, a.spp, "directional", True)
+    r.lp.ext.maxBounces = a.bounces
     r.lp.ext.frameID = rank  # independent frames per rank
     paths_per_step = a.width * a.height * a.spp
     stream = torch.cuda.current_stream()
@@ -279,12 +295,16 @@ def run_ours(a):
     learned = None
     if rank == 0 and not a.no_learned:
         from owlexastitcher_gb300 import datagen
-        learned = {
-            # the small config's field (3 levels, 32^3 root) with its 32^3 majorant grid
-            "small_field": run_learned(a, local, datagen.Dataset("small"), (32, 32, 32), flush),
-            # the same method on this workload's field and majorant grid
-            "workload_field": run_learned(a, local, ds, NUM_MCS, flush),
-        }
+        if a.config == "cloud":
+            # the large cloud: 2^21 table entries per level
+            learned = {"workload_field": run_learned(a, local, ds, NUM_MCS, flush, log2T=21)}
+        else:
+            learned = {
+                # the small config's field (3 levels, 32^3 root) with its 32^3 majorant grid
+                "small_field": run_learned(a, local, datagen.Dataset("small"), (32, 32, 32), flush),
+                # the same method on this workload's field and majorant grid
+                "workload_field": run_learned(a, local, ds, NUM_MCS, flush),
+            }
 
     if rank == 0:
         line = {
@@ -321,7 +341,7 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
-def run_learned(a, local, ds, num_mcs, flush, timed=3):
+def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
     """The learned field on one dataset: training, per-macrocell error
     bounds, memory, and the same path-traced frame rendered with the exact
     sampler and with the learned field (+ exact fallback), both through
@@ -337,9 +357,10 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3):
     r.spp = a.spp
     setup_render(r.lp, orbit_camera(lo, hi, a.width, a.height), a.width, a.height, E.PATH_TRACING_INTEGRATOR,
                  a.spp, "directional", True)
+    r.lp.ext.maxBounces = a.bounces
     stream = torch.cuda.current_stream()
     t0 = time.perf_counter()
-    S = E.Surrogate(ctx, log2TableSize=19, baseResolution=16, growth=1.5, numSamples=1 << 24, batch=1 << 18,
+    S = E.Surrogate(ctx, log2TableSize=log2T, baseResolution=16, growth=1.5, numSamples=1 << 24, batch=1 << 18,
                     importanceFraction=0.5, seed=1234)
     torch.cuda.synchronize()
     sample_s = time.perf_counter() - t0
@@ -404,7 +425,7 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3):
     rmse = float(np.sqrt(np.mean((imgs["exact"] - imgs["learned"]) ** 2)))
     out = {
         "dataset": ds.config if hasattr(ds, "config") else None, "majorant_grid": list(num_mcs),
-        "encoding": {"levels": 16, "features": 2, "table_entries_per_level": 1 << 19, "base_resolution": 16,
+        "encoding": {"levels": 16, "features": 2, "table_entries_per_level": 1 << log2T, "base_resolution": 16,
                      "growth": 1.5},
         "mlp": "32-64-64-1 ReLU, BF16 weights, FP32 accumulate (mma.sync m16n8k16)",
         "training": {"pairs": 1 << 24, "importance_fraction": 0.5, "batch": 1 << 18, "steps": a.learned_steps,
@@ -586,6 +607,10 @@ def run_reference(a):
     own path needs OptiX/OWL, which are not available)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if a.config == "cloud":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement's field structures for the "
+                          "~400M-cell cloud exceed a bounded CPU sample; the reference arm is defined on medium"}))
         return
     import ctypes as C
     import pyoracle

@@ -248,6 +248,49 @@ int exa_model_create(exa_context *ctx,
                      const int32_t *indices, uint64_t numElems,
                      const exa_gridlet *gridlets, uint64_t numGridlets,
                      const float *gridletScalars, uint64_t numGridletScalars);
+
+/* On-disk inputs.  Host-only parsers (no context, no device): call once
+ * with null output arrays to get the counts, then again with arrays of
+ * those sizes.  Files are little-endian as the reference writes them. */
+
+/* '.grids' + '.scalars' as ExaStitchModel::load reads them
+ * (model/ExaStitchModel.cpp:44-55, 191-247): per gridlet int32 lower[3],
+ * level, dims[3] and (dims+1)^3 int32 scalar IDs into the '.scalars' file
+ * (raw float32); IDs outside that file become NaN (absent).  Gridlet
+ * 'begin' offsets are assigned in file order. */
+int exa_read_grids(const char *gridsFile, const char *scalarsFile, exa_gridlet *gridlets, uint64_t *numGridlets,
+                   float *gridletScalars, uint64_t *numGridletScalars);
+/* ExaStitchModel::load for a gridlet-only model (no '.umesh' part: that
+ * format belongs to the un-vendored umesh library): exa_read_grids then
+ * exa_model_create. */
+int exa_model_load(exa_context *ctx, const char *gridsFile, const char *scalarsFile);
+
+/* '.xf' transfer function (headless.cpp:258-283): uint64 magic
+ * 0x1235abc000, float opacityScale, absDomain (2 floats), relDomain (2
+ * floats, percent), int32 count, float4 colours. */
+typedef struct exa_xf {
+  float opacityScale;
+  exa_range1f absDomain, relDomain;
+  int32_t numColors;
+} exa_xf;
+int exa_read_xf(const char *xfFile, exa_xf *xf, exa_vec4f *colors, int32_t maxColors);
+/* The value range the transfer function spans (Headless::xfRange,
+ * headless.cpp:285-298): absDomain ordered, relDomain / 100 ordered,
+ * range = lerp(abs, rel.lower) .. lerp(abs, rel.upper). */
+exa_range1f exa_xf_range(const exa_xf *xf);
+/* LaunchParams.transferFunc.opacityScale for a viewer opacity setting s:
+ * 1.1^(s - 100) (OWLRenderer.cpp:743). */
+float exa_opacity_scale(float s);
+
+/* AMR '.cells' (tools/amrMakeDualMesh/makeDual.cpp:932-940): 16-byte
+ * records int32 pos[3], level; the matching scalars are a raw float32 file
+ * in the same order. */
+typedef struct exa_amr_cell {
+  exa_vec3i pos;
+  int32_t level;
+} exa_amr_cell;
+int exa_read_cells(const char *cellsFile, exa_amr_cell *cells, uint64_t *numCells);
+
 /* Model::cellBounds / Model::valueRange (model/Model.h:54-55). */
 int exa_model_get_bounds(exa_context *ctx, exa_box3f *cellBounds,
                          exa_range1f *valueRange);

@@ -1,6 +1,7 @@
 // exa_api.cpp -- host classes (Model, ExaStitchModel, ExaStitchSampler,
 // Grid) and the C ABI of exastitch.h.  No exception crosses the C boundary.
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -602,6 +603,8 @@ uint64_t exa_abi_sizeof(int32_t which)
     case 7: return sizeof(exa_surrogate_geometry);
     case 8: return sizeof(exa_batch_frame);
     case 9: return sizeof(exa_batch_tuning);
+    case 10: return sizeof(exa_xf);
+    case 11: return sizeof(exa_amr_cell);
     default: return 0;
   }
 }
@@ -695,6 +698,150 @@ int exa_model_create(exa_context *ctx, const exa_vec4f *vertices, uint64_t numVe
     m->assign(vertices, numVertices, indices, numElems, gridlets, numGridlets, gridletScalars, numGridletScalars);
     ctx->model = m;
     ctx->sampler.reset();
+  });
+}
+
+namespace {
+std::vector<char> readFile(const char *path, bool required)
+{
+  std::vector<char> data;
+  if (!path || !*path) {
+    if (required) throw Error(EXA_ERR_INVALID, "no file name");
+    return data;
+  }
+  FILE *f = std::fopen(path, "rb");
+  if (!f) {
+    if (required) throw Error(EXA_ERR_INVALID, std::string("cannot open ") + path);
+    return data;  // the loader treats a missing scalars file as empty
+  }
+  std::fseek(f, 0, SEEK_END);
+  const long n = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (n > 0) {
+    data.resize((size_t)n);
+    if (std::fread(data.data(), 1, (size_t)n, f) != (size_t)n) {
+      std::fclose(f);
+      throw Error(EXA_ERR_INVALID, std::string("short read of ") + path);
+    }
+  }
+  std::fclose(f);
+  return data;
+}
+
+// ExaStitchModel::load's gridlet loop: records until the data runs out
+void parseGrids(const std::vector<char> &g, const std::vector<char> &sc, std::vector<exa_gridlet> &gl,
+                std::vector<float> &vals)
+{
+  const size_t nsc = sc.size() / sizeof(float);
+  const float *scalars = reinterpret_cast<const float *>(sc.data());
+  size_t off = 0;
+  while (off + 28 <= g.size()) {
+    exa_gridlet q;
+    int32_t hdr[7];
+    std::memcpy(hdr, g.data() + off, 28);
+    off += 28;
+    q.lower = exa_vec3i{hdr[0], hdr[1], hdr[2]};
+    q.level = hdr[3];
+    q.dims = exa_vec3i{hdr[4], hdr[5], hdr[6]};
+    if (q.dims.x < 0 || q.dims.y < 0 || q.dims.z < 0 || q.level < 0 || q.level > 30)
+      throw Error(EXA_ERR_INVALID, "corrupt .grids record");
+    const size_t ns = (size_t)(q.dims.x + 1) * (size_t)(q.dims.y + 1) * (size_t)(q.dims.z + 1);
+    if (off + ns * 4 > g.size()) throw Error(EXA_ERR_INVALID, "truncated .grids record");
+    q.begin = (uint32_t)vals.size();
+    for (size_t i = 0; i < ns; ++i) {
+      int32_t id;
+      std::memcpy(&id, g.data() + off + 4 * i, 4);
+      vals.push_back((unsigned)id < nsc ? scalars[(unsigned)id] : NAN);
+    }
+    off += ns * 4;
+    gl.push_back(q);
+  }
+}
+}  // namespace
+
+int exa_read_grids(const char *gridsFile, const char *scalarsFile, exa_gridlet *gridlets, uint64_t *numGridlets,
+                   float *gridletScalars, uint64_t *numGridletScalars)
+{
+  return guarded([&] {
+    need(numGridlets && numGridletScalars, EXA_ERR_INVALID, "null count");
+    std::vector<exa_gridlet> gl;
+    std::vector<float> vals;
+    parseGrids(readFile(gridsFile, true), readFile(scalarsFile, false), gl, vals);
+    if (gridlets || gridletScalars) {
+      need(gridlets && gridletScalars && *numGridlets >= gl.size() && *numGridletScalars >= vals.size(),
+           EXA_ERR_INVALID, "output arrays too small");
+      std::memcpy(gridlets, gl.data(), gl.size() * sizeof(exa_gridlet));
+      std::memcpy(gridletScalars, vals.data(), vals.size() * sizeof(float));
+    }
+    *numGridlets = gl.size();
+    *numGridletScalars = vals.size();
+  });
+}
+
+int exa_model_load(exa_context *ctx, const char *gridsFile, const char *scalarsFile)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    std::vector<exa_gridlet> gl;
+    std::vector<float> vals;
+    parseGrids(readFile(gridsFile, true), readFile(scalarsFile, false), gl, vals);
+    need(gl.size() < 0x7fffffffull && vals.size() <= 0xffffffffull, EXA_ERR_INVALID, "model too large");
+    auto m = std::make_shared<ExaStitchModel>();
+    m->assign(nullptr, 0, nullptr, 0, gl.data(), gl.size(), vals.data(), vals.size());
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+int exa_read_xf(const char *xfFile, exa_xf *xf, exa_vec4f *colors, int32_t maxColors)
+{
+  return guarded([&] {
+    need(xf != nullptr, EXA_ERR_INVALID, "null xf");
+    const std::vector<char> d = readFile(xfFile, true);
+    const uint64_t kMagic = 0x1235abc000ull;
+    need(d.size() >= 8 + 5 * 4 + 4, EXA_ERR_INVALID, "not a valid '.xf' transfer function file");
+    uint64_t magic;
+    std::memcpy(&magic, d.data(), 8);
+    need(magic == kMagic, EXA_ERR_INVALID, "not a valid '.xf' transfer function file");
+    float f[5];
+    std::memcpy(f, d.data() + 8, 20);
+    int32_t n;
+    std::memcpy(&n, d.data() + 28, 4);
+    need(n >= 0 && d.size() >= 32 + (size_t)n * 16, EXA_ERR_INVALID, "truncated '.xf' file");
+    xf->opacityScale = f[0];
+    xf->absDomain = exa_range1f{f[1], f[2]};
+    xf->relDomain = exa_range1f{f[3], f[4]};
+    xf->numColors = n;
+    if (colors) {
+      need(maxColors >= n, EXA_ERR_INVALID, "colour array too small");
+      std::memcpy(colors, d.data() + 32, (size_t)n * 16);
+    }
+  });
+}
+
+exa_range1f exa_xf_range(const exa_xf *xf)
+{
+  if (!xf) return exa_range1f{0.f, 1.f};
+  const float a0 = std::min(xf->absDomain.lower, xf->absDomain.upper);
+  const float a1 = std::max(xf->absDomain.lower, xf->absDomain.upper);
+  const float r0 = .01f * xf->relDomain.lower, r1 = .01f * xf->relDomain.upper;
+  const float q0 = std::min(r0, r1), q1 = std::max(r0, r1);
+  return exa_range1f{(1.f - q0) * a0 + q0 * a1, (1.f - q1) * a0 + q1 * a1};
+}
+
+float exa_opacity_scale(float s) { return std::pow(1.1f, s - 100.f); }
+
+int exa_read_cells(const char *cellsFile, exa_amr_cell *cells, uint64_t *numCells)
+{
+  return guarded([&] {
+    need(numCells != nullptr, EXA_ERR_INVALID, "null count");
+    const std::vector<char> d = readFile(cellsFile, true);
+    const size_t n = d.size() / sizeof(exa_amr_cell);
+    if (cells) {
+      need(*numCells >= n, EXA_ERR_INVALID, "output array too small");
+      std::memcpy(cells, d.data(), n * sizeof(exa_amr_cell));
+    }
+    *numCells = n;
   });
 }
 

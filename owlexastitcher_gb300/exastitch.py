@@ -12,6 +12,7 @@ All compute goes through libexastitch.so; there is no Python or CPU
 fallback.  Device buffers are torch tensors (plumbing only).
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -207,6 +208,14 @@ class SurrogateGeometry(C.Structure):
 SURROGATE_PARAMS = 64 * 32 + 64 * 64 + 64  # W1 | W2 | w3
 
 
+class Xf(C.Structure):
+    _fields_ = [("opacityScale", C.c_float), ("absDomain", range1f), ("relDomain", range1f), ("numColors", C.c_int32)]
+
+
+class AmrCell(C.Structure):
+    _fields_ = [("pos", vec3i), ("level", C.c_int32)]
+
+
 class BatchFrame(C.Structure):
     _fields_ = [("org", vec3f), ("dir_00", vec3f), ("dir_du", vec3f), ("dir_dv", vec3f), ("width", C.c_int32),
                 ("height", C.c_int32), ("spp", C.c_int32), ("tf", C.c_int32), ("accumID", C.c_uint32),
@@ -232,6 +241,7 @@ EXPORTED = [
     "exa_surrogate_get_params", "exa_surrogate_set_params", "exa_surrogate_gradients",
     "exa_surrogate_get_macrocells", "exa_render_surrogate", "exa_batch_set_transfer_functions",
     "exa_batch_set_majorant_grid", "exa_batch_set_tile_width", "exa_render_batch", "exa_batch_autotune",
+    "exa_read_grids", "exa_model_load", "exa_read_xf", "exa_xf_range", "exa_opacity_scale", "exa_read_cells",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -289,13 +299,19 @@ def lib():
         "exa_batch_set_tile_width": ([ctx_p, i32], C.c_int),
         "exa_render_batch": ([ctx_p, C.POINTER(LaunchParams), vp, i32, i32], C.c_int),
         "exa_batch_autotune": ([ctx_p, C.POINTER(LaunchParams), vp, i32, i32, C.POINTER(BatchTuning)], C.c_int),
+        "exa_read_grids": ([C.c_char_p, C.c_char_p, vp, C.POINTER(u64), vp, C.POINTER(u64)], C.c_int),
+        "exa_model_load": ([ctx_p, C.c_char_p, C.c_char_p], C.c_int),
+        "exa_read_xf": ([C.c_char_p, C.POINTER(Xf), vp, i32], C.c_int),
+        "exa_xf_range": ([C.POINTER(Xf)], range1f),
+        "exa_opacity_scale": ([C.c_float], C.c_float),
+        "exa_read_cells": ([C.c_char_p, vp, C.POINTER(u64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = res
     for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt), (5, SurrogateParams),
-                    (6, SurrogateStats), (7, SurrogateGeometry), (8, BatchFrame), (9, BatchTuning)):
+                    (6, SurrogateStats), (7, SurrogateGeometry), (8, BatchFrame), (9, BatchTuning), (10, Xf), (11, AmrCell)):
         if L.exa_abi_sizeof(key) != C.sizeof(st):
             raise RuntimeError(f"ABI layout mismatch for {st.__name__}: C {L.exa_abi_sizeof(key)} vs ctypes {C.sizeof(st)}")
     _lib = L
@@ -681,3 +697,38 @@ class Batch:
         return {"dims": (t.dims.x, t.dims.y, t.dims.z), "tileWidth": t.tileWidth, "msBest": t.msBest,
                 "trials": [((t.trialDims[i].x, t.trialDims[i].y, t.trialDims[i].z), t.trialTileWidth[i], t.trialMs[i])
                            for i in range(t.numTrials)]}
+
+
+# ------------------------------------------------------------- file formats
+def read_grids(grids_file, scalars_file):
+    """'.grids' + '.scalars' -> (gridlets structured array, gridlet scalars)"""
+    L = lib()
+    ng, ns = C.c_uint64(0), C.c_uint64(0)
+    g, sf = os.fsencode(grids_file), os.fsencode(scalars_file) if scalars_file else None
+    _check(L.exa_read_grids(g, sf, None, C.byref(ng), None, C.byref(ns)))
+    gl = np.zeros(ng.value, GRIDLET_DTYPE)
+    sc = np.zeros(ns.value, np.float32)
+    _check(L.exa_read_grids(g, sf, _np_ptr(gl), C.byref(ng), _np_ptr(sc), C.byref(ns)))
+    return gl, sc
+
+
+def read_xf(xf_file):
+    """'.xf' -> dict(opacityScale, absDomain, relDomain, colorMap, range)"""
+    L = lib()
+    xf = Xf()
+    _check(L.exa_read_xf(os.fsencode(xf_file), C.byref(xf), None, 0))
+    cm = np.zeros((xf.numColors, 4), np.float32)
+    _check(L.exa_read_xf(os.fsencode(xf_file), C.byref(xf), _np_ptr(cm), xf.numColors))
+    r = L.exa_xf_range(C.byref(xf))
+    return {"opacityScale": xf.opacityScale, "absDomain": (xf.absDomain.lower, xf.absDomain.upper),
+            "relDomain": (xf.relDomain.lower, xf.relDomain.upper), "colorMap": cm, "range": (r.lower, r.upper)}
+
+
+def read_cells(cells_file):
+    """AMR '.cells' -> structured array (pos[3], level)"""
+    L = lib()
+    n = C.c_uint64(0)
+    _check(L.exa_read_cells(os.fsencode(cells_file), None, C.byref(n)))
+    out = np.zeros(n.value, np.dtype([("pos", "<i4", 3), ("level", "<i4")]))
+    _check(L.exa_read_cells(os.fsencode(cells_file), _np_ptr(out), C.byref(n)))
+    return out
