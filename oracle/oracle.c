@@ -1150,6 +1150,57 @@ static v4 direct_light(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
   return color;
 }
 
+/* rayMarchingIntegrate + integrateDVR (deviceCode.cu:348-398, 1213-1260):
+ * TF samples at spacing render.dt from the jittered first sample of
+ * firstSampleT (:104-112), composited front to back, early exit at opacity
+ * 0.99, over the background (over(), :151-154).  The shading normal is
+ * g / |g + 1e-4| with the gradient g left at 0 (its computation is
+ * commented out in the reference), so each light adds cd * 0. */
+#define OC_MARCH_CAP (1ll << 24)
+static v4 ray_march(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights)
+{
+  const exa_launch_params *lp = c->lp;
+  v4 color = bg;
+  float t0 = 1e30f, t1 = -1e30f;
+  if (!box_test(ray, lp->worldSpaceBounds, &t0, &t1)) return color;
+  const float ils = oc_rng_next(rng);
+  const v3 org = xfm_point(&lp->voxelSpaceTransform, ray.org);
+  const v3 vd = norm3(xfm_vector(&lp->voxelSpaceTransform, ray.dir));
+  const float dt = lp->render.dt;
+  const float numSegsf = floorf((t0 - dt * ils) / dt);
+  float t = dt * (ils + numSegsf);
+  if (t < t0) t += dt;
+  const v3 g = mk3(0.f, 0.f, 0.f);
+  const v3 N = muls(g, 1.f / len3(add3(g, mk3(1e-4f, 1e-4f, 1e-4f))));
+  const int cull = lp->ext.cullTransparentPrims != 0;
+  v4 acc = {0.f, 0.f, 0.f, 0.f};
+  for (long long k = 0; t <= t1; t += dt, ++k) {
+    if (k >= OC_MARCH_CAP) { c->err |= EXA_DEVERR_TRACK_CAP; break; }
+    const v3 pos = add3(org, muls(vd, t));
+    const exa_sample smp = oc_sample(c->f, pos, cull);
+    if (smp.primID < 0) continue;
+    const v4 xf = lookup_tf(lp, smp.value);
+    const v3 cd = mk3(xf.x, xf.y, xf.z);
+    v3 shaded = smul(.1f, cd);
+    if (numLights == 0) shaded = cd;
+    for (int l = 0; l < numLights; ++l) {
+      const v3 lv = sub3(lp->lights[l].pos, pos);
+      const v3 L = norm3(lv);
+      const float ld = len3(lv);
+      shaded = add3(shaded, muls(cd, (.9f * dot3(N, L)) / (ld * ld) * lp->lights[l].intensity));
+    }
+    const float a = (1.f - acc.w) * xf.w;
+    acc.x += a * shaded.x;
+    acc.y += a * shaded.y;
+    acc.z += a * shaded.z;
+    acc.w += a * 1.f;
+    if (acc.w >= 0.99f) break;
+  }
+  const float r = 1.f - acc.w;
+  v4 out = {acc.x + r * color.x, acc.y + r * color.y, acc.z + r * color.z, acc.w + r * color.w};
+  return out;
+}
+
 static inline uint32_t make_8bit(float f)
 {
   return (uint32_t)imin_t(255, imax_t(0, (int)(f * 256.f)));
@@ -1182,6 +1233,8 @@ static void render_pixel(rctx *c, int width, int height, int px, int py)
     v4 col;
     if (lp->integrator == EXA_PATH_TRACING_INTEGRATOR)
       col = path_trace(c, ray, &rng, bg, numLights, s == 0 ? &tHit : NULL, s == 0 ? &trv : NULL);
+    else if (lp->integrator == EXA_RAY_MARCHING_INTEGRATOR)
+      col = ray_march(c, ray, &rng, bg, numLights);
     else
       col = direct_light(c, ray, &rng, bg, numLights, s == 0 ? &tHit : NULL, s == 0 ? &trv : NULL);
     acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;

@@ -530,8 +530,11 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     need(lp->render.spp >= 1, EXA_ERR_INVALID, "spp must be >= 1");
     need((long long)((width + 15) / 16) * ((height + 7) / 8) * 128 * lp->render.spp < 0xffffffffll, EXA_ERR_INVALID,
          "frame too large: width*height*spp must stay below 2^32 samples per launch");
-    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
-         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+    need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR ||
+             (lp->integrator == EXA_RAY_MARCHING_INTEGRATOR && !learned),
+         EXA_ERR_INVALID, "integrator not supported");
+    need(lp->integrator != EXA_RAY_MARCHING_INTEGRATOR || (lp->render.dt > 0.f && std::isfinite(lp->render.dt)),
+         EXA_ERR_INVALID, "ray marching needs render.dt > 0");
     need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
          "shade mode not supported");
     need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
@@ -557,7 +560,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
       lpUse.maxOpacities = S->majorants.ptr;
       sv = S->deviceView();
     }
-    if (useWavefront() || learned) {
+    if ((useWavefront() || learned) && lpUse.integrator != EXA_RAY_MARCHING_INTEGRATOR) {
       // queue capacity: the frame's samples, at most 4M records in flight
       const unsigned cap = (unsigned)std::min<size_t>((size_t)((width + 15) / 16) * ((height + 7) / 8) * 128 *
                                                           (size_t)lp->render.spp, (size_t)1 << 22);
@@ -1370,7 +1373,7 @@ void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch
   BatchState &B = batchOf(ctx);
   need(!B.tfColors.empty(), EXA_ERR_STATE, "no transfer functions (exa_batch_set_transfer_functions)");
   need(tpl->integrator == EXA_PATH_TRACING_INTEGRATOR || tpl->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
-       EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+       EXA_ERR_INVALID, "integrator not supported (batches render path tracing and direct lighting)");
   need(tpl->shadeMode == EXA_SHADE_MODE_DEFAULT || tpl->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
        "shade mode not supported");
   need(!tpl->clipPlanes[0].enabled && !tpl->subImage.active && !tpl->render.heatMapEnabled && tpl->meshBVH == 0,
@@ -1601,7 +1604,7 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
                                        " exceeds its static scratch of " + std::to_string(EXA_NOALLOC_MAX_SAMPLES) +
                                        " samples; use exa_render for larger frames");
     need(lp->integrator == EXA_PATH_TRACING_INTEGRATOR || lp->integrator == EXA_DIRECT_LIGHT_INTEGRATOR,
-         EXA_ERR_INVALID, "integrator not supported (ray marching is not built)");
+         EXA_ERR_INVALID, "integrator not supported (exa_render_noalloc renders path tracing and direct lighting)");
     need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
          "shade mode not supported");
     need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");

@@ -764,6 +764,108 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(con
   flush_counters(c, lp);
 }
 
+// rayMarchingIntegrate + integrateDVR (deviceCode.cu:348-398, 1213-1260)
+// for one camera sample: front-to-back compositing of TF samples at
+// spacing lp.render.dt from a jittered first sample (firstSampleT,
+// deviceCode.cu:104-112), early exit at opacity 0.99, over the background.
+// The shading normal is g / |g + 1e-4| with the gradient g left at 0 (its
+// computation is commented out in the reference), so lights add cd * 0.
+// Clip planes and surface meshes are not part of this path.
+constexpr long long kMarchCap = 1ll << 24;  // samples per ray
+
+EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int height, int numLights)
+{
+  const exa_launch_params &lp = c.lp;
+  Rng rng;
+  rng.init((uint32_t)pixelID, (uint32_t)lp.accumID, lp.ext.frameID, (uint32_t)s);
+  const float tb = __fdiv_rn((float)py, (float)height);
+  const float4 bg = make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
+  const float rx = rng.next();
+  const float ry = rng.next();
+  const float sx = (float)px + rx, sy = (float)py + ry;
+  V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
+  dir = norm3(dir);
+  if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
+  if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
+  if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+  RayS ray;
+  ray.org = mk3(lp.camera.org);
+  ray.dir = dir;
+  ray.tmin = 0.f;
+  ray.tmax = 1e10f;
+  float4 color = bg;
+  float t0 = 1e30f, t1 = -1e30f;
+  if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
+    const float ils = rng.next();
+    const V3 org = xfm_point(lp.voxelSpaceTransform, ray.org);
+    const V3 vd = norm3(xfm_vector(lp.voxelSpaceTransform, ray.dir));
+    const float dt = lp.render.dt;
+    const float numSegsf = floorf(__fdiv_rn(t0 - dt * ils, dt));
+    float t = dt * (ils + numSegsf);
+    if (t < t0) t += dt;
+    const V3 g = mk3(0.f, 0.f, 0.f);
+    const V3 N = muls(g, __fdiv_rn(1.f, len3(add3(g, mk3(1e-4f, 1e-4f, 1e-4f)))));
+    const bool cull = lp.ext.cullTransparentPrims != 0;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (long long k = 0; t <= t1; t += dt, ++k) {
+      if (k >= kMarchCap) {
+        c.err |= EXA_DEVERR_TRACK_CAP;
+        break;
+      }
+      const V3 pos = add3(org, muls(vd, t));
+      const exa_sample smp = sample_field(c.A, pos, cull, c.err);
+      if (smp.primID < 0) continue;
+      const float4 xf = lookup_tf(lp, smp.value);
+      const V3 cd = mk3(xf.x, xf.y, xf.z);
+      V3 shaded = smul(.1f, cd);
+      if (numLights == 0) shaded = cd;
+      for (int l = 0; l < numLights; ++l) {
+        const V3 lv = sub3(mk3(lp.lights[l].pos), pos);
+        const V3 L = norm3(lv);
+        const float ld = len3(lv);
+        shaded = add3(shaded, muls(cd, __fdiv_rn(.9f * dot3(N, L), ld * ld) * lp.lights[l].intensity));
+      }
+      const float a = (1.f - acc.w) * xf.w;
+      acc.x += a * shaded.x;
+      acc.y += a * shaded.y;
+      acc.z += a * shaded.z;
+      acc.w += a * 1.f;
+      if (acc.w >= 0.99f) break;
+    }
+    // over(A, B) = A + (1 - A.w) B  (deviceCode.cu:151-154)
+    const float r = 1.f - acc.w;
+    color = make_float4(acc.x + r * color.x, acc.y + r * color.y, acc.z + r * color.z, acc.w + r * color.w);
+  }
+  return color;
+}
+
+// ray marching: one thread per camera sample (pixel-major), colours to
+// scratch, resolved by k_resolve
+__global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_march(const __grid_constant__ AccelView A,
+                                                                             const __grid_constant__ exa_launch_params lp,
+                                                                             int width, int height, float4 *colors)
+{
+  const int spp = lp.render.spp;
+  const int tilesX = (width + 15) / 16;
+  const unsigned job = blockIdx.x * 128u + threadIdx.x;
+  const unsigned pj = job / (unsigned)spp;
+  const int s = (int)(job - pj * (unsigned)spp);
+  const int tile = (int)(pj >> 7), within = (int)(pj & 127);
+  const int px = (tile % tilesX) * 16 + (within & 15);
+  const int py = (tile / tilesX) * 8 + (within >> 4);
+  PathCtx c = make_ctx(A, lp);
+  if (px < width && py < height) {
+    const int pixelID = px + width * py;
+    colors[(size_t)pixelID * spp + s] = raymarch_sample(c, px, py, pixelID, s, height, num_lights(lp));
+    cnt_add(c, CNT_PATHS);
+    if (s == 0) {
+      if (lp.ext.traceT) lp.ext.traceT[pixelID] = -1.f;
+      if (lp.ext.traceTr) lp.ext.traceTr[pixelID] = -1.f;
+    }
+  }
+  flush_counters(c, lp);
+}
+
 // S2: one thread per camera sample (pixel-major), colours to scratch
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_sample(const __grid_constant__ AccelView A,
@@ -1734,6 +1836,13 @@ void launchRender(const AccelView &A, const exa_launch_params &lp, int width, in
   const bool pt = lp.integrator == EXA_PATH_TRACING_INTEGRATOR;
   const int tiles = ((width + 15) / 16) * ((height + 7) / 8);
   const long long jobs = (long long)tiles * 128 * lp.render.spp;
+  if (lp.integrator == EXA_RAY_MARCHING_INTEGRATOR) {
+    k_render_march<<<(unsigned)((jobs + 127) / 128), 128, 0, s>>>(A, lp, width, height, colors);
+    cudaCheck(cudaGetLastError(), "k_render_march");
+    k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
+    cudaCheck(cudaGetLastError(), "k_resolve");
+    return;
+  }
   if (EXA_RENDER_STRATEGY == 1) {
     if (pt) k_render_pixel<EXA_PATH_TRACING_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);
     else k_render_pixel<EXA_DIRECT_LIGHT_INTEGRATOR><<<tiles, 128, 0, s>>>(A, lp, width, height);

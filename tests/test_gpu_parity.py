@@ -219,3 +219,22 @@ def test_render_axis_parallel_rays(scenes, torch_cuda):
         assert acc.cpu().numpy().reshape(-1, 4).tobytes() == hacc.tobytes()
     finally:
         lp.lights[0].pos = E._v3([0.4, 0.8, 0.45])
+
+
+@pytest.mark.parametrize("light,dt", [("none", 0.5), ("point", 0.25), ("directional", 1.0)])
+def test_render_ray_marching_bit_exact(scenes, torch_cuda, light, dt):
+    """The ray-marching integrator (RAY_MARCHING_INTEGRATOR, deviceCode.cu:
+    348-398, 1213-1260): compositing at spacing render.dt from a jittered
+    first sample, early exit at opacity 0.99."""
+    ds, g, o = scenes
+    w, h = 40, 32
+    cam = orbit_camera(g.lo, g.hi, w, h)
+    lp = setup_render(g.lp, cam, w, h, 2, 2, light, False, g.lo, g.hi)
+    lp.render.dt = dt
+    try:
+        fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, w, h, 2, 2, light, False)
+    finally:
+        g.lp.render.dt = 1.0
+    assert np.array_equal(fb, hfb)
+    assert acc.tobytes() == hacc.tobytes()
+    assert len(np.unique(fb)) > 4
