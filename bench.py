@@ -288,6 +288,10 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
 
+    small = None
+    if rank == 0 and world == 1 and a.config != "cloud":
+        small = run_small_config(a, local, flush, cpu=not a.no_cpu_baseline)
+
     batched = None
     if rank == 0 and not a.no_batched:
         batched = run_batched(a, local, flush)
@@ -331,6 +335,7 @@ def run_ours(a):
             "render": render_stats,
             "learned_field": learned,
             "batched_frames": batched,
+            "small_config": small,
             "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
                                                   "numWedges", "numHexes", "numTets")} | {
                 "field_bytes": ds.field_bytes, "gen_seconds": gen_s},
@@ -552,6 +557,100 @@ def run_batched(a, local, flush):
         "sequential_exa_render_grid32": {"paths_per_s": paths / (ms_seq / 1e3), "ms": ms_seq},
         "speedup_batched_autotuned_over_sequential": ms_seq / ms_tuned,
     }
+    ctx.close()
+    return out
+
+
+def run_small_config(a, local, flush, cpu=True):
+    """The small configuration's own workloads: (i) 1M uniform points in the
+    cell bounds -> field samples/s, (ii) 256x256 primary rays, 1 spp,
+    single scatter (direct lighting), one directional light, 32^3 grid ->
+    paths/s; plus the majorant build (value ranges + max opacities) at 32^3
+    and 128^3.  CPU figures: the oracle on all host cores."""
+    import ctypes as C
+    import torch
+    import pyoracle
+    from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import datagen
+    from owlexastitcher_gb300 import exastitch as E
+    ds = datagen.Dataset("small")
+    stream = torch.cuda.current_stream()
+    out = {"workload": "small field (3 levels, 32^3 root): 1M uniform points; 256x256 x 1 spp direct lighting"}
+    builds = {}
+    for dims in ((32, 32, 32), (128, 128, 128)):
+        ctx = E.Context(local)
+        model = E.ExaStitchModel.from_dataset(ctx, ds)
+        model.setNumGridCells(dims)
+        sampler = E.ExaStitchSampler(ctx)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sampler.build(model)
+        vr = model.valueRange
+        xf = (np.float32(vr[0]), np.float32(vr[1]))
+        sampler.computeMaxOpacities(ramp_tf(), xf)
+        ctx.sync()
+        builds[f"{dims[0]}^3_gpu_ms"] = (time.perf_counter() - t0) * 1e3
+        if dims == (32, 32, 32):
+            keep = (ctx, model, sampler, xf)
+        else:
+            ctx.close()
+    ctx, model, sampler, xf = keep
+    lo, hi = model.cellBounds
+    rng = np.random.default_rng(42)
+    P = rng.uniform(lo, hi, (1 << 20, 3)).astype(np.float32)
+    pd = torch.from_numpy(P).cuda()
+    res = torch.empty((1 << 20) * 3, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        sampler.sample_device(pd.data_ptr(), res.data_ptr(), len(P), cull=False)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(5.0)
+    e0.record(stream)
+    for _ in range(10):
+        sampler.sample_device(pd.data_ptr(), res.data_ptr(), len(P), cull=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["points_per_s"] = 10 * len(P) / (e0.elapsed_time(e1) / 1e3)
+    lp = E.new_launch_params()
+    sampler.setLPs(lp)
+    w = h = 256
+    setup_render(lp, orbit_camera(lo, hi, w, h), w, h, E.DIRECT_LIGHT_INTEGRATOR, 1, "directional", False)
+    fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+    acc = torch.zeros(w * h * 4, dtype=torch.float32, device="cuda")
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+    lp.ext.traceT = lp.ext.traceTr = None
+    for _ in range(3):
+        E._check(E.lib().exa_render(ctx.h, C.byref(lp), w, h))
+    ms = []
+    for _ in range(5):
+        flush.fill_(6.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        E._check(E.lib().exa_render(ctx.h, C.byref(lp), w, h))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    ctx.sync()
+    out["render_256_1spp_dl"] = {"paths_per_s": w * h / (statistics.median(ms) / 1e3), "ms": statistics.median(ms)}
+    out["majorant_build"] = builds
+    if cpu:
+        n = os.cpu_count()
+        f = pyoracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+        f.sample(P[:1000], cull=0, nthreads=n)
+        t0 = time.perf_counter()
+        f.sample(P, cull=0, nthreads=n)
+        cpu_pts = len(P) / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        f.sample(P[:1 << 17], cull=0, nthreads=1)
+        cpu_pts1 = (1 << 17) / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        f.majorants((32, 32, 32), lo, hi)
+        maj32 = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        f.majorants((128, 128, 128), lo, hi)
+        maj128 = (time.perf_counter() - t0) * 1e3
+        out["cpu"] = {"cores": n, "kind": "port", "points_per_s": cpu_pts, "points_per_s_1_core": cpu_pts1,
+                      "majorant_build_32^3_ms": maj32, "majorant_build_128^3_ms": maj128,
+                      "note": "oracle/oracle.c point location (uniform-grid accel) and majorant build"}
     ctx.close()
     return out
 

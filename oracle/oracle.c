@@ -854,6 +854,27 @@ static int box_test(ray_t r, exa_box3f b, float *t0, float *t1)
   return *t0 < *t1;
 }
 
+/* clip planes after the box test (deviceCode.cu:53-60 intersect; :882-893,
+ * 1010-1021, 1097-1106, 1143-1154, 1229-1240): a front-facing plane moves
+ * t0 forward, a back-facing one t1 back; a ray parallel to a plane gets
+ * FLT_MAX with backFace false, which moves t0 to FLT_MAX */
+static void clip_planes(const exa_launch_params *lp, ray_t r, float *t0, float *t1)
+{
+  for (int i = 0; i < EXA_CLIP_PLANES_MAX; ++i) {
+    if (!lp->clipPlanes[i].enabled) continue;
+    const v3 N = lp->clipPlanes[i].N;
+    const float sd = dot3(N, r.dir);
+    int backFace = 0;
+    float pt = 3.40282347e+38f;
+    if (sd != 0.f) {
+      backFace = sd > 0.f;
+      pt = (lp->clipPlanes[i].d - dot3(N, r.org)) / sd;
+    }
+    if (pt > *t0 && !backFace) *t0 = fmax_t(*t0, pt);
+    if (pt < *t1 && backFace) *t1 = fmin_t(pt, *t1);
+  }
+}
+
 /* sampler/ExaStitchSampler.h:108-126 */
 static exa_sample test_sample(const oc_field *f, v3 pos, int primID)
 {
@@ -1038,6 +1059,7 @@ static v3 sample_light(rctx *c, v3 pos, oc_rng *rng, int numLights, float *trOut
     ray.dir = norm3(lp->lights[which].pos);
     ray.tmax = 1e30f;
     box_test(ray, lp->worldSpaceBounds, &t00, &t11);
+    clip_planes(lp, ray, &t00, &t11);
     ray.tmax = t11;
     sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
     if (trOut) *trOut = Tr;
@@ -1051,6 +1073,7 @@ static v3 sample_light(rctx *c, v3 pos, oc_rng *rng, int numLights, float *trOut
   ray.dir = lightDir;
   ray.tmax = ldWorld;
   box_test(ray, lp->worldSpaceBounds, &t00, &t11);
+  clip_planes(lp, ray, &t00, &t11);
   ray.tmax = t11;
   sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
   if (trOut) *trOut = Tr;
@@ -1099,6 +1122,7 @@ static v4 path_trace(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
   float t0 = 1e30f, t1 = -1e30f;
   const unsigned maxB = (unsigned)lp->ext.maxBounces;
   if (box_test(ray, lp->worldSpaceBounds, &t0, &t1)) {
+    clip_planes(lp, ray, &t0, &t1);
     ray.org = add3(ray.org, muls(ray.dir, t0));
     t1 -= t0;
     while (1) {
@@ -1121,6 +1145,7 @@ static v4 path_trace(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
       ray.org = pos;
       ray.dir = sd;
       box_test(ray, lp->worldSpaceBounds, &t0, &t1);
+      clip_planes(lp, ray, &t0, &t1);
     }
   }
   if (numLights == 0) Ld = mk3(1.f, 1.f, 1.f);
@@ -1137,6 +1162,7 @@ static v4 direct_light(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
   v3 throughput = mk3(1.f, 1.f, 1.f);
   float t0 = 1e30f, t1 = -1e30f;
   if (!box_test(ray, lp->worldSpaceBounds, &t0, &t1)) return bg;
+  clip_planes(lp, ray, &t0, &t1);
   ray.org = add3(ray.org, muls(ray.dir, t0));
   t1 -= t0;
   ray.tmax = t1;
@@ -1163,6 +1189,7 @@ static v4 ray_march(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights)
   v4 color = bg;
   float t0 = 1e30f, t1 = -1e30f;
   if (!box_test(ray, lp->worldSpaceBounds, &t0, &t1)) return color;
+  clip_planes(lp, ray, &t0, &t1);
   const float ils = oc_rng_next(rng);
   const v3 org = xfm_point(&lp->voxelSpaceTransform, ray.org);
   const v3 vd = norm3(xfm_vector(&lp->voxelSpaceTransform, ray.dir));

@@ -537,7 +537,6 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
          EXA_ERR_INVALID, "ray marching needs render.dt > 0");
     need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
          "shade mode not supported");
-    need(!lp->clipPlanes[0].enabled, EXA_ERR_INVALID, "clip planes are not supported");
     need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
     need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
     need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
@@ -1376,8 +1375,8 @@ void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch
        EXA_ERR_INVALID, "integrator not supported (batches render path tracing and direct lighting)");
   need(tpl->shadeMode == EXA_SHADE_MODE_DEFAULT || tpl->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
        "shade mode not supported");
-  need(!tpl->clipPlanes[0].enabled && !tpl->subImage.active && !tpl->render.heatMapEnabled && tpl->meshBVH == 0,
-       EXA_ERR_INVALID, "clip planes, sub-image, heat map and surface meshes are not supported");
+  need(!tpl->subImage.active && !tpl->render.heatMapEnabled && tpl->meshBVH == 0, EXA_ERR_INVALID,
+       "sub-image, heat map and surface meshes are not supported");
   need(tpl->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
        "lpTemplate.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
   need(tpl->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");

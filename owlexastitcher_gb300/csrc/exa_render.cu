@@ -128,6 +128,28 @@ EXA_D bool dda_next(Dda &d)
   return true;
 }
 
+// clip planes as the integrators apply them after the box test
+// (deviceCode.cu:53-60 intersect; :882-893, 1010-1021, 1097-1106, 1143-1154,
+// 1229-1240): a front-facing plane moves t0 forward, a back-facing one t1
+// back.  A ray parallel to a plane gets FLT_MAX with backFace false, which
+// moves t0 to FLT_MAX, as in the reference.
+EXA_D void clip_planes(const exa_launch_params &lp, const RayS &ray, float &t0, float &t1)
+{
+  for (int i = 0; i < EXA_CLIP_PLANES_MAX; ++i) {
+    if (!lp.clipPlanes[i].enabled) continue;
+    const V3 N = mk3(lp.clipPlanes[i].N);
+    const float sd = dot3(N, ray.dir);
+    bool backFace = false;
+    float pt = 3.40282347e+38f;
+    if (sd != 0.f) {
+      backFace = sd > 0.f;
+      pt = __fdiv_rn(lp.clipPlanes[i].d - dot3(N, ray.org), sd);
+    }
+    if (pt > t0 && !backFace) t0 = fmax_t(t0, pt);
+    if (pt < t1 && backFace) t1 = fmin_t(pt, t1);
+  }
+}
+
 struct PathCtx {
   const AccelView &A;
   const exa_launch_params &lp;
@@ -401,6 +423,7 @@ struct Machine {
       else finish_sample(L, background(L));
       return;
     }
+    clip_planes(lp, L.ray, t0, t1);
     L.ray.org = add3(L.ray.org, muls(L.ray.dir, t0));
     t1 -= t0;
     L.ray.tmax = t1;
@@ -423,6 +446,7 @@ struct Machine {
       ray.dir = norm3(mk3(lp.lights[which].pos));
       ray.tmax = 1e30f;
       box_test(ray, lp.worldSpaceBounds, t00, t11);
+      clip_planes(lp, ray, t00, t11);
       ray.tmax = t11;
       L.lightDirectional = true;
     } else {
@@ -433,6 +457,7 @@ struct Machine {
       ray.dir = lightDir;
       ray.tmax = ldWorld;
       box_test(ray, lp.worldSpaceBounds, t00, t11);
+      clip_planes(lp, ray, t00, t11);
       ray.tmax = t11;
       L.lightDen = ld * ld;
       L.lightDirectional = false;
@@ -460,6 +485,7 @@ struct Machine {
     L.ray.dir = sd;
     float t0 = 1e30f, t1 = -1e30f;
     box_test(L.ray, lp.worldSpaceBounds, t0, t1);
+    clip_planes(lp, L.ray, t0, t1);
     L.ray.tmax = t1;
     L.shadow = false;
     walk_begin(L.w, lp, L.ray);
@@ -622,6 +648,7 @@ EXA_D V3 light_nested(PathCtx &c, V3 pos, Rng &rng, int numLights, float *trOut)
     ray.dir = norm3(mk3(lp.lights[which].pos));
     ray.tmax = 1e30f;
     box_test(ray, lp.worldSpaceBounds, t00, t11);
+    clip_planes(lp, ray, t00, t11);
     ray.tmax = t11;
     track<true>(c, ray, np, Tr, xf, rng, tt);
     if (trOut) *trOut = Tr;
@@ -635,6 +662,7 @@ EXA_D V3 light_nested(PathCtx &c, V3 pos, Rng &rng, int numLights, float *trOut)
   ray.dir = lightDir;
   ray.tmax = ldWorld;
   box_test(ray, lp.worldSpaceBounds, t00, t11);
+  clip_planes(lp, ray, t00, t11);
   ray.tmax = t11;
   track<true>(c, ray, np, Tr, xf, rng, tt);
   if (trOut) *trOut = Tr;
@@ -670,6 +698,7 @@ EXA_D float4 sample_nested(PathCtx &c, int px, int py, int pixelID, int s, int h
     unsigned bounce = 0;
     const unsigned maxB = (unsigned)lp.ext.maxBounces;
     if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
+      clip_planes(lp, ray, t0, t1);
       ray.org = add3(ray.org, muls(ray.dir, t0));
       t1 -= t0;
       while (true) {
@@ -702,6 +731,7 @@ EXA_D float4 sample_nested(PathCtx &c, int px, int py, int pixelID, int s, int h
         ray.org = pos;
         ray.dir = sd;
         box_test(ray, lp.worldSpaceBounds, t0, t1);
+        clip_planes(lp, ray, t0, t1);
       }
     }
     if (numLights == 0) Ld = mk3(1.f, 1.f, 1.f);
@@ -710,6 +740,7 @@ EXA_D float4 sample_nested(PathCtx &c, int px, int py, int pixelID, int s, int h
   } else {
     V3 throughput = mk3(1.f, 1.f, 1.f);
     if (!box_test(ray, lp.worldSpaceBounds, t0, t1)) return bg;
+    clip_planes(lp, ray, t0, t1);
     ray.org = add3(ray.org, muls(ray.dir, t0));
     t1 -= t0;
     ray.tmax = t1;
@@ -796,6 +827,7 @@ EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int
   float4 color = bg;
   float t0 = 1e30f, t1 = -1e30f;
   if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
+    clip_planes(lp, ray, t0, t1);
     const float ils = rng.next();
     const V3 org = xfm_point(lp.voxelSpaceTransform, ray.org);
     const V3 vd = norm3(xfm_vector(lp.voxelSpaceTransform, ray.dir));

@@ -238,3 +238,32 @@ def test_render_ray_marching_bit_exact(scenes, torch_cuda, light, dt):
     assert np.array_equal(fb, hfb)
     assert acc.tobytes() == hacc.tobytes()
     assert len(np.unique(fb)) > 4
+
+
+@pytest.mark.parametrize("integrator,flip", [(0, False), (0, True), (1, False), (2, True)])
+def test_render_clip_plane_bit_exact(scenes, torch_cuda, integrator, flip):
+    """A clip plane through the volume's centre (deviceCode.cu:53-60 and the
+    integrators' clipping after the box test), for both orientations."""
+    ds, g, o = scenes
+    w, h = 40, 32
+    c = 0.5 * (g.lo + g.hi)
+    n = np.array([0.6, 0.1, 0.8], np.float32)
+    n /= np.linalg.norm(n)
+    if flip:
+        n = -n
+    g.lp.clipPlanes[0].enabled = 1
+    g.lp.clipPlanes[0].N = tuple_to_v3(n)
+    g.lp.clipPlanes[0].d = float(np.dot(n, c))
+    try:
+        fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, w, h, integrator, 2, "point",
+                                                              integrator == 0)
+    finally:
+        g.lp.clipPlanes[0].enabled = 0
+    assert np.array_equal(fb, hfb)
+    assert acc.tobytes() == hacc.tobytes()
+    assert len(np.unique(fb)) > 4
+
+
+def tuple_to_v3(v):
+    from owlexastitcher_gb300 import exastitch as E
+    return E._v3(v)
