@@ -52,6 +52,8 @@ typedef struct {
   uint64_t numSkippedDegenerate;
   double   seconds;
   float    fieldMin, fieldMax;
+  double   stageSeconds[6];  /* field set-up, Gaussian tables, tree + 2:1
+                                balance, cell values, elements, gridlets  */
 } exa_gen_stats;
 
 /* Fills p with the defaults of the small config (3 levels, 32^3 root,

@@ -844,13 +844,18 @@ int exa_gen_run(const exa_gen_params *p, exa_gen_result **out)
     r->params = *p;
     std::memset(&r->stats, 0, sizeof(r->stats));
     Builder B(*p, *r);
-    B.setupField();
-    B.buildGaussTables();
-    B.buildTree();
+    auto stage = [&](int k, auto &&fn) {
+      const auto a = std::chrono::steady_clock::now();
+      fn();
+      r->stats.stageSeconds[k] = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+    };
+    stage(0, [&] { B.setupField(); });
+    stage(1, [&] { B.buildGaussTables(); });
+    stage(2, [&] { B.buildTree(); });
     if (r->stats.numAmrCells >= 0x7fffffffull) throw std::runtime_error("too many AMR cells for 32-bit ids");
-    B.computeValues();
-    B.buildElements();
-    B.buildGridlets();
+    stage(3, [&] { B.computeValues(); });
+    stage(4, [&] { B.buildElements(); });
+    stage(5, [&] { B.buildGridlets(); });
     r->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     *out = r;
     return 0;

@@ -52,6 +52,7 @@ class GenStats(C.Structure):
         ("seconds", C.c_double),
         ("fieldMin", C.c_float),
         ("fieldMax", C.c_float),
+        ("stageSeconds", C.c_double * 6),
     ]
 
 
@@ -127,7 +128,8 @@ class Dataset:
         self._h = h
         st = GenStats()
         lib().exa_gen_get_stats(h, C.byref(st))
-        self.stats = {f: getattr(st, f) for f, _ in GenStats._fields_ if f != "numCellsPerLevel"}
+        self.stats = {f: getattr(st, f) for f, _ in GenStats._fields_ if f not in ("numCellsPerLevel", "stageSeconds")}
+        self.stats["stageSeconds"] = list(st.stageSeconds)
         self.stats["numCellsPerLevel"] = list(st.numCellsPerLevel)[: self.params.numLevels]
         self.vertices = self._arr("vertices", np.float32, 4)
         self.indices = self._arr("indices", np.int32, 8)
