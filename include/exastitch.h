@@ -291,6 +291,27 @@ typedef struct exa_amr_cell {
 } exa_amr_cell;
 int exa_read_cells(const char *cellsFile, exa_amr_cell *cells, uint64_t *numCells);
 
+/* Surface meshes (TriangleMesh.cpp:27-76; OWLRenderer.cpp:446-545).  A mesh
+ * file is a sequence of meshes, each int32 numVerts, numVerts float3,
+ * int32 numTris, numTris int3; an index outside its mesh is "broken
+ * triangle model".  exa_read_mesh concatenates the meshes into one
+ * triangle soup (indices offset by the vertices before them); call it with
+ * null arrays for the counts, then with arrays that large. */
+int exa_read_mesh(const char *meshFile, exa_vec3f *vertices, uint64_t *numVertices,
+                  exa_vec3i *indices, uint64_t *numTriangles);
+/* The context's surface mesh (one triangle soup; the reference's instance
+ * group of meshes without transforms): uploads it and builds its BVH
+ * (replacing the OptiX triangle GAS and TLAS).  numTriangles == 0 removes
+ * the mesh.  While a mesh is set, exa_sampler_set_lps sets lp->meshBVH to
+ * it and extends worldSpaceBounds by the triangles' bounds
+ * (OWLRenderer.cpp:453-465, 520).  Meshes are drawn by the path tracer,
+ * the direct-light integrator (wavefront path) and the ray marcher; the
+ * batched and the no-allocation entry points reject them. */
+int exa_mesh_set(exa_context *ctx, const exa_vec3f *vertices, uint64_t numVertices,
+                 const exa_vec3i *indices, uint64_t numTriangles);
+/* bounds of the mesh's triangles; EXA_ERR_STATE when none is set */
+int exa_mesh_get_bounds(exa_context *ctx, exa_box3f *bounds);
+
 /* Model::cellBounds / Model::valueRange (model/Model.h:54-55). */
 int exa_model_get_bounds(exa_context *ctx, exa_box3f *cellBounds,
                          exa_range1f *valueRange);

@@ -431,6 +431,10 @@ struct oc_field {
   exa_box3f gb; v3i gd; v3 cs;
   uint32_t *cellBegin; /* gd.x*gd.y*gd.z + 1 */
   int32_t *items;      /* >= 0: gridlet id; < 0: -(elem id) - 1 */
+  /* surface mesh, traced where lp->meshBVH != 0 */
+  const exa_vec3f *meshVertices;
+  const exa_vec3i *meshIndices;
+  uint64_t numTris;
 };
 
 static exa_box3f gridlet_bounds(const exa_gridlet *g)
@@ -544,6 +548,13 @@ void oc_field_destroy(oc_field *f)
   free(f->cellBegin);
   free(f->items);
   free(f);
+}
+
+void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices, const exa_vec3i *indices, uint64_t numTris)
+{
+  f->meshVertices = vertices;
+  f->meshIndices = indices;
+  f->numTris = numTris;
 }
 
 void oc_field_set_prim_opacities(oc_field *f, const float *g, const float *e)
@@ -1042,6 +1053,68 @@ static int sample_interaction(rctx *c, ray_t ray, int shadow, v3 *posOut,
   return type;
 }
 
+/* Surface meshes (MeshGeomCH, deviceCode.cu:306-318): the closest hit by
+ * brute force over all triangles -- the smallest t in [0, tmax], the lowest
+ * triangle index among equal t.  Triangle test: Moeller and Trumbore 1997,
+ * no back-face culling; Ng = normalize(cross(b - a, c - a)), kd = 0.8. */
+typedef struct { int prim; float t; v3 Ng; } mesh_hit;
+
+static int tri_intersect(v3 org, v3 dir, v3 a, v3 b, v3 c, float tmax, float *t)
+{
+  const v3 e1 = sub3(b, a), e2 = sub3(c, a);
+  const v3 p = cross3(dir, e2);
+  const float det = dot3(e1, p);
+  if (!(det != 0.f)) return 0;
+  const float inv = 1.f / det;
+  const v3 s = sub3(org, a);
+  const float u = dot3(s, p) * inv;
+  if (!(u >= 0.f && u <= 1.f)) return 0;
+  const v3 q = cross3(s, e1);
+  const float v = dot3(dir, q) * inv;
+  if (!(v >= 0.f && u + v <= 1.f)) return 0;
+  *t = dot3(e2, q) * inv;
+  return *t >= 0.f && *t <= tmax;
+}
+
+static v3 mesh_vertex(const oc_field *f, int32_t i)
+{
+  const exa_vec3f v = f->meshVertices[i];
+  return mk3(v.x, v.y, v.z);
+}
+
+static mesh_hit mesh_trace(const oc_field *f, v3 org, v3 dir, float tmax)
+{
+  mesh_hit h = {-1, tmax, {0.f, 0.f, 0.f}};
+  float best = tmax;
+  for (uint64_t k = 0; k < f->numTris; ++k) {
+    const exa_vec3i id = f->meshIndices[k];
+    float t;
+    if (tri_intersect(org, dir, mesh_vertex(f, id.x), mesh_vertex(f, id.y), mesh_vertex(f, id.z), best, &t) &&
+        (h.prim < 0 || t < best)) {
+      best = t;
+      h.prim = (int)k;
+    }
+  }
+  if (h.prim >= 0) {
+    const exa_vec3i id = f->meshIndices[h.prim];
+    const v3 a = mesh_vertex(f, id.x), b = mesh_vertex(f, id.y), c = mesh_vertex(f, id.z);
+    h.t = best;
+    h.Ng = norm3(cross3(sub3(b, a), sub3(c, a)));
+  }
+  return h;
+}
+
+/* the surface test of the integrators: trace when the launch has a mesh,
+ * clip ray.tmax at the hit (deviceCode.cu:1032-1039) */
+static mesh_hit mesh_clip(rctx *c, ray_t *ray)
+{
+  mesh_hit h = {-1, 0.f, {0.f, 0.f, 0.f}};
+  if (!c->lp->meshBVH) return h;
+  h = mesh_trace(c->f, ray->org, ray->dir, ray->tmax);
+  if (h.prim >= 0) ray->tmax = fmin_t(ray->tmax, h.t);
+  return h;
+}
+
 /* sampleLight (deviceCode.cu:856-926); directional lights are an
  * extension: lights[i].pos is the direction towards the light, no
  * distance falloff */
@@ -1061,9 +1134,11 @@ static v3 sample_light(rctx *c, v3 pos, oc_rng *rng, int numLights, float *trOut
     box_test(ray, lp->worldSpaceBounds, &t00, &t11);
     clip_planes(lp, ray, &t00, &t11);
     ray.tmax = t11;
-    sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
+    const mesh_hit mh = mesh_clip(c, &ray);
+    const int ct = sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
     if (trOut) *trOut = Tr;
-    const float I = Tr * lp->lights[which].intensity;
+    const float I = ct == BOUNDARY && mh.prim >= 0 ? fmaxf(0.f, dot3(mh.Ng, ray.dir)) * Tr * lp->lights[which].intensity
+                                                   : Tr * lp->lights[which].intensity;
     return mk3(I, I, I);
   }
   v3 lightDir = sub3(lp->lights[which].pos, pos);
@@ -1075,9 +1150,13 @@ static v3 sample_light(rctx *c, v3 pos, oc_rng *rng, int numLights, float *trOut
   box_test(ray, lp->worldSpaceBounds, &t00, &t11);
   clip_planes(lp, ray, &t00, &t11);
   ray.tmax = t11;
-  sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
+  const mesh_hit mh = mesh_clip(c, &ray);
+  const int ct = sample_interaction(c, ray, 1, &np, &Tr, &xf, rng, NULL);
   if (trOut) *trOut = Tr;
-  const float I = Tr / (ld * ld) * lp->lights[which].intensity;
+  /* a shadow ray that reached a surface: max(0, N.l) (:921-925) */
+  const float I = ct == BOUNDARY && mh.prim >= 0
+                      ? fmaxf(0.f, dot3(mh.Ng, lightDir)) * Tr / (ld * ld) * lp->lights[which].intensity
+                      : Tr / (ld * ld) * lp->lights[which].intensity;
   return mk3(I, I, I);
 }
 
@@ -1086,6 +1165,21 @@ static void onb(v3 *u, v3 *v, v3 w)
 {
   *v = fabsf(w.x) > fabsf(w.y) ? norm3(mk3(-w.z, 0.f, w.x)) : norm3(mk3(0.f, w.z, -w.y));
   *u = cross3(*v, w);
+}
+
+/* lambertianSample (deviceCode.cu:932-951): cosine-weighted about N; the
+ * draws in order u1, u2; 2 pi u2 by the turn-based sine/cosine */
+static v3 lambertian_sample(v3 N, oc_rng *rng)
+{
+  v3 u, v;
+  onb(&u, &v, N);
+  const float u1 = oc_rng_next(rng);
+  const float u2 = oc_rng_next(rng);
+  const float r = sqrtf(u1);
+  float sn, cs;
+  oc_sincos_turns(u2, &sn, &cs);
+  const v3 sp = mk3(r * cs, r * sn, sqrtf(1.f - u1));
+  return norm3(add3(add3(smul(sp.x, u), smul(sp.y, v)), smul(sp.z, N)));
 }
 
 /* henyeyGreensteinSample (deviceCode.cu:965-985); direction only */
@@ -1128,10 +1222,19 @@ static v4 path_trace(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
     while (1) {
       float Tr; v3 pos; v4 xf = {0.f, 0.f, 0.f, 0.f};
       ray.tmax = t1;
+      const mesh_hit mh = mesh_clip(c, &ray);
       const int ct = sample_interaction(c, ray, 0, &pos, &Tr, &xf, rng, bounce == 0 ? tHit : NULL);
-      if (ct == BOUNDARY) break;
+      const int surface = ct == BOUNDARY && mh.prim >= 0;
+      if (ct == BOUNDARY && !surface) break;
       if (bounce++ >= maxB) { throughput = mk3(0.f, 0.f, 0.f); break; }
-      const v3 albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
+      v3 albedo;
+      if (surface) {
+        /* just past the surface (eps 1, :1056-1058), kd 0.8 */
+        pos = add3(add3(ray.org, muls(ray.dir, mh.t)), muls(norm3(ray.dir), 1.f));
+        albedo = mk3(.8f, .8f, .8f);
+      } else {
+        albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
+      }
       throughput = mul3(throughput, albedo);
       const float P = rmax3(throughput);
       if (P < 0.2f) {
@@ -1140,8 +1243,16 @@ static v4 path_trace(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
       }
       throughput = add3(throughput, mk3(0.f, 0.f, 0.f)); /* += Le (always 0) */
       if (numLights > 0) Ld = add3(Ld, mul3(throughput, sample_light(c, pos, rng, numLights, bounce == 1 ? trOut : NULL)));
-      const v3 wo = mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z);
-      const v3 sd = hg_sample(wo, lp->ext.hgG, rng);
+      v3 sd;
+      if (surface) {
+        /* Lambertian BRDF, then 16 units off the surface (:1084-1087) */
+        sd = lambertian_sample(mh.Ng, rng);
+        throughput = muls(throughput, fmaxf(0.f, dot3(sd, mh.Ng)));
+        pos = add3(pos, smul(16.f, norm3(sd)));
+      } else {
+        const v3 wo = mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z);
+        sd = hg_sample(wo, lp->ext.hgG, rng);
+      }
       ray.org = pos;
       ray.dir = sd;
       box_test(ray, lp->worldSpaceBounds, &t0, &t1);
@@ -1166,12 +1277,25 @@ static v4 direct_light(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights,
   ray.org = add3(ray.org, muls(ray.dir, t0));
   t1 -= t0;
   ray.tmax = t1;
+  const mesh_hit mh = mesh_clip(c, &ray);
   float Tr; v3 pos; v4 xf = {0.f, 0.f, 0.f, 0.f};
   const int ct = sample_interaction(c, ray, 0, &pos, &Tr, &xf, rng, tHit);
-  if (ct == BOUNDARY) return bg;
-  const v3 albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
-  if (numLights > 0) throughput = mul3(throughput, mul3(albedo, sample_light(c, pos, rng, numLights, trOut)));
-  else throughput = mul3(throughput, albedo);
+  const int surface = ct == BOUNDARY && mh.prim >= 0;
+  if (ct == BOUNDARY && !surface) return bg;
+  v3 albedo;
+  if (surface) {
+    pos = add3(add3(ray.org, muls(ray.dir, mh.t)), muls(norm3(ray.dir), 1.f));
+    albedo = mk3(.8f, .8f, .8f);
+  } else {
+    albedo = lp->ext.albedo < 0.f ? xyz(xf) : mk3(lp->ext.albedo, lp->ext.albedo, lp->ext.albedo);
+  }
+  if (numLights > 0) {
+    throughput = mul3(throughput, mul3(albedo, sample_light(c, pos, rng, numLights, trOut)));
+  } else {
+    throughput = mul3(throughput, albedo);
+    /* surfaces without lights: a headlight (:1196-1198) */
+    if (surface) throughput = muls(throughput, fmaxf(0.f, dot3(mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z), mh.Ng)));
+  }
   v4 color = {throughput.x, throughput.y, throughput.z, 1.f};
   return color;
 }
@@ -1190,6 +1314,15 @@ static v4 ray_march(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights)
   float t0 = 1e30f, t1 = -1e30f;
   if (!box_test(ray, lp->worldSpaceBounds, &t0, &t1)) return color;
   clip_planes(lp, ray, &t0, &t1);
+  if (lp->meshBVH) {
+    /* a surface ends the march, shaded by a headlight (:1243-1251) */
+    const mesh_hit mh = mesh_trace(c->f, ray.org, ray.dir, ray.tmax);
+    if (mh.prim >= 0) {
+      t1 = fmin_t(t1, mh.t);
+      const float cs = fmaxf(0.f, dot3(mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z), mh.Ng));
+      color.x = cs; color.y = cs; color.z = cs; color.w = cs;
+    }
+  }
   const float ils = oc_rng_next(rng);
   const v3 org = xfm_point(&lp->voxelSpaceTransform, ray.org);
   const v3 vd = norm3(xfm_vector(&lp->voxelSpaceTransform, ray.dir));

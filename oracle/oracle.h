@@ -58,6 +58,10 @@ void oc_field_destroy(oc_field *f);
 /* per-primitive max opacities used for culling (NULL: no culling data) */
 void oc_field_set_prim_opacities(oc_field *f, const float *gridletMaxOps,
                                  const float *elemMaxOps);
+/* surface mesh the integrators trace where lp->meshBVH != 0 (arrays are
+ * not copied: numTris int3 rows into the float3 vertices) */
+void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices,
+                       const exa_vec3i *indices, uint64_t numTris);
 /* cellBounds / valueRange as ExaStitchModel::load computes them */
 void oc_field_bounds(const oc_field *f, exa_box3f *cellBounds,
                      exa_range1f *valueRange);

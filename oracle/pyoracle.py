@@ -90,6 +90,7 @@ def lib():
         L.oc_field_create.argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64, vp, C.c_uint64]
         L.oc_field_destroy.argtypes = [vp]
         L.oc_field_set_prim_opacities.argtypes = [vp, vp, vp]
+        L.oc_field_set_mesh.argtypes = [vp, vp, vp, C.c_uint64]
         L.oc_field_bounds.argtypes = [vp, C.POINTER(Box3f), C.POINTER(Range1f)]
         L.oc_sample.restype = Sample
         L.oc_sample.argtypes = [vp, Vec3f, C.c_int]
@@ -168,6 +169,12 @@ class Field:
         self._gops = None if gridlet_ops is None else np.ascontiguousarray(gridlet_ops, dtype=np.float32)
         self._eops = None if elem_ops is None else np.ascontiguousarray(elem_ops, dtype=np.float32)
         lib().oc_field_set_prim_opacities(self.h, _ptr(self._gops), _ptr(self._eops))
+
+    def set_mesh(self, vertices, indices):
+        """surface mesh: float3 vertices, int3 triangles (kept alive here)"""
+        self._mv = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        self._mi = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)
+        lib().oc_field_set_mesh(self.h, _ptr(self._mv), _ptr(self._mi), len(self._mi))
 
     def bounds(self):
         b, r = Box3f(), Range1f()

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "exa_host.h"
+#include "exa_mesh.cuh"
 
 namespace exa {
 
@@ -460,6 +461,19 @@ struct exa_context {
   std::unique_ptr<Surrogate> surrogate;
   float surrogateTol = 0.f;
   std::unique_ptr<struct BatchState> batch;
+  std::unique_ptr<struct MeshState> mesh;
+};
+
+// the context's surface mesh: float4 vertices, 8-int triangle rows (a, b, c,
+// then -1: the element BVH builder's row format), its BVH and the device
+// copy of the view the kernels trace
+struct MeshState {
+  DBuf<float4> vertices;
+  DBuf<int32_t> indices;
+  DBuf<BvhNode> nodes;
+  DBuf<int32_t> parents, leafElem;
+  DBuf<MeshView> view;
+  exa_box3f bounds{};
 };
 
 // state of exa_render_batch: transfer functions, the batch's majorant grid,
@@ -538,7 +552,10 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
          "shade mode not supported");
     need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
-    need(lp->meshBVH == 0, EXA_ERR_INVALID, "surface meshes are not supported");
+    need(lp->meshBVH == 0 || (ctx->mesh && lp->meshBVH == (uint64_t)(uintptr_t)ctx->mesh->view.ptr), EXA_ERR_INVALID,
+         "lp.meshBVH is not this context's mesh (call exa_mesh_set and exa_sampler_set_lps)");
+    need(lp->meshBVH == 0 || useWavefront() || learned || lp->integrator == EXA_RAY_MARCHING_INTEGRATOR,
+         EXA_ERR_INVALID, "surface meshes need the wavefront renderer");
     need(lp->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
          "lp.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
@@ -847,6 +864,104 @@ int exa_read_cells(const char *cellsFile, exa_amr_cell *cells, uint64_t *numCell
   });
 }
 
+// TriangleMesh::load / loadOne (TriangleMesh.cpp:27-76), the meshes
+// concatenated; a file that ends inside a mesh record is an error (the
+// reference keeps the zero-filled remainder)
+int exa_read_mesh(const char *meshFile, exa_vec3f *vertices, uint64_t *numVertices, exa_vec3i *indices,
+                  uint64_t *numTriangles)
+{
+  return guarded([&] {
+    need(numVertices && numTriangles, EXA_ERR_INVALID, "null count");
+    const std::vector<char> d = readFile(meshFile, true);
+    size_t at = 0, nv = 0, nt = 0;
+    auto take = [&](void *dst, size_t bytes) {
+      need(d.size() - at >= bytes, EXA_ERR_INVALID, "truncated mesh file");
+      if (dst) std::memcpy(dst, d.data() + at, bytes);
+      at += bytes;
+    };
+    const bool fill = vertices && indices;
+    const uint64_t capV = fill ? *numVertices : 0, capT = fill ? *numTriangles : 0;
+    while (d.size() - at >= sizeof(int32_t)) {
+      int32_t mv = 0, mt = 0;
+      take(&mv, sizeof(mv));
+      need(mv >= 0, EXA_ERR_INVALID, "broken triangle model");
+      need(fill ? nv + (size_t)mv <= capV : true, EXA_ERR_INVALID, "vertex array too small");
+      take(fill ? vertices + nv : nullptr, (size_t)mv * sizeof(exa_vec3f));
+      take(&mt, sizeof(mt));
+      need(mt >= 0, EXA_ERR_INVALID, "broken triangle model");
+      need(fill ? nt + (size_t)mt <= capT : true, EXA_ERR_INVALID, "triangle array too small");
+      std::vector<exa_vec3i> tri((size_t)mt);
+      take(tri.data(), (size_t)mt * sizeof(exa_vec3i));
+      for (exa_vec3i &t : tri) {
+        need(t.x >= 0 && t.x < mv && t.y >= 0 && t.y < mv && t.z >= 0 && t.z < mv, EXA_ERR_INVALID,
+             "broken triangle model");
+        if (fill) indices[nt++] = exa_vec3i{t.x + (int32_t)nv, t.y + (int32_t)nv, t.z + (int32_t)nv};
+      }
+      if (!fill) nt += (size_t)mt;
+      nv += (size_t)mv;
+      need(nv < 0x7fffffffull && nt < 0x7fffffffull, EXA_ERR_INVALID, "mesh too large");
+    }
+    *numVertices = nv;
+    *numTriangles = nt;
+  });
+}
+
+int exa_mesh_set(exa_context *ctx, const exa_vec3f *vertices, uint64_t numVertices, const exa_vec3i *indices,
+                 uint64_t numTriangles)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    setDevice(ctx);
+    if (numTriangles == 0) {
+      cudaCheck(cudaStreamSynchronize(ctx->stream), "mesh release");
+      ctx->mesh.reset();
+      return;
+    }
+    need(vertices && indices, EXA_ERR_INVALID, "null mesh arrays");
+    need(numVertices < 0x7fffffffull && numTriangles < 0x7fffffffull, EXA_ERR_INVALID, "mesh too large");
+    std::vector<float4> v((size_t)numVertices);
+    for (size_t i = 0; i < v.size(); ++i) v[i] = make_float4(vertices[i].x, vertices[i].y, vertices[i].z, 0.f);
+    std::vector<int32_t> rows((size_t)numTriangles * 8, -1);
+    exa_box3f b;
+    b.lower = {INFINITY, INFINITY, INFINITY};
+    b.upper = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t t = 0; t < (size_t)numTriangles; ++t) {
+      const int32_t id[3] = {indices[t].x, indices[t].y, indices[t].z};
+      for (int k = 0; k < 3; ++k) {
+        need(id[k] >= 0 && (uint64_t)id[k] < numVertices, EXA_ERR_INVALID, "broken triangle model");
+        rows[t * 8 + k] = id[k];
+        const exa_vec3f &p = vertices[id[k]];
+        b.lower = {std::min(b.lower.x, p.x), std::min(b.lower.y, p.y), std::min(b.lower.z, p.z)};
+        b.upper = {std::max(b.upper.x, p.x), std::max(b.upper.y, p.y), std::max(b.upper.z, p.z)};
+      }
+    }
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "mesh replace");
+    auto M = std::make_unique<MeshState>();
+    const size_t nt = (size_t)numTriangles;
+    M->vertices.upload(v.data(), v.size(), ctx->stream);
+    M->indices.upload(rows.data(), rows.size(), ctx->stream);
+    M->nodes.alloc(nt > 1 ? nt - 1 : 1);
+    M->parents.alloc((nt > 1 ? nt - 1 : 0) + nt);
+    M->leafElem.alloc(nt);
+    launchBuildBVH(M->vertices.ptr, M->indices.ptr, nt, b, M->nodes.ptr, M->parents.ptr, M->leafElem.ptr,
+                   ctx->stream);
+    MeshView mv{M->vertices.ptr, M->indices.ptr, M->nodes.ptr, (int)nt};
+    M->view.upload(&mv, 1, ctx->stream);
+    cudaCheck(cudaStreamSynchronize(ctx->stream), "mesh upload");
+    M->bounds = b;
+    ctx->mesh = std::move(M);
+  });
+}
+
+int exa_mesh_get_bounds(exa_context *ctx, exa_box3f *bounds)
+{
+  return guarded([&] {
+    need(ctx && bounds, EXA_ERR_INVALID, "null argument");
+    need(ctx->mesh != nullptr, EXA_ERR_STATE, "no mesh");
+    *bounds = ctx->mesh->bounds;
+  });
+}
+
 int exa_model_get_bounds(exa_context *ctx, exa_box3f *cellBounds, exa_range1f *valueRange)
 {
   return guarded([&] {
@@ -940,6 +1055,14 @@ int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp)
     lp->majorantGrid = m.grid->deviceTraversable;         // OWLRenderer.cpp:435-436
     lp->maxOpacities = ctx->sampler->maxOpacities;         // :655-657
     lp->worldSpaceBounds = m.getBounds();                  // :548-555
+    lp->meshBVH = 0;
+    if (ctx->mesh) {                                       // :453-465, 520, 544
+      lp->meshBVH = (uint64_t)(uintptr_t)ctx->mesh->view.ptr;
+      exa_box3f &b = lp->worldSpaceBounds;
+      const exa_box3f &mb = ctx->mesh->bounds;
+      b.lower = {std::min(b.lower.x, mb.lower.x), std::min(b.lower.y, mb.lower.y), std::min(b.lower.z, mb.lower.z)};
+      b.upper = {std::max(b.upper.x, mb.upper.x), std::max(b.upper.y, mb.upper.y), std::max(b.upper.z, mb.upper.z)};
+    }
     lp->voxelSpaceTransform = m.voxelSpaceTransform;       // :577
     lp->lightSpaceTransform = m.lightSpaceTransform;       // :578
     lp->ext.voxelSpaceTransformInv = m.voxelSpaceTransformInv;

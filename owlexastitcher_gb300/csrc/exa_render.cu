@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "exa_host.h"
+#include "exa_mesh.cuh"
 #include "exa_surrogate.cuh"
 
 namespace exa {
@@ -367,10 +368,33 @@ struct Lane {
   float lightDen, lightI;  // point light: (Tr / lightDen) * lightI; directional: Tr * lightI
   bool lightDirectional = false;
   bool shadow;             // the running walk is a shadow walk
+  // surface mesh: the first triangle on the running walk's ray (-1: none;
+  // after a primary walk, >= 0 only if the walk ended on that surface)
+  int meshPrim = -1;
+  float meshT = 0.f;
+  V3 meshNg = {0.f, 0.f, 0.f};
+  float shadowMesh = -1.f; // shadow walk that reached a surface: max(0, N.l), else -1
   int phase;
   Rng rng;
   Walk w;
 };
+
+// lambertianSample (deviceCode.cu:932-951): cosine-weighted direction about
+// N; the two draws are taken in order (u1, then u2), 2 pi u2 via the
+// project's turn-based sine/cosine
+EXA_D V3 lambertian_sample(V3 N, Rng &rng)
+{
+  const V3 w = N;
+  const V3 v = fabsf(w.x) > fabsf(w.y) ? norm3(mk3(-w.z, 0.f, w.x)) : norm3(mk3(0.f, w.z, -w.y));
+  const V3 u = cross3(v, w);
+  const float u1 = rng.next();
+  const float u2 = rng.next();
+  const float r = __fsqrt_rn(u1);
+  float sn, cs;
+  exa_sincos_turns(u2, sn, cs);
+  const V3 sp = mk3(r * cs, r * sn, __fsqrt_rn(1.f - u1));
+  return norm3(add3(add3(smul(sp.x, u), smul(sp.y, v)), smul(sp.z, w)));
+}
 
 template <int INTEGRATOR>
 struct Machine {
@@ -427,9 +451,37 @@ struct Machine {
     L.ray.org = add3(L.ray.org, muls(L.ray.dir, t0));
     t1 -= t0;
     L.ray.tmax = t1;
+    mesh_clip(L, L.ray);
     L.shadow = false;
     walk_begin(L.w, lp, L.ray);
     L.phase = PH_TRACK;
+  }
+
+  // the first surface along a walk's ray ends the walk there
+  // (deviceCode.cu:1032-1039)
+  EXA_D void mesh_clip(Lane &L, RayS &ray)
+  {
+    L.meshPrim = -1;
+    if (!lp.meshBVH) return;
+    const MeshHit h = trace_mesh(*reinterpret_cast<const MeshView *>(lp.meshBVH), ray.org, ray.dir, ray.tmax);
+    if (h.primID >= 0) {
+      L.meshPrim = h.primID;
+      L.meshT = h.t;
+      L.meshNg = h.Ng;
+      ray.tmax = fmin_t(ray.tmax, h.t);
+    }
+  }
+
+  // sampleLight's mesh test (deviceCode.cu:897-904, 921-922)
+  EXA_D void shadow_mesh(Lane &L, RayS &ray)
+  {
+    L.shadowMesh = -1.f;
+    if (!lp.meshBVH) return;
+    const MeshHit h = trace_mesh(*reinterpret_cast<const MeshView *>(lp.meshBVH), ray.org, ray.dir, ray.tmax);
+    if (h.primID >= 0) {
+      ray.tmax = fmin_t(ray.tmax, h.t);
+      L.shadowMesh = fmaxf(0.f, dot3(h.Ng, ray.dir));
+    }
   }
 
   // sampleLight prologue (deviceCode.cu:866-895): pick a light, start the
@@ -448,6 +500,7 @@ struct Machine {
       box_test(ray, lp.worldSpaceBounds, t00, t11);
       clip_planes(lp, ray, t00, t11);
       ray.tmax = t11;
+      shadow_mesh(L, ray);
       L.lightDirectional = true;
     } else {
       V3 lightDir = sub3(mk3(lp.lights[which].pos), L.pos);
@@ -459,6 +512,7 @@ struct Machine {
       box_test(ray, lp.worldSpaceBounds, t00, t11);
       clip_planes(lp, ray, t00, t11);
       ray.tmax = t11;
+      shadow_mesh(L, ray);
       L.lightDen = ld * ld;
       L.lightDirectional = false;
     }
@@ -479,14 +533,23 @@ struct Machine {
   // pathTracingIntegrate (:1092-1107): phase function, next segment
   EXA_D void scatter(Lane &L)
   {
-    const V3 wo = mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z);
-    const V3 sd = hg_sample(wo, lp.ext.hgG, L.rng);
+    V3 sd;
+    if (L.meshPrim >= 0) {
+      // the event was a surface: Lambertian BRDF (deviceCode.cu:1084-1087)
+      sd = lambertian_sample(L.meshNg, L.rng);
+      L.throughput = muls(L.throughput, fmaxf(0.f, dot3(sd, L.meshNg)));
+      L.pos = add3(L.pos, smul(16.f, norm3(sd)));
+    } else {
+      const V3 wo = mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z);
+      sd = hg_sample(wo, lp.ext.hgG, L.rng);
+    }
     L.ray.org = L.pos;
     L.ray.dir = sd;
     float t0 = 1e30f, t1 = -1e30f;
     box_test(L.ray, lp.worldSpaceBounds, t0, t1);
     clip_planes(lp, L.ray, t0, t1);
     L.ray.tmax = t1;
+    mesh_clip(L, L.ray);
     L.shadow = false;
     walk_begin(L.w, lp, L.ray);
   }
@@ -497,14 +560,20 @@ struct Machine {
     if (L.s == 0 && L.bounce == 0 && L.w.type == SCATTERING && lp.ext.traceT) lp.ext.traceT[L.pixelID] = L.w.t;
     L.pos = xfm_point(lp.ext.voxelSpaceTransformInv, L.w.pos);
     const float4 xf = L.w.xf;
+    const bool surface = L.w.type == BOUNDARY && L.meshPrim >= 0;
+    if (!surface) L.meshPrim = -1;  // scatter() reads it as "the event was a surface"
+    // a surface event (deviceCode.cu:1056-1059, 1182-1185): just past the hit, albedo kd = 0.8
+    if (surface) L.pos = add3(add3(L.ray.org, muls(L.ray.dir, L.meshT)), muls(norm3(L.ray.dir), 1.f));
     if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
-      if (L.w.type == BOUNDARY) { finish_path(L); return; }
+      if (L.w.type == BOUNDARY && !surface) { finish_path(L); return; }
       if (L.bounce++ >= maxB) {
         L.throughput = mk3(0.f, 0.f, 0.f);
         finish_path(L);
         return;
       }
-      const V3 albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+      const V3 albedo = surface ? mk3(.8f, .8f, .8f)
+                                : (lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z)
+                                                       : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo));
       L.throughput = mul3(L.throughput, albedo);
       const float P = rmax3(L.throughput);
       if (P < 0.2f) {
@@ -519,12 +588,16 @@ struct Machine {
       if (numLights > 0) begin_light(L);
       else scatter(L);
     } else {
-      if (L.w.type == BOUNDARY) { finish_sample(L, background(L)); return; }
-      L.albedo = lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z) : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo);
+      if (L.w.type == BOUNDARY && !surface) { finish_sample(L, background(L)); return; }
+      L.albedo = surface ? mk3(.8f, .8f, .8f)
+                         : (lp.ext.albedo < 0.f ? mk3(xf.x, xf.y, xf.z)
+                                                : mk3(lp.ext.albedo, lp.ext.albedo, lp.ext.albedo));
       if (numLights > 0) {
         begin_light(L);
       } else {
-        const V3 tp = mul3(mk3(1.f, 1.f, 1.f), L.albedo);
+        V3 tp = mul3(mk3(1.f, 1.f, 1.f), L.albedo);
+        // surfaces without lights: a headlight (deviceCode.cu:1196-1198)
+        if (surface) tp = muls(tp, fmaxf(0.f, dot3(mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z), L.meshNg)));
         finish_sample(L, make_float4(tp.x, tp.y, tp.z, 1.f));
       }
     }
@@ -532,7 +605,12 @@ struct Machine {
 
   EXA_D void shadow_done(Lane &L)
   {
-    const float I = L.lightDirectional ? L.w.Tr * L.lightI : __fdiv_rn(L.w.Tr, L.lightDen) * L.lightI;
+    // a shadow walk that reached a surface scales by max(0, N.l)
+    // (deviceCode.cu:921-925)
+    const bool lit = L.w.type == BOUNDARY && L.shadowMesh >= 0.f;
+    float I;
+    if (L.lightDirectional) I = lit ? L.shadowMesh * L.w.Tr * L.lightI : L.w.Tr * L.lightI;
+    else I = lit ? __fdiv_rn(L.shadowMesh * L.w.Tr, L.lightDen) * L.lightI : __fdiv_rn(L.w.Tr, L.lightDen) * L.lightI;
     const bool first = L.s == 0 && (INTEGRATOR != EXA_PATH_TRACING_INTEGRATOR || L.bounce == 1);
     if (first && lp.ext.traceTr) lp.ext.traceTr[L.pixelID] = L.w.Tr;
     if (INTEGRATOR == EXA_PATH_TRACING_INTEGRATOR) {
@@ -828,6 +906,16 @@ EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int
   float t0 = 1e30f, t1 = -1e30f;
   if (box_test(ray, lp.worldSpaceBounds, t0, t1)) {
     clip_planes(lp, ray, t0, t1);
+    if (lp.meshBVH) {
+      // a surface ends the march and shades the background behind the
+      // volume with a headlight (deviceCode.cu:1243-1251)
+      const MeshHit h = trace_mesh(*reinterpret_cast<const MeshView *>(lp.meshBVH), ray.org, ray.dir, ray.tmax);
+      if (h.primID >= 0) {
+        t1 = fmin_t(t1, h.t);
+        const float cs = fmaxf(0.f, dot3(mk3(-ray.dir.x, -ray.dir.y, -ray.dir.z), h.Ng));
+        color = make_float4(cs, cs, cs, cs);
+      }
+    }
     const float ils = rng.next();
     const V3 org = xfm_point(lp.voxelSpaceTransform, ray.org);
     const V3 vd = norm3(xfm_vector(lp.voxelSpaceTransform, ray.dir));
@@ -970,8 +1058,9 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
 // + walk part (SoA: word k of record i at (kPathStride + k) * cap + i); the
 // walk kernel reads and writes only walk parts, and an ended walk leaves a
 // short event record that points at its path part.
-constexpr int kPathWords = 26;
-constexpr int kPathStride = 28;  // path words padded to whole 16-byte vectors
+constexpr int kPathWords = 31;
+constexpr int kPathStride = 32;  // path words padded to whole 16-byte vectors
+static_assert(kPathWords <= kPathStride && kPathStride % 4 == 0, "path part: whole uint4 vectors");
 constexpr int kWalkWords = 35;
 constexpr int kLaneWords = kPathStride + kWalkWords;
 static_assert(kLaneWords == kWfLaneWords, "record size");
@@ -1009,7 +1098,9 @@ EXA_D void wf_store_path(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
   p[3] = make_uint4(f(L.throughput.z), f(L.Ld.x), f(L.Ld.y), f(L.Ld.z));
   p[4] = make_uint4(f(L.pos.x), f(L.pos.y), f(L.pos.z), f(L.albedo.x));
   p[5] = make_uint4(f(L.albedo.y), f(L.albedo.z), L.bounce, f(L.lightDen));
-  p[6] = make_uint4(f(L.lightI), (L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1), 0u, 0u);
+  p[6] = make_uint4(f(L.lightI), (L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1), (uint32_t)L.meshPrim,
+                    f(L.meshT));
+  p[7] = make_uint4(f(L.meshNg.x), f(L.meshNg.y), f(L.meshNg.z), f(L.shadowMesh));
 }
 
 EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width)
@@ -1017,7 +1108,7 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   (void)cap;
   const uint4 *p = reinterpret_cast<const uint4 *>(b + (size_t)i * kPathStride);
   const uint4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4),
-              q5 = __ldg(p + 5), q6 = __ldg(p + 6);
+              q5 = __ldg(p + 5), q6 = __ldg(p + 6), q7 = __ldg(p + 7);
   const auto f = [](uint32_t v) { return __uint_as_float(v); };
   L.px = (int)q0.x; L.py = (int)q0.y; L.s = (int)q0.z;
   L.pixelID = L.px + width * L.py;
@@ -1031,6 +1122,10 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   L.bounce = q5.z; L.lightDen = f(q5.w); L.lightI = f(q6.x);
   L.lightDirectional = (q6.y & 1u) != 0u;
   L.frame = (int)(q6.y >> 1);
+  L.meshPrim = (int)q6.z;
+  L.meshT = f(q6.w);
+  L.meshNg = mk3(f(q7.x), f(q7.y), f(q7.z));
+  L.shadowMesh = f(q7.w);
 }
 
 // shadow flag, RNG and the walk
@@ -1079,6 +1174,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
 // and the slot of the walk's path part, which stays in the round's input
 // queue (that buffer is rewritten only in the next round)
 constexpr int kEventWords = 14;
+static_assert(kEventWords <= kWfLaneWords, "an event record fits a queue slot");
 
 EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, unsigned src)
 {
@@ -1130,7 +1226,6 @@ EXA_D void wf_load(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsign
 
 EXA_D void wf_copy_path(const uint32_t *__restrict__ src, unsigned i, uint32_t *dst, unsigned j, unsigned cap)
 {
-#pragma unroll
   (void)cap;
   const uint4 *a = reinterpret_cast<const uint4 *>(src + (size_t)i * kPathStride);
   uint4 *d = reinterpret_cast<uint4 *>(dst + (size_t)j * kPathStride);

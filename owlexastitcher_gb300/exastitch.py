@@ -242,6 +242,7 @@ EXPORTED = [
     "exa_surrogate_get_macrocells", "exa_render_surrogate", "exa_batch_set_transfer_functions",
     "exa_batch_set_majorant_grid", "exa_batch_set_tile_width", "exa_render_batch", "exa_batch_autotune",
     "exa_read_grids", "exa_model_load", "exa_read_xf", "exa_xf_range", "exa_opacity_scale", "exa_read_cells",
+    "exa_read_mesh", "exa_mesh_set", "exa_mesh_get_bounds",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -305,6 +306,9 @@ def lib():
         "exa_xf_range": ([C.POINTER(Xf)], range1f),
         "exa_opacity_scale": ([C.c_float], C.c_float),
         "exa_read_cells": ([C.c_char_p, vp, C.POINTER(u64)], C.c_int),
+        "exa_read_mesh": ([C.c_char_p, vp, C.POINTER(u64), vp, C.POINTER(u64)], C.c_int),
+        "exa_mesh_set": ([ctx_p, vp, u64, vp, u64], C.c_int),
+        "exa_mesh_get_bounds": ([ctx_p, C.POINTER(box3f)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -542,6 +546,13 @@ class Renderer:
             self.sampler.computeMaxOpacities(self.colorMap, self._xf_range())
             self.sampler.setLPs(self.lp)
 
+    def setMesh(self, vertices, indices):
+        """surface mesh (OWLRenderer.cpp:446-545): float3 vertices, int3
+        triangles; an empty triangle list removes it"""
+        set_mesh(self.ctx, vertices, indices)
+        self.sampler.setLPs(self.lp)
+        self.accumID = 0
+
     def setOpacityScale(self, s):
         self.lp.transferFunc.opacityScale = float(np.power(np.float32(1.1), np.float32(s - 100)))
 
@@ -732,3 +743,29 @@ def read_cells(cells_file):
     out = np.zeros(n.value, np.dtype([("pos", "<i4", 3), ("level", "<i4")]))
     _check(L.exa_read_cells(os.fsencode(cells_file), _np_ptr(out), C.byref(n)))
     return out
+
+
+def read_mesh(mesh_file):
+    """triangle-mesh file (TriangleMesh.cpp:27-76) -> (float32 [n, 3]
+    vertices, int32 [m, 3] triangles), all meshes of the file concatenated"""
+    L = lib()
+    nv, nt = C.c_uint64(0), C.c_uint64(0)
+    _check(L.exa_read_mesh(os.fsencode(mesh_file), None, C.byref(nv), None, C.byref(nt)))
+    v = np.zeros((nv.value, 3), np.float32)
+    t = np.zeros((nt.value, 3), np.int32)
+    _check(L.exa_read_mesh(os.fsencode(mesh_file), _np_ptr(v), C.byref(nv), _np_ptr(t), C.byref(nt)))
+    return v, t
+
+
+def set_mesh(ctx, vertices, indices):
+    """the context's surface mesh (exa_mesh_set); no triangles removes it"""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
+    _check(lib().exa_mesh_set(ctx.h, _np_ptr(v), len(v), _np_ptr(t), len(t)))
+
+
+def mesh_bounds(ctx):
+    b = box3f()
+    _check(lib().exa_mesh_get_bounds(ctx.h, C.byref(b)))
+    return (np.array([b.lower.x, b.lower.y, b.lower.z], np.float32),
+            np.array([b.upper.x, b.upper.y, b.upper.z], np.float32))

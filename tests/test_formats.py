@@ -120,3 +120,43 @@ def test_model_load_matches_arrays(tmp_path, native):
     s2.build(m2)
     r2, _ = s2.majorants((8, 8, 8))
     assert r1.tobytes() == r2.tobytes()
+
+
+def _mesh_record(v, t):
+    return (np.array([len(v)], np.int32).tobytes() + np.asarray(v, np.float32).tobytes() +
+            np.array([len(t)], np.int32).tobytes() + np.asarray(t, np.int32).tobytes())
+
+
+def test_read_mesh(tmp_path, native):
+    """TriangleMesh::load (TriangleMesh.cpp:27-76): meshes back to back; read
+    as one soup with each mesh's indices offset by the vertices before it."""
+    from owlexastitcher_gb300 import exastitch as E
+    rng = np.random.default_rng(5)
+    v1 = rng.uniform(-1, 1, (7, 3)).astype(np.float32)
+    t1 = rng.integers(0, 7, (5, 3)).astype(np.int32)
+    v2 = rng.uniform(-1, 1, (4, 3)).astype(np.float32)
+    t2 = np.array([[0, 1, 2], [1, 2, 3]], np.int32)
+    # two stray bytes at the end: too short for a count, the loader stops there
+    (tmp_path / "m.mesh").write_bytes(_mesh_record(v1, t1) + _mesh_record(v2, t2) + b"\0\0")
+    v, t = E.read_mesh(str(tmp_path / "m.mesh"))
+    assert v.tobytes() == np.concatenate([v1, v2]).tobytes()
+    assert np.array_equal(t, np.concatenate([t1, t2 + 7]))
+    (tmp_path / "e.mesh").write_bytes(b"")
+    v, t = E.read_mesh(str(tmp_path / "e.mesh"))
+    assert v.shape == (0, 3) and t.shape == (0, 3)
+
+
+def test_read_mesh_errors(tmp_path, native):
+    from owlexastitcher_gb300 import exastitch as E
+    v = np.zeros((3, 3), np.float32)
+    (tmp_path / "b.mesh").write_bytes(_mesh_record(v, [[0, 1, 3]]))
+    with pytest.raises(E.ExaError, match="broken triangle model"):
+        E.read_mesh(str(tmp_path / "b.mesh"))
+    (tmp_path / "n.mesh").write_bytes(_mesh_record(v, [[0, -1, 2]]))
+    with pytest.raises(E.ExaError, match="broken triangle model"):
+        E.read_mesh(str(tmp_path / "n.mesh"))
+    (tmp_path / "t.mesh").write_bytes(_mesh_record(v, [[0, 1, 2]])[:-4])
+    with pytest.raises(E.ExaError, match="truncated"):
+        E.read_mesh(str(tmp_path / "t.mesh"))
+    with pytest.raises(E.ExaError, match="cannot open"):
+        E.read_mesh(str(tmp_path / "missing.mesh"))

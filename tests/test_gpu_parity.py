@@ -267,3 +267,95 @@ def test_render_clip_plane_bit_exact(scenes, torch_cuda, integrator, flip):
 def tuple_to_v3(v):
     from owlexastitcher_gb300 import exastitch as E
     return E._v3(v)
+
+
+def mesh_scene(lo, hi, rings=10, segs=16):
+    """A UV sphere inside the volume and a ground quad that reaches past its
+    bounds (so it extends the world bounds): float3 vertices, int3 triangles."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    ext = hi - lo
+    c = lo + ext * np.array([0.55, 0.45, 0.5])
+    r = 0.22 * ext.min()
+    verts, tris = [], []
+    for i in range(rings + 1):
+        th = np.pi * i / rings
+        for j in range(segs):
+            ph = 2 * np.pi * j / segs
+            verts.append(c + r * np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)]))
+    for i in range(rings):
+        for j in range(segs):
+            a, b = i * segs + j, i * segs + (j + 1) % segs
+            tris += [(a, a + segs, b), (b, a + segs, b + segs)]
+    z = lo[2] + 0.2 * ext[2]
+    base = len(verts)
+    verts += [(lo[0] - 0.3 * ext[0], lo[1] - 0.3 * ext[1], z), (hi[0] + 0.3 * ext[0], lo[1] - 0.3 * ext[1], z),
+              (hi[0] + 0.3 * ext[0], hi[1] + 0.3 * ext[1], z), (lo[0] - 0.3 * ext[0], hi[1] + 0.3 * ext[1], z)]
+    tris += [(base, base + 1, base + 2), (base, base + 2, base + 3)]
+    return np.array(verts, np.float32), np.array(tris, np.int32)
+
+
+@pytest.mark.parametrize("integrator,spp,light,ext", [
+    (0, 2, "point", True),         # path tracer: Lambertian bounces off the surfaces
+    (0, 1, "none", False),         # path tracer, ambient light
+    (1, 2, "directional", False),  # direct light: shadow rays that end on a surface
+    (1, 1, "none", False),         # direct light without lights: headlight shading
+    (2, 2, "point", False),        # ray marcher: the surface ends the march
+])
+def test_render_mesh_bit_exact(scenes, torch_cuda, integrator, spp, light, ext):
+    """Surface meshes (MeshGeomCH and the integrators' mesh tests,
+    deviceCode.cu:295-318, 897-925, 1032-1087, 1165-1198, 1243-1251): the
+    BVH closest hit on the GPU against the oracle's brute force."""
+    ds, g, o = scenes
+    from owlexastitcher_gb300 import exastitch as E
+    v, t = mesh_scene(g.lo, g.hi)
+    E.set_mesh(g.ctx, v, t)
+    g.sampler.setLPs(g.lp)
+    o.f.set_mesh(v, t)
+    mlo, mhi = E.mesh_bounds(g.ctx)
+    assert np.array_equal(mlo, v[t.ravel()].min(0)) and np.array_equal(mhi, v[t.ravel()].max(0))
+    wb = g.lp.worldSpaceBounds
+    assert wb.lower.x == min(mlo[0], g.model.getBounds()[0][0]) and wb.lower.z == min(mlo[2], g.lo[2])
+    assert g.lp.meshBVH != 0
+    try:
+        w, h = 40, 32
+        fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, w, h, integrator, spp, light, ext)
+        assert g.ctx.device_errors() == 0
+    finally:
+        E.set_mesh(g.ctx, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
+        g.sampler.setLPs(g.lp)
+        o.f.set_mesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
+    assert g.lp.meshBVH == 0
+    assert np.array_equal(fb, hfb)
+    assert acc.tobytes() == hacc.tobytes()
+    assert tT.tobytes() == htT.tobytes()
+    assert tTr.tobytes() == htTr.tobytes()
+    assert len(np.unique(fb)) > 4
+
+
+def test_mesh_rejected_where_unsupported(scenes, torch_cuda):
+    """lp.meshBVH must be this context's mesh; the batched and no-allocation
+    entry points reject meshes."""
+    ds, g, o = scenes
+    from owlexastitcher_gb300 import exastitch as E
+    w, h = 16, 16
+    cam = orbit_camera(g.lo, g.hi, w, h)
+    lp = setup_render(g.lp, cam, w, h, 1, 1, "none", False, g.lo, g.hi)
+    fb = torch_cuda.zeros(w * h, dtype=torch_cuda.int32, device="cuda")
+    acc = torch_cuda.zeros(w * h * 4, dtype=torch_cuda.float32, device="cuda")
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+    lp.ext.traceT = lp.ext.traceTr = None
+    lp.meshBVH = 16  # not a mesh of this context
+    try:
+        assert E.lib().exa_render(g.ctx.h, E.C.byref(lp), w, h) == E.EXA_ERR_INVALID
+        assert b"meshBVH" in E.lib().exa_last_error()
+        v, t = mesh_scene(g.lo, g.hi, 4, 6)
+        E.set_mesh(g.ctx, v, t)
+        g.sampler.setLPs(lp)
+        assert E.lib().exa_render_noalloc(g.ctx.h, E.C.byref(lp), w, h) == E.EXA_ERR_INVALID
+        with pytest.raises(E.ExaError, match="broken triangle model"):
+            E.set_mesh(g.ctx, v, t + len(v))
+    finally:
+        E.set_mesh(g.ctx, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
+        g.sampler.setLPs(g.lp)
+    assert g.lp.meshBVH == 0

@@ -112,3 +112,57 @@ def test_dda_axis_parallel_ray(oracle, zero_axes):
         for a in zero_axes:
             assert np.all(cells[:, a] == start[a])
         assert np.all(np.isfinite(t0)) and np.all(np.isfinite(t1)) and np.all(t1 >= t0)
+
+
+def test_mesh_headlight_shading(oracle, native):
+    """A transparent volume and one quad across every ray at x = 4, facing
+    the camera: the direct-light integrator without lights shades a surface
+    hit by kd * max(0, -dir . Ng) (deviceCode.cu:1182-1198), kd = 0.8."""
+    from helpers import host_lp
+    from owlexastitcher_gb300 import exastitch as E
+    g = np.zeros(1, oracle.GRIDLET_DTYPE)
+    g["lower"], g["level"], g["dims"], g["begin"] = (0, 0, 0), 0, (8, 8, 8), 0
+    f = oracle.Field(np.zeros((0, 4), np.float32), np.zeros((0, 8), np.int32), g, np.full(9 ** 3, 0.5, np.float32))
+    lo, hi, _ = f.bounds()
+    quad = np.float32([[4, -10, -10], [4, 20, -10], [4, 20, 20], [4, -10, 20]])
+    f.set_mesh(quad, np.int32([[0, 2, 1], [0, 3, 2]]))   # winding: Ng = -x, towards the camera
+    tf = np.tile(np.float32([[1, 1, 1, 0.0]]), (16, 1))
+    ranges = f.majorants((4, 4, 4), lo, hi)
+    ops = oracle.max_opacities(ranges, tf, (0.0, 1.0))
+    W, H = 32, 32
+    lp = E.LaunchParams()
+    E.lib().exa_launch_params_init(C.byref(lp))
+    lp.integrator = 1
+    lp.render.spp = 1
+    lp.meshBVH = 1   # any non-zero handle: the oracle traces its own mesh
+    lp.transferFunc.domain.lower, lp.transferFunc.domain.upper = 0.0, 1.0
+    lp.transferFunc.numValues = 16
+    lp.majorantGrid.dims = E.vec3i(4, 4, 4)
+    lp.majorantGrid.bounds = E._box(lo, hi)
+    lp.worldSpaceBounds = E._box(lo, hi)
+    lp.camera.org = E._v3([-50.0, 4.5, 4.5])
+    sp = 0.05   # rays spread over y, z in 4.5 +- 0.8 at x = 0.5: all cross the volume
+    lp.camera.dir_00 = E._v3([1.0, -sp * W / 2 / 50, -sp * H / 2 / 50])
+    lp.camera.dir_du = E._v3([0.0, sp / 50, 0.0])
+    lp.camera.dir_dv = E._v3([0.0, 0.0, sp / 50])
+
+    class O:
+        pass
+    o = O()
+    o.f, o.tf, o.max_ops = f, tf, ops
+    hl, fb, acc, tT, tTr = host_lp(lp, o, W, H)
+    f.render(bytes(hl), W, H)
+    # cos = d.x / |d| for the jittered d = dir_00 + (px + rx) du + (py + ry) dv,
+    # rx, ry in [0, 1): each pixel lies between the values at its corners
+    px, py = np.meshgrid(np.arange(W), np.arange(H))
+    corner = []
+    for rx, ry in ((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (1.0, 1.0)):
+        dy = (-W / 2 + px + rx) * sp / 50
+        dz = (-H / 2 + py + ry) * sp / 50
+        corner.append((0.8 / np.sqrt(1 + dy * dy + dz * dz)).ravel())
+    lo_c = np.min(corner, 0) - 1e-6
+    hi_c = np.max(corner, 0) + 1e-6
+    col = acc[:, 0]
+    assert np.all((col >= lo_c) & (col <= hi_c))
+    assert np.array_equal(acc[:, 0], acc[:, 1]) and np.array_equal(acc[:, 0], acc[:, 2])
+    assert np.all(acc[:, 3] == 1.0)
