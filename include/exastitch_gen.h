@@ -7,7 +7,8 @@
  *   gridlets (.grids)  -> makeGrids.cpp:191-209, 114-168 (8^3 bricks)
  *   ExaStitch arrays   -> model/ExaStitchModel.cpp:24-257 (vertex values,
  *                         8-wide index rows, NaN for absent gridlet scalars)
- * Host code only (C++/OpenMP); the output feeds exa_model_create.
+ * Host code (C++/OpenMP) and a GPU version of the same stages (CUDA); the
+ * output feeds exa_model_create.
  *
  * Level convention (the reference's): level L cells are 2^L finest units
  * wide, level 0 is the finest; the root level is numLevels-1.
@@ -61,6 +62,11 @@ typedef struct {
 void exa_gen_params_default(exa_gen_params *p);
 /* Generates AMR cells, their dual mesh and the ExaStitch arrays. */
 int  exa_gen_run(const exa_gen_params *p, exa_gen_result **out);
+/* The same generator with every stage after the field set-up as CUDA
+ * kernels on GPU `device`; the result is identical bit for bit to
+ * exa_gen_run's and is returned in host memory like it (stageSeconds time
+ * the GPU stages, including the copies back). */
+int  exa_gen_run_gpu(const exa_gen_params *p, int32_t device, exa_gen_result **out);
 void exa_gen_free(exa_gen_result *r);
 void exa_gen_get_stats(const exa_gen_result *r, exa_gen_stats *s);
 /* Borrowed pointers into the result (valid until exa_gen_free). */

@@ -1,6 +1,6 @@
 """Builds the native parts in-tree:
   libexastitch.so -- the CUDA path (sm_103a kernels + C++ host + C ABI)
-  libexagen.so    -- the dataset generator (host C++)
+  libexagen.so    -- the dataset generator (host C++ and its CUDA version)
 Compiles translation units in parallel and skips up-to-date outputs.
 
     python -m owlexastitcher_gb300.build
@@ -73,12 +73,30 @@ def build_exastitch(verbose=False):
 
 
 def build_exagen():
+    """libexagen.so: the CPU generator (g++, OpenMP) and its GPU version
+    (nvcc), both without contracted multiply-adds so that they evaluate the
+    shared field code identically."""
+    os.makedirs(BUILD, exist_ok=True)
     out = os.path.join(PKG, "libexagen.so")
-    src = os.path.join(CSRC, "gen", "exagen.cpp")
-    deps = [src, os.path.join(INCLUDE, "exastitch_gen.h"), os.path.join(INCLUDE, "exastitch.h")]
-    if _newer(out, deps):
+    gen = os.path.join(CSRC, "gen")
+    hdrs = [os.path.join(gen, h) for h in ("exagen_field.h", "exagen_internal.h")] + [
+        os.path.join(INCLUDE, "exastitch_gen.h"), os.path.join(INCLUDE, "exastitch.h")]
+    cpu_src, gpu_src = os.path.join(gen, "exagen.cpp"), os.path.join(gen, "exagen_gpu.cu")
+    cpu_obj, gpu_obj = os.path.join(BUILD, "exagen.cpp.o"), os.path.join(BUILD, "exagen_gpu.cu.o")
+    jobs = []
+    if _newer(cpu_obj, [cpu_src] + hdrs):
         cxx = shutil.which("g++") or "g++"
-        _run([cxx, "-O3", "-fPIC", "-shared", "-fopenmp", "-std=c++17", "-o", out, src])
+        jobs.append([cxx, "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-Wall", "-c", cpu_src,
+                     "-o", cpu_obj])
+    if _newer(gpu_obj, [gpu_src] + hdrs):
+        jobs.append([nvcc()] + ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                                       "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off",
+                                       "-Xcompiler", "-Wall", "-c", gpu_src, "-o", gpu_obj])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
+    if _newer(out, [cpu_obj, gpu_obj]):
+        _run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-Xcompiler", "-fopenmp", "-o", out, cpu_obj,
+                                gpu_obj, "-lgomp"])
     return out
 
 

@@ -18,7 +18,7 @@
 // point is a short descent from the root.  Dual cells are generated once,
 // by the lowest (y, x, z) cell of the finest level among their corners
 // (makeDual.cpp:641-655), exactly as in the reference.
-#include "../../../include/exastitch_gen.h"
+#include "exagen_internal.h"
 
 #include <algorithm>
 #include <atomic>
@@ -32,125 +32,102 @@
 #include <omp.h>
 #endif
 
+using exagen::Field;
+using exagen::FieldView;
+using exagen::Stream;
+
 namespace {
-
 thread_local std::string g_err;
+} // namespace
 
-// ---------------------------------------------------------------- rng
-inline uint64_t mix64(uint64_t z)
+namespace exagen {
+
+void setLastError(const std::string &msg) { g_err = msg; }
+
+int numThreadsOf(const exa_gen_params *p)
 {
-  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-  return z ^ (z >> 31);
+#ifdef _OPENMP
+  return p->numThreads > 0 ? p->numThreads : omp_get_max_threads();
+#else
+  (void)p;
+  return 1;
+#endif
 }
 
-struct Stream {
-  uint64_t s;
-  explicit Stream(uint64_t seed) : s(seed) {}
-  double next01()
-  {
-    s += 0x9e3779b97f4a7c15ull;
-    return (double)(mix64(s) >> 11) * (1.0 / 9007199254740992.0);
-  }
-  double uniform(double a, double b) { return a + (b - a) * next01(); }
-};
+void checkParams(const exa_gen_params *p)
+{
+  if (!p) throw std::runtime_error("null argument");
+  if (p->numLevels < 1 || p->numLevels > kMaxLevels) throw std::runtime_error("numLevels must be in [1,16]");
+  for (int a = 0; a < 3; ++a)
+    if (p->rootDims[a] < 1) throw std::runtime_error("rootDims must be positive");
+  if (p->noiseOctaves < 0 || p->noiseOctaves > kMaxOctaves) throw std::runtime_error("noiseOctaves must be in [0,16]");
+}
 
-// ---------------------------------------------------------------- field
-struct Field {
-  int kind = EXA_FIELD_GAUSSIANS;
-  int K = 0;
-  std::vector<double> cx, cy, cz, sx, sy, sz, amp;
-  double noiseAmp = 0.1;
-  int octaves = 4;
-  uint64_t seed = 0;
-  double extent[3] = {1, 1, 1};  // finest units per axis
-  // cloud mapping f = clamp((exp(3 fbm) - lo) / (hi - lo), 0, 1)
-  double cloudLo = 0.0, cloudHi = 1.0;
-
+void Field::setup(const exa_gen_params &P)
+{
+  const int Lroot = P.numLevels - 1;
+  kind = P.fieldKind;
+  seed = P.seed;
+  noiseAmp = P.noiseAmplitude;
+  octaves = P.noiseOctaves;
+  for (int a = 0; a < 3; ++a) extent[a] = (double)((int64_t)P.rootDims[a] << Lroot);
   // lattice values of each octave inside the unit cube, precomputed
-  std::vector<std::vector<float>> latTab;
-  std::vector<int> latN;
-  void buildLattices(int n, double f0)
-  {
-    latTab.assign(n, {});
-    latN.assign(n, 0);
-    double f = f0;
-    for (int o = 0; o < n; ++o, f *= 2.0) {
-      const int m = (int)f + 2;
-      latN[o] = m;
-      latTab[o].resize((size_t)m * m * m);
-      for (int k = 0; k < m; ++k)
-        for (int j = 0; j < m; ++j)
-          for (int i = 0; i < m; ++i) latTab[o][((size_t)k * m + j) * m + i] = (float)lattice(i, j, k, o);
+  const FieldView v0 = view();
+  latTab.assign(octaves, {});
+  latN.assign(octaves, 0);
+  double f = kind == EXA_FIELD_GAUSSIANS ? 4.0 : 2.0;
+  for (int o = 0; o < octaves; ++o, f *= 2.0) {
+    const int m = (int)f + 2;
+    latN[o] = m;
+    latTab[o].resize((size_t)m * m * m);
+    for (int k = 0; k < m; ++k)
+      for (int j = 0; j < m; ++j)
+        for (int i = 0; i < m; ++i) latTab[o][((size_t)k * m + j) * m + i] = (float)lattice(v0, i, j, k, o);
+  }
+  if (kind == EXA_FIELD_GAUSSIANS) {
+    Stream s(P.seed);
+    K = P.numGaussians;
+    for (int k = 0; k < K; ++k) {
+      cx.push_back(s.next01()); cy.push_back(s.next01()); cz.push_back(s.next01());
+      sx.push_back(s.uniform(0.03, 0.15)); sy.push_back(s.uniform(0.03, 0.15));
+      sz.push_back(s.uniform(0.03, 0.15));
+      amp.push_back(s.uniform(0.2, 1.0));
     }
   }
-  double latticeFast(int64_t i, int64_t j, int64_t k, int o) const
-  {
-    const int m = o < (int)latN.size() ? latN[o] : 0;
-    if (i >= 0 && j >= 0 && k >= 0 && i < m && j < m && k < m)
-      return (double)latTab[o][((size_t)k * m + j) * m + i];
-    return lattice(i, j, k, o);
+}
+
+FieldView Field::view() const
+{
+  FieldView v{};
+  v.kind = kind;
+  v.K = K;
+  v.octaves = octaves;
+  v.seed = seed;
+  v.noiseAmp = noiseAmp;
+  for (int a = 0; a < 3; ++a) v.extent[a] = extent[a];
+  v.cloudLo = cloudLo;
+  v.cloudHi = cloudHi;
+  for (int o = 0; o < (int)latTab.size() && o < kMaxOctaves; ++o) {
+    v.lat[o] = latTab[o].data();
+    v.latN[o] = latN[o];
   }
-  double lattice(int64_t i, int64_t j, int64_t k, int o) const
-  {
-    uint64_t h = mix64(seed ^ 0x243f6a8885a308d3ull);
-    h = mix64(h ^ (uint64_t)(i * 73856093ll));
-    h = mix64(h ^ (uint64_t)(j * 19349663ll));
-    h = mix64(h ^ (uint64_t)(k * 83492791ll));
-    h = mix64(h ^ (uint64_t)o);
-    return (double)(float)((double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0);
-  }
-  // value noise: hashed lattice values, smoothstep-weighted trilinear
-  double vnoise(double x, double y, double z, int o) const
-  {
-    const double fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
-    const int64_t i = (int64_t)fx, j = (int64_t)fy, k = (int64_t)fz;
-    double tx = x - fx, ty = y - fy, tz = z - fz;
-    tx = tx * tx * (3 - 2 * tx); ty = ty * ty * (3 - 2 * ty); tz = tz * tz * (3 - 2 * tz);
-    double c[2][2][2];
-    for (int a = 0; a < 2; ++a)
-      for (int b = 0; b < 2; ++b)
-        for (int d = 0; d < 2; ++d) c[a][b][d] = latticeFast(i + d, j + b, k + a, o);
-    const double x00 = c[0][0][0] + tx * (c[0][0][1] - c[0][0][0]);
-    const double x01 = c[0][1][0] + tx * (c[0][1][1] - c[0][1][0]);
-    const double x10 = c[1][0][0] + tx * (c[1][0][1] - c[1][0][0]);
-    const double x11 = c[1][1][0] + tx * (c[1][1][1] - c[1][1][0]);
-    const double y0 = x00 + ty * (x01 - x00), y1 = x10 + ty * (x11 - x10);
-    return y0 + tz * (y1 - y0);
-  }
-  // octave sum normalised by the sum of weights 0.5^o; base frequency f0
-  double octaveNoise(double x, double y, double z, double f0, int n) const
-  {
-    double sum = 0, wsum = 0, w = 1, f = f0;
-    for (int o = 0; o < n; ++o) {
-      sum += w * vnoise(x * f, y * f, z * f, o);
-      wsum += w;
-      w *= 0.5;
-      f *= 2.0;
-    }
-    return sum / wsum;
-  }
-  double gauss1(int k, int axis, double p) const
-  {
-    const double c = axis == 0 ? cx[k] : axis == 1 ? cy[k] : cz[k];
-    const double s = axis == 0 ? sx[k] : axis == 1 ? sy[k] : sz[k];
-    const double t = (p - c) / s;
-    return std::exp(-0.5 * t * t);
-  }
-  // unit-cube coordinates
-  double evalUnit(double x, double y, double z) const
-  {
-    if (kind == EXA_FIELD_CLOUD) return cloud(octaveNoise(x, y, z, 2.0, octaves));
-    double g = 0;
-    for (int k = 0; k < K; ++k) g += amp[k] * gauss1(k, 0, x) * gauss1(k, 1, y) * gauss1(k, 2, z);
-    return g + noiseAmp * octaveNoise(x, y, z, 4.0, octaves);
-  }
-  double cloud(double fbm) const
-  {
-    const double v = (std::exp(3.0 * fbm) - cloudLo) / (cloudHi - cloudLo);
-    return v < 0 ? 0 : (v > 1 ? 1 : v);
-  }
-};
+  for (int a = 0; a < 3; ++a)
+    for (int L = 0; L < (int)gtab[a].size() && L < kMaxLevels; ++L) v.gtab[a][L] = gtab[a][L].data();
+  return v;
+}
+
+double Field::evalUnit(double x, double y, double z) const
+{
+  const FieldView v = view();
+  if (kind == EXA_FIELD_CLOUD) return cloud_map(v, cloud_raw(v, x, y, z));
+  double g = 0;
+  for (int k = 0; k < K; ++k) g += amp[k] * gauss1(k, 0, x) * gauss1(k, 1, y) * gauss1(k, 2, z);
+  return g + noiseAmp * octave_noise(v, x, y, z, 4.0, octaves);
+}
+
+} // namespace exagen
+
+namespace {
 
 // ---------------------------------------------------------------- bitsets
 struct Bits {
@@ -194,31 +171,7 @@ struct LeafRef { int level; uint64_t lin; uint64_t id; };
 
 struct Elem { int type; uint32_t v[8]; };  // type 0 tet, 1 pyr, 2 wedge, 3 hex; v = leaf ids
 
-int numThreadsOf(const exa_gen_params *p)
-{
-#ifdef _OPENMP
-  return p->numThreads > 0 ? p->numThreads : omp_get_max_threads();
-#else
-  (void)p;
-  return 1;
-#endif
-}
-
-} // namespace
-
-struct exa_gen_result {
-  exa_gen_params params;
-  Field field;
-  std::vector<exa_vec4f> vertices;
-  std::vector<int32_t> indices;
-  std::vector<exa_gridlet> gridlets;
-  std::vector<float> gridletScalars;
-  std::vector<int32_t> amrCells;
-  std::vector<float> amrScalars;
-  exa_gen_stats stats;
-};
-
-namespace {
+using exagen::numThreadsOf;
 
 struct Builder {
   const exa_gen_params &P;
@@ -235,67 +188,42 @@ struct Builder {
       for (int a = 0; a < 3; ++a) lv[L].n[a] = (int64_t)p.rootDims[a] << (Lroot - L);
   }
 
-  double center(int L, int64_t i) const { return ((double)i + 0.5) * (double)(1ll << L); }
-  // per level and axis: exp(-0.5((c_i - c_k)/s_k)^2) * (amp_k on x), row i
-  std::vector<std::vector<double>> gtab[3];
+  double center(int L, int64_t i) const { return exagen::cell_center(L, i); }
+  FieldView fv{};  // the field as the evaluations read it (after set-up)
+
   void buildGaussTables()
   {
-    const Field &F = R.field;
-    for (int a = 0; a < 3; ++a) gtab[a].assign(lv.size(), {});
-    if (F.kind != EXA_FIELD_GAUSSIANS) return;
-    for (int L = 0; L <= Lroot; ++L)
-      for (int a = 0; a < 3; ++a) {
-        const int64_t n = lv[L].n[a];
-        auto &T = gtab[a][L];
-        T.resize((size_t)n * F.K);
+    Field &F = R.field;
+    for (int a = 0; a < 3; ++a) F.gtab[a].assign(lv.size(), {});
+    if (F.kind == EXA_FIELD_GAUSSIANS) {
+      for (int L = 0; L <= Lroot; ++L)
+        for (int a = 0; a < 3; ++a) {
+          const int64_t n = lv[L].n[a];
+          auto &T = F.gtab[a][L];
+          T.resize((size_t)n * F.K);
 #pragma omp parallel for schedule(static) num_threads(numThreadsOf(&P))
-        for (int64_t i = 0; i < n; ++i)
-          for (int k = 0; k < F.K; ++k)
-            T[(size_t)i * F.K + k] = F.gauss1(k, a, center(L, i) / F.extent[a]) * (a == 0 ? F.amp[k] : 1.0);
-      }
+          for (int64_t i = 0; i < n; ++i) F.gaussRow(a, L, i, &T[(size_t)i * F.K]);
+        }
+    }
+    fv = F.view();
   }
-  double evalCell(int L, int64_t i, int64_t j, int64_t k) const
-  {
-    const Field &F = R.field;
-    const double x = center(L, i) / F.extent[0], y = center(L, j) / F.extent[1], z = center(L, k) / F.extent[2];
-    if (F.kind != EXA_FIELD_GAUSSIANS) return F.evalUnit(x, y, z);
-    const double *gx = &gtab[0][L][(size_t)i * F.K];
-    const double *gy = &gtab[1][L][(size_t)j * F.K];
-    const double *gz = &gtab[2][L][(size_t)k * F.K];
-    double g = 0;
-    for (int q = 0; q < F.K; ++q) g += gx[q] * gy[q] * gz[q];
-    return g + F.noiseAmp * F.octaveNoise(x, y, z, 4.0, F.octaves);
-  }
+  double evalCell(int L, int64_t i, int64_t j, int64_t k) const { return exagen::eval_cell(fv, L, i, j, k); }
 
   void setupField()
   {
     Field &F = R.field;
-    F.kind = P.fieldKind;
-    F.seed = P.seed;
-    F.noiseAmp = P.noiseAmplitude;
-    F.octaves = P.noiseOctaves;
-    for (int a = 0; a < 3; ++a) F.extent[a] = (double)((int64_t)P.rootDims[a] << Lroot);
-    F.buildLattices(F.octaves, F.kind == EXA_FIELD_GAUSSIANS ? 4.0 : 2.0);
-    if (F.kind == EXA_FIELD_GAUSSIANS) {
-      Stream s(P.seed);
-      F.K = P.numGaussians;
-      for (int k = 0; k < F.K; ++k) {
-        F.cx.push_back(s.next01()); F.cy.push_back(s.next01()); F.cz.push_back(s.next01());
-        F.sx.push_back(s.uniform(0.03, 0.15)); F.sy.push_back(s.uniform(0.03, 0.15));
-        F.sz.push_back(s.uniform(0.03, 0.15));
-        F.amp.push_back(s.uniform(0.2, 1.0));
-      }
-    } else {
+    F.setup(P);
+    if (F.kind == EXA_FIELD_CLOUD) {
       // cloud: the mapping sends the requested fraction of root cells to 0
+      const FieldView v = F.view();
       Level &R0 = lv[Lroot];
       const uint64_t n = (uint64_t)R0.n[0] * R0.n[1] * R0.n[2];
       std::vector<double> raw(n);
-      F.cloudLo = 0.0; F.cloudHi = 1.0;
 #pragma omp parallel for schedule(static) num_threads(numThreadsOf(&P))
       for (int64_t c = 0; c < (int64_t)n; ++c) {
         const int64_t i = c % R0.n[0], j = (c / R0.n[0]) % R0.n[1], k = c / (R0.n[0] * R0.n[1]);
-        raw[c] = std::exp(3.0 * F.octaveNoise(center(Lroot, i) / F.extent[0], center(Lroot, j) / F.extent[1],
-                                              center(Lroot, k) / F.extent[2], 2.0, F.octaves));
+        raw[c] = exagen::cloud_raw(v, center(Lroot, i) / F.extent[0], center(Lroot, j) / F.extent[1],
+                                   center(Lroot, k) / F.extent[2]);
       }
       std::vector<double> sorted = raw;
       const size_t q = std::min(n - 1, (size_t)(P.cloudEmptyFraction * (double)n));
@@ -309,11 +237,7 @@ struct Builder {
 
   bool refineCrit(double v, int L, double maxAbs) const
   {
-    if (P.fieldKind == EXA_FIELD_GAUSSIANS) return std::fabs(v) > (double)P.refineThreshold * maxAbs;
-    // cloud: deeper levels need denser cloud (thresholds t, 2t, 4t, ...), so
-    // that with t well below 1/2^(levels-2) every level is populated
-    const int depth = Lroot - L;
-    return v > (double)P.refineThreshold * std::pow(2.0, depth);
+    return exagen::refine_crit(P.fieldKind, v, L, Lroot, (double)P.refineThreshold, maxAbs);
   }
 
   void buildTree()
@@ -835,10 +759,8 @@ void exa_gen_params_default(exa_gen_params *p)
 int exa_gen_run(const exa_gen_params *p, exa_gen_result **out)
 {
   try {
-    if (!p || !out) throw std::runtime_error("null argument");
-    if (p->numLevels < 1 || p->numLevels > 16) throw std::runtime_error("numLevels must be in [1,16]");
-    for (int a = 0; a < 3; ++a)
-      if (p->rootDims[a] < 1) throw std::runtime_error("rootDims must be positive");
+    if (!out) throw std::runtime_error("null argument");
+    exagen::checkParams(p);
     auto t0 = std::chrono::steady_clock::now();
     exa_gen_result *r = new exa_gen_result();
     r->params = *p;

@@ -68,6 +68,8 @@ def lib():
         L.exa_gen_params_default.argtypes = [C.POINTER(GenParams)]
         L.exa_gen_run.restype = C.c_int
         L.exa_gen_run.argtypes = [C.POINTER(GenParams), C.POINTER(vp)]
+        L.exa_gen_run_gpu.restype = C.c_int
+        L.exa_gen_run_gpu.argtypes = [C.POINTER(GenParams), C.c_int32, C.POINTER(vp)]
         L.exa_gen_free.argtypes = [vp]
         L.exa_gen_get_stats.argtypes = [vp, C.POINTER(GenStats)]
         for n in ("vertices", "indices", "gridlets", "gridlet_scalars", "amr_cells", "amr_scalars"):
@@ -116,13 +118,19 @@ def params(config="small", **overrides):
 
 
 class Dataset:
-    """Generated ExaStitch arrays (numpy copies) plus the analytic field."""
+    """Generated ExaStitch arrays (numpy copies) plus the analytic field.
+    device=None runs the CPU generator, device=k its GPU version on CUDA
+    device k (identical output)."""
 
-    def __init__(self, config="small", **overrides):
+    def __init__(self, config="small", device=None, **overrides):
         self.config = config
+        self.device = device
         self.params = params(config, **overrides)
         h = C.c_void_p()
-        rc = lib().exa_gen_run(C.byref(self.params), C.byref(h))
+        if device is None:
+            rc = lib().exa_gen_run(C.byref(self.params), C.byref(h))
+        else:
+            rc = lib().exa_gen_run_gpu(C.byref(self.params), int(device), C.byref(h))
         if rc != 0:
             raise RuntimeError("exa_gen_run: " + lib().exa_gen_last_error().decode())
         self._h = h
