@@ -147,15 +147,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_scene(a, rank):
-    """Dataset, model, sampler and launch parameters of the workload."""
-    from helpers import orbit_camera, ramp_tf, setup_render
+def make_scene(a, device):
+    """The workload's dataset, made by the GPU generator; returns it and the
+    generator record (wall seconds, per-stage seconds; the CPU generator's
+    wall time beside it unless the CPU baselines are off)."""
     from owlexastitcher_gb300 import datagen
-    from owlexastitcher_gb300 import exastitch as E
     t0 = time.time()
-    ds = datagen.Dataset(a.config)
-    gen_s = time.time() - t0
-    return ds, gen_s
+    ds = datagen.Dataset(a.config, device=device)
+    gen = {"gpu_seconds": time.time() - t0, "gpu_stage_seconds": ds.stats["stageSeconds"], "cpu_seconds": None}
+    if not a.no_cpu_baseline and not a.profile_only:
+        t0 = time.time()
+        cpu = datagen.Dataset(a.config)
+        gen["cpu_seconds"] = time.time() - t0
+        gen["cpu_stage_seconds"] = cpu.stats["stageSeconds"]
+        gen["identical"] = all(getattr(cpu, k).tobytes() == getattr(ds, k).tobytes() for k in (
+            "vertices", "indices", "gridlets", "gridlet_scalars", "amr_cells", "amr_scalars"))
+        del cpu
+    return ds, gen
 
 
 def run_ours(a):
@@ -175,7 +183,7 @@ def run_ours(a):
         if world > 1:
             dist.barrier()
 
-    ds, gen_s = make_scene(a, rank)
+    ds, gen = make_scene(a, local)
     ctx = E.Context(local)
     r = E.Renderer(ctx, E.ExaStitchModel.from_dataset(ctx, ds), NUM_MCS)
     lo, hi = r.model.cellBounds
@@ -338,7 +346,7 @@ def run_ours(a):
             "small_config": small,
             "dataset": {k: ds.stats[k] for k in ("numAmrCells", "numGridlets", "numGridletScalars", "numPyramids",
                                                   "numWedges", "numHexes", "numTets")} | {
-                "field_bytes": ds.field_bytes, "gen_seconds": gen_s},
+                "field_bytes": ds.field_bytes, "generator": gen},
             "step_ms": step_ms,
         }
         print(json.dumps(line), flush=True)

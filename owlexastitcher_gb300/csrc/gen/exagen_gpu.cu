@@ -130,6 +130,34 @@ __device__ __forceinline__ uint64_t leaf_id(const LevelD &l, uint64_t c)
   const uint64_t nwarps_ = (gridDim.x * (uint64_t)blockDim.x) / 32;                                   \
   for (uint64_t w = warp0_, c = w * 32 + lane; w < nwords_; w += nwarps_, c = w * 32 + lane)
 
+// Calls f(c, i, j, k) for every set bit c of a level's bit set.  A warp
+// loads 32 words at once (one per lane, coalesced) and then works through
+// the non-zero ones together, one lane per bit, so the mostly empty words of
+// the fine levels cost one load each.
+template <typename Fn>
+__device__ __forceinline__ void for_set_bits(const uint32_t *bits, const LevelD &l, Fn &&f)
+{
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+  const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) / 32;
+  for (uint64_t w0 = warp * 32; w0 < l.words; w0 += nwarps * 32) {
+    const uint64_t mw = w0 + lane;
+    const uint32_t mine = mw < l.words ? bits[mw] : 0u;
+    uint32_t nz = __ballot_sync(0xffffffffu, mine != 0u);
+    while (nz) {
+      const int src = __ffs(nz) - 1;
+      nz &= nz - 1;
+      const uint32_t word = __shfl_sync(0xffffffffu, mine, src);
+      if ((word >> lane) & 1u) {
+        const uint64_t c = (w0 + src) * 32 + lane;
+        int64_t i, j, k;
+        coords(l, c, i, j, k);
+        f(c, i, j, k);
+      }
+    }
+  }
+}
+
 // the cloud's raw root values exp(3 fBm), for its mapping range
 __global__ void k_cloud_raw(FieldView F, TreeD T, double *raw)
 {
@@ -175,22 +203,20 @@ __global__ void k_root_refine(TreeD T, const float *rootVal, int kind, double th
 }
 
 // level L < root: children of refined parents, refined where the field says
+// (the child level's bits start zeroed)
 __global__ void k_refine_level(FieldView F, TreeD T, int L, int kind, double thr, double maxAbs)
 {
   const LevelD &l = T.lv[L];
   const LevelD &p = T.lv[L + 1];
-  FOR_WORD_CELLS(l.cells, c, w, lane)
-  {
-    bool r = false;
-    if (c < l.cells) {
-      int64_t i, j, k;
-      coords(l, c, i, j, k);
-      if (bit(p.refined, lin(p, i >> 1, j >> 1, k >> 1)))
-        r = exagen::refine_crit(kind, exagen::eval_cell(F, L, i, j, k), L, T.Lroot, thr, maxAbs);
+  for_set_bits(p.refined, p, [&](uint64_t, int64_t pi, int64_t pj, int64_t pk) {
+    for (int d = 0; d < 8; ++d) {
+      const int64_t i = 2 * pi + (d & 1), j = 2 * pj + ((d >> 1) & 1), k = 2 * pk + (d >> 2);
+      if (exagen::refine_crit(kind, exagen::eval_cell(F, L, i, j, k), L, T.Lroot, thr, maxAbs)) {
+        const uint64_t c = lin(l, i, j, k);
+        atomicOr(l.refined + (c >> 5), 1u << (c & 31));
+      }
     }
-    const uint32_t b = __ballot_sync(0xffffffffu, r);
-    if (lane == 0) l.refined[w] = b;
-  }
+  });
 }
 
 // 2:1 balance: the parents of all same-level neighbours of a refined cell
@@ -242,6 +268,35 @@ __global__ void k_leaf_bits(TreeD T, int L)
   }
 }
 
+// the same, a word at a time, for levels whose rows are whole words
+// (n.x % 32 == 0): the 32 cells of a word have 16 parents that are 16
+// aligned bits of one parent word, each parent bit standing for two cells
+__global__ void k_leaf_words(TreeD T, int L)
+{
+  const LevelD &l = T.lv[L];
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < l.words;
+       w += gridDim.x * (uint64_t)blockDim.x) {
+    const uint32_t ref = L > 0 ? l.refined[w] : 0u;
+    uint32_t out;
+    if (L == T.Lroot) {
+      out = ~ref;
+    } else {
+      const LevelD &p = T.lv[L + 1];
+      int64_t i, j, k;
+      coords(l, w * 32, i, j, k);
+      const uint64_t pc = lin(p, i >> 1, j >> 1, k >> 1);
+      uint32_t x = (p.refined[pc >> 5] >> (pc & 31)) & 0xffffu;
+      // spread the 16 bits to the even positions, then double them
+      x = (x | (x << 8)) & 0x00ff00ffu;
+      x = (x | (x << 4)) & 0x0f0f0f0fu;
+      x = (x | (x << 2)) & 0x33333333u;
+      x = (x | (x << 1)) & 0x55555555u;
+      out = (x | (x << 1)) & ~ref;
+    }
+    l.leaf[w] = out;
+  }
+}
+
 // per-word popcounts scanned within blocks of kScanBlock words
 constexpr int kScanBlock = 1024;
 
@@ -267,11 +322,7 @@ __global__ void k_rank_add(uint32_t *rank, uint64_t words, const uint32_t *block
 __global__ void k_values(FieldView F, TreeD T, int L, float *value, int32_t *cells)
 {
   const LevelD &l = T.lv[L];
-  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < l.cells;
-       c += gridDim.x * (uint64_t)blockDim.x) {
-    if (!bit(l.leaf, c)) continue;
-    int64_t i, j, k;
-    coords(l, c, i, j, k);
+  for_set_bits(l.leaf, l, [&](uint64_t c, int64_t i, int64_t j, int64_t k) {
     const uint64_t id = leaf_id(l, c);
     value[id] = (float)exagen::eval_cell(F, L, i, j, k);
     int4 rec;
@@ -280,7 +331,7 @@ __global__ void k_values(FieldView F, TreeD T, int L, float *value, int32_t *cel
     rec.z = (int32_t)(k << L);
     rec.w = L;
     reinterpret_cast<int4 *>(cells)[id] = rec;
-  }
+  });
 }
 
 // ------------------------------------------------------------------ dual cells
@@ -478,17 +529,13 @@ __device__ void do_cell(const TreeD &T, int L, int64_t ci, int64_t cj, int64_t c
 __global__ void k_elem_count(TreeD T, int L, uint32_t *packed, unsigned long long *skipped)
 {
   const LevelD &l = T.lv[L];
-  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < l.cells;
-       c += gridDim.x * (uint64_t)blockDim.x) {
-    if (!bit(l.leaf, c)) continue;
-    int64_t i, j, k;
-    coords(l, c, i, j, k);
+  for_set_bits(l.leaf, l, [&](uint64_t c, int64_t i, int64_t j, int64_t k) {
     Emit E{};
     E.write = false;
     do_cell(T, L, i, j, k, E);
     packed[leaf_id(l, c)] = E.n[0] | (E.n[1] << 8) | (E.n[2] << 16) | (E.n[3] << 24);
     if (E.skipped) atomicAdd(skipped, (unsigned long long)E.skipped);
-  }
+  });
 }
 
 __global__ void k_flag_nonzero(const uint32_t *packed, uint64_t n, uint32_t *flag)
@@ -874,7 +921,7 @@ struct GpuBuilder {
       sync("root refine");
     }
     for (int L = Lroot - 1; L >= 1; --L) {
-      k_refine_level<<<blocksFor(T.lv[L].cells), kThreads, 0, s>>>(fv, T, L, P.fieldKind, thr, maxAbs);
+      k_refine_level<<<blocksFor(T.lv[L + 1].words), kThreads, 0, s>>>(fv, T, L, P.fieldKind, thr, maxAbs);
       launched("k_refine_level");
     }
     if (P.balance)
@@ -884,8 +931,13 @@ struct GpuBuilder {
       }
     uint64_t off = 0;
     for (int L = 0; L <= Lroot; ++L) {
-      k_leaf_bits<<<blocksFor(T.lv[L].cells), kThreads, 0, s>>>(T, L);
-      launched("k_leaf_bits");
+      if (T.lv[L].n[0] % 32 == 0) {
+        k_leaf_words<<<blocksFor(T.lv[L].words), kThreads, 0, s>>>(T, L);
+        launched("k_leaf_words");
+      } else {
+        k_leaf_bits<<<blocksFor(T.lv[L].cells), kThreads, 0, s>>>(T, L);
+        launched("k_leaf_bits");
+      }
       buildRank(L);
       T.lv[L].leafOffset = off;
       off += R.stats.numCellsPerLevel[L];
@@ -899,7 +951,7 @@ struct GpuBuilder {
     value.alloc(n);
     cells.alloc(n * 4);
     for (int L = 0; L <= T.Lroot; ++L) {
-      k_values<<<blocksFor(T.lv[L].cells), kThreads, 0, s>>>(fv, T, L, value.p, cells.p);
+      k_values<<<blocksFor(T.lv[L].words), kThreads, 0, s>>>(fv, T, L, value.p, cells.p);
       launched("k_values");
     }
     Dev<float> mm(2);
@@ -943,7 +995,7 @@ struct GpuBuilder {
     Dev<unsigned long long> skipped(1);
     skipped.zero(s);
     for (int L = 0; L <= T.Lroot; ++L) {
-      k_elem_count<<<blocksFor(T.lv[L].cells), kThreads, 0, s>>>(T, L, packed.p, skipped.p);
+      k_elem_count<<<blocksFor(T.lv[L].words), kThreads, 0, s>>>(T, L, packed.p, skipped.p);
       launched("k_elem_count");
     }
     // the leaves that emit elements, in leaf-id order
