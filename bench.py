@@ -660,6 +660,64 @@ def run_small_config(a, local, flush, cpu=True):
                       "majorant_build_32^3_ms": maj32, "majorant_build_128^3_ms": maj128,
                       "note": "oracle/oracle.c point location (uniform-grid accel) and majorant build"}
     ctx.close()
+    out["amrcell_sampler"] = run_amrcell_small(ds, local, P, flush, stream)
+    return out
+
+
+def run_amrcell_small(ds, local, P, flush, stream):
+    """The same two workloads through the AMR-cell comparison sampler (tent
+    basis over the small field's AMR cells): points/s and 256^2 x 1 spp
+    direct-lighting paths/s."""
+    import ctypes as C
+    import torch
+    from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import exastitch as E
+    ctx = E.Context(local)
+    model = E.AMRCellModel.from_dataset(ctx, ds)
+    model.setNumGridCells((32, 32, 32))
+    sampler = E.AMRCellSampler(ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sampler.build(model)
+    vr = model.valueRange
+    sampler.computeMaxOpacities(ramp_tf(), (np.float32(vr[0]), np.float32(vr[1])))
+    ctx.sync()
+    out = {"cells": len(ds.amr_cells), "build_32^3_ms": (time.perf_counter() - t0) * 1e3}
+    pd = torch.from_numpy(P).cuda()
+    res = torch.empty(len(P) * 3, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        sampler.sample_device(pd.data_ptr(), res.data_ptr(), len(P))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(7.0)
+    e0.record(stream)
+    for _ in range(10):
+        sampler.sample_device(pd.data_ptr(), res.data_ptr(), len(P))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["points_per_s"] = 10 * len(P) / (e0.elapsed_time(e1) / 1e3)
+    lo, hi = model.cellBounds
+    lp = E.new_launch_params()
+    sampler.setLPs(lp)
+    w = h = 256
+    setup_render(lp, orbit_camera(lo, hi, w, h), w, h, E.DIRECT_LIGHT_INTEGRATOR, 1, "directional", False)
+    fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+    acc = torch.zeros(w * h * 4, dtype=torch.float32, device="cuda")
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+    lp.ext.traceT = lp.ext.traceTr = None
+    for _ in range(3):
+        E._check(E.lib().exa_render(ctx.h, C.byref(lp), w, h))
+    ms = []
+    for _ in range(5):
+        flush.fill_(8.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        E._check(E.lib().exa_render(ctx.h, C.byref(lp), w, h))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    ctx.sync()
+    out["render_256_1spp_dl"] = {"paths_per_s": w * h / (statistics.median(ms) / 1e3), "ms": statistics.median(ms)}
+    ctx.close()
     return out
 
 

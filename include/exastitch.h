@@ -97,6 +97,11 @@ typedef struct {
   float       *gridletScalarBuffer;
 } exa_stitch_lp;
 
+/* sampler/AMRCellSampler.h:30-35: the AMR-cell sampler's handle. */
+typedef struct {
+  uint64_t     sampleBVH;
+} exa_amrcell_lp;
+
 #define EXA_CLIP_PLANES_MAX 1   /* common.h:36 */
 #define EXA_LIGHTS_MAX      4   /* common.h:37 */
 
@@ -141,10 +146,11 @@ typedef struct {
 } exa_lp_ext;
 
 /* LaunchParams.h:56-119, field order and types kept; the sampler union
- * holds only the ExaStitch member; transferFunc is the buffer variant
- * (values/numValues, LaunchParams.h:84-87). */
+ * holds the ExaStitch and the AMR-cell members (both start with sampleBVH);
+ * transferFunc is the buffer variant (values/numValues,
+ * LaunchParams.h:84-87). */
 typedef struct {
-  struct { exa_stitch_lp ess; } sampler;
+  union { exa_stitch_lp ess; exa_amrcell_lp acs; } sampler;
   uint32_t  *fbPointer;
   float     *fbDepth;
   exa_vec4f *accumBuffer;
@@ -206,6 +212,8 @@ typedef struct {
   uint64_t deviceFieldBytes;     /* field arrays resident in HBM           */
   uint64_t deviceAccelBytes;     /* point-location tables + element BVH     */
   uint64_t deviceMajorantBytes;  /* value ranges + max opacities            */
+  uint64_t amrCellBytes;         /* AMR-cell model: cells (AMRCellModel::memStats) */
+  uint64_t amrScalarBytes;       /* AMR-cell model: scalars                 */
 } exa_mem_stats;
 
 typedef struct exa_context exa_context;
@@ -290,6 +298,18 @@ typedef struct exa_amr_cell {
   int32_t level;
 } exa_amr_cell;
 int exa_read_cells(const char *cellsFile, exa_amr_cell *cells, uint64_t *numCells);
+/* AMRCellModel (model/AMRCellModel.h, AMRCellModel.cpp:24-67): the
+ * context's model becomes the AMR leaf cells with one scalar each (numScalars
+ * >= numCells; a cell's pos must be a multiple of its width 2^level, and no
+ * cell may repeat).  cellBounds is the union of the cells [pos, pos + 2^level],
+ * valueRange spans the non-NaN scalars of the cells.  exa_sampler_build then
+ * builds the AMRCellSampler (tent-basis reconstruction, the reference's
+ * comparison sampler; sampler/AMRCellSampler.*). */
+int exa_amrcell_model_create(exa_context *ctx, const exa_amr_cell *cells, uint64_t numCells, const float *scalars,
+                             uint64_t numScalars);
+/* AMRCellModel::load (AMRCellModel.cpp:24-67): '.cells' records and a raw
+ * float32 scalars file. */
+int exa_amrcell_model_load(exa_context *ctx, const char *cellsFile, const char *scalarsFile);
 
 /* Surface meshes (TriangleMesh.cpp:27-76; OWLRenderer.cpp:446-545).  A mesh
  * file is a sequence of meshes, each int32 numVerts, numVerts float3,
@@ -348,6 +368,9 @@ int exa_sampler_compute_max_opacities(exa_context *ctx,
 int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp);
 /* Sampler::className (sampler/ExaStitchSampler.h:59). */
 const char *exa_sampler_class_name(void);
+/* className() of the context's built sampler ("ExaStitchSampler" or
+ * "AMRCellSampler"), "" before exa_sampler_build. */
+const char *exa_sampler_get_class_name(exa_context *ctx);
 /* Grid::valueRanges / Grid::maxOpacities (Grid.h:70-73), copied to host
  * arrays of numMCs entries (either pointer may be NULL). */
 int exa_get_majorants(exa_context *ctx, exa_range1f *valueRanges,

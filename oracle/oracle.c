@@ -431,6 +431,14 @@ struct oc_field {
   exa_box3f gb; v3i gd; v3 cs;
   uint32_t *cellBegin; /* gd.x*gd.y*gd.z + 1 */
   int32_t *items;      /* >= 0: gridlet id; < 0: -(elem id) - 1 */
+  /* AMR cells (oc_field_set_amr): the field is their tent-basis
+   * reconstruction; cells are looked up by (level, z, y, x) keys sorted
+   * ascending, lattice boxes per level as the GPU builds them */
+  const int32_t *amrCells; uint64_t numAmr;
+  const float *amrScalars;
+  uint64_t *amrKeys; uint32_t *amrOrder;
+  int amrLevels;
+  int amrHas[16], amrLo[16][3], amrN[16][3];
   /* surface mesh, traced where lp->meshBVH != 0 */
   const exa_vec3f *meshVertices;
   const exa_vec3i *meshIndices;
@@ -545,9 +553,134 @@ oc_field *oc_field_create(const v4 *vertices, uint64_t numVertices,
 void oc_field_destroy(oc_field *f)
 {
   if (!f) return;
+  free(f->amrKeys);
+  free(f->amrOrder);
   free(f->cellBegin);
   free(f->items);
   free(f);
+}
+
+/* ------------------------------------------------ AMR cells
+ * AMRCellSampler (sampler/AMRCellSampler.h:66-84, programs/
+ * AMRCellSampler.cu:26-69): every cell whose support [pos - w/2,
+ * pos + w + w/2] holds the point (inclusive) adds its scalar with the tent
+ * weight prod(1 - |p - c| / (size / 2)); the sample is the weighted mean,
+ * absent when the weights sum to 0.  Summation order (OptiX's is
+ * unspecified): levels ascending, then cells in z, y, x order. */
+static uint64_t amr_key(int level, int64_t x, int64_t y, int64_t z)
+{
+  return ((uint64_t)level << 60) | ((uint64_t)z << 40) | ((uint64_t)y << 20) | (uint64_t)x;
+}
+
+static const uint64_t *g_sort_keys;
+static int amr_cmp(const void *a, const void *b)
+{
+  const uint64_t ka = g_sort_keys[*(const uint32_t *)a], kb = g_sort_keys[*(const uint32_t *)b];
+  return ka < kb ? -1 : (ka > kb ? 1 : 0);
+}
+
+int oc_field_set_amr(oc_field *f, const int32_t *cells, uint64_t n, const float *scalars, uint64_t numScalars)
+{
+  if (numScalars < n) return 1;
+  f->amrCells = cells;
+  f->numAmr = n;
+  f->amrScalars = scalars;
+  f->amrLevels = 0;
+  memset(f->amrHas, 0, sizeof(f->amrHas));
+  int hi[16][3];
+  for (uint64_t i = 0; i < n; ++i) {
+    const int L = cells[i * 4 + 3];
+    if (L < 0 || L > 15) return 2;
+    for (int a = 0; a < 3; ++a) {
+      const int q = cells[i * 4 + a] >> L;
+      if (cells[i * 4 + a] & ((1 << L) - 1)) return 3;
+      if (!f->amrHas[L] || q < f->amrLo[L][a]) f->amrLo[L][a] = q;
+      if (!f->amrHas[L] || q > hi[L][a]) hi[L][a] = q;
+    }
+    f->amrHas[L] = 1;
+    if (L + 1 > f->amrLevels) f->amrLevels = L + 1;
+  }
+  for (int L = 0; L < 16; ++L)
+    for (int a = 0; a < 3; ++a) f->amrN[L][a] = f->amrHas[L] ? hi[L][a] - f->amrLo[L][a] + 1 : 0;
+  free(f->amrKeys);
+  free(f->amrOrder);
+  f->amrKeys = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  f->amrOrder = (uint32_t *)malloc((n ? n : 1) * sizeof(uint32_t));
+  uint64_t *k = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  for (uint64_t i = 0; i < n; ++i) {
+    const int L = cells[i * 4 + 3];
+    const int64_t x = (cells[i * 4] >> L) - f->amrLo[L][0], y = (cells[i * 4 + 1] >> L) - f->amrLo[L][1],
+                  z = (cells[i * 4 + 2] >> L) - f->amrLo[L][2];
+    if (x >= (1 << 20) || y >= (1 << 20) || z >= (1 << 20)) { free(k); return 4; }
+    k[i] = amr_key(L, x, y, z);
+    f->amrOrder[i] = (uint32_t)i;
+  }
+  g_sort_keys = k;
+  qsort(f->amrOrder, n, sizeof(uint32_t), amr_cmp);
+  for (uint64_t i = 0; i < n; ++i) f->amrKeys[i] = k[f->amrOrder[i]];
+  free(k);
+  for (uint64_t i = 1; i < n; ++i)
+    if (f->amrKeys[i] == f->amrKeys[i - 1]) return 5; /* duplicate cell */
+  return 0;
+}
+
+/* model cell index of level-L lattice cell (x, y, z), or -1 */
+static int64_t amr_find(const oc_field *f, int L, int x, int y, int z)
+{
+  const int64_t lx = x - f->amrLo[L][0], ly = y - f->amrLo[L][1], lz = z - f->amrLo[L][2];
+  if (lx < 0 || ly < 0 || lz < 0 || lx >= f->amrN[L][0] || ly >= f->amrN[L][1] || lz >= f->amrN[L][2]) return -1;
+  const uint64_t key = amr_key(L, lx, ly, lz);
+  uint64_t lo = 0, hi = f->numAmr;
+  while (lo < hi) {
+    const uint64_t m = (lo + hi) / 2;
+    if (f->amrKeys[m] < key) lo = m + 1; else hi = m;
+  }
+  return lo < f->numAmr && f->amrKeys[lo] == key ? (int64_t)f->amrOrder[lo] : -1;
+}
+
+static exa_sample amr_sample(const oc_field *f, v3 pos)
+{
+  float sumW = 0.f, sumWV = 0.f;
+  const float P[3] = {pos.x, pos.y, pos.z};
+  for (int L = 0; L < f->amrLevels; ++L) {
+    if (!f->amrHas[L]) continue;
+    const int w = 1 << L;
+    const float half = (float)w * .5f;
+    int cand[3][3], nc[3] = {0, 0, 0};
+    int any = 1;
+    for (int a = 0; a < 3 && any; ++a) {
+      nc[a] = 0;
+      const float q = floorf(P[a] / (float)w);
+      if (!(q >= (float)f->amrLo[L][a] - 2.f && q <= (float)(f->amrLo[L][a] + f->amrN[L][a]) + 1.f)) { any = 0; break; }
+      const int b = (int)q;
+      for (int i = b - 1; i <= b + 1; ++i) {
+        if (i < f->amrLo[L][a] || i >= f->amrLo[L][a] + f->amrN[L][a]) continue;
+        const float lower = (float)(i * w) - half, upper = (float)(i * w + w) + half;
+        if (lower <= P[a] && P[a] <= upper) cand[a][nc[a]++] = i;
+      }
+      any = nc[a] > 0;
+    }
+    if (!any) continue;
+    for (int kz = 0; kz < nc[2]; ++kz)
+      for (int ky = 0; ky < nc[1]; ++ky)
+        for (int kx = 0; kx < nc[0]; ++kx) {
+          const int id[3] = {cand[0][kx], cand[1][ky], cand[2][kz]};
+          const int64_t c = amr_find(f, L, id[0], id[1], id[2]);
+          if (c < 0) continue;
+          float wgt = 1.f;
+          for (int a = 0; a < 3; ++a) {
+            const float lower = (float)(id[a] * w) - half, upper = (float)(id[a] * w + w) + half;
+            const float center = (lower + upper) / 2.f, size = upper - lower;
+            wgt = wgt * (1.f - fabsf(P[a] - center) / (size * .5f));
+          }
+          const float scalar = f->amrScalars[c];
+          sumW += wgt;
+          sumWV += scalar * wgt;
+        }
+  }
+  exa_sample s = {-1, -1, 0.f};
+  if (sumW > 0.f) { s.primID = 0; s.value = sumWV / sumW; }
+  return s;
 }
 
 void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices, const exa_vec3i *indices, uint64_t numTris)
@@ -592,6 +725,18 @@ void oc_field_bounds(const oc_field *f, exa_box3f *cb, exa_range1f *vr)
     b.lower = min3(b.lower, gb.lower); b.upper = max3(b.upper, gb.lower);
     b.lower = min3(b.lower, gb.upper); b.upper = max3(b.upper, gb.upper);
   }
+  /* AMRCellModel::load (AMRCellModel.cpp:56-64) */
+  for (uint64_t i = 0; i < f->numAmr; ++i) {
+    const int32_t *c = &f->amrCells[i * 4];
+    const int w = 1 << c[3];
+    const v3 lo = mk3((float)c[0], (float)c[1], (float)c[2]);
+    const v3 hi = mk3((float)(c[0] + w), (float)(c[1] + w), (float)(c[2] + w));
+    b.lower = min3(b.lower, lo); b.upper = max3(b.upper, lo);
+    b.lower = min3(b.lower, hi); b.upper = max3(b.upper, hi);
+    const float s = f->amrScalars[i];
+    if (s < r.lower) r.lower = s;
+    if (r.upper < s) r.upper = s;
+  }
   *cb = b;
   *vr = r;
 }
@@ -622,6 +767,7 @@ static inline int64_t lookup_cell(const oc_field *f, v3 p)
  * invisible when culling (programs/ExaStitchSampler.cu:35-41,81-83). */
 exa_sample oc_sample(const oc_field *f, v3 pos, int cull)
 {
+  if (f->numAmr) return amr_sample(f, pos);
   exa_sample s = {-1, -1, 0.f};
   const int64_t c = lookup_cell(f, pos);
   if (c < 0) return s;
@@ -698,6 +844,21 @@ void oc_build_majorants(const oc_field *f, v3i dims, exa_box3f wb, exa_range1f *
 {
   const size_t numMCs = (size_t)dims.x * dims.y * dims.z;
   for (size_t i = 0; i < numMCs; ++i) { vr[i].lower = 1e30f; vr[i].upper = -1e30f; } /* Grid.cu:61-70 */
+  /* AMR cells: the cell's support projected onto the grid (Grid.cu:248-285) */
+  for (uint64_t i = 0; i < f->numAmr; ++i) {
+    const int32_t *c = &f->amrCells[i * 4];
+    const float value = f->amrScalars[i];
+    if (isnan(value)) continue;
+    const int w = 1 << c[3];
+    const float half = (float)w * .5f;
+    const v3 lo3 = mk3((float)c[0] - half, (float)c[1] - half, (float)c[2] - half);
+    const v3 hi3 = mk3((float)(c[0] + w) + half, (float)(c[1] + w) + half, (float)(c[2] + w) + half);
+    const v3i lo = oc_project_on_grid(lo3, dims, wb), hi = oc_project_on_grid(hi3, dims, wb);
+    const exa_range1f r = {value, value};
+    for (int z = lo.z; z <= hi.z; ++z)
+      for (int y = lo.y; y <= hi.y; ++y)
+        for (int x = lo.x; x <= hi.x; ++x) { v3i id = {x, y, z}; update_mc(vr, id, dims, r); }
+  }
   /* elements: buildGrid<8> (Grid.cu:73-117) */
   for (uint64_t e = 0; e < f->numElems; ++e) {
     const int32_t *I = &f->indices[e * 8];

@@ -58,6 +58,12 @@ void oc_field_destroy(oc_field *f);
 /* per-primitive max opacities used for culling (NULL: no culling data) */
 void oc_field_set_prim_opacities(oc_field *f, const float *gridletMaxOps,
                                  const float *elemMaxOps);
+/* the field becomes the tent-basis reconstruction over AMR cells (16-byte
+ * records pos[3], level; one scalar each; arrays not copied).  0 on
+ * success; non-zero for fewer scalars than cells, a bad level, a position
+ * that is not a multiple of the cell width, or a duplicate cell. */
+int oc_field_set_amr(oc_field *f, const int32_t *cells, uint64_t numCells,
+                     const float *scalars, uint64_t numScalars);
 /* surface mesh the integrators trace where lp->meshBVH != 0 (arrays are
  * not copied: numTris int3 rows into the float3 vertices) */
 void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices,

@@ -91,6 +91,8 @@ def lib():
         L.oc_field_destroy.argtypes = [vp]
         L.oc_field_set_prim_opacities.argtypes = [vp, vp, vp]
         L.oc_field_set_mesh.argtypes = [vp, vp, vp, C.c_uint64]
+        L.oc_field_set_amr.restype = C.c_int
+        L.oc_field_set_amr.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]
         L.oc_field_bounds.argtypes = [vp, C.POINTER(Box3f), C.POINTER(Range1f)]
         L.oc_sample.restype = Sample
         L.oc_sample.argtypes = [vp, Vec3f, C.c_int]
@@ -169,6 +171,19 @@ class Field:
         self._gops = None if gridlet_ops is None else np.ascontiguousarray(gridlet_ops, dtype=np.float32)
         self._eops = None if elem_ops is None else np.ascontiguousarray(elem_ops, dtype=np.float32)
         lib().oc_field_set_prim_opacities(self.h, _ptr(self._gops), _ptr(self._eops))
+
+    @classmethod
+    def amr(cls, cells, scalars):
+        """a field of AMR cells (int32 [n, 4]: pos, level) with their scalars,
+        reconstructed by the AMR-cell sampler's tent basis"""
+        f = cls(np.zeros((0, 4), np.float32), np.zeros((0, 8), np.int32), np.zeros(0, GRIDLET_DTYPE),
+                np.zeros(0, np.float32))
+        f._cells = np.ascontiguousarray(cells, dtype=np.int32).reshape(-1, 4)
+        f._cscal = np.ascontiguousarray(scalars, dtype=np.float32)
+        rc = lib().oc_field_set_amr(f.h, _ptr(f._cells), len(f._cells), _ptr(f._cscal), len(f._cscal))
+        if rc:
+            raise ValueError(f"bad AMR cells ({rc})")
+        return f
 
     def set_mesh(self, vertices, indices):
         """surface mesh: float3 vertices, int3 triangles (kept alive here)"""

@@ -55,6 +55,24 @@ struct ElemOccupancy {
   const uint32_t *bits;
 };
 
+// AMR cells (the comparison sampler of sampler/AMRCellSampler.h): per level
+// a dense box of the level's cell lattice with one existence bit per cell,
+// the exclusive prefix popcount per 32-bit word, and the model index of
+// each present cell in lattice order (x fastest)
+struct AmrLevel {
+  int lo[3];               // first lattice index per axis (cell pos / 2^level)
+  int n[3];                // lattice cells per axis; 0: no cells on this level
+  const uint32_t *bits;
+  const uint32_t *rank;
+  const int32_t *cell;     // rank -> model cell index
+};
+
+struct AmrCellView {
+  int numLevels;           // highest level present + 1
+  const float *scalars;    // per model cell
+  AmrLevel lv[kMaxLevels];
+};
+
 struct AccelView {
   const exa_gridlet *gridlets;
   const float *scalars;
@@ -69,6 +87,7 @@ struct AccelView {
   int tablesSorted;             // 1: tables in ascending gridlet-index order
   ElemOccupancy occ;
   GridletTable tables[kMaxLevels];
+  const AmrCellView *amr;       // non-null: the AMR-cell sampler (no gridlets, no elements)
 };
 
 EXA_HD int occ_coord(float p, float origin, float cs, int n)
@@ -213,8 +232,74 @@ static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, b
 }
 
 // sample() (sampler/ExaStitchSampler.h:128-140); sets EXA_DEVERR bits in err
+// AMRCellSampler's sample() (sampler/AMRCellSampler.h:66-84) with the
+// intersection program AMRCellGeomIsect (programs/AMRCellSampler.cu:43-69):
+// every cell whose support -- its box grown by half a cell on each side --
+// contains pos (inclusive) adds its scalar with the tent weight
+// prod(1 - |p - c| / (size / 2)); the sample is the weighted mean, absent
+// (primID -1) when the weights sum to 0.  The reference sums in OptiX's
+// traversal order; here the order is fixed: levels ascending, then cells in
+// z, y, x order.  The candidates per level are the 3 lattice cells per axis
+// around floor(p / w), which contain every cell whose support can hold p.
+static __device__ __noinline__ exa_sample amr_sample(const AmrCellView &V, V3 pos)
+{
+  float sumW = 0.f, sumWV = 0.f;
+  const float P[3] = {pos.x, pos.y, pos.z};
+  for (int L = 0; L < V.numLevels; ++L) {
+    const AmrLevel &l = V.lv[L];
+    if (l.n[0] <= 0) continue;
+    const int w = 1 << L;
+    const float half = (float)w * .5f;
+    int cand[3][3], nc[3];
+    bool any = true;
+    for (int a = 0; a < 3 && any; ++a) {
+      nc[a] = 0;
+      const float q = floorf(P[a] / (float)w);
+      // outside the level's lattice (with a margin of 2 cells): nothing here
+      if (!(q >= (float)l.lo[a] - 2.f && q <= (float)(l.lo[a] + l.n[a]) + 1.f)) { any = false; break; }
+      const int b = (int)q;
+      for (int i = b - 1; i <= b + 1; ++i) {
+        if (i < l.lo[a] || i >= l.lo[a] + l.n[a]) continue;
+        const float lower = (float)(i * w) - half, upper = (float)(i * w + w) + half;
+        if (lower <= P[a] && P[a] <= upper) cand[a][nc[a]++] = i;
+      }
+      any = nc[a] > 0;
+    }
+    if (!any) continue;
+    for (int kz = 0; kz < nc[2]; ++kz)
+      for (int ky = 0; ky < nc[1]; ++ky)
+        for (int kx = 0; kx < nc[0]; ++kx) {
+          const int i = cand[0][kx], j = cand[1][ky], k = cand[2][kz];
+          const size_t c = ((size_t)(k - l.lo[2]) * l.n[1] + (j - l.lo[1])) * l.n[0] + (i - l.lo[0]);
+          const uint32_t word = __ldg(l.bits + (c >> 5));
+          if (!((word >> (c & 31)) & 1u)) continue;
+          const int cellIdx = __ldg(l.cell + __ldg(l.rank + (c >> 5)) + __popc(word & ((1u << (c & 31)) - 1u)));
+          const int id[3] = {i, j, k};
+          float wgt = 1.f;
+          for (int a = 0; a < 3; ++a) {
+            const float lower = (float)(id[a] * w) - half, upper = (float)(id[a] * w + w) + half;
+            const float center = (lower + upper) / 2.f, size = upper - lower;
+            wgt = wgt * (1.f - fabsf(P[a] - center) / (size * .5f));
+          }
+          const float scalar = __ldg(V.scalars + cellIdx);
+          sumW += wgt;
+          sumWV += scalar * wgt;
+        }
+  }
+  exa_sample s;
+  s.primID = -1;
+  s.cellID = -1;
+  s.value = 0.f;
+  if (sumW > 0.f) {
+    s.primID = 0;
+    s.value = sumWV / sumW;
+  }
+  return s;
+}
+
 EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
 {
+  if (A.amr) return amr_sample(*A.amr, pos);
   exa_sample s;
   s.primID = -1;
   s.cellID = -1;

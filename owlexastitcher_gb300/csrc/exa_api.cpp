@@ -145,6 +145,11 @@ void ExaStitchModel::memStats(size_t &elemVertexBytes, size_t &elemIndexBytes, s
 }
 
 // ================================================================ sampler
+size_t ExaStitchSampler::fieldBytes() const
+{
+  return gridletBuffer.bytes() + gridletScalarBuffer.bytes() + vertexBuffer.bytes() + indexBuffer.bytes();
+}
+
 size_t ExaStitchSampler::accelBytes() const
 {
   size_t b = bvhNodes.bytes() + bvhParents.bytes() + bvhLeafElem.bytes() + occBits.bytes();
@@ -436,6 +441,173 @@ void ExaStitchSampler::setLPs(exa_launch_params &lp)
   lp.sampler.ess.gridletScalarBuffer = gridletScalarBuffer.ptr;
 }
 
+// ================================================================ AMR cells
+// model/AMRCellModel.cpp:56-64 (bounds and value range of the loaded cells)
+void AMRCellModel::assign(const exa_amr_cell *c, size_t nc, const float *s, size_t ns)
+{
+  if (ns < nc) throw Error(EXA_ERR_INVALID, "fewer scalars than AMR cells");
+  cells.assign(c, c + nc);
+  scalars.assign(s, s + ns);
+  exa_box3f b;
+  b.lower = {INFINITY, INFINITY, INFINITY};
+  b.upper = {-INFINITY, -INFINITY, -INFINITY};
+  exa_range1f r{1e30f, -1e30f};
+  for (size_t i = 0; i < nc; ++i) {
+    const exa_amr_cell &a = cells[i];
+    if (a.level < 0 || a.level > 30) throw Error(EXA_ERR_INVALID, "AMR cell level out of range");
+    const int64_t w = 1ll << a.level;
+    const int64_t p[3] = {a.pos.x, a.pos.y, a.pos.z};
+    for (int k = 0; k < 3; ++k) {
+      if (p[k] % w != 0) throw Error(EXA_ERR_INVALID, "AMR cell position is not a multiple of its width");
+      if (p[k] + w > 0x7fffffffll) throw Error(EXA_ERR_INVALID, "AMR cell position out of range");
+    }
+    const float lo[3] = {(float)a.pos.x, (float)a.pos.y, (float)a.pos.z};
+    const float hi[3] = {(float)(a.pos.x + (int32_t)w), (float)(a.pos.y + (int32_t)w), (float)(a.pos.z + (int32_t)w)};
+    b.lower = {std::min(b.lower.x, lo[0]), std::min(b.lower.y, lo[1]), std::min(b.lower.z, lo[2])};
+    b.upper = {std::max(b.upper.x, hi[0]), std::max(b.upper.y, hi[1]), std::max(b.upper.z, hi[2])};
+    const float v = scalars[i];
+    if (!std::isnan(v)) {
+      r.lower = std::min(r.lower, v);
+      r.upper = std::max(r.upper, v);
+    }
+  }
+  cellBounds = b;
+  valueRange = r;
+}
+
+void AMRCellModel::memStats(size_t &cellsBytes, size_t &scalarsBytes) const
+{
+  cellsBytes = cells.size() * sizeof(exa_amr_cell);
+  scalarsBytes = cells.empty() ? 0 : scalars.size() * sizeof(float);
+}
+
+size_t AMRCellSampler::fieldBytes() const { return cellBuffer.bytes() + scalarBuffer.bytes(); }
+
+size_t AMRCellSampler::accelBytes() const
+{
+  size_t b = deviceView.bytes();
+  for (auto &x : levelBits) b += x.bytes();
+  for (auto &x : levelRank) b += x.bytes();
+  for (auto &x : levelCell) b += x.bytes();
+  return b;
+}
+
+// sampler/AMRCellSampler.cpp:23-108: the cells on the device, their point
+// location (dense per-level lattices instead of the OptiX user-geometry
+// BVH) and the majorant grid over cellBounds (Grid::build, Grid.cu:314-364)
+bool AMRCellSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
+{
+  if (!mod) return false;
+  model = std::dynamic_pointer_cast<AMRCellModel>(mod);
+  if (!model || model->cells.empty()) return false;
+  if (!model->grid || model->grid->dims.x == 0) return false;
+  const size_t n = model->cells.size();
+  cellBuffer.upload(model->cells.data(), n, s);
+  scalarBuffer.upload(model->scalars.data(), model->scalars.size(), s);
+  // per-level lattice boxes (host pass over the cells)
+  int lo[kMaxLevels][3], hi[kMaxLevels][3];
+  bool has[kMaxLevels] = {};
+  int maxLevel = 0;
+  for (const exa_amr_cell &c : model->cells) {
+    if (c.level >= kMaxLevels) throw Error(EXA_ERR_INVALID, "AMR cell level above 15");
+    const int L = c.level;
+    const int q[3] = {c.pos.x >> L, c.pos.y >> L, c.pos.z >> L};
+    for (int a = 0; a < 3; ++a) {
+      lo[L][a] = has[L] ? std::min(lo[L][a], q[a]) : q[a];
+      hi[L][a] = has[L] ? std::max(hi[L][a], q[a]) : q[a];
+    }
+    has[L] = true;
+    maxLevel = std::max(maxLevel, L);
+  }
+  std::memset(&view, 0, sizeof(view));
+  view.numLevels = maxLevel + 1;
+  view.scalars = scalarBuffer.ptr;
+  levelBits.clear();
+  levelRank.clear();
+  levelCell.clear();
+  levelBits.resize(view.numLevels);
+  levelRank.resize(view.numLevels);
+  levelCell.resize(view.numLevels);
+  DBuf<unsigned> dup;
+  dup.alloc(1);
+  cudaCheck(cudaMemsetAsync(dup.ptr, 0, sizeof(unsigned), s), "memset");
+  uint64_t totalBits = 0;
+  for (int L = 0; L < view.numLevels; ++L) {
+    if (!has[L]) continue;
+    int nl[3];
+    uint64_t bits = 1;
+    for (int a = 0; a < 3; ++a) {
+      nl[a] = hi[L][a] - lo[L][a] + 1;
+      bits *= (uint64_t)nl[a];
+    }
+    totalBits += bits;
+    if (totalBits > (1ull << 37))
+      throw Error(EXA_ERR_INVALID, "AMR cells too sparse for the dense per-level lattices");
+    const size_t words = (size_t)((bits + 31) / 32);
+    levelBits[L].alloc(words);
+    levelRank[L].alloc(words);
+    cudaCheck(cudaMemsetAsync(levelBits[L].ptr, 0, levelBits[L].bytes(), s), "memset bits");
+    launchAmrLevelBits(cellBuffer.ptr, n, L, lo[L], nl, levelBits[L].ptr, dup.ptr, s);
+    launchAmrLevelRank(levelBits[L].ptr, words, levelRank[L].ptr, s);
+    size_t count = 0;
+    for (const exa_amr_cell &c : model->cells) count += c.level == L;
+    levelCell[L].alloc(count);
+    launchAmrLevelCells(cellBuffer.ptr, n, L, lo[L], nl, levelBits[L].ptr, levelRank[L].ptr, levelCell[L].ptr, s);
+    AmrLevel &V = view.lv[L];
+    for (int a = 0; a < 3; ++a) {
+      V.lo[a] = lo[L][a];
+      V.n[a] = nl[a];
+    }
+    V.bits = levelBits[L].ptr;
+    V.rank = levelRank[L].ptr;
+    V.cell = levelCell[L].ptr;
+  }
+  unsigned dupHost = 0;
+  cudaCheck(cudaMemcpyAsync(&dupHost, dup.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "dup flag");
+  cudaCheck(cudaStreamSynchronize(s), "amr lattices");
+  if (dupHost) throw Error(EXA_ERR_INVALID, "duplicate AMR cell");
+  deviceView.upload(&view, 1, s);
+  std::memset(&accel, 0, sizeof(accel));
+  accel.amr = deviceView.ptr;
+  // the majorant grid over cellBounds (Grid.cu:314-364)
+  Grid &g = *model->grid;
+  g.worldBounds = model->cellBounds;
+  const size_t numMCs = (size_t)g.dims.x * g.dims.y * g.dims.z;
+  g.valueRanges.alloc(numMCs);
+  g.maxOpacities.alloc(numMCs);
+  cudaCheck(cudaMemsetAsync(g.maxOpacities.ptr, 0, g.maxOpacities.bytes(), s), "memset maxOpacities");
+  launchInitRanges(g.valueRanges.ptr, numMCs, s);
+  launchAmrCellMajorants(cellBuffer.ptr, scalarBuffer.ptr, n, g.dims, g.worldBounds, g.valueRanges.ptr, s);
+  g.deviceTraversable.dims = g.dims;
+  g.deviceTraversable.bounds = g.worldBounds;
+  deviceAccel.alloc(1);
+  cudaCheck(cudaMemcpyAsync(deviceAccel.ptr, &accel, sizeof(accel), cudaMemcpyHostToDevice, s), "accel handle");
+  cudaCheck(cudaStreamSynchronize(s), "sampler build");
+  majorantAccel.grid = model->grid;
+  maxOpacities = g.maxOpacities.ptr;
+  hasTF = false;
+  return true;
+}
+
+// AMRCellSampler.cpp:112-118 (Grid::computeMaxOpacities)
+void AMRCellSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors, exa_range1f xf, cudaStream_t s)
+{
+  if (!model || !model->grid || model->grid->dims.x == 0) return;
+  if (numColors <= 0) throw Error(EXA_ERR_INVALID, "empty color map");
+  colorMap.upload(reinterpret_cast<const float4 *>(cmap), (size_t)numColors, s);
+  Grid &g = *model->grid;
+  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, g.maxOpacities.ptr, s);
+  cudaCheck(cudaStreamSynchronize(s), "computeMaxOpacities");
+  hasTF = true;
+}
+
+// AMRCellSampler.cpp:133-140
+void AMRCellSampler::setLPs(exa_launch_params &lp)
+{
+  std::memset(&lp.sampler, 0, sizeof(lp.sampler));
+  lp.sampler.acs.sampleBVH = (uint64_t)(uintptr_t)deviceAccel.ptr;
+}
+
 } // namespace exa
 
 // ================================================================ C ABI
@@ -445,8 +617,8 @@ struct exa_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool ownStream = false;
-  std::shared_ptr<ExaStitchModel> model;
-  std::shared_ptr<ExaStitchSampler> sampler;
+  std::shared_ptr<Model> model;
+  std::shared_ptr<Sampler> sampler;
   exa_range1f xfRange{0.f, 1.f};
   int numColors = 0;
   DBuf<uint32_t> errors;
@@ -532,6 +704,21 @@ void need(bool c, int code, const char *msg)
 }
 
 void setDevice(exa_context *ctx) { cudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+
+// the context's model / sampler where a call needs the ExaStitch kind
+ExaStitchModel &esModel(exa_context *ctx)
+{
+  auto *m = dynamic_cast<ExaStitchModel *>(ctx->model.get());
+  need(m != nullptr, EXA_ERR_STATE, "this call needs an ExaStitch model");
+  return *m;
+}
+
+ExaStitchSampler &esSampler(exa_context *ctx)
+{
+  auto *s = dynamic_cast<ExaStitchSampler *>(ctx->sampler.get());
+  need(s != nullptr, EXA_ERR_STATE, "this call needs an ExaStitch sampler");
+  return *s;
+}
 } // namespace
 
 namespace {
@@ -561,6 +748,9 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    // the AMR-cell sampler renders shade mode default (renderFrame_AMRCellSampler, deviceCode.cu:1360-1364)
+    need(ctx->sampler->accel.amr == nullptr || (lp->shadeMode == EXA_SHADE_MODE_DEFAULT && !learned),
+         EXA_ERR_INVALID, "the AMR-cell sampler renders shade mode default with the exact field only");
     setDevice(ctx);
     const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
     if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
@@ -631,6 +821,12 @@ uint64_t exa_abi_sizeof(int32_t which)
 const char *exa_last_error(void) { return g_lastError.c_str(); }
 
 const char *exa_sampler_class_name(void) { return "ExaStitchSampler"; }
+
+const char *exa_sampler_get_class_name(exa_context *ctx)
+{
+  if (!ctx || !ctx->sampler) return "";
+  return dynamic_cast<AMRCellSampler *>(ctx->sampler.get()) ? "AMRCellSampler" : "ExaStitchSampler";
+}
 
 int exa_context_create(exa_context **out, int device, uint64_t stream)
 {
@@ -715,6 +911,21 @@ int exa_model_create(exa_context *ctx, const exa_vec4f *vertices, uint64_t numVe
          EXA_ERR_INVALID, "array too large for 32-bit indices");
     auto m = std::make_shared<ExaStitchModel>();
     m->assign(vertices, numVertices, indices, numElems, gridlets, numGridlets, gridletScalars, numGridletScalars);
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+int exa_amrcell_model_create(exa_context *ctx, const exa_amr_cell *cells, uint64_t numCells, const float *scalars,
+                             uint64_t numScalars)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    need(numCells == 0 || cells, EXA_ERR_INVALID, "cells is null");
+    need(numScalars == 0 || scalars, EXA_ERR_INVALID, "scalars is null");
+    need(numCells < 0x7fffffffull, EXA_ERR_INVALID, "array too large for 32-bit indices");
+    auto m = std::make_shared<AMRCellModel>();
+    m->assign(cells, numCells, scalars, numScalars);
     ctx->model = m;
     ctx->sampler.reset();
   });
@@ -807,6 +1018,26 @@ int exa_model_load(exa_context *ctx, const char *gridsFile, const char *scalarsF
     need(gl.size() < 0x7fffffffull && vals.size() <= 0xffffffffull, EXA_ERR_INVALID, "model too large");
     auto m = std::make_shared<ExaStitchModel>();
     m->assign(nullptr, 0, nullptr, 0, gl.data(), gl.size(), vals.data(), vals.size());
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+// AMRCellModel::load (AMRCellModel.cpp:24-67): a missing scalars file
+// leaves the model without scalars (the build then fails)
+int exa_amrcell_model_load(exa_context *ctx, const char *cellsFile, const char *scalarsFile)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    const std::vector<char> c = readFile(cellsFile, true);
+    const std::vector<char> v = readFile(scalarsFile, false);
+    std::vector<exa_amr_cell> cells(c.size() / sizeof(exa_amr_cell));
+    std::vector<float> vals(v.size() / sizeof(float));
+    if (!cells.empty()) std::memcpy(cells.data(), c.data(), cells.size() * sizeof(exa_amr_cell));
+    if (!vals.empty()) std::memcpy(vals.data(), v.data(), vals.size() * sizeof(float));
+    need(cells.size() < 0x7fffffffull, EXA_ERR_INVALID, "model too large");
+    auto m = std::make_shared<AMRCellModel>();
+    m->assign(cells.data(), cells.size(), vals.data(), vals.size());
     ctx->model = m;
     ctx->sampler.reset();
   });
@@ -999,22 +1230,29 @@ int exa_model_mem_stats(exa_context *ctx, exa_mem_stats *out)
 {
   return guarded([&] {
     need(ctx && ctx->model && out, EXA_ERR_STATE, "no model");
-    size_t a, b, c, d, e;
-    ctx->model->memStats(a, b, c, d, e);
     std::memset(out, 0, sizeof(*out));
-    out->elemVertexBytes = a;
-    out->elemIndexBytes = b;
-    out->gridletBytes = c;
-    out->emptyScalarsBytes = d;
-    out->nonEmptyScalarsBytes = e;
+    if (auto *em = dynamic_cast<ExaStitchModel *>(ctx->model.get())) {
+      size_t a, b, c, d, e;
+      em->memStats(a, b, c, d, e);
+      out->elemVertexBytes = a;
+      out->elemIndexBytes = b;
+      out->gridletBytes = c;
+      out->emptyScalarsBytes = d;
+      out->nonEmptyScalarsBytes = e;
+    } else if (auto *am = dynamic_cast<AMRCellModel *>(ctx->model.get())) {
+      size_t a, b;
+      am->memStats(a, b);
+      out->amrCellBytes = a;
+      out->amrScalarBytes = b;
+    }
     if (auto &S = ctx->sampler) {
-      out->deviceFieldBytes = S->gridletBuffer.bytes() + S->gridletScalarBuffer.bytes() + S->vertexBuffer.bytes() +
-                              S->indexBuffer.bytes();
+      out->deviceFieldBytes = S->fieldBytes();
       out->deviceAccelBytes = S->accelBytes();
       const auto &g = *ctx->model->grid;
-      out->deviceMajorantBytes = g.valueRanges.bytes() + g.maxOpacities.bytes() + S->gridletValueRanges.bytes() +
-                                 S->gridletMaxOpacities.bytes() + S->elemValueRanges.bytes() +
-                                 S->umeshMaxOpacities.bytes();
+      out->deviceMajorantBytes = g.valueRanges.bytes() + g.maxOpacities.bytes();
+      if (auto *es = dynamic_cast<ExaStitchSampler *>(S.get()))
+        out->deviceMajorantBytes += es->gridletValueRanges.bytes() + es->gridletMaxOpacities.bytes() +
+                                    es->elemValueRanges.bytes() + es->umeshMaxOpacities.bytes();
     }
   });
 }
@@ -1025,8 +1263,13 @@ int exa_sampler_build(exa_context *ctx)
     need(ctx && ctx->model, EXA_ERR_STATE, "no model");
     need(ctx->model->grid != nullptr, EXA_ERR_STATE, "numGridCells not set");
     setDevice(ctx);
-    auto s = std::make_shared<ExaStitchSampler>();
-    if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, "ExaStitchSampler::build failed");
+    // the sampler that goes with the model (OWLRenderer.cpp:150-200)
+    std::shared_ptr<Sampler> s;
+    if (dynamic_cast<AMRCellModel *>(ctx->model.get()))
+      s = std::make_shared<AMRCellSampler>();
+    else
+      s = std::make_shared<ExaStitchSampler>();
+    if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, s->className() + "::build failed");
     ctx->sampler = s;
   });
 }
@@ -1097,7 +1340,7 @@ int exa_get_prim_majorants(exa_context *ctx, exa_range1f *gridletRanges, float *
   return guarded([&] {
     need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
     setDevice(ctx);
-    auto &S = *ctx->sampler;
+    auto &S = esSampler(ctx);
     if (gridletRanges && S.gridletValueRanges.count)
       cudaCheck(cudaMemcpyAsync(gridletRanges, S.gridletValueRanges.ptr, S.gridletValueRanges.bytes(),
                                 cudaMemcpyDeviceToHost, ctx->stream), "copy");
@@ -1222,9 +1465,9 @@ int exa_surrogate_create(exa_context *ctx, const exa_surrogate_params *p)
     c.lrFinal = p->learningRateFinal;
     c.seed = p->seed;
     auto S = std::make_unique<Surrogate>();
-    S->configure(c, *ctx->model);
+    S->configure(c, esModel(ctx));
     S->allocate(ctx->stream);
-    S->generateSamples(*ctx->sampler, ctx->stream);
+    S->generateSamples(esSampler(ctx), ctx->stream);
     ctx->surrogate = std::move(S);
   });
 }
@@ -1250,7 +1493,7 @@ int exa_surrogate_evaluate(exa_context *ctx, float tolerance, uint64_t pointsTar
     setDevice(ctx);
     Surrogate &S = *ctx->surrogate;
     const Grid &g = *ctx->model->grid;
-    S.evaluate(*ctx->sampler, g, (double)tolerance, (size_t)std::max<uint64_t>(pointsTarget, 1), ctx->stream);
+    S.evaluate(esSampler(ctx), g, (double)tolerance, (size_t)std::max<uint64_t>(pointsTarget, 1), ctx->stream);
     S.computeMajorants(ctx->sampler->colorMap.ptr, ctx->numColors, ctx->xfRange, ctx->stream);
     cudaCheck(cudaStreamSynchronize(ctx->stream), "surrogate majorants");
     ctx->surrogateTol = tolerance;
@@ -1263,7 +1506,7 @@ namespace {
 // structures
 size_t fallbackBytes(exa_context *ctx)
 {
-  const ExaStitchModel &m = *ctx->model;
+  const ExaStitchModel &m = esModel(ctx);
   const Grid &g = *m.grid;
   const size_t nmc = (size_t)g.dims.x * g.dims.y * g.dims.z;
   std::vector<uint8_t> mode(nmc);
@@ -1333,7 +1576,7 @@ int exa_surrogate_get_stats(exa_context *ctx, exa_surrogate_stats *out)
     out->tableBytes = S.table16.bytes();
     out->weightBytes = S.wbf.bytes();
     out->inferenceBytes = S.inferenceBytes();
-    const ExaStitchSampler &sm = *ctx->sampler;
+    const ExaStitchSampler &sm = esSampler(ctx);
     out->fieldBytes = sm.gridletBuffer.bytes() + sm.gridletScalarBuffer.bytes() + sm.vertexBuffer.bytes() +
                       sm.indexBuffer.bytes() + sm.accelBytes();
     out->fallbackFieldBytes = S.evaluated ? fallbackBytes(ctx) : out->fieldBytes;
@@ -1429,8 +1672,8 @@ BatchState &batchOf(exa_context *ctx)
 // every transfer function's max opacities on it
 void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
 {
-  const ExaStitchSampler &S = *ctx->sampler;
-  const ExaStitchModel &m = *ctx->model;
+  const ExaStitchSampler &S = esSampler(ctx);
+  const ExaStitchModel &m = esModel(ctx);
   const size_t n = (size_t)B.dims.x * B.dims.y * B.dims.z;
   B.ranges.alloc(n);
   launchInitRanges(B.ranges.ptr, n, ctx->stream);
@@ -1455,7 +1698,7 @@ void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
 // computeMaxOpacities for each one, into the batch's own buffers)
 void rebuildBatchCulling(exa_context *ctx, BatchState &B)
 {
-  ExaStitchSampler &S = *ctx->sampler;
+  ExaStitchSampler &S = esSampler(ctx);
   const size_t ng = S.gridletValueRanges.count, ne = (size_t)S.accel.numElems;
   const size_t nt = B.tfColors.size();
   B.gOps.clear();

@@ -2,7 +2,9 @@
 // (Grid.cu:61-246), per-primitive value ranges and max opacities
 // (sampler/ExaStitchSampler.cu:27-227, Grid.cu:687-719) and the GPU linear
 // BVH over stitching elements that replaces the OptiX BLAS build.
+#include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "exa_host.h"
 
@@ -177,6 +179,128 @@ void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa
   if (!ne) return;
   k_elem_majorants<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, ne, dims, wb, mcRanges, elemRanges);
   cudaCheck(cudaGetLastError(), "k_elem_majorants");
+}
+
+// Grid.cu:248-285 (the AMR-cell overload of buildGrid): a cell's support
+// [pos - w/2, pos + w + w/2] projected onto the grid; NaN values add nothing
+__global__ void k_amrcell_majorants(const exa_amr_cell *__restrict__ cells, const float *__restrict__ scalars,
+                                    size_t n, exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const exa_amr_cell c = cells[i];
+  const float value = scalars[i];
+  if (isnan(value)) return;
+  const int w = 1 << c.level;
+  const float half = (float)w * .5f;
+  const V3 lo = mk3((float)c.pos.x - half, (float)c.pos.y - half, (float)c.pos.z - half);
+  const V3 hi = mk3((float)(c.pos.x + w) + half, (float)(c.pos.y + w) + half, (float)(c.pos.z + w) + half);
+  const V3i D = {dims.x, dims.y, dims.z};
+  const V3i a = project_on_grid(lo, D, wb), b = project_on_grid(hi, D, wb);
+  for (int z = a.z; z <= b.z; ++z)
+    for (int y = a.y; y <= b.y; ++y)
+      for (int x = a.x; x <= b.x; ++x) update_mc(mcRanges, dims, x, y, z, value, value);
+}
+
+void launchAmrCellMajorants(const exa_amr_cell *cells, const float *scalars, size_t n, exa_vec3i dims, exa_box3f wb,
+                            exa_range1f *mcRanges, cudaStream_t s)
+{
+  if (!n) return;
+  k_amrcell_majorants<<<gridFor(n, 256), 256, 0, s>>>(cells, scalars, n, dims, wb, mcRanges);
+  cudaCheck(cudaGetLastError(), "k_amrcell_majorants");
+}
+
+__device__ __forceinline__ bool amr_lattice(const exa_amr_cell &c, int level, const int *lo, const int *nl,
+                                            size_t &lin)
+{
+  if (c.level != level) return false;
+  const int x = (c.pos.x >> level) - lo[0], y = (c.pos.y >> level) - lo[1], z = (c.pos.z >> level) - lo[2];
+  lin = ((size_t)z * nl[1] + y) * nl[0] + x;
+  return true;
+}
+
+struct AmrLattice {
+  int lo[3], n[3];
+};
+
+__global__ void k_amr_level_bits(const exa_amr_cell *cells, size_t n, int level, AmrLattice G, uint32_t *bits,
+                                 unsigned *dupFlag)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  size_t c;
+  if (!amr_lattice(cells[i], level, G.lo, G.n, c)) return;
+  const uint32_t m = 1u << (c & 31);
+  if (atomicOr(bits + (c >> 5), m) & m) atomicOr(dupFlag, 1u);
+}
+
+void launchAmrLevelBits(const exa_amr_cell *cells, size_t n, int level, const int lo[3], const int nl[3],
+                        uint32_t *bits, unsigned *dupFlag, cudaStream_t s)
+{
+  if (!n) return;
+  const AmrLattice G{{lo[0], lo[1], lo[2]}, {nl[0], nl[1], nl[2]}};
+  k_amr_level_bits<<<gridFor(n, 256), 256, 0, s>>>(cells, n, level, G, bits, dupFlag);
+  cudaCheck(cudaGetLastError(), "k_amr_level_bits");
+}
+
+constexpr int kRankBlock = 1024;
+
+__global__ void k_rank_blocks(const uint32_t *bits, size_t words, uint32_t *rank, uint32_t *blockSum)
+{
+  typedef cub::BlockScan<uint32_t, kRankBlock> Scan;
+  __shared__ typename Scan::TempStorage tmp;
+  const size_t w = blockIdx.x * (size_t)kRankBlock + threadIdx.x;
+  const uint32_t v = w < words ? (uint32_t)__popc(bits[w]) : 0u;
+  uint32_t ex, total;
+  Scan(tmp).ExclusiveSum(v, ex, total);
+  if (w < words) rank[w] = ex;
+  if (threadIdx.x == 0) blockSum[blockIdx.x] = total;
+}
+
+__global__ void k_rank_add(uint32_t *rank, size_t words, const uint32_t *blockBase)
+{
+  const size_t w = blockIdx.x * (size_t)kRankBlock + threadIdx.x;
+  if (w < words) rank[w] += blockBase[blockIdx.x];
+}
+
+// exclusive prefix popcount per word: block scans, a scan of the block sums
+void launchAmrLevelRank(const uint32_t *bits, size_t words, uint32_t *rank, cudaStream_t s)
+{
+  if (!words) return;
+  const size_t nb = (words + kRankBlock - 1) / kRankBlock;
+  if (nb >= 0x7fffffffull) throw Error(EXA_ERR_INVALID, "AMR level lattice too large");
+  DBuf<uint32_t> bsum, bbase;
+  bsum.alloc(nb);
+  bbase.alloc(nb);
+  k_rank_blocks<<<(unsigned)nb, kRankBlock, 0, s>>>(bits, words, rank, bsum.ptr);
+  cudaCheck(cudaGetLastError(), "k_rank_blocks");
+  size_t tb = 0;
+  cudaCheck(cub::DeviceScan::ExclusiveSum(nullptr, tb, bsum.ptr, bbase.ptr, (int)nb, s), "scan size");
+  DBuf<unsigned char> tmp;
+  tmp.alloc(tb ? tb : 1);
+  cudaCheck(cub::DeviceScan::ExclusiveSum(tmp.ptr, tb, bsum.ptr, bbase.ptr, (int)nb, s), "scan");
+  k_rank_add<<<(unsigned)nb, kRankBlock, 0, s>>>(rank, words, bbase.ptr);
+  cudaCheck(cudaGetLastError(), "k_rank_add");
+  cudaCheck(cudaStreamSynchronize(s), "amr rank");
+}
+
+__global__ void k_amr_level_cells(const exa_amr_cell *cells, size_t n, int level, AmrLattice G, const uint32_t *bits,
+                                  const uint32_t *rank, int32_t *cellOf)
+{
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  size_t c;
+  if (!amr_lattice(cells[i], level, G.lo, G.n, c)) return;
+  cellOf[rank[c >> 5] + __popc(bits[c >> 5] & ((1u << (c & 31)) - 1u))] = (int32_t)i;
+}
+
+void launchAmrLevelCells(const exa_amr_cell *cells, size_t n, int level, const int lo[3], const int nl[3],
+                         const uint32_t *bits, const uint32_t *rank, int32_t *cellOf, cudaStream_t s)
+{
+  if (!n) return;
+  const AmrLattice G{{lo[0], lo[1], lo[2]}, {nl[0], nl[1], nl[2]}};
+  k_amr_level_cells<<<gridFor(n, 256), 256, 0, s>>>(cells, n, level, G, bits, rank, cellOf);
+  cudaCheck(cudaGetLastError(), "k_amr_level_cells");
 }
 
 // Grid.cu:687-719; the color map is staged in shared memory

@@ -105,6 +105,17 @@ struct ExaStitchModel : Model {  // model/ExaStitchModel.h:26-55
                 size_t &nonEmptyScalarsBytes) const;
 };
 
+// AMRCellModel (model/AMRCellModel.h:26-44): leaf cells of an AMR
+// hierarchy (position in finest units, level) with one scalar each
+struct AMRCellModel : Model {
+  std::vector<exa_amr_cell> cells;
+  std::vector<float> scalars;
+  // arrays in, then AMRCellModel::load's bounds / value-range pass
+  // (model/AMRCellModel.cpp:56-64)
+  void assign(const exa_amr_cell *c, size_t nc, const float *s, size_t ns);
+  void memStats(size_t &cellsBytes, size_t &scalarsBytes) const;  // AMRCellModel.cpp:69-73
+};
+
 struct Sampler {  // sampler/Sampler.h:28-69
   virtual ~Sampler() = default;
   virtual bool build(std::shared_ptr<Model> model, cudaStream_t s) = 0;
@@ -112,10 +123,19 @@ struct Sampler {  // sampler/Sampler.h:28-69
                                    cudaStream_t s) = 0;
   virtual void setLPs(exa_launch_params &lp) = 0;
   virtual std::string className() = 0;
+  // device footprint: field arrays, point-location structures
+  virtual size_t fieldBytes() const = 0;
+  virtual size_t accelBytes() const = 0;
   struct {
     std::shared_ptr<Grid> grid;
   } majorantAccel;
   float *maxOpacities = nullptr;
+  // the point-location view the kernels read; its device copy is the
+  // handle stored in LP.sampler.*.sampleBVH
+  AccelView accel{};
+  DBuf<AccelView> deviceAccel;
+  bool hasTF = false;
+  DBuf<float4> colorMap;
 };
 
 class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
@@ -142,16 +162,35 @@ class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
   DBuf<int32_t> bvhParents;     // internal nodes then leaves: parent*2+slot
   DBuf<int32_t> bvhLeafElem;    // leaf (sorted position) -> element id
   DBuf<uint32_t> occBits;       // element occupancy bitmap
-  DBuf<AccelView> deviceAccel;  // the handle stored in LP.sampler.ess.sampleBVH
-  AccelView accel{};
-  bool hasTF = false;
-  DBuf<float4> colorMap;
 
-  size_t accelBytes() const;
+  size_t fieldBytes() const override;
+  size_t accelBytes() const override;
 
  private:
   void buildGridletTables(cudaStream_t s);
   void buildElementBVH(cudaStream_t s);
+};
+
+// AMRCellSampler (sampler/AMRCellSampler.h:26-56, AMRCellSampler.cpp): the
+// tent-basis field over AMR cells.  Point location by dense per-level
+// lattices (replacing the OptiX user-geometry BVH); the majorant grid over
+// the cells' supports (Grid.cu:248-285, 314-364).
+class AMRCellSampler : public Sampler {
+ public:
+  bool build(std::shared_ptr<Model> model, cudaStream_t s) override;
+  void computeMaxOpacities(const exa_vec4f *colorMap, int numColors, exa_range1f xfRange, cudaStream_t s) override;
+  void setLPs(exa_launch_params &lp) override;
+  std::string className() override { return "AMRCellSampler"; }
+  size_t fieldBytes() const override;
+  size_t accelBytes() const override;
+
+  std::shared_ptr<AMRCellModel> model;
+  DBuf<exa_amr_cell> cellBuffer;
+  DBuf<float> scalarBuffer;
+  std::vector<DBuf<uint32_t>> levelBits, levelRank;
+  std::vector<DBuf<int32_t>> levelCell;
+  AmrCellView view{};
+  DBuf<AmrCellView> deviceView;
 };
 
 // ---------------------------------------------------------------- kernels
@@ -161,6 +200,17 @@ void launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t n
                             exa_range1f *mcRanges, exa_range1f *gridletRanges, cudaStream_t s);
 void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa_vec3i dims, exa_box3f wb,
                          exa_range1f *mcRanges, exa_range1f *elemRanges, cudaStream_t s);
+// Grid.cu:248-285: every cell's value into the macrocells its support
+// projects onto
+void launchAmrCellMajorants(const exa_amr_cell *cells, const float *scalars, size_t n, exa_vec3i dims, exa_box3f wb,
+                            exa_range1f *mcRanges, cudaStream_t s);
+// the AMR sampler's level lattices: existence bits (with a duplicate
+// check), ranks, and the rank -> cell map
+void launchAmrLevelBits(const exa_amr_cell *cells, size_t n, int level, const int lo[3], const int nl[3],
+                        uint32_t *bits, unsigned *dupFlag, cudaStream_t s);
+void launchAmrLevelRank(const uint32_t *bits, size_t words, uint32_t *rank, cudaStream_t s);
+void launchAmrLevelCells(const exa_amr_cell *cells, size_t n, int level, const int lo[3], const int nl[3],
+                         const uint32_t *bits, const uint32_t *rank, int32_t *cellOf, cudaStream_t s);
 void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf,
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,

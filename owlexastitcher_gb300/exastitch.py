@@ -101,8 +101,12 @@ class StitchLP(C.Structure):
     _fields_ = [("sampleBVH", C.c_uint64), ("gridletBuffer", C.c_void_p), ("gridletScalarBuffer", C.c_void_p)]
 
 
-class _SamplerUnion(C.Structure):
-    _fields_ = [("ess", StitchLP)]
+class AmrCellLP(C.Structure):
+    _fields_ = [("sampleBVH", C.c_uint64)]
+
+
+class _SamplerUnion(C.Union):
+    _fields_ = [("ess", StitchLP), ("acs", AmrCellLP)]
 
 
 class _TF(C.Structure):
@@ -183,7 +187,7 @@ class RenderStats(C.Structure):
 class MemStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "elemVertexBytes", "elemIndexBytes", "gridletBytes", "emptyScalarsBytes", "nonEmptyScalarsBytes",
-        "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes")]
+        "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes", "amrCellBytes", "amrScalarBytes")]
 
 
 class SurrogateParams(C.Structure):
@@ -243,6 +247,7 @@ EXPORTED = [
     "exa_batch_set_majorant_grid", "exa_batch_set_tile_width", "exa_render_batch", "exa_batch_autotune",
     "exa_read_grids", "exa_model_load", "exa_read_xf", "exa_xf_range", "exa_opacity_scale", "exa_read_cells",
     "exa_read_mesh", "exa_mesh_set", "exa_mesh_get_bounds",
+    "exa_amrcell_model_create", "exa_amrcell_model_load", "exa_sampler_get_class_name",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -309,6 +314,9 @@ def lib():
         "exa_read_mesh": ([C.c_char_p, vp, C.POINTER(u64), vp, C.POINTER(u64)], C.c_int),
         "exa_mesh_set": ([ctx_p, vp, u64, vp, u64], C.c_int),
         "exa_mesh_get_bounds": ([ctx_p, C.POINTER(box3f)], C.c_int),
+        "exa_amrcell_model_create": ([ctx_p, vp, u64, vp, u64], C.c_int),
+        "exa_amrcell_model_load": ([ctx_p, C.c_char_p, C.c_char_p], C.c_int),
+        "exa_sampler_get_class_name": ([ctx_p], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -382,22 +390,8 @@ class Context:
             pass
 
 
-class ExaStitchModel:
-    """model/ExaStitchModel.h:26-55, built from in-memory arrays."""
-
-    def __init__(self, ctx, vertices, indices, gridlets, gridlet_scalars):
-        self.ctx = ctx
-        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
-        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1, 8)
-        self.gridlets = np.ascontiguousarray(gridlets, GRIDLET_DTYPE)
-        self.gridlet_scalars = np.ascontiguousarray(gridlet_scalars, np.float32)
-        _check(lib().exa_model_create(ctx.h, _np_ptr(self.vertices), len(self.vertices), _np_ptr(self.indices),
-                                      len(self.indices), _np_ptr(self.gridlets), len(self.gridlets),
-                                      _np_ptr(self.gridlet_scalars), len(self.gridlet_scalars)))
-
-    @classmethod
-    def from_dataset(cls, ctx, ds):
-        return cls(ctx, ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+class _Model:
+    """model/Model.h:29-65: the calls every model kind shares."""
 
     @property
     def cellBounds(self):
@@ -428,8 +422,44 @@ class ExaStitchModel:
         return {f: getattr(m, f) for f, _ in MemStats._fields_}
 
 
+class AMRCellModel(_Model):
+    """model/AMRCellModel.h:26-44: AMR leaf cells (pos[3], level; 16 B
+    records) with one scalar each."""
+
+    def __init__(self, ctx, cells, scalars):
+        self.ctx = ctx
+        self.cells = np.ascontiguousarray(cells, np.int32).reshape(-1, 4)
+        self.scalars = np.ascontiguousarray(scalars, np.float32)
+        _check(lib().exa_amrcell_model_create(ctx.h, _np_ptr(self.cells), len(self.cells), _np_ptr(self.scalars),
+                                              len(self.scalars)))
+
+    @classmethod
+    def from_dataset(cls, ctx, ds):
+        return cls(ctx, ds.amr_cells, ds.amr_scalars)
+
+
+class ExaStitchModel(_Model):
+    """model/ExaStitchModel.h:26-55, built from in-memory arrays."""
+
+    def __init__(self, ctx, vertices, indices, gridlets, gridlet_scalars):
+        self.ctx = ctx
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1, 8)
+        self.gridlets = np.ascontiguousarray(gridlets, GRIDLET_DTYPE)
+        self.gridlet_scalars = np.ascontiguousarray(gridlet_scalars, np.float32)
+        _check(lib().exa_model_create(ctx.h, _np_ptr(self.vertices), len(self.vertices), _np_ptr(self.indices),
+                                      len(self.indices), _np_ptr(self.gridlets), len(self.gridlets),
+                                      _np_ptr(self.gridlet_scalars), len(self.gridlet_scalars)))
+
+    @classmethod
+    def from_dataset(cls, ctx, ds):
+        return cls(ctx, ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+
+
 class ExaStitchSampler:
-    """sampler/ExaStitchSampler.h:37-106."""
+    """sampler/ExaStitchSampler.h:37-106 (exa_sampler_build picks the
+    sampler that goes with the context's model; AMRCellSampler below is the
+    same wrapper for the AMR-cell model)."""
 
     def __init__(self, ctx):
         self.ctx = ctx
@@ -439,6 +469,9 @@ class ExaStitchSampler:
     @staticmethod
     def className():
         return lib().exa_sampler_class_name().decode()
+
+    def builtClassName(self):
+        return lib().exa_sampler_get_class_name(self.ctx.h).decode()
 
     def build(self, model):
         _check(lib().exa_sampler_build(self.ctx.h))
@@ -479,6 +512,18 @@ class ExaStitchSampler:
         out = np.zeros(len(pos), SAMPLE_DTYPE)
         _check(lib().exa_sample_points_host(self.ctx.h, _np_ptr(pos), len(pos), _np_ptr(out), int(bool(cull))))
         return out
+
+
+class AMRCellSampler(ExaStitchSampler):
+    """sampler/AMRCellSampler.h:26-56: tent-basis reconstruction over AMR
+    cells."""
+
+    @staticmethod
+    def className():
+        return "AMRCellSampler"
+
+    def prim_majorants(self):
+        raise ExaError(EXA_ERR_STATE, "the AMR-cell sampler has no per-primitive majorants")
 
 
 def new_launch_params():
