@@ -660,29 +660,41 @@ def run_small_config(a, local, flush, cpu=True):
                       "majorant_build_32^3_ms": maj32, "majorant_build_128^3_ms": maj128,
                       "note": "oracle/oracle.c point location (uniform-grid accel) and majorant build"}
     ctx.close()
-    out["amrcell_sampler"] = run_amrcell_small(ds, local, P, flush, stream)
+    out["amrcell_sampler"] = run_comparison_small(ds, local, P, flush, stream, "amrcell")
+    out["exabrick_sampler"] = run_comparison_small(ds, local, P, flush, stream, "exabrick")
     return out
 
 
-def run_amrcell_small(ds, local, P, flush, stream):
-    """The same two workloads through the AMR-cell comparison sampler (tent
-    basis over the small field's AMR cells): points/s and 256^2 x 1 spp
+def run_comparison_small(ds, local, P, flush, stream, kind):
+    """The same two workloads through a comparison sampler over the small
+    field's AMR cells: "amrcell" (tent basis over the cells) or "exabrick"
+    (bricks of x-runs of cells, region basis): points/s and 256^2 x 1 spp
     direct-lighting paths/s."""
     import ctypes as C
     import torch
     from helpers import orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import datagen
     from owlexastitcher_gb300 import exastitch as E
     ctx = E.Context(local)
-    model = E.AMRCellModel.from_dataset(ctx, ds)
+    if kind == "amrcell":
+        model = E.AMRCellModel.from_dataset(ctx, ds)
+        sampler = E.AMRCellSampler(ctx)
+        out = {"cells": len(ds.amr_cells)}
+    else:
+        t0 = time.perf_counter()
+        b, s = datagen.amr_to_bricks(ds.amr_cells, ds.amr_scalars)
+        model = E.ExaBrickModel(ctx, b, s)
+        sampler = E.ExaBrickSampler(ctx)
+        out = {"bricks": len(b), "regions": len(model.abrs()[0]),
+               "host_model_ms": (time.perf_counter() - t0) * 1e3}
     model.setNumGridCells((32, 32, 32))
-    sampler = E.AMRCellSampler(ctx)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sampler.build(model)
     vr = model.valueRange
     sampler.computeMaxOpacities(ramp_tf(), (np.float32(vr[0]), np.float32(vr[1])))
     ctx.sync()
-    out = {"cells": len(ds.amr_cells), "build_32^3_ms": (time.perf_counter() - t0) * 1e3}
+    out["build_32^3_ms"] = (time.perf_counter() - t0) * 1e3
     pd = torch.from_numpy(P).cuda()
     res = torch.empty(len(P) * 3, dtype=torch.int32, device="cuda")
     for _ in range(3):

@@ -102,6 +102,37 @@ typedef struct {
   uint64_t     sampleBVH;
 } exa_amrcell_lp;
 
+/* model/ABRs.h:28-63: a brick of size.x*size.y*size.z level-`level` cells
+ * from `lower` (finest units); its scalars start at scalars[begin], x
+ * fastest. */
+typedef struct {
+  exa_vec3i lower;
+  exa_vec3i size;
+  int32_t   level;
+  uint32_t  begin;
+} exa_brick;
+
+/* model/ABRs.h:65-77: an active brick region, a box in which a fixed set of
+ * bricks' basis functions overlap (leafList[leafListBegin ..
+ * leafListBegin + leafListSize), ascending brick ids). */
+typedef struct {
+  exa_box3f   domain;
+  exa_range1f valueRange;
+  int32_t     leafListBegin;
+  int32_t     leafListSize;
+  float       finestLevelCellWidth;
+} exa_abr;
+
+/* sampler/ExaBrickSampler.h:37-46: the ExaBrick sampler's handle and
+ * buffers. */
+typedef struct {
+  uint64_t   sampleBVH;
+  exa_brick *brickBuffer;
+  exa_abr   *abrBuffer;
+  float     *scalarBuffer;
+  int32_t   *abrLeafListBuffer;
+} exa_exabrick_lp;
+
 #define EXA_CLIP_PLANES_MAX 1   /* common.h:36 */
 #define EXA_LIGHTS_MAX      4   /* common.h:37 */
 
@@ -146,11 +177,12 @@ typedef struct {
 } exa_lp_ext;
 
 /* LaunchParams.h:56-119, field order and types kept; the sampler union
- * holds the ExaStitch and the AMR-cell members (both start with sampleBVH);
+ * holds the ExaStitch, AMR-cell and ExaBrick members (all start with
+ * sampleBVH);
  * transferFunc is the buffer variant (values/numValues,
  * LaunchParams.h:84-87). */
 typedef struct {
-  union { exa_stitch_lp ess; exa_amrcell_lp acs; } sampler;
+  union { exa_stitch_lp ess; exa_amrcell_lp acs; exa_exabrick_lp ebs; } sampler;
   uint32_t  *fbPointer;
   float     *fbDepth;
   exa_vec4f *accumBuffer;
@@ -214,6 +246,10 @@ typedef struct {
   uint64_t deviceMajorantBytes;  /* value ranges + max opacities            */
   uint64_t amrCellBytes;         /* AMR-cell model: cells (AMRCellModel::memStats) */
   uint64_t amrScalarBytes;       /* AMR-cell model: scalars                 */
+  uint64_t bricksBytes;          /* ExaBrick model (ExaBrickModel::memStats) */
+  uint64_t brickScalarsBytes;
+  uint64_t abrsBytes;
+  uint64_t abrLeafListBytes;
 } exa_mem_stats;
 
 typedef struct exa_context exa_context;
@@ -310,6 +346,24 @@ int exa_amrcell_model_create(exa_context *ctx, const exa_amr_cell *cells, uint64
 /* AMRCellModel::load (AMRCellModel.cpp:24-67): '.cells' records and a raw
  * float32 scalars file. */
 int exa_amrcell_model_load(exa_context *ctx, const char *cellsFile, const char *scalarsFile);
+/* ExaBrickModel::load(bricks, scalars, numBricks) (model/ExaBrickModel.cpp:
+ * 120-143) and init() (:145-168): the context's model becomes the bricks;
+ * the scalars array holds the bricks' cells (bricks[i].begin +
+ * size.x*size.y*size.z <= numScalars).  The active brick regions are built
+ * on the host (ABRs::buildFrom, model/ABRs.cpp).  exa_sampler_build then
+ * builds the ExaBrickSampler in the reference's "majorant grid + DDA"
+ * traversal mode (EXA_STITCH_EXA_BRICK_TRAVERSAL_MODE 1) with ABR sampling
+ * (sampler mode 0). */
+int exa_exabrick_model_create(exa_context *ctx, const exa_brick *bricks, uint64_t numBricks, const float *scalars,
+                              uint64_t numScalars);
+/* ExaBrickModel::load(brickFile, scalarFile) (ExaBrickModel.cpp:28-117):
+ * '.bricks' records int32 size[3], lower[3], level, then size.x*size.y*size.z
+ * int32 cell ids into the float32 scalars file. */
+int exa_exabrick_model_load(exa_context *ctx, const char *bricksFile, const char *scalarsFile);
+/* the model's active brick regions and their leaf list (null arrays: counts
+ * only) */
+int exa_exabrick_get_abrs(exa_context *ctx, exa_abr *abrs, uint64_t *numAbrs, int32_t *leafList,
+                          uint64_t *leafListSize);
 
 /* Surface meshes (TriangleMesh.cpp:27-76; OWLRenderer.cpp:446-545).  A mesh
  * file is a sequence of meshes, each int32 numVerts, numVerts float3,
@@ -368,8 +422,8 @@ int exa_sampler_compute_max_opacities(exa_context *ctx,
 int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp);
 /* Sampler::className (sampler/ExaStitchSampler.h:59). */
 const char *exa_sampler_class_name(void);
-/* className() of the context's built sampler ("ExaStitchSampler" or
- * "AMRCellSampler"), "" before exa_sampler_build. */
+/* className() of the context's built sampler ("ExaStitchSampler",
+ * "AMRCellSampler" or "ExaBrickSampler"), "" before exa_sampler_build. */
 const char *exa_sampler_get_class_name(exa_context *ctx);
 /* Grid::valueRanges / Grid::maxOpacities (Grid.h:70-73), copied to host
  * arrays of numMCs entries (either pointer may be NULL). */

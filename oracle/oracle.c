@@ -439,6 +439,12 @@ struct oc_field {
   uint64_t *amrKeys; uint32_t *amrOrder;
   int amrLevels;
   int amrHas[16], amrLo[16][3], amrN[16][3];
+  /* ExaBricks (oc_field_set_bricks): bricks, their scalars, the active
+   * brick regions built here; the uniform grid above then lists regions */
+  const exa_brick *bricks; uint64_t numBricks;
+  const float *brickScalars;
+  exa_abr *abrs; uint64_t numAbrs;
+  int32_t *leafList; uint64_t leafListSize, leafListCap;
   /* surface mesh, traced where lp->meshBVH != 0 */
   const exa_vec3f *meshVertices;
   const exa_vec3i *meshIndices;
@@ -553,6 +559,8 @@ oc_field *oc_field_create(const v4 *vertices, uint64_t numVertices,
 void oc_field_destroy(oc_field *f)
 {
   if (!f) return;
+  free(f->abrs);
+  free(f->leafList);
   free(f->amrKeys);
   free(f->amrOrder);
   free(f->cellBegin);
@@ -683,6 +691,277 @@ static exa_sample amr_sample(const oc_field *f, v3 pos)
   return s;
 }
 
+/* ------------------------------------------------ ExaBricks
+ * ABRs::buildFrom / buildRec / addLeaf / computeValueRange (model/ABRs.cpp)
+ * and ExaBrickSampler's sample() in the grid + DDA traversal mode
+ * (sampler/ExaBrickSampler.h:113-239).  Split choice: the primitive face
+ * closest to the domain centre per axis, the widest axis first (ties: the
+ * lowest axis); the upper half is recursed into first; a region lists its
+ * bricks in ascending id order.  Sampling takes the lowest-index region
+ * whose closed domain holds the point (OptiX's order is unspecified). */
+static inline int64_t lookup_cell(const oc_field *f, v3 p);
+
+typedef struct { float lo[3], hi[3]; int id; } bprim;
+
+static void abr_add_leaf(oc_field *f, const bprim *p, size_t n, const float *lo, const float *hi)
+{
+  for (int a = 0; a < 3; ++a)
+    if (lo[a] >= hi[a]) return;
+  if (!n) return;
+  int *ids = (int *)malloc(n * sizeof(int));
+  for (size_t i = 0; i < n; ++i) ids[i] = p[i].id;
+  /* ascending unique ids (std::set) */
+  for (size_t i = 1; i < n; ++i) {
+    const int v = ids[i];
+    size_t j = i;
+    while (j > 0 && ids[j - 1] > v) { ids[j] = ids[j - 1]; --j; }
+    ids[j] = v;
+  }
+  size_t u = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (i == 0 || ids[i] != ids[i - 1]) ids[u++] = ids[i];
+  if (f->leafListSize + u > f->leafListCap) {
+    f->leafListCap = (f->leafListSize + u) * 2 + 16;
+    f->leafList = (int32_t *)realloc(f->leafList, f->leafListCap * sizeof(int32_t));
+  }
+  exa_abr r;
+  memset(&r, 0, sizeof(r));
+  r.domain.lower = mk3(lo[0], lo[1], lo[2]);
+  r.domain.upper = mk3(hi[0], hi[1], hi[2]);
+  r.leafListBegin = (int32_t)f->leafListSize;
+  r.leafListSize = (int32_t)u;
+  for (size_t i = 0; i < u; ++i) f->leafList[f->leafListSize++] = ids[i];
+  free(ids);
+  f->abrs = (exa_abr *)realloc(f->abrs, (f->numAbrs + 1) * sizeof(exa_abr));
+  f->abrs[f->numAbrs++] = r;
+}
+
+static void abr_build_rec(oc_field *f, bprim *p, size_t n, const float *lo, const float *hi)
+{
+  if (!n) { free(p); return; }
+  for (int a = 0; a < 3; ++a)
+    if (hi[a] == lo[a]) { free(p); return; }
+  float tgt[3], bestPos[3], bestDist[3], span[3];
+  for (int a = 0; a < 3; ++a) {
+    tgt[a] = (lo[a] + hi[a]) * 0.5f;
+    bestPos[a] = lo[a];
+    span[a] = hi[a] - lo[a];
+    bestDist[a] = span[a];
+  }
+  for (size_t i = 0; i < n; ++i)
+    for (int dim = 0; dim < 3; ++dim)
+      for (int side = 0; side < 2; ++side) {
+        const float pos = side ? p[i].lo[dim] : p[i].hi[dim];
+        if (pos <= lo[dim] || pos >= hi[dim]) continue;
+        const float dist = fabsf(tgt[dim] - pos);
+        if (dist < bestDist[dim]) { bestPos[dim] = pos; bestDist[dim] = dist; }
+      }
+  const int widest = (span[0] >= span[1] && span[0] >= span[2]) ? 0 : (span[1] >= span[2] ? 1 : 2);
+  int splitDim = -1;
+  float splitPos = 0.f;
+  for (int i = 0; i < 3; ++i) {
+    const int dim = (widest + i) % 3;
+    if (bestPos[dim] <= lo[dim] || bestPos[dim] >= hi[dim]) continue;
+    splitDim = dim;
+    splitPos = bestPos[dim];
+    break;
+  }
+  if (splitDim < 0) { abr_add_leaf(f, p, n, lo, hi); free(p); return; }
+  float lhi[3] = {hi[0], hi[1], hi[2]}, rlo[3] = {lo[0], lo[1], lo[2]};
+  lhi[splitDim] = splitPos;
+  rlo[splitDim] = splitPos;
+  bprim *pl = (bprim *)malloc(n * sizeof(bprim)), *pr = (bprim *)malloc(n * sizeof(bprim));
+  size_t nl = 0, nr = 0;
+  for (size_t i = 0; i < n; ++i) {
+    bprim cl, cr;
+    int okl = 1, okr = 1;
+    for (int a = 0; a < 3; ++a) {
+      cl.lo[a] = fmax_t(p[i].lo[a], lo[a]); cl.hi[a] = fmin_t(p[i].hi[a], lhi[a]);
+      cr.lo[a] = fmax_t(p[i].lo[a], rlo[a]); cr.hi[a] = fmin_t(p[i].hi[a], hi[a]);
+      okl = okl && cl.lo[a] < cl.hi[a];
+      okr = okr && cr.lo[a] < cr.hi[a];
+    }
+    cl.id = cr.id = p[i].id;
+    if (okl) pl[nl++] = cl;
+    if (okr) pr[nr++] = cr;
+  }
+  free(p);
+  abr_build_rec(f, pr, nr, rlo, hi);
+  abr_build_rec(f, pl, nl, lo, lhi);
+}
+
+static void abr_value_range(exa_abr *r, const exa_brick *bricks, const float *scalars, const int32_t *leafList)
+{
+  r->valueRange.lower = 1e30f;
+  r->valueRange.upper = -1e30f;
+  const float dlo[3] = {r->domain.lower.x, r->domain.lower.y, r->domain.lower.z};
+  const float dhi[3] = {r->domain.upper.x, r->domain.upper.y, r->domain.upper.z};
+  for (int i = 0; i < r->leafListSize; ++i) {
+    const exa_brick *b = &bricks[leafList[r->leafListBegin + i]];
+    const float cw = (float)(1 << b->level);
+    const int lower[3] = {b->lower.x, b->lower.y, b->lower.z}, size[3] = {b->size.x, b->size.y, b->size.z};
+    for (int iz = 0; iz < size[2]; ++iz) {
+      const float pz = (float)lower[2] + ((float)iz + .5f) * cw;
+      if (!((pz - cw) <= dhi[2] && (pz + cw) >= dlo[2])) continue;
+      for (int iy = 0; iy < size[1]; ++iy) {
+        const float py = (float)lower[1] + ((float)iy + .5f) * cw;
+        if (!((py - cw) <= dhi[1] && (py + cw) >= dlo[1])) continue;
+        for (int ix = 0; ix < size[0]; ++ix) {
+          const float px = (float)lower[0] + ((float)ix + .5f) * cw;
+          if (!((px - cw) <= dhi[0] && (px + cw) >= dlo[0])) continue;
+          const float v = scalars[(size_t)b->begin + ix + (size_t)size[0] * iy + (size_t)size[0] * size[1] * iz];
+          if (v < r->valueRange.lower) r->valueRange.lower = v;
+          if (r->valueRange.upper < v) r->valueRange.upper = v;
+        }
+      }
+    }
+  }
+}
+
+int oc_field_set_bricks(oc_field *f, const exa_brick *bricks, uint64_t nb, const float *scalars, uint64_t ns)
+{
+  for (uint64_t i = 0; i < nb; ++i) {
+    if (bricks[i].level < 0 || bricks[i].level > 30) return 1;
+    if (bricks[i].size.x < 1 || bricks[i].size.y < 1 || bricks[i].size.z < 1) return 2;
+    if ((uint64_t)bricks[i].begin + (uint64_t)bricks[i].size.x * bricks[i].size.y * bricks[i].size.z > ns) return 3;
+  }
+  f->bricks = bricks; f->numBricks = nb; f->brickScalars = scalars;
+  free(f->abrs); free(f->leafList);
+  f->abrs = NULL; f->numAbrs = 0; f->leafList = NULL; f->leafListSize = f->leafListCap = 0;
+  bprim *p = (bprim *)malloc((nb ? nb : 1) * sizeof(bprim));
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint64_t i = 0; i < nb; ++i) {
+    const float cw = (float)(1 << bricks[i].level);
+    const int lower[3] = {bricks[i].lower.x, bricks[i].lower.y, bricks[i].lower.z};
+    const int size[3] = {bricks[i].size.x, bricks[i].size.y, bricks[i].size.z};
+    for (int a = 0; a < 3; ++a) {
+      p[i].lo[a] = (float)lower[a] - 0.5f * cw;                 /* ExaBrick::getDomain */
+      p[i].hi[a] = (float)lower[a] + ((float)size[a] + 0.5f) * cw;
+      lo[a] = fmin_t(lo[a], p[i].lo[a]);
+      hi[a] = fmax_t(hi[a], p[i].hi[a]);
+    }
+    p[i].id = (int)i;
+  }
+  abr_build_rec(f, p, nb, lo, hi);
+  for (uint64_t i = 0; i < f->numAbrs; ++i) {
+    exa_abr *r = &f->abrs[i];
+    int finest = 1 << 30;
+    for (int k = 0; k < r->leafListSize; ++k) finest = imin_t(finest, bricks[f->leafList[r->leafListBegin + k]].level);
+    r->finestLevelCellWidth = (float)(1 << finest);
+    abr_value_range(r, bricks, scalars, f->leafList);
+  }
+  /* the uniform grid lists regions (closed boxes) in ascending index */
+  free(f->cellBegin); free(f->items);
+  exa_box3f all;
+  all.lower = mk3(lo[0], lo[1], lo[2]);
+  all.upper = mk3(hi[0], hi[1], hi[2]);
+  if (!nb) { all.lower = mk3(0.f, 0.f, 0.f); all.upper = mk3(1.f, 1.f, 1.f); }
+  f->gb = all;
+  const v3 ext = sub3(all.upper, all.lower);
+  const double maxExt = fmax(fmax(ext.x, ext.y), ext.z);
+  double cellW = maxExt / fmin(256.0, fmax(4.0, 2.0 * cbrt((double)f->numAbrs)));
+  if (cellW <= 0.0) cellW = 1.0;
+  f->gd.x = imax_t(1, (int)ceil(ext.x / cellW));
+  f->gd.y = imax_t(1, (int)ceil(ext.y / cellW));
+  f->gd.z = imax_t(1, (int)ceil(ext.z / cellW));
+  f->cs = mk3(fmax_t(ext.x, 1e-30f) / (float)f->gd.x, fmax_t(ext.y, 1e-30f) / (float)f->gd.y,
+              fmax_t(ext.z, 1e-30f) / (float)f->gd.z);
+  const uint64_t nc = (uint64_t)f->gd.x * f->gd.y * f->gd.z;
+  f->cellBegin = (uint32_t *)calloc(nc + 1, sizeof(uint32_t));
+  f->items = NULL;
+  for (int pass = 0; pass < 2; ++pass) {
+    uint32_t *cursor = NULL;
+    if (pass == 1) {
+      uint64_t acc = 0;
+      for (uint64_t c = 0; c < nc; ++c) { const uint32_t k = f->cellBegin[c]; f->cellBegin[c] = (uint32_t)acc; acc += k; }
+      f->cellBegin[nc] = (uint32_t)acc;
+      f->items = (int32_t *)malloc((acc ? acc : 1) * sizeof(int32_t));
+      cursor = (uint32_t *)malloc(nc * sizeof(uint32_t));
+      memcpy(cursor, f->cellBegin, nc * sizeof(uint32_t));
+    }
+    for (uint64_t k = 0; k < f->numAbrs; ++k) {
+      v3i a, b;
+      cell_range(f, f->abrs[k].domain, &a, &b);
+      for (int z = a.z; z <= b.z; ++z)
+        for (int y = a.y; y <= b.y; ++y)
+          for (int x = a.x; x <= b.x; ++x) {
+            const uint64_t c = ((uint64_t)z * f->gd.y + y) * f->gd.x + x;
+            if (pass == 0) f->cellBegin[c]++;
+            else f->items[cursor[c]++] = (int32_t)k;
+          }
+    }
+    free(cursor);
+  }
+  return 0;
+}
+
+void oc_field_abrs(const oc_field *f, const exa_abr **abrs, uint64_t *numAbrs, const int32_t **leafList,
+                   uint64_t *leafListSize)
+{
+  *abrs = f->abrs; *numAbrs = f->numAbrs; *leafList = f->leafList; *leafListSize = f->leafListSize;
+}
+
+/* addBasisFunctions (sampler/ExaBrickSampler.h:113-200) */
+static void add_basis(const oc_field *f, int brickID, v3 pos, float *sumWV, float *sumW)
+{
+  const exa_brick *b = &f->bricks[brickID];
+  const float cw = (float)(1 << b->level);
+  const float lx = (pos.x - (float)b->lower.x) / cw - .5f;
+  const float ly = (pos.y - (float)b->lower.y) / cw - .5f;
+  const float lz = (pos.z - (float)b->lower.z) / cw - .5f;
+  const int ilx = imax_t(-1, (int)floorf(lx)), ily = imax_t(-1, (int)floorf(ly)), ilz = imax_t(-1, (int)floorf(lz));
+  const int ihx = ilx + 1, ihy = ily + 1, ihz = ilz + 1;
+  const float fx = lx - (float)ilx, fy = ly - (float)ily, fz = lz - (float)ilz;
+  const float nx = 1.f - fx, ny = 1.f - fy, nz = 1.f - fz;
+  const float *S = f->brickScalars + b->begin;
+  const int sx = b->size.x, sy = b->size.y, sz = b->size.z;
+#define OC_ADD(x, y, z, w) do { const float wt = (w); const float sc = S[(x) + (y) * sx + (z) * sx * sy]; \
+    *sumW += wt; *sumWV += wt * sc; } while (0)
+  if (ilz >= 0 && ilz < sz) {
+    if (ily >= 0 && ily < sy) {
+      if (ilx >= 0 && ilx < sx) OC_ADD(ilx, ily, ilz, nz * ny * nx);
+      if (ihx < sx) OC_ADD(ihx, ily, ilz, nz * ny * fx);
+    }
+    if (ihy < sy) {
+      if (ilx >= 0 && ilx < sx) OC_ADD(ilx, ihy, ilz, nz * fy * nx);
+      if (ihx < sx) OC_ADD(ihx, ihy, ilz, nz * fy * fx);
+    }
+  }
+  if (ihz < sz) {
+    if (ily >= 0 && ily < sy) {
+      if (ilx >= 0 && ilx < sx) OC_ADD(ilx, ily, ihz, fz * ny * nx);
+      if (ihx < sx) OC_ADD(ihx, ily, ihz, fz * ny * fx);
+    }
+    if (ihy < sy) {
+      if (ilx >= 0 && ilx < sx) OC_ADD(ilx, ihy, ihz, fz * fy * nx);
+      if (ihx < sx) OC_ADD(ihx, ihy, ihz, fz * fy * fx);
+    }
+  }
+#undef OC_ADD
+}
+
+static exa_sample brick_sample(const oc_field *f, v3 pos)
+{
+  exa_sample s = {0, -1, 0.f};
+  const int64_t c = lookup_cell(f, pos);
+  if (c < 0) return s;
+  int best = -1;
+  for (uint32_t i = f->cellBegin[c]; i < f->cellBegin[c + 1]; ++i) {
+    const exa_abr *r = &f->abrs[f->items[i]];
+    if (r->domain.lower.x <= pos.x && r->domain.lower.y <= pos.y && r->domain.lower.z <= pos.z &&
+        pos.x <= r->domain.upper.x && pos.y <= r->domain.upper.y && pos.z <= r->domain.upper.z) {
+      best = f->items[i];
+      break;
+    }
+  }
+  if (best < 0) return s;
+  const exa_abr *r = &f->abrs[best];
+  float sumWV = 0.f, sumW = 0.f;
+  for (int i = 0; i < r->leafListSize; ++i) add_basis(f, f->leafList[r->leafListBegin + i], pos, &sumWV, &sumW);
+  if (sumW > 0.f) s.value = sumWV / sumW;
+  return s;
+}
+
 void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices, const exa_vec3i *indices, uint64_t numTris)
 {
   f->meshVertices = vertices;
@@ -724,6 +1003,21 @@ void oc_field_bounds(const oc_field *f, exa_box3f *cb, exa_range1f *vr)
     const exa_box3f gb = gridlet_bounds(gl);
     b.lower = min3(b.lower, gb.lower); b.upper = max3(b.upper, gb.lower);
     b.lower = min3(b.lower, gb.upper); b.upper = max3(b.upper, gb.upper);
+  }
+  /* ExaBrickModel::init (ExaBrickModel.cpp:157-166): bricks' bounds, the
+   * regions' value ranges */
+  for (uint64_t i = 0; i < f->numBricks; ++i) {
+    const exa_brick *bk = &f->bricks[i];
+    const int w = 1 << bk->level;
+    const v3 lo = mk3((float)bk->lower.x, (float)bk->lower.y, (float)bk->lower.z);
+    const v3 hi = mk3((float)(bk->lower.x + bk->size.x * w), (float)(bk->lower.y + bk->size.y * w),
+                      (float)(bk->lower.z + bk->size.z * w));
+    b.lower = min3(b.lower, lo); b.upper = max3(b.upper, lo);
+    b.lower = min3(b.lower, hi); b.upper = max3(b.upper, hi);
+  }
+  for (uint64_t i = 0; i < f->numAbrs && f->numBricks; ++i) {
+    r.lower = fminf(r.lower, f->abrs[i].valueRange.lower);
+    r.upper = fmaxf(r.upper, f->abrs[i].valueRange.upper);
   }
   /* AMRCellModel::load (AMRCellModel.cpp:56-64) */
   for (uint64_t i = 0; i < f->numAmr; ++i) {
@@ -768,6 +1062,7 @@ static inline int64_t lookup_cell(const oc_field *f, v3 p)
 exa_sample oc_sample(const oc_field *f, v3 pos, int cull)
 {
   if (f->numAmr) return amr_sample(f, pos);
+  if (f->numBricks) return brick_sample(f, pos);
   exa_sample s = {-1, -1, 0.f};
   const int64_t c = lookup_cell(f, pos);
   if (c < 0) return s;
@@ -844,6 +1139,26 @@ void oc_build_majorants(const oc_field *f, v3i dims, exa_box3f wb, exa_range1f *
 {
   const size_t numMCs = (size_t)dims.x * dims.y * dims.z;
   for (size_t i = 0; i < numMCs; ++i) { vr[i].lower = 1e30f; vr[i].upper = -1e30f; } /* Grid.cu:61-70 */
+  /* ExaBrick cells: the cell box grown by half a cell (Grid.cu:399-430) */
+  for (uint64_t bi = 0; bi < f->numBricks; ++bi) {
+    const exa_brick *b = &f->bricks[bi];
+    const int w = 1 << b->level;
+    const float half = (float)w * .5f;
+    for (int z = 0; z < b->size.z; ++z)
+      for (int y = 0; y < b->size.y; ++y)
+        for (int x = 0; x < b->size.x; ++x) {
+          const float value = f->brickScalars[(size_t)b->begin + x + (size_t)b->size.x * (y + (size_t)b->size.y * z)];
+          if (isnan(value)) continue;
+          const int lx = b->lower.x + x * w, ly = b->lower.y + y * w, lz = b->lower.z + z * w;
+          const v3 lo3 = mk3((float)lx - half, (float)ly - half, (float)lz - half);
+          const v3 hi3 = mk3((float)(lx + w) + half, (float)(ly + w) + half, (float)(lz + w) + half);
+          const v3i lo = oc_project_on_grid(lo3, dims, wb), hi = oc_project_on_grid(hi3, dims, wb);
+          const exa_range1f r = {value, value};
+          for (int mz = lo.z; mz <= hi.z; ++mz)
+            for (int my = lo.y; my <= hi.y; ++my)
+              for (int mx = lo.x; mx <= hi.x; ++mx) { v3i id = {mx, my, mz}; update_mc(vr, id, dims, r); }
+        }
+  }
   /* AMR cells: the cell's support projected onto the grid (Grid.cu:248-285) */
   for (uint64_t i = 0; i < f->numAmr; ++i) {
     const int32_t *c = &f->amrCells[i * 4];

@@ -64,6 +64,13 @@ void oc_field_set_prim_opacities(oc_field *f, const float *gridletMaxOps,
  * that is not a multiple of the cell width, or a duplicate cell. */
 int oc_field_set_amr(oc_field *f, const int32_t *cells, uint64_t numCells,
                      const float *scalars, uint64_t numScalars);
+/* the field becomes the ExaBrick basis over bricks (arrays not copied); the
+ * active brick regions are built here.  0 on success; non-zero for a bad
+ * level, an empty brick or scalars past the end. */
+int oc_field_set_bricks(oc_field *f, const exa_brick *bricks, uint64_t numBricks,
+                        const float *scalars, uint64_t numScalars);
+void oc_field_abrs(const oc_field *f, const exa_abr **abrs, uint64_t *numAbrs,
+                   const int32_t **leafList, uint64_t *leafListSize);
 /* surface mesh the integrators trace where lp->meshBVH != 0 (arrays are
  * not copied: numTris int3 rows into the float3 vertices) */
 void oc_field_set_mesh(oc_field *f, const exa_vec3f *vertices,

@@ -65,6 +65,10 @@ _lib = None
 _ref = None
 
 
+ABR_DTYPE = np.dtype([("domain", "<f4", 6), ("valueRange", "<f4", 2), ("leafListBegin", "<i4"),
+                      ("leafListSize", "<i4"), ("finestLevelCellWidth", "<f4")])
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -92,6 +96,9 @@ def lib():
         L.oc_field_set_prim_opacities.argtypes = [vp, vp, vp]
         L.oc_field_set_mesh.argtypes = [vp, vp, vp, C.c_uint64]
         L.oc_field_set_amr.restype = C.c_int
+        L.oc_field_set_bricks.restype = C.c_int
+        L.oc_field_set_bricks.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]
+        L.oc_field_abrs.argtypes = [vp, C.POINTER(vp), C.POINTER(C.c_uint64), C.POINTER(vp), C.POINTER(C.c_uint64)]
         L.oc_field_set_amr.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64]
         L.oc_field_bounds.argtypes = [vp, C.POINTER(Box3f), C.POINTER(Range1f)]
         L.oc_sample.restype = Sample
@@ -184,6 +191,31 @@ class Field:
         if rc:
             raise ValueError(f"bad AMR cells ({rc})")
         return f
+
+    @classmethod
+    def bricks(cls, bricks, scalars):
+        """a field of ExaBricks (BRICK_DTYPE records) and their scalars,
+        reconstructed by the ExaBrick basis over the active brick regions"""
+        f = cls(np.zeros((0, 4), np.float32), np.zeros((0, 8), np.int32), np.zeros(0, GRIDLET_DTYPE),
+                np.zeros(0, np.float32))
+        f._bricks = np.ascontiguousarray(bricks)
+        f._bscal = np.ascontiguousarray(scalars, dtype=np.float32)
+        rc = lib().oc_field_set_bricks(f.h, _ptr(f._bricks), len(f._bricks), _ptr(f._bscal), len(f._bscal))
+        if rc:
+            raise ValueError(f"bad bricks ({rc})")
+        return f
+
+    def abrs(self):
+        """(regions as ABR_DTYPE, leaf list int32)"""
+        a, la = C.c_void_p(), C.c_void_p()
+        n, nl = C.c_uint64(), C.c_uint64()
+        lib().oc_field_abrs(self.h, C.byref(a), C.byref(n), C.byref(la), C.byref(nl))
+        regions, leaf = np.zeros(0, ABR_DTYPE), np.zeros(0, np.int32)
+        if n.value:
+            regions = np.frombuffer((C.c_char * (n.value * ABR_DTYPE.itemsize)).from_address(a.value), ABR_DTYPE).copy()
+        if nl.value:
+            leaf = np.frombuffer((C.c_char * (nl.value * 4)).from_address(la.value), np.int32).copy()
+        return regions, leaf
 
     def set_mesh(self, vertices, indices):
         """surface mesh: float3 vertices, int3 triangles (kept alive here)"""

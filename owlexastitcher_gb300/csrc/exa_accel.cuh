@@ -73,6 +73,18 @@ struct AmrCellView {
   AmrLevel lv[kMaxLevels];
 };
 
+// ExaBricks (the comparison sampler of sampler/ExaBrickSampler.h): bricks,
+// their scalars, the active brick regions with their leaf lists, and an
+// LBVH over the regions' domains (rows of two corner vertices)
+struct BrickView {
+  const exa_brick *bricks;
+  const float *scalars;
+  const exa_abr *abrs;
+  const int32_t *leafList;
+  const BvhNode *nodes;
+  int numAbrs;
+};
+
 struct AccelView {
   const exa_gridlet *gridlets;
   const float *scalars;
@@ -88,6 +100,7 @@ struct AccelView {
   ElemOccupancy occ;
   GridletTable tables[kMaxLevels];
   const AmrCellView *amr;       // non-null: the AMR-cell sampler (no gridlets, no elements)
+  const BrickView *bricks;      // non-null: the ExaBrick sampler (no gridlets, no elements)
 };
 
 EXA_HD int occ_coord(float p, float origin, float cs, int n)
@@ -297,9 +310,103 @@ static __device__ __noinline__ exa_sample amr_sample(const AmrCellView &V, V3 po
   return s;
 }
 
+// addBasisFunctions (sampler/ExaBrickSampler.h:113-200): the brick's
+// trilinear basis functions around pos, in the reference's corner order
+EXA_D void add_basis(const BrickView &V, int brickID, V3 pos, float &sumWV, float &sumW)
+{
+  const exa_brick b = V.bricks[brickID];
+  const float cw = (float)(1 << b.level);
+  const float lx = (pos.x - (float)b.lower.x) / cw - .5f;
+  const float ly = (pos.y - (float)b.lower.y) / cw - .5f;
+  const float lz = (pos.z - (float)b.lower.z) / cw - .5f;
+  const int ilx = max(-1, (int)floorf(lx)), ily = max(-1, (int)floorf(ly)), ilz = max(-1, (int)floorf(lz));
+  const int ihx = ilx + 1, ihy = ily + 1, ihz = ilz + 1;
+  const float fx = lx - (float)ilx, fy = ly - (float)ily, fz = lz - (float)ilz;
+  const float nx = 1.f - fx, ny = 1.f - fy, nz = 1.f - fz;
+  const float *S = V.scalars + b.begin;
+  auto add = [&](int x, int y, int z, float w) {
+    const float scalar = __ldg(S + x + y * b.size.x + z * b.size.x * b.size.y);
+    sumW += w;
+    sumWV += w * scalar;
+  };
+  if (ilz >= 0 && ilz < b.size.z) {
+    if (ily >= 0 && ily < b.size.y) {
+      if (ilx >= 0 && ilx < b.size.x) add(ilx, ily, ilz, nz * ny * nx);
+      if (ihx < b.size.x) add(ihx, ily, ilz, nz * ny * fx);
+    }
+    if (ihy < b.size.y) {
+      if (ilx >= 0 && ilx < b.size.x) add(ilx, ihy, ilz, nz * fy * nx);
+      if (ihx < b.size.x) add(ihx, ihy, ilz, nz * fy * fx);
+    }
+  }
+  if (ihz < b.size.z) {
+    if (ily >= 0 && ily < b.size.y) {
+      if (ilx >= 0 && ilx < b.size.x) add(ilx, ily, ihz, fz * ny * nx);
+      if (ihx < b.size.x) add(ihx, ily, ihz, fz * ny * fx);
+    }
+    if (ihy < b.size.y) {
+      if (ilx >= 0 && ilx < b.size.x) add(ilx, ihy, ihz, fz * fy * nx);
+      if (ihx < b.size.x) add(ihx, ihy, ihz, fz * fy * fx);
+    }
+  }
+}
+
+// ExaBrickSampler's sample() in the grid + DDA traversal mode (sampler/
+// ExaBrickSampler.h:202-239, programs/ExaBrickSampler.cu:67-89): the region
+// whose closed domain holds pos adds the basis functions of its bricks;
+// value sumWV / sumW, 0 where no region holds pos or the weights sum to 0
+// (primID is 0 in every case, as there).  Where several regions share a
+// face the lowest-index one is taken (OptiX reports them in an unspecified
+// order).  The region is found by a complete walk of the region LBVH.
+static __device__ __noinline__ exa_sample brick_sample(const BrickView &V, V3 pos, uint32_t &err)
+{
+  exa_sample s;
+  s.primID = 0;
+  s.cellID = -1;
+  s.value = 0.f;
+  if (V.numAbrs <= 0) return s;
+  int best = 0x7fffffff;
+  int stack[kBvhStack];
+  int sp = 0, node = 0;
+  bool done = false;
+  for (int visits = 0; visits <= V.numAbrs + 1 && !done; ++visits) {
+    const float4 *np = reinterpret_cast<const float4 *>(V.nodes + node);
+    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+    const float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
+    const float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
+    const int c[2] = {__float_as_int(q3.x), __float_as_int(q3.y)};
+    const bool in[2] = {box_contains(lo0, hi0, pos), box_contains(lo1, hi1, pos)};
+    int next = -1;
+    for (int k = 0; k < 2; ++k) {
+      if (!in[k]) continue;
+      if (c[k] < 0) {
+        best = min(best, ~c[k]);
+      } else if (next < 0) {
+        next = c[k];
+      } else if (sp < kBvhStack) {
+        stack[sp++] = c[k];
+      } else {
+        err |= EXA_DEVERR_BVH_STACK;
+      }
+    }
+    if (next < 0) {
+      if (sp == 0) done = true;
+      else next = stack[--sp];
+    }
+    node = next;
+  }
+  if (best == 0x7fffffff) return s;
+  const exa_abr R = V.abrs[best];
+  float sumWV = 0.f, sumW = 0.f;
+  for (int i = 0; i < R.leafListSize; ++i) add_basis(V, __ldg(V.leafList + R.leafListBegin + i), pos, sumWV, sumW);
+  if (sumW > 0.f) s.value = sumWV / sumW;
+  return s;
+}
+
 EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
 {
   if (A.amr) return amr_sample(*A.amr, pos);
+  if (A.bricks) return brick_sample(*A.bricks, pos, err);
   exa_sample s;
   s.primID = -1;
   s.cellID = -1;

@@ -748,9 +748,11 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
-    // the AMR-cell sampler renders shade mode default (renderFrame_AMRCellSampler, deviceCode.cu:1360-1364)
-    need(ctx->sampler->accel.amr == nullptr || (lp->shadeMode == EXA_SHADE_MODE_DEFAULT && !learned),
-         EXA_ERR_INVALID, "the AMR-cell sampler renders shade mode default with the exact field only");
+    // the AMR-cell and ExaBrick samplers render shade mode default
+    // (renderFrame_AMRCellSampler / _ExaBrickSampler, deviceCode.cu:1360-1387)
+    need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||
+             (lp->shadeMode == EXA_SHADE_MODE_DEFAULT && !learned),
+         EXA_ERR_INVALID, "the AMR-cell and ExaBrick samplers render shade mode default with the exact field only");
     setDevice(ctx);
     const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
     if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
@@ -825,7 +827,9 @@ const char *exa_sampler_class_name(void) { return "ExaStitchSampler"; }
 const char *exa_sampler_get_class_name(exa_context *ctx)
 {
   if (!ctx || !ctx->sampler) return "";
-  return dynamic_cast<AMRCellSampler *>(ctx->sampler.get()) ? "AMRCellSampler" : "ExaStitchSampler";
+  if (dynamic_cast<AMRCellSampler *>(ctx->sampler.get())) return "AMRCellSampler";
+  if (dynamic_cast<ExaBrickSampler *>(ctx->sampler.get())) return "ExaBrickSampler";
+  return "ExaStitchSampler";
 }
 
 int exa_context_create(exa_context **out, int device, uint64_t stream)
@@ -1043,6 +1047,85 @@ int exa_amrcell_model_load(exa_context *ctx, const char *cellsFile, const char *
   });
 }
 
+int exa_exabrick_model_create(exa_context *ctx, const exa_brick *bricks, uint64_t numBricks, const float *scalars,
+                              uint64_t numScalars)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    need(numBricks == 0 || bricks, EXA_ERR_INVALID, "bricks is null");
+    need(numScalars == 0 || scalars, EXA_ERR_INVALID, "scalars is null");
+    need(numBricks < 0x3fffffffull && numScalars <= 0xffffffffull, EXA_ERR_INVALID, "model too large");
+    auto m = std::make_shared<ExaBrickModel>();
+    m->assign(bricks, numBricks, scalars, numScalars);
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+// ExaBrickModel::load (model/ExaBrickModel.cpp:28-117): brick records until
+// the data runs out; every cell id must index the scalars file
+int exa_exabrick_model_load(exa_context *ctx, const char *bricksFile, const char *scalarsFile)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_INVALID, "null context");
+    const std::vector<char> d = readFile(bricksFile, true);
+    const std::vector<char> sv = readFile(scalarsFile, false);
+    const size_t numValues = sv.size() / sizeof(float);
+    std::vector<float> ordered(numValues);
+    if (numValues) std::memcpy(ordered.data(), sv.data(), numValues * sizeof(float));
+    std::vector<exa_brick> bricks;
+    std::vector<float> scalars;
+    size_t at = 0;
+    while (d.size() - at >= 7 * sizeof(int32_t)) {
+      int32_t h[7];
+      std::memcpy(h, d.data() + at, sizeof(h));
+      exa_brick b;
+      b.size = {h[0], h[1], h[2]};
+      b.lower = {h[3], h[4], h[5]};
+      b.level = h[6];
+      need(b.size.x > 0 && b.size.y > 0 && b.size.z > 0, EXA_ERR_INVALID, "bad brick size");
+      const uint64_t n = (uint64_t)b.size.x * b.size.y * b.size.z;
+      if (d.size() - at - sizeof(h) < n * sizeof(int32_t)) break;  // the loader stops at a short record
+      at += sizeof(h);
+      b.begin = (uint32_t)scalars.size();
+      for (uint64_t k = 0; k < n; ++k) {
+        int32_t id;
+        std::memcpy(&id, d.data() + at + k * sizeof(int32_t), sizeof(id));
+        need(id >= 0, EXA_ERR_INVALID, "negative cell ID");
+        need((size_t)id < numValues, EXA_ERR_INVALID, "invalid cell ID");
+        scalars.push_back(ordered[id]);
+      }
+      at += n * sizeof(int32_t);
+      need(scalars.size() <= 0xffffffffull, EXA_ERR_INVALID, "model too large");
+      bricks.push_back(b);
+    }
+    auto m = std::make_shared<ExaBrickModel>();
+    m->assign(bricks.data(), bricks.size(), scalars.data(), scalars.size());
+    ctx->model = m;
+    ctx->sampler.reset();
+  });
+}
+
+int exa_exabrick_get_abrs(exa_context *ctx, exa_abr *abrs, uint64_t *numAbrs, int32_t *leafList,
+                          uint64_t *leafListSize)
+{
+  return guarded([&] {
+    need(ctx && numAbrs && leafListSize, EXA_ERR_INVALID, "null argument");
+    auto *m = dynamic_cast<ExaBrickModel *>(ctx->model.get());
+    need(m != nullptr, EXA_ERR_STATE, "no ExaBrick model");
+    if (abrs) {
+      need(*numAbrs >= m->abrs.size(), EXA_ERR_INVALID, "region array too small");
+      std::memcpy(abrs, m->abrs.data(), m->abrs.size() * sizeof(exa_abr));
+    }
+    if (leafList) {
+      need(*leafListSize >= m->leafList.size(), EXA_ERR_INVALID, "leaf list array too small");
+      std::memcpy(leafList, m->leafList.data(), m->leafList.size() * sizeof(int32_t));
+    }
+    *numAbrs = m->abrs.size();
+    *leafListSize = m->leafList.size();
+  });
+}
+
 int exa_read_xf(const char *xfFile, exa_xf *xf, exa_vec4f *colors, int32_t maxColors)
 {
   return guarded([&] {
@@ -1244,6 +1327,13 @@ int exa_model_mem_stats(exa_context *ctx, exa_mem_stats *out)
       am->memStats(a, b);
       out->amrCellBytes = a;
       out->amrScalarBytes = b;
+    } else if (auto *bm = dynamic_cast<ExaBrickModel *>(ctx->model.get())) {
+      size_t a, b, c, d;
+      bm->memStats(a, b, c, d);
+      out->bricksBytes = a;
+      out->brickScalarsBytes = b;
+      out->abrsBytes = c;
+      out->abrLeafListBytes = d;
     }
     if (auto &S = ctx->sampler) {
       out->deviceFieldBytes = S->fieldBytes();
@@ -1267,6 +1357,8 @@ int exa_sampler_build(exa_context *ctx)
     std::shared_ptr<Sampler> s;
     if (dynamic_cast<AMRCellModel *>(ctx->model.get()))
       s = std::make_shared<AMRCellSampler>();
+    else if (dynamic_cast<ExaBrickModel *>(ctx->model.get()))
+      s = std::make_shared<ExaBrickSampler>();
     else
       s = std::make_shared<ExaStitchSampler>();
     if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, s->className() + "::build failed");

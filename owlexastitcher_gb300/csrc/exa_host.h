@@ -116,6 +116,19 @@ struct AMRCellModel : Model {
   void memStats(size_t &cellsBytes, size_t &scalarsBytes) const;  // AMRCellModel.cpp:69-73
 };
 
+// ExaBrickModel (model/ExaBrickModel.h:27-52): bricks of same-level cells
+// and their scalars; init() builds the active brick regions (ABRs::buildFrom,
+// model/ABRs.cpp:264-333), cellBounds and valueRange
+struct ExaBrickModel : Model {
+  std::vector<exa_brick> bricks;
+  std::vector<float> scalars;
+  std::vector<exa_abr> abrs;
+  std::vector<int32_t> leafList;
+  void assign(const exa_brick *b, size_t nb, const float *s, size_t ns);
+  void init();
+  void memStats(size_t &bricksBytes, size_t &scalarsBytes, size_t &abrsBytes, size_t &leafListBytes) const;
+};
+
 struct Sampler {  // sampler/Sampler.h:28-69
   virtual ~Sampler() = default;
   virtual bool build(std::shared_ptr<Model> model, cudaStream_t s) = 0;
@@ -193,6 +206,32 @@ class AMRCellSampler : public Sampler {
   DBuf<AmrCellView> deviceView;
 };
 
+// ExaBrickSampler (sampler/ExaBrickSampler.h:30-96, ExaBrickSampler.cpp) in
+// the majorant grid + DDA traversal mode: region point location by an LBVH
+// over the region domains (replacing the OptiX ABR BVH); the majorant grid
+// from every brick cell's basis support (Grid.cu:362-430)
+class ExaBrickSampler : public Sampler {
+ public:
+  bool build(std::shared_ptr<Model> model, cudaStream_t s) override;
+  void computeMaxOpacities(const exa_vec4f *colorMap, int numColors, exa_range1f xfRange, cudaStream_t s) override;
+  void setLPs(exa_launch_params &lp) override;
+  std::string className() override { return "ExaBrickSampler"; }
+  size_t fieldBytes() const override;
+  size_t accelBytes() const override;
+
+  std::shared_ptr<ExaBrickModel> model;
+  DBuf<exa_brick> brickBuffer;
+  DBuf<float> scalarBuffer;
+  DBuf<exa_abr> abrBuffer;
+  DBuf<int32_t> abrLeafListBuffer;
+  DBuf<float4> abrCorners;     // two corners per region: the BVH's vertex rows
+  DBuf<int32_t> abrRows;
+  DBuf<BvhNode> abrNodes;
+  DBuf<int32_t> abrParents, abrLeafElem;
+  BrickView view{};
+  DBuf<BrickView> deviceView;
+};
+
 // ---------------------------------------------------------------- kernels
 // launchers implemented in exa_build.cu / exa_render.cu
 void launchInitRanges(exa_range1f *r, size_t n, cudaStream_t s);
@@ -211,6 +250,10 @@ void launchAmrLevelBits(const exa_amr_cell *cells, size_t n, int level, const in
 void launchAmrLevelRank(const uint32_t *bits, size_t words, uint32_t *rank, cudaStream_t s);
 void launchAmrLevelCells(const exa_amr_cell *cells, size_t n, int level, const int lo[3], const int nl[3],
                          const uint32_t *bits, const uint32_t *rank, int32_t *cellOf, cudaStream_t s);
+// Grid.cu:399-430: every brick cell's value into the macrocells its basis
+// support projects onto
+void launchBrickMajorants(const exa_brick *bricks, size_t nb, const float *scalars, exa_vec3i dims, exa_box3f wb,
+                          exa_range1f *mcRanges, cudaStream_t s);
 void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf,
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,

@@ -181,3 +181,40 @@ class Dataset:
     def field_bytes(self):
         """Bytes of the ExaStitch field arrays (memStats total)."""
         return (self.vertices.nbytes + self.indices.nbytes + self.gridlets.nbytes + self.gridlet_scalars.nbytes)
+
+
+BRICK_DTYPE = np.dtype([("lower", "<i4", 3), ("size", "<i4", 3), ("level", "<i4"), ("begin", "<u4")])
+
+
+def amr_to_bricks(cells, scalars, max_len=8):
+    """ExaBricks (model/ABRs.h: same-level cell boxes with their scalars,
+    x fastest) from AMR leaf cells: per level, runs of consecutive cells
+    along x within 8-aligned segments of a row become bricks of size
+    (run, 1, 1).  Returns (bricks as BRICK_DTYPE, scalars in brick order)."""
+    cells = np.asarray(cells, np.int64).reshape(-1, 4)
+    scalars = np.asarray(scalars, np.float32)
+    out_b, out_s = [], []
+    begin = 0
+    for L in np.unique(cells[:, 3]):
+        sel = np.nonzero(cells[:, 3] == L)[0]
+        q = cells[sel, :3] >> int(L)
+        order = np.lexsort((q[:, 0], q[:, 1], q[:, 2]))
+        q, idx = q[order], sel[order]
+        cont = np.zeros(len(q), bool)
+        cont[1:] = ((q[1:, 2] == q[:-1, 2]) & (q[1:, 1] == q[:-1, 1]) & (q[1:, 0] == q[:-1, 0] + 1) &
+                    (q[1:, 0] // max_len == q[:-1, 0] // max_len))
+        starts = np.nonzero(~cont)[0]
+        lens = np.diff(np.append(starts, len(q)))
+        b = np.zeros(len(starts), BRICK_DTYPE)
+        b["lower"] = q[starts] << int(L)
+        b["size"][:, 0] = lens
+        b["size"][:, 1:] = 1
+        b["level"] = L
+        b["begin"] = begin + starts
+        begin += len(q)
+        out_b.append(b)
+        out_s.append(scalars[idx])
+    if not out_b:
+        return np.zeros(0, BRICK_DTYPE), np.zeros(0, np.float32)
+    return np.concatenate(out_b), np.concatenate(out_s)
+

@@ -105,8 +105,13 @@ class AmrCellLP(C.Structure):
     _fields_ = [("sampleBVH", C.c_uint64)]
 
 
+class ExaBrickLP(C.Structure):
+    _fields_ = [("sampleBVH", C.c_uint64), ("brickBuffer", C.c_void_p), ("abrBuffer", C.c_void_p),
+                ("scalarBuffer", C.c_void_p), ("abrLeafListBuffer", C.c_void_p)]
+
+
 class _SamplerUnion(C.Union):
-    _fields_ = [("ess", StitchLP), ("acs", AmrCellLP)]
+    _fields_ = [("ess", StitchLP), ("acs", AmrCellLP), ("ebs", ExaBrickLP)]
 
 
 class _TF(C.Structure):
@@ -187,7 +192,8 @@ class RenderStats(C.Structure):
 class MemStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "elemVertexBytes", "elemIndexBytes", "gridletBytes", "emptyScalarsBytes", "nonEmptyScalarsBytes",
-        "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes", "amrCellBytes", "amrScalarBytes")]
+        "deviceFieldBytes", "deviceAccelBytes", "deviceMajorantBytes", "amrCellBytes", "amrScalarBytes", "bricksBytes", "brickScalarsBytes",
+        "abrsBytes", "abrLeafListBytes")]
 
 
 class SurrogateParams(C.Structure):
@@ -248,6 +254,7 @@ EXPORTED = [
     "exa_read_grids", "exa_model_load", "exa_read_xf", "exa_xf_range", "exa_opacity_scale", "exa_read_cells",
     "exa_read_mesh", "exa_mesh_set", "exa_mesh_get_bounds",
     "exa_amrcell_model_create", "exa_amrcell_model_load", "exa_sampler_get_class_name",
+    "exa_exabrick_model_create", "exa_exabrick_model_load", "exa_exabrick_get_abrs",
 ]
 NOALLOC_MAX_SAMPLES = 1 << 20
 
@@ -317,6 +324,9 @@ def lib():
         "exa_amrcell_model_create": ([ctx_p, vp, u64, vp, u64], C.c_int),
         "exa_amrcell_model_load": ([ctx_p, C.c_char_p, C.c_char_p], C.c_int),
         "exa_sampler_get_class_name": ([ctx_p], C.c_char_p),
+        "exa_exabrick_model_create": ([ctx_p, vp, u64, vp, u64], C.c_int),
+        "exa_exabrick_model_load": ([ctx_p, C.c_char_p, C.c_char_p], C.c_int),
+        "exa_exabrick_get_abrs": ([ctx_p, vp, C.POINTER(u64), vp, C.POINTER(u64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -438,6 +448,32 @@ class AMRCellModel(_Model):
         return cls(ctx, ds.amr_cells, ds.amr_scalars)
 
 
+BRICK_DTYPE = np.dtype([("lower", "<i4", 3), ("size", "<i4", 3), ("level", "<i4"), ("begin", "<u4")])
+ABR_DTYPE = np.dtype([("domain", "<f4", 6), ("valueRange", "<f4", 2), ("leafListBegin", "<i4"),
+                      ("leafListSize", "<i4"), ("finestLevelCellWidth", "<f4")])
+
+
+class ExaBrickModel(_Model):
+    """model/ExaBrickModel.h:27-52: bricks of same-level cells (BRICK_DTYPE)
+    and their scalars; the active brick regions are built on creation."""
+
+    def __init__(self, ctx, bricks, scalars):
+        self.ctx = ctx
+        self.bricks = np.ascontiguousarray(bricks, BRICK_DTYPE)
+        self.scalars = np.ascontiguousarray(scalars, np.float32)
+        _check(lib().exa_exabrick_model_create(ctx.h, _np_ptr(self.bricks), len(self.bricks), _np_ptr(self.scalars),
+                                               len(self.scalars)))
+
+    def abrs(self):
+        """(regions as ABR_DTYPE, leaf list int32)"""
+        n, nl = C.c_uint64(), C.c_uint64()
+        _check(lib().exa_exabrick_get_abrs(self.ctx.h, None, C.byref(n), None, C.byref(nl)))
+        r = np.zeros(n.value, ABR_DTYPE)
+        leaf = np.zeros(nl.value, np.int32)
+        _check(lib().exa_exabrick_get_abrs(self.ctx.h, _np_ptr(r), C.byref(n), _np_ptr(leaf), C.byref(nl)))
+        return r, leaf
+
+
 class ExaStitchModel(_Model):
     """model/ExaStitchModel.h:26-55, built from in-memory arrays."""
 
@@ -524,6 +560,17 @@ class AMRCellSampler(ExaStitchSampler):
 
     def prim_majorants(self):
         raise ExaError(EXA_ERR_STATE, "the AMR-cell sampler has no per-primitive majorants")
+
+
+class ExaBrickSampler(ExaStitchSampler):
+    """sampler/ExaBrickSampler.h:30-96 (grid + DDA traversal, ABR sampling)."""
+
+    @staticmethod
+    def className():
+        return "ExaBrickSampler"
+
+    def prim_majorants(self):
+        raise ExaError(EXA_ERR_STATE, "the ExaBrick sampler has no per-primitive majorants")
 
 
 def new_launch_params():
