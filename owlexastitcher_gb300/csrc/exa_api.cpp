@@ -59,6 +59,13 @@ static exa_affine3f affine_mul_diag(const exa_affine3f &A, const exa_affine3f &B
 }
 
 // Model.cpp:35-48: voxel = voxelCoordSys * rcp(worldCoordSys)
+Model::Model()
+{
+  voxelSpaceTransform = affine_identity();
+  voxelSpaceTransformInv = affine_identity();
+  lightSpaceTransform = affine_identity();
+}
+
 void Model::setVoxelSpaceTransform(exa_box3f from, exa_box3f to)
 {
   voxelSpaceTransform = affine_mul_diag(affine_box(from, false), affine_box(to, true));

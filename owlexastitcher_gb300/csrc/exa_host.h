@@ -78,6 +78,7 @@ struct Grid {  // Grid.h:33-86
 };
 
 struct Model {  // model/Model.h:29-65
+  Model();  // identity voxel- and light-space transforms (Model.h:57-61)
   virtual ~Model() = default;
   void setNumGridCells(exa_vec3i numMCs);                     // Model.cpp:25-33
   void setVoxelSpaceTransform(exa_box3f from, exa_box3f to);  // Model.cpp:35-48

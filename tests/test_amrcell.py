@@ -127,6 +127,13 @@ class TestGpu:
         assert tT.cpu().numpy().tobytes() == htT.tobytes()
         assert tTr.cpu().numpy().tobytes() == htTr.tobytes()
         assert len(np.unique(hfb)) > 4
+        if integrator != 2:
+            assert (htT >= 0).mean() > 0.2      # rays interact with the volume
+        else:
+            # the march composites the volume over the background gradient
+            tb = (np.arange(h, dtype=np.float32) / h).repeat(w)
+            bg = np.stack([(1 - tb) + tb * 0.5, (1 - tb) + tb * 0.7, (1 - tb) + tb * 1.0], 1)
+            assert (np.abs(hacc[:, :3] / 2 - bg).max(1) > 1e-3).mean() > 0.2
 
     def test_load_from_files(self, scene, tmp_path):
         """AMRCellModel::load: '.cells' records and a raw float32 scalars file"""
