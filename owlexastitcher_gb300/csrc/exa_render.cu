@@ -346,6 +346,35 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
   return walk_collide(w, c, rng, shadow, s);
 }
 
+// The wavefront walk kernels' unit of work per loop iteration: up to
+// EXA_WF_ITER_STEPS steps, each with up to EXA_WF_ADVANCE_MAX macrocell
+// advances before its sample.  A lane's own sequence of operations (and so
+// its result) does not depend on these; they trade loop overhead against
+// divergence between lanes.  Measured on the 1024^2 x 16 spp medium
+// workload: 1 advance per iteration 182 M paths/s, 2: 218 M, 3: 231 M,
+// 4: 232 M, 6: 226 M, 8: 219 M, 64: 188 M; two steps per iteration no
+// better.
+#ifndef EXA_WF_ADVANCE_MAX
+#define EXA_WF_ADVANCE_MAX 4
+#endif
+#ifndef EXA_WF_ITER_STEPS
+#define EXA_WF_ITER_STEPS 1
+#endif
+EXA_D bool walk_iteration(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
+{
+  for (int k = 0; k < EXA_WF_ITER_STEPS; ++k) {
+    int st, a = 0;
+    do {
+      st = walk_advance(w, c, rng);
+    } while (st == WALK_ON && ++a < EXA_WF_ADVANCE_MAX);
+    if (st == WALK_END) return false;
+    if (st == WALK_ON) continue;
+    const exa_sample s = walk_sample_exact(w, c);
+    if (!walk_collide(w, c, rng, shadow, s)) return false;
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------------
 // renderFrame_Impl (deviceCode.cu:1268-1345) with directLightingIntegrate
 // (:1126-1207) or pathTracingIntegrate (:991-1120) and sampleLight
@@ -1325,7 +1354,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
       }
       break;
     }
-    const bool ended = active && !walk_step(L.w, c, L.rng, L.shadow);
+    const bool ended = active && !walk_iteration(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
       wf_store_event(L, Q.ev, Q.cap, slot, src);
@@ -1394,7 +1423,10 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     }
     bool ended = false;
     if (active && !pending) {
-      const int st = walk_advance(L.w, c, L.rng);
+      int st, a = 0;
+      do {
+        st = walk_advance(L.w, c, L.rng);
+      } while (st == WALK_ON && ++a < EXA_WF_ADVANCE_MAX);
       if (st == WALK_END) {
         ended = true;
       } else if (st == WALK_SAMPLE) {
@@ -1687,7 +1719,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
     bool ended = false;
     if (active) {
       PathCtx cf{*fa, *flp, 0u, c.counting};
-      ended = !walk_step(L.w, cf, L.rng, L.shadow);
+      ended = !walk_iteration(L.w, cf, L.rng, L.shadow);
       c.err |= cf.err;
     }
     const unsigned slot = warp_append(&Q.cnt[2], ended);
