@@ -1158,15 +1158,23 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
 }
 
 // shadow flag, RNG and the walk
-EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
+// A walk that has not taken a step yet (walk_begin's state) is stored
+// "fresh": flags, RNG, ray and DDA state (the first 21 of the 35 words); the
+// loader sets the rest to walk_begin's values.  (Storing only the ray and
+// re-running dda_init in the walk kernel saves more traffic but costs the
+// latency-bound walk kernel more than it saves.)
+constexpr uint32_t kWalkFresh = 0x80000000u;
+
+EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, bool fresh = false)
 {
   unsigned k = kPathStride;
   const Walk &w = L.w;
-  W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2));
+  W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2) | (fresh ? kWalkFresh : 0u));
   W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
   WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
   W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
+  if (fresh) return;
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z); WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
   WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
   W((uint32_t)w.primID); W((uint32_t)w.steps); W((uint32_t)w.ncells);
@@ -1180,7 +1188,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   const uint32_t flags = R();
   L.shadow = flags & 1u;
   w.needCell = (flags >> 1) & 1u;
-  w.type = (int)(flags >> 2);
+  w.type = (int)((flags & ~kWalkFresh) >> 2);
   const uint32_t lo = R(), hi = R();
   L.rng.key = ((uint64_t)hi << 32) | lo;
   L.rng.counter = R();
@@ -1193,6 +1201,16 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.dda.step.x = w.dir.x > 0.f ? 1 : -1; w.dda.step.y = w.dir.y > 0.f ? 1 : -1; w.dda.step.z = w.dir.z > 0.f ? 1 : -1;
   w.dda.stop.x = w.dir.x > 0.f ? G.dims.x : -1; w.dda.stop.y = w.dir.y > 0.f ? G.dims.y : -1;
   w.dda.stop.z = w.dir.z > 0.f ? G.dims.z : -1;
+  if (flags & kWalkFresh) {
+    w.pos = mk3(0.f, 0.f, 0.f);
+    w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.t = w.t1 = w.maj = 0.f;
+    w.Tr = 1.f;
+    w.primID = -1;
+    w.steps = 0;
+    w.ncells = 0;
+    return;
+  }
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
   w.t = RF(); w.t1 = RF(); w.maj = RF(); w.Tr = RF();
@@ -1240,10 +1258,11 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
 #undef R
 #undef RF
 
+// a lane that has just begun a walk
 EXA_D void wf_store(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
 {
   wf_store_path(L, b, cap, i);
-  wf_store_walk(L, b, cap, i);
+  wf_store_walk(L, b, cap, i, true);
 }
 
 EXA_D void wf_load(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width,
