@@ -330,7 +330,7 @@ struct Surrogate {
 };
 void launchSurrogatePoints(const SurrogateView &S, const exa_vec3f *pos, size_t n, float *out, cudaStream_t s);
 bool useWavefront();
-constexpr int kWfLaneWords = 67;
+constexpr int kWfLaneWords = 63;
 
 // ---------------------------------------------------------- batched frames
 struct WfFrame {                    // per frame of a batch (device table)

@@ -401,7 +401,6 @@ struct Lane {
   // after a primary walk, >= 0 only if the walk ended on that surface)
   int meshPrim = -1;
   float meshT = 0.f;
-  V3 meshNg = {0.f, 0.f, 0.f};
   float shadowMesh = -1.f; // shadow walk that reached a surface: max(0, N.l), else -1
   int phase;
   Rng rng;
@@ -496,9 +495,17 @@ struct Machine {
     if (h.primID >= 0) {
       L.meshPrim = h.primID;
       L.meshT = h.t;
-      L.meshNg = h.Ng;
       ray.tmax = fmin_t(ray.tmax, h.t);
     }
+  }
+
+  // the geometric normal of mesh triangle prim, as the closest hit computes
+  // it (path records keep the triangle, not its normal)
+  EXA_D V3 mesh_normal(int prim) const
+  {
+    const MeshView &M = *reinterpret_cast<const MeshView *>(lp.meshBVH);
+    const V3 a = tri_vertex(M, prim, 0), b = tri_vertex(M, prim, 1), c = tri_vertex(M, prim, 2);
+    return norm3(cross3(sub3(b, a), sub3(c, a)));
   }
 
   // sampleLight's mesh test (deviceCode.cu:897-904, 921-922)
@@ -565,8 +572,9 @@ struct Machine {
     V3 sd;
     if (L.meshPrim >= 0) {
       // the event was a surface: Lambertian BRDF (deviceCode.cu:1084-1087)
-      sd = lambertian_sample(L.meshNg, L.rng);
-      L.throughput = muls(L.throughput, fmaxf(0.f, dot3(sd, L.meshNg)));
+      const V3 Ng = mesh_normal(L.meshPrim);
+      sd = lambertian_sample(Ng, L.rng);
+      L.throughput = muls(L.throughput, fmaxf(0.f, dot3(sd, Ng)));
       L.pos = add3(L.pos, smul(16.f, norm3(sd)));
     } else {
       const V3 wo = mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z);
@@ -626,7 +634,8 @@ struct Machine {
       } else {
         V3 tp = mul3(mk3(1.f, 1.f, 1.f), L.albedo);
         // surfaces without lights: a headlight (deviceCode.cu:1196-1198)
-        if (surface) tp = muls(tp, fmaxf(0.f, dot3(mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z), L.meshNg)));
+        if (surface)
+          tp = muls(tp, fmaxf(0.f, dot3(mk3(-L.ray.dir.x, -L.ray.dir.y, -L.ray.dir.z), mesh_normal(L.meshPrim))));
         finish_sample(L, make_float4(tp.x, tp.y, tp.z, 1.f));
       }
     }
@@ -1087,8 +1096,9 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
 // + walk part (SoA: word k of record i at (kPathStride + k) * cap + i); the
 // walk kernel reads and writes only walk parts, and an ended walk leaves a
 // short event record that points at its path part.
-constexpr int kPathWords = 31;
-constexpr int kPathStride = 32;  // path words padded to whole 16-byte vectors
+constexpr int kPathWords = 28;
+constexpr int kPathStride = 28;  // path words padded to whole 16-byte vectors
+constexpr int kPathFrameWord = 24;  // light kind | frame << 1
 static_assert(kPathWords <= kPathStride && kPathStride % 4 == 0, "path part: whole uint4 vectors");
 constexpr int kWalkWords = 35;
 constexpr int kLaneWords = kPathStride + kWalkWords;
@@ -1104,6 +1114,12 @@ struct WfQueues {
 // a warp whose input is used up parks its unfinished walks in the next
 // round's input once fewer than this many of its lanes are still walking,
 // instead of stepping the round's longest walks with the other lanes idle
+// preferred shared-memory carveout of the walk kernel in percent (-1: the
+// driver's choice)
+#ifndef EXA_WALK_CARVEOUT
+#define EXA_WALK_CARVEOUT -1
+#endif
+
 #ifndef EXA_WF_PARK_LANES
 #define EXA_WF_PARK_LANES 28
 #endif
@@ -1121,15 +1137,14 @@ EXA_D void wf_store_path(const Lane &L, uint32_t *b, unsigned cap, unsigned i)
   (void)cap;
   uint4 *p = reinterpret_cast<uint4 *>(b + (size_t)i * kPathStride);
   const auto f = [](float v) { return __float_as_uint(v); };
-  p[0] = make_uint4((uint32_t)L.px, (uint32_t)L.py, (uint32_t)L.s, f(L.ray.org.x));
-  p[1] = make_uint4(f(L.ray.org.y), f(L.ray.org.z), f(L.ray.dir.x), f(L.ray.dir.y));
-  p[2] = make_uint4(f(L.ray.dir.z), f(L.ray.tmax), f(L.throughput.x), f(L.throughput.y));
-  p[3] = make_uint4(f(L.throughput.z), f(L.Ld.x), f(L.Ld.y), f(L.Ld.z));
-  p[4] = make_uint4(f(L.pos.x), f(L.pos.y), f(L.pos.z), f(L.albedo.x));
-  p[5] = make_uint4(f(L.albedo.y), f(L.albedo.z), L.bounce, f(L.lightDen));
-  p[6] = make_uint4(f(L.lightI), (L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1), (uint32_t)L.meshPrim,
-                    f(L.meshT));
-  p[7] = make_uint4(f(L.meshNg.x), f(L.meshNg.y), f(L.meshNg.z), f(L.shadowMesh));
+  p[0] = make_uint4((uint32_t)L.pixelID, (uint32_t)L.s, f(L.ray.org.x), f(L.ray.org.y));
+  p[1] = make_uint4(f(L.ray.org.z), f(L.ray.dir.x), f(L.ray.dir.y), f(L.ray.dir.z));
+  p[2] = make_uint4(f(L.ray.tmax), f(L.throughput.x), f(L.throughput.y), f(L.throughput.z));
+  p[3] = make_uint4(f(L.Ld.x), f(L.Ld.y), f(L.Ld.z), f(L.pos.x));
+  p[4] = make_uint4(f(L.pos.y), f(L.pos.z), f(L.albedo.x), f(L.albedo.y));
+  p[5] = make_uint4(f(L.albedo.z), L.bounce, f(L.lightDen), f(L.lightI));
+  p[6] = make_uint4((L.lightDirectional ? 1u : 0u) | ((uint32_t)L.frame << 1), (uint32_t)L.meshPrim, f(L.meshT),
+                    f(L.shadowMesh));
 }
 
 EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, int width)
@@ -1137,24 +1152,26 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   (void)cap;
   const uint4 *p = reinterpret_cast<const uint4 *>(b + (size_t)i * kPathStride);
   const uint4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3), q4 = __ldg(p + 4),
-              q5 = __ldg(p + 5), q6 = __ldg(p + 6), q7 = __ldg(p + 7);
+              q5 = __ldg(p + 5), q6 = __ldg(p + 6);
   const auto f = [](uint32_t v) { return __uint_as_float(v); };
-  L.px = (int)q0.x; L.py = (int)q0.y; L.s = (int)q0.z;
-  L.pixelID = L.px + width * L.py;
-  L.ray.org = mk3(f(q0.w), f(q1.x), f(q1.y));
-  L.ray.dir = mk3(f(q1.z), f(q1.w), f(q2.x));
-  L.ray.tmax = f(q2.y); L.ray.tmin = 0.f;
-  L.throughput = mk3(f(q2.z), f(q2.w), f(q3.x));
-  L.Ld = mk3(f(q3.y), f(q3.z), f(q3.w));
-  L.pos = mk3(f(q4.x), f(q4.y), f(q4.z));
-  L.albedo = mk3(f(q4.w), f(q5.x), f(q5.y));
-  L.bounce = q5.z; L.lightDen = f(q5.w); L.lightI = f(q6.x);
-  L.lightDirectional = (q6.y & 1u) != 0u;
-  L.frame = (int)(q6.y >> 1);
-  L.meshPrim = (int)q6.z;
-  L.meshT = f(q6.w);
-  L.meshNg = mk3(f(q7.x), f(q7.y), f(q7.z));
-  L.shadowMesh = f(q7.w);
+  L.pixelID = (int)q0.x; L.s = (int)q0.y;
+  if (width > 0) {  // (a batch's frame width is known only after the frame index)
+    L.py = (int)((unsigned)L.pixelID / (unsigned)width);
+    L.px = L.pixelID - L.py * width;
+  }
+  L.ray.org = mk3(f(q0.z), f(q0.w), f(q1.x));
+  L.ray.dir = mk3(f(q1.y), f(q1.z), f(q1.w));
+  L.ray.tmax = f(q2.x); L.ray.tmin = 0.f;
+  L.throughput = mk3(f(q2.y), f(q2.z), f(q2.w));
+  L.Ld = mk3(f(q3.x), f(q3.y), f(q3.z));
+  L.pos = mk3(f(q3.w), f(q4.x), f(q4.y));
+  L.albedo = mk3(f(q4.z), f(q4.w), f(q5.x));
+  L.bounce = q5.y; L.lightDen = f(q5.z); L.lightI = f(q5.w);
+  L.lightDirectional = (q6.x & 1u) != 0u;
+  L.frame = (int)(q6.x >> 1);
+  L.meshPrim = (int)q6.y;
+  L.meshT = f(q6.z);
+  L.shadowMesh = f(q6.w);
 }
 
 // shadow flag, RNG and the walk
@@ -1536,6 +1553,12 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
               "walk smem");
     cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk_sur, 128, kSurWalkSmem), "occupancy");
   } else {
+#if EXA_WALK_CARVEOUT >= 0
+    // the walk kernel needs little shared memory; the rest of the unified
+    // L1 / shared array serves as L1 for its field and table loads
+    cudaCheck(cudaFuncSetAttribute(k_wf_walk, cudaFuncAttributePreferredSharedMemoryCarveout, EXA_WALK_CARVEOUT),
+              "walk carveout");
+#endif
     cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk, 128, 0), "occupancy");
   }
   const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
@@ -1716,7 +1739,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
         if (idx < n) {
           wf_load_walk(L, in, Q.cap, idx, lp0.majorantGrid);
           // the frame index sits in the path part of the record
-          L.frame = (int)(__ldg(in + (size_t)idx * kPathStride + 25) >> 1);
+          L.frame = (int)(__ldg(in + (size_t)idx * kPathStride + kPathFrameWord) >> 1);
           flp = B.lps + L.frame;
           fa = B.accels + B.frames[L.frame].tf;
           active = true;
@@ -1765,7 +1788,8 @@ __global__ void __launch_bounds__(128) k_wfb_events(const __grid_constant__ Acce
     if (i < n) {
       wf_load_path(L, Q.buf[ctl->flip], Q.cap, wf_load_event(L, Q.ev, Q.cap, i), 0);
       const WfFrame F = B.frames[L.frame];
-      L.pixelID = L.px + F.width * L.py;
+      L.py = (int)((unsigned)L.pixelID / (unsigned)F.width);
+      L.px = L.pixelID - L.py * F.width;
       const exa_launch_params &flp = B.lps[L.frame];
       PathCtx cf{A, flp, 0u, c.counting};
       Machine<INTEGRATOR> M{cf, flp, F.width, F.height, num_lights(flp), (unsigned)flp.ext.maxBounces,
