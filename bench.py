@@ -172,9 +172,8 @@ def run_ours(a):
     from helpers import orbit_camera, ramp_tf, setup_render
     from owlexastitcher_gb300 import exastitch as E
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from owlexastitcher_gb300 import replicas
+    world, rank, local = replicas.world_from_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -193,7 +192,7 @@ def run_ours(a):
     cam = orbit_camera(lo, hi, a.width, a.height)
     setup_render(r.lp, cam, a.width, a.height, E.PATH_TRACING_INTEGRATOR, a.spp, "directional", True)
     r.lp.ext.maxBounces = a.bounces
-    r.lp.ext.frameID = rank  # independent frames per rank
+    r.lp.ext.frameID = replicas.frame_id(rank)  # independent frames per rank
     paths_per_step = a.width * a.height * a.spp
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -227,12 +226,8 @@ def run_ours(a):
     ctx.sync()
     render_stats = ctx.render_stats()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * paths_per_step / (ms / 1e3)
+    ms = replicas.slowest_ms(sum(step_ms) / len(step_ms), world, device="cuda")
+    value = replicas.job_paths_per_s(world, paths_per_step, ms)
     clocks = clk.summary()
 
     # counting launch (same frame): algorithmic work of one launch
