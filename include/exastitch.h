@@ -142,6 +142,7 @@ typedef struct {
 
 #define EXA_SHADE_MODE_DEFAULT  0       /* common.h:50-52 */
 #define EXA_SHADE_MODE_GRIDLETS 1
+#define EXA_SHADE_MODE_TEASER   2
 
 #define EXA_LIGHT_POINT       0
 #define EXA_LIGHT_DIRECTIONAL 1
@@ -174,6 +175,8 @@ typedef struct {
                              /* if the ray left the volume                  */
   float    *traceTr;         /* optional, per pixel: transmittance of the   */
                              /* first sample's first shadow ray, -1 if none */
+  uint32_t *heatCounts;      /* set by the library: per-pixel work of the   */
+                             /* heat map (render.heatMapEnabled)            */
 } exa_lp_ext;
 
 /* LaunchParams.h:56-119, field order and types kept; the sampler union

@@ -1314,6 +1314,8 @@ typedef struct {
   const oc_field *f;
   const exa_launch_params *lp;
   uint32_t err;
+  int px, py, width, height;  /* the pixel being rendered (Teaser shade mode) */
+  uint64_t work;              /* heat map: DDA cells of the walks, march positions */
 } rctx;
 
 /* deviceCode.cu:320-341, buffer variant */
@@ -1387,6 +1389,31 @@ static v4 classify(const rctx *c, exa_sample s)
       col = (iz % 2 == 0) ? col : !col;
       if (col == 0) { xf.x = 1.f; xf.y = 1.f; xf.z = 1.f; }
       else { xf.x = 0.f; xf.y = 0.f; xf.z = 0.7f; }
+    }
+  } else if (c->lp->shadeMode == EXA_SHADE_MODE_TEASER) {
+    /* deviceCode.cu:652-695: the TF colour and the checker colour blended
+     * across a screen-space diagonal band */
+    v3 rgb2;
+    if (s.cellID == -1) rgb2 = mk3(1.f, 0.f, 0.f);
+    else {
+      const exa_gridlet *g = &c->f->gridlets[s.primID];
+      const int ix = s.cellID % g->dims.x;
+      const int iy = s.cellID / g->dims.x % g->dims.y;
+      const int iz = s.cellID / (g->dims.x * g->dims.y);
+      int col = (ix % 2 == iy % 2);
+      col = (iz % 2 == 0) ? col : !col;
+      rgb2 = col == 0 ? mk3(1.f, 1.f, 1.f) : mk3(0.f, 0.f, .7f);
+    }
+    const v3 rgb1 = mk3(xf.x, xf.y, xf.z);
+    const float u = (float)c->px / (float)c->width, v = (float)c->py / (float)c->height;
+    const float A = .6f - .4f, B = .4f - .6f;
+    const float C1 = A * .4f + B * .6f, C2 = A * .6f + B * .4f, C = A * u + B * v;
+    if (C <= C1) { xf.x = rgb1.x; xf.y = rgb1.y; xf.z = rgb1.z; }
+    else if (C >= C2) { xf.x = rgb2.x; xf.y = rgb2.y; xf.z = rgb2.z; }
+    else {
+      xf.x = (rgb1.x * (C2 - C) + rgb2.x * (C - C1)) / (C2 - C1);
+      xf.y = (rgb1.y * (C2 - C) + rgb2.y * (C - C1)) / (C2 - C1);
+      xf.z = (rgb1.z * (C2 - C) + rgb2.z * (C - C1)) / (C2 - C1);
     }
   }
   return xf;
@@ -1523,6 +1550,7 @@ static int sample_interaction(rctx *c, ray_t ray, int shadow, v3 *posOut,
     if (done) break;
     if (!dda_next(&dda)) break;
   }
+  c->work += (uint64_t)ncells;
   *posOut = xfm_point(&lp->ext.voxelSpaceTransformInv, pos);
   *TrOut = Tr;
   *xfOut = xf;
@@ -1812,6 +1840,7 @@ static v4 ray_march(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights)
   v4 acc = {0.f, 0.f, 0.f, 0.f};
   for (long long k = 0; t <= t1; t += dt, ++k) {
     if (k >= OC_MARCH_CAP) { c->err |= EXA_DEVERR_TRACK_CAP; break; }
+    c->work++;
     const v3 pos = add3(org, muls(vd, t));
     const exa_sample smp = oc_sample(c->f, pos, cull);
     if (smp.primID < 0) continue;
@@ -1837,6 +1866,9 @@ static v4 ray_march(rctx *c, ray_t ray, oc_rng *rng, v4 bg, int numLights)
   return out;
 }
 
+/* __saturatef: clamp to [0, 1], NaN to 0 */
+static inline float sat_f(float x) { return x > 0.f ? (x < 1.f ? x : 1.f) : 0.f; }
+
 static inline uint32_t make_8bit(float f)
 {
   return (uint32_t)imin_t(255, imax_t(0, (int)(f * 256.f)));
@@ -1858,7 +1890,14 @@ static void render_pixel(rctx *c, int width, int height, int px, int py)
     oc_rng_init(&rng, (uint32_t)pixelID, (uint32_t)lp->accumID, lp->ext.frameID, (uint32_t)s);
     const float rx = oc_rng_next(&rng);
     const float ry = oc_rng_next(&rng);
-    const float sx = (float)px + rx, sy = (float)py + ry;
+    float sx = (float)px + rx, sy = (float)py + ry;
+    if (lp->subImage.active) {  /* deviceCode.cu:1286-1294 */
+      const float W = (float)width, H = (float)height;
+      sx = sx / W; sy = sy / H;
+      sx = (1.f - sx) * lp->subImage.value.lower.x + sx * lp->subImage.value.upper.x;
+      sy = (1.f - sy) * lp->subImage.value.lower.y + sy * lp->subImage.value.upper.y;
+      sx *= W; sy *= H;
+    }
     /* generateRay, deviceCode.cu:88-101 */
     v3 dir = add3(add3(lp->camera.dir_00, smul(sx, lp->camera.dir_du)), smul(sy, lp->camera.dir_dv));
     dir = norm3(dir);
@@ -1875,6 +1914,19 @@ static void render_pixel(rctx *c, int width, int height, int px, int py)
       col = direct_light(c, ray, &rng, bg, numLights, s == 0 ? &tHit : NULL, s == 0 ? &trv : NULL);
     acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
   }
+  if (lp->render.heatMapEnabled) {
+    /* deviceCode.cu:1323-1327 with the pixel's work in place of its clock
+     * cycles; temperature_to_rgb / hue_to_rgb (:155-170) */
+    const float t = (float)c->work * (lp->render.heatMapScale / (float)lp->render.spp);
+    const float K = 4.0f / 6.0f;
+    const float hue = K - K * t, v = .5f + 0.5f * t;
+    const float sh = sat_f(hue) * 6.0f;
+    const float r = sat_f(fabsf(sh - 3.f) - 1.0f), g = sat_f(2.0f - fabsf(sh - 2.0f)), b = sat_f(2.0f - fabsf(sh - 4.0f));
+    acc.x = v * r + (1.f - .5f) * acc.x;
+    acc.y = v * g + (1.f - .5f) * acc.y;
+    acc.z = v * b + (1.f - .5f) * acc.z;
+    acc.w = .5f + (1.f - .5f) * acc.w;
+  }
   if (lp->accumID > 0 && lp->accumBuffer) {
     const v4 o = lp->accumBuffer[pixelID];
     acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
@@ -1882,6 +1934,15 @@ static void render_pixel(rctx *c, int width, int height, int px, int py)
   if (lp->accumBuffer) lp->accumBuffer[pixelID] = acc;
   const float inv = 1.f / (float)(lp->accumID + 1);
   acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+  if (lp->subImage.selecting) {  /* deviceCode.cu:1337-1342 */
+    const int lx = imin_t(imax_t((int)(lp->subImage.selection.lower.x * (float)width), 0), width - 1);
+    const int ly = imin_t(imax_t((int)(lp->subImage.selection.lower.y * (float)height), 0), height - 1);
+    const int hx = imin_t(imax_t((int)(lp->subImage.selection.upper.x * (float)width), 0), width - 1);
+    const int hy = imin_t(imax_t((int)(lp->subImage.selection.upper.y * (float)height), 0), height - 1);
+    if (((px == lx || px == hx) && py >= ly && py <= hy) || ((py == ly || py == hy) && px >= lx && px <= hx)) {
+      acc.x = 1.f - acc.x; acc.y = 1.f - acc.y; acc.z = 1.f - acc.z; acc.w = 1.f - acc.w;
+    }
+  }
   const float is = 1.f / (float)lp->render.spp;
   const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) |
                         (make_8bit(acc.z * is) << 16) | (make_8bit(acc.w * is) << 24);
@@ -1900,7 +1961,7 @@ uint32_t oc_render(const oc_field *f, const exa_launch_params *lp, int width,
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : err)
 #endif
   for (int64_t p = pb; p < pe; ++p) {
-    rctx c = {f, lp, 0};
+    rctx c = {f, lp, 0, (int)(p % width), (int)(p / width), width, height, 0};
     render_pixel(&c, width, height, (int)(p % width), (int)(p / width));
     err |= c.err;
   }

@@ -637,6 +637,7 @@ struct exa_context {
   exa_render_stats lastStats{};
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
+  DBuf<uint32_t> heat;       // heat map: per-pixel work of the frame
   std::unique_ptr<Surrogate> surrogate;
   float surrogateTol = 0.f;
   std::unique_ptr<struct BatchState> batch;
@@ -743,9 +744,15 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
          EXA_ERR_INVALID, "integrator not supported");
     need(lp->integrator != EXA_RAY_MARCHING_INTEGRATOR || (lp->render.dt > 0.f && std::isfinite(lp->render.dt)),
          EXA_ERR_INVALID, "ray marching needs render.dt > 0");
-    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS, EXA_ERR_INVALID,
-         "shade mode not supported");
-    need(!lp->subImage.active && !lp->render.heatMapEnabled, EXA_ERR_INVALID, "sub-image / heat map not supported");
+    need(lp->shadeMode == EXA_SHADE_MODE_DEFAULT || lp->shadeMode == EXA_SHADE_MODE_GRIDLETS ||
+             lp->shadeMode == EXA_SHADE_MODE_TEASER,
+         EXA_ERR_INVALID, "shade mode not supported");
+    // the non-wavefront build renders path tracing and direct lighting
+    // without these (the ray marcher and the wavefront renderer have them)
+    const bool wavefrontOrMarch = useWavefront() || learned || lp->integrator == EXA_RAY_MARCHING_INTEGRATOR;
+    need(wavefrontOrMarch || (!lp->subImage.active && !lp->render.heatMapEnabled &&
+                              lp->shadeMode != EXA_SHADE_MODE_TEASER),
+         EXA_ERR_INVALID, "sub-image, heat map and the teaser shade mode need the wavefront renderer");
     need(lp->meshBVH == 0 || (ctx->mesh && lp->meshBVH == (uint64_t)(uintptr_t)ctx->mesh->view.ptr), EXA_ERR_INVALID,
          "lp.meshBVH is not this context's mesh (call exa_mesh_set and exa_sampler_set_lps)");
     need(lp->meshBVH == 0 || useWavefront() || learned || lp->integrator == EXA_RAY_MARCHING_INTEGRATOR,
@@ -764,6 +771,13 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
     if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
     exa_launch_params lpUse = *lp;
+    lpUse.ext.heatCounts = nullptr;
+    if (lp->render.heatMapEnabled) {
+      // per-pixel work of this frame for the heat map
+      if (ctx->heat.count < (size_t)width * height) ctx->heat.alloc((size_t)width * height);
+      cudaCheck(cudaMemsetAsync(ctx->heat.ptr, 0, (size_t)width * height * sizeof(uint32_t), ctx->stream), "heat");
+      lpUse.ext.heatCounts = ctx->heat.ptr;
+    }
     SurrogateView sv{};
     if (learned) {
       Surrogate *S = ctx->surrogate.get();
@@ -797,7 +811,8 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
       ctx->lastStats.eventMs = st.eventMs;
     } else {
       ctx->lastStats = exa_render_stats{};
-      launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr, ctx->stream);
+      launchRender(ctx->sampler->accel, lpUse, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr,
+                   ctx->stream);
     }
   }
 }

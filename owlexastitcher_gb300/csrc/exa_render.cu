@@ -66,6 +66,58 @@ EXA_D bool box_test(const RayS &r, const exa_box3f &b, float &t0, float &t1)
   return t0 < t1;
 }
 
+// generateRay (deviceCode.cu:88-101) for the jittered screen position
+// (px + rx, py + ry), remapped into the sub-image window when one is active
+// (renderFrame_Impl, deviceCode.cu:1286-1294)
+EXA_D V3 camera_dir(const exa_launch_params &lp, int px, int py, float rx, float ry, int width, int height)
+{
+  float sx = (float)px + rx, sy = (float)py + ry;
+  if (lp.subImage.active) {
+    const float W = (float)width, H = (float)height;
+    sx = __fdiv_rn(sx, W);
+    sy = __fdiv_rn(sy, H);
+    sx = (1.f - sx) * lp.subImage.value.lower.x + sx * lp.subImage.value.upper.x;
+    sy = (1.f - sy) * lp.subImage.value.lower.y + sy * lp.subImage.value.upper.y;
+    sx *= W;
+    sy *= H;
+  }
+  V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
+  dir = norm3(dir);
+  if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
+  if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
+  if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+  return dir;
+}
+
+// the gridlet checker of the Gridlets and Teaser shade modes
+// (deviceCode.cu:635-649, 655-670): 0 stitching element (red), 1 white,
+// 2 blue cell
+EXA_D int checker_index(const AccelView &A, const exa_sample &s)
+{
+  if (s.cellID == -1) return 0;
+  const exa_gridlet g = A.gridlets[s.primID];
+  const int ix = s.cellID % g.dims.x, iy = s.cellID / g.dims.x % g.dims.y, iz = s.cellID / (g.dims.x * g.dims.y);
+  int col = (ix % 2 == iy % 2);
+  col = (iz % 2 == 0) ? col : !col;
+  return col == 0 ? 1 : 2;
+}
+
+// the Teaser shade mode's colour (deviceCode.cu:652-695): the TF colour
+// rgb1 on one side of a screen-space diagonal band, the checker colour on
+// the other, blended across the band
+EXA_D V3 teaser_rgb(V3 rgb1, int checker, int px, int py, int width, int height)
+{
+  const V3 rgb2 = checker == 0 ? mk3(1.f, 0.f, 0.f) : (checker == 1 ? mk3(1.f, 1.f, 1.f) : mk3(0.f, 0.f, .7f));
+  const float u = __fdiv_rn((float)px, (float)width), v = __fdiv_rn((float)py, (float)height);
+  const float A = .6f - .4f, B = .4f - .6f;
+  const float C1 = A * .4f + B * .6f, C2 = A * .6f + B * .4f, C = A * u + B * v;
+  if (C <= C1) return rgb1;
+  if (C >= C2) return rgb2;
+  return mk3(__fdiv_rn(rgb1.x * (C2 - C) + rgb2.x * (C - C1), C2 - C1),
+             __fdiv_rn(rgb1.y * (C2 - C) + rgb2.y * (C - C1), C2 - C1),
+             __fdiv_rn(rgb1.z * (C2 - C) + rgb2.z * (C - C1), C2 - C1));
+}
+
 // deviceCode.cu:625-651 (Default, Gridlets)
 EXA_D float4 classify(const AccelView &A, const exa_launch_params &lp, const exa_sample &s)
 {
@@ -351,6 +403,10 @@ EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const 
     if (sigmaT * scale >= u * w.maj) {
       w.Tr = 0.f;
       w.type = SCATTERING;
+      // the Teaser shade mode blends the albedo by screen position at the
+      // event; the walk passes on the sample's checker colour in xf.w,
+      // which the event does not read otherwise
+      if (lp.shadeMode == EXA_SHADE_MODE_TEASER) w.xf.w = (float)checker_index(c.A, s);
       return false;
     }
   } else {
@@ -481,12 +537,7 @@ struct Machine {
     }
     const float rx = L.rng.next();
     const float ry = L.rng.next();
-    const float sx = (float)L.px + rx, sy = (float)L.py + ry;
-    V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
-    dir = norm3(dir);
-    if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
-    if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
-    if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+    const V3 dir = camera_dir(lp, L.px, L.py, rx, ry, width, height);
     L.ray.org = mk3(lp.camera.org);
     L.ray.dir = dir;
     L.ray.tmin = 0.f;
@@ -621,7 +672,11 @@ struct Machine {
     // first interaction of the pixel's first sample: its free-flight distance
     if (L.s == 0 && L.bounce == 0 && L.w.type == SCATTERING && lp.ext.traceT) lp.ext.traceT[L.pixelID] = L.w.t;
     L.pos = xfm_point(lp.ext.voxelSpaceTransformInv, L.w.pos);
-    const float4 xf = L.w.xf;
+    float4 xf = L.w.xf;
+    if (lp.shadeMode == EXA_SHADE_MODE_TEASER && L.w.type == SCATTERING) {
+      const V3 rgb = teaser_rgb(mk3(xf.x, xf.y, xf.z), (int)xf.w, L.px, L.py, width, height);
+      xf.x = rgb.x; xf.y = rgb.y; xf.z = rgb.z;
+    }
     const bool surface = L.w.type == BOUNDARY && L.meshPrim >= 0;
     if (!surface) L.meshPrim = -1;  // scatter() reads it as "the event was a surface"
     // a surface event (deviceCode.cu:1056-1059, 1182-1185): just past the hit, albedo kd = 0.8
@@ -945,7 +1000,9 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_pixel(con
 // Clip planes and surface meshes are not part of this path.
 constexpr long long kMarchCap = 1ll << 24;  // samples per ray
 
-EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int height, int numLights)
+// steps: the march's sample positions (the heat map's work measure)
+EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int width, int height, int numLights,
+                             unsigned &steps)
 {
   const exa_launch_params &lp = c.lp;
   Rng rng;
@@ -954,12 +1011,8 @@ EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int
   const float4 bg = make_float4((1.f - tb) * 1.f + tb * 0.5f, (1.f - tb) * 1.f + tb * 0.7f, (1.f - tb) * 1.f + tb * 1.f, 1.f);
   const float rx = rng.next();
   const float ry = rng.next();
-  const float sx = (float)px + rx, sy = (float)py + ry;
-  V3 dir = add3(add3(mk3(lp.camera.dir_00), smul(sx, mk3(lp.camera.dir_du))), smul(sy, mk3(lp.camera.dir_dv)));
-  dir = norm3(dir);
-  if (fabsf(dir.x) < 1e-5f) dir.x = 1e-5f;
-  if (fabsf(dir.y) < 1e-5f) dir.y = 1e-5f;
-  if (fabsf(dir.z) < 1e-5f) dir.z = 1e-5f;
+  const V3 dir = camera_dir(lp, px, py, rx, ry, width, height);
+  steps = 0;
   RayS ray;
   ray.org = mk3(lp.camera.org);
   ray.dir = dir;
@@ -995,6 +1048,7 @@ EXA_D float4 raymarch_sample(PathCtx &c, int px, int py, int pixelID, int s, int
         c.err |= EXA_DEVERR_TRACK_CAP;
         break;
       }
+      ++steps;
       const V3 pos = add3(org, muls(vd, t));
       const exa_sample smp = sample_field(c.A, pos, cull, c.err);
       if (smp.primID < 0) continue;
@@ -1039,7 +1093,9 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_march(con
   PathCtx c = make_ctx(A, lp);
   if (px < width && py < height) {
     const int pixelID = px + width * py;
-    colors[(size_t)pixelID * spp + s] = raymarch_sample(c, px, py, pixelID, s, height, num_lights(lp));
+    unsigned steps;
+    colors[(size_t)pixelID * spp + s] = raymarch_sample(c, px, py, pixelID, s, width, height, num_lights(lp), steps);
+    if (lp.render.heatMapEnabled && lp.ext.heatCounts) atomicAdd(lp.ext.heatCounts + pixelID, steps);
     cnt_add(c, CNT_PATHS);
     if (s == 0) {
       if (lp.ext.traceT) lp.ext.traceT[pixelID] = -1.f;
@@ -1080,6 +1136,19 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_render_sample(co
 
 // renderFrame_Impl (deviceCode.cu:1283-1344) after the spp loop: sum the
 // pixel's samples in order, progressive accumulation, RGBA8 output
+// temperature_to_rgb / hue_to_rgb (deviceCode.cu:155-170)
+EXA_D V3 heat_map(float t)
+{
+  const float K = 4.0f / 6.0f;
+  const float hue = K - K * t;
+  const float v = .5f + 0.5f * t;
+  const float s = __saturatef(hue) * 6.0f;
+  const float r = __saturatef(fabsf(s - 3.f) - 1.0f);
+  const float g = __saturatef(2.0f - fabsf(s - 2.0f));
+  const float b = __saturatef(2.0f - fabsf(s - 4.0f));
+  return mk3(v * r, v * g, v * b);
+}
+
 __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int width, int height,
                           const float4 *__restrict__ colors)
 {
@@ -1092,6 +1161,17 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
     const float4 col = __ldg(cp + s);
     acc.x += col.x; acc.y += col.y; acc.z += col.z; acc.w += col.w;
   }
+  if (lp.render.heatMapEnabled && lp.ext.heatCounts) {
+    // the heat map over the pixel's samples (deviceCode.cu:1323-1327): the
+    // pixel's work (DDA cells of its walks; march positions of the ray
+    // marcher) in place of the reference's clock cycles
+    const float t = (float)lp.ext.heatCounts[pixelID] * __fdiv_rn(lp.render.heatMapScale, (float)spp);
+    const V3 h = heat_map(t);
+    acc.x = h.x + (1.f - .5f) * acc.x;
+    acc.y = h.y + (1.f - .5f) * acc.y;
+    acc.z = h.z + (1.f - .5f) * acc.z;
+    acc.w = .5f + (1.f - .5f) * acc.w;
+  }
   if (lp.accumID > 0 && lp.accumBuffer) {
     const float4 o = reinterpret_cast<const float4 *>(lp.accumBuffer)[pixelID];
     acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
@@ -1099,6 +1179,17 @@ __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int widt
   if (lp.accumBuffer) reinterpret_cast<float4 *>(lp.accumBuffer)[pixelID] = acc;
   const float inv = __fdiv_rn(1.f, (float)(lp.accumID + 1));
   acc.x *= inv; acc.y *= inv; acc.z *= inv; acc.w *= inv;
+  if (lp.subImage.selecting) {
+    // the selection window's border, inverted (deviceCode.cu:1337-1342)
+    const int px = pixelID % width, py = pixelID / width;
+    const int lx = min(max((int)(lp.subImage.selection.lower.x * (float)width), 0), width - 1);
+    const int ly = min(max((int)(lp.subImage.selection.lower.y * (float)height), 0), height - 1);
+    const int hx = min(max((int)(lp.subImage.selection.upper.x * (float)width), 0), width - 1);
+    const int hy = min(max((int)(lp.subImage.selection.upper.y * (float)height), 0), height - 1);
+    if (((px == lx || px == hx) && py >= ly && py <= hy) || ((py == ly || py == hy) && px >= lx && px <= hx)) {
+      acc.x = 1.f - acc.x; acc.y = 1.f - acc.y; acc.z = 1.f - acc.z; acc.w = 1.f - acc.w;
+    }
+  }
   const float is = __fdiv_rn(1.f, (float)spp);
   const uint32_t rgba = make_8bit(acc.x * is) | (make_8bit(acc.y * is) << 8) | (make_8bit(acc.z * is) << 16) |
                         (make_8bit(acc.w * is) << 24);
@@ -1271,7 +1362,7 @@ EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, 
 {
   unsigned k = 0;
   const Walk &w = L.w;
-  W((uint32_t)L.shadow | ((uint32_t)w.type << 2));
+  W((uint32_t)L.shadow | ((uint32_t)w.type << 2) | ((uint32_t)w.ncells << 8));
   W(src);
   W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
   WF(w.t); WF(w.Tr);
@@ -1286,7 +1377,8 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
   Walk &w = L.w;
   const uint32_t flags = R();
   L.shadow = flags & 1u;
-  w.type = (int)(flags >> 2);
+  w.type = (int)((flags >> 2) & 0x3fu);
+  w.ncells = (int)(flags >> 8);
   const unsigned src = R();
   const uint32_t lo = R(), hi = R();
   L.rng.key = ((uint64_t)hi << 32) | lo;
@@ -1543,6 +1635,7 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
     bool tracking = false;
     if (i < n) {
       wf_load_path(L, Q.in, Q.cap, wf_load_event(L, Q.ev, Q.cap, i), width);
+      if (lp.render.heatMapEnabled && lp.ext.heatCounts) atomicAdd(lp.ext.heatCounts + L.pixelID, (unsigned)L.w.ncells);
       L.phase = PH_TRACK;
       if (L.shadow) M.shadow_done(L);
       else M.primary_done(L);

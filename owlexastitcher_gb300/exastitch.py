@@ -31,6 +31,7 @@ DIRECT_LIGHT_INTEGRATOR = 1
 RAY_MARCHING_INTEGRATOR = 2
 SHADE_MODE_DEFAULT = 0
 SHADE_MODE_GRIDLETS = 1
+SHADE_MODE_TEASER = 2
 LIGHT_POINT = 0
 LIGHT_DIRECTIONAL = 1
 
@@ -151,6 +152,7 @@ class LPExt(C.Structure):
         ("stepCounters", C.c_void_p),
         ("traceT", C.c_void_p),
         ("traceTr", C.c_void_p),
+        ("heatCounts", C.c_void_p),
     ]
 
 

@@ -359,3 +359,44 @@ def test_mesh_rejected_where_unsupported(scenes, torch_cuda):
         E.set_mesh(g.ctx, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
         g.sampler.setLPs(g.lp)
     assert g.lp.meshBVH == 0
+
+
+@pytest.mark.parametrize("feature,integrator", [
+    ("subimage", 0), ("subimage", 1), ("subimage", 2),
+    ("selecting", 1),
+    ("teaser", 0), ("teaser", 1),
+    ("heatmap", 0), ("heatmap", 1), ("heatmap", 2),
+])
+def test_render_features_bit_exact(scenes, torch_cuda, feature, integrator):
+    """The sub-image window and its selection border (deviceCode.cu:114-142,
+    1286-1294, 1337-1342), the Teaser shade mode (:652-695) and the heat map
+    (:155-177, 1323-1327; here the pixel's walk DDA cells or march positions
+    stand in for its clock cycles)."""
+    ds, g, o = scenes
+    lp = g.lp
+    if feature == "subimage":
+        lp.subImage.active = 1
+        lp.subImage.value.lower.x, lp.subImage.value.lower.y = 0.25, 0.3
+        lp.subImage.value.upper.x, lp.subImage.value.upper.y = 0.7, 0.85
+    elif feature == "selecting":
+        lp.subImage.selecting = 1
+        lp.subImage.selection.lower.x, lp.subImage.selection.lower.y = 0.2, 0.25
+        lp.subImage.selection.upper.x, lp.subImage.selection.upper.y = 0.8, 0.6
+    elif feature == "teaser":
+        lp.shadeMode = 2
+    else:
+        lp.render.heatMapEnabled = 1
+        lp.render.heatMapScale = 0.02
+    lp.render.dt = 0.5
+    try:
+        fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, 40, 32, integrator, 2, "point",
+                                                              integrator == 0, frames=2)
+    finally:
+        lp.subImage.active = lp.subImage.selecting = 0
+        lp.shadeMode = 0
+        lp.render.heatMapEnabled = 0
+        lp.render.dt = 1.0
+    assert np.array_equal(fb, hfb)
+    assert acc.tobytes() == hacc.tobytes()
+    assert tT.tobytes() == htT.tobytes()
+    assert len(np.unique(fb)) > 4
