@@ -287,6 +287,10 @@ def run_ours(a):
     q_e2e = 5 * len(P) / (time.perf_counter() - t0)
     ctx.sync()
 
+    majorants = None
+    if rank == 0 and not a.profile_only:
+        majorants = majorant_build(ds, local, NUM_MCS, peak, peak_kind)
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
@@ -336,6 +340,7 @@ def run_ours(a):
             "clocks": clocks,
             "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
             "render": render_stats,
+            "majorant_build": majorants,
             "learned_field": learned,
             "batched_frames": batched,
             "small_config": small,
@@ -347,6 +352,36 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def majorant_build(ds, local, num_mcs, peak, peak_kind, reps=3):
+    """Grid::build on the workload's field and majorant grid: the GPU times
+    of the gridlet and element value-range kernels from the build's own CUDA
+    events (median of `reps` builds after one untimed build; each build
+    uploads the field first, so the scalars are not L2-resident), with the
+    gridlet kernel's roofline.  Algorithmic bytes of that kernel: 4 B per
+    corner scalar and 32 B per gridlet header read, 8 B per gridlet range
+    and 8 B per macrocell range written."""
+    from owlexastitcher_gb300 import exastitch as E
+    ctx = E.Context(local)
+    model = E.ExaStitchModel.from_dataset(ctx, ds)
+    model.setNumGridCells(num_mcs)
+    sampler = E.ExaStitchSampler(ctx)
+    stats = []
+    for _ in range(reps + 1):
+        sampler.build(model)
+        stats.append(ctx.build_stats())
+    ctx.close()
+    stats = stats[1:]
+    g_ms = statistics.median(s["gridletMajorantMs"] for s in stats)
+    n_mc = int(np.prod(num_mcs))
+    alg = 4 * int(ds.stats["numGridletScalars"]) + 40 * int(ds.stats["numGridlets"]) + 8 * n_mc
+    achieved = alg / (g_ms / 1e3) / 1e9
+    return {"kernel": "k_gridlet_majorants", "majorant_grid": list(num_mcs), "gpu_ms": g_ms,
+            "elem_kernel_ms": statistics.median(s["elemMajorantMs"] for s in stats),
+            "build_total_ms": statistics.median(s["totalMs"] for s in stats), "blocks": stats[0]["majorantBlocks"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg}}
 
 
 def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):

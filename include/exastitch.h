@@ -43,6 +43,7 @@ extern "C" {
 #define EXA_DEVERR_BVH_STACK    4u  /* element-BVH traversal stack overflow     */
 #define EXA_DEVERR_BOUNCE_CAP   8u  /* path exceeded the hard bounce cap        */
 #define EXA_DEVERR_WATCHDOG    16u  /* persistent-kernel work loop cap          */
+#define EXA_DEVERR_COPY_WAIT   32u  /* bulk copy to shared memory: wait limit   */
 
 /* ------------------------------------------------------------------ */
 /* plain data types (layouts equal to the owl::common types they       */
@@ -483,6 +484,17 @@ typedef struct {
   float    eventMs;        /* summed GPU time of the event kernels        */
 } exa_render_stats;
 int exa_get_render_stats(exa_context *ctx, exa_render_stats *out);
+
+/* How the last exa_sampler_build ran (no reference counterpart): GPU times
+ * from CUDA events on the context's stream around the majorant kernels
+ * (ExaStitch sampler; 0 for the other samplers) and the call's host time. */
+typedef struct {
+  float    totalMs;           /* exa_sampler_build, host wall time          */
+  float    elemMajorantMs;    /* element value ranges into the grid         */
+  float    gridletMajorantMs; /* gridlet value ranges into the grid         */
+  uint32_t majorantBlocks;    /* blocks of the gridlet majorant kernel      */
+} exa_build_stats;
+int exa_get_build_stats(exa_context *ctx, exa_build_stats *out);
 
 /* ------------------------------------------------------------------ */
 /* allocation-free rendering                                           */

@@ -1,6 +1,7 @@
 // exa_api.cpp -- host classes (Model, ExaStitchModel, ExaStitchSampler,
 // Grid) and the C ABI of exastitch.h.  No exception crosses the C boundary.
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cmath>
 #include <cstring>
@@ -368,6 +369,37 @@ void ExaStitchSampler::buildElementBVH(cudaStream_t s)
   O.bits = occBits.ptr;
 }
 
+// CUDA events recorded on a stream; times between them once it has synchronised
+struct StreamTimer {
+  std::vector<cudaEvent_t> ev;
+  cudaStream_t s;
+  StreamTimer(int n, cudaStream_t st) : ev((size_t)n, nullptr), s(st)
+  {
+    for (auto &e : ev) cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
+  }
+  ~StreamTimer()
+  {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  void mark(int i) { cudaCheck(cudaEventRecord(ev[(size_t)i], s), "cudaEventRecord"); }
+  float ms(int a, int b) const
+  {
+    float t = 0.f;
+    cudaCheck(cudaEventElapsedTime(&t, ev[(size_t)a], ev[(size_t)b]), "cudaEventElapsedTime");
+    return t;
+  }
+};
+
+// the build kernels' error bits, read after the build's stream synchronised
+static void checkBuildErrors(const uint32_t *dev)
+{
+  uint32_t e = 0;
+  if (dev) cudaCheck(cudaMemcpy(&e, dev, sizeof(e), cudaMemcpyDeviceToHost), "read build errors");
+  if (e & EXA_DEVERR_COPY_WAIT)
+    throw Error(EXA_ERR_CUDA, "majorant build: a bulk copy into shared memory did not complete");
+}
+
 // sampler/ExaStitchSampler.cpp:23-340
 bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
 {
@@ -404,15 +436,27 @@ bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
   cudaCheck(cudaMemsetAsync(g.maxOpacities.ptr, 0, g.maxOpacities.bytes(), s), "memset maxOpacities");
   launchInitRanges(g.valueRanges.ptr, numMCs, s);
   launchInitRanges(gridletValueRanges.ptr, gridletValueRanges.count, s);
+  if (!buildErrors.ptr) buildErrors.alloc(1);
+  cudaCheck(cudaMemsetAsync(buildErrors.ptr, 0, sizeof(uint32_t), s), "memset build errors");
+  StreamTimer timer(3, s);
+  timer.mark(0);
   launchElemMajorants(vertexBuffer.ptr, indexBuffer.ptr, model->indices.size() / 8, g.dims, g.worldBounds,
                       g.valueRanges.ptr, elemValueRanges.ptr, s);
-  launchGridletMajorants(gridletBuffer.ptr, gridletScalarBuffer.ptr, model->gridlets.size(), g.dims, g.worldBounds,
-                         g.valueRanges.ptr, gridletValueRanges.ptr, s);
+  timer.mark(1);
+  buildStats = {};
+  buildStats.majorantBlocks =
+      launchGridletMajorants(gridletBuffer.ptr, gridletScalarBuffer.ptr, model->gridlets.size(),
+                             model->gridletScalars.size(), g.dims, g.worldBounds, g.valueRanges.ptr,
+                             gridletValueRanges.ptr, buildErrors.ptr, s);
+  timer.mark(2);
   g.deviceTraversable.dims = g.dims;
   g.deviceTraversable.bounds = g.worldBounds;
   deviceAccel.alloc(1);
   cudaCheck(cudaMemcpyAsync(deviceAccel.ptr, &accel, sizeof(accel), cudaMemcpyHostToDevice, s), "accel handle");
   cudaCheck(cudaStreamSynchronize(s), "sampler build");
+  checkBuildErrors(buildErrors.ptr);
+  buildStats.elemMajorantMs = timer.ms(0, 1);
+  buildStats.gridletMajorantMs = timer.ms(1, 2);
   majorantAccel.grid = model->grid;
   maxOpacities = g.maxOpacities.ptr;
   hasTF = false;
@@ -635,6 +679,7 @@ struct exa_context {
   DBuf<unsigned> wfCounters; // wavefront queue sizes
   unsigned wfCap = 0;
   exa_render_stats lastStats{};
+  exa_build_stats lastBuild{};
   DBuf<exa_vec3f> hostPos;   // staging for exa_sample_points_host
   DBuf<exa_sample> hostOut;
   DBuf<uint32_t> heat;       // heat map: per-pixel work of the frame
@@ -1383,8 +1428,21 @@ int exa_sampler_build(exa_context *ctx)
       s = std::make_shared<ExaBrickSampler>();
     else
       s = std::make_shared<ExaStitchSampler>();
+    const auto t0 = std::chrono::steady_clock::now();
     if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, s->className() + "::build failed");
     ctx->sampler = s;
+    ctx->lastBuild = {};
+    if (auto *es = dynamic_cast<ExaStitchSampler *>(s.get())) ctx->lastBuild = es->buildStats;
+    ctx->lastBuild.totalMs =
+        std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  });
+}
+
+int exa_get_build_stats(exa_context *ctx, exa_build_stats *out)
+{
+  return guarded([&] {
+    need(ctx && out, EXA_ERR_INVALID, "null argument");
+    *out = ctx->lastBuild;
   });
 }
 
@@ -1798,14 +1856,16 @@ void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
   launchInitRanges(er.ptr, er.count, ctx->stream);
   launchElemMajorants(S.vertexBuffer.ptr, S.indexBuffer.ptr, m.indices.size() / 8, B.dims, m.cellBounds, B.ranges.ptr,
                       er.ptr, ctx->stream);
-  launchGridletMajorants(S.gridletBuffer.ptr, S.gridletScalarBuffer.ptr, m.gridlets.size(), B.dims, m.cellBounds,
-                         B.ranges.ptr, gr.ptr, ctx->stream);
+  cudaCheck(cudaMemsetAsync(S.buildErrors.ptr, 0, sizeof(uint32_t), ctx->stream), "memset build errors");
+  launchGridletMajorants(S.gridletBuffer.ptr, S.gridletScalarBuffer.ptr, m.gridlets.size(), m.gridletScalars.size(),
+                         B.dims, m.cellBounds, B.ranges.ptr, gr.ptr, S.buildErrors.ptr, ctx->stream);
   B.maxOps.resize(B.tfColors.size());
   for (size_t t = 0; t < B.tfColors.size(); ++t) {
     B.maxOps[t].alloc(n);
     launchMaxOpacity(B.ranges.ptr, n, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], B.maxOps[t].ptr, ctx->stream);
   }
   cudaCheck(cudaStreamSynchronize(ctx->stream), "batch majorants");
+  checkBuildErrors(S.buildErrors.ptr);
 }
 
 // the culling data of every transfer function (ExaStitchSampler::

@@ -48,91 +48,364 @@ __device__ __forceinline__ void update_mc(exa_range1f *mc, const exa_vec3i dims,
   atomic_max_float(&m->upper, hi);
 }
 
-// Grid.cu:134-246 fused with computeGridletValueRangesGPU
-// (sampler/ExaStitchSampler.cu:52-142): one block per gridlet, one thread
-// per cell.  A cell only tests the macrocells within one of its own
-// projection (the reference tests every macrocell of the gridlet's range;
-// the exact overlap test below decides in both cases, so the set of
-// updated macrocells is the same).
-__global__ void __launch_bounds__(128) k_gridlet_majorants(const exa_gridlet *__restrict__ gridlets,
-                                                           const float *__restrict__ scalars, exa_vec3i dims,
-                                                           exa_box3f wb, exa_range1f *mcRanges,
-                                                           exa_range1f *gridletRanges)
+// ------------------------------------------------------------------------
+// Bulk copies into shared memory: cp.async.bulk (the TMA unit's untiled
+// copy; both addresses and the size multiples of 16 bytes), completed on an
+// mbarrier that the issuing thread arms with the expected byte count.
+EXA_D uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+EXA_D void mbar_init(uint64_t *bar)
 {
-  const exa_gridlet g = gridlets[blockIdx.x];
-  const float cw = (float)(1 << g.level);
-  exa_box3f gb;
-  gb.lower.x = ((float)g.lower.x + 0.5f) * cw;
-  gb.lower.y = ((float)g.lower.y + 0.5f) * cw;
-  gb.lower.z = ((float)g.lower.z + 0.5f) * cw;
-  gb.upper.x = (((float)g.lower.x + (float)g.dims.x) + 0.5f) * cw;
-  gb.upper.y = (((float)g.lower.y + (float)g.dims.y) + 0.5f) * cw;
-  gb.upper.z = (((float)g.lower.z + (float)g.dims.z) + 0.5f) * cw;
-  const V3i D = {dims.x, dims.y, dims.z};
-  const V3i loMC = project_on_grid(mk3(gb.lower), D, wb);
-  const V3i hiMC = project_on_grid(mk3(gb.upper), D, wb);
-  const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
-  const int nx = g.dims.x + 1, ny = g.dims.y + 1;
-  const int ncells = g.dims.x * g.dims.y * g.dims.z;
-  const float *S = scalars + g.begin;
-  float glo = 1e30f, ghi = -1e30f;
-  for (int c = threadIdx.x; c < ncells; c += blockDim.x) {
-    const int x = c % g.dims.x, y = (c / g.dims.x) % g.dims.y, z = c / (g.dims.x * g.dims.y);
-    const float f[8] = {__ldg(S + (z * ny + y) * nx + x), __ldg(S + (z * ny + y) * nx + x + 1),
-                        __ldg(S + (z * ny + y + 1) * nx + x), __ldg(S + (z * ny + y + 1) * nx + x + 1),
-                        __ldg(S + ((z + 1) * ny + y) * nx + x), __ldg(S + ((z + 1) * ny + y) * nx + x + 1),
-                        __ldg(S + ((z + 1) * ny + y + 1) * nx + x), __ldg(S + ((z + 1) * ny + y + 1) * nx + x + 1)};
-    float lo = 1e30f, hi = -1e30f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (!isnan(f[k])) { lo = fminf(lo, f[k]); hi = fmaxf(hi, f[k]); }
-    glo = fminf(glo, lo);
-    ghi = fmaxf(ghi, hi);
-    if (hi < lo) continue;  // no non-NaN corner: the reference's update is a no-op
-    // Grid.cu:181-182
-    const V3 clo = add3(muls(mk3((float)(g.lower.x + x), (float)(g.lower.y + y), (float)(g.lower.z + z)), cw),
-                        mk3(0.5f * cw, 0.5f * cw, 0.5f * cw));
-    const V3 chi = add3(muls(mk3((float)(g.lower.x + x + 1), (float)(g.lower.y + y + 1), (float)(g.lower.z + z + 1)), cw),
-                        mk3(0.5f * cw, 0.5f * cw, 0.5f * cw));
-    const V3i pl = project_on_grid(clo, D, wb), ph = project_on_grid(chi, D, wb);
-    const int x0 = imax_t(loMC.x, pl.x - 1), x1 = imin_t(hiMC.x, ph.x + 1);
-    const int y0 = imax_t(loMC.y, pl.y - 1), y1 = imin_t(hiMC.y, ph.y + 1);
-    const int z0 = imax_t(loMC.z, pl.z - 1), z1 = imin_t(hiMC.z, ph.z + 1);
-    for (int mz = z0; mz <= z1; ++mz)
-      for (int my = y0; my <= y1; ++my)
-        for (int mx = x0; mx <= x1; ++mx) {
-          const V3 mlo = add3(mk3(wb.lower), mul3(mk3((float)mx, (float)my, (float)mz), mcSize));
-          const V3 mhi = add3(mk3(wb.lower), mul3(mk3((float)(mx + 1), (float)(my + 1), (float)(mz + 1)), mcSize));
-          if (mlo.x <= chi.x && mlo.y <= chi.y && mlo.z <= chi.z && clo.x <= mhi.x && clo.y <= mhi.y &&
-              clo.z <= mhi.z)
-            update_mc(mcRanges, dims, mx, my, mz, lo, hi);
-        }
-  }
-  // block reduction of the gridlet's range
-  __shared__ float sLo[4], sHi[4];
-  for (int o = 16; o > 0; o >>= 1) {
-    glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
-    ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
-  }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) { sLo[warp] = glo; sHi[warp] = ghi; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { glo = fminf(glo, sLo[w]); ghi = fmaxf(ghi, sHi[w]); }
-    gridletRanges[blockIdx.x].lower = glo;
-    gridletRanges[blockIdx.x].upper = ghi;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+
+EXA_D void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// orders this thread's earlier generic-proxy accesses to shared memory (made
+// visible to it by a block barrier) before its next bulk copy
+EXA_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+EXA_D void bulk_load_smem(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+EXA_D bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// waits for the phase of the given parity to complete; false when it did
+// not within the poll limit
+constexpr int kMbarPollLimit = 1 << 24;
+EXA_D bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+  for (int i = 0; i < kMbarPollLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// ------------------------------------------------------------------------
+// Grid.cu:134-246 fused with computeGridletValueRangesGPU
+// (sampler/ExaStitchSampler.cu:52-142).
+//
+// Persistent blocks take gridlets in turn.  A gridlet's corner scalars (one
+// contiguous brick of (dims+1)^3 floats, <= 729 for makeGrids' 8^3 cells)
+// are staged in shared memory by one bulk copy, double-buffered so that the
+// next gridlet's copy runs while this one is processed.  The copy starts at
+// the 16-byte boundary at or below the brick and ends at the 16-byte
+// boundary at or above it, clipped to the last boundary inside the scalar
+// buffer; the at most 3 scalars past that clip are loaded by threads.
+//
+// A thread takes one x-row of cells and reuses each x-face of corners for
+// the next cell.  The macrocell overlap test of Grid.cu:172-183 is an AND of
+// per-axis interval tests, so a cell's macrocells are the product of three
+// index ranges: the row's y and z ranges are computed once, the x range per
+// cell, each from the candidates within one macrocell of the cell's own
+// projection (the reference tests every macrocell of the gridlet's range;
+// the exact test decides in both cases, so the same macrocells are
+// updated).  Runs of cells with the same x range are merged first; the
+// updates then go to a shared-memory copy of the gridlet's macrocell window
+// and from there, one atomic min and max per touched macrocell, to the
+// grid.  Windows larger than kMajWindow update the grid directly.  Min and
+// max are exact, so none of this changes the result; merges use the same
+// total order (-0 below +0) as the atomics.
+constexpr int kMajThreads = 64;
+constexpr int kBrickCap = 736;    // floats per staging buffer: 729 scalars + alignment (multiple of 4)
+constexpr int kMajWindow = 512;   // macrocells of a gridlet reduced in shared memory
+
+constexpr int kAxisTab = 64;      // cells per axis whose macrocell ranges are tabled per gridlet
+
+struct alignas(16) MajSmem {
+  float brick[2][kBrickCap];
+  float winLo[kMajWindow], winHi[kMajWindow];
+  int2 axisRange[3][kAxisTab];    // per axis and cell index: its macrocell range [x, y]
+  uint64_t bar[2];
+  float redLo[kMajThreads / 32], redHi[kMajThreads / 32];
+};
+
+// the staging of one gridlet's scalars: copy [f0, f0 + bulk/4) in bulk and
+// `tail` floats after it by threads; the brick starts `lead` floats in
+struct BrickPlan {
+  size_t f0;
+  uint32_t bulk;
+  int lead, tail;
+  bool staged;
+};
+
+EXA_D BrickPlan brick_plan(const exa_gridlet &g, size_t nScalars, bool stage)
+{
+  BrickPlan p;
+  const size_t n = (size_t)(g.dims.x + 1) * (g.dims.y + 1) * (g.dims.z + 1);
+  const size_t s0 = (uint32_t)g.begin, s1 = s0 + n;
+  p.f0 = s0 & ~(size_t)3;
+  p.lead = (int)(s0 - p.f0);
+  // s1 - f0 + 3 bounds the rounded-up copy
+  p.staged = stage && s1 - p.f0 + 3 <= (size_t)kBrickCap;
+  size_t f1 = (s1 + 3) & ~(size_t)3;
+  const size_t fend = nScalars & ~(size_t)3;
+  if (f1 > fend) f1 = fend > p.f0 ? fend : p.f0;
+  p.bulk = p.staged ? (uint32_t)((f1 - p.f0) * 4) : 0u;
+  p.tail = p.staged && s1 > f1 ? (int)(s1 - f1) : 0;
+  return p;
+}
+
+// projectOnGrid (Grid.cuh:55-63) along one axis
+EXA_D int proj_axis(float v, float lo, float hi, int n)
+{
+  return iclamp((int)(((v - lo) / (hi - lo)) * (float)n), 0, n - 1);
+}
+
+// the macrocells [m0, m1] along one axis whose slab overlaps the closed
+// interval [clo, chi]: the candidates within one of the interval's own
+// projection and the gridlet's range, tested as Grid.cu:172-183 does
+// (empty: m0 > m1)
+EXA_D void mc_axis_range(float clo, float chi, float wlo, float whi, float size, int n, int loMC, int hiMC, int &m0,
+                         int &m1)
+{
+  const int c0 = imax_t(loMC, proj_axis(clo, wlo, whi, n) - 1);
+  const int c1 = imin_t(hiMC, proj_axis(chi, wlo, whi, n) + 1);
+  m0 = 0;
+  m1 = -1;
+  for (int m = c0; m <= c1; ++m) {
+    const float mlo = wlo + (float)m * size, mhi = wlo + (float)(m + 1) * size;
+    if (mlo <= chi && clo <= mhi) {
+      if (m1 < m0) m0 = m;
+      m1 = m;
+    }
   }
 }
 
-void launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, exa_vec3i dims, exa_box3f wb,
-                            exa_range1f *mcRanges, exa_range1f *gridletRanges, cudaStream_t s)
+// the order of atomic_min_float / atomic_max_float: -0 below +0
+EXA_D uint32_t ord_key(float v)
 {
-  if (!ng) return;
-  for (size_t off = 0; off < ng; off += 0x7fffffff) {
-    const size_t cnt = ng - off < 0x7fffffff ? ng - off : 0x7fffffff;
-    k_gridlet_majorants<<<(unsigned)cnt, 128, 0, s>>>(g + off, scalars, dims, wb, mcRanges, gridletRanges + off);
+  const uint32_t b = __float_as_uint(v);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+EXA_D float min_ord(float a, float b) { return ord_key(b) < ord_key(a) ? b : a; }
+EXA_D float max_ord(float a, float b) { return ord_key(b) > ord_key(a) ? b : a; }
+
+// thread 0: the bulk copy of gridlet gi's brick into buffer buf
+EXA_D void issue_brick(MajSmem &sm, int buf, const exa_gridlet *gridlets, size_t gi, const float *scalars,
+                       size_t nScalars, bool stage)
+{
+  const BrickPlan P = brick_plan(gridlets[gi], nScalars, stage);
+  if (P.bulk) bulk_load_smem(sm.brick[buf], scalars + P.f0, P.bulk, &sm.bar[buf]);
+}
+
+__global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa_gridlet *__restrict__ gridlets, size_t ng,
+                                                                   const float *__restrict__ scalars, size_t nScalars,
+                                                                   bool stage, exa_vec3i dims, exa_box3f wb,
+                                                                   exa_range1f *mcRanges, exa_range1f *gridletRanges,
+                                                                   uint32_t *errors)
+{
+  __shared__ MajSmem sm;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0]);
+    mbar_init(&sm.bar[1]);
+    mbar_init_fence();
   }
+  __syncthreads();
+  if (tid == 0 && blockIdx.x < ng) issue_brick(sm, 0, gridlets, blockIdx.x, scalars, nScalars, stage);
+  const V3i D = {dims.x, dims.y, dims.z};
+  const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
+  uint32_t parity = 0;  // bit b: parity of the next phase of buffer b
+  int it = 0;
+  for (size_t gi = blockIdx.x; gi < ng; gi += gridDim.x, ++it) {
+    const int buf = it & 1;
+    const exa_gridlet g = gridlets[gi];
+    const BrickPlan P = brick_plan(g, nScalars, stage);
+    const size_t gn = gi + gridDim.x;
+    if (tid == 0 && gn < ng) {
+      fence_proxy_async_smem();
+      issue_brick(sm, buf ^ 1, gridlets, gn, scalars, nScalars, stage);
+    }
+    const float *S = scalars + (uint32_t)g.begin;
+    if (P.staged) {
+      bool ok = true;
+      if (P.bulk) {
+        ok = mbar_wait(&sm.bar[buf], (parity >> buf) & 1u);
+        parity ^= 1u << buf;
+      }
+      if (__syncthreads_or(!ok)) {
+        // give up: flag it, let the other buffer's copy land, return
+        if (tid == 0) {
+          if (errors) atomicOr(errors, EXA_DEVERR_COPY_WAIT);
+          if (gn < ng && brick_plan(gridlets[gn], nScalars, stage).bulk)
+            (void)mbar_wait(&sm.bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
+        }
+        return;
+      }
+      float *B = sm.brick[buf];
+      for (int k = tid; k < P.tail; k += blockDim.x) B[P.bulk / 4 + k] = __ldg(scalars + P.f0 + P.bulk / 4 + k);
+      S = B + P.lead;
+    }
+    const float cw = (float)(1 << g.level);
+    exa_box3f gb;
+    gb.lower.x = ((float)g.lower.x + 0.5f) * cw;
+    gb.lower.y = ((float)g.lower.y + 0.5f) * cw;
+    gb.lower.z = ((float)g.lower.z + 0.5f) * cw;
+    gb.upper.x = (((float)g.lower.x + (float)g.dims.x) + 0.5f) * cw;
+    gb.upper.y = (((float)g.lower.y + (float)g.dims.y) + 0.5f) * cw;
+    gb.upper.z = (((float)g.lower.z + (float)g.dims.z) + 0.5f) * cw;
+    const V3i loMC = project_on_grid(mk3(gb.lower), D, wb);
+    const V3i hiMC = project_on_grid(mk3(gb.upper), D, wb);
+    const int wx = hiMC.x - loMC.x + 1, wy = hiMC.y - loMC.y + 1, wz = hiMC.z - loMC.z + 1;
+    const int wn = wx * wy * wz;
+    const bool useWin = wn <= kMajWindow;
+    if (useWin)
+      for (int k = tid; k < wn; k += blockDim.x) {
+        sm.winLo[k] = 1e30f;
+        sm.winHi[k] = -1e30f;
+      }
+    const float hc = 0.5f * cw;
+    // a cell's macrocell range along an axis depends only on its index
+    // along that axis: table them once per gridlet
+    const bool tabled = g.dims.x <= kAxisTab && g.dims.y <= kAxisTab && g.dims.z <= kAxisTab;
+    auto axis_range = [&](int a, int i, int &m0, int &m1) {
+      const int lower = a == 0 ? g.lower.x : a == 1 ? g.lower.y : g.lower.z;
+      const float wlo = a == 0 ? wb.lower.x : a == 1 ? wb.lower.y : wb.lower.z;
+      const float whi = a == 0 ? wb.upper.x : a == 1 ? wb.upper.y : wb.upper.z;
+      const float size = a == 0 ? mcSize.x : a == 1 ? mcSize.y : mcSize.z;
+      const int n = a == 0 ? dims.x : a == 1 ? dims.y : dims.z;
+      const int lo = a == 0 ? loMC.x : a == 1 ? loMC.y : loMC.z;
+      const int hi = a == 0 ? hiMC.x : a == 1 ? hiMC.y : hiMC.z;
+      mc_axis_range((float)(lower + i) * cw + hc, (float)(lower + i + 1) * cw + hc, wlo, whi, size, n, lo, hi, m0,
+                    m1);
+    };
+    if (tabled)
+      for (int k = tid; k < g.dims.x + g.dims.y + g.dims.z; k += blockDim.x) {
+        const int a = k < g.dims.x ? 0 : k < g.dims.x + g.dims.y ? 1 : 2;
+        const int i = a == 0 ? k : a == 1 ? k - g.dims.x : k - g.dims.x - g.dims.y;
+        int m0, m1;
+        axis_range(a, i, m0, m1);
+        sm.axisRange[a][i] = make_int2(m0, m1);
+      }
+    __syncthreads();
+    const int nx = g.dims.x + 1, ny = g.dims.y + 1;
+    float glo = 1e30f, ghi = -1e30f;
+    for (int r = tid; r < g.dims.y * g.dims.z; r += blockDim.x) {
+      const int y = r % g.dims.y, z = r / g.dims.y;
+      int my0, my1, mz0, mz1;
+      if (tabled) {
+        const int2 ry = sm.axisRange[1][y], rz = sm.axisRange[2][z];
+        my0 = ry.x; my1 = ry.y; mz0 = rz.x; mz1 = rz.y;
+      } else {
+        axis_range(1, y, my0, my1);
+        axis_range(2, z, mz0, mz1);
+      }
+      const bool rowHits = my0 <= my1 && mz0 <= mz1;
+      const float *R0 = S + (z * ny + y) * nx, *R1 = R0 + nx, *R2 = R0 + nx * ny, *R3 = R2 + nx;
+      float a0 = R0[0], a1 = R1[0], a2 = R2[0], a3 = R3[0];
+      int rx0 = 0, rx1 = -1;
+      float rlo = 1e30f, rhi = -1e30f;
+      auto flush = [&]() {
+        if (rx1 < rx0) return;
+        for (int mz = mz0; mz <= mz1; ++mz)
+          for (int my = my0; my <= my1; ++my)
+            for (int mx = rx0; mx <= rx1; ++mx) {
+              if (useWin) {
+                const int k = ((mz - loMC.z) * wy + (my - loMC.y)) * wx + (mx - loMC.x);
+                atomic_min_float(&sm.winLo[k], rlo);
+                atomic_max_float(&sm.winHi[k], rhi);
+              } else {
+                update_mc(mcRanges, dims, mx, my, mz, rlo, rhi);
+              }
+            }
+      };
+      for (int x = 0; x < g.dims.x; ++x) {
+        const float b0 = R0[x + 1], b1 = R1[x + 1], b2 = R2[x + 1], b3 = R3[x + 1];
+        const float f[8] = {a0, b0, a1, b1, a2, b2, a3, b3};
+        a0 = b0; a1 = b1; a2 = b2; a3 = b3;
+        float lo = 1e30f, hi = -1e30f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (!isnan(f[k])) { lo = fminf(lo, f[k]); hi = fmaxf(hi, f[k]); }
+        glo = fminf(glo, lo);
+        ghi = fmaxf(ghi, hi);
+        if (hi < lo || !rowHits) continue;  // no non-NaN corner: the reference's update is a no-op
+        int mx0, mx1;
+        if (tabled) {
+          const int2 rx = sm.axisRange[0][x];
+          mx0 = rx.x; mx1 = rx.y;
+        } else {
+          axis_range(0, x, mx0, mx1);
+        }
+        if (mx1 < mx0) continue;
+        if (mx0 == rx0 && mx1 == rx1) {
+          rlo = min_ord(rlo, lo);
+          rhi = max_ord(rhi, hi);
+        } else {
+          flush();
+          rx0 = mx0;
+          rx1 = mx1;
+          rlo = lo;
+          rhi = hi;
+        }
+      }
+      flush();
+    }
+    // the gridlet's own range
+    for (int o = 16; o > 0; o >>= 1) {
+      glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+      ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+    }
+    if ((tid & 31) == 0) {
+      sm.redLo[tid >> 5] = glo;
+      sm.redHi[tid >> 5] = ghi;
+    }
+    __syncthreads();
+    if (useWin)
+      for (int k = tid; k < wn; k += blockDim.x) {
+        const float lo = sm.winLo[k], hi = sm.winHi[k];
+        if (!(lo <= hi)) continue;  // untouched
+        const int mx = loMC.x + k % wx, my = loMC.y + (k / wx) % wy, mz = loMC.z + k / (wx * wy);
+        update_mc(mcRanges, dims, mx, my, mz, lo, hi);
+      }
+    if (tid == 0) {
+      for (int w = 1; w < kMajThreads / 32; ++w) {
+        glo = fminf(glo, sm.redLo[w]);
+        ghi = fmaxf(ghi, sm.redHi[w]);
+      }
+      gridletRanges[gi].lower = glo;
+      gridletRanges[gi].upper = ghi;
+    }
+    // buffer, window and reduction slots are free for the next gridlet
+    __syncthreads();
+  }
+}
+
+unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
+                                exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
+                                uint32_t *errors, cudaStream_t s)
+{
+  if (!ng) return 0;
+  int dev = 0, sms = 0;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  // as many resident blocks of 64 threads (~11 KB of shared memory each)
+  // as fit on every SM
+  int perSM = 0;
+  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_gridlet_majorants, kMajThreads, 0),
+            "occupancy");
+  const size_t blocks = std::min<size_t>(ng, (size_t)std::max(sms, 1) * (size_t)std::max(perSM, 1));
+  const bool stage = (reinterpret_cast<uintptr_t>(scalars) & 15u) == 0;
+  k_gridlet_majorants<<<(unsigned)blocks, kMajThreads, 0, s>>>(g, ng, scalars, nScalars, stage, dims, wb, mcRanges,
+                                                               gridletRanges, errors);
   cudaCheck(cudaGetLastError(), "k_gridlet_majorants");
+  return (unsigned)blocks;
 }
 
 // Grid.cu:73-117 (buildGrid<8>) plus the element's own range with the

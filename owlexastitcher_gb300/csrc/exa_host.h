@@ -170,6 +170,10 @@ class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
   DBuf<float> gridletMaxOpacities;
   DBuf<exa_range1f> elemValueRanges;
   DBuf<float> umeshMaxOpacities;
+  // EXA_DEVERR_* bits of the build kernels
+  DBuf<uint32_t> buildErrors;
+  // GPU times of the last build's majorant kernels
+  exa_build_stats buildStats{};
   // point-location accel
   std::vector<DBuf<int32_t>> tableEntries, tableItems;
   DBuf<BvhNode> bvhNodes;
@@ -236,8 +240,10 @@ class ExaBrickSampler : public Sampler {
 // ---------------------------------------------------------------- kernels
 // launchers implemented in exa_build.cu / exa_render.cu
 void launchInitRanges(exa_range1f *r, size_t n, cudaStream_t s);
-void launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, exa_vec3i dims, exa_box3f wb,
-                            exa_range1f *mcRanges, exa_range1f *gridletRanges, cudaStream_t s);
+// returns the number of blocks launched
+unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
+                                exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
+                                uint32_t *errors, cudaStream_t s);
 void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa_vec3i dims, exa_box3f wb,
                          exa_range1f *mcRanges, exa_range1f *elemRanges, cudaStream_t s);
 // Grid.cu:248-285: every cell's value into the macrocells its support

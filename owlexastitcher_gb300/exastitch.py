@@ -191,6 +191,11 @@ class RenderStats(C.Structure):
                 ("walkMs", C.c_float), ("eventMs", C.c_float)]
 
 
+class BuildStats(C.Structure):
+    _fields_ = [("totalMs", C.c_float), ("elemMajorantMs", C.c_float), ("gridletMajorantMs", C.c_float),
+                ("majorantBlocks", C.c_uint32)]
+
+
 class MemStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "elemVertexBytes", "elemIndexBytes", "gridletBytes", "emptyScalarsBytes", "nonEmptyScalarsBytes",
@@ -247,7 +252,7 @@ EXPORTED = [
     "exa_model_set_voxel_space_transform", "exa_model_get_world_bounds", "exa_model_mem_stats",
     "exa_sampler_build", "exa_sampler_compute_max_opacities", "exa_sampler_set_lps", "exa_sampler_class_name",
     "exa_get_majorants", "exa_get_prim_majorants", "exa_sample_points", "exa_sample_points_host",
-    "exa_launch_params_init", "exa_render", "exa_render_noalloc", "exa_get_render_stats",
+    "exa_launch_params_init", "exa_render", "exa_render_noalloc", "exa_get_render_stats", "exa_get_build_stats",
     "exa_surrogate_params_default", "exa_surrogate_create", "exa_surrogate_train", "exa_surrogate_evaluate",
     "exa_surrogate_get_stats", "exa_surrogate_get_geometry", "exa_surrogate_sample_points",
     "exa_surrogate_get_params", "exa_surrogate_set_params", "exa_surrogate_gradients",
@@ -297,6 +302,7 @@ def lib():
         "exa_render": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
         "exa_render_noalloc": ([ctx_p, C.POINTER(LaunchParams), i32, i32], C.c_int),
         "exa_get_render_stats": ([ctx_p, C.POINTER(RenderStats)], C.c_int),
+        "exa_get_build_stats": ([ctx_p, C.POINTER(BuildStats)], C.c_int),
         "exa_surrogate_params_default": ([C.POINTER(SurrogateParams)], None),
         "exa_surrogate_create": ([ctx_p, C.POINTER(SurrogateParams)], C.c_int),
         "exa_surrogate_train": ([ctx_p, i32, C.POINTER(C.c_float)], C.c_int),
@@ -384,6 +390,11 @@ class Context:
         st = RenderStats()
         _check(lib().exa_get_render_stats(self.h, C.byref(st)))
         return {f: getattr(st, f) for f, _ in RenderStats._fields_}
+
+    def build_stats(self):
+        st = BuildStats()
+        _check(lib().exa_get_build_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in BuildStats._fields_}
 
     def device_errors(self):
         b = C.c_uint32()
