@@ -119,21 +119,13 @@ EXA_D bool mbar_wait(uint64_t *bar, uint32_t parity)
 // updates then go to a shared-memory copy of the gridlet's macrocell window
 // and from there, one atomic min and max per touched macrocell, to the
 // grid.  Windows larger than kMajWindow update the grid directly.  Min and
-// max are exact, so none of this changes the result; merges use the same
-// total order (-0 below +0) as the atomics.
+// max are exact, so none of this changes the result; merges and the window
+// use the same total order (-0 below +0) as the atomics.
 constexpr int kMajThreads = 64;
 constexpr int kBrickCap = 736;    // floats per staging buffer: 729 scalars + alignment (multiple of 4)
 constexpr int kMajWindow = 512;   // macrocells of a gridlet reduced in shared memory
 
 constexpr int kAxisTab = 64;      // cells per axis whose macrocell ranges are tabled per gridlet
-
-struct alignas(16) MajSmem {
-  float brick[2][kBrickCap];
-  float winLo[kMajWindow], winHi[kMajWindow];
-  int2 axisRange[3][kAxisTab];    // per axis and cell index: its macrocell range [x, y]
-  uint64_t bar[2];
-  float redLo[kMajThreads / 32], redHi[kMajThreads / 32];
-};
 
 // the staging of one gridlet's scalars: copy [f0, f0 + bulk/4) in bulk and
 // `tail` floats after it by threads; the brick starts `lead` floats in
@@ -161,6 +153,23 @@ EXA_D BrickPlan brick_plan(const exa_gridlet &g, size_t nScalars, bool stage)
   return p;
 }
 
+// what the block needs to know of a gridlet before its cells: prepared by
+// thread 0 when it issues the gridlet's copy, one gridlet ahead
+struct GridletPlan {
+  exa_gridlet g;
+  BrickPlan P;
+  V3i loMC, hiMC;   // the gridlet's macrocell range (projectOnGrid of its box)
+};
+
+struct alignas(16) MajSmem {
+  float brick[2][kBrickCap];
+  uint32_t winLo[kMajWindow], winHi[kMajWindow];  // ord_key of the window's ranges
+  int2 axisRange[3][kAxisTab];    // per axis and cell index: its macrocell range [x, y]
+  GridletPlan plan[2];            // of the gridlet in each staging buffer
+  uint64_t bar[2];
+  float redLo[kMajThreads / 32], redHi[kMajThreads / 32];
+};
+
 // projectOnGrid (Grid.cuh:55-63) along one axis
 EXA_D int proj_axis(float v, float lo, float hi, int n)
 {
@@ -187,21 +196,32 @@ EXA_D void mc_axis_range(float clo, float chi, float wlo, float whi, float size,
   }
 }
 
-// the order of atomic_min_float / atomic_max_float: -0 below +0
+// keys in the order of atomic_min_float / atomic_max_float (-0 below +0),
+// compared as unsigned integers; ord_value inverts ord_key
 EXA_D uint32_t ord_key(float v)
 {
   const uint32_t b = __float_as_uint(v);
   return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
-EXA_D float min_ord(float a, float b) { return ord_key(b) < ord_key(a) ? b : a; }
-EXA_D float max_ord(float a, float b) { return ord_key(b) > ord_key(a) ? b : a; }
+EXA_D float ord_value(uint32_t k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
 
-// thread 0: the bulk copy of gridlet gi's brick into buffer buf
-EXA_D void issue_brick(MajSmem &sm, int buf, const exa_gridlet *gridlets, size_t gi, const float *scalars,
-                       size_t nScalars, bool stage)
+// thread 0: the plan of gridlet gi and the bulk copy of its brick into
+// buffer buf
+EXA_D void prepare_gridlet(MajSmem &sm, int buf, const exa_gridlet *gridlets, size_t gi, const float *scalars,
+                           size_t nScalars, bool stage, const V3i D, const exa_box3f &wb)
 {
-  const BrickPlan P = brick_plan(gridlets[gi], nScalars, stage);
-  if (P.bulk) bulk_load_smem(sm.brick[buf], scalars + P.f0, P.bulk, &sm.bar[buf]);
+  GridletPlan &pl = sm.plan[buf];
+  pl.g = gridlets[gi];
+  pl.P = brick_plan(pl.g, nScalars, stage);
+  if (pl.P.bulk) bulk_load_smem(sm.brick[buf], scalars + pl.P.f0, pl.P.bulk, &sm.bar[buf]);
+  const exa_gridlet &g = pl.g;
+  const float cw = (float)(1 << g.level);
+  const V3 lo = mk3(((float)g.lower.x + 0.5f) * cw, ((float)g.lower.y + 0.5f) * cw, ((float)g.lower.z + 0.5f) * cw);
+  const V3 hi = mk3((((float)g.lower.x + (float)g.dims.x) + 0.5f) * cw,
+                    (((float)g.lower.y + (float)g.dims.y) + 0.5f) * cw,
+                    (((float)g.lower.z + (float)g.dims.z) + 0.5f) * cw);
+  pl.loMC = project_on_grid(lo, D, wb);
+  pl.hiMC = project_on_grid(hi, D, wb);
 }
 
 __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa_gridlet *__restrict__ gridlets, size_t ng,
@@ -212,25 +232,26 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
 {
   __shared__ MajSmem sm;
   const int tid = threadIdx.x;
+  const V3i D = {dims.x, dims.y, dims.z};
   if (tid == 0) {
     mbar_init(&sm.bar[0]);
     mbar_init(&sm.bar[1]);
     mbar_init_fence();
+    if (blockIdx.x < ng) prepare_gridlet(sm, 0, gridlets, blockIdx.x, scalars, nScalars, stage, D, wb);
   }
   __syncthreads();
-  if (tid == 0 && blockIdx.x < ng) issue_brick(sm, 0, gridlets, blockIdx.x, scalars, nScalars, stage);
-  const V3i D = {dims.x, dims.y, dims.z};
   const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
   uint32_t parity = 0;  // bit b: parity of the next phase of buffer b
   int it = 0;
   for (size_t gi = blockIdx.x; gi < ng; gi += gridDim.x, ++it) {
     const int buf = it & 1;
-    const exa_gridlet g = gridlets[gi];
-    const BrickPlan P = brick_plan(g, nScalars, stage);
+    const exa_gridlet g = sm.plan[buf].g;
+    const BrickPlan P = sm.plan[buf].P;
+    const V3i loMC = sm.plan[buf].loMC, hiMC = sm.plan[buf].hiMC;
     const size_t gn = gi + gridDim.x;
     if (tid == 0 && gn < ng) {
       fence_proxy_async_smem();
-      issue_brick(sm, buf ^ 1, gridlets, gn, scalars, nScalars, stage);
+      prepare_gridlet(sm, buf ^ 1, gridlets, gn, scalars, nScalars, stage, D, wb);
     }
     const float *S = scalars + (uint32_t)g.begin;
     if (P.staged) {
@@ -243,7 +264,7 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
         // give up: flag it, let the other buffer's copy land, return
         if (tid == 0) {
           if (errors) atomicOr(errors, EXA_DEVERR_COPY_WAIT);
-          if (gn < ng && brick_plan(gridlets[gn], nScalars, stage).bulk)
+          if (gn < ng && sm.plan[buf ^ 1].P.bulk)
             (void)mbar_wait(&sm.bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
         }
         return;
@@ -253,22 +274,13 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
       S = B + P.lead;
     }
     const float cw = (float)(1 << g.level);
-    exa_box3f gb;
-    gb.lower.x = ((float)g.lower.x + 0.5f) * cw;
-    gb.lower.y = ((float)g.lower.y + 0.5f) * cw;
-    gb.lower.z = ((float)g.lower.z + 0.5f) * cw;
-    gb.upper.x = (((float)g.lower.x + (float)g.dims.x) + 0.5f) * cw;
-    gb.upper.y = (((float)g.lower.y + (float)g.dims.y) + 0.5f) * cw;
-    gb.upper.z = (((float)g.lower.z + (float)g.dims.z) + 0.5f) * cw;
-    const V3i loMC = project_on_grid(mk3(gb.lower), D, wb);
-    const V3i hiMC = project_on_grid(mk3(gb.upper), D, wb);
     const int wx = hiMC.x - loMC.x + 1, wy = hiMC.y - loMC.y + 1, wz = hiMC.z - loMC.z + 1;
     const int wn = wx * wy * wz;
     const bool useWin = wn <= kMajWindow;
     if (useWin)
       for (int k = tid; k < wn; k += blockDim.x) {
-        sm.winLo[k] = 1e30f;
-        sm.winHi[k] = -1e30f;
+        sm.winLo[k] = 0xffffffffu;  // untouched: lower key above upper key
+        sm.winHi[k] = 0u;
       }
     const float hc = 0.5f * cw;
     // a cell's macrocell range along an axis depends only on its index
@@ -310,7 +322,7 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
       const float *R0 = S + (z * ny + y) * nx, *R1 = R0 + nx, *R2 = R0 + nx * ny, *R3 = R2 + nx;
       float a0 = R0[0], a1 = R1[0], a2 = R2[0], a3 = R3[0];
       int rx0 = 0, rx1 = -1;
-      float rlo = 1e30f, rhi = -1e30f;
+      uint32_t rlo = 0xffffffffu, rhi = 0u;  // the run's range as ord_key
       auto flush = [&]() {
         if (rx1 < rx0) return;
         for (int mz = mz0; mz <= mz1; ++mz)
@@ -318,10 +330,10 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
             for (int mx = rx0; mx <= rx1; ++mx) {
               if (useWin) {
                 const int k = ((mz - loMC.z) * wy + (my - loMC.y)) * wx + (mx - loMC.x);
-                atomic_min_float(&sm.winLo[k], rlo);
-                atomic_max_float(&sm.winHi[k], rhi);
+                atomicMin(&sm.winLo[k], rlo);
+                atomicMax(&sm.winHi[k], rhi);
               } else {
-                update_mc(mcRanges, dims, mx, my, mz, rlo, rhi);
+                update_mc(mcRanges, dims, mx, my, mz, ord_value(rlo), ord_value(rhi));
               }
             }
       };
@@ -329,10 +341,14 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
         const float b0 = R0[x + 1], b1 = R1[x + 1], b2 = R2[x + 1], b3 = R3[x + 1];
         const float f[8] = {a0, b0, a1, b1, a2, b2, a3, b3};
         a0 = b0; a1 = b1; a2 = b2; a3 = b3;
+        // fminf / fmaxf return the other operand where one is NaN, so NaN
+        // corners drop out as the reference's isnan tests drop them
         float lo = 1e30f, hi = -1e30f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (!isnan(f[k])) { lo = fminf(lo, f[k]); hi = fmaxf(hi, f[k]); }
+        for (int k = 0; k < 8; ++k) {
+          lo = fminf(lo, f[k]);
+          hi = fmaxf(hi, f[k]);
+        }
         glo = fminf(glo, lo);
         ghi = fmaxf(ghi, hi);
         if (hi < lo || !rowHits) continue;  // no non-NaN corner: the reference's update is a no-op
@@ -345,14 +361,14 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
         }
         if (mx1 < mx0) continue;
         if (mx0 == rx0 && mx1 == rx1) {
-          rlo = min_ord(rlo, lo);
-          rhi = max_ord(rhi, hi);
+          rlo = min(rlo, ord_key(lo));
+          rhi = max(rhi, ord_key(hi));
         } else {
           flush();
           rx0 = mx0;
           rx1 = mx1;
-          rlo = lo;
-          rhi = hi;
+          rlo = ord_key(lo);
+          rhi = ord_key(hi);
         }
       }
       flush();
@@ -369,10 +385,10 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
     __syncthreads();
     if (useWin)
       for (int k = tid; k < wn; k += blockDim.x) {
-        const float lo = sm.winLo[k], hi = sm.winHi[k];
-        if (!(lo <= hi)) continue;  // untouched
+        const uint32_t lo = sm.winLo[k], hi = sm.winHi[k];
+        if (lo > hi) continue;  // untouched
         const int mx = loMC.x + k % wx, my = loMC.y + (k / wx) % wy, mz = loMC.z + k / (wx * wy);
-        update_mc(mcRanges, dims, mx, my, mz, lo, hi);
+        update_mc(mcRanges, dims, mx, my, mz, ord_value(lo), ord_value(hi));
       }
     if (tid == 0) {
       for (int w = 1; w < kMajThreads / 32; ++w) {
