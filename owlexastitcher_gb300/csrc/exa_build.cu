@@ -205,13 +205,13 @@ EXA_D uint32_t ord_key(float v)
 }
 EXA_D float ord_value(uint32_t k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
 
-// thread 0: the plan of gridlet gi and the bulk copy of its brick into
+// thread 0: the plan of gridlet g and the bulk copy of its brick into
 // buffer buf
-EXA_D void prepare_gridlet(MajSmem &sm, int buf, const exa_gridlet *gridlets, size_t gi, const float *scalars,
-                           size_t nScalars, bool stage, const V3i D, const exa_box3f &wb)
+EXA_D void prepare_gridlet(MajSmem &sm, int buf, const exa_gridlet &hdr, const float *scalars, size_t nScalars,
+                           bool stage, const V3i D, const exa_box3f &wb)
 {
   GridletPlan &pl = sm.plan[buf];
-  pl.g = gridlets[gi];
+  pl.g = hdr;
   pl.P = brick_plan(pl.g, nScalars, stage);
   if (pl.P.bulk) bulk_load_smem(sm.brick[buf], scalars + pl.P.f0, pl.P.bulk, &sm.bar[buf]);
   const exa_gridlet &g = pl.g;
@@ -233,11 +233,15 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
   __shared__ MajSmem sm;
   const int tid = threadIdx.x;
   const V3i D = {dims.x, dims.y, dims.z};
+  // thread 0 holds the header of the gridlet after the next one, loaded an
+  // iteration before it is planned
+  exa_gridlet ahead{};
   if (tid == 0) {
     mbar_init(&sm.bar[0]);
     mbar_init(&sm.bar[1]);
     mbar_init_fence();
-    if (blockIdx.x < ng) prepare_gridlet(sm, 0, gridlets, blockIdx.x, scalars, nScalars, stage, D, wb);
+    if (blockIdx.x < ng) prepare_gridlet(sm, 0, gridlets[blockIdx.x], scalars, nScalars, stage, D, wb);
+    if (blockIdx.x + gridDim.x < ng) ahead = gridlets[blockIdx.x + gridDim.x];
   }
   __syncthreads();
   const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
@@ -251,7 +255,8 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
     const size_t gn = gi + gridDim.x;
     if (tid == 0 && gn < ng) {
       fence_proxy_async_smem();
-      prepare_gridlet(sm, buf ^ 1, gridlets, gn, scalars, nScalars, stage, D, wb);
+      prepare_gridlet(sm, buf ^ 1, ahead, scalars, nScalars, stage, D, wb);
+      if (gn + gridDim.x < ng) ahead = gridlets[gn + gridDim.x];
     }
     const float *S = scalars + (uint32_t)g.begin;
     if (P.staged) {

@@ -388,8 +388,11 @@ EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
 
 // the collision test of one step given its sample; primID -1 is empty
 // space, -2 a value of the learned field (never cached).  Returns false
-// when the walk ended.
-EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const exa_sample &s)
+// when the walk ended.  `teaser`: the frame renders the Teaser shade mode
+// (a compile-time constant in every caller, so that the other frames carry
+// none of its code).
+EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const exa_sample &s,
+                        const bool teaser = false)
 {
   const exa_launch_params &lp = c.lp;
   const float scale = lp.transferFunc.opacityScale;
@@ -406,7 +409,7 @@ EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const 
       // the Teaser shade mode blends the albedo by screen position at the
       // event; the walk passes on the sample's checker colour in xf.w,
       // which the event does not read otherwise
-      if (lp.shadeMode == EXA_SHADE_MODE_TEASER) w.xf.w = (float)checker_index(c.A, s);
+      if (teaser) w.xf.w = (float)checker_index(c.A, s);
       return false;
     }
   } else {
@@ -441,6 +444,7 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
 #ifndef EXA_WF_ITER_STEPS
 #define EXA_WF_ITER_STEPS 1
 #endif
+template <bool TEASER = false>
 EXA_D bool walk_iteration(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
 {
   for (int k = 0; k < EXA_WF_ITER_STEPS; ++k) {
@@ -451,7 +455,7 @@ EXA_D bool walk_iteration(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
     if (st == WALK_END) return false;
     if (st == WALK_ON) continue;
     const exa_sample s = walk_sample_exact(w, c);
-    if (!walk_collide(w, c, rng, shadow, s)) return false;
+    if (!walk_collide(w, c, rng, shadow, s, TEASER)) return false;
   }
   return true;
 }
@@ -1469,6 +1473,7 @@ __global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ Accel
 // queue and fetches the next walk (one atomic per warp).  Lanes stay busy
 // until the input is used up; then, in a large round, a warp left with few
 // walking lanes parks their walks in the next round's input and exits.
+template <bool TEASER>
 __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __grid_constant__ AccelView A,
                                                                         const __grid_constant__ exa_launch_params lp,
                                                                         WfQueues Q)
@@ -1509,7 +1514,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
       }
       break;
     }
-    const bool ended = active && !walk_iteration(L.w, c, L.rng, L.shadow);
+    const bool ended = active && !walk_iteration<TEASER>(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
       wf_store_event(L, Q.ev, Q.cap, slot, src);
@@ -1676,10 +1681,11 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
 #if EXA_WALK_CARVEOUT >= 0
     // the walk kernel needs little shared memory; the rest of the unified
     // L1 / shared array serves as L1 for its field and table loads
-    cudaCheck(cudaFuncSetAttribute(k_wf_walk, cudaFuncAttributePreferredSharedMemoryCarveout, EXA_WALK_CARVEOUT),
-              "walk carveout");
+    for (auto *k : {k_wf_walk<false>, k_wf_walk<true>})
+      cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, EXA_WALK_CARVEOUT),
+                "walk carveout");
 #endif
-    cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk, 128, 0), "occupancy");
+    cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk<false>, 128, 0), "occupancy");
   }
   const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
   // per-kernel-class timing on this stream: camera, walk, events
@@ -1705,7 +1711,8 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     }
     cudaCheck(cudaEventRecord(ev[1], s), "event");
     if (sur) k_wf_walk_sur<<<walkGrid, 128, kSurWalkSmem, s>>>(A, lp, Q, *sur);
-    else k_wf_walk<<<walkGrid, 128, 0, s>>>(A, lp, Q);
+    else if (lp.shadeMode == EXA_SHADE_MODE_TEASER) k_wf_walk<true><<<walkGrid, 128, 0, s>>>(A, lp, Q);
+    else k_wf_walk<false><<<walkGrid, 128, 0, s>>>(A, lp, Q);
     cudaCheck(cudaEventRecord(ev[2], s), "event");
     if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
     else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
