@@ -101,19 +101,19 @@ EXA_D void exa_sincos_turns(float u, float &s, float &c)
 // deviceCode.cu:41,1278): key from (pixel, accumID, frameID, sample); the
 // n-th draw is mix64(key + n*golden) >> 40 scaled by 2^-24.  One stream per
 // camera sample makes every (pixel, sample) an independent unit of work.
+// The state is the running sum key + n*golden (mod 2^64), so a draw is one
+// 64-bit add and the mix.
 struct Rng {
-  uint64_t key;
-  uint32_t counter;
+  uint64_t state;
   EXA_D void init(uint32_t pixelID, uint32_t accumID, uint32_t frameID, uint32_t sampleID)
   {
-    key = mix64((((uint64_t)pixelID << 32) | (uint64_t)accumID) ^
-                mix64((((uint64_t)frameID << 32) | (uint64_t)sampleID) + 0x5851f42d4c957f2dull));
-    counter = 0;
+    state = mix64((((uint64_t)pixelID << 32) | (uint64_t)accumID) ^
+                  mix64((((uint64_t)frameID << 32) | (uint64_t)sampleID) + 0x5851f42d4c957f2dull));
   }
   EXA_D float next()
   {
-    counter += 1;
-    const uint64_t z = mix64(key + (uint64_t)counter * 0x9e3779b97f4a7c15ull);
+    state += 0x9e3779b97f4a7c15ull;
+    const uint64_t z = mix64(state);
     return (float)(uint32_t)(z >> 40) * 5.96046448e-08f;
   }
 };

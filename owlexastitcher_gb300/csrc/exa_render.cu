@@ -1309,7 +1309,7 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, b
   unsigned k = kPathStride;
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2) | (fresh ? kWalkFresh : 0u));
-  W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 3: unused
   WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
   W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
@@ -1329,8 +1329,8 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.needCell = (flags >> 1) & 1u;
   w.type = (int)((flags & ~kWalkFresh) >> 2);
   const uint32_t lo = R(), hi = R();
-  L.rng.key = ((uint64_t)hi << 32) | lo;
-  L.rng.counter = R();
+  L.rng.state = ((uint64_t)hi << 32) | lo;
+  ++k;
   w.org.x = RF(); w.org.y = RF(); w.org.z = RF(); w.dir.x = RF(); w.dir.y = RF(); w.dir.z = RF();
   w.dda.tnext.x = RF(); w.dda.tnext.y = RF(); w.dda.tnext.z = RF();
   w.dda.dist.x = RF(); w.dda.dist.y = RF(); w.dda.dist.z = RF();
@@ -1368,7 +1368,7 @@ EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, 
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.type << 2) | ((uint32_t)w.ncells << 8));
   W(src);
-  W((uint32_t)L.rng.key); W((uint32_t)(L.rng.key >> 32)); W(L.rng.counter);
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 4: unused
   WF(w.t); WF(w.Tr);
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z);
   WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
@@ -1385,8 +1385,8 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
   w.ncells = (int)(flags >> 8);
   const unsigned src = R();
   const uint32_t lo = R(), hi = R();
-  L.rng.key = ((uint64_t)hi << 32) | lo;
-  L.rng.counter = R();
+  L.rng.state = ((uint64_t)hi << 32) | lo;
+  ++k;
   w.t = RF(); w.Tr = RF();
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
