@@ -78,3 +78,21 @@ def test_majorant_build_edges(cuda, native, oracle, case, dims):
     gr, _, _ = sampler.prim_majorants()
     assert same_floats(gr, f.gridlet_value_ranges())
     ctx.close()
+
+
+def test_build_stats(cuda, native):
+    """exa_get_build_stats: the build's own CUDA-event times of the majorant
+    kernels (no reference counterpart)"""
+    from owlexastitcher_gb300 import exastitch as E
+    gl, s = edge_model(CASES[0][1])
+    ctx = E.Context(0)
+    assert ctx.build_stats()["majorantBlocks"] == 0
+    model = E.ExaStitchModel(ctx, np.zeros((0, 4), np.float32), np.zeros((0, 8), np.int32), gl, s)
+    model.setNumGridCells((16, 16, 16))
+    E.ExaStitchSampler(ctx).build(model)
+    st = ctx.build_stats()
+    assert 0 < st["majorantBlocks"] <= len(gl)
+    assert st["gridletMajorantMs"] > 0 and st["elemMajorantMs"] >= 0
+    assert st["totalMs"] >= st["gridletMajorantMs"]
+    assert ctx.device_errors() == 0
+    ctx.close()
