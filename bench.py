@@ -608,7 +608,7 @@ def run_small_config(a, local, flush, cpu=True):
     import ctypes as C
     import torch
     import pyoracle
-    from helpers import orbit_camera, ramp_tf, setup_render
+    from helpers import host_lp, orbit_camera, ramp_tf, setup_render
     from owlexastitcher_gb300 import datagen
     from owlexastitcher_gb300 import exastitch as E
     ds = datagen.Dataset("small")
@@ -686,9 +686,18 @@ def run_small_config(a, local, flush, cpu=True):
         t0 = time.perf_counter()
         f.majorants((128, 128, 128), lo, hi)
         maj128 = (time.perf_counter() - t0) * 1e3
+        # (ii) on the host: the oracle integrator renders the same frame (the
+        # parity tests show it bit-identical), all threads and one thread
+        _, ops = sampler.majorants((32, 32, 32))
+        _, gops, eops = sampler.prim_majorants()
+        o = _oracle_scene(a, ds, lp, ops, gops, eops, ramp_tf())
+        hl, *_ = host_lp(lp, o, w, h)
+        dl_n, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, n)
+        dl_1, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, 1)
         out["cpu"] = {"cores": n, "kind": "port", "points_per_s": cpu_pts, "points_per_s_1_core": cpu_pts1,
+                      "render_256_1spp_dl_paths_per_s": dl_n, "render_256_1spp_dl_paths_per_s_1_core": dl_1,
                       "majorant_build_32^3_ms": maj32, "majorant_build_128^3_ms": maj128,
-                      "note": "oracle/oracle.c point location (uniform-grid accel) and majorant build"}
+                      "note": "oracle/oracle.c point location (uniform-grid accel), integrator and majorant build"}
     ctx.close()
     out["amrcell_sampler"] = run_comparison_small(ds, local, P, flush, stream, "amrcell")
     out["exabrick_sampler"] = run_comparison_small(ds, local, P, flush, stream, "exabrick")
