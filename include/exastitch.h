@@ -279,7 +279,10 @@ int exa_get_device_errors(exa_context *ctx, uint32_t *bits);
 const char *exa_version(void);
 /* sizeof of the ABI structs, for FFI bindings to check their layouts:
  * 0 exa_launch_params, 1 exa_gridlet, 2 exa_sample, 3 exa_mem_stats,
- * 4 exa_lp_ext; 0 for other keys. */
+ * 4 exa_lp_ext, 5 exa_surrogate_params, 6 exa_surrogate_stats,
+ * 7 exa_surrogate_geometry, 8 exa_batch_frame, 9 exa_batch_tuning,
+ * 10 exa_xf, 11 exa_amr_cell, 12 exa_render_stats, 13 exa_build_stats,
+ * 14 exa_brick, 15 exa_abr; 0 for other keys. */
 uint64_t exa_abi_sizeof(int32_t which);
 
 /* ------------------------------------------------------------------ */

@@ -883,6 +883,10 @@ uint64_t exa_abi_sizeof(int32_t which)
     case 9: return sizeof(exa_batch_tuning);
     case 10: return sizeof(exa_xf);
     case 11: return sizeof(exa_amr_cell);
+    case 12: return sizeof(exa_render_stats);
+    case 13: return sizeof(exa_build_stats);
+    case 14: return sizeof(exa_brick);
+    case 15: return sizeof(exa_abr);
     default: return 0;
   }
 }

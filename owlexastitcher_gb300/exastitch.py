@@ -341,9 +341,13 @@ def lib():
         f.argtypes = args
         f.restype = res
     for key, st in ((0, LaunchParams), (1, Gridlet), (2, Sample), (3, MemStats), (4, LPExt), (5, SurrogateParams),
-                    (6, SurrogateStats), (7, SurrogateGeometry), (8, BatchFrame), (9, BatchTuning), (10, Xf), (11, AmrCell)):
+                    (6, SurrogateStats), (7, SurrogateGeometry), (8, BatchFrame), (9, BatchTuning), (10, Xf), (11, AmrCell),
+                    (12, RenderStats), (13, BuildStats)):
         if L.exa_abi_sizeof(key) != C.sizeof(st):
             raise RuntimeError(f"ABI layout mismatch for {st.__name__}: C {L.exa_abi_sizeof(key)} vs ctypes {C.sizeof(st)}")
+    for key, dt in ((14, BRICK_DTYPE), (15, ABR_DTYPE)):
+        if L.exa_abi_sizeof(key) != dt.itemsize:
+            raise RuntimeError(f"ABI layout mismatch for key {key}: C {L.exa_abi_sizeof(key)} vs numpy {dt.itemsize}")
     _lib = L
     return L
 

@@ -43,6 +43,9 @@ def test_abi_sizes(native):
     L = E.lib()
     assert L.exa_abi_sizeof(0) == E.C.sizeof(E.LaunchParams)
     assert L.exa_abi_sizeof(1) == 32 and L.exa_abi_sizeof(2) == 12
+    assert L.exa_abi_sizeof(12) == E.C.sizeof(E.RenderStats) and L.exa_abi_sizeof(13) == E.C.sizeof(E.BuildStats)
+    assert L.exa_abi_sizeof(14) == E.BRICK_DTYPE.itemsize and L.exa_abi_sizeof(15) == E.ABR_DTYPE.itemsize
+    assert L.exa_abi_sizeof(16) == 0
     assert L.exa_sampler_class_name() == b"ExaStitchSampler"
 
 
