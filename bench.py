@@ -8,6 +8,12 @@ JSON line (rank 0).  `--impl reference` times the CPU oracle's restatement
 of the same integrator on the host cores instead (a bounded pixel sample per
 step).  Multi-GPU runs (torchrun) render independent frames per rank
 (replicas: no data-path collective), scaling = weak.
+
+Beside the headline, the line carries: the walk kernel's roofline, field
+sample rates, the end-to-end rate through the C ABI, the CPU baseline, SM
+clocks, the majorant build of the workload's field (`majorant_build`: the
+gridlet kernel's CUDA-event time and roofline), the learned field, the
+batched frames and the small configuration (with its host timings).
 """
 import argparse
 import json
