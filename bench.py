@@ -698,8 +698,9 @@ def run_small_config(a, local, flush, cpu=True):
         _, gops, eops = sampler.prim_majorants()
         o = _oracle_scene(a, ds, lp, ops, gops, eops, ramp_tf())
         hl, *_ = host_lp(lp, o, w, h)
-        dl_n, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, n)
-        dl_1, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, 1)
+        # 32-row bands: a 256-pixel row per call is too little work to spread over the cores
+        dl_n, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, n, band_rows=32)
+        dl_1, _, _ = _cpu_render_rate(o, hl, w, h, 1, 2.0, 1, band_rows=32)
         out["cpu"] = {"cores": n, "kind": "port", "points_per_s": cpu_pts, "points_per_s_1_core": cpu_pts1,
                       "render_256_1spp_dl_paths_per_s": dl_n, "render_256_1spp_dl_paths_per_s_1_core": dl_1,
                       "majorant_build_32^3_ms": maj32, "majorant_build_128^3_ms": maj128,
@@ -791,16 +792,15 @@ def _oracle_scene(a, ds, lp_src, max_ops, gops, eops, tf):
     return o
 
 
-def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads):
-    """Renders bands of rows spread over the frame until budget_s is used;
-    returns (paths/s, pixels rendered, seconds)."""
+def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads, band_rows=1):
+    """Renders bands of `band_rows` rows spread over the frame until
+    budget_s is used; returns (paths/s, pixels rendered, seconds)."""
     rows = h
     bands = 16
-    band_rows = 1
     total_px, total_s = 0, 0.0
     for b in range(bands * 64):
         y = (b * 37) % rows
-        pb, pe = y * w, (y + band_rows) * w
+        pb, pe = y * w, min(y + band_rows, rows) * w
         t0 = time.perf_counter()
         o.f.render(bytes(hl), w, h, pb, pe, nthreads)
         total_s += time.perf_counter() - t0
