@@ -231,6 +231,9 @@ def run_ours(a):
         barrier()
     ctx.sync()
     render_stats = ctx.render_stats()
+    # the last timed frame (accumID 0: the accumulation buffer holds its
+    # per-pixel sums) for the CPU leg's bit-for-bit comparison
+    timed_frame = (r.accum.cpu().numpy().reshape(-1, 4).copy(), r.fb.cpu().numpy().view(np.uint32).copy())
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = replicas.slowest_ms(sum(step_ms) / len(step_ms), world, device="cuda")
     value = replicas.job_paths_per_s(world, paths_per_step, ms)
@@ -297,9 +300,9 @@ def run_ours(a):
     if rank == 0 and not a.profile_only:
         majorants = majorant_build(ds, local, NUM_MCS, peak, peak_kind)
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, ds, r, budget_s=a.cpu_seconds)
+        cpu, parity = cpu_baseline(a, ds, r, a.cpu_seconds, timed_frame)
 
     small = None
     if rank == 0 and world == 1 and a.config != "cloud":
@@ -343,6 +346,7 @@ def run_ours(a):
             "e2e": {"value": world * paths_per_step / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": lp_bytes,
                     "d2h_bytes_per_step": a.width * a.height * 4},
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clocks,
             "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
             "render": render_stats,
@@ -792,9 +796,10 @@ def _oracle_scene(a, ds, lp_src, max_ops, gops, eops, tf):
     return o
 
 
-def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads, band_rows=1):
+def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads, band_rows=1, rows_out=None):
     """Renders bands of `band_rows` rows spread over the frame until
-    budget_s is used; returns (paths/s, pixels rendered, seconds)."""
+    budget_s is used; returns (paths/s, pixels rendered, seconds).  The
+    first rows of the bands rendered are appended to rows_out."""
     rows = h
     bands = 16
     total_px, total_s = 0, 0.0
@@ -805,23 +810,76 @@ def _cpu_render_rate(o, hl, w, h, spp, budget_s, nthreads, band_rows=1):
         o.f.render(bytes(hl), w, h, pb, pe, nthreads)
         total_s += time.perf_counter() - t0
         total_px += pe - pb
+        if rows_out is not None:
+            rows_out.append(y)
         if total_s >= budget_s:
             break
     return total_px * spp / total_s, total_px, total_s
 
 
-def cpu_baseline(a, ds, r, budget_s):
-    """The oracle integrator on the host cores, all threads (OpenMP)."""
+def _oracle_workload(ds, tf):
+    """The workload's scene on the oracle, built from the dataset arrays
+    alone: its own bounds, value range, majorant build and max opacities."""
+    import pyoracle
+    f = pyoracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+    lo, hi, vr = f.bounds()
+    xf = (np.float32(vr[0]), np.float32(vr[1]))
+    t0 = time.perf_counter()
+    ranges = f.majorants(NUM_MCS, lo, hi)
+    build_s = time.perf_counter() - t0
+    ops = pyoracle.max_opacities(ranges, tf, xf)
+    gops = pyoracle.max_opacities(f.gridlet_value_ranges(), tf, xf) if len(ds.gridlets) else np.zeros(0, np.float32)
+    eops = f.elem_max_opacities(tf, xf) if len(ds.indices) else np.zeros(0, np.float32)
+    f.set_prim_opacities(gops if len(gops) else None, eops if len(eops) else None)
+
+    class O:
+        pass
+    o = O()
+    o.f, o.tf, o.max_ops = f, np.ascontiguousarray(tf, np.float32), np.ascontiguousarray(ops)
+    o.ranges, o.lo, o.hi, o.xf, o.build_s = ranges, lo, hi, xf, build_s
+    return o
+
+
+def _same_floats(a, b):
+    """bit-equal float arrays, except that +0 and -0 compare equal (the
+    sign of a zero from competing min/max updates is order dependent in the
+    reference too)"""
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    return bool(np.array_equal(a, b) and np.array_equal(np.isnan(a), np.isnan(b)))
+
+
+def cpu_baseline(a, ds, r, budget_s, timed_frame):
+    """The oracle integrator on the host cores, all threads (OpenMP), on
+    rows of the benchmarked frame, with the oracle's own majorant build.
+    Returns (cpu_baseline, parity): parity compares the oracle's majorant
+    ranges and max opacities with the GPU build, and the oracle's rendered
+    rows with the same rows of the last timed GPU frame, bit for bit."""
     from helpers import host_lp
     n = os.cpu_count()
-    ranges, ops = r.sampler.majorants(NUM_MCS)
-    _, gops, eops = r.sampler.prim_majorants()
-    o = _oracle_scene(a, ds, r.lp, ops, gops, eops, r.colorMap)
-    hl, *_ = host_lp(r.lp, o, a.width, a.height)
-    rate, px, secs = _cpu_render_rate(o, hl, a.width, a.height, a.spp, budget_s, n)
-    return {"value": rate, "unit": "paths/s", "cores": n, "kind": "port",
-            "sample": f"{px} pixels x {a.spp} spp (rows spread over the frame), {secs:.1f} s, oracle/oracle.c "
-                      f"with OpenMP; majorants taken from the GPU build (bit-identical in the parity tests)"}
+    o = _oracle_workload(ds, r.colorMap)
+    g_ranges, g_ops = r.sampler.majorants(NUM_MCS)
+    glo, ghi = r.model.cellBounds
+    hl, hfb, hacc, _, _ = host_lp(r.lp, o, a.width, a.height)
+    rows = []
+    rate, px, secs = _cpu_render_rate(o, hl, a.width, a.height, a.spp, budget_s, n, rows_out=rows)
+    acc, fb = timed_frame
+    sel = np.concatenate([np.arange(y * a.width, (y + 1) * a.width) for y in sorted(set(rows))])
+    bad_px = int(np.count_nonzero((acc[sel] != hacc[sel]).any(axis=1) | (fb[sel] != hfb[sel])))
+    parity = {
+        "against": "oracle/oracle.c (own bounds, majorant build and max opacities from the dataset arrays)",
+        "majorant_grid": list(NUM_MCS),
+        "cell_bounds_equal": bool(np.array_equal(o.lo, glo) and np.array_equal(o.hi, ghi)),
+        "majorant_ranges_bit_exact": _same_floats(o.ranges, g_ranges),
+        "max_opacities_bit_exact": bool(o.max_ops.tobytes() == g_ops.tobytes()),
+        "oracle_majorant_build_s": o.build_s,
+        "frame": "the last timed frame (accumulation buffer sums and RGBA8 pixels)",
+        "rows": len(set(rows)), "pixels": int(len(sel)), "mismatched_pixels": bad_px,
+        "bit_exact": bool(acc[sel].tobytes() == hacc[sel].tobytes() and np.array_equal(fb[sel], hfb[sel])),
+    }
+    cpu = {"value": rate, "unit": "paths/s", "cores": n, "kind": "port",
+           "sample": f"{px} pixels x {a.spp} spp (rows spread over the frame), {secs:.1f} s, oracle/oracle.c "
+                     f"with OpenMP, majorants from the oracle's own build"}
+    return cpu, parity
 
 
 def run_reference(a):
@@ -834,21 +892,25 @@ def run_reference(a):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement's field structures for the "
                           "~400M-cell cloud exceed a bounded CPU sample; the reference arm is defined on medium"}))
         return
-    import ctypes as C
-    import pyoracle
+    import shutil
+    import tempfile
     from helpers import host_lp, orbit_camera, ramp_tf, setup_render
-    from owlexastitcher_gb300 import datagen
-    from owlexastitcher_gb300 import exastitch as E
-    ds = datagen.Dataset(a.config)
-    f = pyoracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
-    lo, hi, vr = f.bounds()
+    from owlexastitcher_gb300 import exastitch as E  # launch-parameter layout only; no library is loaded
+    # the dataset's arrays come from the generator run as a separate process
+    # (as the reference's amrMakeDualMesh tool writes files its renderer
+    # loads): this process loads no library of the GPU path
+    tmp = tempfile.mkdtemp(prefix="exa_ref_")
+    try:
+        path = os.path.join(tmp, a.config + ".npz")
+        subprocess.check_call([sys.executable, "-m", "owlexastitcher_gb300.datagen", "--config", a.config, "--out",
+                               path], cwd=ROOT)
+        with np.load(path) as z:
+            ds = type("Arrays", (), {k: z[k] for k in ("vertices", "indices", "gridlets", "gridlet_scalars")})
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
     tf = ramp_tf()
-    xf = (np.float32(vr[0]), np.float32(vr[1]))
-    ranges = f.majorants(NUM_MCS, lo, hi)
-    ops = pyoracle.max_opacities(ranges, tf, xf)
-    gops = pyoracle.max_opacities(f.gridlet_value_ranges(), tf, xf) if len(ds.gridlets) else np.zeros(0, np.float32)
-    eops = f.elem_max_opacities(tf, xf) if len(ds.indices) else np.zeros(0, np.float32)
-    f.set_prim_opacities(gops if len(gops) else None, eops if len(eops) else None)
+    o = _oracle_workload(ds, tf)
+    lo, hi, xf = o.lo, o.hi, o.xf
     lp = E.LaunchParams()
     lp.integrator = 0
     lp.render.dt = 1.0
@@ -863,11 +925,6 @@ def run_reference(a):
     lp.ext.cullTransparentPrims = 1
     cam = orbit_camera(lo, hi, a.width, a.height)
     setup_render(lp, cam, a.width, a.height, 0, a.spp, "directional", True)
-
-    class O:
-        pass
-    o = O()
-    o.f, o.tf, o.max_ops = f, np.ascontiguousarray(tf), np.ascontiguousarray(ops)
     hl, *_ = host_lp(lp, o, a.width, a.height)
     n = os.cpu_count()
     per_step = max(1.0, a.cpu_seconds / max(1, a.steps + a.warmup))

@@ -2158,6 +2158,11 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    // as in exa_render: the AMR-cell and ExaBrick samplers have no gridlet
+    // cells to colour
+    need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||
+             lp->shadeMode == EXA_SHADE_MODE_DEFAULT,
+         EXA_ERR_INVALID, "the AMR-cell and ExaBrick samplers render shade mode default only");
     need(ctx->device >= 0 && ctx->device < 256, EXA_ERR_INVALID, "device index out of range");
     setDevice(ctx);
     float4 *scratch = nullptr;

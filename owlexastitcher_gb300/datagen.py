@@ -218,3 +218,24 @@ def amr_to_bricks(cells, scalars, max_len=8):
         return np.zeros(0, BRICK_DTYPE), np.zeros(0, np.float32)
     return np.concatenate(out_b), np.concatenate(out_s)
 
+
+
+def main(argv=None):
+    """Writes a configuration's dual-mesh arrays (vertices, indices,
+    gridlets, gridlet_scalars) to an uncompressed .npz file:
+        python -m owlexastitcher_gb300.datagen --config medium --out medium.npz"""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="small")
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--balance", type=int, default=None)
+    a = ap.parse_args(argv)
+    kw = {} if a.balance is None else {"balance": a.balance}
+    ds = Dataset(a.config, **kw)
+    with open(a.out, "wb") as f:
+        np.savez(f, vertices=ds.vertices, indices=ds.indices, gridlets=ds.gridlets,
+                 gridlet_scalars=ds.gridlet_scalars)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""Stitching elements on the CUDA path against the golden vectors that the
+reference's own headers produced (tests/golden/elements.npz, made by
+tests/golden/make_golden.py from Plane.h:57-99 intersectTet with its
+`fa > 1` tests at :89,92,95, and UElems.h intersectPyrEXT / intersectWedgeEXT /
+intersectHexEXT).
+
+Each element type's 400 golden elements form one element-only model; every
+golden point is sampled through exa_sample_points_host.  Where the point lies
+in no other element of the model (the oracle's list of every containing
+primitive decides), the GPU's answer must be the golden one: the hit flag,
+the element id and the value's bits.  A quarter of the points sit on a
+vertex or an edge midpoint (boundary cases of the inside tests)."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def element_model(V):
+    """vertices (x, y, z, value) and 8-wide -1 padded index rows of n
+    elements with nv vertices each"""
+    n, nv, _ = V.shape
+    verts = np.ascontiguousarray(V.reshape(-1, 4), np.float32)
+    idx = -np.ones((n, 8), np.int32)
+    idx[:, :nv] = np.arange(n * nv, dtype=np.int32).reshape(n, nv)
+    return verts, idx
+
+
+@pytest.mark.parametrize("nv", [4, 5, 6, 8], ids=["tet", "pyramid", "wedge", "hex"])
+def test_elements_golden_on_gpu(cuda, native, oracle, nv):
+    from owlexastitcher_gb300 import exastitch as E
+    g = np.load(os.path.join(GOLD, "elements.npz"))
+    V, P, hit, val = g[f"V_{nv}"], g[f"P_{nv}"], g[f"hit_{nv}"], g[f"val_{nv}"]
+    verts, idx = element_model(V)
+    ctx = E.Context(0)
+    model = E.ExaStitchModel(ctx, verts, idx, np.zeros(0, E.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    model.setNumGridCells((8, 8, 8))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    got = sampler.sample_host(P)
+    assert ctx.device_errors() == 0
+    f = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    checked = hits = 0
+    for i in range(len(P)):
+        others = [pid for kind, pid, _ in f.sample_all(P[i]) if pid != i]
+        if others:
+            continue  # another golden element contains the point as well
+        checked += 1
+        if hit[i]:
+            hits += 1
+            assert got["primID"][i] == i and got["cellID"][i] == -1, i
+            assert got["value"][i:i + 1].tobytes() == val[i:i + 1].tobytes(), (i, got["value"][i], val[i])
+        else:
+            assert got["primID"][i] < 0, i
+    assert checked >= 0.95 * len(P)
+    assert hits > 20
+    ctx.close()
+
+
+def test_tets_in_unbalanced_dataset_sampled(cuda, native, oracle):
+    """The unbalanced small dataset's dual mesh holds tetrahedra: points at
+    their centroids (and at their vertices) sample bit-exact with the oracle
+    and mostly report a tet."""
+    from conftest import dataset
+    from owlexastitcher_gb300 import exastitch as E
+    ds = dataset("small", balance=0)
+    nvs = np.count_nonzero(ds.indices >= 0, axis=1)
+    tets = np.nonzero(nvs == 4)[0]
+    assert len(tets) > 1000
+    corners = ds.vertices[ds.indices[tets, :4]][:, :, :3]
+    P = np.concatenate([corners.mean(axis=1), corners[:, 0]]).astype(np.float32)
+    ctx = E.Context(0)
+    model = E.ExaStitchModel.from_dataset(ctx, ds)
+    model.setNumGridCells((32, 32, 32))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    got = sampler.sample_host(P)
+    want = oracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars).sample(P)
+    assert np.array_equal(got["primID"], want["primID"]) and np.array_equal(got["cellID"], want["cellID"])
+    assert got["value"].tobytes() == want["value"].tobytes()
+    centroid = got[: len(tets)]
+    is_tet = (centroid["cellID"] == -1) & (centroid["primID"] >= 0)
+    is_tet[is_tet] = nvs[centroid["primID"][is_tet]] == 4
+    assert is_tet.mean() > 0.5
+    ctx.close()

@@ -15,7 +15,10 @@ from helpers import GpuScene, OracleScene, host_lp, orbit_camera, ramp_tf, setup
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = [("tiny", (8, 8, 8)), ("small", (32, 32, 32))]
+# (name, generator configuration, generator overrides, majorant grid); the
+# unbalanced small field (no 2:1 balance) has tetrahedra in its dual mesh
+CONFIGS = [("tiny", "tiny", {}, (8, 8, 8)), ("small", "small", {}, (32, 32, 32)),
+           ("small_unbalanced", "small", {"balance": 0}, (32, 32, 32))]
 
 
 @pytest.fixture(scope="module")
@@ -28,8 +31,8 @@ def torch_cuda():
 
 @pytest.fixture(scope="module", params=CONFIGS, ids=[c[0] for c in CONFIGS])
 def scenes(request, torch_cuda, native, oracle):
-    cfg, dims = request.param
-    ds = dataset(cfg)
+    name, cfg, kw, dims = request.param
+    ds = dataset(cfg, **kw)
     g = GpuScene(ds, dims)
     o = OracleScene(oracle, ds, dims, g.lo, g.hi, g.tf, g.xf)
     return ds, g, o

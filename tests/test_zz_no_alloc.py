@@ -75,3 +75,35 @@ def test_noalloc_rejects_oversized_frame(scene):
     rc = E.lib().exa_render_noalloc(g.ctx.h, C.byref(lp), 1024, 1024)
     assert rc == E.EXA_ERR_INVALID
     assert b"exceeds its static scratch" in E.lib().exa_last_error()
+
+
+def test_noalloc_rejects_gridlet_shading_without_gridlets(scene):
+    """The AMR-cell sampler has no gridlet cells to colour: both entry points
+    refuse shade mode "gridlets" for it instead of painting every sample."""
+    torch, _ = scene
+    from owlexastitcher_gb300 import exastitch as E
+    ds = dataset("tiny")
+    ctx = E.Context(0)
+    model = E.AMRCellModel.from_dataset(ctx, ds)
+    model.setNumGridCells((8, 8, 8))
+    sampler = E.AMRCellSampler(ctx)
+    sampler.build(model)
+    vr = model.valueRange
+    from helpers import ramp_tf
+    sampler.computeMaxOpacities(ramp_tf(), (np.float32(vr[0]), np.float32(vr[1])))
+    lp = E.new_launch_params()
+    sampler.setLPs(lp)
+    lo, hi = model.cellBounds
+    w = h = 16
+    setup_render(lp, orbit_camera(lo, hi, w, h), w, h, E.DIRECT_LIGHT_INTEGRATOR, 1, "directional", False)
+    fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), None
+    lp.ext.traceT = lp.ext.traceTr = None
+    lp.shadeMode = E.SHADE_MODE_GRIDLETS
+    for entry in ("exa_render", "exa_render_noalloc"):
+        assert getattr(E.lib(), entry)(ctx.h, C.byref(lp), w, h) == E.EXA_ERR_INVALID, entry
+        assert b"shade mode default" in E.lib().exa_last_error()
+    lp.shadeMode = E.SHADE_MODE_DEFAULT
+    E._check(E.lib().exa_render_noalloc(ctx.h, C.byref(lp), w, h))
+    ctx.sync()
+    ctx.close()
