@@ -41,9 +41,14 @@ extern "C" {
 #define EXA_DEVERR_DDA_CAP      1u  /* DDA walked more cells than the grid has */
 #define EXA_DEVERR_TRACK_CAP    2u  /* delta/ratio tracking step cap            */
 #define EXA_DEVERR_BVH_STACK    4u  /* element-BVH traversal stack overflow     */
-#define EXA_DEVERR_BOUNCE_CAP   8u  /* path exceeded the hard bounce cap        */
+#define EXA_DEVERR_BOUNCE_CAP   8u  /* reserved (paths end at ext.maxBounces)    */
 #define EXA_DEVERR_WATCHDOG    16u  /* persistent-kernel work loop cap          */
 #define EXA_DEVERR_COPY_WAIT   32u  /* bulk copy to shared memory: wait limit   */
+
+/* exa_debug_set_flags: simulations of error paths for tests */
+#define EXA_DEBUG_COPY_WAIT_TIMEOUT 1u  /* the majorant build's first bulk-copy */
+                                        /* wait in block 0 counts as timed out  */
+                                        /* after the copy completed             */
 
 /* ------------------------------------------------------------------ */
 /* plain data types (layouts equal to the owl::common types they       */
@@ -148,6 +153,19 @@ typedef struct {
 #define EXA_LIGHT_POINT       0
 #define EXA_LIGHT_DIRECTIONAL 1
 
+/* Transfer-function lookup (deviceCode.cu:320-341).  NEAREST is the
+ * reference's buffer variant: the entry int(f * N) of the clamped,
+ * normalised value f.  LINEAR restates its default texture variant
+ * (EXASTITCH_CUDA_TEXTURE_TF, CMakeLists.txt:179-187; the texture set up in
+ * OWLRenderer.cpp:659-707: normalised coordinates, linear filtering, border
+ * address mode with a zero border colour) in binary32 arithmetic:
+ * xB = f * N - 0.5, i = floor(xB), a = xB - i,
+ * result = (1 - a) * T[i] + a * T[i + 1] per channel, limited to the
+ * channel's range of the two entries, with T[k] = 0 outside [0, N).  The
+ * hardware filter's 8-bit fraction of `a` is not reproduced. */
+#define EXA_TF_FILTER_NEAREST 0
+#define EXA_TF_FILTER_LINEAR  1
+
 /* Fields appended after the reference's LaunchParams fields.  They have no
  * reference counterpart; their defaults (exa_launch_params_init) reproduce
  * the reference's hard-coded behaviour. */
@@ -170,7 +188,9 @@ typedef struct {
                              /* [4] paths; wavefront renderer also: [5]      */
                              /* gridlet-cache misses, [6] table queries,     */
                              /* [7] gridlet tests, [8] element-BVH walks,     */
-                             /* [9] walks                                    */
+                             /* [9] walks, [10] learned-field samples,       */
+                             /* [11] learned samples limited to the         */
+                             /* macrocell's widened majorant                 */
   float    *traceT;          /* optional, per pixel: distance (voxel space) */
                              /* of the first sample's first interaction, -1 */
                              /* if the ray left the volume                  */
@@ -178,6 +198,16 @@ typedef struct {
                              /* first sample's first shadow ray, -1 if none */
   uint32_t *heatCounts;      /* set by the library: per-pixel work of the   */
                              /* heat map (render.heatMapEnabled)            */
+  int32_t   tfFilter;        /* EXA_TF_FILTER_NEAREST / _LINEAR; set by    */
+                             /* exa_sampler_set_lps from the filter the max */
+                             /* opacities were computed for                 */
+  int32_t   trackStepCap;    /* > 0: tracking steps per macrocell after     */
+                             /* which a walk ends with EXA_DEVERR_TRACK_CAP; */
+                             /* 0: the built-in cap (2^22)                  */
+  int32_t   ddaCellCap;      /* > 0: macrocells a walk may visit before it  */
+                             /* ends with EXA_DEVERR_DDA_CAP; 0: the grid's */
+                             /* dims.x + dims.y + dims.z + 3                */
+  int32_t   pad0;
 } exa_lp_ext;
 
 /* LaunchParams.h:56-119, field order and types kept; the sampler union
@@ -275,6 +305,11 @@ const char *exa_last_error(void);
 int exa_sync(exa_context *ctx);
 /* Reads and clears the context's device error bits (EXA_DEVERR_*). */
 int exa_get_device_errors(exa_context *ctx, uint32_t *bits);
+/* Test hook without a reference counterpart: EXA_DEBUG_* flags for the
+ * context's next sampler builds (0 clears them).  A simulated failure
+ * follows the real failure's path (the build returns EXA_ERR_CUDA) without
+ * leaving any device work unfinished. */
+int exa_debug_set_flags(exa_context *ctx, uint32_t flags);
 /* Library version string. */
 const char *exa_version(void);
 /* sizeof of the ABI structs, for FFI bindings to check their layouts:
@@ -423,6 +458,18 @@ int exa_sampler_build(exa_context *ctx);
 int exa_sampler_compute_max_opacities(exa_context *ctx,
                                       const exa_vec4f *colorMap,
                                       int32_t numColors, exa_range1f xfRange);
+/* The transfer-function lookup of the context's renders
+ * (EXA_TF_FILTER_NEAREST, the default, or EXA_TF_FILTER_LINEAR); replaces
+ * the reference's compile-time choice EXASTITCH_CUDA_TEXTURE_TF
+ * (CMakeLists.txt:179-187).  Takes effect at the next
+ * exa_sampler_compute_max_opacities: under LINEAR the max opacities of a
+ * value range take every entry the filter can blend for it, floor(l*N-0.5)
+ * to floor(u*N-0.5)+1 (the reference maps a range to int(l*(N-1)) ..
+ * int(u*(N-1))+1 for both lookups, which under its texture filter can miss
+ * an entry the filter reads), so that they stay a bound on the filtered
+ * opacity.  exa_sampler_set_lps writes the filter to lp.ext.tfFilter; a
+ * render whose lp.ext.tfFilter differs is rejected. */
+int exa_set_transfer_function_filter(exa_context *ctx, int32_t filter);
 /* ExaStitchSampler::setLPs (sampler/ExaStitchSampler.cpp:356-365) plus the
  * majorant-grid and max-opacity LP variables OWLRenderer::initGPU and
  * setColorMap set (OWLRenderer.cpp:435-436, 652-657). */

@@ -1044,6 +1044,23 @@ static inline int elem_visible(const oc_field *f, int e, int cull)
   return !(cull && f->elemMaxOps && f->elemMaxOps[e] == 0.f);
 }
 
+/* an element is a candidate only where its bounding box (the box of its
+ * vertices, StitchGeomBounds_Impl in programs/ExaStitchSampler.cu:73-92)
+ * holds the point, inclusively: OptiX calls the intersection program only
+ * for primitives whose box the query ray meets, and the element tests'
+ * tolerances (UElems.h) accept points just outside an element */
+static inline int elem_box_contains(const oc_field *f, int e, v3 p)
+{
+  const int32_t *I = &f->indices[(uint64_t)e * 8];
+  v3 lo = mk3(INFINITY, INFINITY, INFINITY), hi = mk3(-INFINITY, -INFINITY, -INFINITY);
+  for (int i = 0; i < 8 && I[i] >= 0; ++i) {
+    const v4 v = f->vertices[I[i]];
+    lo = mk3(fmin_t(lo.x, v.x), fmin_t(lo.y, v.y), fmin_t(lo.z, v.z));
+    hi = mk3(fmax_t(hi.x, v.x), fmax_t(hi.y, v.y), fmax_t(hi.z, v.z));
+  }
+  return p.x >= lo.x && p.y >= lo.y && p.z >= lo.z && p.x <= hi.x && p.y <= hi.y && p.z <= hi.z;
+}
+
 static inline int64_t lookup_cell(const oc_field *f, v3 p)
 {
   if (!(p.x >= f->gb.lower.x && p.y >= f->gb.lower.y && p.z >= f->gb.lower.z &&
@@ -1081,7 +1098,7 @@ exa_sample oc_sample(const oc_field *f, v3 pos, int cull)
     } else if (bestG < 0) {
       const int e = -it - 1;
       if (bestE >= 0 && e >= bestE) continue;
-      if (!elem_visible(f, e, cull)) continue;
+      if (!elem_visible(f, e, cull) || !elem_box_contains(f, e, pos)) continue;
       float v;
       if (oc_intersect_elem(&v, pos, &f->indices[(uint64_t)e * 8], f->vertices)) {
         bestE = e; ev = v;
@@ -1115,7 +1132,7 @@ int oc_sample_all(const oc_field *f, v3 pos, int cull, int maxOut, int *kinds,
     }
   }
   for (uint64_t e = 0; e < f->numElems && n < maxOut; ++e) {
-    if (!elem_visible(f, (int)e, cull)) continue;
+    if (!elem_visible(f, (int)e, cull) || !elem_box_contains(f, (int)e, pos)) continue;
     float v;
     if (oc_intersect_elem(&v, pos, &f->indices[e * 8], f->vertices)) {
       kinds[n] = 1; ids[n] = (int)e; values[n] = v; n++;
@@ -1245,26 +1262,45 @@ void oc_build_majorants(const oc_field *f, v3i dims, exa_box3f wb, exa_range1f *
   }
 }
 
+/* the entries the linear transfer-function filter (EXA_TF_FILTER_LINEAR)
+ * can blend for normalised values in [l, u]: floor(l*N - 0.5) ..
+ * floor(u*N - 0.5) + 1, clipped to the table; 0 when none is inside it */
+static int tf_linear_span(float l, float u, int n, int *lo, int *hi)
+{
+  const float N = (float)n;
+  const float a = floorf(l * N - 0.5f), b = floorf(u * N - 0.5f) + 1.f;
+  if (!(b >= 0.f) || !(a <= N - 1.f)) return 0;
+  *lo = a < 0.f ? 0 : (int)a;
+  *hi = b > N - 1.f ? n - 1 : (int)b;
+  return 1;
+}
+
 /* Grid.cu:687-719 (== computeGridletMaxOpacitiesGPU,
- * sampler/ExaStitchSampler.cu:144-176) */
-static float range_max_opacity(exa_range1f vr, const v4 *cm, int n, exa_range1f xf)
+ * sampler/ExaStitchSampler.cu:144-176); under the linear filter the span
+ * of tf_linear_span */
+static float range_max_opacity(exa_range1f vr, const v4 *cm, int n, exa_range1f xf, int filter)
 {
   if (vr.upper < vr.lower) return 0.f;
   vr.lower -= xf.lower;
   vr.lower /= xf.upper - xf.lower;
   vr.upper -= xf.lower;
   vr.upper /= xf.upper - xf.lower;
-  const int lo = iclamp((int)(vr.lower * (float)(n - 1)), 0, n - 1);
-  const int hi = iclamp((int)(vr.upper * (float)(n - 1)) + 1, 0, n - 1);
+  int lo, hi;
+  if (filter == EXA_TF_FILTER_LINEAR) {
+    if (!tf_linear_span(vr.lower, vr.upper, n, &lo, &hi)) return 0.f;
+  } else {
+    lo = iclamp((int)(vr.lower * (float)(n - 1)), 0, n - 1);
+    hi = iclamp((int)(vr.upper * (float)(n - 1)) + 1, 0, n - 1);
+  }
   float m = 0.f;
   for (int i = lo; i <= hi; ++i) m = fmaxf(m, cm[i].w);
   return m;
 }
 
 void oc_compute_max_opacities(const exa_range1f *r, uint64_t n, const v4 *cm,
-                              int nc, exa_range1f xf, float *out)
+                              int nc, exa_range1f xf, int filter, float *out)
 {
-  for (uint64_t i = 0; i < n; ++i) out[i] = range_max_opacity(r[i], cm, nc, xf);
+  for (uint64_t i = 0; i < n; ++i) out[i] = range_max_opacity(r[i], cm, nc, xf, filter);
 }
 
 /* sampler/ExaStitchSampler.cu:52-142: min/max over the non-NaN corners of
@@ -1286,7 +1322,7 @@ void oc_gridlet_value_ranges(const oc_field *f, exa_range1f *out)
 
 /* sampler/ExaStitchSampler.cu:178-227 (computeUmeshMaxOpacitiesGPU<8>) */
 void oc_elem_max_opacities(const oc_field *f, const v4 *cm, int nc,
-                           exa_range1f xf, float *out)
+                           exa_range1f xf, int filter, float *out)
 {
   for (uint64_t e = 0; e < f->numElems; ++e) {
     exa_range1f r = {1e30f, -1e30f};
@@ -1297,7 +1333,7 @@ void oc_elem_max_opacities(const oc_field *f, const v4 *cm, int nc,
       r.lower = fmin_t(r.lower, w);
       r.upper = fmax_t(r.upper, w);
     }
-    out[e] = range_max_opacity(r, cm, nc, xf);
+    out[e] = range_max_opacity(r, cm, nc, xf, filter);
   }
 }
 
@@ -1318,7 +1354,35 @@ typedef struct {
   uint64_t work;              /* heat map: DDA cells of the walks, march positions */
 } rctx;
 
-/* deviceCode.cu:320-341, buffer variant */
+/* one channel of the linear filter: the blend of the two entries, limited
+ * to their range */
+static float tf_lerp(float p, float q, float a)
+{
+  const float r = (1.f - a) * p + a * q;
+  return fminf(fmaxf(r, fminf(p, q)), fmaxf(p, q));
+}
+
+/* EXA_TF_FILTER_LINEAR: deviceCode.cu:331-332 (tex2D of the texture that
+ * OWLRenderer.cpp:659-707 sets up: normalised coordinates, linear
+ * filtering, border address mode with a zero border colour; at y = .5 of a
+ * one-row texture only row 0 has weight) in binary32: xB = f*N - 0.5,
+ * i = floor(xB), a = xB - i, (1-a)*T[i] + a*T[i+1] */
+static v4 lookup_tf_linear(const v4 *T, int n, float f)
+{
+  v4 z = {0.f, 0.f, 0.f, 0.f};
+  const float xB = f * (float)n - 0.5f;
+  if (!(xB >= -1.f && xB < (float)n)) return z;
+  const float fi = floorf(xB);
+  const int i = (int)fi;
+  const float a = xB - fi;
+  const v4 p = i >= 0 ? T[i] : z;
+  const v4 q = i + 1 < n ? T[i + 1] : z;
+  v4 r = {tf_lerp(p.x, q.x, a), tf_lerp(p.y, q.y, a), tf_lerp(p.z, q.z, a), tf_lerp(p.w, q.w, a)};
+  return r;
+}
+
+/* deviceCode.cu:320-341: the buffer variant, or the texture variant under
+ * EXA_TF_FILTER_LINEAR */
 static v4 lookup_tf(const exa_launch_params *lp, float f)
 {
   const exa_range1f d = lp->transferFunc.domain;
@@ -1327,9 +1391,18 @@ static v4 lookup_tf(const exa_launch_params *lp, float f)
   f -= d.lower;
   f /= (d.upper - d.lower);
   if (lp->transferFunc.numValues == 0) return zero;
+  if (lp->ext.tfFilter == EXA_TF_FILTER_LINEAR)
+    return lookup_tf_linear(lp->transferFunc.values, lp->transferFunc.numValues, f);
   f = fmax_t(0.f, fmin_t(1.f, f));
   const int i = imin_t(lp->transferFunc.numValues - 1, (int)(f * (float)lp->transferFunc.numValues));
   return lp->transferFunc.values[i];
+}
+
+/* the transfer-function lookup of lp (filter, domain, table) at value f */
+void oc_lookup_tf(const exa_launch_params *lp, float f, exa_vec4f *out)
+{
+  const v4 r = lookup_tf(lp, f);
+  out->x = r.x; out->y = r.y; out->z = r.z; out->w = r.w;
 }
 
 /* sampler/Sampler.h:105-122 */
@@ -1503,7 +1576,7 @@ static int sample_interaction(rctx *c, ray_t ray, int shadow, v3 *posOut,
   oc_dda dda;
   dda_init(&dda, ray.org, ray.dir, ray.tmin, ray.tmax, lp->majorantGrid.dims, lp->majorantGrid.bounds);
   const v3i dims = lp->majorantGrid.dims;
-  const int cellCap = dims.x + dims.y + dims.z + 3;
+  const int cellCap = lp->ext.ddaCellCap > 0 ? lp->ext.ddaCellCap : dims.x + dims.y + dims.z + 3;
   int ncells = 0;
   int done = 0;
   while (!done) {
@@ -1519,7 +1592,11 @@ static int sample_interaction(rctx *c, ray_t ray, int shadow, v3 *posOut,
       int steps = 0;
       while (1) {
         if (majorant <= 0.f) break;
-        if (++steps > OC_TRACK_CAP) { c->err |= EXA_DEVERR_TRACK_CAP; done = 1; break; }
+        if (++steps > (lp->ext.trackStepCap > 0 ? lp->ext.trackStepCap : OC_TRACK_CAP)) {
+          c->err |= EXA_DEVERR_TRACK_CAP;
+          done = 1;
+          break;
+        }
         t -= oc_log(1.f - oc_rng_next(rng)) / (majorant * scale);
         if (t >= t1) break;
         pos = add3(ray.org, muls(ray.dir, t));
@@ -1988,6 +2065,22 @@ static double d_lookup_alpha(const exa_launch_params *lp, double v, double rgb[3
   const exa_range1f d = lp->transferFunc.domain;
   if (d.lower >= d.upper || lp->transferFunc.numValues == 0) { rgb[0] = rgb[1] = rgb[2] = 0; return 0; }
   double fv = (v - d.lower) / ((double)d.upper - d.lower);
+  if (lp->ext.tfFilter == EXA_TF_FILTER_LINEAR) {
+    /* the linear filter of lookup_tf_linear in binary64 */
+    const int n = lp->transferFunc.numValues;
+    const double xB = fv * n - 0.5;
+    rgb[0] = rgb[1] = rgb[2] = 0;
+    if (!(xB >= -1.0 && xB < n)) return 0;
+    const double fi = floor(xB), a = xB - fi;
+    const int i = (int)fi;
+    const v4 z = {0.f, 0.f, 0.f, 0.f};
+    const v4 p = i >= 0 ? lp->transferFunc.values[i] : z;
+    const v4 q = i + 1 < n ? lp->transferFunc.values[i + 1] : z;
+    rgb[0] = (1 - a) * p.x + a * q.x;
+    rgb[1] = (1 - a) * p.y + a * q.y;
+    rgb[2] = (1 - a) * p.z + a * q.z;
+    return (1 - a) * p.w + a * q.w;
+  }
   if (fv < 0) fv = 0;
   if (fv > 1) fv = 1;
   int i = (int)(fv * lp->transferFunc.numValues);
@@ -2026,6 +2119,198 @@ static double d_transmittance(const oc_field *f, const exa_launch_params *lp,
   return Tr;
 }
 
+/* ---- binary64 path tracing (the expectation of pathTracingIntegrate,
+ * deviceCode.cu:991-1120, with the launch parameters' albedo, HG g and
+ * bounce limit): independent random numbers, every quantity in binary64,
+ * tracking through the majorant grid by a binary64 DDA (Amanatides and Woo
+ * 1987) -- delta tracking for free flights and ratio tracking for shadow
+ * rays, both unbiased for any majorant that bounds the extinction, as the
+ * max opacities do.  No surface meshes and no clip planes. */
+static double d_rand(uint64_t *rs)
+{
+  *rs = oc_mix64(*rs + 0x9e3779b97f4a7c15ull);
+  return ((*rs >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+/* boxTest (sampler/Sampler.h:105-122) in binary64 */
+static int d_box(d3 o, d3 dir, double tmin, double tmax, const exa_box3f *b, double *t0, double *t1)
+{
+  const double lo[3] = {b->lower.x, b->lower.y, b->lower.z}, hi[3] = {b->upper.x, b->upper.y, b->upper.z};
+  const double oo[3] = {o.x, o.y, o.z}, dd[3] = {dir.x, dir.y, dir.z};
+  double a0 = tmin, a1 = tmax;
+  for (int a = 0; a < 3; ++a) {
+    double ta = (lo[a] - oo[a]) / dd[a], tb = (hi[a] - oo[a]) / dd[a];
+    if (ta > tb) { const double tt = ta; ta = tb; tb = tt; }
+    if (ta > a0) a0 = ta;
+    if (tb < a1) a1 = tb;
+  }
+  *t0 = a0;
+  *t1 = a1;
+  return a0 < a1;
+}
+
+/* tracking along o + t dir for t in [0, tmax] through the majorant grid.
+ * shadow = 0: delta tracking, returns 1 at a collision (*tHit, rgb, alpha);
+ * shadow = 1: ratio tracking, *Tr the transmittance estimate */
+static int d_track(const oc_field *f, const exa_launch_params *lp, d3 o, d3 dir, double tmax, int shadow,
+                   uint64_t *rs, double *tHit, double rgb[3], double *Tr)
+{
+  const int cull = lp->ext.cullTransparentPrims;
+  const double scale = lp->transferFunc.opacityScale;
+  const v3i D = lp->majorantGrid.dims;
+  const exa_box3f B = lp->majorantGrid.bounds;
+  *Tr = 1.0;
+  double tin, tout;
+  if (!d_box(o, dir, 0.0, tmax, &B, &tin, &tout)) return 0;
+  const double lo[3] = {B.lower.x, B.lower.y, B.lower.z};
+  const double cs[3] = {((double)B.upper.x - B.lower.x) / D.x, ((double)B.upper.y - B.lower.y) / D.y,
+                        ((double)B.upper.z - B.lower.z) / D.z};
+  const double oo[3] = {o.x, o.y, o.z}, dd[3] = {dir.x, dir.y, dir.z};
+  const int n[3] = {D.x, D.y, D.z};
+  int cell[3], step[3];
+  double tnext[3], tdelta[3];
+  const double tm = 0.5 * (tin + tout);  /* locate the first cell mid-way into it */
+  for (int a = 0; a < 3; ++a) {
+    const double pe = oo[a] + dd[a] * tin;
+    int c = (int)floor((pe - lo[a]) / cs[a]);
+    if (dd[a] == 0.0) c = (int)floor((oo[a] + dd[a] * tm - lo[a]) / cs[a]);
+    cell[a] = c < 0 ? 0 : (c >= n[a] ? n[a] - 1 : c);
+    step[a] = dd[a] > 0 ? 1 : -1;
+    if (dd[a] == 0.0) { tnext[a] = INFINITY; tdelta[a] = INFINITY; continue; }
+    const double bound = lo[a] + (cell[a] + (dd[a] > 0 ? 1 : 0)) * cs[a];
+    tnext[a] = (bound - oo[a]) / dd[a];
+    tdelta[a] = cs[a] / fabs(dd[a]);
+  }
+  double t = tin;
+  for (int guard = 0; guard < n[0] + n[1] + n[2] + 8; ++guard) {
+    double t1 = tnext[0] < tnext[1] ? tnext[0] : tnext[1];
+    if (tnext[2] < t1) t1 = tnext[2];
+    if (tout < t1) t1 = tout;
+    const double maj = lp->maxOpacities[((int64_t)cell[2] * n[1] + cell[1]) * n[0] + cell[0]] * scale;
+    if (maj > 0) {
+      double tt = t;
+      for (int k = 0; k < OC_TRACK_CAP; ++k) {
+        tt -= log(d_rand(rs)) / maj;
+        if (tt >= t1) break;
+        int hit;
+        double c3[3];
+        const double v = d_sample_value(f, dk(o.x + dir.x * tt, o.y + dir.y * tt, o.z + dir.z * tt), cull, &hit);
+        if (!hit) continue;
+        const double a = d_lookup_alpha(lp, v, c3) * scale;
+        if (!shadow) {
+          if (a >= d_rand(rs) * maj) {
+            *tHit = tt;
+            rgb[0] = c3[0]; rgb[1] = c3[1]; rgb[2] = c3[2];
+            return 1;
+          }
+        } else {
+          *Tr *= 1.0 - a / maj;
+        }
+      }
+    }
+    if (t1 >= tout) return 0;
+    t = t1;
+    int ax = 0;
+    if (tnext[1] < tnext[ax]) ax = 1;
+    if (tnext[2] < tnext[ax]) ax = 2;
+    cell[ax] += step[ax];
+    if (cell[ax] < 0 || cell[ax] >= n[ax]) return 0;
+    tnext[ax] += tdelta[ax];
+  }
+  return 0;
+}
+
+/* the light sample of sampleLight (deviceCode.cu:856-926) in expectation
+ * over the uniformly chosen light: mean of intensity x transmittance (x
+ * 1/d^2 for point lights, d in light space) */
+static double d_light(const oc_field *f, const exa_launch_params *lp, d3 pos, int numLights, uint64_t *rs)
+{
+  double L = 0.0;
+  for (int li = 0; li < EXA_LIGHTS_MAX; ++li) {
+    if (!lp->lights[li].on) continue;
+    d3 ldir;
+    double tmax = 1e30, fall = 1.0;
+    if (lp->ext.lightType[li] == EXA_LIGHT_DIRECTIONAL) {
+      ldir = dk(lp->lights[li].pos.x, lp->lights[li].pos.y, lp->lights[li].pos.z);
+    } else {
+      ldir = dk(lp->lights[li].pos.x - pos.x, lp->lights[li].pos.y - pos.y, lp->lights[li].pos.z - pos.z);
+      const exa_affine3f *T = &lp->lightSpaceTransform;
+      const d3 lv = dk(T->l.vx.x * ldir.x + T->l.vy.x * ldir.y + T->l.vz.x * ldir.z,
+                       T->l.vx.y * ldir.x + T->l.vy.y * ldir.y + T->l.vz.y * ldir.z,
+                       T->l.vx.z * ldir.x + T->l.vy.z * ldir.y + T->l.vz.z * ldir.z);
+      fall = 1.0 / (lv.x * lv.x + lv.y * lv.y + lv.z * lv.z);
+      tmax = sqrt(ldir.x * ldir.x + ldir.y * ldir.y + ldir.z * ldir.z);
+    }
+    const double nl = sqrt(ldir.x * ldir.x + ldir.y * ldir.y + ldir.z * ldir.z);
+    ldir = dk(ldir.x / nl, ldir.y / nl, ldir.z / nl);
+    double t0, t1, Tr = 1.0, th, c3[3];
+    if (d_box(pos, ldir, 0.0, tmax, &lp->worldSpaceBounds, &t0, &t1)) d_track(f, lp, pos, ldir, t1, 1, rs, &th, c3, &Tr);
+    L += Tr * fall * lp->lights[li].intensity;
+  }
+  return L / numLights;
+}
+
+/* henyeyGreensteinSample (deviceCode.cu:965-985) in binary64 */
+static d3 d_hg(d3 wo, double g, uint64_t *rs)
+{
+  const double u1 = d_rand(rs), u2 = d_rand(rs);
+  double cost;
+  if (fabs(g) >= 1.19209290e-07) {
+    const double a = (1 - g * g) / (1 - g + 2 * g * u1);
+    cost = (1 + g * g - a * a) / (2 * g);
+  } else {
+    cost = 1 - 2 * u1;
+  }
+  const double sint = sqrt(fmax(0.0, 1 - cost * cost));
+  const double phi = 2 * 3.14159265358979323846 * u2;
+  d3 v = fabs(wo.x) > fabs(wo.y) ? dk(-wo.z, 0, wo.x) : dk(0, wo.z, -wo.y);
+  const double vn = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  v = dk(v.x / vn, v.y / vn, v.z / vn);
+  const d3 u = dk(v.y * wo.z - v.z * wo.y, v.z * wo.x - v.x * wo.z, v.x * wo.y - v.y * wo.x);
+  const double a = sint * cos(phi), b = sint * sin(phi);
+  return dk(u.x * a + v.x * b - wo.x * cost, u.y * a + v.y * b - wo.y * cost, u.z * a + v.z * b - wo.z * cost);
+}
+
+static void d_path_trace(const oc_field *f, const exa_launch_params *lp, d3 o, d3 dir, int numLights,
+                         const double bg[3], uint64_t *rs, double out[3])
+{
+  double thr[3] = {1, 1, 1}, Ld[3] = {0, 0, 0};
+  unsigned bounce = 0;
+  const unsigned maxB = (unsigned)lp->ext.maxBounces;
+  double t0, t1;
+  if (d_box(o, dir, 0.0, 1e30, &lp->worldSpaceBounds, &t0, &t1)) {
+    o = dk(o.x + dir.x * t0, o.y + dir.y * t0, o.z + dir.z * t0);
+    t1 -= t0;
+    while (1) {
+      double th, rgb[3], Tr;
+      if (!d_track(f, lp, o, dir, t1, 0, rs, &th, rgb, &Tr)) break;
+      if (bounce++ >= maxB) { thr[0] = thr[1] = thr[2] = 0; break; }
+      const d3 pos = dk(o.x + dir.x * th, o.y + dir.y * th, o.z + dir.z * th);
+      for (int k = 0; k < 3; ++k) thr[k] *= lp->ext.albedo < 0.f ? rgb[k] : (double)lp->ext.albedo;
+      double P = thr[0] > thr[1] ? thr[0] : thr[1];
+      if (thr[2] > P) P = thr[2];
+      if (P < 0.2) {
+        if (d_rand(rs) > P) { thr[0] = thr[1] = thr[2] = 0; break; }
+        for (int k = 0; k < 3; ++k) thr[k] /= P;
+      }
+      if (numLights > 0) {
+        const double L = d_light(f, lp, pos, numLights, rs);
+        for (int k = 0; k < 3; ++k) Ld[k] += thr[k] * L;
+      }
+      dir = d_hg(dk(-dir.x, -dir.y, -dir.z), lp->ext.hgG, rs);
+      o = pos;
+      /* the next segment keeps the previous segment's end as its limit
+       * (boxTest with ray.tmax = t1, deviceCode.cu:1029, 1107) */
+      double n0, n1;
+      d_box(o, dir, 0.0, t1, &lp->worldSpaceBounds, &n0, &n1);
+      t1 = n1;
+    }
+  }
+  if (numLights == 0) Ld[0] = Ld[1] = Ld[2] = 1;
+  if (!bounce) { out[0] = bg[0]; out[1] = bg[1]; out[2] = bg[2]; return; }
+  for (int k = 0; k < 3; ++k) out[k] = Ld[k] * thr[k];
+}
+
 void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
                    int height, int64_t pb, int64_t pe, double *out, int nthreads)
 {
@@ -2058,6 +2343,12 @@ void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
       const double dl = sqrt(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
       dir = dk(dir.x / dl, dir.y / dl, dir.z / dl);
       const d3 o = dk(lp->camera.org.x, lp->camera.org.y, lp->camera.org.z);
+      if (lp->integrator == EXA_PATH_TRACING_INTEGRATOR) {
+        double c3[3];
+        d_path_trace(f, lp, o, dir, numLights, bg, &rs, c3);
+        acc[0] += c3[0]; acc[1] += c3[1]; acc[2] += c3[2];
+        continue;
+      }
       /* box test against world bounds (identity voxel transform assumed
        * by the caller for this reference) */
       double t0 = 0, t1 = 1e10;

@@ -92,22 +92,27 @@ void oc_build_majorants(const oc_field *f, exa_vec3i dims, exa_box3f bounds,
                         exa_range1f *valueRanges);
 void oc_compute_max_opacities(const exa_range1f *ranges, uint64_t n,
                               const exa_vec4f *colorMap, int numColors,
-                              exa_range1f xfRange, float *out);
+                              exa_range1f xfRange, int filter, float *out);
 void oc_gridlet_value_ranges(const oc_field *f, exa_range1f *out);
 void oc_elem_max_opacities(const oc_field *f, const exa_vec4f *colorMap,
-                           int numColors, exa_range1f xfRange, float *out);
+                           int numColors, exa_range1f xfRange, int filter, float *out);
 
 /* ---- rendering (deviceCode.cu) ----
  * lp holds HOST pointers: transferFunc.values, maxOpacities, accumBuffer,
  * fbPointer.  Renders pixels [pixelBegin, pixelEnd) of a width x height
  * frame.  Returns the OR of EXA_DEVERR_* bits raised. */
+void oc_lookup_tf(const exa_launch_params *lp, float f, exa_vec4f *out);
 uint32_t oc_render(const oc_field *f, const exa_launch_params *lp,
                    int width, int height, int64_t pixelBegin, int64_t pixelEnd,
                    int nthreads);
-/* Same frame computed in binary64 arithmetic with ratio-tracking
- * transmittance for the direct-lighting integrator: the converged
- * reference image for RMSE checks.  Writes linear RGB (3 doubles/pixel,
- * averaged over spp) into outRGB for pixels [pixelBegin, pixelEnd). */
+/* Same frame computed in binary64 arithmetic with independent random
+ * numbers: the converged reference image for RMSE checks.  The
+ * direct-lighting integrator tracks under the global majorant (delta
+ * tracking to the first collision, ratio-tracking shadow rays); the path
+ * tracer (integrator 0: albedo, HG g and bounce limit of lp.ext; no
+ * meshes or clip planes) tracks through the majorant grid with a binary64
+ * DDA.  Writes linear RGB (3 doubles/pixel, averaged over spp) into
+ * outRGB for pixels [pixelBegin, pixelEnd). */
 void oc_render_f64(const oc_field *f, const exa_launch_params *lp, int width,
                    int height, int64_t pixelBegin, int64_t pixelEnd,
                    double *outRGB, int nthreads);

@@ -107,9 +107,10 @@ def lib():
         L.oc_sample_all.restype = C.c_int
         L.oc_sample_all.argtypes = [vp, Vec3f, C.c_int, C.c_int, vp, vp, vp]
         L.oc_build_majorants.argtypes = [vp, Vec3i, Box3f, vp]
-        L.oc_compute_max_opacities.argtypes = [vp, C.c_uint64, vp, C.c_int, Range1f, vp]
+        L.oc_compute_max_opacities.argtypes = [vp, C.c_uint64, vp, C.c_int, Range1f, C.c_int, vp]
         L.oc_gridlet_value_ranges.argtypes = [vp, vp]
-        L.oc_elem_max_opacities.argtypes = [vp, vp, C.c_int, Range1f, vp]
+        L.oc_elem_max_opacities.argtypes = [vp, vp, C.c_int, Range1f, C.c_int, vp]
+        L.oc_lookup_tf.argtypes = [vp, C.c_float, vp]
         L.oc_render.restype = C.c_uint32
         L.oc_render.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int]
         L.oc_render_f64.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int64, C.c_int64, vp, C.c_int]
@@ -254,10 +255,10 @@ class Field:
         lib().oc_gridlet_value_ranges(self.h, _ptr(out))
         return out
 
-    def elem_max_opacities(self, cmap, xf_range):
+    def elem_max_opacities(self, cmap, xf_range, tf_filter=0):
         cmap = np.ascontiguousarray(cmap, dtype=np.float32).reshape(-1, 4)
         out = np.zeros(len(self.indices), np.float32)
-        lib().oc_elem_max_opacities(self.h, _ptr(cmap), len(cmap), Range1f(*xf_range), _ptr(out))
+        lib().oc_elem_max_opacities(self.h, _ptr(cmap), len(cmap), Range1f(*xf_range), int(tf_filter), _ptr(out))
         return out
 
     def render(self, lp_bytes, width, height, pixel_begin=0, pixel_end=None, nthreads=0):
@@ -273,11 +274,25 @@ class Field:
         return out
 
 
-def max_opacities(ranges, cmap, xf_range):
+def max_opacities(ranges, cmap, xf_range, tf_filter=0):
+    """tf_filter: 0 nearest (the reference's buffer lookup), 1 linear (its
+    texture lookup)"""
     ranges = np.ascontiguousarray(ranges, dtype=np.float32).reshape(-1, 2)
     cmap = np.ascontiguousarray(cmap, dtype=np.float32).reshape(-1, 4)
     out = np.zeros(len(ranges), np.float32)
-    lib().oc_compute_max_opacities(_ptr(ranges), len(ranges), _ptr(cmap), len(cmap), Range1f(*xf_range), _ptr(out))
+    lib().oc_compute_max_opacities(_ptr(ranges), len(ranges), _ptr(cmap), len(cmap), Range1f(*xf_range),
+                                   int(tf_filter), _ptr(out))
+    return out
+
+
+def lookup_tf(lp_bytes, values):
+    """RGBA of the transfer-function lookup of a launch-parameter block (its
+    filter, domain and table; the table pointer is the caller's) at each of
+    the float32 values"""
+    values = np.ascontiguousarray(values, np.float32).ravel()
+    out = np.zeros((len(values), 4), np.float32)
+    for i, v in enumerate(values):
+        lib().oc_lookup_tf(lp_bytes, float(v), out[i].ctypes.data)
     return out
 
 

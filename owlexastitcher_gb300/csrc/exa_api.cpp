@@ -447,7 +447,7 @@ bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
   buildStats.majorantBlocks =
       launchGridletMajorants(gridletBuffer.ptr, gridletScalarBuffer.ptr, model->gridlets.size(),
                              model->gridletScalars.size(), g.dims, g.worldBounds, g.valueRanges.ptr,
-                             gridletValueRanges.ptr, buildErrors.ptr, s);
+                             gridletValueRanges.ptr, buildErrors.ptr, debugFlags, s);
   timer.mark(2);
   g.deviceTraversable.dims = g.dims;
   g.deviceTraversable.bounds = g.worldBounds;
@@ -470,10 +470,11 @@ void ExaStitchSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors,
   if (numColors <= 0) throw Error(EXA_ERR_INVALID, "empty color map");
   colorMap.upload(reinterpret_cast<const float4 *>(cmap), (size_t)numColors, s);
   Grid &g = *model->grid;
-  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, g.maxOpacities.ptr, s);
-  launchMaxOpacity(gridletValueRanges.ptr, gridletValueRanges.count, colorMap.ptr, numColors, xf,
+  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, tfFilter, g.maxOpacities.ptr, s);
+  launchMaxOpacity(gridletValueRanges.ptr, gridletValueRanges.count, colorMap.ptr, numColors, xf, tfFilter,
                    gridletMaxOpacities.ptr, s);
-  launchMaxOpacity(elemValueRanges.ptr, elemValueRanges.count, colorMap.ptr, numColors, xf, umeshMaxOpacities.ptr, s);
+  launchMaxOpacity(elemValueRanges.ptr, elemValueRanges.count, colorMap.ptr, numColors, xf, tfFilter, umeshMaxOpacities.ptr,
+                   s);
   if (accel.numElems > 0)
     launchRefitBVH(vertexBuffer.ptr, indexBuffer.ptr, (size_t)accel.numElems, bvhNodes.ptr, bvhParents.ptr,
                    bvhLeafElem.ptr, umeshMaxOpacities.ptr, false, s);
@@ -647,7 +648,7 @@ void AMRCellSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors, e
   if (numColors <= 0) throw Error(EXA_ERR_INVALID, "empty color map");
   colorMap.upload(reinterpret_cast<const float4 *>(cmap), (size_t)numColors, s);
   Grid &g = *model->grid;
-  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, g.maxOpacities.ptr, s);
+  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, tfFilter, g.maxOpacities.ptr, s);
   cudaCheck(cudaStreamSynchronize(s), "computeMaxOpacities");
   hasTF = true;
 }
@@ -672,6 +673,8 @@ struct exa_context {
   std::shared_ptr<Sampler> sampler;
   exa_range1f xfRange{0.f, 1.f};
   int numColors = 0;
+  int tfFilter = EXA_TF_FILTER_NEAREST;  // for the next computeMaxOpacities
+  uint32_t debugFlags = 0;               // EXA_DEBUG_*, for the next sampler build
   DBuf<uint32_t> errors;
   DBuf<unsigned> jobCounter; // work counter of the persistent render kernel
   DBuf<float4> sampleColors; // one colour per camera sample of the frame
@@ -758,6 +761,16 @@ void need(bool c, int code, const char *msg)
 
 void setDevice(exa_context *ctx) { cudaCheck(cudaSetDevice(ctx->device), "cudaSetDevice"); }
 
+// the launch parameters' filter and loop caps: the filter must be the one
+// the max opacities were computed for (else they may not bound the
+// filtered opacity); the caps are non-negative
+void needLpCaps(const exa_launch_params &lp, int samplerFilter)
+{
+  need(lp.ext.tfFilter == samplerFilter, EXA_ERR_INVALID,
+       "lp.ext.tfFilter differs from the filter of the max opacities (call exa_sampler_set_lps)");
+  need(lp.ext.trackStepCap >= 0 && lp.ext.ddaCellCap >= 0, EXA_ERR_INVALID, "negative loop cap");
+}
+
 // the context's model / sampler where a call needs the ExaStitch kind
 ExaStitchModel &esModel(exa_context *ctx)
 {
@@ -807,6 +820,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    needLpCaps(*lp, ctx->sampler->tfFilter);
     // the AMR-cell and ExaBrick samplers render shade mode default
     // (renderFrame_AMRCellSampler / _ExaBrickSampler, deviceCode.cu:1360-1387)
     need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||
@@ -1433,6 +1447,7 @@ int exa_sampler_build(exa_context *ctx)
     else
       s = std::make_shared<ExaStitchSampler>();
     const auto t0 = std::chrono::steady_clock::now();
+    s->debugFlags = ctx->debugFlags;
     if (!s->build(ctx->model, ctx->stream)) throw Error(EXA_ERR_STATE, s->className() + "::build failed");
     ctx->sampler = s;
     ctx->lastBuild = {};
@@ -1457,11 +1472,32 @@ int exa_sampler_compute_max_opacities(exa_context *ctx, const exa_vec4f *colorMa
     need(ctx && ctx->sampler, EXA_ERR_STATE, "sampler not built");
     need(colorMap && numColors > 0, EXA_ERR_INVALID, "empty color map");
     setDevice(ctx);
+    ctx->sampler->tfFilter = ctx->tfFilter;
     ctx->sampler->computeMaxOpacities(colorMap, numColors, xfRange, ctx->stream);
     ctx->xfRange = xfRange;
     ctx->numColors = numColors;
     if (ctx->surrogate && ctx->surrogate->evaluated)
-      ctx->surrogate->computeMajorants(ctx->sampler->colorMap.ptr, numColors, xfRange, ctx->stream);
+      ctx->surrogate->computeMajorants(ctx->sampler->colorMap.ptr, numColors, xfRange, ctx->sampler->tfFilter,
+                                       ctx->stream);
+  });
+}
+
+int exa_debug_set_flags(exa_context *ctx, uint32_t flags)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_STATE, "null context");
+    need((flags & ~(uint32_t)EXA_DEBUG_COPY_WAIT_TIMEOUT) == 0, EXA_ERR_INVALID, "unknown debug flag");
+    ctx->debugFlags = flags;
+  });
+}
+
+int exa_set_transfer_function_filter(exa_context *ctx, int32_t filter)
+{
+  return guarded([&] {
+    need(ctx != nullptr, EXA_ERR_STATE, "null context");
+    need(filter == EXA_TF_FILTER_NEAREST || filter == EXA_TF_FILTER_LINEAR, EXA_ERR_INVALID,
+         "unknown transfer-function filter");
+    ctx->tfFilter = filter;
   });
 }
 
@@ -1490,6 +1526,7 @@ int exa_sampler_set_lps(exa_context *ctx, exa_launch_params *lp)
       lp->transferFunc.numValues = ctx->numColors;
       lp->transferFunc.domain = ctx->xfRange;
     }
+    lp->ext.tfFilter = ctx->sampler->tfFilter;
     lp->ext.deviceErrors = ctx->errors.ptr;
   });
 }
@@ -1670,7 +1707,7 @@ int exa_surrogate_evaluate(exa_context *ctx, float tolerance, uint64_t pointsTar
     Surrogate &S = *ctx->surrogate;
     const Grid &g = *ctx->model->grid;
     S.evaluate(esSampler(ctx), g, (double)tolerance, (size_t)std::max<uint64_t>(pointsTarget, 1), ctx->stream);
-    S.computeMajorants(ctx->sampler->colorMap.ptr, ctx->numColors, ctx->xfRange, ctx->stream);
+    S.computeMajorants(ctx->sampler->colorMap.ptr, ctx->numColors, ctx->xfRange, ctx->sampler->tfFilter, ctx->stream);
     cudaCheck(cudaStreamSynchronize(ctx->stream), "surrogate majorants");
     ctx->surrogateTol = tolerance;
   });
@@ -1862,11 +1899,12 @@ void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
                       er.ptr, ctx->stream);
   cudaCheck(cudaMemsetAsync(S.buildErrors.ptr, 0, sizeof(uint32_t), ctx->stream), "memset build errors");
   launchGridletMajorants(S.gridletBuffer.ptr, S.gridletScalarBuffer.ptr, m.gridlets.size(), m.gridletScalars.size(),
-                         B.dims, m.cellBounds, B.ranges.ptr, gr.ptr, S.buildErrors.ptr, ctx->stream);
+                         B.dims, m.cellBounds, B.ranges.ptr, gr.ptr, S.buildErrors.ptr, 0u, ctx->stream);
   B.maxOps.resize(B.tfColors.size());
   for (size_t t = 0; t < B.tfColors.size(); ++t) {
     B.maxOps[t].alloc(n);
-    launchMaxOpacity(B.ranges.ptr, n, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], B.maxOps[t].ptr, ctx->stream);
+    launchMaxOpacity(B.ranges.ptr, n, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], ctx->sampler->tfFilter,
+                     B.maxOps[t].ptr, ctx->stream);
   }
   cudaCheck(cudaStreamSynchronize(ctx->stream), "batch majorants");
   checkBuildErrors(S.buildErrors.ptr);
@@ -1889,9 +1927,9 @@ void rebuildBatchCulling(exa_context *ctx, BatchState &B)
   for (size_t t = 0; t < nt; ++t) {
     B.gOps[t].alloc(std::max<size_t>(ng, 1));
     B.eOps[t].alloc(std::max<size_t>(S.elemValueRanges.count, 1));
-    launchMaxOpacity(S.gridletValueRanges.ptr, ng, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], B.gOps[t].ptr,
+    launchMaxOpacity(S.gridletValueRanges.ptr, ng, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], S.tfFilter, B.gOps[t].ptr,
                      ctx->stream);
-    launchMaxOpacity(S.elemValueRanges.ptr, S.elemValueRanges.count, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t],
+    launchMaxOpacity(S.elemValueRanges.ptr, S.elemValueRanges.count, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], S.tfFilter,
                      B.eOps[t].ptr, ctx->stream);
     if (ne > 0) {
       B.nodes[t].alloc(S.bvhNodes.count);
@@ -1924,6 +1962,7 @@ void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch
   need(tpl->sampler.ess.sampleBVH == (uint64_t)(uintptr_t)ctx->sampler->deviceAccel.ptr, EXA_ERR_INVALID,
        "lpTemplate.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
   need(tpl->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+  needLpCaps(*tpl, ctx->sampler->tfFilter);
   need(B.tileW == 8 || B.tileW == 16 || B.tileW == 32, EXA_ERR_INVALID, "bad tile width");
   setDevice(ctx);
   const int th = 128 / B.tileW;
@@ -2158,6 +2197,7 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
     need(lp->maxOpacities != nullptr && lp->transferFunc.values != nullptr, EXA_ERR_STATE,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
+    needLpCaps(*lp, ctx->sampler->tfFilter);
     // as in exa_render: the AMR-cell and ExaBrick samplers have no gridlet
     // cells to colour
     need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
                                                                    const float *__restrict__ scalars, size_t nScalars,
                                                                    bool stage, exa_vec3i dims, exa_box3f wb,
                                                                    exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                                                   uint32_t *errors)
+                                                                   uint32_t *errors, uint32_t debugFlags)
 {
   __shared__ MajSmem sm;
   const int tid = threadIdx.x;
@@ -261,14 +261,22 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
     const float *S = scalars + (uint32_t)g.begin;
     if (P.staged) {
       bool ok = true;
+      const uint32_t ph = (parity >> buf) & 1u;
       if (P.bulk) {
-        ok = mbar_wait(&sm.bar[buf], (parity >> buf) & 1u);
+        ok = mbar_wait(&sm.bar[buf], ph);
+        // the simulated time-out of the error-path test: block 0 treats its
+        // first wait as failed after it completed, so no copy is in flight
+        if ((debugFlags & EXA_DEBUG_COPY_WAIT_TIMEOUT) && blockIdx.x == 0 && it == 0) ok = false;
         parity ^= 1u << buf;
       }
       if (__syncthreads_or(!ok)) {
-        // give up: flag it, let the other buffer's copy land, return
+        // give up: flag it and wait (bounded again) for this buffer's copy
+        // and the other buffer's before the block's shared memory is
+        // released.  A copy that never completes is still in flight when
+        // the block exits; the host reports the build as failed.
         if (tid == 0) {
           if (errors) atomicOr(errors, EXA_DEVERR_COPY_WAIT);
+          if (P.bulk) (void)mbar_wait(&sm.bar[buf], ph);
           if (gn < ng && sm.plan[buf ^ 1].P.bulk)
             (void)mbar_wait(&sm.bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
         }
@@ -410,7 +418,7 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
 
 unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
                                 exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                uint32_t *errors, cudaStream_t s)
+                                uint32_t *errors, uint32_t debugFlags, cudaStream_t s)
 {
   if (!ng) return 0;
   int dev = 0, sms = 0;
@@ -424,7 +432,7 @@ unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size
   const size_t blocks = std::min<size_t>(ng, (size_t)std::max(sms, 1) * (size_t)std::max(perSM, 1));
   const bool stage = (reinterpret_cast<uintptr_t>(scalars) & 15u) == 0;
   k_gridlet_majorants<<<(unsigned)blocks, kMajThreads, 0, s>>>(g, ng, scalars, nScalars, stage, dims, wb, mcRanges,
-                                                               gridletRanges, errors);
+                                                               gridletRanges, errors, debugFlags);
   cudaCheck(cudaGetLastError(), "k_gridlet_majorants");
   return (unsigned)blocks;
 }
@@ -599,33 +607,34 @@ void launchAmrLevelCells(const exa_amr_cell *cells, size_t n, int level, const i
 
 // Grid.cu:687-719; the color map is staged in shared memory
 __global__ void k_max_opacity(const exa_range1f *__restrict__ ranges, size_t n, const float4 *__restrict__ cmap,
-                              int ncolors, exa_range1f xf, float *out)
+                              int ncolors, exa_range1f xf, int filter, float *out)
 {
   extern __shared__ float4 sCmap[];
   for (int i = threadIdx.x; i < ncolors; i += blockDim.x) sCmap[i] = cmap[i];
   __syncthreads();
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  out[i] = range_max_opacity(ranges[i], sCmap, ncolors, xf);
+  out[i] = range_max_opacity(ranges[i], sCmap, ncolors, xf, filter);
 }
 
 __global__ void k_max_opacity_global(const exa_range1f *__restrict__ ranges, size_t n,
-                                     const float4 *__restrict__ cmap, int ncolors, exa_range1f xf, float *out)
+                                     const float4 *__restrict__ cmap, int ncolors, exa_range1f xf, int filter,
+                                     float *out)
 {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  out[i] = range_max_opacity(ranges[i], cmap, ncolors, xf);
+  out[i] = range_max_opacity(ranges[i], cmap, ncolors, xf, filter);
 }
 
 void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf,
-                      float *out, cudaStream_t s)
+                      int filter, float *out, cudaStream_t s)
 {
   if (!n) return;
   const size_t smem = (size_t)ncolors * sizeof(float4);
   if (smem <= 48 * 1024)
-    k_max_opacity<<<gridFor(n, 256), 256, smem, s>>>(ranges, n, cmap, ncolors, xf, out);
+    k_max_opacity<<<gridFor(n, 256), 256, smem, s>>>(ranges, n, cmap, ncolors, xf, filter, out);
   else
-    k_max_opacity_global<<<gridFor(n, 256), 256, 0, s>>>(ranges, n, cmap, ncolors, xf, out);
+    k_max_opacity_global<<<gridFor(n, 256), 256, 0, s>>>(ranges, n, cmap, ncolors, xf, filter, out);
   cudaCheck(cudaGetLastError(), "k_max_opacity");
 }
 

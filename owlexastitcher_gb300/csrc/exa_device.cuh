@@ -318,16 +318,37 @@ EXA_HD V3i project_on_grid(V3 V, V3i dims, const exa_box3f &b)
   return r;
 }
 
-// Grid.cu:687-719 (== sampler/ExaStitchSampler.cu:144-176, 208-226)
-EXA_HD float range_max_opacity(exa_range1f vr, const float4 *cm, int n, exa_range1f xf)
+// the table entries the linear transfer-function filter
+// (EXA_TF_FILTER_LINEAR) can blend for normalised values in [l, u]:
+// floor(l*N - 0.5) .. floor(u*N - 0.5) + 1, clipped to the table (the
+// products and differences are the lookup's own operations, so a value in
+// [l, u] never reads outside the span); false when the span misses the table
+EXA_HD bool tf_linear_span(float l, float u, int n, int &lo, int &hi)
+{
+  const float N = (float)n;
+  const float a = floorf(l * N - 0.5f), b = floorf(u * N - 0.5f) + 1.f;
+  if (!(b >= 0.f) || !(a <= N - 1.f)) return false;
+  lo = a < 0.f ? 0 : (int)a;
+  hi = b > N - 1.f ? n - 1 : (int)b;
+  return true;
+}
+
+// Grid.cu:687-719 (== sampler/ExaStitchSampler.cu:144-176, 208-226); under
+// the linear filter the entry span of tf_linear_span
+EXA_HD float range_max_opacity(exa_range1f vr, const float4 *cm, int n, exa_range1f xf, int filter)
 {
   if (vr.upper < vr.lower) return 0.f;
   vr.lower -= xf.lower;
   vr.lower /= xf.upper - xf.lower;
   vr.upper -= xf.lower;
   vr.upper /= xf.upper - xf.lower;
-  const int lo = iclamp((int)(vr.lower * (float)(n - 1)), 0, n - 1);
-  const int hi = iclamp((int)(vr.upper * (float)(n - 1)) + 1, 0, n - 1);
+  int lo, hi;
+  if (filter == EXA_TF_FILTER_LINEAR) {
+    if (!tf_linear_span(vr.lower, vr.upper, n, lo, hi)) return 0.f;
+  } else {
+    lo = iclamp((int)(vr.lower * (float)(n - 1)), 0, n - 1);
+    hi = iclamp((int)(vr.upper * (float)(n - 1)) + 1, 0, n - 1);
+  }
   float m = 0.f;
   for (int i = lo; i <= hi; ++i) m = fmaxf(m, cm[i].w);
   return m;

@@ -358,7 +358,7 @@ void ExaBrickSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors, 
   if (numColors <= 0) throw Error(EXA_ERR_INVALID, "empty color map");
   colorMap.upload(reinterpret_cast<const float4 *>(cmap), (size_t)numColors, s);
   Grid &g = *model->grid;
-  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, g.maxOpacities.ptr, s);
+  launchMaxOpacity(g.valueRanges.ptr, g.valueRanges.count, colorMap.ptr, numColors, xf, tfFilter, g.maxOpacities.ptr, s);
   cudaCheck(cudaStreamSynchronize(s), "computeMaxOpacities");
   hasTF = true;
 }

@@ -150,6 +150,11 @@ struct Sampler {  // sampler/Sampler.h:28-69
   DBuf<AccelView> deviceAccel;
   bool hasTF = false;
   DBuf<float4> colorMap;
+  // EXA_TF_FILTER_* the max opacities are computed for (set before
+  // computeMaxOpacities)
+  int tfFilter = EXA_TF_FILTER_NEAREST;
+  // EXA_DEBUG_* simulations of the build's error paths (set before build)
+  uint32_t debugFlags = 0;
 };
 
 class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
@@ -243,7 +248,7 @@ void launchInitRanges(exa_range1f *r, size_t n, cudaStream_t s);
 // returns the number of blocks launched
 unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
                                 exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                uint32_t *errors, cudaStream_t s);
+                                uint32_t *errors, uint32_t debugFlags, cudaStream_t s);
 void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa_vec3i dims, exa_box3f wb,
                          exa_range1f *mcRanges, exa_range1f *elemRanges, cudaStream_t s);
 // Grid.cu:248-285: every cell's value into the macrocells its support
@@ -261,7 +266,7 @@ void launchAmrLevelCells(const exa_amr_cell *cells, size_t n, int level, const i
 // support projects onto
 void launchBrickMajorants(const exa_brick *bricks, size_t nb, const float *scalars, exa_vec3i dims, exa_box3f wb,
                           exa_range1f *mcRanges, cudaStream_t s);
-void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf,
+void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, int ncolors, exa_range1f xf, int filter,
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,
                     int32_t *parents, int32_t *leafElem, cudaStream_t s);
@@ -330,7 +335,7 @@ struct Surrogate {
   float trainSteps(int steps, cudaStream_t s);
   void gradients(const float4 *hostSamples, int n, float *gW, float *gTable, float *loss, cudaStream_t s);
   void evaluate(const ExaStitchSampler &sampler, const Grid &grid, double tol, size_t pointsTarget, cudaStream_t s);
-  void computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, cudaStream_t s);
+  void computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, int filter, cudaStream_t s);
   SurrogateView deviceView() const;
   size_t inferenceBytes() const;
 };

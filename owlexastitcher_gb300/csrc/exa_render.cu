@@ -42,7 +42,32 @@ struct RayS {
 
 enum { BOUNDARY = 0, SCATTERING = 1 };
 
-// deviceCode.cu:320-341, buffer variant
+// one channel of the linear filter: the blend of the two entries, limited
+// to their range (so the filtered opacity never exceeds the larger entry)
+EXA_D float tf_lerp(float p, float q, float a)
+{
+  const float r = (1.f - a) * p + a * q;
+  return fminf(fmaxf(r, fminf(p, q)), fmaxf(p, q));
+}
+
+// EXA_TF_FILTER_LINEAR: the texture fetch of deviceCode.cu:331-332 with
+// the texture of OWLRenderer.cpp:659-707 (normalised coordinates, linear
+// filtering, zero border) in binary32 arithmetic
+EXA_D float4 lookup_tf_linear(const float4 *__restrict__ T, int n, float f)
+{
+  const float xB = f * (float)n - 0.5f;
+  if (!(xB >= -1.f && xB < (float)n)) return make_float4(0.f, 0.f, 0.f, 0.f);  // both entries are border
+  const float fi = floorf(xB);
+  const int i = (int)fi;
+  const float a = xB - fi;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 p = i >= 0 ? __ldg(T + i) : z;
+  const float4 q = i + 1 < n ? __ldg(T + i + 1) : z;
+  return make_float4(tf_lerp(p.x, q.x, a), tf_lerp(p.y, q.y, a), tf_lerp(p.z, q.z, a), tf_lerp(p.w, q.w, a));
+}
+
+// deviceCode.cu:320-341: the buffer variant, or the texture variant under
+// EXA_TF_FILTER_LINEAR
 EXA_D float4 lookup_tf(const exa_launch_params &lp, float f)
 {
   const exa_range1f d = lp.transferFunc.domain;
@@ -50,6 +75,8 @@ EXA_D float4 lookup_tf(const exa_launch_params &lp, float f)
   f -= d.lower;
   f /= (d.upper - d.lower);
   if (lp.transferFunc.numValues == 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lp.ext.tfFilter == EXA_TF_FILTER_LINEAR)
+    return lookup_tf_linear(reinterpret_cast<const float4 *>(lp.transferFunc.values), lp.transferFunc.numValues, f);
   f = fmax_t(0.f, fmin_t(1.f, f));
   const int i = imin_t(lp.transferFunc.numValues - 1, (int)(f * (float)lp.transferFunc.numValues));
   return __ldg(reinterpret_cast<const float4 *>(lp.transferFunc.values) + i);
@@ -334,7 +361,7 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
   const exa_grid_traversable &G = lp.majorantGrid;
   const float scale = lp.transferFunc.opacityScale;
   while (w.needCell) {
-    if (++w.ncells > G.dims.x + G.dims.y + G.dims.z + 3) {
+    if (++w.ncells > (lp.ext.ddaCellCap > 0 ? lp.ext.ddaCellCap : G.dims.x + G.dims.y + G.dims.z + 3)) {
       c.err |= EXA_DEVERR_DDA_CAP;
       return WALK_END;
     }
@@ -351,7 +378,7 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
     }
     w.needCell = false;
   }
-  if (++w.steps > kTrackCap) {
+  if (++w.steps > (lp.ext.trackStepCap > 0 ? lp.ext.trackStepCap : kTrackCap)) {
     c.err |= EXA_DEVERR_TRACK_CAP;
     return WALK_END;
   }
@@ -400,10 +427,16 @@ EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const 
   if (s.cellID != -1) w.primID = s.primID;
   w.xf = classify(c.A, lp, s);
   const float sigmaT = w.xf.w;
-  if (s.primID == -2 && c.counting && sigmaT * scale > w.maj) cnt_add(c, CNT_VIOL);
+  float sigmaS = sigmaT * scale;
+  if (s.primID == -2 && sigmaS > w.maj) {
+    // a learned density above the macrocell's widened majorant is limited
+    // to it: tracking stays unbiased for the limited field
+    if (c.counting) cnt_add(c, CNT_VIOL);
+    sigmaS = w.maj;
+  }
   if (!shadow) {
     const float u = rng.next();
-    if (sigmaT * scale >= u * w.maj) {
+    if (sigmaS >= u * w.maj) {
       w.Tr = 0.f;
       w.type = SCATTERING;
       // the Teaser shade mode blends the albedo by screen position at the
@@ -413,7 +446,7 @@ EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const 
       return false;
     }
   } else {
-    w.Tr *= 1.f - __fdiv_rn(sigmaT * scale, w.maj);
+    w.Tr *= 1.f - __fdiv_rn(sigmaS, w.maj);
     if (w.Tr <= 0.f) {
       w.type = SCATTERING;
       return false;

@@ -771,10 +771,10 @@ void Surrogate::evaluate(const ExaStitchSampler &sampler, const Grid &grid, doub
   evaluated = true;
 }
 
-void Surrogate::computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, cudaStream_t s)
+void Surrogate::computeMajorants(const float4 *cmap, int ncolors, exa_range1f xf, int filter, cudaStream_t s)
 {
   if (!evaluated) return;
-  launchMaxOpacity(widenedRanges.ptr, widenedRanges.count, cmap, ncolors, xf, majorants.ptr, s);
+  launchMaxOpacity(widenedRanges.ptr, widenedRanges.count, cmap, ncolors, xf, filter, majorants.ptr, s);
 }
 
 size_t Surrogate::inferenceBytes() const

@@ -34,6 +34,14 @@ SHADE_MODE_GRIDLETS = 1
 SHADE_MODE_TEASER = 2
 LIGHT_POINT = 0
 LIGHT_DIRECTIONAL = 1
+TF_FILTER_NEAREST = 0   # the reference's buffer lookup
+TF_FILTER_LINEAR = 1    # its texture lookup (EXASTITCH_CUDA_TEXTURE_TF)
+DEVERR_DDA_CAP = 1
+DEVERR_TRACK_CAP = 2
+DEVERR_BVH_STACK = 4
+DEVERR_WATCHDOG = 16
+DEVERR_COPY_WAIT = 32
+DEBUG_COPY_WAIT_TIMEOUT = 1
 
 
 class ExaError(RuntimeError):
@@ -153,6 +161,10 @@ class LPExt(C.Structure):
         ("traceT", C.c_void_p),
         ("traceTr", C.c_void_p),
         ("heatCounts", C.c_void_p),
+        ("tfFilter", C.c_int32),
+        ("trackStepCap", C.c_int32),
+        ("ddaCellCap", C.c_int32),
+        ("pad0", C.c_int32),
     ]
 
 
@@ -293,6 +305,8 @@ def lib():
         "exa_sampler_build": ([ctx_p], C.c_int),
         "exa_sampler_compute_max_opacities": ([ctx_p, vp, i32, range1f], C.c_int),
         "exa_sampler_set_lps": ([ctx_p, C.POINTER(LaunchParams)], C.c_int),
+        "exa_set_transfer_function_filter": ([ctx_p, i32], C.c_int),
+        "exa_debug_set_flags": ([ctx_p, C.c_uint32], C.c_int),
         "exa_sampler_class_name": ([], C.c_char_p),
         "exa_get_majorants": ([ctx_p, vp, vp], C.c_int),
         "exa_get_prim_majorants": ([ctx_p, vp, vp, vp], C.c_int),
@@ -389,6 +403,11 @@ class Context:
 
     def sync(self):
         _check(lib().exa_sync(self.h))
+
+    def set_tf_filter(self, f):
+        """TF_FILTER_NEAREST or TF_FILTER_LINEAR for the next
+        computeMaxOpacities and the renders after it"""
+        _check(lib().exa_set_transfer_function_filter(self.h, int(f)))
 
     def render_stats(self):
         st = RenderStats()

@@ -61,14 +61,15 @@ class GpuScene:
 class OracleScene:
     """The same scene on the oracle, built independently from the arrays."""
 
-    def __init__(self, oracle, ds, num_mcs, lo, hi, tf, xf):
+    def __init__(self, oracle, ds, num_mcs, lo, hi, tf, xf, tf_filter=0):
         self.O = oracle
         self.f = oracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
         self.ranges = self.f.majorants(num_mcs, lo, hi)
-        self.max_ops = oracle.max_opacities(self.ranges, tf, xf)
+        self.max_ops = oracle.max_opacities(self.ranges, tf, xf, tf_filter)
         self.g_ranges = self.f.gridlet_value_ranges()
-        self.g_ops = oracle.max_opacities(self.g_ranges, tf, xf) if len(self.g_ranges) else np.zeros(0, np.float32)
-        self.e_ops = self.f.elem_max_opacities(tf, xf) if len(ds.indices) else np.zeros(0, np.float32)
+        self.g_ops = (oracle.max_opacities(self.g_ranges, tf, xf, tf_filter) if len(self.g_ranges)
+                      else np.zeros(0, np.float32))
+        self.e_ops = self.f.elem_max_opacities(tf, xf, tf_filter) if len(ds.indices) else np.zeros(0, np.float32)
         self.f.set_prim_opacities(self.g_ops if len(self.g_ops) else None, self.e_ops if len(self.e_ops) else None)
         self.tf = np.ascontiguousarray(tf, np.float32)
 
@@ -122,4 +123,28 @@ def setup_render(lp, cam, width, height, integrator, spp=1, light="directional",
         lp.ext.albedo = 0.8
         lp.ext.hgG = 0.3
         lp.ext.maxBounces = 8
+    return lp
+
+
+def oracle_only_lp(lo, hi, dims, tf, xf, width, height, integrator, spp, light="directional", baseline_ext=True):
+    """Launch parameters for an oracle-only render (no GPU): identity
+    transforms, the majorant grid over [lo, hi], the transfer function's
+    domain and size (the table and max-opacity pointers are set by
+    host_lp), culling on."""
+    from owlexastitcher_gb300 import exastitch as E
+    lp = E.LaunchParams()
+    lp.integrator = integrator
+    lp.render.dt = 1.0
+    lp.transferFunc.opacityScale = 1.0
+    lp.transferFunc.domain.lower, lp.transferFunc.domain.upper = float(xf[0]), float(xf[1])
+    lp.transferFunc.numValues = len(tf)
+    for A in (lp.voxelSpaceTransform, lp.lightSpaceTransform, lp.ext.voxelSpaceTransformInv):
+        A.l.vx.x = A.l.vy.y = A.l.vz.z = 1.0
+    lp.majorantGrid.dims = E.vec3i(*[int(d) for d in dims])
+    lp.majorantGrid.bounds = E._box(lo, hi)
+    lp.worldSpaceBounds = E._box(lo, hi)
+    lp.ext.cullTransparentPrims = 1
+    lp.ext.maxBounces = 1024
+    lp.ext.albedo = -1.0
+    setup_render(lp, orbit_camera(lo, hi, width, height), width, height, integrator, spp, light, baseline_ext)
     return lp

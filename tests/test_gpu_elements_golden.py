@@ -15,8 +15,6 @@ import os
 import numpy as np
 import pytest
 
-pytestmark = pytest.mark.gpu
-
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
@@ -38,6 +36,7 @@ def element_model(V):
     return verts, idx
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("nv", [4, 5, 6, 8], ids=["tet", "pyramid", "wedge", "hex"])
 def test_elements_golden_on_gpu(cuda, native, oracle, nv):
     from owlexastitcher_gb300 import exastitch as E
@@ -69,6 +68,7 @@ def test_elements_golden_on_gpu(cuda, native, oracle, nv):
     ctx.close()
 
 
+@pytest.mark.gpu
 def test_tets_in_unbalanced_dataset_sampled(cuda, native, oracle):
     """The unbalanced small dataset's dual mesh holds tetrahedra: points at
     their centroids (and at their vertices) sample bit-exact with the oracle
@@ -94,4 +94,40 @@ def test_tets_in_unbalanced_dataset_sampled(cuda, native, oracle):
     is_tet = (centroid["cellID"] == -1) & (centroid["primID"] >= 0)
     is_tet[is_tet] = nvs[centroid["primID"][is_tet]] == 4
     assert is_tet.mean() > 0.5
+    ctx.close()
+
+
+def test_element_box_bounds_the_tolerance(oracle):
+    """The hex test accepts points up to 1e-6 outside the element in its
+    parametric coordinates (UElems.h), so it reports a hit just above the
+    top face; the element's bounding box (its bounds program,
+    programs/ExaStitchSampler.cu:73-92) does not hold that point, so OptiX
+    never calls the test there.  The oracle's sampler keeps that rule."""
+    V = np.array([[0, 0, 0, 1], [1, 0, 0, 2], [1, 1, 0, 3], [0, 1, 0, 4], [0, 0, 1, 5], [1, 0, 1, 6], [1, 1, 1, 7],
+                  [0, 1, 1, 8]], np.float32)
+    P = np.array([[0.5, 0.5, 1 + 5e-7], [0.5, 0.5, 1.0], [0.25, 0.5, 0.75]], np.float32)
+    assert P[0, 2] > 1 and oracle.intersect_elem(P[0], V)[0]  # the tolerance accepts it
+    verts, idx = element_model(V[None])
+    f = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    s = f.sample(P)
+    assert list(s["primID"]) == [-1, 0, 0]
+    assert [k for k, _, _ in f.sample_all(P[0])] == []
+
+
+@pytest.mark.gpu
+def test_element_box_bounds_the_tolerance_gpu(cuda, native, oracle):
+    from owlexastitcher_gb300 import exastitch as E
+    V = np.array([[0, 0, 0, 1], [1, 0, 0, 2], [1, 1, 0, 3], [0, 1, 0, 4], [0, 0, 1, 5], [1, 0, 1, 6], [1, 1, 1, 7],
+                  [0, 1, 1, 8]], np.float32)
+    P = np.array([[0.5, 0.5, 1 + 5e-7], [0.5, 0.5, 1.0], [0.25, 0.5, 0.75]], np.float32)
+    verts, idx = element_model(V[None])
+    ctx = E.Context(0)
+    model = E.ExaStitchModel(ctx, verts, idx, np.zeros(0, E.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    model.setNumGridCells((2, 2, 2))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    got = sampler.sample_host(P)
+    want = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32)).sample(P)
+    assert list(got["primID"]) == [-1, 0, 0]
+    assert got.tobytes() == want.tobytes()
     ctx.close()

@@ -166,3 +166,35 @@ def test_mesh_headlight_shading(oracle, native):
     assert np.all((col >= lo_c) & (col <= hi_c))
     assert np.array_equal(acc[:, 0], acc[:, 1]) and np.array_equal(acc[:, 0], acc[:, 2])
     assert np.all(acc[:, 3] == 1.0)
+
+
+def test_f64_path_tracer_agrees_with_f32(oracle):
+    """The binary64 path tracer (the converged reference of the learned
+    field's image checks) against the FP32 restatement of
+    pathTracingIntegrate at the same sample count, with independent random
+    numbers: image means within 1 %, and the RMSE at the level of the noise
+    (two FP32 images of other random streams differ by as much)."""
+    from conftest import dataset
+    from helpers import OracleScene, host_lp, oracle_only_lp, ramp_tf
+    ds = dataset("small")
+    f = oracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+    lo, hi, vr = f.bounds()
+    tf = ramp_tf()
+    xf = (np.float32(vr[0]), np.float32(vr[1]))
+    o = OracleScene(oracle, ds, (32, 32, 32), lo, hi, tf, xf)
+    w = h = 12
+    spp = 2048
+    lp = oracle_only_lp(lo, hi, (32, 32, 32), tf, xf, w, h, 0, spp)
+    hl, _, hacc, _, _ = host_lp(lp, o, w, h)
+    assert o.f.render(bytes(hl), w, h) == 0
+    a = hacc[:, :3].astype(np.float64) / spp
+    hl.ext.frameID = 5
+    hacc[:] = 0
+    assert o.f.render(bytes(hl), w, h) == 0
+    b = hacc[:, :3].astype(np.float64) / spp
+    ref = o.f.render_f64(bytes(hl), w, h)
+    noise = np.sqrt(np.mean((a - b) ** 2))
+    assert 0 < noise < 0.05
+    assert np.sqrt(np.mean((a - ref) ** 2)) < 1.5 * noise
+    assert abs(a.mean() - ref.mean()) < 0.01 * ref.mean()
+    assert ref.mean() > 0.1

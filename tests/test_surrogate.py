@@ -227,10 +227,15 @@ def test_zero_tolerance_render_equals_exact(small_scene, oracle, torch_cuda):
 
 
 @gpu
-def test_learned_render_close_to_exact(small_scene, oracle, torch_cuda):
-    """Converged image of the learned field against the FP64 ratio-tracking
-    oracle, next to the exact sampler's image at the same sample count, and
-    the widened majorants holding on the learned samples."""
+def test_learned_render_converged_rmse(small_scene, oracle, torch_cuda):
+    """The learned-field workload's integrator (path tracing, albedo 0.8,
+    HG g = 0.3, <= 8 bounces, one directional light) on the small field:
+    converged 32x32 images at 32768 spp against the FP64 path-tracing oracle
+    at 32768 spp.  The exact sampler's image is within 0.005 RMSE of it
+    (the noise floor of both), the learned field + exact fallback within
+    0.01 (absolute).  Learned densities above their macrocell's widened
+    majorant are limited to it (so tracking stays unbiased for the limited
+    field); they are counted and must stay rare."""
     torch = torch_cuda
     from owlexastitcher_gb300 import exastitch as E
     ds, g = small_scene
@@ -239,39 +244,43 @@ def test_learned_render_close_to_exact(small_scene, oracle, torch_cuda):
     S.evaluate(0.02, 1 << 21)
     st = S.stats()
     assert st["numSurrogateMacrocells"] > 0
-    w, h, spp = 32, 32, 1024
+    w, h, spp, frames = 32, 32, 4096, 8
     cam = orbit_camera(g.lo, g.hi, w, h)
-    lp = setup_render(g.lp, cam, w, h, 1, spp, "directional", False, g.lo, g.hi)
+    lp = setup_render(g.lp, cam, w, h, E.PATH_TRACING_INTEGRATOR, spp, "directional", True, g.lo, g.hi)
     cnt = torch.zeros(16, dtype=torch.int64, device="cuda")
 
-    def gpu_image(fn, frame, counters=None):
-        fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
-        acc = torch.zeros(w * h * 4, dtype=torch.float32, device="cuda")
-        lp.accumID = 0
-        lp.ext.frameID = frame
-        lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
-        lp.ext.traceT = lp.ext.traceTr = None
-        lp.ext.stepCounters = counters
-        E._check(fn(g.ctx.h, C.byref(lp), w, h))
-        g.ctx.sync()
-        lp.ext.stepCounters = None
-        return acc.cpu().numpy().reshape(-1, 4)[:, :3].astype(np.float64) / spp
+    def gpu_image(fn, counters=None):
+        img = np.zeros((w * h, 3), np.float64)
+        for fr in range(frames):  # independent RNG streams per frame
+            fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+            acc = torch.zeros(w * h * 4, dtype=torch.float32, device="cuda")
+            lp.accumID = 0
+            lp.ext.frameID = fr
+            lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+            lp.ext.traceT = lp.ext.traceTr = None
+            lp.ext.stepCounters = counters
+            E._check(fn(g.ctx.h, C.byref(lp), w, h))
+            g.ctx.sync()
+            lp.ext.stepCounters = None
+            img += acc.cpu().numpy().reshape(-1, 4)[:, :3].astype(np.float64)
+        return img / (spp * frames)
 
-    exact0 = gpu_image(E.lib().exa_render, 0)
-    learned0 = gpu_image(E.lib().exa_render_surrogate, 0, cnt.data_ptr())
+    exact = gpu_image(E.lib().exa_render)
+    learned = gpu_image(E.lib().exa_render_surrogate, cnt.data_ptr())
     lp.ext.frameID = 0
     o = OracleScene(oracle, ds, g.num_mcs, g.lo, g.hi, g.tf, g.xf)
     hl = host_lp(lp, o, w, h)[0]
-    hl.render.spp = 4096
+    hl.render.spp = spp * frames
     ref = o.f.render_f64(bytes(hl), w, h)
     c = cnt.cpu().numpy()
-    learned, violations = int(c[10]), int(c[11])
-    assert learned > 0
-    assert violations <= 1e-3 * learned
+    n_learned, n_limited = int(c[10]), int(c[11])
+    assert n_learned > 0
+    assert n_limited <= 1e-3 * n_learned
 
     def rmse(a, b):
         return float(np.sqrt(np.mean((a - b) ** 2)))
 
-    e_exact, e_learned = rmse(exact0, ref), rmse(learned0, ref)
-    assert e_exact <= 0.03
-    assert e_learned <= max(0.01, 1.5 * e_exact)
+    e_exact, e_learned = rmse(exact, ref), rmse(learned, ref)
+    print(f"RMSE vs FP64: exact {e_exact:.5f}, learned {e_learned:.5f}; limited {n_limited} of {n_learned}")
+    assert e_exact <= 0.005
+    assert e_learned <= 0.01
