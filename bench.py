@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-field (surrogate) measurements")
     ap.add_argument("--learned-steps", type=int, default=1600, help="surrogate training steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-frames measurements")
+    ap.add_argument("--split", default="replicas", choices=["replicas", "bands"],
+                    help="multi-GPU: replicas (a frame per rank, weak scaling) or bands (one frame, a band of rows "
+                         "per rank, gathered on rank 0; strong scaling)")
     a = ap.parse_args()
     big = a.config == "cloud"
     a.width = a.width or (1920 if big else WIDTH)
@@ -198,7 +201,13 @@ def run_ours(a):
     cam = orbit_camera(lo, hi, a.width, a.height)
     setup_render(r.lp, cam, a.width, a.height, E.PATH_TRACING_INTEGRATOR, a.spp, "directional", True)
     r.lp.ext.maxBounces = a.bounces
-    r.lp.ext.frameID = replicas.frame_id(rank)  # independent frames per rank
+    bands = a.split == "bands" and world > 1
+    if bands:
+        # one frame: this rank's band of rows
+        r.lp.ext.rowBegin, r.lp.ext.rowEnd = replicas.band_rows(rank, world, a.height)
+        band = (r.lp.ext.rowBegin, r.lp.ext.rowEnd)
+    else:
+        r.lp.ext.frameID = replicas.frame_id(rank)  # independent frames per rank
     paths_per_step = a.width * a.height * a.spp
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -236,7 +245,8 @@ def run_ours(a):
     timed_frame = (r.accum.cpu().numpy().reshape(-1, 4).copy(), r.fb.cpu().numpy().view(np.uint32).copy())
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = replicas.slowest_ms(sum(step_ms) / len(step_ms), world, device="cuda")
-    value = replicas.job_paths_per_s(world, paths_per_step, ms)
+    # bands: the ranks share one frame's paths; replicas: every rank a frame
+    value = replicas.job_paths_per_s(1 if bands else world, paths_per_step, ms)
     clocks = clk.summary()
 
     # counting launch (same frame): algorithmic work of one launch
@@ -266,13 +276,17 @@ def run_ours(a):
     host_fb = torch.empty(a.width * a.height, dtype=torch.int32, pin_memory=True)
     e2e_t = []
     for i in range(max(3, a.steps)):
+        barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         step()
         host_fb.copy_(r.fb, non_blocking=True)
         torch.cuda.synchronize()
+        if bands:  # rank 0 assembles the frame from the ranks' rows
+            replicas.gather_rows(host_fb.numpy()[band[0] * a.width:band[1] * a.width], rank, world, a.height,
+                                 a.width)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = statistics.median(e2e_t)
+    e2e_s = replicas.slowest_ms(statistics.median(e2e_t) * 1e3, world, device="cuda") / 1e3
     lp_bytes = E.C.sizeof(E.LaunchParams)
 
     # field point queries (1M uniform points in cellBounds), device and e2e
@@ -329,9 +343,11 @@ def run_ours(a):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": a.steps,
-            "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "strong" if bands else "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded AMR Gaussians + value noise)",
-            "config": workload_config(a),
+            "config": workload_config(a) | {"multi_gpu": "bands: one frame, a band of rows per rank, gathered on "
+                                                          "rank 0" if bands else "replicas: a frame per rank"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_wf_walk (summed over the frame's launches)" if render_stats["wavefront"] else
@@ -343,8 +359,8 @@ def run_ours(a):
                               "dda_cells_per_step": dda_cells,
                               "point_query_per_s": q_dev, "point_query_e2e_per_s": q_e2e,
                               "point_query_n": len(P), "work_per_step": work},
-            "e2e": {"value": world * paths_per_step / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": lp_bytes,
-                    "d2h_bytes_per_step": a.width * a.height * 4},
+            "e2e": {"value": (1 if bands else world) * paths_per_step / e2e_s, "unit": "paths/s",
+                    "h2d_bytes_per_step": lp_bytes, "d2h_bytes_per_step": a.width * a.height * 4},
             "cpu_baseline": cpu,
             "parity": parity,
             "clocks": clocks,

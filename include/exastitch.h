@@ -44,6 +44,8 @@ extern "C" {
 #define EXA_DEVERR_BOUNCE_CAP   8u  /* reserved (paths end at ext.maxBounces)    */
 #define EXA_DEVERR_WATCHDOG    16u  /* persistent-kernel work loop cap          */
 #define EXA_DEVERR_COPY_WAIT   32u  /* bulk copy to shared memory: wait limit   */
+#define EXA_DEVERR_BOUNDS      64u  /* bounds-checked build (EXA_CHECKS=1): an  */
+                                    /* index out of range, its access skipped  */
 
 /* exa_debug_set_flags: simulations of error paths for tests */
 #define EXA_DEBUG_COPY_WAIT_TIMEOUT 1u  /* the majorant build's first bulk-copy */
@@ -207,7 +209,15 @@ typedef struct {
   int32_t   ddaCellCap;      /* > 0: macrocells a walk may visit before it  */
                              /* ends with EXA_DEVERR_DDA_CAP; 0: the grid's */
                              /* dims.x + dims.y + dims.z + 3                */
+  int32_t   rowBegin;        /* rowEnd > 0: exa_render / _surrogate render  */
+  int32_t   rowEnd;          /* only the frame's rows [rowBegin, rowEnd)    */
+                             /* (rowBegin a multiple of 8; rowEnd a multiple */
+                             /* of 8 or the height), each pixel exactly as   */
+                             /* in the whole frame (same rays and random     */
+                             /* numbers); the other rows' outputs are not    */
+                             /* written.  A frame split across GPUs.         */
   int32_t   pad0;
+  int32_t   pad1;
 } exa_lp_ext;
 
 /* LaunchParams.h:56-119, field order and types kept; the sampler union
@@ -542,7 +552,8 @@ typedef struct {
   float    totalMs;           /* exa_sampler_build, host wall time          */
   float    elemMajorantMs;    /* element value ranges into the grid         */
   float    gridletMajorantMs; /* gridlet value ranges into the grid         */
-  uint32_t majorantBlocks;    /* blocks of the gridlet majorant kernel      */
+  uint32_t majorantBlocks;    /* gridlet pipelines (warps) of the majorant  */
+                              /* build's separable kernel                   */
 } exa_build_stats;
 int exa_get_build_stats(exa_context *ctx, exa_build_stats *out);
 

@@ -13,7 +13,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libexaref.so")
-REF_TREE = "/root/reference"
+# the owlExaStitcher source tree (only where it is present): the
+# EXA_REFERENCE_TREE environment variable, else the build container's mount
+REF_TREE = os.environ.get("EXA_REFERENCE_TREE", "/root/reference")
 
 
 def build(ref=True):

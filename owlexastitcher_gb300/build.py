@@ -47,19 +47,24 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build_exastitch(verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
-    out = os.path.join(PKG, "libexastitch.so")
+def build_exastitch(verbose=False, variant=None):
+    """variant "checks": libexastitch_checks.so, built with EXA_CHECKS=1 (the
+    kernels test every index they read through before the access, record
+    EXA_DEVERR_BOUNDS and skip it), objects in _build/checks"""
+    build = BUILD if variant is None else os.path.join(BUILD, variant)
+    os.makedirs(build, exist_ok=True)
+    out = os.path.join(PKG, "libexastitch.so" if variant is None else f"libexastitch_{variant}.so")
+    vflags = [] if variant is None else {"checks": ["-DEXA_CHECKS=1"]}[variant]
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "exastitch.h")]
     objs, jobs = [], []
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(build, src + ".o")
         objs.append(o)
         if _newer(o, [s] + hdrs):
             # EXA_NVCC_EXTRA: extra nvcc flags (e.g. -DEXA_RENDER_MIN_BLOCKS=3)
             extra = os.environ.get("EXA_NVCC_EXTRA", "").split()
-            cmd = [nvcc()] + ARCH + NVFLAGS + extra + ["-x", "cu", "-c", s, "-o", o]
+            cmd = [nvcc()] + ARCH + NVFLAGS + vflags + extra + ["-x", "cu", "-c", s, "-o", o]
             if verbose:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

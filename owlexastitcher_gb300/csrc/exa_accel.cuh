@@ -34,6 +34,7 @@ struct GridletTable {
   int n[3];        // blocks per axis
   const int32_t *entries;  // -1 empty; >= 0 gridlet; <= -2 list at items[-e-2]
   const int32_t *items;    // list: count, ids ascending
+  int numItems;            // length of items (for the bounds-checked build)
 };
 
 struct BvhNode {   // 64 B: two child boxes, two child refs, two opacities
@@ -156,7 +157,7 @@ EXA_D int table_entry(const GridletTable &T, int bx, int by, int bz)
 
 // test every candidate gridlet of one table; keeps the lowest index hit
 EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool cull, int &best,
-                       float &bestVal, int &bestCell, QueryStats *qs)
+                       float &bestVal, int &bestCell, QueryStats *qs, uint32_t &err)
 {
   if (qs) qs->tables++;
   int b0[3], nb[3];
@@ -169,12 +170,15 @@ EXA_D void query_table(const AccelView &A, const GridletTable &T, V3 pos, bool c
         int cnt = 1;
         const int32_t *list = nullptr;
         if (e <= -2) {
+          if (!exa_in_range(-e - 2, T.numItems, err)) continue;
           list = T.items + (-e - 2);
           cnt = __ldg(list);
+          if (!exa_in_range(-e - 2 + cnt, T.numItems, err)) continue;
         }
         for (int k = 0; k < cnt; ++k) {
           const int g = list ? __ldg(list + 1 + k) : e;
           if (g >= best) break;  // lists are ascending
+          if (!exa_in_range(g, A.numGridlets, err)) continue;
           if (cull && A.gridletMaxOps && __ldg(A.gridletMaxOps + g) == 0.f) continue;
           float v;
           int c;
@@ -197,7 +201,8 @@ EXA_D bool box_contains(const float *lo, const float *hi, V3 p)
 // overflow (error flag raised by the caller).  Out of line: element samples
 // are rare next to gridlet samples, and keeping the BVH walk and the three
 // Newton solvers out of the tracking loop keeps that loop's code small.
-static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal)
+static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal,
+                                                   uint32_t &err)
 {
   if (A.numElems <= 0) return true;
   int stack[kBvhStack];
@@ -206,6 +211,7 @@ static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, b
   const bool useOps = cull && A.elemMaxOps;
   // a well-formed tree visits each of its numElems-1 nodes at most once
   for (int visits = 0; visits <= A.numElems + 1; ++visits) {
+    if (!exa_in_range(node, A.numElems > 1 ? A.numElems - 1 : 1, err)) return true;
     const float4 *np = reinterpret_cast<const float4 *>(A.nodes + node);
     const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
     const float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
@@ -218,7 +224,10 @@ static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, b
       if (c0 < 0) {
         const int e = ~c0;
         float v;
-        if (e < best && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) { best = e; bestVal = v; }
+        if (e < best && exa_in_range(e, A.numElems, err) && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) {
+          best = e;
+          bestVal = v;
+        }
       } else {
         next = c0;
       }
@@ -227,7 +236,10 @@ static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, b
       if (c1 < 0) {
         const int e = ~c1;
         float v;
-        if (e < best && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) { best = e; bestVal = v; }
+        if (e < best && exa_in_range(e, A.numElems, err) && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) {
+          best = e;
+          bestVal = v;
+        }
       } else if (next < 0) {
         next = c1;
       } else {
@@ -403,31 +415,18 @@ static __device__ __noinline__ exa_sample brick_sample(const BrickView &V, V3 po
   return s;
 }
 
-EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
+// the stitching elements' part of sample(): where no gridlet holds pos
+EXA_D exa_sample sample_elements(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs)
 {
-  if (A.amr) return amr_sample(*A.amr, pos);
-  if (A.bricks) return brick_sample(*A.bricks, pos, err);
   exa_sample s;
   s.primID = -1;
   s.cellID = -1;
   s.value = 0.f;
-  int best = 0x7fffffff, cell = -1;
-  float val = 0.f;
-  for (int t = 0; t < A.numTables; ++t) {
-    query_table(A, A.tables[t], pos, cull, best, val, cell, qs);
-    if (A.tablesSorted && best != 0x7fffffff) break;
-  }
-  if (best != 0x7fffffff) {
-    s.primID = best;
-    s.cellID = cell;
-    s.value = val;
-    return s;
-  }
   int be = 0x7fffffff;
   float ev = 0.f;
   if (A.numElems > 0 && occ_maybe(A.occ, pos)) {
     if (qs) qs->bvhWalks++;
-    if (!query_elements(A, pos, cull, be, ev)) err |= EXA_DEVERR_BVH_STACK;
+    if (!query_elements(A, pos, cull, be, ev, err)) err |= EXA_DEVERR_BVH_STACK;
   }
   if (be != 0x7fffffff) {
     s.primID = be;
@@ -435,6 +434,64 @@ EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &e
     s.value = ev;
   }
   return s;
+}
+
+EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
+{
+  if (A.amr) return amr_sample(*A.amr, pos);
+  if (A.bricks) return brick_sample(*A.bricks, pos, err);
+  int best = 0x7fffffff, cell = -1;
+  float val = 0.f;
+  for (int t = 0; t < A.numTables; ++t) {
+    query_table(A, A.tables[t], pos, cull, best, val, cell, qs, err);
+    if (A.tablesSorted && best != 0x7fffffff) break;
+  }
+  if (best != 0x7fffffff) {
+    exa_sample s;
+    s.primID = best;
+    s.cellID = cell;
+    s.value = val;
+    return s;
+  }
+  return sample_elements(A, pos, cull, err, qs);
+}
+
+// sample_field for a point whose walk last sampled gridlet `hint` (in an
+// earlier macrocell, so the reference's cache does not apply).  Where the
+// point's block of the (single) gridlet table is not on a block face and
+// lists the hint alone, the full query tests the hint and, where it misses,
+// the elements; the hint's header and max opacity then load beside the
+// table entry instead of after it.  Same answer as sample_field in every
+// case.
+EXA_D exa_sample sample_field_hinted(const AccelView &A, V3 pos, bool cull, int hint, uint32_t &err,
+                                     QueryStats *qs = nullptr)
+{
+  if (A.numTables == 1 && !A.amr && !A.bricks && exa_in_range(hint, A.numGridlets, err)) {
+    const GridletTable &T = A.tables[0];
+    int b0[3], nb[3];
+    if (table_block(T, pos, b0, nb) && nb[0] == 1 && nb[1] == 1 && nb[2] == 1) {
+      const int e = table_entry(T, b0[0], b0[1], b0[2]);
+      const int4 h0 = __ldg(reinterpret_cast<const int4 *>(A.gridlets + hint));
+      const int4 h1 = __ldg(reinterpret_cast<const int4 *>(A.gridlets + hint) + 1);
+      const bool visible = !(cull && A.gridletMaxOps) || __ldg(A.gridletMaxOps + hint) != 0.f;
+      if (e == hint) {
+        if (qs) qs->tables++;
+        exa_sample s;
+        s.primID = -1;
+        s.cellID = -1;
+        s.value = 0.f;
+        if (visible) {
+          if (qs) qs->gridletTests++;
+          if (intersect_gridlet_hdr(s.value, s.cellID, pos, h0, h1, A.scalars)) {
+            s.primID = hint;
+            return s;
+          }
+        }
+        return sample_elements(A, pos, cull, err, qs);
+      }
+    }
+  }
+  return sample_field(A, pos, cull, err, qs);
 }
 
 // testSample (sampler/ExaStitchSampler.h:108-126): the cached gridlet only

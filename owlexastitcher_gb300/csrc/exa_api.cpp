@@ -324,6 +324,7 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
     accel.tables[i] = tabs[i].t;
     accel.tables[i].entries = tableEntries[i].ptr;
     accel.tables[i].items = tableItems[i].ptr;
+    accel.tables[i].numItems = (int)tabs[i].items.size();
   }
 }
 
@@ -444,10 +445,11 @@ bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
                       g.valueRanges.ptr, elemValueRanges.ptr, s);
   timer.mark(1);
   buildStats = {};
+  majorantScratch.alloc(model->gridlets.size() + 1);
   buildStats.majorantBlocks =
       launchGridletMajorants(gridletBuffer.ptr, gridletScalarBuffer.ptr, model->gridlets.size(),
                              model->gridletScalars.size(), g.dims, g.worldBounds, g.valueRanges.ptr,
-                             gridletValueRanges.ptr, buildErrors.ptr, debugFlags, s);
+                             gridletValueRanges.ptr, buildErrors.ptr, debugFlags, majorantScratch.ptr, s);
   timer.mark(2);
   g.deviceTraversable.dims = g.dims;
   g.deviceTraversable.bounds = g.worldBounds;
@@ -821,6 +823,14 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     needLpCaps(*lp, ctx->sampler->tfFilter);
+    if (lp->ext.rowEnd > 0) {
+      need(lp->ext.rowBegin >= 0 && lp->ext.rowBegin % 8 == 0 && lp->ext.rowBegin < lp->ext.rowEnd &&
+               lp->ext.rowEnd <= height && (lp->ext.rowEnd % 8 == 0 || lp->ext.rowEnd == height),
+           EXA_ERR_INVALID, "row band: need 0 <= rowBegin < rowEnd <= height, rowBegin a multiple of 8, rowEnd a "
+                            "multiple of 8 or the height");
+      need((useWavefront() || learned) && lp->integrator != EXA_RAY_MARCHING_INTEGRATOR, EXA_ERR_INVALID,
+           "row bands need the wavefront renderer (path tracing or direct lighting)");
+    }
     // the AMR-cell and ExaBrick samplers render shade mode default
     // (renderFrame_AMRCellSampler / _ExaBrickSampler, deviceCode.cu:1360-1387)
     need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||
@@ -830,6 +840,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     const size_t ns = (size_t)width * height * (size_t)lp->render.spp;
     if (ctx->sampleColors.count < ns) ctx->sampleColors.alloc(ns);
     exa_launch_params lpUse = *lp;
+    fillLoopCaps(lpUse);
     lpUse.ext.heatCounts = nullptr;
     if (lp->render.heatMapEnabled) {
       // per-pixel work of this frame for the heat map
@@ -1898,8 +1909,10 @@ void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
   launchElemMajorants(S.vertexBuffer.ptr, S.indexBuffer.ptr, m.indices.size() / 8, B.dims, m.cellBounds, B.ranges.ptr,
                       er.ptr, ctx->stream);
   cudaCheck(cudaMemsetAsync(S.buildErrors.ptr, 0, sizeof(uint32_t), ctx->stream), "memset build errors");
+  DBuf<uint32_t> scratch;
+  scratch.alloc(m.gridlets.size() + 1);
   launchGridletMajorants(S.gridletBuffer.ptr, S.gridletScalarBuffer.ptr, m.gridlets.size(), m.gridletScalars.size(),
-                         B.dims, m.cellBounds, B.ranges.ptr, gr.ptr, S.buildErrors.ptr, 0u, ctx->stream);
+                         B.dims, m.cellBounds, B.ranges.ptr, gr.ptr, S.buildErrors.ptr, 0u, scratch.ptr, ctx->stream);
   B.maxOps.resize(B.tfColors.size());
   for (size_t t = 0; t < B.tfColors.size(); ++t) {
     B.maxOps[t].alloc(n);
@@ -1963,6 +1976,7 @@ void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch
        "lpTemplate.sampler.ess.sampleBVH is not this context's sampler (call exa_sampler_set_lps)");
   need(tpl->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
   needLpCaps(*tpl, ctx->sampler->tfFilter);
+  need(tpl->ext.rowEnd <= 0, EXA_ERR_INVALID, "row bands are not supported in batches");
   need(B.tileW == 8 || B.tileW == 16 || B.tileW == 32, EXA_ERR_INVALID, "bad tile width");
   setDevice(ctx);
   const int th = 128 / B.tileW;
@@ -1991,6 +2005,7 @@ void renderBatch(exa_context *ctx, const exa_launch_params *tpl, const exa_batch
     lp.maxOpacities = B.maxOps[f.tf].ptr;
     lp.majorantGrid.dims = B.dims;
     lp.majorantGrid.bounds = ctx->model->cellBounds;
+    fillLoopCaps(lp);
     lp.ext.traceT = nullptr;
     lp.ext.traceTr = nullptr;
     lp.ext.deviceErrors = ctx->errors.ptr;
@@ -2198,6 +2213,7 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     needLpCaps(*lp, ctx->sampler->tfFilter);
+    need(lp->ext.rowEnd <= 0, EXA_ERR_INVALID, "row bands are not supported (exa_render renders them)");
     // as in exa_render: the AMR-cell and ExaBrick samplers have no gridlet
     // cells to colour
     need((ctx->sampler->accel.amr == nullptr && ctx->sampler->accel.bricks == nullptr) ||
@@ -2215,6 +2231,8 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
       }
       scratch = g_noallocAddr[ctx->device];
     }
-    launchRender(ctx->sampler->accel, *lp, width, height, ctx->jobCounter.ptr, scratch, ctx->stream);
+    exa_launch_params lpUse = *lp;
+    fillLoopCaps(lpUse);
+    launchRender(ctx->sampler->accel, lpUse, width, height, ctx->jobCounter.ptr, scratch, ctx->stream);
   });
 }

@@ -224,15 +224,22 @@ EXA_D void prepare_gridlet(MajSmem &sm, int buf, const exa_gridlet &hdr, const f
   pl.hiMC = project_on_grid(hi, D, wb);
 }
 
+//
+// list != null: the gridlets list[0 .. *listCount) instead of 0 .. ng (the
+// gridlets the separable kernel below leaves to this one).
 __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa_gridlet *__restrict__ gridlets, size_t ng,
                                                                    const float *__restrict__ scalars, size_t nScalars,
                                                                    bool stage, exa_vec3i dims, exa_box3f wb,
                                                                    exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                                                   uint32_t *errors, uint32_t debugFlags)
+                                                                   uint32_t *errors, uint32_t debugFlags,
+                                                                   const uint32_t *__restrict__ list,
+                                                                   const unsigned *__restrict__ listCount)
 {
   __shared__ MajSmem sm;
   const int tid = threadIdx.x;
   const V3i D = {dims.x, dims.y, dims.z};
+  if (list) ng = *listCount;
+  auto idOf = [&](size_t i) -> size_t { return list ? (size_t)list[i] : i; };
   // thread 0 holds the header of the gridlet after the next one, loaded an
   // iteration before it is planned
   exa_gridlet ahead{};
@@ -240,8 +247,8 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
     mbar_init(&sm.bar[0]);
     mbar_init(&sm.bar[1]);
     mbar_init_fence();
-    if (blockIdx.x < ng) prepare_gridlet(sm, 0, gridlets[blockIdx.x], scalars, nScalars, stage, D, wb);
-    if (blockIdx.x + gridDim.x < ng) ahead = gridlets[blockIdx.x + gridDim.x];
+    if (blockIdx.x < ng) prepare_gridlet(sm, 0, gridlets[idOf(blockIdx.x)], scalars, nScalars, stage, D, wb);
+    if (blockIdx.x + gridDim.x < ng) ahead = gridlets[idOf(blockIdx.x + gridDim.x)];
   }
   __syncthreads();
   const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
     if (tid == 0 && gn < ng) {
       fence_proxy_async_smem();
       prepare_gridlet(sm, buf ^ 1, ahead, scalars, nScalars, stage, D, wb);
-      if (gn + gridDim.x < ng) ahead = gridlets[gn + gridDim.x];
+      if (gn + gridDim.x < ng) ahead = gridlets[idOf(gn + gridDim.x)];
     }
     const float *S = scalars + (uint32_t)g.begin;
     if (P.staged) {
@@ -408,33 +415,252 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
         glo = fminf(glo, sm.redLo[w]);
         ghi = fmaxf(ghi, sm.redHi[w]);
       }
-      gridletRanges[gi].lower = glo;
-      gridletRanges[gi].upper = ghi;
+      gridletRanges[idOf(gi)].lower = glo;
+      gridletRanges[idOf(gi)].upper = ghi;
     }
     // buffer, window and reduction slots are free for the next gridlet
     __syncthreads();
   }
 }
 
+// ------------------------------------------------------------------------
+// The same build, separable: one warp per gridlet, no per-cell loop.
+//
+// The macrocells a cell updates are a product of per-axis index ranges (the
+// AND of per-axis interval tests of Grid.cu:172-183, as above), and a cell
+// with a non-NaN corner updates each of them with the min / max over its
+// non-NaN corners (and the +-1e30 of the empty range).  So a corner with a
+// non-NaN value reaches exactly the macrocells in the product over the axes
+// of U_a(j) = the union of the ranges of the (one or two) cells that have
+// corner index j along axis a: every combination of those cells is a cell
+// holding the corner.  A macrocell's update is then the min / max over the
+// corners whose three unions contain it, which is reduced one axis at a
+// time: along x for every corner row and macrocell column (the corners of a
+// column are an interval [ca, cb] of the row), then over the y x z
+// rectangle of rows of each macrocell; one atomic min / max per touched
+// macrocell.  Min and max are exact, so the result is the per-cell loop's.
+//
+// A gridlet takes this path when its brick is staged (<= kBrickCap floats,
+// so <= 8 cells per axis), its macrocell window is at most kSepWin wide on
+// every axis and every macrocell's corner set is an interval; the others
+// are appended to a list for k_gridlet_majorants.
+constexpr int kSepWarps = 4;      // warps (independent gridlet pipelines) per block
+constexpr int kSepWin = 9;        // macrocells per axis of a gridlet's window
+constexpr int kSepRows = 81;      // corner rows (y, z) of an 8^3-cell gridlet
+
+struct alignas(16) SepWarpSmem {
+  float brick[2][kBrickCap];
+  float2 rx[kSepWin * kSepRows];  // (min, max) per (macrocell column, corner row)
+  int2 cellRange[3][8];           // per axis and cell index: its macrocell range
+  int2 cornerIv[3][kSepWin];      // per axis and window macrocell: corners [ca, cb]
+  GridletPlan plan[2];
+  uint64_t bar[2];
+};
+
+__global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
+    const exa_gridlet *__restrict__ gridlets, size_t ng, const float *__restrict__ scalars, size_t nScalars,
+    bool stage, exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges, uint32_t *errors,
+    uint32_t debugFlags, uint32_t *fallback, unsigned *fallbackCount)
+{
+  extern __shared__ __align__(16) unsigned char sepSm[];
+  SepWarpSmem &sm = reinterpret_cast<SepWarpSmem *>(sepSm)[threadIdx.x >> 5];
+  const unsigned lane = threadIdx.x & 31;
+  const size_t w0 = (size_t)blockIdx.x * kSepWarps + (threadIdx.x >> 5);
+  const size_t stride = (size_t)gridDim.x * kSepWarps;
+  const V3i D = {dims.x, dims.y, dims.z};
+  // lane 0 stages a gridlet: its plan and the bulk copy of its brick
+  auto prepare = [&](int buf, const exa_gridlet &hdr) {
+    GridletPlan &pl = sm.plan[buf];
+    pl.g = hdr;
+    pl.P = brick_plan(pl.g, nScalars, stage);
+    if (pl.P.bulk) bulk_load_smem(sm.brick[buf], scalars + pl.P.f0, pl.P.bulk, &sm.bar[buf]);
+    const float cw = (float)(1 << hdr.level);
+    const V3 lo = mk3(((float)hdr.lower.x + 0.5f) * cw, ((float)hdr.lower.y + 0.5f) * cw,
+                      ((float)hdr.lower.z + 0.5f) * cw);
+    const V3 hi = mk3((((float)hdr.lower.x + (float)hdr.dims.x) + 0.5f) * cw,
+                      (((float)hdr.lower.y + (float)hdr.dims.y) + 0.5f) * cw,
+                      (((float)hdr.lower.z + (float)hdr.dims.z) + 0.5f) * cw);
+    pl.loMC = project_on_grid(lo, D, wb);
+    pl.hiMC = project_on_grid(hi, D, wb);
+  };
+  if (lane == 0) {
+    mbar_init(&sm.bar[0]);
+    mbar_init(&sm.bar[1]);
+    mbar_init_fence();
+    if (w0 < ng) prepare(0, gridlets[w0]);
+  }
+  __syncwarp();
+  const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
+  uint32_t parity = 0;
+  int it = 0;
+  for (size_t gi = w0; gi < ng; gi += stride, ++it) {
+    const int buf = it & 1;
+    const exa_gridlet g = sm.plan[buf].g;
+    const BrickPlan P = sm.plan[buf].P;
+    const V3i loMC = sm.plan[buf].loMC, hiMC = sm.plan[buf].hiMC;
+    const size_t gn = gi + stride;
+    if (lane == 0 && gn < ng) {
+      fence_proxy_async_smem();
+      prepare(buf ^ 1, gridlets[gn]);
+    }
+    const uint32_t ph = (parity >> buf) & 1u;
+    bool ok = true;
+    if (P.bulk) {
+      ok = mbar_wait(&sm.bar[buf], ph);
+      // the simulated time-out of the error-path test (see k_gridlet_majorants)
+      if ((debugFlags & EXA_DEBUG_COPY_WAIT_TIMEOUT) && gi == 0) ok = false;
+      parity ^= 1u << buf;
+    }
+    if (__any_sync(0xffffffffu, !ok)) {
+      // give up: flag it and wait (bounded) for both buffers' copies
+      if (lane == 0) {
+        if (errors) atomicOr(errors, EXA_DEVERR_COPY_WAIT);
+        if (P.bulk) (void)mbar_wait(&sm.bar[buf], ph);
+        if (gn < ng && sm.plan[buf ^ 1].P.bulk) (void)mbar_wait(&sm.bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
+      }
+      return;
+    }
+    const int wx = hiMC.x - loMC.x + 1, wy = hiMC.y - loMC.y + 1, wz = hiMC.z - loMC.z + 1;
+    bool sep = P.staged && g.dims.x <= 8 && g.dims.y <= 8 && g.dims.z <= 8 && wx <= kSepWin && wy <= kSepWin &&
+               wz <= kSepWin;
+    const int nx = g.dims.x + 1, ny = g.dims.y + 1, nz = g.dims.z + 1;
+    const int rows = ny * nz;
+    float *B = sm.brick[buf];
+    if (sep) {
+      for (int k = lane; k < P.tail; k += 32) B[P.bulk / 4 + k] = __ldg(scalars + P.f0 + P.bulk / 4 + k);
+      // each cell's macrocell range along each axis
+      const float cw = (float)(1 << g.level), hc = 0.5f * cw;
+      if (lane < g.dims.x + g.dims.y + g.dims.z) {
+        const int a = (int)lane < g.dims.x ? 0 : (int)lane < g.dims.x + g.dims.y ? 1 : 2;
+        const int i = a == 0 ? lane : a == 1 ? lane - g.dims.x : lane - g.dims.x - g.dims.y;
+        const int lower = a == 0 ? g.lower.x : a == 1 ? g.lower.y : g.lower.z;
+        const float wlo = a == 0 ? wb.lower.x : a == 1 ? wb.lower.y : wb.lower.z;
+        const float whi = a == 0 ? wb.upper.x : a == 1 ? wb.upper.y : wb.upper.z;
+        const float size = a == 0 ? mcSize.x : a == 1 ? mcSize.y : mcSize.z;
+        const int n = a == 0 ? dims.x : a == 1 ? dims.y : dims.z;
+        const int lo = a == 0 ? loMC.x : a == 1 ? loMC.y : loMC.z;
+        const int hi = a == 0 ? hiMC.x : a == 1 ? hiMC.y : hiMC.z;
+        int m0, m1;
+        mc_axis_range((float)(lower + i) * cw + hc, (float)(lower + i + 1) * cw + hc, wlo, whi, size, n, lo, hi, m0,
+                      m1);
+        sm.cellRange[a][i] = make_int2(m0, m1);
+      }
+      __syncwarp();
+      // per axis and window macrocell: the corners whose cells reach it, an
+      // interval [ca, cb] (empty: ca > cb); a gap sends the gridlet to the
+      // general kernel
+      bool gap = false;
+      if (lane < wx + wy + wz) {
+        const int a = (int)lane < wx ? 0 : (int)lane < wx + wy ? 1 : 2;
+        const int off = a == 0 ? lane : a == 1 ? lane - wx : lane - wx - wy;
+        const int m = off + (a == 0 ? loMC.x : a == 1 ? loMC.y : loMC.z);
+        const int d = a == 0 ? g.dims.x : a == 1 ? g.dims.y : g.dims.z;
+        int ca = 1 << 20, cb = -1;
+        for (int j = 0; j <= d; ++j) {
+          bool in = false;
+          if (j > 0) { const int2 r = sm.cellRange[a][j - 1]; in = in || (r.x <= m && m <= r.y); }
+          if (j < d) { const int2 r = sm.cellRange[a][j]; in = in || (r.x <= m && m <= r.y); }
+          if (in) {
+            if (cb >= 0 && cb != j - 1) gap = true;
+            if (ca > j) ca = j;
+            cb = j;
+          }
+        }
+        sm.cornerIv[a][off] = make_int2(ca, cb);
+      }
+      sep = !__any_sync(0xffffffffu, gap);
+      __syncwarp();
+    }
+    if (!sep) {
+      if (lane == 0) fallback[atomicAdd(fallbackCount, 1u)] = (uint32_t)gi;
+      __syncwarp();
+      continue;
+    }
+    // the gridlet's own range: over every scalar (cell-less gridlets: empty)
+    float glo = 1e30f, ghi = -1e30f;
+    if (g.dims.x > 0 && g.dims.y > 0 && g.dims.z > 0)
+      for (int k = lane; k < nx * rows; k += 32) {
+        const float v = B[P.lead + k];
+        glo = fminf(glo, v);
+        ghi = fmaxf(ghi, v);
+      }
+    // along x: every (macrocell column, corner row)
+    for (int k = lane; k < wx * rows; k += 32) {
+      const int m = k / rows, r = k - m * rows;
+      const int2 iv = sm.cornerIv[0][m];
+      const float *R = B + P.lead + r * nx;
+      float lo = 1e30f, hi = -1e30f;
+      for (int j = iv.x; j <= iv.y; ++j) {
+        const float v = R[j];
+        lo = fminf(lo, v);
+        hi = fmaxf(hi, v);
+      }
+      sm.rx[k] = make_float2(lo, hi);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+      ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+    }
+    if (lane == 0) {
+      gridletRanges[gi].lower = glo;
+      gridletRanges[gi].upper = ghi;
+    }
+    __syncwarp();
+    // over the y x z rectangle of rows of each window macrocell
+    for (int k = lane; k < wx * wy * wz; k += 32) {
+      const int mx = k % wx, my = (k / wx) % wy, mz = k / (wx * wy);
+      const int2 iy = sm.cornerIv[1][my], iz = sm.cornerIv[2][mz];
+      const float2 *X = sm.rx + mx * rows;
+      float lo = 1e30f, hi = -1e30f;
+      for (int cz = iz.x; cz <= iz.y; ++cz)
+        for (int cy = iy.x; cy <= iy.y; ++cy) {
+          const float2 v = X[cz * ny + cy];
+          lo = fminf(lo, v.x);
+          hi = fmaxf(hi, v.y);
+        }
+      if (lo <= hi) update_mc(mcRanges, dims, loMC.x + mx, loMC.y + my, loMC.z + mz, lo, hi);
+    }
+    // this buffer and the tables are free for the next gridlets
+    __syncwarp();
+  }
+}
+
 unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
                                 exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                uint32_t *errors, uint32_t debugFlags, cudaStream_t s)
+                                uint32_t *errors, uint32_t debugFlags, uint32_t *scratch, cudaStream_t s)
 {
   if (!ng) return 0;
   int dev = 0, sms = 0;
   cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
   cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-  // as many resident blocks of 64 threads (~11 KB of shared memory each)
-  // as fit on every SM
+  const bool stage = (reinterpret_cast<uintptr_t>(scalars) & 15u) == 0;
+  // scratch: [0] the count of gridlets left to the general kernel, then
+  // their indices
+  unsigned *count = scratch;
+  uint32_t *list = scratch + 1;
+  cudaCheck(cudaMemsetAsync(count, 0, sizeof(unsigned), s), "memset fallback count");
+  const size_t sepSmem = kSepWarps * sizeof(SepWarpSmem);
+  cudaCheck(cudaFuncSetAttribute(k_gridlet_majorants_sep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sepSmem),
+            "separable majorant kernel shared memory");
+  int sepPerSM = 0;
+  cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sepPerSM, k_gridlet_majorants_sep, kSepWarps * 32,
+                                                          sepSmem),
+            "occupancy");
+  const size_t sepBlocks = std::min<size_t>((ng + kSepWarps - 1) / kSepWarps,
+                                            (size_t)std::max(sms, 1) * (size_t)std::max(sepPerSM, 1));
+  k_gridlet_majorants_sep<<<(unsigned)sepBlocks, kSepWarps * 32, sepSmem, s>>>(
+      g, ng, scalars, nScalars, stage, dims, wb, mcRanges, gridletRanges, errors, debugFlags, list, count);
+  cudaCheck(cudaGetLastError(), "k_gridlet_majorants_sep");
+  // the general kernel over the list (its blocks read the count)
   int perSM = 0;
   cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_gridlet_majorants, kMajThreads, 0),
             "occupancy");
   const size_t blocks = std::min<size_t>(ng, (size_t)std::max(sms, 1) * (size_t)std::max(perSM, 1));
-  const bool stage = (reinterpret_cast<uintptr_t>(scalars) & 15u) == 0;
   k_gridlet_majorants<<<(unsigned)blocks, kMajThreads, 0, s>>>(g, ng, scalars, nScalars, stage, dims, wb, mcRanges,
-                                                               gridletRanges, errors, debugFlags);
+                                                               gridletRanges, errors, 0u, list, count);
   cudaCheck(cudaGetLastError(), "k_gridlet_majorants");
-  return (unsigned)blocks;
+  return (unsigned)std::min<size_t>(sepBlocks * kSepWarps, ng);
 }
 
 // Grid.cu:73-117 (buildGrid<8>) plus the element's own range with the

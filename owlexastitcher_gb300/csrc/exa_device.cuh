@@ -18,6 +18,21 @@
 #define EXA_HD __host__ __device__ __forceinline__
 #define EXA_D __device__ __forceinline__
 
+// The bounds-checked build (EXA_CHECKS=1, libexastitch_checks.so): the
+// kernels test the indices they read through (gridlet and element ids from
+// tables, lists, caches and BVH leaves, BVH nodes, macrocells, queue slots)
+// before the access; an index out of range sets EXA_DEVERR_BOUNDS and the
+// access is skipped.  Compiled out otherwise.
+#ifndef EXA_CHECKS
+#define EXA_CHECKS 0
+#endif
+EXA_HD bool exa_in_range(long long i, long long n, uint32_t &err)
+{
+  if (!EXA_CHECKS || (i >= 0 && i < n)) return true;
+  err |= EXA_DEVERR_BOUNDS;
+  return false;
+}
+
 namespace exa {
 
 struct V3 { float x, y, z; };
@@ -121,11 +136,11 @@ struct Rng {
 // ------------------------------------------------------------------ Gridlet.h
 EXA_D float lerpf_(float a, float b, float x) { return (1.f - x) * a + x * b; }  // common.h:64-68
 
-// Gridlet.h:39-98.  Header loaded as two 16-byte vectors (one 32 B sector).
-EXA_D bool intersect_gridlet(float &value, int &cellID, V3 pos, const exa_gridlet *gp, const float *__restrict__ scalars)
+// Gridlet.h:39-98 for a header already loaded: h0 = (lower, level),
+// h1 = (dims, begin)
+EXA_D bool intersect_gridlet_hdr(float &value, int &cellID, V3 pos, const int4 h0, const int4 h1,
+                                 const float *__restrict__ scalars)
 {
-  const int4 h0 = __ldg(reinterpret_cast<const int4 *>(gp));
-  const int4 h1 = __ldg(reinterpret_cast<const int4 *>(gp) + 1);
   const int level = h0.w;
   const float cw = (float)(1 << level);
   const V3 lo = muls(mk3((float)h0.x + 0.5f, (float)h0.y + 0.5f, (float)h0.z + 0.5f), cw);
@@ -160,6 +175,14 @@ EXA_D bool intersect_gridlet(float &value, int &cellID, V3 pos, const exa_gridle
   value = lerpf_(f1234, f5678, frac.z);
   cellID = iz * h1.y * h1.x + iy * h1.x + ix;
   return true;
+}
+
+// Gridlet.h:39-98.  Header loaded as two 16-byte vectors (one 32 B sector).
+EXA_D bool intersect_gridlet(float &value, int &cellID, V3 pos, const exa_gridlet *gp, const float *__restrict__ scalars)
+{
+  const int4 h0 = __ldg(reinterpret_cast<const int4 *>(gp));
+  const int4 h1 = __ldg(reinterpret_cast<const int4 *>(gp) + 1);
+  return intersect_gridlet_hdr(value, cellID, pos, h0, h1, scalars);
 }
 
 // ------------------------------------------------------------------ Plane.h

@@ -175,6 +175,8 @@ class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
   DBuf<float> gridletMaxOpacities;
   DBuf<exa_range1f> elemValueRanges;
   DBuf<float> umeshMaxOpacities;
+  // the majorant build's list of gridlets for its general kernel
+  DBuf<uint32_t> majorantScratch;
   // EXA_DEVERR_* bits of the build kernels
   DBuf<uint32_t> buildErrors;
   // GPU times of the last build's majorant kernels
@@ -242,13 +244,27 @@ class ExaBrickSampler : public Sampler {
   DBuf<BrickView> deviceView;
 };
 
+// default delta / ratio tracking steps per macrocell (EXA_DEVERR_TRACK_CAP)
+constexpr int kTrackCapDefault = 1 << 22;
+
+// the walks' loop caps the kernels read: lp.ext's values, or the defaults
+// where they are 0 (tracking steps per macrocell; macrocells per walk:
+// dims.x + dims.y + dims.z + 3, more than a DDA walk visits)
+inline void fillLoopCaps(exa_launch_params &lp)
+{
+  if (lp.ext.trackStepCap <= 0) lp.ext.trackStepCap = kTrackCapDefault;
+  if (lp.ext.ddaCellCap <= 0)
+    lp.ext.ddaCellCap = lp.majorantGrid.dims.x + lp.majorantGrid.dims.y + lp.majorantGrid.dims.z + 3;
+}
+
 // ---------------------------------------------------------------- kernels
 // launchers implemented in exa_build.cu / exa_render.cu
 void launchInitRanges(exa_range1f *r, size_t n, cudaStream_t s);
-// returns the number of blocks launched
+// scratch: ng + 1 words (the gridlets the separable kernel leaves to the
+// general one); returns the number of warps of the separable kernel
 unsigned launchGridletMajorants(const exa_gridlet *g, const float *scalars, size_t ng, size_t nScalars,
                                 exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges,
-                                uint32_t *errors, uint32_t debugFlags, cudaStream_t s);
+                                uint32_t *errors, uint32_t debugFlags, uint32_t *scratch, cudaStream_t s);
 void launchElemMajorants(const float4 *verts, const int32_t *idx, size_t ne, exa_vec3i dims, exa_box3f wb,
                          exa_range1f *mcRanges, exa_range1f *elemRanges, cudaStream_t s);
 // Grid.cu:248-285: every cell's value into the macrocells its support
@@ -315,6 +331,7 @@ struct Surrogate {
   DBuf<float4> samples;                        // (x, y, z, value or NaN)
   DBuf<__nv_bfloat16> feats;
   DBuf<float> dfeat, lossBuf;
+  DBuf<uint32_t> trainErrors;  // EXA_DEVERR_* of the tensor-core training kernel
   DBuf<uint8_t> mcMode;
   DBuf<unsigned long long> mcErr;
   DBuf<unsigned> mcEmpty;

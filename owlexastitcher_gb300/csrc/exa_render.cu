@@ -17,7 +17,6 @@
 
 namespace exa {
 
-constexpr int kTrackCap = 1 << 22;  // delta / ratio tracking steps per macrocell
 
 // resident 128-thread blocks per SM the render kernel is compiled for
 // (bounds its registers: 65536 / (128 * n))
@@ -326,12 +325,15 @@ struct Walk {
   V3 pos;           // last sample position (voxel space)
   float4 xf;        // last classified sample
   float t, t1, maj, Tr;
-  int primID, steps, ncells;
+  int primID;       // the cached gridlet (>= 0), a hint -2 - id, or none (-1)
+  int steps, ncells;
   int type;
   bool needCell;
 };
 
-EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
+// `hint`: a gridlet near the walk's start for its first full query (-1:
+// none; see Walk::primID)
+EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray, int hint = -1)
 {
   ray.org = xfm_point(lp.voxelSpaceTransform, ray.org);
   ray.dir = xfm_vector(lp.voxelSpaceTransform, ray.dir);
@@ -347,8 +349,12 @@ EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
   w.Tr = 1.f;
   w.type = BOUNDARY;
   w.ncells = 0;
+  w.primID = hint;   // no cached gridlet
   w.needCell = true;
 }
+
+// the hint for a walk that starts where walk w ended: w's last gridlet
+EXA_D int walk_hint(const Walk &w) { return w.primID >= 0 ? -2 - w.primID : w.primID; }
 
 // walk_advance: the DDA advance and the free flight of one step.
 // Returns 0 when the walk ended, 1 when the step took no sample (the flight
@@ -361,16 +367,20 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
   const exa_grid_traversable &G = lp.majorantGrid;
   const float scale = lp.transferFunc.opacityScale;
   while (w.needCell) {
-    if (++w.ncells > (lp.ext.ddaCellCap > 0 ? lp.ext.ddaCellCap : G.dims.x + G.dims.y + G.dims.z + 3)) {
+    if (++w.ncells > lp.ext.ddaCellCap) {  // the host fills the caps (fillLoopCaps)
       c.err |= EXA_DEVERR_DDA_CAP;
       return WALK_END;
     }
     w.t1 = fmin_t(rmin3(w.dda.tnext), w.dda.tmax);
     const int leafID = (w.dda.cell.z * G.dims.y + w.dda.cell.y) * G.dims.x + w.dda.cell.x;
     cnt_add(c, CNT_DDA);
+    if (!exa_in_range(leafID, (long long)G.dims.x * G.dims.y * G.dims.z, c.err)) return WALK_END;
     w.maj = __ldg(lp.maxOpacities + leafID);
     w.t = w.dda.t0;
-    w.primID = -1;
+    // the reference's gridlet cache ends with the macrocell
+    // (deviceCode.cu:731-760); the gridlet stays as a hint for the next
+    // full query, encoded -2 - id
+    if (w.primID >= 0) w.primID = -2 - w.primID;
     w.steps = 0;
     if (w.maj <= 0.f) {
       if (!dda_next_dir(w.dda, w.dir, G.dims)) return WALK_END;
@@ -378,7 +388,7 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
     }
     w.needCell = false;
   }
-  if (++w.steps > (lp.ext.trackStepCap > 0 ? lp.ext.trackStepCap : kTrackCap)) {
+  if (++w.steps > lp.ext.trackStepCap) {
     c.err |= EXA_DEVERR_TRACK_CAP;
     return WALK_END;
   }
@@ -391,14 +401,30 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
   return WALK_SAMPLE;
 }
 
+// the full point location of a step whose cached gridlet (if any) missed;
+// EXA_SAMPLE_MISS_NOINLINE=1 builds it out of line
+#ifndef EXA_SAMPLE_MISS_NOINLINE
+#define EXA_SAMPLE_MISS_NOINLINE 0
+#endif
+#if EXA_SAMPLE_MISS_NOINLINE
+static __device__ __noinline__
+#else
+EXA_D
+#endif
+exa_sample sample_miss(const AccelView &A, V3 pos, bool cull, int primID, uint32_t &err, QueryStats *q)
+{
+  return primID <= -2 ? sample_field_hinted(A, pos, cull, -2 - primID, err, q) : sample_field(A, pos, cull, err, q);
+}
+
 // the exact sampler at w.pos: the cached gridlet first (testSample,
 // deviceCode.cu:749), then the full point location
 EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
 {
-  exa_sample s = test_sample(c.A, w.pos, w.primID);
+  exa_sample s =
+      test_sample(c.A, w.pos, w.primID < 0 || exa_in_range(w.primID, c.A.numGridlets, c.err) ? w.primID : -1);
   if (s.primID < 0) {
     QueryStats q{0u, 0u, 0u};
-    s = sample_field(c.A, w.pos, c.lp.ext.cullTransparentPrims != 0, c.err, &q);
+    s = sample_miss(c.A, w.pos, c.lp.ext.cullTransparentPrims != 0, w.primID, c.err, &q);
     if (c.counting) {
       cnt_add(c, CNT_MISS);
       cnt_add(c, CNT_TABLES, q.tables);
@@ -415,11 +441,12 @@ EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
 
 // the collision test of one step given its sample; primID -1 is empty
 // space, -2 a value of the learned field (never cached).  Returns false
-// when the walk ended.  `teaser`: the frame renders the Teaser shade mode
-// (a compile-time constant in every caller, so that the other frames carry
-// none of its code).
+// when the walk ended.  `teaser`: the frame renders the Teaser shade mode;
+// `learned`: the sample may come from the learned field (both compile-time
+// constants in every caller, so that the other walks carry none of their
+// code).
 EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const exa_sample &s,
-                        const bool teaser = false)
+                        const bool teaser = false, const bool learned = false)
 {
   const exa_launch_params &lp = c.lp;
   const float scale = lp.transferFunc.opacityScale;
@@ -428,7 +455,7 @@ EXA_D bool walk_collide(Walk &w, PathCtx &c, Rng &rng, const bool shadow, const 
   w.xf = classify(c.A, lp, s);
   const float sigmaT = w.xf.w;
   float sigmaS = sigmaT * scale;
-  if (s.primID == -2 && sigmaS > w.maj) {
+  if (learned && s.primID == -2 && sigmaS > w.maj) {
     // a learned density above the macrocell's widened majorant is limited
     // to it: tracking stays unbiased for the limited field
     if (c.counting) cnt_add(c, CNT_VIOL);
@@ -667,7 +694,7 @@ struct Machine {
     }
     L.lightI = lp.lights[which].intensity;
     L.shadow = true;
-    walk_begin(L.w, lp, ray);
+    walk_begin(L.w, lp, ray, walk_hint(L.w));
     L.phase = PH_TRACK;
   }
 
@@ -701,7 +728,7 @@ struct Machine {
     L.ray.tmax = t1;
     mesh_clip(L, L.ray);
     L.shadow = false;
-    walk_begin(L.w, lp, L.ray);
+    walk_begin(L.w, lp, L.ray, walk_hint(L.w));
   }
 
   EXA_D void primary_done(Lane &L)
@@ -1187,10 +1214,10 @@ EXA_D V3 heat_map(float t)
 }
 
 __global__ void k_resolve(const __grid_constant__ exa_launch_params lp, int width, int height,
-                          const float4 *__restrict__ colors)
+                          const float4 *__restrict__ colors, int pixelBegin = 0, int pixelEnd = -1)
 {
-  const int pixelID = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pixelID >= width * height) return;
+  const int pixelID = pixelBegin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (pixelID >= (pixelEnd < 0 ? width * height : pixelEnd)) return;
   const int spp = lp.render.spp;
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 *cp = colors + (size_t)pixelID * spp;
@@ -1333,7 +1360,8 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
 
 // shadow flag, RNG and the walk
 // A walk that has not taken a step yet (walk_begin's state) is stored
-// "fresh": flags, RNG, ray and DDA state (the first 21 of the 35 words); the
+// "fresh": flags, RNG, gridlet hint, ray and DDA state (the first 21 of the
+// 35 words); the
 // loader sets the rest to walk_begin's values.  (Storing only the ray and
 // re-running dda_init in the walk kernel saves more traffic but costs the
 // latency-bound walk kernel more than it saves.)
@@ -1344,14 +1372,14 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, b
   unsigned k = kPathStride;
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2) | (fresh ? kWalkFresh : 0u));
-  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 3: unused
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); W((uint32_t)w.primID);
   WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
   W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
   if (fresh) return;
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z); WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
   WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
-  W((uint32_t)w.primID); W((uint32_t)w.steps); W((uint32_t)w.ncells);
+  ++k; W((uint32_t)w.steps); W((uint32_t)w.ncells);  // word 32: unused
 }
 
 EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i,
@@ -1365,7 +1393,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.type = (int)((flags & ~kWalkFresh) >> 2);
   const uint32_t lo = R(), hi = R();
   L.rng.state = ((uint64_t)hi << 32) | lo;
-  ++k;
+  w.primID = (int)R();
   w.org.x = RF(); w.org.y = RF(); w.org.z = RF(); w.dir.x = RF(); w.dir.y = RF(); w.dir.z = RF();
   w.dda.tnext.x = RF(); w.dda.tnext.y = RF(); w.dda.tnext.z = RF();
   w.dda.dist.x = RF(); w.dda.dist.y = RF(); w.dda.dist.z = RF();
@@ -1380,7 +1408,6 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
     w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
     w.t = w.t1 = w.maj = 0.f;
     w.Tr = 1.f;
-    w.primID = -1;
     w.steps = 0;
     w.ncells = 0;
     return;
@@ -1388,7 +1415,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
   w.t = RF(); w.t1 = RF(); w.maj = RF(); w.Tr = RF();
-  w.primID = (int)R(); w.steps = (int)R(); w.ncells = (int)R();
+  ++k; w.steps = (int)R(); w.ncells = (int)R();
 }
 
 // event record of a walk that ended: the fields the integrator step reads,
@@ -1408,7 +1435,7 @@ EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, 
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.type << 2) | ((uint32_t)w.ncells << 8));
   W(src);
-  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 4: unused
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); W((uint32_t)w.primID);
   WF(w.t); WF(w.Tr);
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z);
   WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
@@ -1428,7 +1455,7 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
   const unsigned src = R();
   const uint32_t lo = R(), hi = R();
   L.rng.state = ((uint64_t)hi << 32) | lo;
-  ++k;
+  w.primID = (int)R();
   w.t = RF(); w.Tr = RF();
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
@@ -1654,7 +1681,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
         s.value = S.vmin + y * S.vrange;
         cnt_add(c, CNT_SURR);
         pending = false;
-        ended = !walk_collide(L.w, c, L.rng, L.shadow, s);
+        ended = !walk_collide(L.w, c, L.rng, L.shadow, s, false, true);
       }
     }
     ended = active && ended;
@@ -1704,13 +1731,17 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   int dev = 0, sms = 152;
   cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
   cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-  const unsigned long long total = (unsigned long long)((width + 15) / 16) * ((height + 7) / 8) * 128ull * lp.render.spp;
+  // the jobs of the frame (16 x 8-pixel tiles, row-major, spp each), or of
+  // its band of rows [rowBegin, rowEnd): the band's tile rows
+  const int rowBegin = lp.ext.rowEnd > 0 ? lp.ext.rowBegin : 0, rowEnd = lp.ext.rowEnd > 0 ? lp.ext.rowEnd : height;
+  const unsigned long long jobsPerTileRow = (unsigned long long)((width + 15) / 16) * 128ull * lp.render.spp;
+  const unsigned long long total = jobsPerTileRow * (unsigned long long)((rowEnd + 7) / 8);
   // path parts are read as 16-byte vectors: every queue must start 16-byte
   // aligned (capacities are multiples of the 128-job tile)
   if (cap % 4 != 0) throw Error(EXA_ERR_INVALID, "queue capacity must be a multiple of 4");
   const size_t words = (size_t)kLaneWords * cap;
   uint32_t *buf[3] = {bufs, bufs + words, bufs + 2 * words};
-  unsigned long long issued = 0;
+  unsigned long long issued = jobsPerTileRow * (unsigned long long)(rowBegin / 8);
   unsigned nIn = 0;
   int inIdx = 0, outIdx = 1;
   const unsigned grid = (unsigned)sms * 16;
@@ -1782,7 +1813,8 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     cudaCheck(cudaMemcpyAsync(counters, next, sizeof(next), cudaMemcpyHostToDevice, s), "swap queues");
     std::swap(inIdx, outIdx);
   }
-  k_resolve<<<(unsigned)(((long long)width * height + 255) / 256), 256, 0, s>>>(lp, width, height, colors);
+  const int pb = rowBegin * width, pe = rowEnd * width;
+  k_resolve<<<(unsigned)(((long long)(pe - pb) + 255) / 256), 256, 0, s>>>(lp, width, height, colors, pb, pe);
   cudaCheck(cudaGetLastError(), "k_resolve");
 }
 

@@ -29,6 +29,7 @@
 
 #include "exa_host.h"
 #include "exa_surrogate.cuh"
+#include "exa_tcgen05.cuh"
 
 namespace exa {
 
@@ -372,6 +373,271 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_sur_mlp_train(
   if (threadIdx.x == 0) atomicAdd(lossOut, S.loss);
 }
 
+// ------------------------------------------------ MLP training, tcgen05
+// The same forward and backward on the 5th-generation tensor cores: one
+// block of 128 threads per SM takes 128-pair tiles in turn; every product is
+// a tcgen05.mma of M = 128 rows with BF16 operands in shared memory
+// (K-major tiles, exa_tcgen05.cuh) and an FP32 accumulator in tensor memory,
+// issued by one thread and completed on an mbarrier; thread r owns pair r
+// of the tile (tensor-memory lane r) for the element-wise steps:
+//   layer 1  D1 = x W1^T            (K 32)  -> h1 = bf16(relu(D1))
+//   layer 2  D2 = h1 W2^T           (K 64)  -> h2, y, g, gw3, d2
+//   d1       D1 = d2 W2             (K 64)  -> d1 = bf16(D1) where h1 > 0
+//   din      D2 = d1 W1             (K 64)  -> din (FP32) to global
+//   weights  GW += [d2^T; d1^T] [h1 | x]   (K = the tile's 128 pairs): rows
+//            0..63 x columns 0..63 are gw2, rows 64..127 x columns 64..95
+//            gw1 (the two other blocks are not read); GW accumulates over
+//            the block's tiles and is added to gw once.
+// Operands and tensor-memory columns are reused step by step; every step
+// starts after the previous one's commit.  Waits are bounded: a wait that
+// gives up sets EXA_DEVERR_WATCHDOG in *errors and the block stops.
+struct alignas(1024) TcTrainSmem {
+  __nv_bfloat16 w1[kSurHidden * kSurIn];        // B of layer 1: (j, k), K 32
+  __nv_bfloat16 w2[kSurHidden * kSurHidden];    // B of layer 2: (j, i), K 64
+  __nv_bfloat16 w2t[kSurHidden * kSurHidden];   // B of d1: (i, j), K 64
+  __nv_bfloat16 w1t[kSurIn * kSurHidden];       // B of din: (k, j), K 64
+  __nv_bfloat16 x[128 * kSurIn];                // A of layer 1: (r, k)
+  __nv_bfloat16 h1[128 * kSurHidden];           // A of layer 2: (r, i); then A of din: d1 (r, j)
+  __nv_bfloat16 d2[128 * kSurHidden];           // A of d1: (r, j)
+  __nv_bfloat16 aw[128 * 128];                  // A of the weight product: d2^T, d1^T; K = pair
+  __nv_bfloat16 bw[96 * 128];                   // B of the weight product: h1^T, x^T; K = pair
+  float w3[kSurHidden];
+  float gw3[kSurHidden];
+  float loss;
+  uint32_t tmem;
+  uint32_t stop;
+  uint64_t bar;
+};
+constexpr uint32_t kTcCols = 256;    // tensor-memory columns per block
+constexpr uint32_t kColD1 = 0, kColD2 = 64, kColGW = 128;
+
+__global__ void __launch_bounds__(128, 1) k_sur_mlp_train_tc(
+    const __nv_bfloat16 *__restrict__ w1g, const __nv_bfloat16 *__restrict__ w2g, const __nv_bfloat16 *__restrict__ w3g,
+    const __nv_bfloat16 *__restrict__ feats, const float4 *__restrict__ samples, size_t first, size_t numSamples, int B,
+    float vmin, float invRange, float invB, float *gw, float *lossOut, float *dfeat, uint32_t *errors)
+{
+  extern __shared__ __align__(1024) unsigned char tcSmRaw[];
+  TcTrainSmem &S = *reinterpret_cast<TcTrainSmem *>(tcSmRaw);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < kSurHidden * kSurIn; i += blockDim.x) {
+    const int j = i / kSurIn, k = i % kSurIn;
+    S.w1[tc::kmajor(j, k, kSurIn)] = w1g[i];
+    S.w1t[tc::kmajor(k, j, kSurHidden)] = w1g[i];
+  }
+  for (int i = tid; i < kSurHidden * kSurHidden; i += blockDim.x) {
+    const int j = i / kSurHidden, k = i % kSurHidden;
+    S.w2[tc::kmajor(j, k, kSurHidden)] = w2g[i];
+    S.w2t[tc::kmajor(k, j, kSurHidden)] = w2g[i];
+  }
+  if (tid < kSurHidden) {
+    S.w3[tid] = __bfloat162float(w3g[tid]);
+    S.gw3[tid] = 0.f;
+  }
+  if (tid == 0) {
+    S.loss = 0.f;
+    S.stop = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::smem_addr(&S.bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tc::tmem_alloc(&S.tmem, kTcCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lane quarter
+  uint32_t phase = 0;
+  // operands written by the threads -> visible to the tensor core, then one
+  // thread issues
+  auto sync_operands = [&]() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  };
+  // every thread waits for the committed products (bounded)
+  auto wait_products = [&]() -> bool {
+    bool done = false;
+    for (int i = 0; i < (1 << 24) && !done; ++i) done = tc::mbar_try_wait(&S.bar, phase);
+    phase ^= 1u;
+    if (!done) atomicOr(&S.stop, 1u);
+    __syncthreads();
+    tc::fence_after_sync();
+    return S.stop == 0;
+  };
+  float gw3acc[kSurHidden];
+#pragma unroll
+  for (int j = 0; j < kSurHidden; ++j) gw3acc[j] = 0.f;
+  float lossAcc = 0.f;
+  const int tiles = (B + 127) / 128;
+  bool any = false;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int r = tile * 128 + tid;
+    const bool inB = r < B;
+    // inputs (x and x^T) and the target
+    uint4 q[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+    float target = 0.f;
+    bool valid = false;
+    if (inB) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(feats + (size_t)r * kSurIn);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) q[c] = src[c];
+      const float v = samples[(first + (size_t)r) % numSamples].w;
+      valid = v == v;
+      target = valid ? (v - vmin) * invRange : 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4 *>(S.x + tc::kmajor(tid, 8 * c, kSurIn)) = q[c];
+    {
+      const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(q);
+#pragma unroll
+      for (int k = 0; k < kSurIn; ++k) S.bw[tc::kmajor(64 + k, tid, 128)] = e[k];
+    }
+    sync_operands();
+    // layer 1
+    if (tid == 0) {
+      for (int kk = 0; kk < kSurIn / 16; ++kk)
+        tc::mma_bf16(tmem + kColD1, tc::desc_kslice(S.x, kSurIn, kk), tc::desc_kslice(S.w1, kSurIn, kk),
+                     tc::idesc_bf16_f32(128, kSurHidden), kk > 0);
+      tc::commit(&S.bar);
+    }
+    if (!wait_products()) break;
+    for (int c = 0; c < kSurHidden / 16; ++c) {
+      float v[16];
+      tc::ld16(lanes + kColD1 + 16 * c, v);
+      __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) h[j] = __float2bfloat16_rn(fmaxf(v[j], 0.f));
+      *reinterpret_cast<uint4 *>(S.h1 + tc::kmajor(tid, 16 * c, kSurHidden)) = *reinterpret_cast<const uint4 *>(h);
+      *reinterpret_cast<uint4 *>(S.h1 + tc::kmajor(tid, 16 * c + 8, kSurHidden)) =
+          *reinterpret_cast<const uint4 *>(h + 8);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) S.bw[tc::kmajor(16 * c + j, tid, 128)] = h[j];
+    }
+    sync_operands();
+    // layer 2
+    if (tid == 0) {
+      for (int kk = 0; kk < kSurHidden / 16; ++kk)
+        tc::mma_bf16(tmem + kColD2, tc::desc_kslice(S.h1, kSurHidden, kk), tc::desc_kslice(S.w2, kSurHidden, kk),
+                     tc::idesc_bf16_f32(128, kSurHidden), kk > 0);
+      tc::commit(&S.bar);
+    }
+    if (!wait_products()) break;
+    // output, loss and its gradient (pair tid)
+    float y = 0.f;
+    for (int c = 0; c < kSurHidden / 16; ++c) {
+      float v[16];
+      tc::ld16(lanes + kColD2 + 16 * c, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) y += bf16_round(fmaxf(v[j], 0.f)) * S.w3[16 * c + j];
+    }
+    const float diff = y - target;
+    const float gr = (inB && valid) ? 2.f * diff * invB : 0.f;
+    if (inB && valid) lossAcc += diff * diff;
+    // gw3 and d2 = bf16(g w3) where h2 > 0
+#pragma unroll
+    for (int c = 0; c < kSurHidden / 16; ++c) {
+      float v[16];
+      tc::ld16(lanes + kColD2 + 16 * c, v);
+      __align__(16) __nv_bfloat16 d[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const float h2 = bf16_round(fmaxf(v[j], 0.f));
+        gw3acc[16 * c + j] += gr * h2;
+        d[j] = __float2bfloat16_rn(h2 > 0.f ? gr * S.w3[16 * c + j] : 0.f);
+      }
+      *reinterpret_cast<uint4 *>(S.d2 + tc::kmajor(tid, 16 * c, kSurHidden)) = *reinterpret_cast<const uint4 *>(d);
+      *reinterpret_cast<uint4 *>(S.d2 + tc::kmajor(tid, 16 * c + 8, kSurHidden)) =
+          *reinterpret_cast<const uint4 *>(d + 8);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) S.aw[tc::kmajor(16 * c + j, tid, 128)] = d[j];
+    }
+    sync_operands();
+    // d1 = d2 W2
+    if (tid == 0) {
+      for (int kk = 0; kk < kSurHidden / 16; ++kk)
+        tc::mma_bf16(tmem + kColD1, tc::desc_kslice(S.d2, kSurHidden, kk), tc::desc_kslice(S.w2t, kSurHidden, kk),
+                     tc::idesc_bf16_f32(128, kSurHidden), kk > 0);
+      tc::commit(&S.bar);
+    }
+    if (!wait_products()) break;
+    for (int c = 0; c < kSurHidden / 16; ++c) {
+      float v[16];
+      tc::ld16(lanes + kColD1 + 16 * c, v);
+      __align__(16) __nv_bfloat16 h[16], d[16];
+      *reinterpret_cast<uint4 *>(h) = *reinterpret_cast<const uint4 *>(S.h1 + tc::kmajor(tid, 16 * c, kSurHidden));
+      *reinterpret_cast<uint4 *>(h + 8) =
+          *reinterpret_cast<const uint4 *>(S.h1 + tc::kmajor(tid, 16 * c + 8, kSurHidden));
+#pragma unroll
+      for (int j = 0; j < 16; ++j) d[j] = __float2bfloat16_rn(__bfloat162float(h[j]) > 0.f ? v[j] : 0.f);
+      *reinterpret_cast<uint4 *>(S.h1 + tc::kmajor(tid, 16 * c, kSurHidden)) = *reinterpret_cast<const uint4 *>(d);
+      *reinterpret_cast<uint4 *>(S.h1 + tc::kmajor(tid, 16 * c + 8, kSurHidden)) =
+          *reinterpret_cast<const uint4 *>(d + 8);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) S.aw[tc::kmajor(64 + 16 * c + j, tid, 128)] = d[j];
+    }
+    sync_operands();
+    // din = d1 W1 and the weight product
+    if (tid == 0) {
+      for (int kk = 0; kk < kSurHidden / 16; ++kk)
+        tc::mma_bf16(tmem + kColD2, tc::desc_kslice(S.h1, kSurHidden, kk), tc::desc_kslice(S.w1t, kSurHidden, kk),
+                     tc::idesc_bf16_f32(128, kSurIn), kk > 0);
+      for (int kk = 0; kk < 128 / 16; ++kk)
+        tc::mma_bf16(tmem + kColGW, tc::desc_kslice(S.aw, 128, kk), tc::desc_kslice(S.bw, 128, kk),
+                     tc::idesc_bf16_f32(128, 96), any || kk > 0);
+      tc::commit(&S.bar);
+    }
+    any = true;
+    if (!wait_products()) break;
+    if (inB) {
+      float4 *dst = reinterpret_cast<float4 *>(dfeat + (size_t)r * kSurIn);
+      for (int c = 0; c < kSurIn / 16; ++c) {
+        float v[16];
+        tc::ld16(lanes + kColD2 + 16 * c, v);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) dst[4 * c + k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  }
+  if (S.stop && errors && tid == 0) atomicOr(errors, EXA_DEVERR_WATCHDOG);
+  // weight gradients: gw2 (rows 0..63, columns 0..63), gw1 (rows 64..127,
+  // columns 64..95) of the accumulator
+  if (any && !S.stop) {
+    if (tid < kSurHidden) {
+      for (int c = 0; c < kSurHidden / 16; ++c) {
+        float v[16];
+        tc::ld16(lanes + kColGW + 16 * c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (v[j] != 0.f) atomicAdd(gw + kSurHidden * kSurIn + tid * kSurHidden + 16 * c + j, v[j]);
+      }
+    } else {
+      for (int c = 0; c < kSurIn / 16; ++c) {
+        float v[16];
+        tc::ld16(lanes + kColGW + 64 + 16 * c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (v[j] != 0.f) atomicAdd(gw + (tid - kSurHidden) * kSurIn + 16 * c + j, v[j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kSurHidden; ++j) atomicAdd(&S.gw3[j], gw3acc[j]);
+  for (int o = 16; o > 0; o >>= 1) lossAcc += __shfl_xor_sync(0xffffffffu, lossAcc, o);
+  if ((tid & 31) == 0) atomicAdd(&S.loss, lossAcc);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < kSurHidden && S.gw3[tid] != 0.f)
+    atomicAdd(gw + kSurHidden * kSurIn + kSurHidden * kSurHidden + tid, S.gw3[tid]);
+  if (tid == 0) atomicAdd(lossOut, S.loss);
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kTcCols);
+  }
+}
+
 // --------------------------------------------------------------------- Adam
 // p -= lr * mhat / (sqrt(vhat) + eps); the gradient is cleared.  n2 pairs.
 __global__ void k_sur_adam_table(float2 *p, float2 *gr, float2 *m, float2 *v, size_t n, float lr, float b1, float b2,
@@ -632,6 +898,37 @@ void Surrogate::generateSamples(const ExaStitchSampler &sampler, cudaStream_t s)
   cudaCheck(cudaStreamSynchronize(s), "surrogate samples");
 }
 
+// the MLP training step of B pairs: the tcgen05 kernel (one block per SM),
+// or with EXA_SUR_TRAIN_TC=0 the mma.sync kernel
+#ifndef EXA_SUR_TRAIN_TC
+#define EXA_SUR_TRAIN_TC 0
+#endif
+static void launchMlpTrain(const SurrogateView &v, const __nv_bfloat16 *feats, const float4 *samples, size_t first,
+                           size_t numSamples, int B, float vmin, float invRange, float invB, float *gw, float *loss,
+                           float *dfeat, uint32_t *errors, cudaStream_t s)
+{
+  int dev = 0, sms = 152;
+  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (EXA_SUR_TRAIN_TC) {
+    cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(TcTrainSmem)),
+              "train smem");
+    const unsigned blocks = (unsigned)std::min<int>((B + 127) / 128, sms);
+    k_sur_mlp_train_tc<<<blocks, 128, sizeof(TcTrainSmem), s>>>(v.w1, v.w2, v.w3, feats, samples, first, numSamples,
+                                                                B, vmin, invRange, invB, gw, loss, dfeat, errors);
+  } else {
+    cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kTrainSmemBytes),
+              "train smem");
+    const unsigned blocks = (unsigned)std::min<int>((B / 32 + kTrainWarps - 1) / kTrainWarps + 1, sms * 2);
+    k_sur_mlp_train<<<blocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(v.w1, v.w2, v.w3, feats, samples, first,
+                                                                      numSamples, B, vmin, invRange, invB, gw, loss,
+                                                                      dfeat);
+  }
+  cudaCheck(cudaGetLastError(), "MLP training step");
+}
+
 float Surrogate::trainSteps(int steps, cudaStream_t s)
 {
   if (!samples.ptr) throw Error(EXA_ERR_INVALID, "no training samples");
@@ -639,14 +936,10 @@ float Surrogate::trainSteps(int steps, cudaStream_t s)
   if (feats.count < (size_t)B * kSurIn) feats.alloc((size_t)B * kSurIn);
   if (dfeat.count < (size_t)B * kSurIn) dfeat.alloc((size_t)B * kSurIn);
   if (!lossBuf.ptr) lossBuf.alloc(2);
-  cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmemBytes),
-            "train smem");
-  int dev = 0, sms = 152;
-  cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
-  cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   const size_t nTab = (size_t)kSurLevels << cfg.log2T;
   const SurrogateView v = deviceView();
-  const unsigned mlpBlocks = (unsigned)std::min<int>((B / 32 + kTrainWarps - 1) / kTrainWarps, sms * 2);
+  if (!trainErrors.ptr) trainErrors.alloc(1);
+  cudaCheck(cudaMemsetAsync(trainErrors.ptr, 0, sizeof(uint32_t), s), "memset train errors");
   cudaCheck(cudaMemsetAsync(lossBuf.ptr, 0, 2 * sizeof(float), s), "memset loss");
   for (int it = 0; it < steps; ++it) {
     const size_t first = (size_t)(cursor % cfg.numSamples);
@@ -654,9 +947,8 @@ float Surrogate::trainSteps(int steps, cudaStream_t s)
     k_sur_encode_fwd<<<gridFor(B, 128), 128, 0, s>>>(v, table.ptr, samples.ptr, first, cfg.numSamples, B, feats.ptr);
     float *lossSlot = lossBuf.ptr + (it == steps - 1 ? 1 : 0);
     if (it == steps - 1) cudaCheck(cudaMemsetAsync(lossSlot, 0, sizeof(float), s), "memset loss");
-    k_sur_mlp_train<<<mlpBlocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(
-        v.w1, v.w2, v.w3, feats.ptr, samples.ptr, first, cfg.numSamples, B, view.vmin, 1.f / view.vrange,
-        1.f / (float)B, gw.ptr, lossSlot, dfeat.ptr);
+    launchMlpTrain(v, feats.ptr, samples.ptr, first, cfg.numSamples, B, view.vmin, 1.f / view.vrange, 1.f / (float)B,
+                   gw.ptr, lossSlot, dfeat.ptr, trainErrors.ptr, s);
     k_sur_encode_bwd<<<gridFor(B, 128), 128, 0, s>>>(v, samples.ptr, first, cfg.numSamples, B, dfeat.ptr, gtable.ptr);
     step++;
     const float b1 = 0.9f, b2 = 0.99f;
@@ -673,8 +965,11 @@ float Surrogate::trainSteps(int steps, cudaStream_t s)
     cudaCheck(cudaGetLastError(), "surrogate training step");
   }
   float h[2] = {0.f, 0.f};
+  uint32_t terr = 0;
   cudaCheck(cudaMemcpyAsync(h, lossBuf.ptr, sizeof(h), cudaMemcpyDeviceToHost, s), "loss");
+  cudaCheck(cudaMemcpyAsync(&terr, trainErrors.ptr, sizeof(terr), cudaMemcpyDeviceToHost, s), "train errors");
   cudaCheck(cudaStreamSynchronize(s), "surrogate training");
+  if (terr) throw Error(EXA_ERR_CUDA, "surrogate training: a tensor-core product did not complete");
   // mean squared error (normalised units) of the last step's batch
   lastLoss = h[1] / (float)B;
   return lastLoss;
@@ -699,21 +994,23 @@ void Surrogate::gradients(const float4 *hostSamples, int n, float *gW, float *gT
   DBuf<float2> gt;
   gt.alloc(nTab);
   cudaCheck(cudaMemsetAsync(gt.ptr, 0, gt.bytes(), s), "memset");
-  cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmemBytes),
-            "train smem");
   const SurrogateView v = deviceView();
   k_sur_encode_fwd<<<gridFor(n, 128), 128, 0, s>>>(v, table.ptr, sm.ptr, 0, (size_t)n, n, f.ptr);
-  const unsigned blocks = (unsigned)(((n + 31) / 32 + kTrainWarps - 1) / kTrainWarps);
-  k_sur_mlp_train<<<blocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(v.w1, v.w2, v.w3, f.ptr, sm.ptr, 0, (size_t)n, n,
-                                                                    view.vmin, 1.f / view.vrange, 1.f / (float)n,
-                                                                    gwl.ptr, lossl.ptr, df.ptr);
+  DBuf<uint32_t> terrBuf;
+  terrBuf.alloc(1);
+  cudaCheck(cudaMemsetAsync(terrBuf.ptr, 0, sizeof(uint32_t), s), "memset train errors");
+  launchMlpTrain(v, f.ptr, sm.ptr, 0, (size_t)n, n, view.vmin, 1.f / view.vrange, 1.f / (float)n, gwl.ptr, lossl.ptr,
+                 df.ptr, terrBuf.ptr, s);
   k_sur_encode_bwd<<<gridFor(n, 128), 128, 0, s>>>(v, sm.ptr, 0, (size_t)n, n, df.ptr, gt.ptr);
   cudaCheck(cudaGetLastError(), "surrogate gradients");
   if (gW) cudaCheck(cudaMemcpyAsync(gW, gwl.ptr, kSurParams * sizeof(float), cudaMemcpyDeviceToHost, s), "d2h");
   if (gTable) cudaCheck(cudaMemcpyAsync(gTable, gt.ptr, gt.bytes(), cudaMemcpyDeviceToHost, s), "d2h");
   float l = 0.f;
+  uint32_t terr = 0;
   cudaCheck(cudaMemcpyAsync(&l, lossl.ptr, sizeof(float), cudaMemcpyDeviceToHost, s), "d2h");
+  cudaCheck(cudaMemcpyAsync(&terr, terrBuf.ptr, sizeof(terr), cudaMemcpyDeviceToHost, s), "d2h");
   cudaCheck(cudaStreamSynchronize(s), "surrogate gradients");
+  if (terr) throw Error(EXA_ERR_CUDA, "surrogate gradients: a tensor-core product did not complete");
   if (loss) *loss = l / (float)n;
 }
 

@@ -164,7 +164,10 @@ class LPExt(C.Structure):
         ("tfFilter", C.c_int32),
         ("trackStepCap", C.c_int32),
         ("ddaCellCap", C.c_int32),
+        ("rowBegin", C.c_int32),
+        ("rowEnd", C.c_int32),
         ("pad0", C.c_int32),
+        ("pad1", C.c_int32),
     ]
 
 
@@ -281,11 +284,14 @@ _lib = None
 
 
 def lib():
-    """Loads libexastitch.so and checks the struct layouts against it."""
+    """Loads libexastitch.so (libexastitch_checks.so, the bounds-checked
+    build, where EXA_LIBRARY_VARIANT=checks) and checks the struct layouts
+    against it."""
     global _lib
     if _lib is not None:
         return _lib
-    L = C.CDLL(_native.lib_path("libexastitch.so"))
+    variant = os.environ.get("EXA_LIBRARY_VARIANT", "")
+    L = C.CDLL(_native.lib_path("libexastitch_%s.so" % variant if variant else "libexastitch.so"))
     vp, i32, u64 = C.c_void_p, C.c_int32, C.c_uint64
     ctx_p = C.c_void_p
     sig = {

@@ -403,3 +403,43 @@ def test_render_features_bit_exact(scenes, torch_cuda, feature, integrator):
     assert acc.tobytes() == hacc.tobytes()
     assert tT.tobytes() == htT.tobytes()
     assert len(np.unique(fb)) > 4
+
+
+@pytest.mark.parametrize("integrator", [0, 1])
+def test_row_bands_equal_whole_frame(scenes, torch_cuda, integrator):
+    """exa_lp_ext.rowBegin / rowEnd (a frame split across GPUs): each band's
+    pixels equal the whole frame's bit for bit, the other rows untouched;
+    bands are rejected where they are not supported."""
+    torch = torch_cuda
+    ds, g, o = scenes
+    from owlexastitcher_gb300 import exastitch as E
+    w, h = 40, 30
+    lp = setup_render(g.lp, orbit_camera(g.lo, g.hi, w, h), w, h, integrator, 2, "point", integrator == 0, g.lo, g.hi)
+    lp.ext.traceT = lp.ext.traceTr = None
+    lp.accumID = 0
+
+    def render(rows):
+        fb = torch.full((w * h,), 7, dtype=torch.int32, device="cuda")
+        acc = torch.full((w * h * 4,), -1.0, dtype=torch.float32, device="cuda")
+        lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+        lp.ext.rowBegin, lp.ext.rowEnd = rows
+        try:
+            E._check(E.lib().exa_render(g.ctx.h, E.C.byref(lp), w, h))
+            g.ctx.sync()
+        finally:
+            lp.ext.rowBegin = lp.ext.rowEnd = 0
+        return fb.cpu().numpy(), acc.cpu().numpy().reshape(-1, 4)
+
+    fb, acc = render((0, 0))
+    for b, e in ((0, 8), (8, 24), (24, 30)):
+        bfb, bacc = render((b, e))
+        assert np.array_equal(bfb[b * w:e * w], fb[b * w:e * w])
+        assert bacc[b * w:e * w].tobytes() == acc[b * w:e * w].tobytes()
+        assert np.all(bfb[:b * w] == 7) and np.all(bfb[e * w:] == 7)
+        assert np.all(bacc[:b * w] == -1.0) and np.all(bacc[e * w:] == -1.0)
+    for bad in ((4, 16), (8, 8), (0, 31), (16, 20)):
+        lp.ext.rowBegin, lp.ext.rowEnd = bad
+        try:
+            assert E.lib().exa_render(g.ctx.h, E.C.byref(lp), w, h) == E.EXA_ERR_INVALID, bad
+        finally:
+            lp.ext.rowBegin = lp.ext.rowEnd = 0
