@@ -731,6 +731,27 @@ class Renderer:
         fn = lib().exa_render_surrogate if self.learned else lib().exa_render
         _check(fn(self.ctx.h, C.byref(self.lp), w, h))
 
+    def checkpoint(self, path):
+        """Saves the progressive render's state: the accumulation buffer (the
+        running per-pixel sums of deviceCode.cu:1329-1332), the next frame's
+        accumID and the frame size and spp.  Every sample's random numbers
+        follow from (pixel, accumID, frameID, sample), so a renderer restored
+        from it continues with exactly the frames an uninterrupted one
+        renders."""
+        w, h = self.fbSize
+        np.savez(path, accum=self.accum.cpu().numpy(), accumID=np.int64(self.accumID), width=np.int64(w),
+                 height=np.int64(h), spp=np.int64(self.spp), frameID=np.int64(self.lp.ext.frameID))
+
+    def restore(self, path):
+        """Continues a progressive render saved by checkpoint() (same model,
+        camera and transfer function)."""
+        with np.load(path) as z:
+            self.resize(int(z["width"]), int(z["height"]))
+            self.spp = int(z["spp"])
+            self.lp.ext.frameID = int(z["frameID"])
+            self.accum.copy_(self.torch.from_numpy(z["accum"]).to(self.accum.device))
+            self.accumID = int(z["accumID"])
+
 
 class Surrogate:
     """The learned field of a context: hash-grid encoding + MLP trained on

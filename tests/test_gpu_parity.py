@@ -443,3 +443,46 @@ def test_row_bands_equal_whole_frame(scenes, torch_cuda, integrator):
             assert E.lib().exa_render(g.ctx.h, E.C.byref(lp), w, h) == E.EXA_ERR_INVALID, bad
         finally:
             lp.ext.rowBegin = lp.ext.rowEnd = 0
+
+
+def test_progressive_checkpoint_resume(scenes, torch_cuda, tmp_path):
+    """Renderer.checkpoint / restore: a progressive render saved after two
+    frames and continued in a new context equals four frames in one go, bit
+    for bit (the accumulation buffer and accumID are its whole state)."""
+    torch = torch_cuda
+    ds, g, o = scenes
+    from owlexastitcher_gb300 import exastitch as E
+    w, h = 32, 24
+
+    def renderer():
+        ctx = E.Context(0)
+        r = E.Renderer(ctx, E.ExaStitchModel.from_dataset(ctx, ds), g.num_mcs)
+        r.setColorMap(g.tf)
+        r.resize(w, h)
+        r.spp = 2
+        lo, hi = r.model.cellBounds
+        setup_render(r.lp, orbit_camera(lo, hi, w, h), w, h, E.PATH_TRACING_INTEGRATOR, 2, "directional", True)
+        r.lp.ext.traceT = r.lp.ext.traceTr = None
+        return ctx, r
+
+    ctx, full = renderer()
+    for _ in range(4):
+        full.render()
+    ctx.sync()
+    want_acc, want_fb = full.accum.cpu().numpy(), full.fb.cpu().numpy()
+    ctx.close()
+    ctx, part = renderer()
+    for _ in range(2):
+        part.render()
+    ctx.sync()
+    part.checkpoint(tmp_path / "progress.npz")
+    ctx.close()
+    ctx, resumed = renderer()
+    resumed.restore(tmp_path / "progress.npz")
+    assert resumed.accumID == 2
+    for _ in range(2):
+        resumed.render()
+    ctx.sync()
+    assert resumed.accum.cpu().numpy().tobytes() == want_acc.tobytes()
+    assert np.array_equal(resumed.fb.cpu().numpy(), want_fb)
+    ctx.close()

@@ -198,3 +198,34 @@ def test_f64_path_tracer_agrees_with_f32(oracle):
     assert np.sqrt(np.mean((a - ref) ** 2)) < 1.5 * noise
     assert abs(a.mean() - ref.mean()) < 0.01 * ref.mean()
     assert ref.mean() > 0.1
+
+
+def test_progressive_render_resumes_bit_exact(oracle, tmp_path):
+    """The accumulation buffer and the next accumID are the whole state of a
+    progressive render (deviceCode.cu:1329-1332): frames 0..3 in one go equal
+    frames 0..1, a save of the buffer to a file, and frames 2..3 from the
+    loaded copy, bit for bit."""
+    from conftest import dataset
+    from helpers import OracleScene, host_lp, oracle_only_lp, ramp_tf
+    ds = dataset("tiny")
+    f = oracle.Field(ds.vertices, ds.indices, ds.gridlets, ds.gridlet_scalars)
+    lo, hi, vr = f.bounds()
+    tf = ramp_tf()
+    xf = (np.float32(vr[0]), np.float32(vr[1]))
+    o = OracleScene(oracle, ds, (8, 8, 8), lo, hi, tf, xf)
+    w, h = 16, 12
+
+    def frames(acc, ids):
+        lp = oracle_only_lp(lo, hi, (8, 8, 8), tf, xf, w, h, 0, 2)
+        for a in ids:
+            lp.accumID = a
+            hl, fb, _, _, _ = host_lp(lp, o, w, h, accum=acc)
+            assert o.f.render(bytes(hl), w, h) == 0
+        return acc, fb
+
+    full, fb_full = frames(np.zeros((w * h, 4), np.float32), range(4))
+    part, _ = frames(np.zeros((w * h, 4), np.float32), range(2))
+    np.save(tmp_path / "accum.npy", part)
+    resumed, fb_res = frames(np.load(tmp_path / "accum.npy"), range(2, 4))
+    assert resumed.tobytes() == full.tobytes() and np.array_equal(fb_res, fb_full)
+    assert len(np.unique(fb_full)) > 4
