@@ -456,44 +456,6 @@ EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &e
   return sample_elements(A, pos, cull, err, qs);
 }
 
-// sample_field for a point whose walk last sampled gridlet `hint` (in an
-// earlier macrocell, so the reference's cache does not apply).  Where the
-// point's block of the (single) gridlet table is not on a block face and
-// lists the hint alone, the full query tests the hint and, where it misses,
-// the elements; the hint's header and max opacity then load beside the
-// table entry instead of after it.  Same answer as sample_field in every
-// case.
-EXA_D exa_sample sample_field_hinted(const AccelView &A, V3 pos, bool cull, int hint, uint32_t &err,
-                                     QueryStats *qs = nullptr)
-{
-  if (A.numTables == 1 && !A.amr && !A.bricks && exa_in_range(hint, A.numGridlets, err)) {
-    const GridletTable &T = A.tables[0];
-    int b0[3], nb[3];
-    if (table_block(T, pos, b0, nb) && nb[0] == 1 && nb[1] == 1 && nb[2] == 1) {
-      const int e = table_entry(T, b0[0], b0[1], b0[2]);
-      const int4 h0 = __ldg(reinterpret_cast<const int4 *>(A.gridlets + hint));
-      const int4 h1 = __ldg(reinterpret_cast<const int4 *>(A.gridlets + hint) + 1);
-      const bool visible = !(cull && A.gridletMaxOps) || __ldg(A.gridletMaxOps + hint) != 0.f;
-      if (e == hint) {
-        if (qs) qs->tables++;
-        exa_sample s;
-        s.primID = -1;
-        s.cellID = -1;
-        s.value = 0.f;
-        if (visible) {
-          if (qs) qs->gridletTests++;
-          if (intersect_gridlet_hdr(s.value, s.cellID, pos, h0, h1, A.scalars)) {
-            s.primID = hint;
-            return s;
-          }
-        }
-        return sample_elements(A, pos, cull, err, qs);
-      }
-    }
-  }
-  return sample_field(A, pos, cull, err, qs);
-}
-
 // testSample (sampler/ExaStitchSampler.h:108-126): the cached gridlet only
 EXA_D exa_sample test_sample(const AccelView &A, V3 pos, int primID)
 {

@@ -325,15 +325,13 @@ struct Walk {
   V3 pos;           // last sample position (voxel space)
   float4 xf;        // last classified sample
   float t, t1, maj, Tr;
-  int primID;       // the cached gridlet (>= 0), a hint -2 - id, or none (-1)
+  int primID;       // the cached gridlet (testSample), -1: none
   int steps, ncells;
   int type;
   bool needCell;
 };
 
-// `hint`: a gridlet near the walk's start for its first full query (-1:
-// none; see Walk::primID)
-EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray, int hint = -1)
+EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
 {
   ray.org = xfm_point(lp.voxelSpaceTransform, ray.org);
   ray.dir = xfm_vector(lp.voxelSpaceTransform, ray.dir);
@@ -349,12 +347,9 @@ EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray, int hint =
   w.Tr = 1.f;
   w.type = BOUNDARY;
   w.ncells = 0;
-  w.primID = hint;   // no cached gridlet
+  w.primID = -1;
   w.needCell = true;
 }
-
-// the hint for a walk that starts where walk w ended: w's last gridlet
-EXA_D int walk_hint(const Walk &w) { return w.primID >= 0 ? -2 - w.primID : w.primID; }
 
 // walk_advance: the DDA advance and the free flight of one step.
 // Returns 0 when the walk ended, 1 when the step took no sample (the flight
@@ -377,10 +372,7 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
     if (!exa_in_range(leafID, (long long)G.dims.x * G.dims.y * G.dims.z, c.err)) return WALK_END;
     w.maj = __ldg(lp.maxOpacities + leafID);
     w.t = w.dda.t0;
-    // the reference's gridlet cache ends with the macrocell
-    // (deviceCode.cu:731-760); the gridlet stays as a hint for the next
-    // full query, encoded -2 - id
-    if (w.primID >= 0) w.primID = -2 - w.primID;
+    w.primID = -1;  // the gridlet cache ends with the macrocell (deviceCode.cu:731-760)
     w.steps = 0;
     if (w.maj <= 0.f) {
       if (!dda_next_dir(w.dda, w.dir, G.dims)) return WALK_END;
@@ -401,21 +393,6 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
   return WALK_SAMPLE;
 }
 
-// the full point location of a step whose cached gridlet (if any) missed;
-// EXA_SAMPLE_MISS_NOINLINE=1 builds it out of line
-#ifndef EXA_SAMPLE_MISS_NOINLINE
-#define EXA_SAMPLE_MISS_NOINLINE 0
-#endif
-#if EXA_SAMPLE_MISS_NOINLINE
-static __device__ __noinline__
-#else
-EXA_D
-#endif
-exa_sample sample_miss(const AccelView &A, V3 pos, bool cull, int primID, uint32_t &err, QueryStats *q)
-{
-  return primID <= -2 ? sample_field_hinted(A, pos, cull, -2 - primID, err, q) : sample_field(A, pos, cull, err, q);
-}
-
 // the exact sampler at w.pos: the cached gridlet first (testSample,
 // deviceCode.cu:749), then the full point location
 EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
@@ -424,7 +401,7 @@ EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
       test_sample(c.A, w.pos, w.primID < 0 || exa_in_range(w.primID, c.A.numGridlets, c.err) ? w.primID : -1);
   if (s.primID < 0) {
     QueryStats q{0u, 0u, 0u};
-    s = sample_miss(c.A, w.pos, c.lp.ext.cullTransparentPrims != 0, w.primID, c.err, &q);
+    s = sample_field(c.A, w.pos, c.lp.ext.cullTransparentPrims != 0, c.err, &q);
     if (c.counting) {
       cnt_add(c, CNT_MISS);
       cnt_add(c, CNT_TABLES, q.tables);
@@ -694,7 +671,7 @@ struct Machine {
     }
     L.lightI = lp.lights[which].intensity;
     L.shadow = true;
-    walk_begin(L.w, lp, ray, walk_hint(L.w));
+    walk_begin(L.w, lp, ray);
     L.phase = PH_TRACK;
   }
 
@@ -728,7 +705,7 @@ struct Machine {
     L.ray.tmax = t1;
     mesh_clip(L, L.ray);
     L.shadow = false;
-    walk_begin(L.w, lp, L.ray, walk_hint(L.w));
+    walk_begin(L.w, lp, L.ray);
   }
 
   EXA_D void primary_done(Lane &L)
@@ -1360,8 +1337,7 @@ EXA_D void wf_load_path(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
 
 // shadow flag, RNG and the walk
 // A walk that has not taken a step yet (walk_begin's state) is stored
-// "fresh": flags, RNG, gridlet hint, ray and DDA state (the first 21 of the
-// 35 words); the
+// "fresh": flags, RNG, ray and DDA state (the first 21 of the 35 words); the
 // loader sets the rest to walk_begin's values.  (Storing only the ray and
 // re-running dda_init in the walk kernel saves more traffic but costs the
 // latency-bound walk kernel more than it saves.)
@@ -1372,14 +1348,14 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, b
   unsigned k = kPathStride;
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.needCell << 1) | ((uint32_t)w.type << 2) | (fresh ? kWalkFresh : 0u));
-  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); W((uint32_t)w.primID);
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 3: unused
   WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
   W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
   if (fresh) return;
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z); WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
   WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
-  ++k; W((uint32_t)w.steps); W((uint32_t)w.ncells);  // word 32: unused
+  W((uint32_t)w.primID); W((uint32_t)w.steps); W((uint32_t)w.ncells);
 }
 
 EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i,
@@ -1393,7 +1369,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.type = (int)((flags & ~kWalkFresh) >> 2);
   const uint32_t lo = R(), hi = R();
   L.rng.state = ((uint64_t)hi << 32) | lo;
-  w.primID = (int)R();
+  ++k;
   w.org.x = RF(); w.org.y = RF(); w.org.z = RF(); w.dir.x = RF(); w.dir.y = RF(); w.dir.z = RF();
   w.dda.tnext.x = RF(); w.dda.tnext.y = RF(); w.dda.tnext.z = RF();
   w.dda.dist.x = RF(); w.dda.dist.y = RF(); w.dda.dist.z = RF();
@@ -1408,6 +1384,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
     w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
     w.t = w.t1 = w.maj = 0.f;
     w.Tr = 1.f;
+    w.primID = -1;
     w.steps = 0;
     w.ncells = 0;
     return;
@@ -1415,7 +1392,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
   w.t = RF(); w.t1 = RF(); w.maj = RF(); w.Tr = RF();
-  ++k; w.steps = (int)R(); w.ncells = (int)R();
+  w.primID = (int)R(); w.steps = (int)R(); w.ncells = (int)R();
 }
 
 // event record of a walk that ended: the fields the integrator step reads,
@@ -1435,7 +1412,7 @@ EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, 
   const Walk &w = L.w;
   W((uint32_t)L.shadow | ((uint32_t)w.type << 2) | ((uint32_t)w.ncells << 8));
   W(src);
-  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); W((uint32_t)w.primID);
+  W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 4: unused
   WF(w.t); WF(w.Tr);
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z);
   WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
@@ -1455,7 +1432,7 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
   const unsigned src = R();
   const uint32_t lo = R(), hi = R();
   L.rng.state = ((uint64_t)hi << 32) | lo;
-  w.primID = (int)R();
+  ++k;
   w.t = RF(); w.Tr = RF();
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
   w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();

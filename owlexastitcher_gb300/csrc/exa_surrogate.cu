@@ -390,7 +390,9 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_sur_mlp_train(
 //            the block's tiles and is added to gw once.
 // Operands and tensor-memory columns are reused step by step; every step
 // starts after the previous one's commit.  Waits are bounded: a wait that
-// gives up sets EXA_DEVERR_WATCHDOG in *errors and the block stops.
+// gives up sets EXA_DEVERR_WATCHDOG in *errors and the block stops.  The
+// tensor-memory loads (tcgen05.ld) are warp-collective: every thread of a
+// warp executes each of them, also for pairs past the batch.
 struct alignas(1024) TcTrainSmem {
   __nv_bfloat16 w1[kSurHidden * kSurIn];        // B of layer 1: (j, k), K 32
   __nv_bfloat16 w2[kSurHidden * kSurHidden];    // B of layer 2: (j, i), K 64
@@ -454,10 +456,12 @@ __global__ void __launch_bounds__(128, 1) k_sur_mlp_train_tc(
     __syncthreads();
     tc::fence_after_sync();
   };
-  // every thread waits for the committed products (bounded)
+  // every thread waits for the committed products, at most about a second
   auto wait_products = [&]() -> bool {
-    bool done = false;
-    for (int i = 0; i < (1 << 24) && !done; ++i) done = tc::mbar_try_wait(&S.bar, phase);
+    bool done = tc::mbar_try_wait(&S.bar, phase);
+    const uint64_t t0 = tc::globaltimer_ns();
+    for (int i = 0; i < (1 << 22) && !done && tc::globaltimer_ns() - t0 < 1000000000ull; ++i)
+      done = tc::mbar_try_wait(&S.bar, phase);
     phase ^= 1u;
     if (!done) atomicOr(&S.stop, 1u);
     __syncthreads();
@@ -588,11 +592,13 @@ __global__ void __launch_bounds__(128, 1) k_sur_mlp_train_tc(
     }
     any = true;
     if (!wait_products()) break;
-    if (inB) {
-      float4 *dst = reinterpret_cast<float4 *>(dfeat + (size_t)r * kSurIn);
-      for (int c = 0; c < kSurIn / 16; ++c) {
-        float v[16];
-        tc::ld16(lanes + kColD2 + 16 * c, v);
+    // every thread of a warp takes part in the (warp-collective) loads;
+    // pairs past B store nothing
+    for (int c = 0; c < kSurIn / 16; ++c) {
+      float v[16];
+      tc::ld16(lanes + kColD2 + 16 * c, v);
+      if (inB) {
+        float4 *dst = reinterpret_cast<float4 *>(dfeat + (size_t)r * kSurIn);
 #pragma unroll
         for (int k = 0; k < 4; ++k) dst[4 * c + k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
       }
@@ -963,6 +969,12 @@ float Surrogate::trainSteps(int steps, cudaStream_t s)
     k_sur_adam_mlp<<<gridFor(kSurParams, 256), 256, 0, s>>>(w32.ptr, gw.ptr, mw.ptr, vw.ptr, kSurParams, lrM, b1, b2,
                                                            c1, c2, 1e-15f, wbf.ptr);
     cudaCheck(cudaGetLastError(), "surrogate training step");
+    if ((it & 63) == 63) {  // a failed step ends the training early
+      uint32_t terr = 0;
+      cudaCheck(cudaMemcpyAsync(&terr, trainErrors.ptr, sizeof(terr), cudaMemcpyDeviceToHost, s), "train errors");
+      cudaCheck(cudaStreamSynchronize(s), "surrogate training");
+      if (terr) throw Error(EXA_ERR_CUDA, "surrogate training: a tensor-core product did not complete");
+    }
   }
   float h[2] = {0.f, 0.f};
   uint32_t terr = 0;

@@ -89,6 +89,14 @@ EXA_D bool mbar_try_wait(uint64_t *bar, uint32_t parity)
   return done != 0;
 }
 
+// the global nanosecond timer (bounds waits in time)
+EXA_D uint64_t globaltimer_ns()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 EXA_D void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 EXA_D void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
