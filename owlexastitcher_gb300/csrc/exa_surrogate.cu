@@ -9,9 +9,11 @@
 // refined levels.  One training step on a batch of B pairs is three kernels:
 //   k_sur_encode_fwd  encoding of the batch from the FP32 master table
 //                     (one thread per pair) -> BF16 inputs [B][32]
-//   k_sur_mlp_train   forward and backward of the MLP on the tensor cores,
-//                     32 pairs per warp; weight gradients summed per block in
-//                     shared memory; input gradients [B][32] FP32
+//   k_sur_mlp_train_tc forward and backward of the MLP on the 5th-generation
+//                     tensor cores (tcgen05.mma, accumulators in tensor
+//                     memory), 128 pairs per tile; weight gradients
+//                     accumulated in tensor memory per block; input
+//                     gradients [B][32] FP32
 //   k_sur_encode_bwd  scatter of the input gradients into the table
 //                     gradient (float2 atomics)
 // then Adam over the table and the weights, which also refreshes the FP16
@@ -126,251 +128,6 @@ __global__ void k_sur_encode_bwd(const __grid_constant__ SurrogateView S, const 
 #pragma unroll
     for (int k = 0; k < 8; ++k) atomicAdd(tab + idx[k], make_float2(w[k] * g0, w[k] * g1));
   }
-}
-
-// ------------------------------------------------------------ MLP training
-struct alignas(16) TrainSmem {
-  __nv_bfloat16 w1[kSurHidden * kSurLdIn];    // [64][40]  W1 (j, i)
-  __nv_bfloat16 w1t[kSurIn * kSurLdHid];      // [32][72]  W1^T (i, j)
-  __nv_bfloat16 w2[kSurHidden * kSurLdHid];   // [64][72]  W2 (j, i)
-  __nv_bfloat16 w2t[kSurHidden * kSurLdHid];  // [64][72]  W2^T (i, j)
-  float w3[kSurHidden];
-  float gw1[kSurHidden * kSurIn];
-  float gw2[kSurHidden * kSurHidden];
-  float gw3[kSurHidden];
-  float loss;
-};
-
-struct alignas(16) TrainWarpSmem {
-  __nv_bfloat16 a[32 * kSurLdIn];         // inputs (r, i)
-  __nv_bfloat16 at[kSurIn * kSurLdIn];    // inputs^T (i, r)
-  __nv_bfloat16 h1[32 * kSurLdHid];       // (r, j)
-  __nv_bfloat16 h1t[kSurHidden * kSurLdIn];  // (j, r)
-  __nv_bfloat16 h2[32 * kSurLdHid];       // (r, j), then d1 (r, i)
-  __nv_bfloat16 d2[32 * kSurLdHid];       // (r, j), then din as FP32 [32][36]
-  __nv_bfloat16 d2t[kSurHidden * kSurLdIn];  // (j, r)
-  __nv_bfloat16 d1t[kSurHidden * kSurLdIn];  // (i, r)
-};
-constexpr int kTrainWarps = 4;
-constexpr size_t kTrainSmemBytes = sizeof(TrainSmem) + kTrainWarps * sizeof(TrainWarpSmem);
-static_assert(sizeof(TrainSmem) % 16 == 0 && sizeof(TrainWarpSmem) % 16 == 0, "16-byte rows");
-
-EXA_D void st_bf16x2(__nv_bfloat16 *p, float a, float b) { *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(a, b); }
-
-// Forward and backward of the MLP for B pairs (32 per warp iteration).
-// Loss: mean over valid pairs of (y - target)^2 with target the normalised
-// value.  Gradients (see exa_surrogate.cuh for the forward):
-//   g = 2 (y - target) / B;  gw3 += g h2
-//   d2 = bf16(g w3) where h2 > 0;  gw2 += d2 (x) h1
-//   d1 = bf16(W2^T d2) where h1 > 0;  gw1 += d1 (x) a0
-//   din = W1^T d1 (FP32)
-__global__ void __launch_bounds__(32 * kTrainWarps) k_sur_mlp_train(
-    const __nv_bfloat16 *__restrict__ w1g, const __nv_bfloat16 *__restrict__ w2g, const __nv_bfloat16 *__restrict__ w3g,
-    const __nv_bfloat16 *__restrict__ feats, const float4 *__restrict__ samples, size_t first, size_t numSamples, int B,
-    float vmin, float invRange, float invB, float *gw, float *lossOut, float *dfeat)
-{
-  extern __shared__ __align__(16) unsigned char smraw[];
-  TrainSmem &S = *reinterpret_cast<TrainSmem *>(smraw);
-  TrainWarpSmem &ws = reinterpret_cast<TrainWarpSmem *>(smraw + sizeof(TrainSmem))[threadIdx.x >> 5];
-  for (int i = threadIdx.x; i < kSurHidden * kSurIn; i += blockDim.x) {
-    const int j = i / kSurIn, k = i % kSurIn;
-    S.w1[j * kSurLdIn + k] = w1g[i];
-    S.w1t[k * kSurLdHid + j] = w1g[i];
-    S.gw1[i] = 0.f;
-  }
-  for (int i = threadIdx.x; i < kSurHidden * kSurHidden; i += blockDim.x) {
-    const int j = i / kSurHidden, k = i % kSurHidden;
-    S.w2[j * kSurLdHid + k] = w2g[i];
-    S.w2t[k * kSurLdHid + j] = w2g[i];
-    S.gw2[i] = 0.f;
-  }
-  for (int i = threadIdx.x; i < kSurHidden; i += blockDim.x) {
-    S.w3[i] = __bfloat162float(w3g[i]);
-    S.gw3[i] = 0.f;
-  }
-  if (threadIdx.x == 0) S.loss = 0.f;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int warpsTotal = gridDim.x * kTrainWarps;
-  const int tiles = (B + 31) / 32;
-  float acc3lo = 0.f, acc3hi = 0.f, lossAcc = 0.f;
-  for (int tile = blockIdx.x * kTrainWarps + (threadIdx.x >> 5); tile < tiles; tile += warpsTotal) {
-    const int r = tile * 32 + lane;
-    const bool inB = r < B;
-    // inputs and target
-    float target = 0.f;
-    bool valid = false;
-    {
-      uint4 q[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
-      if (inB) {
-        const uint4 *src = reinterpret_cast<const uint4 *>(feats + (size_t)r * kSurIn);
-        for (int k = 0; k < 4; ++k) q[k] = src[k];
-        const float v = samples[(first + (size_t)r) % numSamples].w;
-        valid = v == v;
-        target = valid ? (v - vmin) * invRange : 0.f;
-      }
-      uint4 *dst = reinterpret_cast<uint4 *>(ws.a + lane * kSurLdIn);
-      for (int k = 0; k < 4; ++k) dst[k] = q[k];
-      const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(q);
-      for (int i = 0; i < kSurIn; ++i) ws.at[i * kSurLdIn + lane] = e[i];
-    }
-    __syncwarp();
-    // layer 1
-    for (int mt = 0; mt < 2; ++mt)
-      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kSurIn / 16; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.a, kSurLdIn, mt * 16, kt * 16, lane);
-          frag_b(b, S.w1, kSurLdIn, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
-        const __nv_bfloat16 v0 = __float2bfloat16_rn(fmaxf(d[0], 0.f)), v1 = __float2bfloat16_rn(fmaxf(d[1], 0.f));
-        const __nv_bfloat16 v2 = __float2bfloat16_rn(fmaxf(d[2], 0.f)), v3 = __float2bfloat16_rn(fmaxf(d[3], 0.f));
-        ws.h1[rr * kSurLdHid + c] = v0;
-        ws.h1[rr * kSurLdHid + c + 1] = v1;
-        ws.h1[(rr + 8) * kSurLdHid + c] = v2;
-        ws.h1[(rr + 8) * kSurLdHid + c + 1] = v3;
-        ws.h1t[c * kSurLdIn + rr] = v0;
-        ws.h1t[(c + 1) * kSurLdIn + rr] = v1;
-        ws.h1t[c * kSurLdIn + rr + 8] = v2;
-        ws.h1t[(c + 1) * kSurLdIn + rr + 8] = v3;
-      }
-    __syncwarp();
-    // layer 2
-    for (int mt = 0; mt < 2; ++mt)
-      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.h1, kSurLdHid, mt * 16, kt * 16, lane);
-          frag_b(b, S.w2, kSurLdHid, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
-        st_bf16x2(ws.h2 + rr * kSurLdHid + c, fmaxf(d[0], 0.f), fmaxf(d[1], 0.f));
-        st_bf16x2(ws.h2 + (rr + 8) * kSurLdHid + c, fmaxf(d[2], 0.f), fmaxf(d[3], 0.f));
-      }
-    __syncwarp();
-    // output, loss and its gradient (row of this lane)
-    float y = 0.f;
-    for (int j = 0; j < kSurHidden; ++j) y += __bfloat162float(ws.h2[lane * kSurLdHid + j]) * S.w3[j];
-    const float diff = y - target;
-    const float gr = (inB && valid) ? 2.f * diff * invB : 0.f;
-    if (inB && valid) lossAcc += diff * diff;
-    // gw3 (columns lane and lane + 32) and d2 = bf16(g w3) where h2 > 0
-    for (int rr = 0; rr < 32; ++rr) {
-      const float gv = __shfl_sync(0xffffffffu, gr, rr);
-      acc3lo += gv * __bfloat162float(ws.h2[rr * kSurLdHid + lane]);
-      acc3hi += gv * __bfloat162float(ws.h2[rr * kSurLdHid + lane + 32]);
-    }
-    __syncwarp();
-    for (int j = 0; j < kSurHidden; ++j) {
-      const bool on = __bfloat162float(ws.h2[lane * kSurLdHid + j]) > 0.f;
-      const __nv_bfloat16 v = __float2bfloat16_rn(on ? gr * S.w3[j] : 0.f);
-      ws.d2[lane * kSurLdHid + j] = v;
-      ws.d2t[j * kSurLdIn + lane] = v;
-    }
-    __syncwarp();
-    // d1 = bf16(d2 W2) where h1 > 0, into the h2 buffer (h2 is no longer read)
-    for (int mt = 0; mt < 2; ++mt)
-      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.d2, kSurLdHid, mt * 16, kt * 16, lane);
-          frag_b(b, S.w2t, kSurLdHid, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
-        const float m0 = __bfloat162float(ws.h1[rr * kSurLdHid + c]) > 0.f ? d[0] : 0.f;
-        const float m1 = __bfloat162float(ws.h1[rr * kSurLdHid + c + 1]) > 0.f ? d[1] : 0.f;
-        const float m2 = __bfloat162float(ws.h1[(rr + 8) * kSurLdHid + c]) > 0.f ? d[2] : 0.f;
-        const float m3 = __bfloat162float(ws.h1[(rr + 8) * kSurLdHid + c + 1]) > 0.f ? d[3] : 0.f;
-        const __nv_bfloat16 v0 = __float2bfloat16_rn(m0), v1 = __float2bfloat16_rn(m1);
-        const __nv_bfloat16 v2 = __float2bfloat16_rn(m2), v3 = __float2bfloat16_rn(m3);
-        ws.h2[rr * kSurLdHid + c] = v0;
-        ws.h2[rr * kSurLdHid + c + 1] = v1;
-        ws.h2[(rr + 8) * kSurLdHid + c] = v2;
-        ws.h2[(rr + 8) * kSurLdHid + c + 1] = v3;
-        ws.d1t[c * kSurLdIn + rr] = v0;
-        ws.d1t[(c + 1) * kSurLdIn + rr] = v1;
-        ws.d1t[c * kSurLdIn + rr + 8] = v2;
-        ws.d1t[(c + 1) * kSurLdIn + rr + 8] = v3;
-      }
-    __syncwarp();
-    // din = d1 W1 (FP32, into the d2 buffer: d2 is no longer read)
-    float *din = reinterpret_cast<float *>(ws.d2);
-    constexpr int ldDin = 36;
-    for (int mt = 0; mt < 2; ++mt)
-      for (int nt = 0; nt < kSurIn / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kSurHidden / 16; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.h2, kSurLdHid, mt * 16, kt * 16, lane);
-          frag_b(b, S.w1t, kSurLdHid, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int rr = mt * 16 + g, c = nt * 8 + 2 * t;
-        din[rr * ldDin + c] = d[0];
-        din[rr * ldDin + c + 1] = d[1];
-        din[(rr + 8) * ldDin + c] = d[2];
-        din[(rr + 8) * ldDin + c + 1] = d[3];
-      }
-    // gw2 += d2^T h1 (m = j, n = i, k = r)
-    for (int mt = 0; mt < kSurHidden / 16; ++mt)
-      for (int nt = 0; nt < kSurHidden / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < 2; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.d2t, kSurLdIn, mt * 16, kt * 16, lane);
-          frag_b(b, ws.h1t, kSurLdIn, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int j = mt * 16 + g, c = nt * 8 + 2 * t;
-        atomicAdd(&S.gw2[j * kSurHidden + c], d[0]);
-        atomicAdd(&S.gw2[j * kSurHidden + c + 1], d[1]);
-        atomicAdd(&S.gw2[(j + 8) * kSurHidden + c], d[2]);
-        atomicAdd(&S.gw2[(j + 8) * kSurHidden + c + 1], d[3]);
-      }
-    // gw1 += d1^T a0 (m = j, n = i, k = r)
-    for (int mt = 0; mt < kSurHidden / 16; ++mt)
-      for (int nt = 0; nt < kSurIn / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < 2; ++kt) {
-          uint32_t a[4], b[2];
-          frag_a(a, ws.d1t, kSurLdIn, mt * 16, kt * 16, lane);
-          frag_b(b, ws.at, kSurLdIn, nt * 8, kt * 16, lane);
-          mma16816(d, a, b);
-        }
-        const int j = mt * 16 + g, c = nt * 8 + 2 * t;
-        atomicAdd(&S.gw1[j * kSurIn + c], d[0]);
-        atomicAdd(&S.gw1[j * kSurIn + c + 1], d[1]);
-        atomicAdd(&S.gw1[(j + 8) * kSurIn + c], d[2]);
-        atomicAdd(&S.gw1[(j + 8) * kSurIn + c + 1], d[3]);
-      }
-    __syncwarp();
-    if (inB) {
-      float4 *dst = reinterpret_cast<float4 *>(dfeat + (size_t)r * kSurIn);
-      const float *src = din + lane * ldDin;
-      for (int k = 0; k < kSurIn / 4; ++k) dst[k] = make_float4(src[4 * k], src[4 * k + 1], src[4 * k + 2], src[4 * k + 3]);
-    }
-    __syncwarp();
-  }
-  atomicAdd(&S.gw3[lane], acc3lo);
-  atomicAdd(&S.gw3[lane + 32], acc3hi);
-  for (int o = 16; o > 0; o >>= 1) lossAcc += __shfl_xor_sync(0xffffffffu, lossAcc, o);
-  if (lane == 0) atomicAdd(&S.loss, lossAcc);
-  __syncthreads();
-  // weight gradient layout in gw: w1 (2048), w2 (4096), w3 (64)
-  for (int i = threadIdx.x; i < kSurHidden * kSurIn; i += blockDim.x)
-    if (S.gw1[i] != 0.f) atomicAdd(gw + i, S.gw1[i]);
-  for (int i = threadIdx.x; i < kSurHidden * kSurHidden; i += blockDim.x)
-    if (S.gw2[i] != 0.f) atomicAdd(gw + kSurHidden * kSurIn + i, S.gw2[i]);
-  for (int i = threadIdx.x; i < kSurHidden; i += blockDim.x)
-    if (S.gw3[i] != 0.f) atomicAdd(gw + kSurHidden * kSurIn + kSurHidden * kSurHidden + i, S.gw3[i]);
-  if (threadIdx.x == 0) atomicAdd(lossOut, S.loss);
 }
 
 // ------------------------------------------------ MLP training, tcgen05
@@ -904,11 +661,8 @@ void Surrogate::generateSamples(const ExaStitchSampler &sampler, cudaStream_t s)
   cudaCheck(cudaStreamSynchronize(s), "surrogate samples");
 }
 
-// the MLP training step of B pairs: the tcgen05 kernel (one block per SM),
-// or with EXA_SUR_TRAIN_TC=0 the mma.sync kernel
-#ifndef EXA_SUR_TRAIN_TC
-#define EXA_SUR_TRAIN_TC 0
-#endif
+// the MLP training step of B pairs on the tensor cores: one block of
+// k_sur_mlp_train_tc per SM (its 124 KB of operands), 128 pairs per tile
 static void launchMlpTrain(const SurrogateView &v, const __nv_bfloat16 *feats, const float4 *samples, size_t first,
                            size_t numSamples, int B, float vmin, float invRange, float invB, float *gw, float *loss,
                            float *dfeat, uint32_t *errors, cudaStream_t s)
@@ -916,22 +670,12 @@ static void launchMlpTrain(const SurrogateView &v, const __nv_bfloat16 *feats, c
   int dev = 0, sms = 152;
   cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
   cudaCheck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-  if (EXA_SUR_TRAIN_TC) {
-    cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(TcTrainSmem)),
-              "train smem");
-    const unsigned blocks = (unsigned)std::min<int>((B + 127) / 128, sms);
-    k_sur_mlp_train_tc<<<blocks, 128, sizeof(TcTrainSmem), s>>>(v.w1, v.w2, v.w3, feats, samples, first, numSamples,
-                                                                B, vmin, invRange, invB, gw, loss, dfeat, errors);
-  } else {
-    cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kTrainSmemBytes),
-              "train smem");
-    const unsigned blocks = (unsigned)std::min<int>((B / 32 + kTrainWarps - 1) / kTrainWarps + 1, sms * 2);
-    k_sur_mlp_train<<<blocks, 32 * kTrainWarps, kTrainSmemBytes, s>>>(v.w1, v.w2, v.w3, feats, samples, first,
-                                                                      numSamples, B, vmin, invRange, invB, gw, loss,
-                                                                      dfeat);
-  }
+  cudaCheck(cudaFuncSetAttribute(k_sur_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(TcTrainSmem)),
+            "train smem");
+  const unsigned blocks = (unsigned)std::min<int>((B + 127) / 128, sms);
+  k_sur_mlp_train_tc<<<blocks, 128, sizeof(TcTrainSmem), s>>>(v.w1, v.w2, v.w3, feats, samples, first, numSamples, B,
+                                                              vmin, invRange, invB, gw, loss, dfeat, errors);
   cudaCheck(cudaGetLastError(), "MLP training step");
 }
 
