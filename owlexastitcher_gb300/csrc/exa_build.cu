@@ -449,14 +449,18 @@ constexpr int kSepWin = 9;        // macrocells per axis of a gridlet's window
 constexpr int kSepRows = 81;      // corner rows (y, z) of an 8^3-cell gridlet
 
 struct alignas(16) SepWarpSmem {
-  float brick[2][kBrickCap];
+  float brick[kBrickCap];
   float2 rx[kSepWin * kSepRows];  // (min, max) per (macrocell column, corner row)
   int2 cellRange[3][8];           // per axis and cell index: its macrocell range
   int2 cornerIv[3][kSepWin];      // per axis and window macrocell: corners [ca, cb]
-  GridletPlan plan[2];
-  uint64_t bar[2];
+  GridletPlan plan;               // of the gridlet whose brick is staged
+  uint64_t bar;
 };
 
+// One staging buffer per warp: the next gridlet's brick is copied in as soon
+// as the current one's corners are reduced along x, so the copy runs during
+// the current gridlet's macrocell updates (and, at 9.4 KB of shared memory
+// per warp, 24 warps per SM hide what it does not cover).
 __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
     const exa_gridlet *__restrict__ gridlets, size_t ng, const float *__restrict__ scalars, size_t nScalars,
     bool stage, exa_vec3i dims, exa_box3f wb, exa_range1f *mcRanges, exa_range1f *gridletRanges, uint32_t *errors,
@@ -468,12 +472,16 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
   const size_t w0 = (size_t)blockIdx.x * kSepWarps + (threadIdx.x >> 5);
   const size_t stride = (size_t)gridDim.x * kSepWarps;
   const V3i D = {dims.x, dims.y, dims.z};
-  // lane 0 stages a gridlet: its plan and the bulk copy of its brick
-  auto prepare = [&](int buf, const exa_gridlet &hdr) {
-    GridletPlan &pl = sm.plan[buf];
+  // lane 0 stages a gridlet: its plan and the bulk copy of its brick (the
+  // buffer's readers are done: a __syncwarp precedes every call)
+  auto prepare = [&](const exa_gridlet &hdr) {
+    GridletPlan &pl = sm.plan;
     pl.g = hdr;
     pl.P = brick_plan(pl.g, nScalars, stage);
-    if (pl.P.bulk) bulk_load_smem(sm.brick[buf], scalars + pl.P.f0, pl.P.bulk, &sm.bar[buf]);
+    if (pl.P.bulk) {
+      fence_proxy_async_smem();
+      bulk_load_smem(sm.brick, scalars + pl.P.f0, pl.P.bulk, &sm.bar);
+    }
     const float cw = (float)(1 << hdr.level);
     const V3 lo = mk3(((float)hdr.lower.x + 0.5f) * cw, ((float)hdr.lower.y + 0.5f) * cw,
                       ((float)hdr.lower.z + 0.5f) * cw);
@@ -484,48 +492,39 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
     pl.hiMC = project_on_grid(hi, D, wb);
   };
   if (lane == 0) {
-    mbar_init(&sm.bar[0]);
-    mbar_init(&sm.bar[1]);
+    mbar_init(&sm.bar);
     mbar_init_fence();
-    if (w0 < ng) prepare(0, gridlets[w0]);
+    if (w0 < ng) prepare(gridlets[w0]);
   }
   __syncwarp();
   const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
   uint32_t parity = 0;
-  int it = 0;
-  for (size_t gi = w0; gi < ng; gi += stride, ++it) {
-    const int buf = it & 1;
-    const exa_gridlet g = sm.plan[buf].g;
-    const BrickPlan P = sm.plan[buf].P;
-    const V3i loMC = sm.plan[buf].loMC, hiMC = sm.plan[buf].hiMC;
+  for (size_t gi = w0; gi < ng; gi += stride) {
+    const exa_gridlet g = sm.plan.g;
+    const BrickPlan P = sm.plan.P;
+    const V3i loMC = sm.plan.loMC, hiMC = sm.plan.hiMC;
     const size_t gn = gi + stride;
-    if (lane == 0 && gn < ng) {
-      fence_proxy_async_smem();
-      prepare(buf ^ 1, gridlets[gn]);
-    }
-    const uint32_t ph = (parity >> buf) & 1u;
     bool ok = true;
     if (P.bulk) {
-      ok = mbar_wait(&sm.bar[buf], ph);
+      ok = mbar_wait(&sm.bar, parity);
       // the simulated time-out of the error-path test (see k_gridlet_majorants)
       if ((debugFlags & EXA_DEBUG_COPY_WAIT_TIMEOUT) && gi == 0) ok = false;
-      parity ^= 1u << buf;
     }
     if (__any_sync(0xffffffffu, !ok)) {
-      // give up: flag it and wait (bounded) for both buffers' copies
+      // give up: flag it and wait (bounded) once more for the copy
       if (lane == 0) {
         if (errors) atomicOr(errors, EXA_DEVERR_COPY_WAIT);
-        if (P.bulk) (void)mbar_wait(&sm.bar[buf], ph);
-        if (gn < ng && sm.plan[buf ^ 1].P.bulk) (void)mbar_wait(&sm.bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
+        (void)mbar_wait(&sm.bar, parity);
       }
       return;
     }
+    if (P.bulk) parity ^= 1u;
     const int wx = hiMC.x - loMC.x + 1, wy = hiMC.y - loMC.y + 1, wz = hiMC.z - loMC.z + 1;
     bool sep = P.staged && g.dims.x <= 8 && g.dims.y <= 8 && g.dims.z <= 8 && wx <= kSepWin && wy <= kSepWin &&
                wz <= kSepWin;
     const int nx = g.dims.x + 1, ny = g.dims.y + 1, nz = g.dims.z + 1;
     const int rows = ny * nz;
-    float *B = sm.brick[buf];
+    float *B = sm.brick;
     if (sep) {
       for (int k = lane; k < P.tail; k += 32) B[P.bulk / 4 + k] = __ldg(scalars + P.f0 + P.bulk / 4 + k);
       // each cell's macrocell range along each axis
@@ -572,7 +571,10 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
       __syncwarp();
     }
     if (!sep) {
-      if (lane == 0) fallback[atomicAdd(fallbackCount, 1u)] = (uint32_t)gi;
+      if (lane == 0) {
+        fallback[atomicAdd(fallbackCount, 1u)] = (uint32_t)gi;
+        if (gn < ng) prepare(gridlets[gn]);
+      }
       __syncwarp();
       continue;
     }
@@ -597,6 +599,9 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
       }
       sm.rx[k] = make_float2(lo, hi);
     }
+    // the brick is read: the next gridlet's copy runs from here on
+    __syncwarp();
+    if (lane == 0 && gn < ng) prepare(gridlets[gn]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
@@ -606,7 +611,6 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
       gridletRanges[gi].lower = glo;
       gridletRanges[gi].upper = ghi;
     }
-    __syncwarp();
     // over the y x z rectangle of rows of each window macrocell
     for (int k = lane; k < wx * wy * wz; k += 32) {
       const int mx = k % wx, my = (k / wx) % wy, mz = k / (wx * wy);
@@ -621,7 +625,7 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
         }
       if (lo <= hi) update_mc(mcRanges, dims, loMC.x + mx, loMC.y + my, loMC.z + mz, lo, hi);
     }
-    // this buffer and the tables are free for the next gridlets
+    // the tables and the plan are free for the next gridlet
     __syncwarp();
   }
 }
