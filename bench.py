@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-field (surrogate) measurements")
     ap.add_argument("--learned-steps", type=int, default=1600, help="surrogate training steps")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-frames measurements")
+    ap.add_argument("--majorant-only", action="store_true",
+                    help="only the majorant build on the workload's field (one untimed and 3 timed builds); prints "
+                         "the majorant_build object (for ncu captures of the build kernels)")
     ap.add_argument("--split", default="replicas", choices=["replicas", "bands"],
                     help="multi-GPU: replicas (a frame per rank, weak scaling) or bands (one frame, a band of rows "
                          "per rank, gathered on rank 0; strong scaling)")
@@ -66,6 +69,8 @@ def parse():
     a.height = a.height or (1080 if big else HEIGHT)
     a.spp = a.spp or (64 if big else SPP)
     a.bounces = 16 if big else 8
+    if a.majorant_only:
+        a.no_cpu_baseline = True
     if big:
         # the oracle's field for ~400M cells is too large for a bounded CPU
         # sample; the batched workload is defined on the small field
@@ -192,6 +197,10 @@ def run_ours(a):
             dist.barrier()
 
     ds, gen = make_scene(a, local)
+    if a.majorant_only:
+        peak, peak_kind = load_peaks()
+        print(json.dumps(majorant_build(ds, local, NUM_MCS, peak, peak_kind)))
+        return
     ctx = E.Context(local)
     r = E.Renderer(ctx, E.ExaStitchModel.from_dataset(ctx, ds), NUM_MCS)
     lo, hi = r.model.cellBounds
@@ -403,7 +412,8 @@ def majorant_build(ds, local, num_mcs, peak, peak_kind, reps=3):
     n_mc = int(np.prod(num_mcs))
     alg = 4 * int(ds.stats["numGridletScalars"]) + 40 * int(ds.stats["numGridlets"]) + 8 * n_mc
     achieved = alg / (g_ms / 1e3) / 1e9
-    return {"kernel": "k_gridlet_majorants", "majorant_grid": list(num_mcs), "gpu_ms": g_ms,
+    return {"kernel": "k_gridlet_majorants_sep, then k_gridlet_majorants over the gridlets it leaves",
+            "majorant_grid": list(num_mcs), "gpu_ms": g_ms,
             "elem_kernel_ms": statistics.median(s["elemMajorantMs"] for s in stats),
             "build_total_ms": statistics.median(s["totalMs"] for s in stats), "blocks": stats[0]["majorantBlocks"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -471,6 +481,7 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
                      "exact_field_samples": int(c[0]), "learned_samples": int(c[10]),
                      "majorant_violations": int(c[11])}
     r.learned = False
+    conv = converged_rmse(a, r, lo, hi)
     # point queries: learned value vs exact sample at 1M uniform points
     rng = np.random.default_rng(42)
     P = rng.uniform(lo, hi, (1 << 20, 3)).astype(np.float32)
@@ -496,7 +507,8 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
         "dataset": ds.config if hasattr(ds, "config") else None, "majorant_grid": list(num_mcs),
         "encoding": {"levels": 16, "features": 2, "table_entries_per_level": 1 << log2T, "base_resolution": 16,
                      "growth": 1.5},
-        "mlp": "32-64-64-1 ReLU, BF16 weights, FP32 accumulate (mma.sync m16n8k16)",
+        "mlp": "32-64-64-1 ReLU, BF16 weights, FP32 accumulate; training: tcgen05.mma (M = 128, accumulators in "
+               "tensor memory); inference inside the walk: mma.sync m16n8k16",
         "training": {"pairs": 1 << 24, "importance_fraction": 0.5, "batch": 1 << 18, "steps": a.learned_steps,
                      "final_batch_mse": loss, "sample_seconds": sample_s, "train_seconds": train_s,
                      "pairs_per_s": a.learned_steps * (1 << 18) / train_s},
@@ -511,10 +523,52 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
         "render": res,
         "paths_per_s_learned_over_exact": res["learned"]["paths_per_s"] / res["exact"]["paths_per_s"],
         "image_rmse_vs_exact_same_rng": rmse,
+        "converged": conv,
         "point_queries_per_s": q,
     }
     ctx.close()
     return out
+
+
+def converged_rmse(a, r, lo, hi, div=16, spp=256, frames=16):
+    """The learned field's bias on a converged image: the frame's camera at
+    1/div of its resolution, frames x spp samples per pixel accumulated
+    progressively, rendered three times -- exact, exact with other random
+    numbers (frameID 1), learned -- and the RMSE of each pair.  The two exact
+    images differ by noise only, so their RMSE is the noise floor a bias has
+    to show above."""
+    from helpers import orbit_camera, setup_render
+    from owlexastitcher_gb300 import exastitch as E
+    w, h = max(a.width // div, 8), max(a.height // div, 8)
+    saved = (r.fbSize, r.spp)
+    r.resize(w, h)
+    r.spp = spp
+    setup_render(r.lp, orbit_camera(lo, hi, w, h), w, h, E.PATH_TRACING_INTEGRATOR, spp, "directional", True)
+    r.lp.ext.maxBounces = a.bounces
+    imgs = {}
+    t0 = time.perf_counter()
+    for name, learned, frame in (("exact", False, 0), ("exact_other_rng", False, 1), ("learned", True, 0)):
+        r.learned = learned
+        r.lp.ext.frameID = frame
+        r.accumID = 0
+        for _ in range(frames):
+            r.render()
+        r.ctx.sync()
+        imgs[name] = r.accum.cpu().numpy().reshape(-1, 4)[:, :3] / (frames * spp)
+    secs = time.perf_counter() - t0
+    r.learned = False
+    r.lp.ext.frameID = 0
+    (fw, fh), r.spp = saved
+    r.resize(fw, fh)
+    setup_render(r.lp, orbit_camera(lo, hi, fw, fh), fw, fh, E.PATH_TRACING_INTEGRATOR, r.spp, "directional", True)
+    r.lp.ext.maxBounces = a.bounces
+
+    def e(x, y):
+        return float(np.sqrt(np.mean((imgs[x] - imgs[y]) ** 2)))
+    return {"width": w, "height": h, "spp": frames * spp, "seconds": secs,
+            "rmse_exact_vs_exact_other_rng": e("exact", "exact_other_rng"),
+            "rmse_learned_vs_exact_other_rng": e("learned", "exact_other_rng"),
+            "rmse_learned_vs_exact_same_rng": e("learned", "exact")}
 
 
 def run_batched(a, local, flush):

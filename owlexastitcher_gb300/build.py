@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 CUDA_SOURCES = ["exa_build.cu", "exa_render.cu", "exa_surrogate.cu", "exa_exabrick.cu", "exa_api.cpp"]
-HEADERS = ["exa_device.cuh", "exa_accel.cuh", "exa_host.h", "exa_mesh.cuh", "exa_surrogate.cuh"]
+HEADERS = ["exa_device.cuh", "exa_accel.cuh", "exa_host.h", "exa_mesh.cuh", "exa_surrogate.cuh", "exa_tcgen05.cuh"]
 
 
 def nvcc():

@@ -436,30 +436,44 @@ __global__ void __launch_bounds__(kMajThreads, 16) k_gridlet_majorants(const exa
 // holding the corner.  A macrocell's update is then the min / max over the
 // corners whose three unions contain it, which is reduced one axis at a
 // time: along x for every corner row and macrocell column (the corners of a
-// column are an interval [ca, cb] of the row), then over the y x z
-// rectangle of rows of each macrocell; one atomic min / max per touched
-// macrocell.  Min and max are exact, so the result is the per-cell loop's.
+// column are an interval [ca, cb] of the row), then along y for every
+// macrocell column and row and corner plane, then along z; one atomic min /
+// max per touched macrocell.  Min and max are exact, so the result is the
+// per-cell loop's.  The gridlet's own range (every scalar) is the min / max
+// of the x step's results when every corner along x lies in some column.
 //
 // A gridlet takes this path when its brick is staged (<= kBrickCap floats,
 // so <= 8 cells per axis), its macrocell window is at most kSepWin wide on
-// every axis and every macrocell's corner set is an interval; the others
-// are appended to a list for k_gridlet_majorants.
+// every axis and every macrocell's corner set is an interval; the others are
+// appended to a list for k_gridlet_majorants.  Where the y step's results do
+// not fit beside the x step's (the widest windows), the y and z steps run as
+// one, over each window macrocell's rectangle of corner rows.
 constexpr int kSepWarps = 4;      // warps (independent gridlet pipelines) per block
 constexpr int kSepWin = 9;        // macrocells per axis of a gridlet's window
-constexpr int kSepRows = 81;      // corner rows (y, z) of an 8^3-cell gridlet
+constexpr int kSepPool = 729;     // (min, max) entries of the x and y steps
 
 struct alignas(16) SepWarpSmem {
   float brick[kBrickCap];
-  float2 rx[kSepWin * kSepRows];  // (min, max) per (macrocell column, corner row)
+  float2 pool[kSepPool];          // x step: (column, corner row); then y step: (column, row, corner plane)
   int2 cellRange[3][8];           // per axis and cell index: its macrocell range
   int2 cornerIv[3][kSepWin];      // per axis and window macrocell: corners [ca, cb]
   GridletPlan plan;               // of the gridlet whose brick is staged
   uint64_t bar;
 };
 
+// k / d for 0 <= k < 2048 and k * d < 2^21 (every index decoded below:
+// k < 729, d <= 81) as a multiply and a shift: with inv = 2^21 / d + 1 the
+// product k * inv / 2^21 exceeds k / d by less than k / 2^21 < 1 / d, which
+// cannot reach the next integer, and k * inv stays below 2^32
+struct SepDiv {
+  uint32_t inv;
+  EXA_D explicit SepDiv(int d) : inv((1u << 21) / (uint32_t)d + 1u) {}
+  EXA_D int operator()(int k) const { return (int)(((uint32_t)k * inv) >> 21); }
+};
+
 // One staging buffer per warp: the next gridlet's brick is copied in as soon
 // as the current one's corners are reduced along x, so the copy runs during
-// the current gridlet's macrocell updates (and, at 9.4 KB of shared memory
+// the current gridlet's macrocell updates (and, at 9.3 KB of shared memory
 // per warp, 24 warps per SM hide what it does not cover).
 __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
     const exa_gridlet *__restrict__ gridlets, size_t ng, const float *__restrict__ scalars, size_t nScalars,
@@ -471,31 +485,43 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
   const unsigned lane = threadIdx.x & 31;
   const size_t w0 = (size_t)blockIdx.x * kSepWarps + (threadIdx.x >> 5);
   const size_t stride = (size_t)gridDim.x * kSepWarps;
-  const V3i D = {dims.x, dims.y, dims.z};
-  // lane 0 stages a gridlet: its plan and the bulk copy of its brick (the
-  // buffer's readers are done: a __syncwarp precedes every call)
+  // the warp stages a gridlet (every lane calls this, with the same header;
+  // the buffer's readers are done: a __syncwarp precedes every call): lane 0
+  // plans the brick and issues its bulk copy, lanes 1..6 project the
+  // gridlet's box on the grid, one bound of one axis each (projectOnGrid)
   auto prepare = [&](const exa_gridlet &hdr) {
     GridletPlan &pl = sm.plan;
-    pl.g = hdr;
-    pl.P = brick_plan(pl.g, nScalars, stage);
-    if (pl.P.bulk) {
-      fence_proxy_async_smem();
-      bulk_load_smem(sm.brick, scalars + pl.P.f0, pl.P.bulk, &sm.bar);
+    if (lane == 0) {
+      pl.g = hdr;
+      pl.P = brick_plan(hdr, nScalars, stage);
+      if (pl.P.bulk) {
+        fence_proxy_async_smem();
+        bulk_load_smem(sm.brick, scalars + pl.P.f0, pl.P.bulk, &sm.bar);
+      }
+    } else if (lane <= 6) {
+      const int a = (int)(lane - 1) % 3;
+      const bool upper = lane > 3;
+      const int lower = a == 0 ? hdr.lower.x : a == 1 ? hdr.lower.y : hdr.lower.z;
+      const int cells = a == 0 ? hdr.dims.x : a == 1 ? hdr.dims.y : hdr.dims.z;
+      const float cw = (float)(1 << hdr.level);
+      const float v = upper ? (((float)lower + (float)cells) + 0.5f) * cw : ((float)lower + 0.5f) * cw;
+      const float wlo = a == 0 ? wb.lower.x : a == 1 ? wb.lower.y : wb.lower.z;
+      const float whi = a == 0 ? wb.upper.x : a == 1 ? wb.upper.y : wb.upper.z;
+      const int n = a == 0 ? dims.x : a == 1 ? dims.y : dims.z;
+      // project_on_grid, one component
+      const int m = iclamp((int)(((v - wlo) / (whi - wlo)) * (float)n), 0, n - 1);
+      V3i &dst = upper ? pl.hiMC : pl.loMC;
+      if (a == 0) dst.x = m;
+      else if (a == 1) dst.y = m;
+      else dst.z = m;
     }
-    const float cw = (float)(1 << hdr.level);
-    const V3 lo = mk3(((float)hdr.lower.x + 0.5f) * cw, ((float)hdr.lower.y + 0.5f) * cw,
-                      ((float)hdr.lower.z + 0.5f) * cw);
-    const V3 hi = mk3((((float)hdr.lower.x + (float)hdr.dims.x) + 0.5f) * cw,
-                      (((float)hdr.lower.y + (float)hdr.dims.y) + 0.5f) * cw,
-                      (((float)hdr.lower.z + (float)hdr.dims.z) + 0.5f) * cw);
-    pl.loMC = project_on_grid(lo, D, wb);
-    pl.hiMC = project_on_grid(hi, D, wb);
   };
   if (lane == 0) {
     mbar_init(&sm.bar);
     mbar_init_fence();
-    if (w0 < ng) prepare(gridlets[w0]);
   }
+  __syncwarp();
+  if (w0 < ng) prepare(gridlets[w0]);
   __syncwarp();
   const V3 mcSize = div3(sub3(mk3(wb.upper), mk3(wb.lower)), mk3((float)dims.x, (float)dims.y, (float)dims.z));
   uint32_t parity = 0;
@@ -504,6 +530,10 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
     const BrickPlan P = sm.plan.P;
     const V3i loMC = sm.plan.loMC, hiMC = sm.plan.hiMC;
     const size_t gn = gi + stride;
+    // the next gridlet's header is loaded now and planned after this one's
+    // x step, when the load has long arrived
+    exa_gridlet next{};
+    if (gn < ng) next = gridlets[gn];
     bool ok = true;
     if (P.bulk) {
       ok = mbar_wait(&sm.bar, parity);
@@ -524,11 +554,17 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
                wz <= kSepWin;
     const int nx = g.dims.x + 1, ny = g.dims.y + 1, nz = g.dims.z + 1;
     const int rows = ny * nz;
+    // the x step's results and, when they fit beside them, the y step's
+    // (else the y and z steps run as one, over the rectangle of rows)
+    sep = sep && wx * rows <= kSepPool;
+    const bool yStep = wx * rows + wx * wy * nz <= kSepPool;
     float *B = sm.brick;
+    bool fold = false;
     if (sep) {
       for (int k = lane; k < P.tail; k += 32) B[P.bulk / 4 + k] = __ldg(scalars + P.f0 + P.bulk / 4 + k);
       // each cell's macrocell range along each axis
       const float cw = (float)(1 << g.level), hc = 0.5f * cw;
+      bool xEmpty = false;
       if (lane < g.dims.x + g.dims.y + g.dims.z) {
         const int a = (int)lane < g.dims.x ? 0 : (int)lane < g.dims.x + g.dims.y ? 1 : 2;
         const int i = a == 0 ? lane : a == 1 ? lane - g.dims.x : lane - g.dims.x - g.dims.y;
@@ -543,65 +579,87 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
         mc_axis_range((float)(lower + i) * cw + hc, (float)(lower + i + 1) * cw + hc, wlo, whi, size, n, lo, hi, m0,
                       m1);
         sm.cellRange[a][i] = make_int2(m0, m1);
+        xEmpty = a == 0 && m1 < m0;
       }
+      // every corner along x is in some column's interval when every cell
+      // along x reaches a macrocell
+      fold = !__any_sync(0xffffffffu, xEmpty) && g.dims.x > 0 && g.dims.y > 0 && g.dims.z > 0;
       __syncwarp();
       // per axis and window macrocell: the corners whose cells reach it, an
       // interval [ca, cb] (empty: ca > cb); a gap sends the gridlet to the
-      // general kernel
+      // general kernel.  Nine lanes per window macrocell, one corner index
+      // each; the ballot gives the macrocell's corner set.
       bool gap = false;
-      if (lane < wx + wy + wz) {
-        const int a = (int)lane < wx ? 0 : (int)lane < wx + wy ? 1 : 2;
-        const int off = a == 0 ? lane : a == 1 ? lane - wx : lane - wx - wy;
-        const int m = off + (a == 0 ? loMC.x : a == 1 ? loMC.y : loMC.z);
-        const int d = a == 0 ? g.dims.x : a == 1 ? g.dims.y : g.dims.z;
-        int ca = 1 << 20, cb = -1;
-        for (int j = 0; j <= d; ++j) {
-          bool in = false;
-          if (j > 0) { const int2 r = sm.cellRange[a][j - 1]; in = in || (r.x <= m && m <= r.y); }
-          if (j < d) { const int2 r = sm.cellRange[a][j]; in = in || (r.x <= m && m <= r.y); }
-          if (in) {
-            if (cb >= 0 && cb != j - 1) gap = true;
-            if (ca > j) ca = j;
-            cb = j;
+      const int nMC = wx + wy + wz;
+      const int q = (int)lane / 9, j = (int)lane - 9 * q;
+      for (int t0 = 0; t0 < nMC; t0 += 3) {
+        const int t = t0 + q;
+        const bool mine = q < 3 && t < nMC;
+        int a = 0, off = 0, d = 0;
+        bool in = false;
+        if (mine) {
+          a = t < wx ? 0 : t < wx + wy ? 1 : 2;
+          off = a == 0 ? t : a == 1 ? t - wx : t - wx - wy;
+          const int m = off + (a == 0 ? loMC.x : a == 1 ? loMC.y : loMC.z);
+          d = a == 0 ? g.dims.x : a == 1 ? g.dims.y : g.dims.z;
+          if (j <= d) {
+            if (j > 0) { const int2 r = sm.cellRange[a][j - 1]; in = in || (r.x <= m && m <= r.y); }
+            if (j < d) { const int2 r = sm.cellRange[a][j]; in = in || (r.x <= m && m <= r.y); }
           }
         }
-        sm.cornerIv[a][off] = make_int2(ca, cb);
+        const unsigned bits = (__ballot_sync(0xffffffffu, in) >> (9 * (q < 3 ? q : 0))) & 0x1ffu;
+        if (mine && j == 0) {
+          if (bits) {
+            const int ca = __ffs(bits) - 1, cb = 31 - __clz(bits);
+            gap = gap || bits != (((2u << cb) - 1u) & ~((1u << ca) - 1u));
+            sm.cornerIv[a][off] = make_int2(ca, cb);
+          } else {
+            sm.cornerIv[a][off] = make_int2(1 << 20, -1);
+          }
+        }
       }
       sep = !__any_sync(0xffffffffu, gap);
       __syncwarp();
     }
     if (!sep) {
-      if (lane == 0) {
-        fallback[atomicAdd(fallbackCount, 1u)] = (uint32_t)gi;
-        if (gn < ng) prepare(gridlets[gn]);
-      }
+      if (lane == 0) fallback[atomicAdd(fallbackCount, 1u)] = (uint32_t)gi;
+      __syncwarp();
+      if (gn < ng) prepare(next);
       __syncwarp();
       continue;
     }
     // the gridlet's own range: over every scalar (cell-less gridlets: empty)
     float glo = 1e30f, ghi = -1e30f;
-    if (g.dims.x > 0 && g.dims.y > 0 && g.dims.z > 0)
+    if (!fold && g.dims.x > 0 && g.dims.y > 0 && g.dims.z > 0)
       for (int k = lane; k < nx * rows; k += 32) {
         const float v = B[P.lead + k];
         glo = fminf(glo, v);
         ghi = fmaxf(ghi, v);
       }
     // along x: every (macrocell column, corner row)
-    for (int k = lane; k < wx * rows; k += 32) {
-      const int m = k / rows, r = k - m * rows;
-      const int2 iv = sm.cornerIv[0][m];
-      const float *R = B + P.lead + r * nx;
-      float lo = 1e30f, hi = -1e30f;
-      for (int j = iv.x; j <= iv.y; ++j) {
-        const float v = R[j];
-        lo = fminf(lo, v);
-        hi = fmaxf(hi, v);
+    float2 *X = sm.pool;
+    {
+      const SepDiv byRows(rows);
+      for (int k = lane; k < wx * rows; k += 32) {
+        const int m = byRows(k), r = k - m * rows;
+        const int2 iv = sm.cornerIv[0][m];
+        const float *R = B + P.lead + r * nx;
+        float lo = 1e30f, hi = -1e30f;
+        for (int c = iv.x; c <= iv.y; ++c) {
+          const float v = R[c];
+          lo = fminf(lo, v);
+          hi = fmaxf(hi, v);
+        }
+        X[k] = make_float2(lo, hi);
+        if (fold) {
+          glo = fminf(glo, lo);
+          ghi = fmaxf(ghi, hi);
+        }
       }
-      sm.rx[k] = make_float2(lo, hi);
     }
     // the brick is read: the next gridlet's copy runs from here on
     __syncwarp();
-    if (lane == 0 && gn < ng) prepare(gridlets[gn]);
+    if (gn < ng) prepare(next);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
@@ -611,19 +669,55 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
       gridletRanges[gi].lower = glo;
       gridletRanges[gi].upper = ghi;
     }
-    // over the y x z rectangle of rows of each window macrocell
-    for (int k = lane; k < wx * wy * wz; k += 32) {
-      const int mx = k % wx, my = (k / wx) % wy, mz = k / (wx * wy);
-      const int2 iy = sm.cornerIv[1][my], iz = sm.cornerIv[2][mz];
-      const float2 *X = sm.rx + mx * rows;
-      float lo = 1e30f, hi = -1e30f;
-      for (int cz = iz.x; cz <= iz.y; ++cz)
+    const SepDiv byX(wx), byXY(wx * wy);
+    if (yStep) {
+      // along y: every (macrocell column, macrocell row, corner plane)
+      float2 *Y = sm.pool + wx * rows;
+      const SepDiv byZ(nz), byY(wy);
+      for (int k = lane; k < wx * wy * nz; k += 32) {
+        const int k1 = byZ(k), cz = k - k1 * nz;
+        const int mx = byY(k1), my = k1 - mx * wy;
+        const int2 iy = sm.cornerIv[1][my];
+        const float2 *S = X + mx * rows + cz * ny;
+        float lo = 1e30f, hi = -1e30f;
         for (int cy = iy.x; cy <= iy.y; ++cy) {
-          const float2 v = X[cz * ny + cy];
+          const float2 v = S[cy];
           lo = fminf(lo, v.x);
           hi = fmaxf(hi, v.y);
         }
-      if (lo <= hi) update_mc(mcRanges, dims, loMC.x + mx, loMC.y + my, loMC.z + mz, lo, hi);
+        Y[k] = make_float2(lo, hi);
+      }
+      __syncwarp();
+      // along z: every window macrocell
+      for (int k = lane; k < wx * wy * wz; k += 32) {
+        const int mz = byXY(k), kxy = k - mz * wx * wy;
+        const int my = byX(kxy), mx = kxy - my * wx;
+        const int2 iz = sm.cornerIv[2][mz];
+        const float2 *S = Y + (mx * wy + my) * nz;
+        float lo = 1e30f, hi = -1e30f;
+        for (int cz = iz.x; cz <= iz.y; ++cz) {
+          const float2 v = S[cz];
+          lo = fminf(lo, v.x);
+          hi = fmaxf(hi, v.y);
+        }
+        if (lo <= hi) update_mc(mcRanges, dims, loMC.x + mx, loMC.y + my, loMC.z + mz, lo, hi);
+      }
+    } else {
+      // wide windows: per window macrocell over its y x z rectangle of rows
+      for (int k = lane; k < wx * wy * wz; k += 32) {
+        const int mz = byXY(k), kxy = k - mz * wx * wy;
+        const int my = byX(kxy), mx = kxy - my * wx;
+        const int2 iy = sm.cornerIv[1][my], iz = sm.cornerIv[2][mz];
+        const float2 *S = X + mx * rows;
+        float lo = 1e30f, hi = -1e30f;
+        for (int cz = iz.x; cz <= iz.y; ++cz)
+          for (int cy = iy.x; cy <= iy.y; ++cy) {
+            const float2 v = S[cz * ny + cy];
+            lo = fminf(lo, v.x);
+            hi = fmaxf(hi, v.y);
+          }
+        if (lo <= hi) update_mc(mcRanges, dims, loMC.x + mx, loMC.y + my, loMC.z + mz, lo, hi);
+      }
     }
     // the tables and the plan are free for the next gridlet
     __syncwarp();
