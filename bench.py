@@ -481,7 +481,7 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
                      "exact_field_samples": int(c[0]), "learned_samples": int(c[10]),
                      "majorant_violations": int(c[11])}
     r.learned = False
-    conv = converged_rmse(a, r, lo, hi)
+    conv = converged_rmse(a, r, lo, hi, S)
     # point queries: learned value vs exact sample at 1M uniform points
     rng = np.random.default_rng(42)
     P = rng.uniform(lo, hi, (1 << 20, 3)).astype(np.float32)
@@ -530,13 +530,15 @@ def run_learned(a, local, ds, num_mcs, flush, timed=3, log2T=19):
     return out
 
 
-def converged_rmse(a, r, lo, hi, div=16, spp=256, frames=16):
+def converged_rmse(a, r, lo, hi, S, div=16, spp=256, frames=16, tolerances=(0.01, 0.005), default_tol=0.02):
     """The learned field's bias on a converged image: the frame's camera at
     1/div of its resolution, frames x spp samples per pixel accumulated
     progressively, rendered three times -- exact, exact with other random
     numbers (frameID 1), learned -- and the RMSE of each pair.  The two exact
     images differ by noise only, so their RMSE is the noise floor a bias has
-    to show above."""
+    to show above.  Then the learned image again with the per-macrocell
+    fallback at each tighter error tolerance (more macrocells on the exact
+    sampler), and the evaluation back at the default tolerance."""
     from helpers import orbit_camera, setup_render
     from owlexastitcher_gb300 import exastitch as E
     w, h = max(a.width // div, 8), max(a.height // div, 8)
@@ -556,19 +558,34 @@ def converged_rmse(a, r, lo, hi, div=16, spp=256, frames=16):
         r.ctx.sync()
         imgs[name] = r.accum.cpu().numpy().reshape(-1, 4)[:, :3] / (frames * spp)
     secs = time.perf_counter() - t0
+
+    def e(x, y):
+        return float(np.sqrt(np.mean((imgs[x] - imgs[y]) ** 2)))
+    sweep = []
+    for tol in tolerances:
+        S.evaluate(tol, 1 << 24)
+        st = S.stats()
+        r.learned = True
+        r.lp.ext.frameID = 0
+        r.accumID = 0
+        for _ in range(frames):
+            r.render()
+        r.ctx.sync()
+        imgs["tol"] = r.accum.cpu().numpy().reshape(-1, 4)[:, :3] / (frames * spp)
+        sweep.append({"tolerance": tol, "fraction_learned": st["numSurrogateMacrocells"] / max(st["numMacrocells"], 1),
+                      "rmse_learned_vs_exact_other_rng": e("tol", "exact_other_rng")})
+    S.evaluate(default_tol, 1 << 24)
     r.learned = False
     r.lp.ext.frameID = 0
     (fw, fh), r.spp = saved
     r.resize(fw, fh)
     setup_render(r.lp, orbit_camera(lo, hi, fw, fh), fw, fh, E.PATH_TRACING_INTEGRATOR, r.spp, "directional", True)
     r.lp.ext.maxBounces = a.bounces
-
-    def e(x, y):
-        return float(np.sqrt(np.mean((imgs[x] - imgs[y]) ** 2)))
-    return {"width": w, "height": h, "spp": frames * spp, "seconds": secs,
+    return {"width": w, "height": h, "spp": frames * spp, "seconds": secs, "tolerance": default_tol,
             "rmse_exact_vs_exact_other_rng": e("exact", "exact_other_rng"),
             "rmse_learned_vs_exact_other_rng": e("learned", "exact_other_rng"),
-            "rmse_learned_vs_exact_same_rng": e("learned", "exact")}
+            "rmse_learned_vs_exact_same_rng": e("learned", "exact"),
+            "tighter_tolerances": sweep}
 
 
 def run_batched(a, local, flush):

@@ -1353,7 +1353,7 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, b
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
   W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
   if (fresh) return;
-  WF(w.pos.x); WF(w.pos.y); WF(w.pos.z); WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
+  k += 7;  // words 21-27 unused: a parked walk's last sample and classification are not read again
   WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
   W((uint32_t)w.primID); W((uint32_t)w.steps); W((uint32_t)w.ncells);
 }
@@ -1389,8 +1389,9 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
     w.ncells = 0;
     return;
   }
-  w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
-  w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
+  w.pos = mk3(0.f, 0.f, 0.f);
+  w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+  k += 7;
   w.t = RF(); w.t1 = RF(); w.maj = RF(); w.Tr = RF();
   w.primID = (int)R(); w.steps = (int)R(); w.ncells = (int)R();
 }
@@ -1560,6 +1561,11 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
       }
       break;
     }
+    // a step's sample position and classification are read only by the
+    // event of a walk that ends in the same iteration: cleared here, they
+    // hold no registers across iterations
+    L.w.pos = mk3(0.f, 0.f, 0.f);
+    L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
     const bool ended = active && !walk_iteration<TEASER>(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
@@ -1628,6 +1634,9 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
       break;
     }
     bool ended = false;
+    // the classification as in k_wf_walk; the position stays for a lane
+    // that waits for its learned sample
+    L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active && !pending) {
       int st, a = 0;
       do {
@@ -1937,6 +1946,8 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
       break;
     }
     bool ended = false;
+    L.w.pos = mk3(0.f, 0.f, 0.f);  // as in k_wf_walk
+    L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
       PathCtx cf{*fa, *flp, 0u, c.counting};
       ended = !walk_iteration(L.w, cf, L.rng, L.shadow);
