@@ -342,6 +342,7 @@ EXA_D void walk_begin(Walk &w, const exa_launch_params &lp, RayS ray)
   w.org = ray.org;
   w.dir = ray.dir;
   dda_init(w.dda, ray.org, ray.dir, ray.tmin, ray.tmax, lp.majorantGrid);
+  w.t = w.dda.t0;  // the walk's position along the ray: here its entry into the grid
   w.pos = mk3(0.f, 0.f, 0.f);
   w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
   w.Tr = 1.f;
@@ -371,10 +372,12 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
     cnt_add(c, CNT_DDA);
     if (!exa_in_range(leafID, (long long)G.dims.x * G.dims.y * G.dims.z, c.err)) return WALK_END;
     w.maj = __ldg(lp.maxOpacities + leafID);
-    w.t = w.dda.t0;
+    // w.t is the macrocell's entry distance: the walk's start, or the exit of
+    // the macrocell before, which is where dda_next_dir puts its t0
     w.primID = -1;  // the gridlet cache ends with the macrocell (deviceCode.cu:731-760)
     w.steps = 0;
     if (w.maj <= 0.f) {
+      w.t = w.t1;
       if (!dda_next_dir(w.dda, w.dir, G.dims)) return WALK_END;
       continue;
     }
@@ -387,6 +390,7 @@ EXA_D int walk_advance(Walk &w, PathCtx &c, Rng &rng)
   w.t -= __fdiv_rn(exa_log(1.f - rng.next()), w.maj * scale);
   if (w.t >= w.t1) {
     w.needCell = true;
+    w.t = w.t1;  // the next macrocell's entry (a walk that ends here reports no distance)
     return dda_next_dir(w.dda, w.dir, G.dims) ? WALK_ON : WALK_END;
   }
   w.pos = add3(w.org, muls(w.dir, w.t));
@@ -1351,7 +1355,7 @@ EXA_D void wf_store_walk(const Lane &L, uint32_t *b, unsigned cap, unsigned i, b
   W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 3: unused
   WF(w.org.x); WF(w.org.y); WF(w.org.z); WF(w.dir.x); WF(w.dir.y); WF(w.dir.z);
   WF(w.dda.tnext.x); WF(w.dda.tnext.y); WF(w.dda.tnext.z); WF(w.dda.dist.x); WF(w.dda.dist.y); WF(w.dda.dist.z);
-  W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.dda.t0); WF(w.dda.tmax);
+  W((uint32_t)w.dda.cell.x); W((uint32_t)w.dda.cell.y); W((uint32_t)w.dda.cell.z); WF(w.t); WF(w.dda.tmax);
   if (fresh) return;
   k += 7;  // words 21-27 unused: a parked walk's last sample and classification are not read again
   WF(w.t); WF(w.t1); WF(w.maj); WF(w.Tr);
@@ -1374,7 +1378,8 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   w.dda.tnext.x = RF(); w.dda.tnext.y = RF(); w.dda.tnext.z = RF();
   w.dda.dist.x = RF(); w.dda.dist.y = RF(); w.dda.dist.z = RF();
   w.dda.cell.x = (int)R(); w.dda.cell.y = (int)R(); w.dda.cell.z = (int)R();
-  w.dda.t0 = RF(); w.dda.tmax = RF();
+  w.t = RF(); w.dda.tmax = RF();
+  w.dda.t0 = w.t;
   // step / stop follow from the ray direction as in dda_init
   w.dda.step.x = w.dir.x > 0.f ? 1 : -1; w.dda.step.y = w.dir.y > 0.f ? 1 : -1; w.dda.step.z = w.dir.z > 0.f ? 1 : -1;
   w.dda.stop.x = w.dir.x > 0.f ? G.dims.x : -1; w.dda.stop.y = w.dir.y > 0.f ? G.dims.y : -1;
@@ -1382,7 +1387,7 @@ EXA_D void wf_load_walk(Lane &L, const uint32_t *__restrict__ b, unsigned cap, u
   if (flags & kWalkFresh) {
     w.pos = mk3(0.f, 0.f, 0.f);
     w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
-    w.t = w.t1 = w.maj = 0.f;
+    w.t1 = w.maj = 0.f;
     w.Tr = 1.f;
     w.primID = -1;
     w.steps = 0;
@@ -1561,11 +1566,12 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
       }
       break;
     }
-    // a step's sample position and classification are read only by the
-    // event of a walk that ends in the same iteration: cleared here, they
-    // hold no registers across iterations
+    // a step's sample position and classification, and the kind of end, are
+    // read only by the event of a walk that ends in the same iteration:
+    // cleared here, they hold no registers across iterations
     L.w.pos = mk3(0.f, 0.f, 0.f);
     L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+    L.w.type = BOUNDARY;
     const bool ended = active && !walk_iteration<TEASER>(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
@@ -1637,6 +1643,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     // the classification as in k_wf_walk; the position stays for a lane
     // that waits for its learned sample
     L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+    L.w.type = BOUNDARY;
     if (active && !pending) {
       int st, a = 0;
       do {
@@ -1948,6 +1955,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wfb_walk(const _
     bool ended = false;
     L.w.pos = mk3(0.f, 0.f, 0.f);  // as in k_wf_walk
     L.w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+    L.w.type = BOUNDARY;
     if (active) {
       PathCtx cf{*fa, *flp, 0u, c.counting};
       ended = !walk_iteration(L.w, cf, L.rng, L.shadow);
