@@ -266,7 +266,7 @@ def run_ours(a):
     r.lp.ext.stepCounters = None
     c = cnt.cpu().numpy()
     field_samples, g_samples, e_samples, dda_cells, paths = (int(x) for x in c[:5])
-    work = dict(zip(["cache_misses", "table_queries", "gridlet_tests", "bvh_walks", "walks"],
+    work = dict(zip(["cache_misses", "table_queries", "gridlet_tests", "element_list_walks", "walks"],
                     (int(x) for x in c[5:10])))
     counts = np.count_nonzero(ds.indices >= 0, axis=1) if len(ds.indices) else np.array([8])
     avg_nv = float(counts.mean())

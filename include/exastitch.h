@@ -40,7 +40,7 @@ extern "C" {
 /* device error-flag bits (exa_get_device_errors) */
 #define EXA_DEVERR_DDA_CAP      1u  /* DDA walked more cells than the grid has */
 #define EXA_DEVERR_TRACK_CAP    2u  /* delta/ratio tracking step cap            */
-#define EXA_DEVERR_BVH_STACK    4u  /* element-BVH traversal stack overflow     */
+#define EXA_DEVERR_BVH_STACK    4u  /* reserved (element point location keeps no stack) */
 #define EXA_DEVERR_BOUNCE_CAP   8u  /* reserved (paths end at ext.maxBounces)    */
 #define EXA_DEVERR_WATCHDOG    16u  /* persistent-kernel work loop cap          */
 #define EXA_DEVERR_COPY_WAIT   32u  /* bulk copy to shared memory: wait limit   */
@@ -189,7 +189,7 @@ typedef struct {
                              /* [2] element samples, [3] DDA cells,          */
                              /* [4] paths; wavefront renderer also: [5]      */
                              /* gridlet-cache misses, [6] table queries,     */
-                             /* [7] gridlet tests, [8] element-BVH walks,     */
+                             /* [7] gridlet tests, [8] element cell-list walks, */
                              /* [9] walks, [10] learned-field samples,       */
                              /* [11] learned samples limited to the         */
                              /* macrocell's widened majorant                 */
@@ -286,7 +286,7 @@ typedef struct {
   uint64_t emptyScalarsBytes;
   uint64_t nonEmptyScalarsBytes;
   uint64_t deviceFieldBytes;     /* field arrays resident in HBM           */
-  uint64_t deviceAccelBytes;     /* point-location tables + element BVH     */
+  uint64_t deviceAccelBytes;     /* gridlet tables + element cell lists      */
   uint64_t deviceMajorantBytes;  /* value ranges + max opacities            */
   uint64_t amrCellBytes;         /* AMR-cell model: cells (AMRCellModel::memStats) */
   uint64_t amrScalarBytes;       /* AMR-cell model: scalars                 */
@@ -458,7 +458,7 @@ int exa_model_mem_stats(exa_context *ctx, exa_mem_stats *out);
 
 /* ExaStitchSampler::build (sampler/ExaStitchSampler.cpp:23-340): uploads
  * the field, builds the per-primitive value ranges, the point-location
- * accel (gridlet tables + element BVH, replacing the OptiX TLAS) and the
+ * accel (gridlet tables + element cell lists, replacing the OptiX TLAS) and the
  * majorant grid (Grid::build, Grid.cu:457-594).  EXA_ERR_STATE where the
  * reference returns false. */
 int exa_sampler_build(exa_context *ctx);

@@ -10,9 +10,11 @@
 // the single gridlet whose extent meets the block's open interior, or an
 // ascending list.  A query on an exact block face also looks at the
 // neighbouring block, so the reference's inclusive box test is honoured.
-// Stitching elements: a linear BVH (Karras 2012, "Maximizing parallelism in
-// the construction of BVHs, octrees and k-d trees") built on the GPU; each
-// 64-byte node stores both child boxes and child max opacities.
+// Stitching elements: a uniform grid of cells over the elements' bounds
+// (about two finest-cell widths wide); a bit per cell marks the cells that
+// some element's closed AABB touches, and each marked cell lists those
+// elements in ascending order, so the first element that holds the point
+// is the lowest-index one.
 //
 // Canonical answer when several primitives contain the point (shared
 // faces): the lowest-index gridlet, else the lowest-index element.
@@ -44,16 +46,24 @@ struct BvhNode {   // 64 B: two child boxes, two child refs, two opacities
   float op[2];          // max opacity of each child subtree
 };
 
-// Conservative element occupancy: one bit per cell of a uniform grid over
-// the elements' bounds, set where any element's closed AABB touches the
-// cell.  cell(p) = floor((p - origin) / cellSize) is monotonic in p, so a
-// point inside an element's AABB always maps to a marked cell; a clear bit
-// proves no element contains the point.
+// Element cells: one bit per cell of a uniform grid over the elements'
+// bounds, set where any element's closed AABB touches the cell.
+// cell(p) = floor((p - origin) / cellSize) is monotonic in p, so a point
+// inside an element's AABB always maps to a marked cell that lists the
+// element; a clear bit proves no element contains the point.  Marked cells
+// are numbered in cell order (rank: the marked cells before each 32-cell
+// word); entry of a marked cell: >= 0 its only element, <= -2 a list at
+// items[-e-2] (count, then the ids ascending).
 struct ElemOccupancy {
   float origin[3];
   float cellSize[3];
   int n[3];
   const uint32_t *bits;
+  const uint32_t *rank;
+  const int32_t *entries;
+  const int32_t *items;
+  const float4 *boxes;     // per element its closed AABB: (lo, hi.x), (hi.y, hi.z, 0, 0)
+  int numMarked, numItems;
 };
 
 // AMR cells (the comparison sampler of sampler/AMRCellSampler.h): per level
@@ -93,7 +103,6 @@ struct AccelView {
   const float4 *vertices;
   const int32_t *indices;
   const float *elemMaxOps;      // may be null
-  const BvhNode *nodes;
   int numGridlets;
   int numElems;
   int numTables;
@@ -110,22 +119,12 @@ EXA_HD int occ_coord(float p, float origin, float cs, int n)
   return f < 0.f ? -1 : (f >= (float)n ? n : (int)f);
 }
 
-// false: no element's AABB contains pos
-EXA_D bool occ_maybe(const ElemOccupancy &O, V3 pos)
-{
-  const int x = occ_coord(pos.x, O.origin[0], O.cellSize[0], O.n[0]);
-  const int y = occ_coord(pos.y, O.origin[1], O.cellSize[1], O.n[1]);
-  const int z = occ_coord(pos.z, O.origin[2], O.cellSize[2], O.n[2]);
-  if (x < 0 || y < 0 || z < 0 || x >= O.n[0] || y >= O.n[1] || z >= O.n[2]) return false;
-  const size_t c = ((size_t)z * O.n[1] + y) * O.n[0] + x;
-  return (__ldg(O.bits + (c >> 5)) >> (c & 31)) & 1u;
-}
 
 EXA_D int floor_div_pow2(int v, int shift) { return v >> shift; }  // arithmetic shift floors
 
 // optional per-thread work counters of the point query (counting launches)
 struct QueryStats {
-  unsigned tables, gridletTests, bvhWalks;
+  unsigned tables, gridletTests, elemLists;
 };
 
 // the block of table T holding pos, and whether pos lies on the block's low
@@ -197,63 +196,53 @@ EXA_D bool box_contains(const float *lo, const float *hi, V3 p)
   return lo[0] <= p.x && lo[1] <= p.y && lo[2] <= p.z && p.x <= hi[0] && p.y <= hi[1] && p.z <= hi[2];
 }
 
-// full traversal: lowest-index containing element; returns false on stack
-// overflow (error flag raised by the caller).  Out of line: element samples
-// are rare next to gridlet samples, and keeping the BVH walk and the three
-// Newton solvers out of the tracking loop keeps that loop's code small.
-static __device__ __noinline__ bool query_elements(const AccelView &A, V3 pos, bool cull, int &best, float &bestVal,
-                                                   uint32_t &err)
+// the lowest-index element that holds pos (its closed AABB, then the
+// element's own test), -1 if none.  Out of line: element samples are rare
+// next to gridlet samples, and keeping the list walk and the three Newton
+// solvers out of the tracking loop keeps that loop's code small.
+static __device__ __noinline__ int query_elements(const AccelView &A, V3 pos, bool cull, float &val, uint32_t &err,
+                                                  QueryStats *qs)
 {
-  if (A.numElems <= 0) return true;
-  int stack[kBvhStack];
-  int sp = 0;
-  int node = 0;
-  const bool useOps = cull && A.elemMaxOps;
-  // a well-formed tree visits each of its numElems-1 nodes at most once
-  for (int visits = 0; visits <= A.numElems + 1; ++visits) {
-    if (!exa_in_range(node, A.numElems > 1 ? A.numElems - 1 : 1, err)) return true;
-    const float4 *np = reinterpret_cast<const float4 *>(A.nodes + node);
-    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-    const float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
-    const float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
-    const int c0 = __float_as_int(q3.x), c1 = __float_as_int(q3.y);
-    const bool in0 = box_contains(lo0, hi0, pos) && !(useOps && q3.z == 0.f);
-    const bool in1 = box_contains(lo1, hi1, pos) && !(useOps && q3.w == 0.f);
-    int next = -1;
-    if (in0) {
-      if (c0 < 0) {
-        const int e = ~c0;
-        float v;
-        if (e < best && exa_in_range(e, A.numElems, err) && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) {
-          best = e;
-          bestVal = v;
-        }
-      } else {
-        next = c0;
-      }
-    }
-    if (in1) {
-      if (c1 < 0) {
-        const int e = ~c1;
-        float v;
-        if (e < best && exa_in_range(e, A.numElems, err) && intersect_elem(v, pos, A.indices + (size_t)e * 8, A.vertices)) {
-          best = e;
-          bestVal = v;
-        }
-      } else if (next < 0) {
-        next = c1;
-      } else {
-        if (sp >= kBvhStack) return false;
-        stack[sp++] = c1;
-      }
-    }
-    if (next < 0) {
-      if (sp == 0) return true;
-      next = stack[--sp];
-    }
-    node = next;
+  const ElemOccupancy &O = A.occ;
+  const int x = occ_coord(pos.x, O.origin[0], O.cellSize[0], O.n[0]);
+  const int y = occ_coord(pos.y, O.origin[1], O.cellSize[1], O.n[1]);
+  const int z = occ_coord(pos.z, O.origin[2], O.cellSize[2], O.n[2]);
+  if (x < 0 || y < 0 || z < 0 || x >= O.n[0] || y >= O.n[1] || z >= O.n[2]) return -1;
+  const size_t c = ((size_t)z * O.n[1] + y) * O.n[0] + x;
+  // the word's bits and its rank do not depend on each other: both loads
+  // are in flight together
+  const uint32_t word = __ldg(O.bits + (c >> 5));
+  const uint32_t before = __ldg(O.rank + (c >> 5));
+  const uint32_t bit = 1u << (c & 31);
+  if (!(word & bit)) return -1;
+  if (qs) qs->elemLists++;
+  const int m = (int)(before + __popc(word & (bit - 1u)));
+  if (!exa_in_range(m, O.numMarked, err)) return -1;
+  const int e = __ldg(O.entries + m);
+  if (e == -1) return -1;  // (a marked cell always lists an element)
+  int cnt = 1;
+  const int32_t *list = nullptr;
+  if (e <= -2) {
+    if (!exa_in_range(-e - 2, O.numItems, err)) return -1;
+    list = O.items + (-e - 2);
+    cnt = __ldg(list);
+    if (!exa_in_range(-e - 2 + cnt, O.numItems, err)) return -1;
   }
-  return false;
+  const bool useOps = cull && A.elemMaxOps;
+  for (int k = 0; k < cnt; ++k) {
+    const int id = list ? __ldg(list + 1 + k) : e;
+    if (!exa_in_range(id, A.numElems, err)) continue;
+    if (useOps && __ldg(A.elemMaxOps + id) == 0.f) continue;
+    const float4 b0 = __ldg(O.boxes + 2 * (size_t)id), b1 = __ldg(O.boxes + 2 * (size_t)id + 1);
+    const float lo[3] = {b0.x, b0.y, b0.z}, hi[3] = {b0.w, b1.x, b1.y};
+    if (!box_contains(lo, hi, pos)) continue;
+    float v;
+    if (intersect_elem(v, pos, A.indices + (size_t)id * 8, A.vertices)) {
+      val = v;
+      return id;  // lists are ascending: the first hit is the lowest index
+    }
+  }
+  return -1;
 }
 
 // sample() (sampler/ExaStitchSampler.h:128-140); sets EXA_DEVERR bits in err
@@ -422,13 +411,9 @@ EXA_D exa_sample sample_elements(const AccelView &A, V3 pos, bool cull, uint32_t
   s.primID = -1;
   s.cellID = -1;
   s.value = 0.f;
-  int be = 0x7fffffff;
   float ev = 0.f;
-  if (A.numElems > 0 && occ_maybe(A.occ, pos)) {
-    if (qs) qs->bvhWalks++;
-    if (!query_elements(A, pos, cull, be, ev, err)) err |= EXA_DEVERR_BVH_STACK;
-  }
-  if (be != 0x7fffffff) {
+  const int be = A.numElems > 0 ? query_elements(A, pos, cull, ev, err, qs) : -1;
+  if (be >= 0) {
     s.primID = be;
     s.cellID = -1;
     s.value = ev;

@@ -160,7 +160,7 @@ size_t ExaStitchSampler::fieldBytes() const
 
 size_t ExaStitchSampler::accelBytes() const
 {
-  size_t b = bvhNodes.bytes() + bvhParents.bytes() + bvhLeafElem.bytes() + occBits.bytes();
+  size_t b = occBits.bytes() + occRank.bytes() + occEntries.bytes() + occItems.bytes() + elemBoxes.bytes();
   for (auto &t : tableEntries) b += t.bytes();
   for (auto &t : tableItems) b += t.bytes();
   return b;
@@ -328,14 +328,10 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
   }
 }
 
-void ExaStitchSampler::buildElementBVH(cudaStream_t s)
+void ExaStitchSampler::buildElementCells(cudaStream_t s)
 {
   const size_t ne = model->indices.size() / 8;
   accel.numElems = (int)ne;
-  if (!ne) { accel.nodes = nullptr; return; }
-  bvhNodes.alloc(ne > 1 ? ne - 1 : 1);
-  bvhParents.alloc((ne > 1 ? ne - 1 : 0) + ne);
-  bvhLeafElem.alloc(ne);
   exa_box3f sb;
   sb.lower = {INFINITY, INFINITY, INFINITY};
   sb.upper = {-INFINITY, -INFINITY, -INFINITY};
@@ -344,9 +340,8 @@ void ExaStitchSampler::buildElementBVH(cudaStream_t s)
     sb.lower.y = std::min(sb.lower.y, v.y); sb.upper.y = std::max(sb.upper.y, v.y);
     sb.lower.z = std::min(sb.lower.z, v.z); sb.upper.z = std::max(sb.upper.z, v.z);
   }
-  launchBuildBVH(vertexBuffer.ptr, indexBuffer.ptr, ne, sb, bvhNodes.ptr, bvhParents.ptr, bvhLeafElem.ptr, s);
-  accel.nodes = bvhNodes.ptr;
-  // occupancy grid: about 2 finest-cell widths per cell, at most 2^27 cells
+  if (!ne) sb.lower = sb.upper = exa_vec3f{0.f, 0.f, 0.f};
+  // cell grid: about 2 finest-cell widths per cell, at most 2^27 cells
   ElemOccupancy &O = accel.occ;
   const float ext[3] = {sb.upper.x - sb.lower.x, sb.upper.y - sb.lower.y, sb.upper.z - sb.lower.z};
   const float org[3] = {sb.lower.x, sb.lower.y, sb.lower.z};
@@ -357,17 +352,12 @@ void ExaStitchSampler::buildElementBVH(cudaStream_t s)
     return t;
   };
   while (cells(cs) > (double)(1 << 27)) cs *= 2.f;
-  size_t nc = 1;
   for (int a = 0; a < 3; ++a) {
     O.origin[a] = org[a];
     O.cellSize[a] = cs;
     O.n[a] = (int)std::max(1.0, std::ceil((double)ext[a] / cs) + 1);
-    nc *= (size_t)O.n[a];
   }
-  const size_t words = (nc + 31) / 32;
-  occBits.alloc(words);
-  launchElemOccupancy(vertexBuffer.ptr, indexBuffer.ptr, ne, O, occBits.ptr, words, s);
-  O.bits = occBits.ptr;
+  launchElemCells(vertexBuffer.ptr, indexBuffer.ptr, ne, O, occBits, occRank, occEntries, occItems, elemBoxes, s);
 }
 
 // CUDA events recorded on a stream; times between them once it has synchronised
@@ -427,7 +417,7 @@ bool ExaStitchSampler::build(std::shared_ptr<Model> mod, cudaStream_t s)
   accel.indices = indexBuffer.ptr;
   accel.numGridlets = (int)model->gridlets.size();
   buildGridletTables(s);
-  buildElementBVH(s);
+  buildElementCells(s);
   // the majorant grid (Grid::build, Grid.cu:457-594) over cellBounds
   Grid &g = *model->grid;
   g.worldBounds = model->cellBounds;
@@ -477,9 +467,6 @@ void ExaStitchSampler::computeMaxOpacities(const exa_vec4f *cmap, int numColors,
                    gridletMaxOpacities.ptr, s);
   launchMaxOpacity(elemValueRanges.ptr, elemValueRanges.count, colorMap.ptr, numColors, xf, tfFilter, umeshMaxOpacities.ptr,
                    s);
-  if (accel.numElems > 0)
-    launchRefitBVH(vertexBuffer.ptr, indexBuffer.ptr, (size_t)accel.numElems, bvhNodes.ptr, bvhParents.ptr,
-                   bvhLeafElem.ptr, umeshMaxOpacities.ptr, false, s);
   accel.gridletMaxOps = gridletMaxOpacities.ptr;
   accel.elemMaxOps = umeshMaxOpacities.ptr;
   cudaCheck(cudaMemcpyAsync(deviceAccel.ptr, &accel, sizeof(accel), cudaMemcpyHostToDevice, s), "accel handle");
@@ -695,7 +682,7 @@ struct exa_context {
 };
 
 // the context's surface mesh: float4 vertices, 8-int triangle rows (a, b, c,
-// then -1: the element BVH builder's row format), its BVH and the device
+// then -1: the LBVH builder's row format), its BVH and the device
 // copy of the view the kernels trace
 struct MeshState {
   DBuf<float4> vertices;
@@ -717,10 +704,9 @@ struct BatchState {
   exa_vec3i dims{0, 0, 0};
   DBuf<exa_range1f> ranges;
   std::vector<DBuf<float>> maxOps;  // per transfer function, on dims
-  // per transfer function: primitive max opacities, the element BVH refit
-  // with them, and the point-location view that culls by them
+  // per transfer function: primitive max opacities and the point-location
+  // view that culls by them
   std::vector<DBuf<float>> gOps, eOps;
-  std::vector<DBuf<BvhNode>> nodes;
   DBuf<AccelView> accels;
   int tileW = 16;
   DBuf<exa_launch_params> lps;
@@ -1928,14 +1914,12 @@ void rebuildBatchMajorants(exa_context *ctx, BatchState &B)
 void rebuildBatchCulling(exa_context *ctx, BatchState &B)
 {
   ExaStitchSampler &S = esSampler(ctx);
-  const size_t ng = S.gridletValueRanges.count, ne = (size_t)S.accel.numElems;
+  const size_t ng = S.gridletValueRanges.count;
   const size_t nt = B.tfColors.size();
   B.gOps.clear();
   B.eOps.clear();
-  B.nodes.clear();
   B.gOps.resize(nt);
   B.eOps.resize(nt);
-  B.nodes.resize(nt);
   std::vector<AccelView> views(nt, S.accel);
   for (size_t t = 0; t < nt; ++t) {
     B.gOps[t].alloc(std::max<size_t>(ng, 1));
@@ -1944,14 +1928,6 @@ void rebuildBatchCulling(exa_context *ctx, BatchState &B)
                      ctx->stream);
     launchMaxOpacity(S.elemValueRanges.ptr, S.elemValueRanges.count, B.tfColors[t].ptr, B.tfCount[t], B.tfRange[t], S.tfFilter,
                      B.eOps[t].ptr, ctx->stream);
-    if (ne > 0) {
-      B.nodes[t].alloc(S.bvhNodes.count);
-      cudaCheck(cudaMemcpyAsync(B.nodes[t].ptr, S.bvhNodes.ptr, S.bvhNodes.bytes(), cudaMemcpyDeviceToDevice,
-                                ctx->stream), "copy BVH");
-      launchRefitBVH(S.vertexBuffer.ptr, S.indexBuffer.ptr, ne, B.nodes[t].ptr, S.bvhParents.ptr, S.bvhLeafElem.ptr,
-                     B.eOps[t].ptr, false, ctx->stream);
-      views[t].nodes = B.nodes[t].ptr;
-    }
     views[t].gridletMaxOps = B.gOps[t].ptr;
     views[t].elemMaxOps = B.eOps[t].ptr;
   }

@@ -1103,21 +1103,31 @@ __global__ void k_bvh_refit(const float4 *verts, const int32_t *indices, int n, 
   }
 }
 
-// element occupancy bitmap: mark every cell an element's closed AABB
-// touches (same monotonic cell mapping as the query)
-__global__ void k_elem_occupancy(const float4 *verts, const int32_t *indices, size_t ne, ElemOccupancy O,
-                                 uint32_t *bits)
+// ------------------------------------------------------------ element cells
+// the cells an element's closed AABB touches, by the query's monotonic cell
+// mapping (occ_coord), clamped to the grid
+EXA_D void elem_cell_range(const ElemOccupancy &O, V3 lo, V3 hi, int &x0, int &y0, int &z0, int &x1, int &y1, int &z1)
+{
+  x0 = imax_t(0, occ_coord(lo.x, O.origin[0], O.cellSize[0], O.n[0]));
+  y0 = imax_t(0, occ_coord(lo.y, O.origin[1], O.cellSize[1], O.n[1]));
+  z0 = imax_t(0, occ_coord(lo.z, O.origin[2], O.cellSize[2], O.n[2]));
+  x1 = imin_t(O.n[0] - 1, occ_coord(hi.x, O.origin[0], O.cellSize[0], O.n[0]));
+  y1 = imin_t(O.n[1] - 1, occ_coord(hi.y, O.origin[1], O.cellSize[1], O.n[1]));
+  z1 = imin_t(O.n[2] - 1, occ_coord(hi.z, O.origin[2], O.cellSize[2], O.n[2]));
+}
+
+// pass 1: each element's AABB, and the bit of every cell it touches
+__global__ void k_elem_cells_mark(const float4 *verts, const int32_t *indices, size_t ne, ElemOccupancy O,
+                                  uint32_t *bits, float4 *boxes)
 {
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= ne) return;
   V3 lo, hi;
   elem_box(verts, indices, e, lo, hi);
-  const int x0 = imax_t(0, occ_coord(lo.x, O.origin[0], O.cellSize[0], O.n[0]));
-  const int y0 = imax_t(0, occ_coord(lo.y, O.origin[1], O.cellSize[1], O.n[1]));
-  const int z0 = imax_t(0, occ_coord(lo.z, O.origin[2], O.cellSize[2], O.n[2]));
-  const int x1 = imin_t(O.n[0] - 1, occ_coord(hi.x, O.origin[0], O.cellSize[0], O.n[0]));
-  const int y1 = imin_t(O.n[1] - 1, occ_coord(hi.y, O.origin[1], O.cellSize[1], O.n[1]));
-  const int z1 = imin_t(O.n[2] - 1, occ_coord(hi.z, O.origin[2], O.cellSize[2], O.n[2]));
+  boxes[2 * e] = make_float4(lo.x, lo.y, lo.z, hi.x);
+  boxes[2 * e + 1] = make_float4(hi.y, hi.z, 0.f, 0.f);
+  int x0, y0, z0, x1, y1, z1;
+  elem_cell_range(O, lo, hi, x0, y0, z0, x1, y1, z1);
   for (int z = z0; z <= z1; ++z)
     for (int y = y0; y <= y1; ++y)
       for (int x = x0; x <= x1; ++x) {
@@ -1126,13 +1136,149 @@ __global__ void k_elem_occupancy(const float4 *verts, const int32_t *indices, si
       }
 }
 
-void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, const ElemOccupancy &O, uint32_t *bits,
-                         size_t words, cudaStream_t s)
+__global__ void k_popc_words(const uint32_t *bits, size_t words, uint32_t *out)
 {
-  cudaCheck(cudaMemsetAsync(bits, 0, words * sizeof(uint32_t), s), "memset occupancy");
+  const size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (w < words) out[w] = (uint32_t)__popc(bits[w]);
+}
+
+EXA_D uint32_t marked_index(const ElemOccupancy &O, const uint32_t *bits, const uint32_t *rank, size_t c)
+{
+  const uint32_t bit = 1u << (c & 31);
+  return rank[c >> 5] + (uint32_t)__popc(bits[c >> 5] & (bit - 1u));
+}
+
+// pass 2 (fill == false): elements per marked cell; pass 3 (fill): the
+// lists, a cell with one element holds it in its entry
+__global__ void k_elem_cells_lists(size_t ne, ElemOccupancy O, const uint32_t *bits, const uint32_t *rank,
+                                   const float4 *boxes, uint32_t *count, const uint32_t *off, uint32_t *cursor,
+                                   int32_t *entries, int32_t *items, bool fill)
+{
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const float4 b0 = boxes[2 * e], b1 = boxes[2 * e + 1];
+  int x0, y0, z0, x1, y1, z1;
+  elem_cell_range(O, mk3(b0.x, b0.y, b0.z), mk3(b0.w, b1.x, b1.y), x0, y0, z0, x1, y1, z1);
+  for (int z = z0; z <= z1; ++z)
+    for (int y = y0; y <= y1; ++y)
+      for (int x = x0; x <= x1; ++x) {
+        const uint32_t m = marked_index(O, bits, rank, ((size_t)z * O.n[1] + y) * O.n[0] + x);
+        if (!fill) {
+          atomicAdd(count + m, 1u);
+        } else if (count[m] == 1u) {
+          entries[m] = (int32_t)e;
+        } else {
+          items[off[m] + 1u + atomicAdd(cursor + m, 1u)] = (int32_t)e;
+        }
+      }
+}
+
+// list lengths: count + 1 words for a cell with two or more elements
+__global__ void k_elem_cells_seg(const uint32_t *count, size_t nm, uint32_t *seg)
+{
+  const size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (m < nm) seg[m] = count[m] >= 2u ? count[m] + 1u : 0u;
+}
+
+__global__ void k_elem_cells_heads(const uint32_t *count, const uint32_t *off, size_t nm, int32_t *entries,
+                                   int32_t *items)
+{
+  const size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (m >= nm) return;
+  if (count[m] >= 2u) {
+    entries[m] = -(int32_t)off[m] - 2;
+    items[off[m]] = (int32_t)count[m];
+  } else {
+    entries[m] = -1;
+  }
+}
+
+// each list in ascending order (insertion sort: lists are short)
+__global__ void k_elem_cells_sort(const uint32_t *count, const uint32_t *off, size_t nm, int32_t *items)
+{
+  const size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (m >= nm || count[m] < 2u) return;
+  int32_t *L = items + off[m] + 1;
+  const int n = (int)count[m];
+  for (int i = 1; i < n; ++i) {
+    const int32_t v = L[i];
+    int j = i - 1;
+    while (j >= 0 && L[j] > v) {
+      L[j + 1] = L[j];
+      --j;
+    }
+    L[j + 1] = v;
+  }
+}
+
+// exclusive prefix sum of n words into out; returns the total
+static uint64_t exclusiveSum(const uint32_t *in, uint32_t *out, size_t n, cudaStream_t s)
+{
+  if (n >= 0x7fffffffull) throw Error(EXA_ERR_INVALID, "element cell grid too large");
+  size_t tb = 0;
+  cudaCheck(cub::DeviceScan::ExclusiveSum(nullptr, tb, in, out, (int)n, s), "scan size");
+  DBuf<unsigned char> temp;
+  temp.alloc(tb ? tb : 1);
+  cudaCheck(cub::DeviceScan::ExclusiveSum(temp.ptr, tb, in, out, (int)n, s), "scan");
+  uint32_t last[2] = {0u, 0u};
+  cudaCheck(cudaMemcpyAsync(&last[0], out + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "scan last");
+  cudaCheck(cudaMemcpyAsync(&last[1], in + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "scan last");
+  cudaCheck(cudaStreamSynchronize(s), "scan");
+  return (uint64_t)last[0] + last[1];
+}
+
+void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOccupancy &O, DBuf<uint32_t> &bits,
+                     DBuf<uint32_t> &rank, DBuf<int32_t> &entries, DBuf<int32_t> &items, DBuf<float4> &boxes,
+                     cudaStream_t s)
+{
+  const size_t nc = (size_t)O.n[0] * O.n[1] * O.n[2];
+  const size_t words = (nc + 31) / 32;
+  bits.alloc(words);
+  rank.alloc(words);
+  boxes.alloc(2 * std::max<size_t>(ne, 1));
+  cudaCheck(cudaMemsetAsync(bits.ptr, 0, words * sizeof(uint32_t), s), "memset cell bits");
+  O.bits = bits.ptr;
+  O.rank = rank.ptr;
+  O.boxes = boxes.ptr;
+  O.entries = nullptr;
+  O.items = nullptr;
+  O.numMarked = O.numItems = 0;
   if (!ne) return;
-  k_elem_occupancy<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, ne, O, bits);
-  cudaCheck(cudaGetLastError(), "k_elem_occupancy");
+  k_elem_cells_mark<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, ne, O, bits.ptr, boxes.ptr);
+  cudaCheck(cudaGetLastError(), "k_elem_cells_mark");
+  DBuf<uint32_t> pc;
+  pc.alloc(words);
+  k_popc_words<<<gridFor(words, 256), 256, 0, s>>>(bits.ptr, words, pc.ptr);
+  cudaCheck(cudaGetLastError(), "k_popc_words");
+  const uint64_t nm = exclusiveSum(pc.ptr, rank.ptr, words, s);
+  if (nm == 0 || nm >= 0x7fffffffull) throw Error(EXA_ERR_INVALID, "element cells: bad marked-cell count");
+  DBuf<uint32_t> count, off, cursor;
+  count.alloc(nm);
+  off.alloc(nm);
+  cursor.alloc(nm);
+  cudaCheck(cudaMemsetAsync(count.ptr, 0, nm * sizeof(uint32_t), s), "memset counts");
+  cudaCheck(cudaMemsetAsync(cursor.ptr, 0, nm * sizeof(uint32_t), s), "memset cursors");
+  entries.alloc(nm);
+  k_elem_cells_lists<<<gridFor(ne, 256), 256, 0, s>>>(ne, O, bits.ptr, rank.ptr, boxes.ptr, count.ptr, nullptr,
+                                                      nullptr, nullptr, nullptr, false);
+  cudaCheck(cudaGetLastError(), "k_elem_cells_lists count");
+  k_elem_cells_seg<<<gridFor(nm, 256), 256, 0, s>>>(count.ptr, nm, cursor.ptr);  // cursor as scratch
+  const uint64_t ni = exclusiveSum(cursor.ptr, off.ptr, nm, s);
+  if (ni >= 0x7fffffffull) throw Error(EXA_ERR_INVALID, "element cells: lists too long");
+  cudaCheck(cudaMemsetAsync(cursor.ptr, 0, nm * sizeof(uint32_t), s), "memset cursors");
+  items.alloc(std::max<uint64_t>(ni, 1));
+  k_elem_cells_heads<<<gridFor(nm, 256), 256, 0, s>>>(count.ptr, off.ptr, nm, entries.ptr, items.ptr);
+  cudaCheck(cudaGetLastError(), "k_elem_cells_heads");
+  k_elem_cells_lists<<<gridFor(ne, 256), 256, 0, s>>>(ne, O, bits.ptr, rank.ptr, boxes.ptr, count.ptr, off.ptr,
+                                                      cursor.ptr, entries.ptr, items.ptr, true);
+  cudaCheck(cudaGetLastError(), "k_elem_cells_lists fill");
+  k_elem_cells_sort<<<gridFor(nm, 256), 256, 0, s>>>(count.ptr, off.ptr, nm, items.ptr);
+  cudaCheck(cudaGetLastError(), "k_elem_cells_sort");
+  cudaCheck(cudaStreamSynchronize(s), "element cells");
+  O.entries = entries.ptr;
+  O.items = items.ptr;
+  O.numMarked = (int)nm;
+  O.numItems = (int)std::max<uint64_t>(ni, 1);
 }
 
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sb, BvhNode *nodes,

@@ -183,17 +183,18 @@ class ExaStitchSampler : public Sampler {  // sampler/ExaStitchSampler.h:37-106
   exa_build_stats buildStats{};
   // point-location accel
   std::vector<DBuf<int32_t>> tableEntries, tableItems;
-  DBuf<BvhNode> bvhNodes;
-  DBuf<int32_t> bvhParents;     // internal nodes then leaves: parent*2+slot
-  DBuf<int32_t> bvhLeafElem;    // leaf (sorted position) -> element id
-  DBuf<uint32_t> occBits;       // element occupancy bitmap
+  // element cells: bits, marked cells before each word, per marked cell its
+  // entry, the lists, and per element its AABB
+  DBuf<uint32_t> occBits, occRank;
+  DBuf<int32_t> occEntries, occItems;
+  DBuf<float4> elemBoxes;
 
   size_t fieldBytes() const override;
   size_t accelBytes() const override;
 
  private:
   void buildGridletTables(cudaStream_t s);
-  void buildElementBVH(cudaStream_t s);
+  void buildElementCells(cudaStream_t s);
 };
 
 // AMRCellSampler (sampler/AMRCellSampler.h:26-56, AMRCellSampler.cpp): the
@@ -286,8 +287,11 @@ void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, i
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,
                     int32_t *parents, int32_t *leafElem, cudaStream_t s);
-void launchElemOccupancy(const float4 *verts, const int32_t *idx, size_t ne, const ElemOccupancy &O, uint32_t *bits,
-                         size_t words, cudaStream_t s);
+// element cells over the grid O (origin, cellSize, n set): fills O's
+// arrays (allocated into the buffers)
+void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOccupancy &O, DBuf<uint32_t> &bits,
+                     DBuf<uint32_t> &rank, DBuf<int32_t> &entries, DBuf<int32_t> &items, DBuf<float4> &boxes,
+                     cudaStream_t s);
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
 // wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 4 words

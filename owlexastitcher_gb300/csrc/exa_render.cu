@@ -27,7 +27,7 @@ namespace exa {
 // work counters of a counting launch (lp.ext.stepCounters set); the index is
 // the slot in stepCounters
 enum : int {
-  CNT_FIELD, CNT_GRIDLET, CNT_ELEM, CNT_DDA, CNT_PATHS, CNT_MISS, CNT_TABLES, CNT_GTESTS, CNT_BVH, CNT_WALKS,
+  CNT_FIELD, CNT_GRIDLET, CNT_ELEM, CNT_DDA, CNT_PATHS, CNT_MISS, CNT_TABLES, CNT_GTESTS, CNT_ELEMQ, CNT_WALKS,
   CNT_SURR, CNT_VIOL, CNT_N
 };
 // one column per thread in shared memory, so that an ordinary launch holds no
@@ -410,7 +410,7 @@ EXA_D exa_sample walk_sample_exact(const Walk &w, PathCtx &c)
       cnt_add(c, CNT_MISS);
       cnt_add(c, CNT_TABLES, q.tables);
       cnt_add(c, CNT_GTESTS, q.gridletTests);
-      cnt_add(c, CNT_BVH, q.bvhWalks);
+      cnt_add(c, CNT_ELEMQ, q.elemLists);
     }
   }
   if (c.counting) {
