@@ -373,7 +373,8 @@ def run_ours(a):
             "cpu_baseline": cpu,
             "parity": parity,
             "clocks": clocks,
-            "gpu_launches": a.steps * (3 * render_stats["rounds"] + 2) if render_stats["wavefront"] else 2 * a.steps,
+            # per launched round: camera, walk, events and round-end kernels; then the resolve
+            "gpu_launches": a.steps * (4 * render_stats["walkLaunches"] + 1) if render_stats["wavefront"] else 2 * a.steps,
             "render": render_stats,
             "majorant_build": majorants,
             "learned_field": learned,

@@ -535,10 +535,10 @@ int exa_render(exa_context *ctx, const exa_launch_params *lp,
 /* How the last exa_render call ran (no reference counterpart). */
 typedef struct {
   uint32_t wavefront;      /* 1: the wavefront renderer ran               */
-  uint32_t rounds;         /* camera / walk / event rounds                */
+  uint32_t rounds;         /* camera / walk / event rounds with work      */
   uint32_t peakQueue;      /* most path records queued after a round      */
   uint32_t queueCapacity;  /* record capacity of each queue               */
-  uint32_t walkLaunches;   /* walk-kernel launches                        */
+  uint32_t walkLaunches;   /* rounds launched (the last group's tail finds no work) */
   float    cameraMs;       /* summed GPU time of the camera kernels       */
   float    walkMs;         /* summed GPU time of the walk kernels         */
   float    eventMs;        /* summed GPU time of the event kernels        */

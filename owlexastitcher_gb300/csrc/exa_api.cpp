@@ -851,7 +851,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
                                                           (size_t)lp->render.spp, (size_t)1 << 22);
       if (ctx->wfCap < cap) {
         ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
-        ctx->wfCounters.alloc(4);
+        ctx->wfCounters.alloc(kWfCounterWords);
         ctx->wfCap = cap;
       }
       WfStats st;

@@ -294,7 +294,8 @@ void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOcc
                      cudaStream_t s);
 void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
                     const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
-// wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters 4 words
+// wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters
+// kWfCounterWords words
 struct WfStats {
   unsigned rounds = 0, peakQueue = 0, walkLaunches = 0;
   float cameraMs = 0.f, walkMs = 0.f, eventMs = 0.f;
@@ -363,6 +364,7 @@ struct Surrogate {
 void launchSurrogatePoints(const SurrogateView &S, const exa_vec3f *pos, size_t n, float *out, cudaStream_t s);
 bool useWavefront();
 constexpr int kWfLaneWords = 63;
+constexpr int kWfCounterWords = 16;  // wavefront queue counters + the frame's round control
 
 // ---------------------------------------------------------- batched frames
 struct WfFrame {                    // per frame of a batch (device table)

@@ -10,6 +10,8 @@
 // bank).
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <vector>
 
 #include "exa_host.h"
 #include "exa_mesh.cuh"
@@ -1265,11 +1267,21 @@ constexpr int kWalkWords = 35;
 constexpr int kLaneWords = kPathStride + kWalkWords;
 static_assert(kLaneWords == kWfLaneWords, "record size");
 
+// round control of a frame on the device (after the queue counters): the
+// jobs issued so far and in all, the round's carried walks and new camera
+// jobs, whether its walk kernel may park, whether another round is needed
+struct WfFrameCtl {
+  unsigned long long issued, total;
+  unsigned nIn, nNew, rounds, peak, park, more, error, pad;
+};
+static_assert(4 * sizeof(unsigned) + sizeof(WfFrameCtl) <= kWfCounterWords * sizeof(unsigned), "counter words");
+
 struct WfQueues {
   uint32_t *in, *out, *ev;  // record buffers (kLaneWords * cap words each)
   unsigned *cnt;            // [0] in, [1] out, [2] ev, [3] walk fetch cursor
   unsigned cap;
   int park;                 // walk kernel may park unfinished walks in out
+  const WfFrameCtl *ctl;    // non-null: camera jobs and parking from here
 };
 
 // a warp whose input is used up parks its unfinished walks in the next
@@ -1410,7 +1422,9 @@ static_assert(kEventWords <= kWfLaneWords, "an event record fits a queue slot");
 // event records are read once, by the next events kernel: streaming stores
 // (for the walk and path records, which the next walk kernel reads, plain
 // stores measured faster)
-EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, unsigned src)
+// (withXf false: the frame's events never read the classification -- a
+// fixed albedo and no Teaser shading -- and those four words are skipped)
+EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, unsigned src, bool withXf = true)
 {
 #undef W
 #define W(v) __stcs(b + (size_t)(k++) * cap + i, (uint32_t)(v))
@@ -1421,13 +1435,19 @@ EXA_D void wf_store_event(const Lane &L, uint32_t *b, unsigned cap, unsigned i, 
   W((uint32_t)L.rng.state); W((uint32_t)(L.rng.state >> 32)); ++k;  // word 4: unused
   WF(w.t); WF(w.Tr);
   WF(w.pos.x); WF(w.pos.y); WF(w.pos.z);
-  WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w);
+  if (withXf) { WF(w.xf.x); WF(w.xf.y); WF(w.xf.z); WF(w.xf.w); }
 #undef W
 #define W(v) b[(size_t)(k++) * cap + i] = (v)
 }
 
+// whether a frame's events read the classification of the walk's last sample
+EXA_D bool events_read_xf(const exa_launch_params &lp)
+{
+  return lp.ext.albedo < 0.f || lp.shadeMode == EXA_SHADE_MODE_TEASER;
+}
+
 // returns the slot of the path part
-EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i)
+EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned cap, unsigned i, bool withXf = true)
 {
   unsigned k = 0;
   Walk &w = L.w;
@@ -1441,7 +1461,11 @@ EXA_D unsigned wf_load_event(Lane &L, const uint32_t *__restrict__ b, unsigned c
   ++k;
   w.t = RF(); w.Tr = RF();
   w.pos.x = RF(); w.pos.y = RF(); w.pos.z = RF();
-  w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
+  if (withXf) {
+    w.xf.x = RF(); w.xf.y = RF(); w.xf.z = RF(); w.xf.w = RF();
+  } else {
+    w.xf = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   return src;
 }
 
@@ -1494,6 +1518,10 @@ __global__ void __launch_bounds__(128) k_wf_camera(const __grid_constant__ Accel
                                                    const __grid_constant__ exa_launch_params lp, int width, int height,
                                                    float4 *colors, WfQueues Q, unsigned first, unsigned n)
 {
+  if (Q.ctl) {
+    first = (unsigned)Q.ctl->issued;
+    n = Q.ctl->nNew;
+  }
   PathCtx c = make_ctx(A, lp);
   Machine<INTEGRATOR> M{c, lp, width, height, num_lights(lp), (unsigned)lp.ext.maxBounces, colors};
   const int spp = lp.render.spp;
@@ -1532,6 +1560,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
 {
   PathCtx c = make_ctx(A, lp);
   const unsigned n = Q.cnt[0];
+  const bool park = Q.ctl ? Q.ctl->park != 0u : Q.park != 0;
   const unsigned lane = threadIdx.x & 31;
   Lane L;
   bool active = false, exhausted = false;
@@ -1556,7 +1585,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
     }
     const unsigned act = __ballot_sync(0xffffffffu, active);
     if (!act) break;
-    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES) {
+    if (exhausted && park && __popc(act) < EXA_WF_PARK_LANES) {
       // the walk record holds the complete walk state (position in the DDA,
       // RNG counter, cached gridlet), so a parked walk resumes exactly
       const unsigned slot = warp_append(&Q.cnt[1], active);
@@ -1575,7 +1604,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk(const __
     const bool ended = active && !walk_iteration<TEASER>(L.w, c, L.rng, L.shadow);
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
-      wf_store_event(L, Q.ev, Q.cap, slot, src);
+      wf_store_event(L, Q.ev, Q.cap, slot, src, events_read_xf(lp));
       active = false;
     }
   }
@@ -1605,6 +1634,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
   PathCtx c = make_ctx(A, lp);
   const exa_grid_traversable &G = lp.majorantGrid;
   const unsigned n = Q.cnt[0];
+  const bool park = Q.ctl ? Q.ctl->park != 0u : Q.park != 0;
   const unsigned lane = threadIdx.x & 31;
   Lane L;
   bool active = false, exhausted = false, pending = false;
@@ -1631,7 +1661,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     if (!act) break;
     // a lane waiting for a learned sample is never parked: its free flight
     // is done, its sample not yet taken
-    if (exhausted && Q.park && __popc(act) < EXA_WF_PARK_LANES && !__any_sync(0xffffffffu, pending)) {
+    if (exhausted && park && __popc(act) < EXA_WF_PARK_LANES && !__any_sync(0xffffffffu, pending)) {
       const unsigned slot = warp_append(&Q.cnt[1], active);
       if (active) {
         wf_store_walk(L, Q.out, Q.cap, slot);
@@ -1680,7 +1710,7 @@ __global__ void __launch_bounds__(128, EXA_RENDER_MIN_BLOCKS) k_wf_walk_sur(cons
     ended = active && ended;
     const unsigned slot = warp_append(&Q.cnt[2], ended);
     if (ended) {
-      wf_store_event(L, Q.ev, Q.cap, slot, src);
+      wf_store_event(L, Q.ev, Q.cap, slot, src, events_read_xf(lp));
       active = false;
     }
   }
@@ -1701,7 +1731,7 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
     Lane L;
     bool tracking = false;
     if (i < n) {
-      wf_load_path(L, Q.in, Q.cap, wf_load_event(L, Q.ev, Q.cap, i), width);
+      wf_load_path(L, Q.in, Q.cap, wf_load_event(L, Q.ev, Q.cap, i, events_read_xf(lp)), width);
       if (lp.render.heatMapEnabled && lp.ext.heatCounts) atomicAdd(lp.ext.heatCounts + L.pixelID, (unsigned)L.w.ncells);
       L.phase = PH_TRACK;
       if (L.shadow) M.shadow_done(L);
@@ -1714,8 +1744,40 @@ __global__ void __launch_bounds__(128) k_wf_events(const __grid_constant__ Accel
   flush_counters(c, lp);
 }
 
-// host loop of the wavefront renderer; synchronizes the stream once per
-// round to read the queue sizes
+// end of a round on the device: the output queue becomes the next input,
+// the camera jobs and the parking of the next round are decided, and
+// whether another round is needed; a round cap stops a frame that makes no
+// progress (EXA_DEVERR_WATCHDOG).  Rounds after the last one find nothing
+// to do.
+__global__ void k_wf_round_end(unsigned *cnt, WfFrameCtl *ctl, unsigned cap, unsigned parkWalks,
+                               uint32_t *deviceErrors)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned nOut = cnt[1], nEv = cnt[2];
+  if (ctl->nIn + ctl->nNew > 0u) ctl->rounds += 1u;
+  ctl->issued += ctl->nNew;
+  if (nEv > ctl->peak) ctl->peak = nEv;
+  cnt[0] = nOut;
+  cnt[1] = cnt[2] = cnt[3] = 0u;
+  const unsigned long long left = ctl->total - ctl->issued;
+  const unsigned nNew = (unsigned)(left < (unsigned long long)(cap - nOut) ? left : (unsigned long long)(cap - nOut));
+  ctl->nIn = nOut;
+  ctl->nNew = nNew;
+  // parking pays while a round has several walks per walk-kernel thread;
+  // small rounds (the end of the frame) run their walks to completion
+  ctl->park = (unsigned long long)nOut + nNew >= (unsigned long long)parkWalks ? 1u : 0u;
+  unsigned more = (nOut > 0u || ctl->issued < ctl->total) ? 1u : 0u;
+  if (more && ctl->rounds >= kBatchRoundCap) {
+    more = 0u;
+    ctl->error = 1u;
+    if (deviceErrors) atomicOr(deviceErrors, EXA_DEVERR_WATCHDOG);
+  }
+  ctl->more = more;
+}
+
+// host loop of the wavefront renderer: rounds are launched in groups and
+// driven by the device (k_wf_round_end); the host reads the round control
+// once per group to see whether the frame is done
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,
                      uint32_t *bufs, unsigned cap, unsigned *counters, cudaStream_t s, WfStats *stats,
                      const SurrogateView *sur)
@@ -1734,9 +1796,6 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   if (cap % 4 != 0) throw Error(EXA_ERR_INVALID, "queue capacity must be a multiple of 4");
   const size_t words = (size_t)kLaneWords * cap;
   uint32_t *buf[3] = {bufs, bufs + words, bufs + 2 * words};
-  unsigned long long issued = jobsPerTileRow * (unsigned long long)(rowBegin / 8);
-  unsigned nIn = 0;
-  int inIdx = 0, outIdx = 1;
   const unsigned grid = (unsigned)sms * 16;
   int perSM = 4;
   if (sur) {
@@ -1754,57 +1813,74 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     cudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_wf_walk<false>, 128, 0), "occupancy");
   }
   const unsigned walkGrid = (unsigned)sms * (unsigned)(perSM > 0 ? perSM : 1);
-  // per-kernel-class timing on this stream: camera, walk, events
-  cudaEvent_t ev[4];
-  for (auto &e : ev) cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
-  struct EvGuard {
-    cudaEvent_t *e;
-    ~EvGuard() { for (int k = 0; k < 4; ++k) cudaEventDestroy(e[k]); }
-  } evGuard{ev};
+  // the first round's control: no carried walks, the first camera jobs
+  WfFrameCtl *ctl = reinterpret_cast<WfFrameCtl *>(counters + 4);
+  WfFrameCtl c0{};
+  c0.issued = jobsPerTileRow * (unsigned long long)(rowBegin / 8);
+  c0.total = total;
+  c0.nNew = (unsigned)std::min<unsigned long long>(cap, total - c0.issued);
+  const unsigned parkWalks = 4u * walkGrid * 128u;
+  c0.park = c0.nNew >= parkWalks ? 1u : 0u;
+  c0.more = 1u;
   cudaCheck(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned), s), "reset queues");
-  for (int round = 0; round < (1 << 24); ++round) {
-    const unsigned nNew = (unsigned)std::min<unsigned long long>(cap - nIn, total - issued);
-    // parking pays while a round has several walks per walk-kernel thread;
-    // small rounds (the end of the frame) run their walks to completion
-    const int park = (unsigned long long)nIn + nNew >= 4ull * walkGrid * 128u ? 1 : 0;
-    WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap, park};
-    cudaCheck(cudaEventRecord(ev[0], s), "event");
-    if (nNew) {
-      const unsigned g = std::min<unsigned>(grid, (nNew + 127) / 128);
-      if (pt) k_wf_camera<EXA_PATH_TRACING_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
-      else k_wf_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, (unsigned)issued, nNew);
-      issued += nNew;
+  cudaCheck(cudaMemcpyAsync(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice, s), "frame control");
+  // per-kernel-class timing on this stream (camera, walk, events), four
+  // events per round from a pool kept across calls
+  thread_local std::map<int, std::vector<cudaEvent_t>> pools;
+  std::vector<cudaEvent_t> &pool = pools[dev];
+  const bool timing = stats != nullptr;
+  int inIdx = 0, outIdx = 1, launched = 0;
+  WfFrameCtl h{};
+  // a frame whose jobs all fit the first round needs no camera launch after it
+  const bool oneIssue = c0.nNew == total - c0.issued;
+  // rounds per host check: few at first (small frames end in a few rounds),
+  // more once the frame proves long
+  for (int group = 0; launched < (int)kBatchRoundCap; ++group) {
+    const int rounds = group == 0 ? 4 : 8;
+    for (int r = 0; r < rounds; ++r, ++launched) {
+      if (timing)
+        while (pool.size() < 4 * (size_t)(launched + 1)) {
+          cudaEvent_t e;
+          cudaCheck(cudaEventCreate(&e), "cudaEventCreate");
+          pool.push_back(e);
+        }
+      cudaEvent_t *ev = timing ? &pool[4 * (size_t)launched] : nullptr;
+      WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap, 0, ctl};
+      if (timing) cudaCheck(cudaEventRecord(ev[0], s), "event");
+      if (launched == 0 || !oneIssue) {
+        // (the first round's job count is known here; later rounds read theirs)
+        const unsigned g = launched == 0 ? std::max(1u, std::min<unsigned>(grid, (c0.nNew + 127) / 128)) : grid;
+        if (pt) k_wf_camera<EXA_PATH_TRACING_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, 0u, 0u);
+        else k_wf_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, 0u, 0u);
+      }
+      if (timing) cudaCheck(cudaEventRecord(ev[1], s), "event");
+      if (sur) k_wf_walk_sur<<<walkGrid, 128, kSurWalkSmem, s>>>(A, lp, Q, *sur);
+      else if (lp.shadeMode == EXA_SHADE_MODE_TEASER) k_wf_walk<true><<<walkGrid, 128, 0, s>>>(A, lp, Q);
+      else k_wf_walk<false><<<walkGrid, 128, 0, s>>>(A, lp, Q);
+      if (timing) cudaCheck(cudaEventRecord(ev[2], s), "event");
+      if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
+      else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
+      if (timing) cudaCheck(cudaEventRecord(ev[3], s), "event");
+      k_wf_round_end<<<1, 32, 0, s>>>(counters, ctl, cap, parkWalks, lp.ext.deviceErrors);
+      cudaCheck(cudaGetLastError(), "wavefront round");
+      std::swap(inIdx, outIdx);
     }
-    cudaCheck(cudaEventRecord(ev[1], s), "event");
-    if (sur) k_wf_walk_sur<<<walkGrid, 128, kSurWalkSmem, s>>>(A, lp, Q, *sur);
-    else if (lp.shadeMode == EXA_SHADE_MODE_TEASER) k_wf_walk<true><<<walkGrid, 128, 0, s>>>(A, lp, Q);
-    else k_wf_walk<false><<<walkGrid, 128, 0, s>>>(A, lp, Q);
-    cudaCheck(cudaEventRecord(ev[2], s), "event");
-    if (pt) k_wf_events<EXA_PATH_TRACING_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
-    else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
-    cudaCheck(cudaEventRecord(ev[3], s), "event");
-    cudaCheck(cudaGetLastError(), "wavefront round");
-    unsigned h[3];
-    cudaCheck(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s), "read queues");
-    cudaCheck(cudaStreamSynchronize(s), "wavefront round");
-    if (stats) {
+    cudaCheck(cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, s), "read frame control");
+    cudaCheck(cudaStreamSynchronize(s), "wavefront rounds");
+    if (!h.more) break;
+  }
+  if (stats) {
+    for (int r = 0; r < launched; ++r) {
       float ms[3] = {0.f, 0.f, 0.f};
-      for (int k = 0; k < 3; ++k) cudaCheck(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]), "event time");
+      for (int k = 0; k < 3; ++k)
+        cudaCheck(cudaEventElapsedTime(&ms[k], pool[4 * (size_t)r + k], pool[4 * (size_t)r + k + 1]), "event time");
       stats->cameraMs += ms[0];
       stats->walkMs += ms[1];
       stats->eventMs += ms[2];
-      stats->walkLaunches++;
     }
-    nIn = h[1];
-    if (stats) {
-      stats->rounds = round + 1;
-      stats->peakQueue = std::max(stats->peakQueue, h[2]);
-    }
-    if (nIn == 0 && issued >= total) break;
-    // next round: the out queue becomes the input
-    const unsigned next[4] = {h[1], 0u, 0u, 0u};
-    cudaCheck(cudaMemcpyAsync(counters, next, sizeof(next), cudaMemcpyHostToDevice, s), "swap queues");
-    std::swap(inIdx, outIdx);
+    stats->rounds = h.rounds;
+    stats->walkLaunches = (unsigned)launched;
+    stats->peakQueue = std::max(stats->peakQueue, h.peak);
   }
   const int pb = rowBegin * width, pe = rowEnd * width;
   k_resolve<<<(unsigned)(((long long)(pe - pb) + 255) / 256), 256, 0, s>>>(lp, width, height, colors, pb, pe);
