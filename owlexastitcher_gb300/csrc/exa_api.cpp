@@ -225,6 +225,9 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
       T.maxIdx = std::max(T.maxIdx, gi);
     }
     for (int a = 0; a < 3; ++a) {
+      // blocks start on multiples of their width in the level's lattice, as
+      // makeGrids' bricks do, so that a brick fills one block
+      lo[a] = floorDiv(lo[a], (int64_t)1 << shift) * ((int64_t)1 << shift);
       if (lo[a] < INT32_MIN / 2 || hi[a] > INT32_MAX / 2) throw Error(EXA_ERR_INVALID, "gridlet lattice out of range");
       T.t.origin[a] = (int)lo[a];
       T.t.n[a] = (int)(((hi[a] - lo[a]) + (1ll << shift) - 1) >> shift) + 1;
@@ -262,10 +265,13 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
       }
     }
     int shift = 3;
-    auto blocks = [&](int sh, int a) { return ((hi[a] - lo[a]) + (1ll << sh) - 1) / (1ll << sh) + 1; };
+    // (origins aligned to the block width, as makeTable places them)
+    auto alignedLo = [&](int sh, int a) { return floorDiv(lo[a], (int64_t)1 << sh) * ((int64_t)1 << sh); };
+    auto blocks = [&](int sh, int a) { return ((hi[a] - alignedLo(sh, a)) + (1ll << sh) - 1) / (1ll << sh) + 1; };
     while (blocks(shift, 0) * blocks(shift, 1) * blocks(shift, 2) > (1ll << 27) && shift < 20) shift++;
-    const int org[3] = {(int)std::max<int64_t>(lo[0], INT32_MIN / 2), (int)std::max<int64_t>(lo[1], INT32_MIN / 2),
-                        (int)std::max<int64_t>(lo[2], INT32_MIN / 2)};
+    const int org[3] = {(int)std::max<int64_t>(alignedLo(shift, 0), INT32_MIN / 2),
+                        (int)std::max<int64_t>(alignedLo(shift, 1), INT32_MIN / 2),
+                        (int)std::max<int64_t>(alignedLo(shift, 2), INT32_MIN / 2)};
     listed = 0;
     for (int gi : ids) {
       int b0[3], b1[3];
