@@ -480,7 +480,8 @@ EXA_D bool walk_step(Walk &w, PathCtx &c, Rng &rng, const bool shadow)
 // divergence between lanes.  Measured on the 1024^2 x 16 spp medium
 // workload: 1 advance per iteration 182 M paths/s, 2: 218 M, 3: 231 M,
 // 4: 232 M, 6: 226 M, 8: 219 M, 64: 188 M; two steps per iteration no
-// better.
+// better.  Again with the later walk kernel: 3: 287.2 M, 4: 287.3 M, 6:
+// 275.4 M.
 #ifndef EXA_WF_ADVANCE_MAX
 #define EXA_WF_ADVANCE_MAX 4
 #endif
@@ -1290,7 +1291,8 @@ struct WfQueues {
 // preferred shared-memory carveout of the walk kernels in percent (-1: the
 // driver's choice).  Measured on the medium workload: 4 %: 160 M paths/s
 // (fewer resident blocks), 8 %: 247 M, 12 %: 247 M, 16 %: 243 M, 25 % and
-// the driver's choice: 243 M, 100 %: 203 M.
+// the driver's choice: 243 M, 100 %: 203 M; with the later walk kernel
+// 6 %: 175.6 M, 10 %: 287.3 M, 16 %: 284.5 M.
 #ifndef EXA_WALK_CARVEOUT
 #define EXA_WALK_CARVEOUT 10
 #endif
