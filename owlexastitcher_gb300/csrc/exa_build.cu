@@ -636,21 +636,19 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
         glo = fminf(glo, v);
         ghi = fmaxf(ghi, v);
       }
-    // along x: every (macrocell column, corner row)
+    // along x: every (macrocell column, corner row), a lane per row
     float2 *X = sm.pool;
-    {
-      const SepDiv byRows(rows);
-      for (int k = lane; k < wx * rows; k += 32) {
-        const int m = byRows(k), r = k - m * rows;
+    for (int r = lane; r < rows; r += 32) {
+      const float *R = B + P.lead + r * nx;
+      for (int m = 0; m < wx; ++m) {
         const int2 iv = sm.cornerIv[0][m];
-        const float *R = B + P.lead + r * nx;
         float lo = 1e30f, hi = -1e30f;
         for (int c = iv.x; c <= iv.y; ++c) {
           const float v = R[c];
           lo = fminf(lo, v);
           hi = fmaxf(hi, v);
         }
-        X[k] = make_float2(lo, hi);
+        X[m * rows + r] = make_float2(lo, hi);
         if (fold) {
           glo = fminf(glo, lo);
           ghi = fmaxf(ghi, hi);
@@ -671,21 +669,23 @@ __global__ void __launch_bounds__(kSepWarps * 32) k_gridlet_majorants_sep(
     }
     const SepDiv byX(wx), byXY(wx * wy);
     if (yStep) {
-      // along y: every (macrocell column, macrocell row, corner plane)
+      // along y: every (macrocell column, macrocell row, corner plane), a
+      // lane per (column, plane)
       float2 *Y = sm.pool + wx * rows;
-      const SepDiv byZ(nz), byY(wy);
-      for (int k = lane; k < wx * wy * nz; k += 32) {
-        const int k1 = byZ(k), cz = k - k1 * nz;
-        const int mx = byY(k1), my = k1 - mx * wy;
-        const int2 iy = sm.cornerIv[1][my];
+      const SepDiv byZ(nz);
+      for (int k = lane; k < wx * nz; k += 32) {
+        const int mx = byZ(k), cz = k - mx * nz;
         const float2 *S = X + mx * rows + cz * ny;
-        float lo = 1e30f, hi = -1e30f;
-        for (int cy = iy.x; cy <= iy.y; ++cy) {
-          const float2 v = S[cy];
-          lo = fminf(lo, v.x);
-          hi = fmaxf(hi, v.y);
+        for (int my = 0; my < wy; ++my) {
+          const int2 iy = sm.cornerIv[1][my];
+          float lo = 1e30f, hi = -1e30f;
+          for (int cy = iy.x; cy <= iy.y; ++cy) {
+            const float2 v = S[cy];
+            lo = fminf(lo, v.x);
+            hi = fmaxf(hi, v.y);
+          }
+          Y[(mx * wy + my) * nz + cz] = make_float2(lo, hi);
         }
-        Y[k] = make_float2(lo, hi);
       }
       __syncwarp();
       // along z: every window macrocell
