@@ -39,11 +39,11 @@ struct GridletTable {
   int numItems;            // length of items (for the bounds-checked build)
 };
 
-struct BvhNode {   // 64 B: two child boxes, two child refs, two opacities
+struct BvhNode {   // 64 B: two child boxes, two child refs (ExaBrick regions, surface meshes)
   float lo0[3], hi0[3];
   float lo1[3], hi1[3];
-  int32_t child[2];     // >= 0 internal node, < 0 leaf element ~child
-  float op[2];          // max opacity of each child subtree
+  int32_t child[2];     // >= 0 internal node, < 0 leaf ~child
+  float op[2];          // 1 (the trees are not culled; keeps the 64-byte node)
 };
 
 // Element cells: one bit per cell of a uniform grid over the elements'

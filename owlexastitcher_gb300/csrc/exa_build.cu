@@ -1063,41 +1063,35 @@ __global__ void k_bvh_single(const uint64_t *keys, BvhNode *nodes, int32_t *pare
   parents[0] = 0;  // leaf position 0 -> node 0 slot 0 (parents[(n-1)+0])
 }
 
-// bottom-up refit: each leaf writes its box and opacity into its parent's
-// slot; the second thread to reach a node merges and moves up
+// bottom-up refit: each leaf writes its box into its parent's slot; the
+// second thread to reach a node merges and moves up (child opacities are
+// left at 1: no query of these trees culls)
 __global__ void k_bvh_refit(const float4 *verts, const int32_t *indices, int n, BvhNode *nodes,
-                            const int32_t *parents, const int32_t *leafElem, const float *elemOps, bool boxes,
-                            unsigned *counters)
+                            const int32_t *parents, const int32_t *leafElem, unsigned *counters)
 {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const int e = leafElem[p];
-  V3 lo = mk3(0.f, 0.f, 0.f), hi = lo;
-  if (boxes) elem_box(verts, indices, (size_t)e, lo, hi);
-  float op = elemOps ? elemOps[e] : 1.f;
+  V3 lo, hi;
+  elem_box(verts, indices, (size_t)e, lo, hi);
   int par = parents[(n - 1) + p];
   // a Karras tree over unique 64-bit keys is at most 64 levels deep
   for (int depth = 0; depth < 128; ++depth) {
     const int node = par >> 1, slot = par & 1;
     volatile BvhNode *vn = nodes + node;
-    if (boxes) {
-      if (slot == 0) {
-        vn->lo0[0] = lo.x; vn->lo0[1] = lo.y; vn->lo0[2] = lo.z;
-        vn->hi0[0] = hi.x; vn->hi0[1] = hi.y; vn->hi0[2] = hi.z;
-      } else {
-        vn->lo1[0] = lo.x; vn->lo1[1] = lo.y; vn->lo1[2] = lo.z;
-        vn->hi1[0] = hi.x; vn->hi1[1] = hi.y; vn->hi1[2] = hi.z;
-      }
+    if (slot == 0) {
+      vn->lo0[0] = lo.x; vn->lo0[1] = lo.y; vn->lo0[2] = lo.z;
+      vn->hi0[0] = hi.x; vn->hi0[1] = hi.y; vn->hi0[2] = hi.z;
+    } else {
+      vn->lo1[0] = lo.x; vn->lo1[1] = lo.y; vn->lo1[2] = lo.z;
+      vn->hi1[0] = hi.x; vn->hi1[1] = hi.y; vn->hi1[2] = hi.z;
     }
-    vn->op[slot] = op;
+    vn->op[slot] = 1.f;
     __threadfence();
     if (atomicAdd(counters + node, 1u) == 0u) return;
     __threadfence();
-    if (boxes) {
-      lo = min3(mk3(vn->lo0[0], vn->lo0[1], vn->lo0[2]), mk3(vn->lo1[0], vn->lo1[1], vn->lo1[2]));
-      hi = max3(mk3(vn->hi0[0], vn->hi0[1], vn->hi0[2]), mk3(vn->hi1[0], vn->hi1[1], vn->hi1[2]));
-    }
-    op = fmaxf(vn->op[0], vn->op[1]);
+    lo = min3(mk3(vn->lo0[0], vn->lo0[1], vn->lo0[2]), mk3(vn->lo1[0], vn->lo1[1], vn->lo1[2]));
+    hi = max3(mk3(vn->hi0[0], vn->hi0[1], vn->hi0[2]), mk3(vn->hi1[0], vn->hi1[1], vn->hi1[2]));
     if (node == 0) return;
     par = parents[node];
   }
@@ -1303,21 +1297,12 @@ void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3
   else
     k_bvh_karras<<<gridFor(ne, 256), 256, 0, s>>>(sorted.ptr, n, nodes, parents, leafElem);
   cudaCheck(cudaGetLastError(), "k_bvh_karras");
-  launchRefitBVH(verts, idx, ne, nodes, parents, leafElem, nullptr, true, s);
-  cudaCheck(cudaStreamSynchronize(s), "bvh build");
-}
-
-void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
-                    const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s)
-{
-  if (!ne) return;
-  const int n = (int)ne;
   DBuf<unsigned> counters;
   counters.alloc(n > 1 ? n - 1 : 1);
   cudaCheck(cudaMemsetAsync(counters.ptr, 0, counters.bytes(), s), "memset counters");
-  k_bvh_refit<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, n, nodes, parents, leafElem, elemOps, boxes, counters.ptr);
+  k_bvh_refit<<<gridFor(ne, 256), 256, 0, s>>>(verts, idx, n, nodes, parents, leafElem, counters.ptr);
   cudaCheck(cudaGetLastError(), "k_bvh_refit");
-  cudaCheck(cudaStreamSynchronize(s), "bvh refit");
+  cudaCheck(cudaStreamSynchronize(s), "bvh build");
 }
 
 } // namespace exa

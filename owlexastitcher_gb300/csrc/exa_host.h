@@ -292,8 +292,6 @@ void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3
 void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOccupancy &O, DBuf<uint32_t> &bits,
                      DBuf<uint32_t> &rank, DBuf<int32_t> &entries, DBuf<int32_t> &items, DBuf<float4> &boxes,
                      cudaStream_t s);
-void launchRefitBVH(const float4 *verts, const int32_t *idx, size_t ne, BvhNode *nodes, const int32_t *parents,
-                    const int32_t *leafElem, const float *elemOps, bool boxes, cudaStream_t s);
 // wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters
 // kWfCounterWords words
 struct WfStats {
