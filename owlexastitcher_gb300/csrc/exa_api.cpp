@@ -184,7 +184,7 @@ size_t ExaStitchSampler::accelBytes() const
 // wider fields get one table per level.  Measured on the cloud (one table
 // at 16-cell blocks against five per-level tables): 69.1 against 65.6 M
 // paths/s (one table lookup per full query instead of 4.9, 1.41 gridlet
-// tests instead of 1.08; the host builds it in 2.1 s instead of 0.35 s).
+// tests instead of 1.08).
 #ifndef EXA_TABLE_UNIFIED_MAX_SHIFT
 #define EXA_TABLE_UNIFIED_MAX_SHIFT 4
 #endif
@@ -243,25 +243,41 @@ void ExaStitchSampler::buildGridletTables(cudaStream_t s)
       T.t.n[a] = (int)(((hi[a] - lo[a]) + (1ll << shift) - 1) >> shift) + 1;
     }
     const size_t nb = (size_t)T.t.n[0] * T.t.n[1] * T.t.n[2];
-    std::vector<std::vector<int32_t>> lists(nb);
-    for (int gi : ids) {
+    // two passes over the listings (count, fill) into flat arrays; ids come
+    // in ascending order, so every list is filled in ascending order
+    auto forBlocks = [&](int gi, auto &&f) {
       int b0[3], b1[3];
       blockRange(gi, lt, T.t.origin, shift, b0, b1);
       for (int z = std::max(b0[2], 0); z <= std::min(b1[2], T.t.n[2] - 1); ++z)
         for (int y = std::max(b0[1], 0); y <= std::min(b1[1], T.t.n[1] - 1); ++y)
           for (int x = std::max(b0[0], 0); x <= std::min(b1[0], T.t.n[0] - 1); ++x)
-            lists[((size_t)z * T.t.n[1] + y) * T.t.n[0] + x].push_back(gi);
-    }
+            f(((size_t)z * T.t.n[1] + y) * T.t.n[0] + x);
+    };
+    std::vector<uint32_t> cnt(nb, 0u), cur(nb, 0u);
+    for (int gi : ids) forBlocks(gi, [&](size_t b) { cnt[b]++; });
     T.entries.assign(nb, -1);
-    for (size_t b = 0; b < nb; ++b) {
-      auto &L = lists[b];
-      if (L.empty()) continue;
-      if (L.size() == 1) { T.entries[b] = L[0]; continue; }
-      std::sort(L.begin(), L.end());
-      T.entries[b] = -(int32_t)T.items.size() - 2;
-      T.items.push_back((int32_t)L.size());
-      T.items.insert(T.items.end(), L.begin(), L.end());
-    }
+    size_t total = 0;
+    for (size_t b = 0; b < nb; ++b)
+      if (cnt[b] >= 2u) {
+        T.entries[b] = -(int32_t)total - 2;
+        cur[b] = (uint32_t)total + 1u;
+        total += (size_t)cnt[b] + 1;
+        if (total >= 0x7fffffffull) throw Error(EXA_ERR_INVALID, "gridlet table lists too long");
+      }
+    T.items.assign(total, 0);
+    for (size_t b = 0; b < nb; ++b)
+      if (cnt[b] >= 2u) T.items[cur[b] - 1u] = (int32_t)cnt[b];
+    for (int gi : ids)
+      forBlocks(gi, [&](size_t b) {
+        if (cnt[b] == 1u) T.entries[b] = gi;
+        else T.items[cur[b]++] = gi;
+      });
+    if (!std::is_sorted(ids.begin(), ids.end()))
+      for (size_t b = 0; b < nb; ++b)
+        if (T.entries[b] <= -2) {
+          int32_t *L = T.items.data() + (-T.entries[b] - 2);
+          std::sort(L + 1, L + 1 + L[0]);
+        }
   };
   // smallest shift >= 3 whose block grid has at most 2^27 blocks
   auto pickShift = [&](const std::vector<int> &ids, int lt, int64_t &listed) {
