@@ -48,7 +48,7 @@ struct BvhNode {   // 64 B: two child boxes, two child refs (ExaBrick regions, s
 
 // Element cells: one bit per cell of a uniform grid over the elements'
 // bounds, set where any element's closed AABB touches the cell.
-// cell(p) = floor((p - origin) / cellSize) is monotonic in p, so a point
+// cell(p) = floor((p - origin) / width) is monotonic in p, so a point
 // inside an element's AABB always maps to a marked cell that lists the
 // element; a clear bit proves no element contains the point.  Marked cells
 // are numbered in cell order (rank: the marked cells before each 32-cell
@@ -56,7 +56,7 @@ struct BvhNode {   // 64 B: two child boxes, two child refs (ExaBrick regions, s
 // items[-e-2] (count, then the ids ascending).
 struct ElemOccupancy {
   float origin[3];
-  float cellSize[3];
+  float invCell[3];        // 1 / cell width (the width a power of two)
   int n[3];
   const uint32_t *bits;
   const uint32_t *rank;
@@ -113,9 +113,11 @@ struct AccelView {
   const BrickView *bricks;      // non-null: the ExaBrick sampler (no gridlets, no elements)
 };
 
-EXA_HD int occ_coord(float p, float origin, float cs, int n)
+// cell of p along one axis: floor((p - origin) / width), the width a power of
+// two, so the multiplication by its reciprocal is the exact quotient
+EXA_HD int occ_coord(float p, float origin, float invWidth, int n)
 {
-  const float f = floorf((p - origin) / cs);
+  const float f = floorf((p - origin) * invWidth);
   return f < 0.f ? -1 : (f >= (float)n ? n : (int)f);
 }
 
@@ -196,17 +198,15 @@ EXA_D bool box_contains(const float *lo, const float *hi, V3 p)
   return lo[0] <= p.x && lo[1] <= p.y && lo[2] <= p.z && p.x <= hi[0] && p.y <= hi[1] && p.z <= hi[2];
 }
 
-// the lowest-index element that holds pos (its closed AABB, then the
-// element's own test), -1 if none.  Out of line: element samples are rare
-// next to gridlet samples, and keeping the list walk and the three Newton
-// solvers out of the tracking loop keeps that loop's code small.
-static __device__ __noinline__ int query_elements(const AccelView &A, V3 pos, bool cull, float &val, uint32_t &err,
-                                                  QueryStats *qs)
+// the entry of pos's element cell: -1 when no element's closed AABB can hold
+// pos (the cell's bit is clear), else the cell's entry (>= 0 its only
+// element, <= -2 its list)
+EXA_D int elem_cell_entry(const AccelView &A, V3 pos, uint32_t &err)
 {
   const ElemOccupancy &O = A.occ;
-  const int x = occ_coord(pos.x, O.origin[0], O.cellSize[0], O.n[0]);
-  const int y = occ_coord(pos.y, O.origin[1], O.cellSize[1], O.n[1]);
-  const int z = occ_coord(pos.z, O.origin[2], O.cellSize[2], O.n[2]);
+  const int x = occ_coord(pos.x, O.origin[0], O.invCell[0], O.n[0]);
+  const int y = occ_coord(pos.y, O.origin[1], O.invCell[1], O.n[1]);
+  const int z = occ_coord(pos.z, O.origin[2], O.invCell[2], O.n[2]);
   if (x < 0 || y < 0 || z < 0 || x >= O.n[0] || y >= O.n[1] || z >= O.n[2]) return -1;
   const size_t c = ((size_t)z * O.n[1] + y) * O.n[0] + x;
   // the word's bits and its rank do not depend on each other: both loads
@@ -215,11 +215,20 @@ static __device__ __noinline__ int query_elements(const AccelView &A, V3 pos, bo
   const uint32_t before = __ldg(O.rank + (c >> 5));
   const uint32_t bit = 1u << (c & 31);
   if (!(word & bit)) return -1;
-  if (qs) qs->elemLists++;
   const int m = (int)(before + __popc(word & (bit - 1u)));
   if (!exa_in_range(m, O.numMarked, err)) return -1;
-  const int e = __ldg(O.entries + m);
-  if (e == -1) return -1;  // (a marked cell always lists an element)
+  return __ldg(O.entries + m);  // (a marked cell always lists an element)
+}
+
+// the lowest-index element of a cell entry that holds pos (its closed AABB,
+// then the element's own test), -1 if none.  Out of line: element samples
+// are rare next to gridlet samples, and keeping the list walk and the three
+// Newton solvers out of the tracking loop keeps that loop's code small.
+static __device__ __noinline__ int query_element_entry(const AccelView &A, V3 pos, int e, bool cull, float &val,
+                                                       uint32_t &err)
+{
+  const ElemOccupancy &O = A.occ;
+  if (e == -1) return -1;
   int cnt = 1;
   const int32_t *list = nullptr;
   if (e <= -2) {
@@ -243,6 +252,14 @@ static __device__ __noinline__ int query_elements(const AccelView &A, V3 pos, bo
     }
   }
   return -1;
+}
+
+EXA_D int query_elements(const AccelView &A, V3 pos, bool cull, float &val, uint32_t &err, QueryStats *qs)
+{
+  const int e = elem_cell_entry(A, pos, err);
+  if (e == -1) return -1;
+  if (qs) qs->elemLists++;
+  return query_element_entry(A, pos, e, cull, val, err);
 }
 
 // sample() (sampler/ExaStitchSampler.h:128-140); sets EXA_DEVERR bits in err
@@ -421,23 +438,29 @@ EXA_D exa_sample sample_elements(const AccelView &A, V3 pos, bool cull, uint32_t
   return s;
 }
 
-EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
+// the gridlet part of sample(): the lowest-index gridlet that holds pos
+// (primID -1: none)
+EXA_D exa_sample sample_gridlets(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
 {
-  if (A.amr) return amr_sample(*A.amr, pos);
-  if (A.bricks) return brick_sample(*A.bricks, pos, err);
   int best = 0x7fffffff, cell = -1;
   float val = 0.f;
   for (int t = 0; t < A.numTables; ++t) {
     query_table(A, A.tables[t], pos, cull, best, val, cell, qs, err);
     if (A.tablesSorted && best != 0x7fffffff) break;
   }
-  if (best != 0x7fffffff) {
-    exa_sample s;
-    s.primID = best;
-    s.cellID = cell;
-    s.value = val;
-    return s;
-  }
+  exa_sample s;
+  s.primID = best != 0x7fffffff ? best : -1;
+  s.cellID = best != 0x7fffffff ? cell : -1;
+  s.value = best != 0x7fffffff ? val : 0.f;
+  return s;
+}
+
+EXA_D exa_sample sample_field(const AccelView &A, V3 pos, bool cull, uint32_t &err, QueryStats *qs = nullptr)
+{
+  if (A.amr) return amr_sample(*A.amr, pos);
+  if (A.bricks) return brick_sample(*A.bricks, pos, err);
+  const exa_sample s = sample_gridlets(A, pos, cull, err, qs);
+  if (s.primID >= 0) return s;
   return sample_elements(A, pos, cull, err, qs);
 }
 

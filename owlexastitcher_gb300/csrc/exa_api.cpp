@@ -388,7 +388,7 @@ void ExaStitchSampler::buildElementCells(cudaStream_t s)
   while (cells(cs) > (double)(1 << 27)) cs *= 2.f;
   for (int a = 0; a < 3; ++a) {
     O.origin[a] = org[a];
-    O.cellSize[a] = cs;
+    O.invCell[a] = 1.f / cs;  // exact: cs is a power of two
     O.n[a] = (int)std::max(1.0, std::ceil((double)ext[a] / cs) + 1);
   }
   launchElemCells(vertexBuffer.ptr, indexBuffer.ptr, ne, O, occBits, occRank, occEntries, occItems, elemBoxes, s);

@@ -1102,12 +1102,12 @@ __global__ void k_bvh_refit(const float4 *verts, const int32_t *indices, int n, 
 // mapping (occ_coord), clamped to the grid
 EXA_D void elem_cell_range(const ElemOccupancy &O, V3 lo, V3 hi, int &x0, int &y0, int &z0, int &x1, int &y1, int &z1)
 {
-  x0 = imax_t(0, occ_coord(lo.x, O.origin[0], O.cellSize[0], O.n[0]));
-  y0 = imax_t(0, occ_coord(lo.y, O.origin[1], O.cellSize[1], O.n[1]));
-  z0 = imax_t(0, occ_coord(lo.z, O.origin[2], O.cellSize[2], O.n[2]));
-  x1 = imin_t(O.n[0] - 1, occ_coord(hi.x, O.origin[0], O.cellSize[0], O.n[0]));
-  y1 = imin_t(O.n[1] - 1, occ_coord(hi.y, O.origin[1], O.cellSize[1], O.n[1]));
-  z1 = imin_t(O.n[2] - 1, occ_coord(hi.z, O.origin[2], O.cellSize[2], O.n[2]));
+  x0 = imax_t(0, occ_coord(lo.x, O.origin[0], O.invCell[0], O.n[0]));
+  y0 = imax_t(0, occ_coord(lo.y, O.origin[1], O.invCell[1], O.n[1]));
+  z0 = imax_t(0, occ_coord(lo.z, O.origin[2], O.invCell[2], O.n[2]));
+  x1 = imin_t(O.n[0] - 1, occ_coord(hi.x, O.origin[0], O.invCell[0], O.n[0]));
+  y1 = imin_t(O.n[1] - 1, occ_coord(hi.y, O.origin[1], O.invCell[1], O.n[1]));
+  z1 = imin_t(O.n[2] - 1, occ_coord(hi.z, O.origin[2], O.invCell[2], O.n[2]));
 }
 
 // pass 1: each element's AABB, and the bit of every cell it touches

@@ -287,7 +287,7 @@ void launchMaxOpacity(const exa_range1f *ranges, size_t n, const float4 *cmap, i
                       float *out, cudaStream_t s);
 void launchBuildBVH(const float4 *verts, const int32_t *idx, size_t ne, exa_box3f sceneBounds, BvhNode *nodes,
                     int32_t *parents, int32_t *leafElem, cudaStream_t s);
-// element cells over the grid O (origin, cellSize, n set): fills O's
+// element cells over the grid O (origin, invCell, n set): fills O's
 // arrays (allocated into the buffers)
 void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOccupancy &O, DBuf<uint32_t> &bits,
                      DBuf<uint32_t> &rank, DBuf<int32_t> &entries, DBuf<int32_t> &items, DBuf<float4> &boxes,
