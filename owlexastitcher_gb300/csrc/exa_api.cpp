@@ -185,6 +185,11 @@ size_t ExaStitchSampler::accelBytes() const
 // at 16-cell blocks against five per-level tables): 69.1 against 65.6 M
 // paths/s (one table lookup per full query instead of 4.9, 1.41 gridlet
 // tests instead of 1.08).
+// records a wavefront queue holds at most (walks in flight per round)
+#ifndef EXA_WF_MAX_QUEUE
+#define EXA_WF_MAX_QUEUE (1u << 22)
+#endif
+
 #ifndef EXA_TABLE_UNIFIED_MAX_SHIFT
 #define EXA_TABLE_UNIFIED_MAX_SHIFT 4
 #endif
@@ -882,7 +887,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
     if ((useWavefront() || learned) && lpUse.integrator != EXA_RAY_MARCHING_INTEGRATOR) {
       // queue capacity: the frame's samples, at most 4M records in flight
       const unsigned cap = (unsigned)std::min<size_t>((size_t)((width + 15) / 16) * ((height + 7) / 8) * 128 *
-                                                          (size_t)lp->render.spp, (size_t)1 << 22);
+                                                          (size_t)lp->render.spp, (size_t)EXA_WF_MAX_QUEUE);
       if (ctx->wfCap < cap) {
         ctx->wfRecords.alloc((size_t)3 * kWfLaneWords * cap);
         ctx->wfCounters.alloc(kWfCounterWords);
