@@ -480,6 +480,18 @@ int exa_sampler_compute_max_opacities(exa_context *ctx,
  * opacity.  exa_sampler_set_lps writes the filter to lp.ext.tfFilter; a
  * render whose lp.ext.tfFilter differs is rejected. */
 int exa_set_transfer_function_filter(exa_context *ctx, int32_t filter);
+/* How exa_render runs a path-traced or direct-light frame (no reference
+ * counterpart; every choice renders the same frame bit for bit):
+ * EXA_RENDER_PATH_AUTO (the default) renders a frame of at most one wave of
+ * samples (about 78K on a GB300) with one launch of a thread per sample and
+ * larger frames with the wavefront renderer; _WAVEFRONT and _SINGLE_LAUNCH
+ * force one.  Frames with a surface mesh, the Teaser shade mode, the heat
+ * map or a band of rows, and learned-field frames, always use the
+ * wavefront renderer. */
+#define EXA_RENDER_PATH_AUTO           0
+#define EXA_RENDER_PATH_WAVEFRONT      1
+#define EXA_RENDER_PATH_SINGLE_LAUNCH  2
+int exa_set_render_path(exa_context *ctx, int32_t path);
 /* ExaStitchSampler::setLPs (sampler/ExaStitchSampler.cpp:356-365) plus the
  * majorant-grid and max-opacity LP variables OWLRenderer::initGPU and
  * setColorMap set (OWLRenderer.cpp:435-436, 652-657). */

@@ -36,6 +36,9 @@ LIGHT_POINT = 0
 LIGHT_DIRECTIONAL = 1
 TF_FILTER_NEAREST = 0   # the reference's buffer lookup
 TF_FILTER_LINEAR = 1    # its texture lookup (EXASTITCH_CUDA_TEXTURE_TF)
+RENDER_PATH_AUTO = 0
+RENDER_PATH_WAVEFRONT = 1
+RENDER_PATH_SINGLE_LAUNCH = 2
 DEVERR_DDA_CAP = 1
 DEVERR_TRACK_CAP = 2
 DEVERR_BVH_STACK = 4
@@ -312,6 +315,7 @@ def lib():
         "exa_sampler_compute_max_opacities": ([ctx_p, vp, i32, range1f], C.c_int),
         "exa_sampler_set_lps": ([ctx_p, C.POINTER(LaunchParams)], C.c_int),
         "exa_set_transfer_function_filter": ([ctx_p, i32], C.c_int),
+        "exa_set_render_path": ([ctx_p, i32], C.c_int),
         "exa_debug_set_flags": ([ctx_p, C.c_uint32], C.c_int),
         "exa_sampler_class_name": ([], C.c_char_p),
         "exa_get_majorants": ([ctx_p, vp, vp], C.c_int),
@@ -409,6 +413,12 @@ class Context:
 
     def sync(self):
         _check(lib().exa_sync(self.h))
+
+    def set_render_path(self, p):
+        """RENDER_PATH_AUTO (small frames in one launch, the rest by the
+        wavefront renderer), RENDER_PATH_WAVEFRONT or
+        RENDER_PATH_SINGLE_LAUNCH; every choice renders the same frame"""
+        _check(lib().exa_set_render_path(self.h, int(p)))
 
     def set_tf_filter(self, f):
         """TF_FILTER_NEAREST or TF_FILTER_LINEAR for the next

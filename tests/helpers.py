@@ -44,6 +44,9 @@ class GpuScene:
         self.E = E
         self.ds = ds
         self.ctx = ctx or E.Context(0)
+        # the parity tests render small frames; they test the wavefront
+        # renderer (the benchmarked path) unless a test picks the other
+        self.ctx.set_render_path(E.RENDER_PATH_WAVEFRONT)
         self.model = E.ExaStitchModel.from_dataset(self.ctx, ds)
         self.num_mcs = tuple(num_mcs)
         self.model.setNumGridCells(self.num_mcs)

@@ -166,10 +166,21 @@ def _render_pair(g, o, torch, w, h, integrator, spp, light, ext, frames=1):
     (0, 2, "directional", True),    # path tracer, albedo 0.8 / HG 0.3 / 8 bounces
     (0, 1, "none", False),          # ambient (no light)
 ])
-def test_render_bit_exact(scenes, torch_cuda, integrator, spp, light, ext):
+@pytest.mark.parametrize("path", ["wavefront", "single_launch", "auto"])
+def test_render_bit_exact(scenes, torch_cuda, integrator, spp, light, ext, path):
+    """Both renderers of exa_render (and the automatic choice, which takes
+    the single launch for a frame this small) against the oracle."""
     ds, g, o = scenes
+    from owlexastitcher_gb300 import exastitch as E
     w, h = 48, 40
-    fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, w, h, integrator, spp, light, ext)
+    g.ctx.set_render_path({"wavefront": E.RENDER_PATH_WAVEFRONT, "single_launch": E.RENDER_PATH_SINGLE_LAUNCH,
+                           "auto": E.RENDER_PATH_AUTO}[path])
+    try:
+        fb, acc, tT, tTr, hfb, hacc, htT, htTr = _render_pair(g, o, torch_cuda, w, h, integrator, spp, light, ext)
+        st = g.ctx.render_stats()
+    finally:
+        g.ctx.set_render_path(E.RENDER_PATH_WAVEFRONT)
+    assert st["wavefront"] == (1 if path == "wavefront" else 0)
     assert np.array_equal(fb, hfb)
     assert acc.tobytes() == hacc.tobytes()
     assert tT.tobytes() == htT.tobytes()      # per-ray free-flight distance
