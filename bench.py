@@ -373,8 +373,9 @@ def run_ours(a):
             "cpu_baseline": cpu,
             "parity": parity,
             "clocks": clocks,
-            # per launched round: camera, walk, events and round-end kernels; then the resolve
-            "gpu_launches": a.steps * (4 * render_stats["walkLaunches"] + 1) if render_stats["wavefront"] else 2 * a.steps,
+            # the library's count of its kernel launches per frame (camera, walk, events and
+            # round-end kernels of each round, the resolve)
+            "gpu_launches": a.steps * render_stats["kernelLaunches"],
             "render": render_stats,
             "majorant_build": majorants,
             "learned_field": learned,

@@ -554,6 +554,7 @@ typedef struct {
   float    cameraMs;       /* summed GPU time of the camera kernels       */
   float    walkMs;         /* summed GPU time of the walk kernels         */
   float    eventMs;        /* summed GPU time of the event kernels        */
+  uint32_t kernelLaunches; /* this library's kernel launches of the frame */
 } exa_render_stats;
 int exa_get_render_stats(exa_context *ctx, exa_render_stats *out);
 

@@ -922,8 +922,10 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
       ctx->lastStats.cameraMs = st.cameraMs;
       ctx->lastStats.walkMs = st.walkMs;
       ctx->lastStats.eventMs = st.eventMs;
+      ctx->lastStats.kernelLaunches = st.kernelLaunches;
     } else {
       ctx->lastStats = exa_render_stats{};
+      ctx->lastStats.kernelLaunches = 2;  // the single launch and the resolve
       launchRender(ctx->sampler->accel, lpUse, width, height, ctx->jobCounter.ptr, ctx->sampleColors.ptr,
                    ctx->stream);
     }

@@ -295,7 +295,7 @@ void launchElemCells(const float4 *verts, const int32_t *idx, size_t ne, ElemOcc
 // wavefront renderer: bufs holds 3 * kWfLaneWords * cap words, counters
 // kWfCounterWords words
 struct WfStats {
-  unsigned rounds = 0, peakQueue = 0, walkLaunches = 0;
+  unsigned rounds = 0, peakQueue = 0, walkLaunches = 0, kernelLaunches = 0;
   float cameraMs = 0.f, walkMs = 0.f, eventMs = 0.f;
 };
 void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width, int height, float4 *colors,

@@ -1834,8 +1834,11 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
   std::vector<cudaEvent_t> &pool = pools[dev];
   const bool timing = stats != nullptr;
   int inIdx = 0, outIdx = 1, launched = 0;
+  unsigned kernels = 0;
   WfFrameCtl h{};
-  // a frame whose jobs all fit the first round needs no camera launch after it
+  // no camera launch once every job is issued: after the first round of a
+  // frame whose jobs all fit it, or once a group's check has seen it
+  bool issuedAll = false;
   const bool oneIssue = c0.nNew == total - c0.issued;
   // rounds per host check: few at first (small frames end in a few rounds),
   // more once the frame proves long
@@ -1851,11 +1854,12 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
       cudaEvent_t *ev = timing ? &pool[4 * (size_t)launched] : nullptr;
       WfQueues Q{buf[inIdx], buf[outIdx], buf[2], counters, cap, 0, ctl};
       if (timing) cudaCheck(cudaEventRecord(ev[0], s), "event");
-      if (launched == 0 || !oneIssue) {
+      if (launched == 0 || (!oneIssue && !issuedAll)) {
         // (the first round's job count is known here; later rounds read theirs)
         const unsigned g = launched == 0 ? std::max(1u, std::min<unsigned>(grid, (c0.nNew + 127) / 128)) : grid;
         if (pt) k_wf_camera<EXA_PATH_TRACING_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, 0u, 0u);
         else k_wf_camera<EXA_DIRECT_LIGHT_INTEGRATOR><<<g, 128, 0, s>>>(A, lp, width, height, colors, Q, 0u, 0u);
+        ++kernels;
       }
       if (timing) cudaCheck(cudaEventRecord(ev[1], s), "event");
       if (sur) k_wf_walk_sur<<<walkGrid, 128, kSurWalkSmem, s>>>(A, lp, Q, *sur);
@@ -1866,12 +1870,14 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
       else k_wf_events<EXA_DIRECT_LIGHT_INTEGRATOR><<<grid, 128, 0, s>>>(A, lp, width, height, colors, Q);
       if (timing) cudaCheck(cudaEventRecord(ev[3], s), "event");
       k_wf_round_end<<<1, 32, 0, s>>>(counters, ctl, cap, parkWalks, lp.ext.deviceErrors);
+      kernels += 3;  // walk, events, round end
       cudaCheck(cudaGetLastError(), "wavefront round");
       std::swap(inIdx, outIdx);
     }
     cudaCheck(cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, s), "read frame control");
     cudaCheck(cudaStreamSynchronize(s), "wavefront rounds");
     if (!h.more) break;
+    issuedAll = h.issued >= h.total;
   }
   if (stats) {
     for (int r = 0; r < launched; ++r) {
@@ -1884,6 +1890,7 @@ void renderWavefront(const AccelView &A, const exa_launch_params &lp, int width,
     }
     stats->rounds = h.rounds;
     stats->walkLaunches = (unsigned)launched;
+    stats->kernelLaunches = kernels + 1;  // and the resolve
     stats->peakQueue = std::max(stats->peakQueue, h.peak);
   }
   const int pb = rowBegin * width, pe = rowEnd * width;

@@ -206,7 +206,7 @@ class LaunchParams(C.Structure):
 class RenderStats(C.Structure):
     _fields_ = [("wavefront", C.c_uint32), ("rounds", C.c_uint32), ("peakQueue", C.c_uint32),
                 ("queueCapacity", C.c_uint32), ("walkLaunches", C.c_uint32), ("cameraMs", C.c_float),
-                ("walkMs", C.c_float), ("eventMs", C.c_float)]
+                ("walkMs", C.c_float), ("eventMs", C.c_float), ("kernelLaunches", C.c_uint32)]
 
 
 class BuildStats(C.Structure):
