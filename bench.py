@@ -161,6 +161,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def clocks_rejected(c, low=0.85):
+    """whether a timed region's clock record fails the timing rules: a
+    hardware or thermal slowdown, or SM clocks well below their maximum with
+    no reason given (a clock lock left by another process); a power cap
+    alone is kept"""
+    if {"hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"} & set(c.get("reasons") or []):
+        return True
+    sm, mx = c.get("sm_mhz"), c.get("sm_max_mhz")
+    return bool(sm and mx and sm < low * mx and not c.get("reasons"))
+
+
 def make_scene(a, device):
     """The workload's dataset, made by the GPU generator; returns it and the
     generator record (wall seconds, per-stage seconds; the CPU generator's
@@ -235,28 +246,36 @@ def run_ours(a):
         torch.cuda.synchronize()
         return
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
-    with ClockSampler(local) as clk:
-        barrier()
-        torch.cuda.synchronize()
-        for i in range(a.steps):
-            flush.fill_(float(i))
-            starts[i].record(stream)
-            step()
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-        barrier()
-    ctx.sync()
+    def timed_steps():
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+        with ClockSampler(local) as clk:
+            barrier()
+            torch.cuda.synchronize()
+            for i in range(a.steps):
+                flush.fill_(float(i))
+                starts[i].record(stream)
+                step()
+                ends[i].record(stream)
+            torch.cuda.synchronize()
+            barrier()
+        ctx.sync()
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)], clk.summary()
+
+    step_ms, clocks = timed_steps()
+    # a timed region whose clocks any rank rejects is timed once more, and
+    # the second record is reported
+    remeasured = replicas.slowest_ms(float(clocks_rejected(clocks)), world, device="cuda") > 0
+    if remeasured:
+        step_ms, clocks = timed_steps()
+    clocks["remeasured"] = remeasured
     render_stats = ctx.render_stats()
     # the last timed frame (accumID 0: the accumulation buffer holds its
     # per-pixel sums) for the CPU leg's bit-for-bit comparison
     timed_frame = (r.accum.cpu().numpy().reshape(-1, 4).copy(), r.fb.cpu().numpy().view(np.uint32).copy())
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = replicas.slowest_ms(sum(step_ms) / len(step_ms), world, device="cuda")
     # bands: the ranks share one frame's paths; replicas: every rank a frame
     value = replicas.job_paths_per_s(1 if bands else world, paths_per_step, ms)
-    clocks = clk.summary()
 
     # counting launch (same frame): algorithmic work of one launch
     cnt = torch.zeros(16, dtype=torch.int64, device="cuda")
