@@ -41,3 +41,29 @@ def test_dataset_gridlets_live(ref):
             a = ref.intersect_gridlet(p, g, d.gridlet_scalars)
             b = ref.ref_intersect_gridlet(p, g, d.gridlet_scalars)
             assert a[0] == b[0] and (not a[0] or (a[2] == b[2] and np.float32(a[1]).tobytes() == np.float32(b[1]).tobytes()))
+
+
+def test_dda_rays_from_outside_live(ref):
+    """rays that start outside the grid box (as camera rays do), with tmin > 0
+    for half of them and a direction component of 1e-6 for some: the cells and
+    their entry / exit distances equal DDA.h's bit for bit (the golden
+    vectors start every ray inside the box)"""
+    rng = np.random.default_rng(7)
+    cells = 0
+    for i in range(600):
+        dims = rng.integers(1, 40, 3).astype(np.int32)
+        lo = rng.uniform(-10, 10, 3).astype(np.float32)
+        hi = (lo + rng.uniform(1, 100, 3)).astype(np.float32)
+        org = rng.uniform(lo - (hi - lo), hi + (hi - lo)).astype(np.float32)
+        d = rng.uniform(lo, hi).astype(np.float64) - org
+        d = (d / np.linalg.norm(d)).astype(np.float32)
+        if i % 7 == 0:
+            d[rng.integers(0, 3)] = np.float32(1e-6)
+        tmin = np.float32(0.0 if i % 2 else rng.uniform(0, 20))
+        tmax = np.float32(1e10 if i % 3 else rng.uniform(0, 150))
+        a = ref.dda3(org, d, tmin, tmax, dims, lo, hi, 1024)
+        b = ref.ref_dda3(org, d, tmin, tmax, dims, lo, hi, 1024)
+        assert np.array_equal(a[0], b[0]), i
+        assert a[1].tobytes() == b[1].tobytes() and a[2].tobytes() == b[2].tobytes(), i
+        cells += len(b[0])
+    assert cells > 10000
