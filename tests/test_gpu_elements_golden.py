@@ -36,6 +36,63 @@ def element_model(V):
     return verts, idx
 
 
+def degenerate_elements(rng, nv, n):
+    """n elements with nv vertices, by turns flattened along an axis (to
+    1e-4..1e-2 of their size), with two vertices collapsed, strongly twisted,
+    or mildly perturbed, each in its own cell of a 40-unit lattice (so no two
+    overlap), and per element three points: one uniform over its bounds
+    widened by 5 %, its vertex mean and one of its vertices"""
+    from golden.make_golden import SHAPES
+    base = SHAPES[nv]
+    V = np.zeros((n, nv, 4), np.float32)
+    P = np.zeros((n, 3, 3), np.float32)
+    for i in range(n):
+        B = base.copy()
+        kind = i % 4
+        if kind == 0:
+            B[:, rng.integers(0, 3)] *= rng.uniform(1e-4, 1e-2)
+        elif kind == 1:
+            a, b = rng.choice(nv, 2, replace=False)
+            B[b] = B[a]
+        elif kind == 2:
+            B = B + rng.normal(0, 0.4, B.shape)
+        else:
+            B = B + rng.normal(0, 0.08, B.shape)
+        cell = np.array([i % 16, (i // 16) % 16, i // 256], np.float32) * 40
+        V[i, :, :3] = B * rng.uniform(0.5, 8) + cell
+        V[i, :, 3] = rng.uniform(-1, 1, nv)
+        lo, hi = V[i, :, :3].min(0), V[i, :, :3].max(0)
+        P[i, 0] = rng.uniform(lo - 0.05 * (hi - lo), hi + 0.05 * (hi - lo))
+        P[i, 1] = V[i, :, :3].mean(0)
+        P[i, 2] = V[i, rng.integers(0, nv), :3]
+    return V, P
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nv", [4, 5, 6, 8], ids=["tet", "pyramid", "wedge", "hex"])
+def test_degenerate_elements_on_gpu(cuda, native, oracle, nv):
+    """flattened, collapsed and twisted elements (where the Newton inversion
+    may stop at its iteration cap) sample bit for bit as the oracle, which
+    equals the reference's headers on them (test_oracle_ref.py)"""
+    from owlexastitcher_gb300 import exastitch as E
+    V, P = degenerate_elements(np.random.default_rng(31), nv, 1024)
+    P = P.reshape(-1, 3)
+    verts, idx = element_model(V)
+    ctx = E.Context(0)
+    model = E.ExaStitchModel(ctx, verts, idx, np.zeros(0, E.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    model.setNumGridCells((16, 16, 8))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    got = sampler.sample_host(P)
+    assert ctx.device_errors() == 0
+    ctx.close()
+    want = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32)).sample(P)
+    assert np.array_equal(got["primID"], want["primID"]) and np.array_equal(got["cellID"], want["cellID"])
+    assert got["value"].tobytes() == want["value"].tobytes()
+    hit = want["primID"] >= 0
+    assert hit.sum() > 200 and np.all(want["primID"][hit] == np.nonzero(hit)[0] // 3)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("nv", [4, 5, 6, 8], ids=["tet", "pyramid", "wedge", "hex"])
 def test_elements_golden_on_gpu(cuda, native, oracle, nv):

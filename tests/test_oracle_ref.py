@@ -67,3 +67,21 @@ def test_dda_rays_from_outside_live(ref):
         assert a[1].tobytes() == b[1].tobytes() and a[2].tobytes() == b[2].tobytes(), i
         cells += len(b[0])
     assert cells > 10000
+
+
+def test_degenerate_elements_live(ref):
+    """flattened, collapsed and twisted elements (the Newton inversion may stop
+    at its iteration cap): the oracle's hit flag and value equal the
+    reference headers' bit for bit; the GPU test of the same elements
+    compares the CUDA path with the oracle"""
+    from test_gpu_elements_golden import degenerate_elements
+    hits = 0
+    for nv in (4, 5, 6, 8):
+        V, P = degenerate_elements(np.random.default_rng(31), nv, 1024)
+        for i in range(len(V)):
+            for p in P[i]:
+                a, b = ref.intersect_elem(p, V[i]), ref.ref_intersect_elem(p, V[i])
+                assert a[0] == b[0], (nv, i, p)
+                assert not a[0] or np.float32(a[1]).tobytes() == np.float32(b[1]).tobytes(), (nv, i, p)
+                hits += bool(b[0])
+    assert hits > 1000
