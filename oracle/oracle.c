@@ -1393,7 +1393,11 @@ static v4 lookup_tf(const exa_launch_params *lp, float f)
   if (lp->transferFunc.numValues == 0) return zero;
   if (lp->ext.tfFilter == EXA_TF_FILTER_LINEAR)
     return lookup_tf_linear(lp->transferFunc.values, lp->transferFunc.numValues, f);
-  f = fmax_t(0.f, fmin_t(1.f, f));
+  /* min(1, f) in std::min's operand order, as fminf also gives it: a NaN
+   * value (an element with collapsed vertices passes its inside tests with
+   * NaN weights) clamps to 1, the last entry, and no NaN reaches the
+   * conversion to int */
+  f = fmax_t(0.f, f < 1.f ? f : 1.f);
   const int i = imin_t(lp->transferFunc.numValues - 1, (int)(f * (float)lp->transferFunc.numValues));
   return lp->transferFunc.values[i];
 }
@@ -2082,7 +2086,7 @@ static double d_lookup_alpha(const exa_launch_params *lp, double v, double rgb[3
     return (1 - a) * p.w + a * q.w;
   }
   if (fv < 0) fv = 0;
-  if (fv > 1) fv = 1;
+  if (!(fv < 1)) fv = 1; /* NaN as well, as the binary32 lookup clamps it */
   int i = (int)(fv * lp->transferFunc.numValues);
   if (i > lp->transferFunc.numValues - 1) i = lp->transferFunc.numValues - 1;
   const v4 c = lp->transferFunc.values[i];

@@ -78,7 +78,10 @@ EXA_D float4 lookup_tf(const exa_launch_params &lp, float f)
   if (lp.transferFunc.numValues == 0) return make_float4(0.f, 0.f, 0.f, 0.f);
   if (lp.ext.tfFilter == EXA_TF_FILTER_LINEAR)
     return lookup_tf_linear(reinterpret_cast<const float4 *>(lp.transferFunc.values), lp.transferFunc.numValues, f);
-  f = fmax_t(0.f, fmin_t(1.f, f));
+  // min(1, f) in std::min's operand order (fminf gives the same): a NaN
+  // value, which an element with collapsed vertices yields, clamps to 1 (the
+  // last entry), and no NaN reaches the conversion to int
+  f = fmax_t(0.f, f < 1.f ? f : 1.f);
   const int i = imin_t(lp.transferFunc.numValues - 1, (int)(f * (float)lp.transferFunc.numValues));
   return __ldg(reinterpret_cast<const float4 *>(lp.transferFunc.values) + i);
 }

@@ -38,7 +38,9 @@ def element_model(V):
 
 def degenerate_elements(rng, nv, n):
     """n elements with nv vertices, by turns flattened along an axis (to
-    1e-4..1e-2 of their size), with two vertices collapsed, strongly twisted,
+    1e-4..1e-2 of their size), perturbed with two vertices then collapsed
+    (a tet becomes a triangle whose inside test passes off its plane with NaN
+    weights, as Plane.h's does), strongly twisted,
     or mildly perturbed, each in its own cell of a 40-unit lattice (so no two
     overlap), and per element three points: one uniform over its bounds
     widened by 5 %, its vertex mean and one of its vertices"""
@@ -51,7 +53,8 @@ def degenerate_elements(rng, nv, n):
         kind = i % 4
         if kind == 0:
             B[:, rng.integers(0, 3)] *= rng.uniform(1e-4, 1e-2)
-        elif kind == 1:
+        elif kind == 1:  # in a general orientation, so that its box is not flat
+            B = B + rng.normal(0, 0.3, B.shape)
             a, b = rng.choice(nv, 2, replace=False)
             B[b] = B[a]
         elif kind == 2:
@@ -88,9 +91,86 @@ def test_degenerate_elements_on_gpu(cuda, native, oracle, nv):
     ctx.close()
     want = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32)).sample(P)
     assert np.array_equal(got["primID"], want["primID"]) and np.array_equal(got["cellID"], want["cellID"])
-    assert got["value"].tobytes() == want["value"].tobytes()
+    # tets with two collapsed vertices hit with NaN values (as Plane.h's test
+    # does); a NaN's bits are the host's or the GPU's default NaN, so NaNs
+    # compare as NaN and every other value bit for bit
+    nan = np.isnan(want["value"])
+    assert np.array_equal(np.isnan(got["value"]), nan)
+    assert got["value"][~nan].tobytes() == want["value"][~nan].tobytes()
     hit = want["primID"] >= 0
     assert hit.sum() > 200 and np.all(want["primID"][hit] == np.nonzero(hit)[0] // 3)
+    assert (nan & hit).any() == (nv == 4)
+
+
+def collapsed_scene(rng, side=4, spacing=6.0, size=10.0):
+    """side^3 overlapping tets of about `size` on a lattice of `spacing`,
+    every other one perturbed and then collapsed to a triangle: about half
+    of the hits in the scene's box carry NaN values"""
+    from golden.make_golden import SHAPES
+    n = side ** 3
+    V = np.zeros((n, 4, 4), np.float32)
+    for i in range(n):
+        B = SHAPES[4] + rng.normal(0, 0.3, (4, 3))
+        if i % 2 == 0:
+            a, b = rng.choice(4, 2, replace=False)
+            B[b] = B[a]
+        cell = np.array([i % side, (i // side) % side, i // side ** 2], np.float32) * spacing
+        V[i, :, :3] = B * size + cell
+        V[i, :, 3] = rng.uniform(-1, 1, 4)
+    return V
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tf_filter", [0, 1], ids=["nearest", "linear"])
+@pytest.mark.parametrize("integrator,light,ext", [(0, "directional", True), (1, "point", False), (2, "none", False)])
+def test_collapsed_tets_render_bit_exact(cuda, native, oracle, tf_filter, integrator, light, ext):
+    """frames over overlapping tets, half of them collapsed: their samples
+    carry NaN values, which the nearest transfer-function lookup clamps to
+    its last entry and the linear one maps to the zero border; the domain
+    ends past the largest value, so under the nearest filter only NaN samples
+    take the last entry (the oracle's frame changes with it); all three
+    integrators render bit for bit as the oracle"""
+    import ctypes as C
+    import types
+
+    from helpers import GpuScene, OracleScene, host_lp, orbit_camera, ramp_tf, setup_render
+    from owlexastitcher_gb300 import exastitch as E
+    verts, idx = element_model(collapsed_scene(np.random.default_rng(5)))
+    ds = types.SimpleNamespace(vertices=verts, indices=idx, gridlets=np.zeros(0, E.GRIDLET_DTYPE),
+                               gridlet_scalars=np.zeros(0, np.float32))
+    dims = (8, 8, 8)
+    g = GpuScene(ds, dims, tf=ramp_tf())
+    vmin, vmax = g.xf
+    g.xf = (vmin, np.float32(vmax + (vmax - vmin) / 8))
+    if tf_filter:
+        g.ctx.set_tf_filter(E.TF_FILTER_LINEAR)
+    g.sampler.computeMaxOpacities(g.tf, g.xf)
+    g.sampler.setLPs(g.lp)
+    o = OracleScene(oracle, ds, dims, g.lo, g.hi, g.tf, g.xf, tf_filter=tf_filter)
+    w, h = 48, 32
+    lp = setup_render(g.lp, orbit_camera(g.lo, g.hi, w, h), w, h, integrator, 2, light, ext, g.lo, g.hi)
+    n = w * h
+    fb = cuda.zeros(n, dtype=cuda.int32, device="cuda")
+    acc = cuda.zeros(n * 4, dtype=cuda.float32, device="cuda")
+    lp.accumID = 0
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), acc.data_ptr()
+    lp.ext.traceT = lp.ext.traceTr = None
+    E._check(E.lib().exa_render(g.ctx.h, C.byref(lp), w, h))
+    g.ctx.sync()
+    assert g.ctx.device_errors() == 0
+    hl, hfb, hacc, _, _ = host_lp(lp, o, w, h)
+    assert o.f.render(bytes(hl), w, h) == 0
+    assert acc.cpu().numpy().reshape(-1, 4).tobytes() == hacc.tobytes()
+    assert np.array_equal(fb.cpu().numpy().view(np.uint32), hfb)
+    assert len(np.unique(hfb)) > 100
+    if tf_filter == 0:
+        tf0 = g.tf.copy()
+        tf0[-1] = 0.0
+        o0 = OracleScene(oracle, ds, dims, g.lo, g.hi, tf0, g.xf)
+        hl0, _, hacc0, _, _ = host_lp(lp, o0, w, h)
+        assert o0.f.render(bytes(hl0), w, h) == 0
+        assert np.count_nonzero(np.any(hacc0 != hacc, axis=1)) > 50
+    g.ctx.close()
 
 
 @pytest.mark.gpu

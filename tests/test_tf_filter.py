@@ -47,8 +47,10 @@ def test_linear_lookup_known_answers(oracle):
     assert out[3, 3] == np.float32(0.5 * tf[-1, 3])
     # the nearest filter clamps instead
     lpn = _lp(E, tf, (0.0, 1.0), E.TF_FILTER_NEAREST)
-    out = oracle.lookup_tf(bytes(lpn), np.array([-1.0, 2.0, 0.49], np.float32))
+    out = oracle.lookup_tf(bytes(lpn), np.array([-1.0, 2.0, 0.49, np.nan], np.float32))
     assert out[0, 3] == tf[0, 3] and out[1, 3] == tf[-1, 3] and out[2, 3] == tf[3, 3]
+    # NaN clamps to 1 as under std::min / fminf: the last entry
+    assert np.array_equal(out[3], tf[-1])
 
 
 @pytest.mark.parametrize("tf_fn", [ramp_tf, two_peak_tf])
