@@ -9,7 +9,12 @@ golden point is sampled through exa_sample_points_host.  Where the point lies
 in no other element of the model (the oracle's list of every containing
 primitive decides), the GPU's answer must be the golden one: the hit flag,
 the element id and the value's bits.  A quarter of the points sit on a
-vertex or an edge midpoint (boundary cases of the inside tests)."""
+vertex or an edge midpoint (boundary cases of the inside tests).
+
+Degenerate elements (flattened, collapsed, twisted) sample as the oracle,
+whose answers on them equal the reference headers' (test_oracle_ref.py), and
+frames over overlapping collapsed tets, whose samples carry NaN values, render
+bit for bit as the oracle under both transfer-function filters."""
 import os
 
 import numpy as np
