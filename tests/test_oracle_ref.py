@@ -85,3 +85,68 @@ def test_degenerate_elements_live(ref):
                 assert not a[0] or np.float32(a[1]).tobytes() == np.float32(b[1]).tobytes(), (nv, i, p)
                 hits += bool(b[0])
     assert hits > 1000
+
+
+def test_extreme_gridlets_live(ref):
+    """gridlets of levels up to 19 at lattice coordinates of +-5000 with NaN
+    holes and signed zeros; points inside, on faces and corners, on cell
+    planes, around the box, and with a NaN or infinite coordinate: the hit,
+    the cell and the value's bits equal Gridlet.h's"""
+    rng = np.random.default_rng(9)
+    hits = 0
+    for i in range(4000):
+        g = np.zeros(1, ref.GRIDLET_DTYPE)[0]
+        dims = rng.integers(0, 9, 3)
+        level = int(rng.integers(0, 20))
+        lower = rng.integers(-5000, 5000, 3)
+        g["lower"], g["level"], g["dims"], g["begin"] = lower, level, dims, 0
+        ns = int(np.prod(dims + 1))
+        sc = rng.uniform(-1, 1, ns).astype(np.float32)
+        sc[rng.uniform(size=ns) < 0.15] = np.nan
+        if i % 9 == 0:
+            sc[rng.uniform(size=ns) < 0.5] = -0.0
+        cw = float(2 ** level)
+        lo, hi = (lower + 0.5) * cw, (lower + dims + 0.5) * cw
+        k = i % 5
+        if k == 0:
+            p = rng.uniform(lo, hi)
+        elif k == 1:
+            p = np.where(rng.random(3) < 0.5, lo, hi)
+        elif k == 2:
+            p = lo + cw * rng.integers(0, 9, 3)
+        elif k == 3:
+            p = rng.uniform(lo, hi)
+            p[rng.integers(0, 3)] = [np.nan, np.inf, -np.inf][i % 3]
+        else:
+            p = rng.uniform(lo - cw, hi + cw)
+        p = p.astype(np.float32)
+        a, b = ref.intersect_gridlet(p, g, sc), ref.ref_intersect_gridlet(p, g, sc)
+        assert a[0] == b[0], (i, p)
+        assert not a[0] or (a[2] == b[2] and np.float32(a[1]).tobytes() == np.float32(b[1]).tobytes()), (i, p)
+        hits += bool(b[0])
+    assert hits > 500
+
+
+def test_extreme_projections_live(ref):
+    """projectOnGrid for boxes of 1e-3 to 1e5 units at +-1e4, grids with a
+    single cell along an axis, and points far outside, up to 1e30, exactly on
+    the box and on cell faces: the cell equals Grid.cuh's"""
+    rng = np.random.default_rng(4)
+    for i in range(4000):
+        dims = rng.integers(1, 512, 3).astype(np.int32)
+        if i % 5 == 0:
+            dims[rng.integers(0, 3)] = 1
+        lo = rng.uniform(-1e4, 1e4, 3).astype(np.float32)
+        ext = np.float32(10.0) ** rng.uniform(-3, 5, 3)
+        hi = (lo + ext).astype(np.float32)
+        k = i % 4
+        if k == 0:
+            V = rng.uniform(lo - 10 * ext, hi + 10 * ext)
+        elif k == 1:
+            V = rng.uniform(-1e30, 1e30, 3)
+        elif k == 2:
+            V = np.where(rng.random(3) < 0.5, lo, hi)
+        else:
+            V = lo + ext * rng.integers(0, 8, 3) / 7.0
+        V = V.astype(np.float32)
+        assert ref.project_on_grid(V, dims, lo, hi) == ref.ref_project_on_grid(V, dims, lo, hi), (i, V)
