@@ -110,9 +110,12 @@ void ExaStitchModel::assign(const exa_vec4f *v, size_t nv, const int32_t *idx, s
     cellBounds.lower.z = std::min(cellBounds.lower.z, z); cellBounds.upper.z = std::max(cellBounds.upper.z, z);
   };
   for (size_t e = 0; e < ne; ++e)
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0, padded = 0; j < 8; ++j) {
       const int id = indices[e * 8 + j];
-      if (id < 0) continue;
+      if (id < 0) { padded = 1; continue; }
+      // rows are -1 padded: a vertex after the padding would leave the
+      // reference's vertex slots unset (programs/ExaStitchSampler.cu:135-143)
+      if (padded) throw Error(EXA_ERR_INVALID, "element index row with a vertex after its -1 padding");
       if ((size_t)id >= nv) throw Error(EXA_ERR_INVALID, "element index out of range");
       const exa_vec4f &p = vertices[id];
       extend(p.x, p.y, p.z);

@@ -313,6 +313,9 @@ EXA_D bool intersect_elem(float &value, V3 P, const int32_t *__restrict__ idx8, 
 {
   const int4 i0 = __ldg(reinterpret_cast<const int4 *>(idx8));
   const int4 i1 = __ldg(reinterpret_cast<const int4 *>(idx8) + 1);
+  // rows of fewer than 4 vertices name no element type and are never hit
+  // (the model rejects rows with a vertex after the padding)
+  if (i0.w < 0) return false;
   const int nv = 4 + (i1.x >= 0) + (i1.y >= 0) + (i1.z >= 0) + (i1.w >= 0);
   float4 v[8];
   v[0] = __ldg(verts + i0.x); v[1] = __ldg(verts + i0.y); v[2] = __ldg(verts + i0.z); v[3] = __ldg(verts + i0.w);

@@ -179,6 +179,43 @@ def test_collapsed_tets_render_bit_exact(cuda, native, oracle, tf_filter, integr
 
 
 @pytest.mark.gpu
+def test_rows_without_an_element_type(cuda, native, oracle):
+    """index rows of 0, 1, 2, 3 and 7 vertices name no element type
+    (programs/ExaStitchSampler.cu:145-148 tests 4, 5, 6 and 8 only): they
+    overlap a hex and are never hit, and the points sample bit for bit as
+    the oracle; a row with a vertex after its -1 padding is rejected"""
+    from owlexastitcher_gb300 import exastitch as E
+    hexv = np.array([[0, 0, 0], [4, 0, 0], [4, 4, 0], [0, 4, 0], [0, 0, 4], [4, 0, 4], [4, 4, 4], [0, 4, 4]],
+                    np.float32)
+    rng = np.random.default_rng(8)
+    extra = rng.uniform(-1, 5, (24, 3)).astype(np.float32)
+    verts = np.zeros((8 + len(extra), 4), np.float32)
+    verts[:8, :3], verts[8:, :3] = hexv, extra
+    verts[:, 3] = rng.uniform(-1, 1, len(verts))
+    idx = -np.ones((6, 8), np.int32)
+    for r, count in enumerate((0, 1, 2, 3, 7)):  # the short rows come first: lower indices
+        idx[r, :count] = 8 + rng.choice(len(extra), count, replace=False)
+    idx[5] = np.arange(8)
+    P = rng.uniform(-0.5, 4.5, (20000, 3)).astype(np.float32)
+    ctx = E.Context(0)
+    model = E.ExaStitchModel(ctx, verts, idx, np.zeros(0, E.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    model.setNumGridCells((4, 4, 4))
+    sampler = E.ExaStitchSampler(ctx)
+    sampler.build(model)
+    got = sampler.sample_host(P)
+    assert ctx.device_errors() == 0
+    want = oracle.Field(verts, idx, np.zeros(0, oracle.GRIDLET_DTYPE), np.zeros(0, np.float32)).sample(P)
+    assert got.tobytes() == want.tobytes()
+    hit = got["primID"] >= 0
+    assert hit.mean() > 0.4 and np.all(got["primID"][hit] == 5)
+    gap = idx.copy()
+    gap[5, 3] = -1  # a hex row with a hole
+    with pytest.raises(E.ExaError):
+        E.ExaStitchModel(ctx, verts, gap, np.zeros(0, E.GRIDLET_DTYPE), np.zeros(0, np.float32))
+    ctx.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("nv", [4, 5, 6, 8], ids=["tet", "pyramid", "wedge", "hex"])
 def test_elements_golden_on_gpu(cuda, native, oracle, nv):
     from owlexastitcher_gb300 import exastitch as E
