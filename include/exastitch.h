@@ -336,9 +336,12 @@ uint64_t exa_abi_sizeof(int32_t which);
 
 /* Replaces ExaStitchModel::load (model/ExaStitchModel.cpp:24-257) for
  * in-memory arrays: vertices (x,y,z,value), indices 8 per element padded
- * with -1 (4 = tet, 5 = pyramid, 6 = wedge, 8 = hex), gridlets and their
- * scalars.  Host pointers; arrays are copied.  Computes cellBounds and
- * valueRange as the loader does.  Either part may be empty. */
+ * with -1 (4 = tet, 5 = pyramid, 6 = wedge, 8 = hex; rows of other counts
+ * are never hit), gridlets and their scalars.  Host pointers; arrays are
+ * copied.  Computes cellBounds and valueRange as the loader does.  Either
+ * part may be empty.  EXA_ERR_INVALID for an index past the vertices, a row
+ * with a vertex after its -1 padding, a gridlet header with negative dims or
+ * a level outside 0..30, or scalars past the scalar array. */
 int exa_model_create(exa_context *ctx,
                      const exa_vec4f *vertices, uint64_t numVertices,
                      const int32_t *indices, uint64_t numElems,
