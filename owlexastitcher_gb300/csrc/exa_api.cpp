@@ -810,6 +810,16 @@ void needLpCaps(const exa_launch_params &lp, int samplerFilter)
   need(lp.ext.trackStepCap >= 0 && lp.ext.ddaCellCap >= 0, EXA_ERR_INVALID, "negative loop cap");
 }
 
+// the DDA indexes lp.maxOpacities by the cells of lp.majorantGrid: its dims
+// must be those of the grid the sampler built (exa_sampler_set_lps copies
+// them), else the walks would read past the max opacities
+void needGridDims(const exa_context *ctx, const exa_launch_params &lp)
+{
+  const exa_vec3i g = ctx->model && ctx->model->grid ? ctx->model->grid->dims : exa_vec3i{0, 0, 0};
+  need(lp.majorantGrid.dims.x == g.x && lp.majorantGrid.dims.y == g.y && lp.majorantGrid.dims.z == g.z,
+       EXA_ERR_INVALID, "lp.majorantGrid.dims are not the built majorant grid's (call exa_sampler_set_lps)");
+}
+
 // the context's model / sampler where a call needs the ExaStitch kind
 ExaStitchModel &esModel(exa_context *ctx)
 {
@@ -860,6 +870,7 @@ void renderFrame(exa_context *ctx, const exa_launch_params *lp, int32_t width, i
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     needLpCaps(*lp, ctx->sampler->tfFilter);
+    needGridDims(ctx, *lp);
     if (lp->ext.rowEnd > 0) {
       need(lp->ext.rowBegin >= 0 && lp->ext.rowBegin % 8 == 0 && lp->ext.rowBegin < lp->ext.rowEnd &&
                lp->ext.rowEnd <= height && (lp->ext.rowEnd % 8 == 0 || lp->ext.rowEnd == height),
@@ -2269,6 +2280,7 @@ extern "C" int exa_render_noalloc(exa_context *ctx, const exa_launch_params *lp,
          "no transfer function (call exa_sampler_compute_max_opacities and exa_sampler_set_lps)");
     need(lp->ext.maxBounces >= 0, EXA_ERR_INVALID, "maxBounces must be >= 0");
     needLpCaps(*lp, ctx->sampler->tfFilter);
+    needGridDims(ctx, *lp);
     need(lp->ext.rowEnd <= 0, EXA_ERR_INVALID, "row bands are not supported (exa_render renders them)");
     // as in exa_render: the AMR-cell and ExaBrick samplers have no gridlet
     // cells to colour

@@ -100,3 +100,30 @@ def test_build_copy_wait_timeout_reported(scene, oracle):
     assert same_floats(ranges, o.ranges)
     assert ctx.device_errors() == 0
     ctx.close()
+
+
+def test_majorant_grid_dims_checked(scene):
+    """launch parameters whose majorant grid is not the built one (the DDA
+    would index the max opacities past their end) are rejected by exa_render
+    and exa_render_noalloc before any launch; the dims set by
+    exa_sampler_set_lps render"""
+    torch, ds, g, o = scene
+    from owlexastitcher_gb300 import exastitch as E
+    w = h = 16
+    lp = setup_render(g.lp, orbit_camera(g.lo, g.hi, w, h), w, h, E.DIRECT_LIGHT_INTEGRATOR, 1, "directional", True,
+                      g.lo, g.hi)
+    fb = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+    lp.fbPointer, lp.accumBuffer = fb.data_ptr(), None
+    lp.ext.traceT = lp.ext.traceTr = None
+    dims = (lp.majorantGrid.dims.x, lp.majorantGrid.dims.y, lp.majorantGrid.dims.z)
+    assert dims == (32, 32, 32)
+    try:
+        lp.majorantGrid.dims = E.vec3i(64, 32, 32)
+        for fn in (E.lib().exa_render, E.lib().exa_render_noalloc):
+            assert fn(g.ctx.h, C.byref(lp), w, h) == E.EXA_ERR_INVALID
+            assert b"majorantGrid" in E.lib().exa_last_error()
+    finally:
+        lp.majorantGrid.dims = E.vec3i(*dims)
+    E._check(E.lib().exa_render(g.ctx.h, C.byref(lp), w, h))
+    g.ctx.sync()
+    assert g.ctx.device_errors() == 0
