@@ -541,9 +541,13 @@ int exa_launch_params_init(exa_launch_params *lp);
 /* One frame: width*height pixels, lp->render.spp samples each, into
  * lp->fbPointer (RGBA8) and lp->accumBuffer (device pointers owned by the
  * caller).  Replaces owlLaunch2D(rayGen,w,h,lp) (OWLRenderer.cpp:621).
- * The wavefront renderer reads its queue sizes back once per round, so
- * the call returns after the frame's kernels have been issued and most of
- * them have run; call exa_sync before reading the outputs. */
+ * The wavefront renderer reads back whether another round is needed once
+ * per group of rounds (4, then 8), so the call returns after the frame's
+ * kernels have been issued and most of them have run; call exa_sync before
+ * reading the outputs.  EXA_ERR_INVALID, before any launch, for launch
+ * parameters that exa_sampler_set_lps did not set for this context's
+ * sampler (the sampler handle, the majorant grid's dims, the transfer-
+ * function filter) and for unsupported options. */
 int exa_render(exa_context *ctx, const exa_launch_params *lp,
                int32_t width, int32_t height);
 
