@@ -63,3 +63,27 @@ def test_calls_without_context_fail_cleanly(native):
     assert L.exa_sampler_build(None) == E.EXA_ERR_STATE
     assert b"no model" in L.exa_last_error()
     assert L.exa_render(None, None, 1, 1) == E.EXA_ERR_STATE
+
+
+def test_python_constants_match_header():
+    """every integer constant of include/exastitch.h that the Python binding
+    mirrors (as EXA_NAME or NAME) has the header's value"""
+    from owlexastitcher_gb300 import exastitch as E
+    src = open(os.path.join(ROOT, "include", "exastitch.h")).read()
+    defs = {}
+    for name, body in re.findall(r"#define\s+(EXA_[A-Z0-9_]+)[ \t]+([^\n/]+)", src):
+        body = body.strip()
+        m = re.fullmatch(r"\(?\s*(-?(?:0x[0-9a-fA-F]+|\d+))u?\s*\)?", body)
+        s = re.fullmatch(r"\(\s*(\d+)u?\s*<<\s*(\d+)\s*\)", body)
+        if m:
+            defs[name] = int(m.group(1), 0)
+        elif s:
+            defs[name] = int(s.group(1)) << int(s.group(2))
+    matched = 0
+    for name, value in defs.items():
+        for py in (name, name[4:]):
+            if hasattr(E, py):
+                assert getattr(E, py) == value, (name, getattr(E, py), value)
+                matched += 1
+                break
+    assert matched >= 25, matched
